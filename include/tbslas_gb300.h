@@ -1,0 +1,173 @@
+/*
+ * tbslas_gb300 -- C ABI of the GB300 (sm_103a) semi-Lagrangian advection step.
+ *
+ * Drop-in for the tbslas SL path: the field-functor concept
+ *   void operator()(const real_t* pos, int n, real_t* out)
+ * (src/tree/tree_functor.h:793-815, used by src/semilag/traj.inc:33,:40 and
+ * src/semilag/semilag.inc:43), ComputeTrajRK2 (src/semilag/traj.inc:48-68),
+ * SolveSemilagInSitu (src/tree/tree_semilag.h:92-135), their tree glue
+ * CollectChebTreeGridPoints / SetTreeGridValues (src/tree/tree_utils.h:442-552),
+ * the Chebyshev helpers new_nodes / GetPt2CoeffMatrix (src/utils/cheb.h:41-196)
+ * and the tricubic regular-grid interpolant fast_interp
+ * (src/tree/tree_functor.h:89-153).
+ *
+ * Conventions
+ *  - Every entry point returns a tbslas_status (0 = success).  The reference
+ *    has no error codes (asserts only); here bad arguments are rejected on the
+ *    host before any launch and tbslas_last_error() gives a message.
+ *  - Pointers named *_dev are device pointers owned by the caller; *_host are
+ *    host pointers.  `stream` is a cudaStream_t (NULL = legacy default stream).
+ *    Device entry points are asynchronous on `stream`; *_host entry points are
+ *    synchronous.
+ *  - All arithmetic is IEEE FP64.
+ *  - Boundary condition `bc`: TBSLAS_BC_FREESPACE or TBSLAS_BC_PERIODIC, the
+ *    reference's pvfmm::FreeSpace / pvfmm::Periodic (sim_config->bc).
+ *  - A point with a NaN coordinate, or outside [0,1]^3 under FreeSpace (after
+ *    the single periodic wrap under Periodic), evaluates to 0 -- the value
+ *    pvfmm::cheb_poly's |x|>1 rule gives such points in the reference.
+ *  - Unlike EvalTree (src/tree/tree_functor.h:442-448, :803), no entry point
+ *    writes the periodic wrap back into the caller's coordinate array.
+ *  - A tree is a complete linear octree of leaves in Morton order (the
+ *    post-order leaf list of the reference's pvfmm::MPI_Tree) with per-leaf
+ *    triangular Chebyshev coefficients of degree q, laid out
+ *    [leaf][dof][Nc], Nc = (q+1)(q+2)(q+3)/6, index order i (z) outer,
+ *    j (y), k (x) inner over i+j+k <= q (src/tree/tree_functor.h:257-267).
+ *  - One context per host thread; calls on one context are not re-entrant.
+ */
+#ifndef TBSLAS_GB300_H_
+#define TBSLAS_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TBSLAS_OK = 0,
+  TBSLAS_ERR_INVALID_ARG = 1, /* null pointer, negative size, bad enum      */
+  TBSLAS_ERR_TREE = 2,        /* leaves are not a complete Morton-ordered octree */
+  TBSLAS_ERR_CUDA = 3,        /* a CUDA runtime call failed                 */
+  TBSLAS_ERR_UNSUPPORTED = 4, /* degree outside the compiled range, ...     */
+  TBSLAS_ERR_ALLOC = 5,       /* device allocation failed                   */
+  TBSLAS_ERR_SIZE = 6,        /* a size exceeds a stated limit              */
+  TBSLAS_ERR_DEVICE = 7       /* a kernel reported an error status          */
+} tbslas_status;
+
+enum { TBSLAS_BC_FREESPACE = 0, TBSLAS_BC_PERIODIC = 1 };
+
+/* Limits: Chebyshev degree 1..TBSLAS_MAX_DEGREE, leaf depth 0..TBSLAS_MAX_DEPTH. */
+#define TBSLAS_MAX_DEGREE 16
+#define TBSLAS_MAX_DEPTH 21
+
+typedef struct tbslas_ctx_s* tbslas_ctx;
+typedef struct tbslas_tree_s* tbslas_tree;
+
+/* ---- errors / version ---------------------------------------------------- */
+const char* tbslas_status_string(int status);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* tbslas_last_error(void);
+int tbslas_version(void);
+
+/* ---- context ------------------------------------------------------------- */
+/* Binds `device`, owns cached scratch buffers.  No reference counterpart
+ * (the reference keeps static buffers: src/tree/tree_functor.h:166,:519-584). */
+int tbslas_ctx_create(int device, tbslas_ctx* out);
+int tbslas_ctx_destroy(tbslas_ctx ctx);
+/* Kernel-side error word (bounded waits that ran out, ...); 0 if clean.
+ * Synchronises the context's device; clears the word. */
+int tbslas_ctx_check(tbslas_ctx ctx, uint32_t* device_error);
+
+/* ---- Chebyshev helpers (host) ---------------------------------------------- */
+/* new_nodes(q,3): (q+1)^3 x 3 nodes in [0,1], x fastest.
+ * Replaces tbslas::new_nodes, src/utils/cheb.h:41-67. */
+int tbslas_cheb_nodes(int q, double* out_host);
+/* (q+1)^3 x Nc matrix M with coeff = values * M (least squares fit of the
+ * total-degree basis at new_nodes).  Replaces tbslas::GetPt2CoeffMatrix,
+ * src/utils/cheb.h:166-196. */
+int tbslas_pt2coeff_matrix(int q, double* M_host);
+
+/* ---- trees ------------------------------------------------------------------- */
+/* Leaves: anchor_host[L*3] (lower corner), depth_host[L]; Morton order,
+ * complete.  Stands in for the pvfmm::MPI_Tree / Cheb_Node leaf list the
+ * reference walks with PostorderFirst/PostorderNxt (src/tree/tree_utils.h:460-495).
+ * Coefficients start at zero. */
+int tbslas_tree_create(tbslas_ctx ctx, int64_t n_leaves, const double* anchor_host,
+                       const int32_t* depth_host, int q, int dof, tbslas_tree* out);
+int tbslas_tree_destroy(tbslas_tree tree);
+int tbslas_tree_info(tbslas_tree tree, int64_t* n_leaves, int* q, int* dof, int* max_depth);
+/* Copy [L][dof][Nc] coefficients in / out (Node::ChebData() of every leaf). */
+int tbslas_tree_set_coeffs_host(tbslas_tree tree, const double* coeff_host);
+int tbslas_tree_get_coeffs_host(tbslas_tree tree, double* coeff_host);
+int tbslas_tree_set_coeffs(tbslas_tree tree, const double* coeff_dev, void* stream);
+int tbslas_tree_get_coeffs(tbslas_tree tree, double* coeff_dev, void* stream);
+
+/* ---- the SL path --------------------------------------------------------------- */
+/* Chebyshev nodes of every leaf, leaves in order: out_dev[L*(q+1)^3*3].
+ * Replaces CollectChebTreeGridPoints, src/tree/tree_utils.h:442-498. */
+int tbslas_collect_grid_points(tbslas_ctx ctx, tbslas_tree tree, double* out_dev, void* stream);
+
+/* Field functor: out_dev[n*dof] (point-major) = tree evaluated at pos_dev[n*3].
+ * Points are bucketed by leaf (counting sort on the leaf's Morton rank), each
+ * leaf's coefficients staged in shared memory, results un-permuted.
+ * Replaces NodeFieldFunctor::operator() -> EvalTree -> EvalNodesLocal,
+ * src/tree/tree_functor.h:397-815. */
+int tbslas_eval_tree(tbslas_ctx ctx, tbslas_tree tree, const double* pos_dev, int64_t n,
+                     double* out_dev, int bc, void* stream);
+/* Synchronous host-buffer form of the same functor (the reference's exact
+ * calling convention: host arrays in, host array out). */
+int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_host, int64_t n,
+                          double* out_host, int bc);
+
+/* RK2 backtrace of n points through a dof-3 velocity tree from tinit to tfinal
+ * in nrk sub-steps: xdep_dev[n*3].  Replaces ComputeTrajRK2 with a
+ * NodeFieldFunctor velocity, src/semilag/traj.inc:20-68. */
+int tbslas_traj_rk2(tbslas_ctx ctx, tbslas_tree vel, const double* x_dev, int64_t n,
+                    double tinit, double tfinal, int nrk, int bc, double* xdep_dev,
+                    void* stream);
+
+/* Node values -> coefficients of every leaf: vals_dev[L][dof][(q+1)^3].
+ * Replaces SetTreeGridValues, src/tree/tree_utils.h:500-552. */
+int tbslas_set_tree_grid_values(tbslas_ctx ctx, tbslas_tree tree, const double* vals_dev,
+                                void* stream);
+
+/* One in-situ SL step: every Chebyshev node of `con` is backtraced through
+ * `vel` (RK2, nrk sub-steps, from timestep*dt to timestep*dt-dt), `con` is
+ * evaluated at the departure points and refitted in place.  Targets are never
+ * materialised.  Replaces SolveSemilagInSitu, src/tree/tree_semilag.h:92-135.
+ * For dof > 1 the node values are refitted per dof (the reference exercises
+ * dof = 1 only). */
+int tbslas_semilag_in_situ(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
+                           double dt, int nrk, int bc, void* stream);
+/* Same step with the coefficients in host memory: copies con's coefficients
+ * in, runs the step, copies them back out (synchronous). */
+int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                double* con_coeff_host, int timestep, double dt, int nrk,
+                                int bc);
+
+/* ---- tricubic regular grid --------------------------------------------------- */
+/* out_dev[n*dof] = tricubic Lagrange interpolant of grid_dev (SoA,
+ * vals[x + N(y + N z) + k N^3]) at pts_dev[n*3].  FREESPACE: the reference's
+ * clamped stencil on nodes i/(N-1), zero outside [0,1]^3.  PERIODIC: nodes i/N,
+ * stencil wrapped mod N.  Replaces tbslas::fast_interp,
+ * src/tree/tree_functor.h:89-153.  Requires n_reg >= 4. */
+int tbslas_fast_interp(tbslas_ctx ctx, const double* grid_dev, int dof, int n_reg,
+                       const double* pts_dev, int64_t n, double* out_dev, int bc, void* stream);
+/* One SL step on the grid: every node is a target, RK2 (nrk sub-steps of
+ * -dt/nrk) through the 3-component velocity grid, tricubic concentration at
+ * the departure points: con_out_dev[N^3].  con_out_dev must not alias
+ * con_dev. */
+int tbslas_semilag_grid(tbslas_ctx ctx, const double* vel_dev, const double* con_dev,
+                        double* con_out_dev, int n_reg, double dt, int nrk, int bc,
+                        void* stream);
+/* Synchronous host-buffer form: vel_host[3N^3], con_host[N^3] in,
+ * con_out_host[N^3] out. */
+int tbslas_semilag_grid_host(tbslas_ctx ctx, const double* vel_host, const double* con_host,
+                             double* con_out_host, int n_reg, double dt, int nrk, int bc);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TBSLAS_GB300_H_ */

@@ -1,0 +1,160 @@
+"""Python face of the oracle (test infrastructure only).
+
+Thin ctypes wrappers around oracle/oracle.cpp (the CPU restatement of the
+tbslas semi-Lagrangian path) plus the point-to-coefficient matrix, restated
+from tbslas::GetPt2CoeffMatrix (src/utils/cheb.h:166-196) as
+pinv(V)^T with an SVD-based pseudo-inverse (numpy/LAPACK), which is how
+PVFMM's Matrix::pinv computes it.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.
+"""
+import ctypes
+import functools
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_f64p = ctypes.POINTER(ctypes.c_double)
+_i32p = ctypes.POINTER(ctypes.c_int)
+
+
+@functools.lru_cache(maxsize=1)
+def lib():
+    path = _build.build()
+    L = ctypes.CDLL(path)
+    i64, i32, f64 = ctypes.c_long, ctypes.c_int, ctypes.c_double
+    L.orc_num_threads.argtypes = [i32]
+    L.orc_new_nodes.argtypes = [i32, _f64p]
+    L.orc_cheb_poly.argtypes = [i32, _f64p, i32, _f64p]
+    L.orc_cheb_basis.argtypes = [i32, _f64p, i64, _f64p]
+    L.orc_collect_grid_points.argtypes = [i64, _f64p, _i32p, i32, _f64p]
+    L.orc_eval_tree.argtypes = [i64, _f64p, _i32p, i32, i32, _f64p, i32, _f64p, i64, _f64p]
+    L.orc_traj_rk2.argtypes = [i64, _f64p, _i32p, i32, _f64p, i32, _f64p, i64, f64, f64, i32,
+                               _f64p]
+    L.orc_set_tree_grid_values.argtypes = [i64, i32, i32, _f64p, _f64p, _f64p]
+    L.orc_semilag_in_situ.argtypes = [i64, _f64p, _i32p, i32, _f64p,
+                                      i64, _f64p, _i32p, i32, i32, _f64p,
+                                      _f64p, i32, f64, i32, i32, _f64p]
+    L.orc_fast_interp.argtypes = [_f64p, i32, i32, _f64p, i64, _f64p, i32]
+    L.orc_semilag_grid.argtypes = [_f64p, _f64p, i32, f64, i32, i32, i64, i64, _f64p]
+    return L
+
+
+def _d(a):
+    return a.ctypes.data_as(_f64p)
+
+
+def _i(a):
+    return a.ctypes.data_as(_i32p)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def num_threads(n=0):
+    return lib().orc_num_threads(int(n))
+
+
+def n_coeff(q):
+    return (q + 1) * (q + 2) * (q + 3) // 6
+
+
+def new_nodes(q):
+    out = np.empty(((q + 1) ** 3, 3))
+    lib().orc_new_nodes(q, _d(out))
+    return out
+
+
+def cheb_poly(q, x):
+    x = _f64(x)
+    out = np.zeros((q + 1, x.size))
+    lib().orc_cheb_poly(q, _d(x), x.size, _d(out))
+    return out
+
+
+def cheb_basis(q, pts):
+    pts = _f64(pts).reshape(-1, 3)
+    V = np.empty((pts.shape[0], n_coeff(q)))
+    lib().orc_cheb_basis(q, _d(pts), pts.shape[0], _d(V))
+    return V
+
+
+@functools.lru_cache(maxsize=None)
+def _pt2coeff_cached(q):
+    V = cheb_basis(q, 2.0 * new_nodes(q) - 1.0)
+    M = np.linalg.pinv(V).T.copy()
+    M.setflags(write=False)
+    return M
+
+
+def pt2coeff(q):
+    """M (Np x Nc) with coeff = vals @ M; restates GetPt2CoeffMatrix."""
+    return _pt2coeff_cached(q)
+
+
+def collect_grid_points(anchor, depth, q):
+    anchor, depth = _f64(anchor), _i32(depth)
+    out = np.empty((depth.size * (q + 1) ** 3, 3))
+    lib().orc_collect_grid_points(depth.size, _d(anchor), _i(depth), q, _d(out))
+    return out
+
+
+def eval_tree(anchor, depth, q, dof, coeff, pos, periodic=False):
+    anchor, depth, coeff, pos = _f64(anchor), _i32(depth), _f64(coeff), _f64(pos).reshape(-1, 3)
+    out = np.empty((pos.shape[0], dof))
+    lib().orc_eval_tree(depth.size, _d(anchor), _i(depth), q, dof, _d(coeff), int(periodic),
+                        _d(pos), pos.shape[0], _d(out))
+    return out
+
+
+def traj_rk2(anchor, depth, q, coeff, x, tinit, tfinal, nrk, periodic=False):
+    anchor, depth, coeff, x = _f64(anchor), _i32(depth), _f64(coeff), _f64(x).reshape(-1, 3)
+    out = np.empty_like(x)
+    lib().orc_traj_rk2(depth.size, _d(anchor), _i(depth), q, _d(coeff), int(periodic), _d(x),
+                       x.shape[0], float(tinit), float(tfinal), int(nrk), _d(out))
+    return out
+
+
+def set_tree_grid_values(L, q, dof, vals, M=None):
+    M = pt2coeff(q) if M is None else _f64(M)
+    vals = _f64(vals)
+    out = np.empty((L, dof, n_coeff(q)))
+    lib().orc_set_tree_grid_values(L, q, dof, _d(M), _d(vals), _d(out))
+    return out
+
+
+def semilag_in_situ(vel, con, timestep, dt, nrk=1, periodic=False, M=None):
+    """One in-situ SL step.  vel/con: dicts with anchor, depth, q, dof, coeff."""
+    qc = con["q"]
+    M = pt2coeff(qc) if M is None else _f64(M)
+    av, dv, cv = _f64(vel["anchor"]), _i32(vel["depth"]), _f64(vel["coeff"])
+    ac, dc, cc = _f64(con["anchor"]), _i32(con["depth"]), _f64(con["coeff"])
+    out = np.empty((dc.size, con["dof"], n_coeff(qc)))
+    lib().orc_semilag_in_situ(dv.size, _d(av), _i(dv), vel["q"], _d(cv),
+                              dc.size, _d(ac), _i(dc), qc, con["dof"], _d(cc),
+                              _d(M), int(timestep), float(dt), int(nrk), int(periodic), _d(out))
+    return out
+
+
+def fast_interp(grid, dof, nreg, pts, periodic=False):
+    grid, pts = _f64(grid), _f64(pts).reshape(-1, 3)
+    out = np.empty((pts.shape[0], dof))
+    lib().orc_fast_interp(_d(grid), dof, nreg, _d(pts), pts.shape[0], _d(out), int(periodic))
+    return out
+
+
+def semilag_grid(vel, con, nreg, dt, nrk=1, periodic=True, node_begin=0, node_end=0):
+    vel, con = _f64(vel), _f64(con)
+    n = nreg ** 3 if node_end <= node_begin else node_end - node_begin
+    out = np.empty(n)
+    lib().orc_semilag_grid(_d(vel), _d(con), nreg, float(dt), int(nrk), int(periodic),
+                           int(node_begin), int(node_end), _d(out))
+    return out

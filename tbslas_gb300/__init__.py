@@ -1,0 +1,10 @@
+"""tbslas_gb300: the tbslas semi-Lagrangian advection step on GB300 (sm_103a).
+
+The compute path is libtbslas_gb300.so (hand-written CUDA behind a C ABI,
+include/tbslas_gb300.h); this package is its Python face.
+"""
+from . import capi  # noqa: F401
+from .api import (  # noqa: F401
+    Context, FreeSpace, NodeFieldFunctor, Periodic, Tree, collect_cheb_tree_grid_points,
+    compute_traj_rk2, fast_interp, get_pt2coeff_matrix, n_coeff, n_points, new_nodes,
+    semilag_grid, set_tree_grid_values, solve_semilag_in_situ)

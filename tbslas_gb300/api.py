@@ -1,0 +1,252 @@
+"""Python mirror of the tbslas SL interface over the C ABI.
+
+Names follow the reference: NodeFieldFunctor (src/tree/tree_functor.h:793-815),
+compute_traj_rk2 (ComputeTrajRK2, src/semilag/traj.inc:48-68),
+solve_semilag_in_situ (SolveSemilagInSitu, src/tree/tree_semilag.h:92-135),
+collect_cheb_tree_grid_points / set_tree_grid_values
+(src/tree/tree_utils.h:442-552), new_nodes / get_pt2coeff_matrix
+(src/utils/cheb.h:41-196) and fast_interp (src/tree/tree_functor.h:89-153).
+
+Device arrays are torch CUDA float64 tensors; host arrays are numpy float64
+arrays (the *_host entry points).  Every call goes to the CUDA library; there
+is no CPU path.
+"""
+import ctypes
+
+import numpy as np
+
+from . import capi
+from .capi import BC_FREESPACE, BC_PERIODIC, call
+
+FreeSpace = BC_FREESPACE
+Periodic = BC_PERIODIC
+
+
+def n_coeff(q):
+    return (q + 1) * (q + 2) * (q + 3) // 6
+
+
+def n_points(q):
+    return (q + 1) ** 3
+
+
+def _ptr(a):
+    """Raw data pointer of a torch tensor or numpy array (must be contiguous f64)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise TypeError("expected a C-contiguous float64 numpy array")
+        return a.ctypes.data
+    import torch
+    if not isinstance(a, torch.Tensor):
+        raise TypeError("expected a torch tensor or numpy array, got %r" % type(a))
+    if a.dtype != torch.float64 or not a.is_contiguous() or not a.is_cuda:
+        raise TypeError("expected a contiguous float64 CUDA tensor")
+    return a.data_ptr()
+
+
+def _stream(stream):
+    if stream is not None:
+        return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+    import torch
+    return torch.cuda.current_stream().cuda_stream
+
+
+def new_nodes(q):
+    if not 0 <= q <= capi.MAX_DEGREE:
+        call("tbslas_cheb_nodes", int(q), None)  # raises the library's error
+    out = np.empty((n_points(q), 3))
+    call("tbslas_cheb_nodes", q, out.ctypes.data)
+    return out
+
+
+def get_pt2coeff_matrix(q):
+    if not 1 <= q <= capi.MAX_DEGREE:
+        call("tbslas_pt2coeff_matrix", int(q), None)  # raises the library's error
+    out = np.empty((n_points(q), n_coeff(q)))
+    call("tbslas_pt2coeff_matrix", q, out.ctypes.data)
+    return out
+
+
+class Context:
+    """One CUDA device plus the library's cached scratch buffers."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        call("tbslas_ctx_create", int(device), ctypes.byref(h))
+        self.handle = h
+        self.device = int(device)
+
+    def close(self):
+        if self.handle:
+            capi.lib().tbslas_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self):
+        """Synchronise and return the device error word (raises if non-zero)."""
+        w = ctypes.c_uint32(0)
+        st = capi.lib().tbslas_ctx_check(self.handle, ctypes.byref(w))
+        capi.check(st, "tbslas_ctx_check")
+        return w.value
+
+
+class Tree:
+    """Complete linear octree (leaves in Morton order) + Chebyshev coefficients."""
+
+    def __init__(self, ctx, anchor, depth, q, dof, coeff=None):
+        anchor = np.ascontiguousarray(anchor, dtype=np.float64).reshape(-1, 3)
+        depth = np.ascontiguousarray(depth, dtype=np.int32).reshape(-1)
+        if anchor.shape[0] != depth.shape[0]:
+            raise ValueError("anchor/depth length mismatch")
+        h = ctypes.c_void_p()
+        call("tbslas_tree_create", ctx.handle, depth.size, anchor.ctypes.data, depth.ctypes.data,
+             int(q), int(dof), ctypes.byref(h))
+        self.ctx, self.handle = ctx, h
+        self.anchor, self.depth, self.q, self.dof = anchor, depth, int(q), int(dof)
+        self.n_leaves = depth.size
+        if coeff is not None:
+            self.set_coeffs(coeff)
+
+    def close(self):
+        if self.handle:
+            capi.lib().tbslas_tree_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def coeff_shape(self):
+        return (self.n_leaves, self.dof, n_coeff(self.q))
+
+    def set_coeffs(self, coeff, stream=None):
+        if isinstance(coeff, np.ndarray):
+            c = np.ascontiguousarray(coeff, dtype=np.float64)
+            if c.size != np.prod(self.coeff_shape):
+                raise ValueError("coefficient array has %d values, tree needs %d"
+                                 % (c.size, np.prod(self.coeff_shape)))
+            call("tbslas_tree_set_coeffs_host", self.handle, c.ctypes.data)
+        else:
+            if coeff.numel() != np.prod(self.coeff_shape):
+                raise ValueError("coefficient tensor has wrong size")
+            call("tbslas_tree_set_coeffs", self.handle, _ptr(coeff), _stream(stream))
+
+    def get_coeffs(self, out=None, stream=None):
+        if out is None:
+            out = np.empty(self.coeff_shape)
+        if isinstance(out, np.ndarray):
+            call("tbslas_tree_get_coeffs_host", self.handle, out.ctypes.data)
+        else:
+            call("tbslas_tree_get_coeffs", self.handle, _ptr(out), _stream(stream))
+        return out
+
+
+class NodeFieldFunctor:
+    """Field functor of a tree: f(pos[n,3]) -> values[n,dof].
+
+    Host numpy arrays go through the synchronous host entry point (the
+    reference's calling convention); torch CUDA tensors stay on the device.
+    Unlike the reference, the caller's coordinates are never modified.
+    """
+
+    def __init__(self, tree, bc=FreeSpace):
+        self.tree, self.bc = tree, int(bc)
+
+    def __call__(self, pos, out=None, stream=None):
+        t = self.tree
+        if isinstance(pos, np.ndarray):
+            pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+            if out is None:
+                out = np.empty((pos.shape[0], t.dof))
+            call("tbslas_eval_tree_host", t.ctx.handle, t.handle, pos.ctypes.data, pos.shape[0],
+                 out.ctypes.data, self.bc)
+            return out
+        import torch
+        n = pos.numel() // 3
+        if out is None:
+            out = torch.empty((n, t.dof), dtype=torch.float64, device=pos.device)
+        call("tbslas_eval_tree", t.ctx.handle, t.handle, _ptr(pos), n, _ptr(out), self.bc,
+             _stream(stream))
+        return out
+
+
+def compute_traj_rk2(vel_functor, xinit, tinit, tfinal, num_rk_step, xsol=None, stream=None):
+    """RK2 departure points of xinit (CUDA tensor [n,3]) through a tree velocity."""
+    import torch
+    t = vel_functor.tree
+    n = xinit.numel() // 3
+    if xsol is None:
+        xsol = torch.empty_like(xinit)
+    call("tbslas_traj_rk2", t.ctx.handle, t.handle, _ptr(xinit), n, float(tinit), float(tfinal),
+         int(num_rk_step), vel_functor.bc, _ptr(xsol), _stream(stream))
+    return xsol
+
+
+def collect_cheb_tree_grid_points(tree, out=None, stream=None):
+    import torch
+    if out is None:
+        out = torch.empty((tree.n_leaves * n_points(tree.q), 3), dtype=torch.float64,
+                          device="cuda:%d" % tree.ctx.device)
+    call("tbslas_collect_grid_points", tree.ctx.handle, tree.handle, _ptr(out), _stream(stream))
+    return out
+
+
+def set_tree_grid_values(tree, vals, stream=None):
+    """vals: CUDA tensor [L, dof, (q+1)^3] of node values -> tree coefficients."""
+    call("tbslas_set_tree_grid_values", tree.ctx.handle, tree.handle, _ptr(vals), _stream(stream))
+
+
+def solve_semilag_in_situ(vel_functor, tree, timestep, dt, num_rk_step=1, stream=None,
+                          coeff_host=None):
+    """One in-situ SL step of `tree` through the velocity functor's tree.
+
+    With coeff_host (numpy [L,dof,Nc]) the coefficients are taken from and
+    returned to host memory (synchronous); otherwise the step is enqueued on
+    the stream and works on the tree's device coefficients.
+    """
+    v = vel_functor.tree
+    if coeff_host is not None:
+        if coeff_host.dtype != np.float64 or not coeff_host.flags.c_contiguous:
+            raise TypeError("coeff_host must be C-contiguous float64")
+        call("tbslas_semilag_in_situ_host", tree.ctx.handle, v.handle, tree.handle,
+             coeff_host.ctypes.data, int(timestep), float(dt), int(num_rk_step), vel_functor.bc)
+        return coeff_host
+    call("tbslas_semilag_in_situ", tree.ctx.handle, v.handle, tree.handle, int(timestep),
+         float(dt), int(num_rk_step), vel_functor.bc, _stream(stream))
+    return None
+
+
+def fast_interp(ctx, grid, dof, n_reg, pts, bc=FreeSpace, out=None, stream=None):
+    import torch
+    n = pts.numel() // 3
+    if out is None:
+        out = torch.empty((n, dof), dtype=torch.float64, device=pts.device)
+    call("tbslas_fast_interp", ctx.handle, _ptr(grid), int(dof), int(n_reg), _ptr(pts), n,
+         _ptr(out), int(bc), _stream(stream))
+    return out
+
+
+def semilag_grid(ctx, vel, con, n_reg, dt, num_rk_step=1, bc=Periodic, out=None, stream=None):
+    """One grid SL step.  vel [3,N,N,N], con [N,N,N] (CUDA tensors or numpy arrays)."""
+    if isinstance(con, np.ndarray):
+        if out is None:
+            out = np.empty_like(con)
+        call("tbslas_semilag_grid_host", ctx.handle, _ptr(vel), _ptr(con), _ptr(out),
+             int(n_reg), float(dt), int(num_rk_step), int(bc))
+        return out
+    import torch
+    if out is None:
+        out = torch.empty_like(con)
+    call("tbslas_semilag_grid", ctx.handle, _ptr(vel), _ptr(con), _ptr(out), int(n_reg),
+         float(dt), int(num_rk_step), int(bc), _stream(stream))
+    return out

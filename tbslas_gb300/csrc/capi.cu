@@ -1,0 +1,840 @@
+// C ABI of libtbslas_gb300.so (include/tbslas_gb300.h): contexts, trees,
+// host-side validation, the bucketing kernels of the tree functor, and the
+// entry points of the SL path.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "host_cheb.h"
+#include "internal.h"
+#include "tbslas_gb300.h"
+
+using namespace tbg;
+
+// ---------------------------------------------------------------------------
+// errors
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(call)                                                                 \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(TBSLAS_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));           \
+  } while (0)
+
+#define TRY(expr)            \
+  do {                       \
+    int s_ = (expr);         \
+    if (s_ != TBSLAS_OK) return s_; \
+  } while (0)
+
+DegreeKernels g_kernels[TBSLAS_MAX_DEGREE + 1];
+std::once_flag g_kernels_once;
+
+void init_kernels() {
+  register_degrees_a(g_kernels);
+  register_degrees_b(g_kernels);
+  register_degrees_c(g_kernels);
+  register_degrees_d(g_kernels);
+  register_degrees_e(g_kernels);
+  register_degrees_f(g_kernels);
+  register_degrees_g(g_kernels);
+  register_degrees_h(g_kernels);
+}
+
+// Point-to-coefficient matrices, computed once per degree per process.
+std::mutex g_M_mutex;
+std::vector<double> g_M_host[TBSLAS_MAX_DEGREE + 1];
+
+const std::vector<double>& host_M(int q) {
+  std::lock_guard<std::mutex> lock(g_M_mutex);
+  if (g_M_host[q].empty()) g_M_host[q] = pt2coeff_matrix(q);
+  return g_M_host[q];
+}
+
+enum Slot {
+  kVals,
+  kLeafOf,
+  kCount,
+  kStart,
+  kCursor,
+  kNTile,
+  kTileOff,
+  kTiles,
+  kPerm,
+  kXA,
+  kXB,
+  kVT,
+  kHostIn,
+  kHostIn2,
+  kHostOut,
+  kNumSlots
+};
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+inline int64_t n_coeff(int q) { return (int64_t)(q + 1) * (q + 2) * (q + 3) / 6; }
+inline int64_t n_points(int q) { return (int64_t)(q + 1) * (q + 1) * (q + 1); }
+inline bool bc_ok(int bc) { return bc == TBSLAS_BC_FREESPACE || bc == TBSLAS_BC_PERIODIC; }
+
+}  // namespace
+
+struct tbslas_ctx_s {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;  // used by the synchronous *_host entry points
+  uint32_t* d_err = nullptr;
+  DevBuf slots[kNumSlots];
+  double* d_M[TBSLAS_MAX_DEGREE + 1] = {};
+};
+
+struct tbslas_tree_s {
+  tbslas_ctx ctx = nullptr;
+  int64_t L = 0;
+  int q = 0, dof = 0, max_depth = 0, T = 0;
+  int64_t stride = 0;
+  uint64_t* d_keys = nullptr;
+  Geom* d_geom = nullptr;
+  double* d_coeff = nullptr;
+  int32_t* d_table = nullptr;
+
+  TreeView view() const {
+    TreeView v;
+    v.keys = d_keys;
+    v.geom = d_geom;
+    v.coeff = d_coeff;
+    v.table = d_table;
+    v.L = L;
+    v.stride = stride;
+    v.T = T;
+    v.q = q;
+    v.dof = dof;
+    return v;
+  }
+};
+
+namespace {
+
+int bind(tbslas_ctx ctx) {
+  if (!ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null context");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  return TBSLAS_OK;
+}
+
+// Grow-only scratch buffer.  Growing frees the old block (cudaFree waits for
+// the device), so no in-flight kernel can still be using it.
+int scratch(tbslas_ctx ctx, Slot s, size_t bytes, void** out) {
+  DevBuf& b = ctx->slots[s];
+  if (b.cap < bytes) {
+    if (b.p) CUDA_TRY(cudaFree(b.p));
+    b.p = nullptr;
+    b.cap = 0;
+    size_t want = std::max(bytes, (size_t)256);
+    if (cudaMalloc(&b.p, want) != cudaSuccess) {
+      cudaGetLastError();
+      b.p = nullptr;
+      return fail(TBSLAS_ERR_ALLOC, "cudaMalloc of %zu bytes of scratch failed", want);
+    }
+    b.cap = want;
+  }
+  *out = b.p;
+  return TBSLAS_OK;
+}
+
+template <class T>
+int scratch_t(tbslas_ctx ctx, Slot s, size_t count, T** out) {
+  void* p = nullptr;
+  TRY(scratch(ctx, s, count * sizeof(T), &p));
+  *out = static_cast<T*>(p);
+  return TBSLAS_OK;
+}
+
+int device_M(tbslas_ctx ctx, int q, const double** out) {
+  if (!ctx->d_M[q]) {
+    const std::vector<double>& M = host_M(q);
+    double* d = nullptr;
+    CUDA_TRY(cudaMalloc(&d, M.size() * sizeof(double)));
+    CUDA_TRY(cudaMemcpy(d, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice));
+    ctx->d_M[q] = d;
+  }
+  *out = ctx->d_M[q];
+  return TBSLAS_OK;
+}
+
+Nodes1D nodes_1d(int q) {
+  Nodes1D n;
+  std::memset(&n, 0, sizeof(n));
+  std::vector<double> x = cheb_nodes_1d(q);
+  for (int i = 0; i <= q; ++i) n.x[i] = x[i];
+  return n;
+}
+
+int check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(TBSLAS_ERR_CUDA, "%s launch: %s", what, cudaGetErrorString(e));
+  return TBSLAS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// small kernels
+
+// Chebyshev nodes of every leaf (CollectChebTreeGridPoints,
+// src/tree/tree_utils.h:477-495): leaf anchor + 2^-depth * node.
+__global__ void k_collect(const TreeView t, const Nodes1D nodes, int d, double* __restrict__ out) {
+  const int64_t np = (int64_t)d * d * d;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= t.L * np) return;
+  const int64_t leaf = i / np;
+  const int p = (int)(i - leaf * np);
+  const Geom g = load_geom(t.geom + leaf);
+  const double h = 2.0 / g.w;
+  out[3 * i + 0] = g.x + h * nodes.x[p % d];
+  out[3 * i + 1] = g.y + h * nodes.x[(p / d) % d];
+  out[3 * i + 2] = g.z + h * nodes.x[p / (d * d)];
+}
+
+// Leaf of every point (Morton key + coarse table + binary search) and a
+// warp-aggregated per-leaf count.  Points that evaluate to 0 (outside the
+// domain, NaN) get their output written here and are not bucketed.
+__global__ void k_classify(const TreeView t, const double* __restrict__ pos, int64_t n,
+                           int periodic, int32_t* __restrict__ leaf_of,
+                           unsigned long long* __restrict__ count, double* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int leaf = -2;
+  if (i < n) {
+    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    const bool per = periodic != 0;
+    if (per) {
+      x = wrap1(x);
+      y = wrap1(y);
+      z = wrap1(z);
+    }
+    if (inside(x, y, z, per)) {
+      leaf = (int)find_leaf(t, morton3(quantise(x), quantise(y), quantise(z)));
+    } else {
+      leaf = -1;
+      for (int l = 0; l < t.dof; ++l) out[i * t.dof + l] = 0.0;
+    }
+    leaf_of[i] = leaf;
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, leaf);
+  if (leaf >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+    atomicAdd(count + leaf, (unsigned long long)__popc(peers));
+}
+
+__global__ void k_ntiles(const unsigned long long* __restrict__ count, int64_t L,
+                         int64_t* __restrict__ ntile) {
+  const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (l < L) ntile[l] = (int64_t)((count[l] + kTile - 1) / kTile);
+}
+
+// Exclusive scan of in[0..m) into out[0..m], out[m] = total.  One CTA walks
+// the array in chunks of 1024 (the arrays are per-leaf, small next to the
+// point work).
+__global__ void __launch_bounds__(1024) k_scan_excl(const int64_t* __restrict__ in,
+                                                    int64_t* __restrict__ out, int64_t m) {
+  __shared__ int64_t wsum[32];
+  __shared__ int64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t base = 0; base < m; base += 1024) {
+    const int64_t i = base + threadIdx.x;
+    const int64_t v = i < m ? in[i] : 0;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int64_t w = wsum[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    const int64_t incl = x + (warp > 0 ? wsum[warp - 1] : 0) + carry;
+    if (i < m) out[i] = incl - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[m] = carry;
+}
+
+__global__ void k_scatter(const int32_t* __restrict__ leaf_of, int64_t n,
+                          const int64_t* __restrict__ start, unsigned long long* __restrict__ cursor,
+                          int64_t* __restrict__ perm) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int leaf = i < n ? leaf_of[i] : -2;
+  const unsigned peers = __match_any_sync(0xffffffffu, leaf);
+  if (leaf >= 0) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(cursor + leaf, (unsigned long long)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    perm[start[leaf] + (int64_t)base + rank] = i;
+  }
+}
+
+__global__ void k_make_tiles(const int64_t* __restrict__ start, const int64_t* __restrict__ tileoff,
+                             int64_t L, Tile* __restrict__ tiles) {
+  const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (l >= L) return;
+  const int64_t s = start[l], c = start[l + 1] - s;
+  int64_t o = tileoff[l];
+  for (int64_t k = 0; k < c; k += kTile, ++o)
+    tiles[o] = Tile{s + k, (int32_t)l, (int32_t)(c - k < kTile ? c - k : kTile)};
+}
+
+// [leaf][node][dof] -> [leaf][dof][node]
+__global__ void k_point_to_dof_major(const double* __restrict__ in, int64_t L, int np, int dof,
+                                     double* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= L * np * dof) return;
+  const int64_t leaf = i / ((int64_t)np * dof);
+  const int64_t r = i - leaf * np * dof;
+  const int p = (int)(r / dof), l = (int)(r % dof);
+  out[(leaf * dof + l) * np + p] = in[i];
+}
+
+inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// The bucketed tree functor on device buffers.
+int eval_tree_dev(tbslas_ctx ctx, tbslas_tree tree, const double* pos, int64_t n, double* out,
+                  int bc, cudaStream_t s) {
+  if (n == 0) return TBSLAS_OK;
+  const TreeView tv = tree->view();
+  const int64_t L = tree->L;
+  const int64_t max_tiles = (n + kTile - 1) / kTile + L;
+  int32_t* leaf_of;
+  unsigned long long *count, *cursor;
+  int64_t *start, *ntile, *tileoff, *perm;
+  Tile* tiles;
+  TRY(scratch_t(ctx, kLeafOf, n, &leaf_of));
+  TRY(scratch_t(ctx, kCount, L, &count));
+  TRY(scratch_t(ctx, kCursor, L, &cursor));
+  TRY(scratch_t(ctx, kStart, L + 1, &start));
+  TRY(scratch_t(ctx, kNTile, L, &ntile));
+  TRY(scratch_t(ctx, kTileOff, L + 1, &tileoff));
+  TRY(scratch_t(ctx, kPerm, n, &perm));
+  TRY(scratch_t(ctx, kTiles, max_tiles, &tiles));
+  CUDA_TRY(cudaMemsetAsync(count, 0, L * sizeof(*count), s));
+  CUDA_TRY(cudaMemsetAsync(cursor, 0, L * sizeof(*cursor), s));
+  k_classify<<<blocks_for(n, 256), 256, 0, s>>>(tv, pos, n, bc, leaf_of, count, out);
+  k_ntiles<<<blocks_for(L, 256), 256, 0, s>>>(count, L, ntile);
+  k_scan_excl<<<1, 1024, 0, s>>>(reinterpret_cast<const int64_t*>(count), start, L);
+  k_scan_excl<<<1, 1024, 0, s>>>(ntile, tileoff, L);
+  k_scatter<<<blocks_for(n, 256), 256, 0, s>>>(leaf_of, n, start, cursor, perm);
+  k_make_tiles<<<blocks_for(L, 256), 256, 0, s>>>(start, tileoff, L, tiles);
+  TRY(check_launch("bucketing"));
+  EvalTilesArgs a;
+  a.tree = tv;
+  a.pos = pos;
+  a.perm = perm;
+  a.tiles = tiles;
+  a.ntiles = tileoff + L;
+  a.periodic = bc;
+  a.out = out;
+  a.err = ctx->d_err;
+  a.grid = (int)std::min<int64_t>(max_tiles, (int64_t)ctx->num_sms * 8);
+  g_kernels[tree->q].eval_tiles(a, s);
+  return check_launch("eval_tiles");
+}
+
+int traj_dev(tbslas_ctx ctx, tbslas_tree vel, const double* x, int64_t n, double tau, int nrk,
+             int bc, double* xdep, cudaStream_t s) {
+  (void)ctx;
+  TrajArgs a;
+  a.vel = vel->view();
+  a.x = x;
+  a.n = n;
+  a.tau = tau;
+  a.nrk = nrk;
+  a.periodic = bc;
+  a.xdep = xdep;
+  g_kernels[vel->q].traj(a, s);
+  return check_launch("traj");
+}
+
+int refit_dev(tbslas_ctx ctx, tbslas_tree tree, const double* vals, cudaStream_t s) {
+  const double* M = nullptr;
+  TRY(device_M(ctx, tree->q, &M));
+  launch_refit(vals, M, tree->L * tree->dof, (int)n_points(tree->q), (int)n_coeff(tree->q),
+               tree->dof, tree->stride, tree->d_coeff, s);
+  return check_launch("refit");
+}
+
+int collect_dev(tbslas_tree tree, double* out, cudaStream_t s) {
+  const int64_t n = tree->L * n_points(tree->q);
+  if (n == 0) return TBSLAS_OK;
+  k_collect<<<blocks_for(n, 256), 256, 0, s>>>(tree->view(), nodes_1d(tree->q), tree->q + 1, out);
+  return check_launch("collect");
+}
+
+int check_tree(tbslas_tree t) {
+  if (!t || !t->ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null tree");
+  return TBSLAS_OK;
+}
+
+// The time step of SolveSemilagRK2 (src/semilag/semilag.inc:26-45):
+// tinit = timestep*dt, tfinal = tinit - dt, tau = (tfinal - tinit)/nrk.
+double sl_tau(int timestep, double dt, int nrk) {
+  const double tinit = timestep * dt;
+  const double tfinal = tinit - dt;
+  return (tfinal - tinit) / nrk;
+}
+
+int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
+                        int nrk, int bc, cudaStream_t s) {
+  const double tau = sl_tau(timestep, dt, nrk);
+  const int64_t np = n_points(con->q);
+  const int64_t N = con->L * np;
+  double* vals;
+  TRY(scratch_t(ctx, kVals, N * con->dof, &vals));
+  if (vel->q == con->q && con->dof == 1) {
+    SemilagTreeArgs a;
+    a.vel = vel->view();
+    a.con = con->view();
+    a.nodes = nodes_1d(con->q);
+    a.tau = tau;
+    a.nrk = nrk;
+    a.periodic = bc;
+    a.vals = vals;
+    g_kernels[con->q].semilag(a, s);
+    TRY(check_launch("semilag_tree"));
+  } else {
+    double *X, *Xdep, *vt;
+    TRY(scratch_t(ctx, kXA, N * 3, &X));
+    TRY(scratch_t(ctx, kXB, N * 3, &Xdep));
+    TRY(scratch_t(ctx, kVT, N * con->dof, &vt));
+    TRY(collect_dev(con, X, s));
+    TRY(traj_dev(ctx, vel, X, N, tau, nrk, bc, Xdep, s));
+    TRY(eval_tree_dev(ctx, con, Xdep, N, vt, bc, s));
+    k_point_to_dof_major<<<blocks_for(N * con->dof, 256), 256, 0, s>>>(vt, con->L, (int)np,
+                                                                      con->dof, vals);
+    TRY(check_launch("transpose"));
+  }
+  return refit_dev(ctx, con, vals, s);
+}
+
+// Validate a leaf list and build the device tree arrays.
+int build_tree(tbslas_tree t, const double* anchor, const int32_t* depth) {
+  const int64_t L = t->L;
+  std::vector<uint64_t> keys(L);
+  std::vector<Geom> geom(L);
+  int maxd = 0;
+  for (int64_t i = 0; i < L; ++i) {
+    const int dl = depth[i];
+    if (dl < 0 || dl > TBSLAS_MAX_DEPTH)
+      return fail(TBSLAS_ERR_TREE, "leaf %lld: depth %d outside [0,%d]", (long long)i, dl,
+                  TBSLAS_MAX_DEPTH);
+    maxd = std::max(maxd, dl);
+    uint64_t a[3];
+    for (int k = 0; k < 3; ++k) {
+      const double c = anchor[3 * i + k];
+      const double s = std::ldexp(c, dl);  // exact
+      if (!(c >= 0.0 && c < 1.0) || s != std::floor(s))
+        return fail(TBSLAS_ERR_TREE, "leaf %lld: anchor %g is not a multiple of 2^-%d in [0,1)",
+                    (long long)i, c, dl);
+      a[k] = (uint64_t)std::ldexp(c, kKeyBits);
+    }
+    keys[i] = morton3(a[0], a[1], a[2]);
+    geom[i] = Geom{anchor[3 * i], anchor[3 * i + 1], anchor[3 * i + 2], std::ldexp(2.0, dl)};
+  }
+  // Complete linear octree in Morton order: each leaf starts where the
+  // previous one ends and the last one ends at the domain's end.
+  uint64_t expect = 0;
+  for (int64_t i = 0; i < L; ++i) {
+    if (keys[i] != expect)
+      return fail(TBSLAS_ERR_TREE,
+                  "leaf %lld: not a complete Morton-ordered octree (gap, overlap or order)",
+                  (long long)i);
+    expect = keys[i] + (1ull << (3 * (kKeyBits - depth[i])));
+  }
+  if (expect != (1ull << (3 * kKeyBits)))
+    return fail(TBSLAS_ERR_TREE, "leaves do not cover the unit cube");
+  const int T = std::min(maxd, 7);
+  const int64_t ncell = 1ll << (3 * T);
+  std::vector<int32_t> table(ncell + 1);
+  {
+    int64_t leaf = 0;
+    for (int64_t c = 0; c < ncell; ++c) {
+      const uint64_t ck = (uint64_t)c << (3 * (kKeyBits - T));
+      while (leaf + 1 < L && keys[leaf + 1] <= ck) ++leaf;
+      table[c] = (int32_t)leaf;
+    }
+    table[ncell] = (int32_t)(L - 1);
+  }
+  t->max_depth = maxd;
+  t->T = T;
+  CUDA_TRY(cudaMalloc(&t->d_keys, L * sizeof(uint64_t)));
+  CUDA_TRY(cudaMalloc(&t->d_geom, L * sizeof(Geom)));
+  CUDA_TRY(cudaMalloc(&t->d_table, (ncell + 1) * sizeof(int32_t)));
+  CUDA_TRY(cudaMalloc(&t->d_coeff, L * t->stride * sizeof(double)));
+  CUDA_TRY(cudaMemcpy(t->d_keys, keys.data(), L * sizeof(uint64_t), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(t->d_geom, geom.data(), L * sizeof(Geom), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(t->d_table, table.data(), (ncell + 1) * sizeof(int32_t),
+                      cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemset(t->d_coeff, 0, L * t->stride * sizeof(double)));
+  return TBSLAS_OK;
+}
+
+int copy_coeffs(tbslas_tree t, double* dst, const double* src, bool to_tree, cudaMemcpyKind kind,
+                cudaStream_t s) {
+  const size_t w = (size_t)t->dof * n_coeff(t->q) * sizeof(double);
+  const size_t pitch = (size_t)t->stride * sizeof(double);
+  if (to_tree)
+    CUDA_TRY(cudaMemcpy2DAsync(dst, pitch, src, w, w, t->L, kind, s));
+  else
+    CUDA_TRY(cudaMemcpy2DAsync(dst, w, src, pitch, w, t->L, kind, s));
+  return TBSLAS_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* tbslas_status_string(int status) {
+  switch (status) {
+    case TBSLAS_OK: return "ok";
+    case TBSLAS_ERR_INVALID_ARG: return "invalid argument";
+    case TBSLAS_ERR_TREE: return "invalid tree";
+    case TBSLAS_ERR_CUDA: return "CUDA error";
+    case TBSLAS_ERR_UNSUPPORTED: return "unsupported";
+    case TBSLAS_ERR_ALLOC: return "allocation failed";
+    case TBSLAS_ERR_SIZE: return "size limit exceeded";
+    case TBSLAS_ERR_DEVICE: return "device-side error";
+    default: return "unknown status";
+  }
+}
+
+const char* tbslas_last_error(void) { return g_err.c_str(); }
+
+int tbslas_version(void) { return 1; }
+
+int tbslas_ctx_create(int device, tbslas_ctx* out) {
+  if (!out) return fail(TBSLAS_ERR_INVALID_ARG, "null output pointer");
+  *out = nullptr;
+  std::call_once(g_kernels_once, init_kernels);
+  int ndev = 0;
+  CUDA_TRY(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev)
+    return fail(TBSLAS_ERR_INVALID_ARG, "device %d outside [0,%d)", device, ndev);
+  CUDA_TRY(cudaSetDevice(device));
+  tbslas_ctx c = new tbslas_ctx_s();
+  c->device = device;
+  cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    tbslas_ctx_destroy(c);
+    return fail(TBSLAS_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
+  }
+  *out = c;
+  return TBSLAS_OK;
+}
+
+int tbslas_ctx_destroy(tbslas_ctx ctx) {
+  if (!ctx) return TBSLAS_OK;
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  for (auto& b : ctx->slots)
+    if (b.p) cudaFree(b.p);
+  for (auto p : ctx->d_M)
+    if (p) cudaFree(p);
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return TBSLAS_OK;
+}
+
+int tbslas_ctx_check(tbslas_ctx ctx, uint32_t* device_error) {
+  TRY(bind(ctx));
+  CUDA_TRY(cudaDeviceSynchronize());
+  uint32_t e = 0;
+  CUDA_TRY(cudaMemcpy(&e, ctx->d_err, sizeof(e), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemset(ctx->d_err, 0, sizeof(uint32_t)));
+  if (device_error) *device_error = e;
+  if (e) return fail(TBSLAS_ERR_DEVICE, "device error word 0x%x", e);
+  return TBSLAS_OK;
+}
+
+int tbslas_cheb_nodes(int q, double* out_host) {
+  if (q < 0 || q > TBSLAS_MAX_DEGREE) return fail(TBSLAS_ERR_UNSUPPORTED, "degree %d", q);
+  if (!out_host) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
+  std::vector<double> y = cheb_nodes_3d(q);
+  std::memcpy(out_host, y.data(), y.size() * sizeof(double));
+  return TBSLAS_OK;
+}
+
+int tbslas_pt2coeff_matrix(int q, double* M_host) {
+  if (q < 1 || q > TBSLAS_MAX_DEGREE) return fail(TBSLAS_ERR_UNSUPPORTED, "degree %d", q);
+  if (!M_host) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
+  const std::vector<double>& M = host_M(q);
+  std::memcpy(M_host, M.data(), M.size() * sizeof(double));
+  return TBSLAS_OK;
+}
+
+int tbslas_tree_create(tbslas_ctx ctx, int64_t n_leaves, const double* anchor_host,
+                       const int32_t* depth_host, int q, int dof, tbslas_tree* out) {
+  if (!out) return fail(TBSLAS_ERR_INVALID_ARG, "null output pointer");
+  *out = nullptr;
+  TRY(bind(ctx));
+  if (n_leaves < 1 || n_leaves > (int64_t)INT32_MAX)
+    return fail(TBSLAS_ERR_INVALID_ARG, "leaf count %lld", (long long)n_leaves);
+  if (!anchor_host || !depth_host) return fail(TBSLAS_ERR_INVALID_ARG, "null leaf arrays");
+  if (q < 1 || q > TBSLAS_MAX_DEGREE)
+    return fail(TBSLAS_ERR_UNSUPPORTED, "Chebyshev degree %d outside [1,%d]", q,
+                TBSLAS_MAX_DEGREE);
+  if (dof < 1 || dof > 16) return fail(TBSLAS_ERR_UNSUPPORTED, "dof %d outside [1,16]", dof);
+  tbslas_tree t = new tbslas_tree_s();
+  t->ctx = ctx;
+  t->L = n_leaves;
+  t->q = q;
+  t->dof = dof;
+  t->stride = (dof * n_coeff(q) + 1) & ~(int64_t)1;
+  int s = build_tree(t, anchor_host, depth_host);
+  if (s != TBSLAS_OK) {
+    std::string msg = g_err;
+    tbslas_tree_destroy(t);
+    g_err = msg;
+    return s;
+  }
+  *out = t;
+  return TBSLAS_OK;
+}
+
+int tbslas_tree_destroy(tbslas_tree t) {
+  if (!t) return TBSLAS_OK;
+  if (t->ctx) cudaSetDevice(t->ctx->device);
+  if (t->d_keys) cudaFree(t->d_keys);
+  if (t->d_geom) cudaFree(t->d_geom);
+  if (t->d_coeff) cudaFree(t->d_coeff);
+  if (t->d_table) cudaFree(t->d_table);
+  delete t;
+  return TBSLAS_OK;
+}
+
+int tbslas_tree_info(tbslas_tree t, int64_t* n_leaves, int* q, int* dof, int* max_depth) {
+  TRY(check_tree(t));
+  if (n_leaves) *n_leaves = t->L;
+  if (q) *q = t->q;
+  if (dof) *dof = t->dof;
+  if (max_depth) *max_depth = t->max_depth;
+  return TBSLAS_OK;
+}
+
+int tbslas_tree_set_coeffs_host(tbslas_tree t, const double* coeff_host) {
+  TRY(check_tree(t));
+  TRY(bind(t->ctx));
+  if (!coeff_host) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
+  TRY(copy_coeffs(t, t->d_coeff, coeff_host, true, cudaMemcpyHostToDevice, t->ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(t->ctx->stream));
+  return TBSLAS_OK;
+}
+
+int tbslas_tree_get_coeffs_host(tbslas_tree t, double* coeff_host) {
+  TRY(check_tree(t));
+  TRY(bind(t->ctx));
+  if (!coeff_host) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
+  CUDA_TRY(cudaDeviceSynchronize());
+  TRY(copy_coeffs(t, coeff_host, t->d_coeff, false, cudaMemcpyDeviceToHost, t->ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(t->ctx->stream));
+  return TBSLAS_OK;
+}
+
+int tbslas_tree_set_coeffs(tbslas_tree t, const double* coeff_dev, void* stream) {
+  TRY(check_tree(t));
+  TRY(bind(t->ctx));
+  if (!coeff_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
+  return copy_coeffs(t, t->d_coeff, coeff_dev, true, cudaMemcpyDeviceToDevice,
+                     (cudaStream_t)stream);
+}
+
+int tbslas_tree_get_coeffs(tbslas_tree t, double* coeff_dev, void* stream) {
+  TRY(check_tree(t));
+  TRY(bind(t->ctx));
+  if (!coeff_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
+  return copy_coeffs(t, coeff_dev, t->d_coeff, false, cudaMemcpyDeviceToDevice,
+                     (cudaStream_t)stream);
+}
+
+int tbslas_collect_grid_points(tbslas_ctx ctx, tbslas_tree tree, double* out_dev, void* stream) {
+  TRY(check_tree(tree));
+  TRY(bind(ctx));
+  if (!out_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
+  return collect_dev(tree, out_dev, (cudaStream_t)stream);
+}
+
+int tbslas_eval_tree(tbslas_ctx ctx, tbslas_tree tree, const double* pos_dev, int64_t n,
+                     double* out_dev, int bc, void* stream) {
+  TRY(check_tree(tree));
+  TRY(bind(ctx));
+  if (n < 0) return fail(TBSLAS_ERR_INVALID_ARG, "negative point count");
+  if (n > 0 && (!pos_dev || !out_dev)) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  return eval_tree_dev(ctx, tree, pos_dev, n, out_dev, bc, (cudaStream_t)stream);
+}
+
+int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_host, int64_t n,
+                          double* out_host, int bc) {
+  TRY(check_tree(tree));
+  TRY(bind(ctx));
+  if (n < 0) return fail(TBSLAS_ERR_INVALID_ARG, "negative point count");
+  if (n == 0) return TBSLAS_OK;
+  if (!pos_host || !out_host) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  double *pos, *out;
+  TRY(scratch_t(ctx, kHostIn, n * 3, &pos));
+  TRY(scratch_t(ctx, kHostOut, n * tree->dof, &out));
+  cudaStream_t s = ctx->stream;
+  CUDA_TRY(cudaMemcpyAsync(pos, pos_host, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
+  TRY(eval_tree_dev(ctx, tree, pos, n, out, bc, s));
+  CUDA_TRY(cudaMemcpyAsync(out_host, out, n * tree->dof * sizeof(double),
+                           cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return TBSLAS_OK;
+}
+
+int tbslas_traj_rk2(tbslas_ctx ctx, tbslas_tree vel, const double* x_dev, int64_t n,
+                    double tinit, double tfinal, int nrk, int bc, double* xdep_dev,
+                    void* stream) {
+  TRY(check_tree(vel));
+  TRY(bind(ctx));
+  if (vel->dof != 3) return fail(TBSLAS_ERR_INVALID_ARG, "velocity tree has dof %d, not 3", vel->dof);
+  if (n < 0 || nrk < 1) return fail(TBSLAS_ERR_INVALID_ARG, "n=%lld nrk=%d", (long long)n, nrk);
+  if (n > 0 && (!x_dev || !xdep_dev)) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  const double tau = (tfinal - tinit) / nrk;
+  if (n == 0) return TBSLAS_OK;
+  return traj_dev(ctx, vel, x_dev, n, tau, nrk, bc, xdep_dev, (cudaStream_t)stream);
+}
+
+int tbslas_set_tree_grid_values(tbslas_ctx ctx, tbslas_tree tree, const double* vals_dev,
+                                void* stream) {
+  TRY(check_tree(tree));
+  TRY(bind(ctx));
+  if (!vals_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null values");
+  return refit_dev(ctx, tree, vals_dev, (cudaStream_t)stream);
+}
+
+static int check_step_args(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, double dt, int nrk,
+                           int bc) {
+  TRY(check_tree(vel));
+  TRY(check_tree(con));
+  TRY(bind(ctx));
+  if (vel->ctx != ctx || con->ctx != ctx)
+    return fail(TBSLAS_ERR_INVALID_ARG, "trees belong to another context");
+  if (vel->dof != 3) return fail(TBSLAS_ERR_INVALID_ARG, "velocity tree has dof %d, not 3", vel->dof);
+  if (nrk < 1) return fail(TBSLAS_ERR_INVALID_ARG, "nrk %d < 1", nrk);
+  if (!std::isfinite(dt)) return fail(TBSLAS_ERR_INVALID_ARG, "dt is not finite");
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  return TBSLAS_OK;
+}
+
+int tbslas_semilag_in_situ(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
+                           double dt, int nrk, int bc, void* stream) {
+  TRY(check_step_args(ctx, vel, con, dt, nrk, bc));
+  return semilag_in_situ_dev(ctx, vel, con, timestep, dt, nrk, bc, (cudaStream_t)stream);
+}
+
+int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                double* con_coeff_host, int timestep, double dt, int nrk,
+                                int bc) {
+  TRY(check_step_args(ctx, vel, con, dt, nrk, bc));
+  if (!con_coeff_host) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
+  cudaStream_t s = ctx->stream;
+  TRY(copy_coeffs(con, con->d_coeff, con_coeff_host, true, cudaMemcpyHostToDevice, s));
+  TRY(semilag_in_situ_dev(ctx, vel, con, timestep, dt, nrk, bc, s));
+  TRY(copy_coeffs(con, con_coeff_host, con->d_coeff, false, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return TBSLAS_OK;
+}
+
+int tbslas_fast_interp(tbslas_ctx ctx, const double* grid_dev, int dof, int n_reg,
+                       const double* pts_dev, int64_t n, double* out_dev, int bc, void* stream) {
+  TRY(bind(ctx));
+  if (n_reg < 4) return fail(TBSLAS_ERR_INVALID_ARG, "grid size %d < 4", n_reg);
+  if ((int64_t)n_reg * n_reg * n_reg > (int64_t)1 << 40)
+    return fail(TBSLAS_ERR_SIZE, "grid size %d too large", n_reg);
+  if (dof < 1 || n < 0) return fail(TBSLAS_ERR_INVALID_ARG, "dof=%d n=%lld", dof, (long long)n);
+  if (n > 0 && (!grid_dev || !pts_dev || !out_dev))
+    return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  launch_fast_interp(grid_dev, dof, n_reg, pts_dev, n, out_dev, bc, (cudaStream_t)stream);
+  return check_launch("fast_interp");
+}
+
+static int check_grid_args(tbslas_ctx ctx, const void* vel, const void* con, const void* cout,
+                           int n_reg, double dt, int nrk, int bc) {
+  TRY(bind(ctx));
+  if (!vel || !con || !cout) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
+  if (con == cout) return fail(TBSLAS_ERR_INVALID_ARG, "con_out aliases con");
+  if (n_reg < 4) return fail(TBSLAS_ERR_INVALID_ARG, "grid size %d < 4", n_reg);
+  if ((int64_t)n_reg * n_reg * n_reg > (int64_t)1 << 40)
+    return fail(TBSLAS_ERR_SIZE, "grid size %d too large", n_reg);
+  if (nrk < 1) return fail(TBSLAS_ERR_INVALID_ARG, "nrk %d < 1", nrk);
+  if (!std::isfinite(dt)) return fail(TBSLAS_ERR_INVALID_ARG, "dt is not finite");
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  return TBSLAS_OK;
+}
+
+int tbslas_semilag_grid(tbslas_ctx ctx, const double* vel_dev, const double* con_dev,
+                        double* con_out_dev, int n_reg, double dt, int nrk, int bc,
+                        void* stream) {
+  TRY(check_grid_args(ctx, vel_dev, con_dev, con_out_dev, n_reg, dt, nrk, bc));
+  const double tau = (-dt - 0.0) / nrk;
+  launch_semilag_grid(vel_dev, con_dev, con_out_dev, n_reg, tau, nrk, bc, (cudaStream_t)stream);
+  return check_launch("semilag_grid");
+}
+
+int tbslas_semilag_grid_host(tbslas_ctx ctx, const double* vel_host, const double* con_host,
+                             double* con_out_host, int n_reg, double dt, int nrk, int bc) {
+  TRY(check_grid_args(ctx, vel_host, con_host, con_out_host, n_reg, dt, nrk, bc));
+  const int64_t n3 = (int64_t)n_reg * n_reg * n_reg;
+  double *vel, *con, *cout;
+  TRY(scratch_t(ctx, kHostIn, n3 * 3, &vel));
+  TRY(scratch_t(ctx, kHostIn2, n3, &con));
+  TRY(scratch_t(ctx, kHostOut, n3, &cout));
+  cudaStream_t s = ctx->stream;
+  CUDA_TRY(cudaMemcpyAsync(vel, vel_host, n3 * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(con, con_host, n3 * sizeof(double), cudaMemcpyHostToDevice, s));
+  const double tau = (-dt - 0.0) / nrk;
+  launch_semilag_grid(vel, con, cout, n_reg, tau, nrk, bc, s);
+  TRY(check_launch("semilag_grid"));
+  CUDA_TRY(cudaMemcpyAsync(con_out_host, cout, n3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return TBSLAS_OK;
+}
+
+}  // extern "C"

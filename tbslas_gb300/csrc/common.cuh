@@ -1,0 +1,188 @@
+// Device-side building blocks of the SL path: Morton keys, leaf lookup,
+// Chebyshev recurrences and the triangular tensor Chebyshev sum.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tbslas_gb300.h"
+
+namespace tbg {
+
+// Bits per axis of a point / leaf Morton key.  Leaves may be at most this
+// deep.  PVFMM keys points at MAX_DEPTH = 30 bits; for leaves of depth <= 21
+// the leaf a point falls in is the same at 21 bits (the low 27 interleaved
+// bits of a leaf anchor are zero), so 63-bit keys lose nothing.
+constexpr int kKeyBits = 21;
+constexpr uint64_t kKeyScale = 1ull << kKeyBits;
+
+// Spread the low 21 bits of v so that bit b lands on bit 3b.
+__host__ __device__ inline uint64_t spread3(uint64_t v) {
+  v &= 0x1fffffull;
+  v = (v | (v << 32)) & 0x1f00000000ffffull;
+  v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+  v = (v | (v << 8)) & 0x100f00f00f00f00full;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
+
+// Interleaved key: inside each level z is the most significant bit, then y,
+// then x -- the order of pvfmm::MortonId's comparison and of the leaves'
+// post-order (child index x + 2y + 4z).
+__host__ __device__ inline uint64_t morton3(uint64_t x, uint64_t y, uint64_t z) {
+  return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
+// Single periodic wrap of one coordinate, src/tree/tree_functor.h:442-448.
+__device__ __forceinline__ double wrap1(double c) {
+  if (c < 0.0) c = c + 1.0;
+  if (c >= 1.0) c = c - 1.0;
+  return c;
+}
+
+// Axis coordinate -> 21-bit integer.  The caller has checked 0 <= c <= 1
+// (c < 1 under periodic).  c == 1.0 is shifted into the last cell as the
+// reference does for non-periodic trees (src/tree/tree_functor.h:464-479).
+__device__ __forceinline__ uint64_t quantise(double c) {
+  return c >= 1.0 ? (kKeyScale - 1) : (uint64_t)(c * (double)kKeyScale);
+}
+
+// Is the (already wrapped) point inside the domain?  NaN compares false.
+__device__ __forceinline__ bool inside(double x, double y, double z, bool periodic) {
+  if (periodic)
+    return x >= 0.0 && x < 1.0 && y >= 0.0 && y < 1.0 && z >= 0.0 && z < 1.0;
+  return x >= 0.0 && x <= 1.0 && y >= 0.0 && y <= 1.0 && z >= 0.0 && z <= 1.0;
+}
+
+// Per-leaf geometry: anchor x, y, z and w = 2*2^depth (the scale that maps
+// the leaf onto [-1,1], src/tree/tree_functor.h:286-294).
+struct __align__(32) Geom {
+  double x, y, z, w;
+};
+__device__ __forceinline__ Geom load_geom(const Geom* p) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  return Geom{a.x, a.y, b.x, b.y};
+}
+
+// Read-only view of a device tree.
+struct TreeView {
+  const uint64_t* __restrict__ keys;   // [L] anchor keys, strictly increasing
+  const Geom* __restrict__ geom;       // [L]
+  const double* __restrict__ coeff;    // [L * stride]
+  const int32_t* __restrict__ table;   // [8^T + 1] coarse-cell -> first leaf
+  int64_t L;
+  int64_t stride;  // doubles per leaf (dof*Nc rounded up to an even count)
+  int T;           // level of the coarse lookup table
+  int q;
+  int dof;
+};
+
+// Index of the leaf containing a point key: the last leaf whose anchor key is
+// <= the point key, i.e. the partition std::lower_bound builds over sorted
+// point keys in EvalNodesLocal (src/tree/tree_functor.h:193-198).  The coarse
+// table narrows the search to the leaves inside one level-T cell.
+__device__ __forceinline__ int64_t find_leaf(const TreeView& t, uint64_t key) {
+  const uint64_t cell = key >> (3 * (kKeyBits - t.T));
+  int64_t lo = __ldg(t.table + cell);
+  int64_t hi = __ldg(t.table + cell + 1);
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (__ldg(t.keys + mid) <= key) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// T_0..T_{D-1}(xi); all zero when |xi| > 1 or xi is NaN (pvfmm::cheb_poly as
+// called at src/tree/tree_functor.h:328-330).
+template <int D>
+__device__ __forceinline__ void cheb_T(double xi, double (&T)[D]) {
+  const bool ok = fabs(xi) <= 1.0;
+  const double x = ok ? xi : 0.0;
+  T[0] = ok ? 1.0 : 0.0;
+  if (D > 1) T[1] = x;
+  const double x2 = 2.0 * x;
+#pragma unroll
+  for (int k = 2; k < D; ++k) T[k] = x2 * T[k - 1] - T[k - 2];
+}
+
+// Triangular tensor Chebyshev sum of one dof:
+//   sum_i tz_i sum_{j<D-i} ty_j sum_{k<D-i-j} c[i][j][k] tx_k
+// with the reference's summation order (pvfmm::vec_eval,
+// src/tree/tree_functor.h:38-77).  Fully unrolled; c is read with
+// compile-time offsets.
+template <int D, class Load>
+__device__ __forceinline__ double tri_sum(Load c, const double (&tx)[D], const double (&ty)[D],
+                                          const double (&tz)[D]) {
+  double u = 0.0;
+  int idx = 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    double v = 0.0;
+#pragma unroll
+    for (int j = 0; j < D - i; ++j) {
+      double w = 0.0;
+#pragma unroll
+      for (int k = 0; k < D - i - j; ++k) {
+        w = fma(c(idx), tx[k], w);
+        ++idx;
+      }
+      v = fma(ty[j], w, v);
+    }
+    u = fma(tz[i], v, u);
+  }
+  return u;
+}
+
+struct GlobalLoad {
+  const double* __restrict__ p;
+  __device__ __forceinline__ double operator()(int i) const { return __ldg(p + i); }
+};
+struct SharedLoad {
+  const double* p;
+  __device__ __forceinline__ double operator()(int i) const { return p[i]; }
+};
+
+// Evaluate DOF components of a tree at one point.  The point is wrapped in
+// place under periodic boundaries (the caller sees the wrapped point, as
+// with EvalTree's in-place wrap, src/tree/tree_functor.h:442-448).
+template <int D, int DOF>
+__device__ __forceinline__ void eval_point(const TreeView& t, double& x, double& y, double& z,
+                                           bool periodic, double (&out)[DOF]) {
+  constexpr int NC = D * (D + 1) * (D + 2) / 6;
+  if (periodic) {
+    x = wrap1(x);
+    y = wrap1(y);
+    z = wrap1(z);
+  }
+  if (!inside(x, y, z, periodic)) {
+#pragma unroll
+    for (int l = 0; l < DOF; ++l) out[l] = 0.0;
+    return;
+  }
+  const uint64_t key = morton3(quantise(x), quantise(y), quantise(z));
+  const int64_t leaf = find_leaf(t, key);
+  const Geom g = load_geom(t.geom + leaf);
+  double tx[D], ty[D], tz[D];
+  cheb_T<D>((x - g.x) * g.w - 1.0, tx);
+  cheb_T<D>((y - g.y) * g.w - 1.0, ty);
+  cheb_T<D>((z - g.z) * g.w - 1.0, tz);
+  const double* c = t.coeff + leaf * t.stride;
+#pragma unroll
+  for (int l = 0; l < DOF; ++l) out[l] = tri_sum<D>(GlobalLoad{c + l * NC}, tx, ty, tz);
+}
+
+// 1-D Chebyshev nodes on [0,1] (new_nodes, src/utils/cheb.h:50-58) passed by
+// value to kernels.
+struct Nodes1D {
+  double x[TBSLAS_MAX_DEGREE + 1];
+};
+
+// Device error word bits.
+enum : uint32_t {
+  kErrBarrierTimeout = 1u << 0,
+  kErrBadLeaf = 1u << 1,
+};
+
+}  // namespace tbg

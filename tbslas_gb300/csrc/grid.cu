@@ -1,0 +1,187 @@
+// Tricubic regular-grid path: the interpolant tbslas::fast_interp
+// (src/tree/tree_functor.h:89-153) and a fused SL step on the grid (every node
+// a target, RK2 through the interpolated velocity, interpolated concentration
+// at the departure point).
+//
+// Grid layout as the reference: SoA, vals[x + N(y + N z) + k N^3].
+//  FREESPACE: nodes i/(N-1); stencil base floor(x(N-1))-1 clamped to
+//             [0, N-4]; points outside [0,1]^3 give 0 (the reference's form).
+//  PERIODIC:  nodes i/N on [0,1); the query is wrapped once (as EvalTree
+//             wraps), stencil base floor(xN)-1, indices taken mod N.
+#include "internal.h"
+
+namespace tbg {
+
+// Cubic Lagrange weights at offset t from the stencil base, formed exactly as
+// the reference does (denominators by repeated division, then the product of
+// (t - l) over l != k in increasing l): src/tree/tree_functor.h:93-99,
+// :126-135.
+__device__ __forceinline__ void lagrange4(double t, double (&w)[4]) {
+  const double den[4] = {-1.0 / 6.0, 0.5, -0.5, 1.0 / 6.0};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double m = den[k];
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+      if (k != l) m *= (t - (double)l);
+    w[k] = m;
+  }
+}
+
+struct Stencil {
+  int64_t ix[4], iy[4], iz[4];  // x offsets, y*N, z*N*N
+  double wx[4], wy[4], wz[4];
+};
+
+// Builds the stencil of a point; returns false when the point evaluates to 0.
+// Under PERIODIC the coordinates are wrapped in place.
+__device__ __forceinline__ bool make_stencil(double& x, double& y, double& z, int N,
+                                             bool periodic, Stencil& s) {
+  if (periodic) {
+    x = wrap1(x);
+    y = wrap1(y);
+    z = wrap1(z);
+  }
+  if (!inside(x, y, z, periodic)) return false;
+  const double scale = periodic ? (double)N : (double)(N - 1);
+  const double c[3] = {x, y, z};
+  int64_t base[3];
+  double t[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double p = c[j] * scale;
+    int64_t g = (int64_t)p - 1;
+    if (!periodic) {
+      if (g < 0) g = 0;
+      if (g > N - 4) g = N - 4;
+    }
+    base[j] = g;
+    t[j] = p - (double)g;
+  }
+  lagrange4(t[0], s.wx);
+  lagrange4(t[1], s.wy);
+  lagrange4(t[2], s.wz);
+  const int64_t NN = (int64_t)N * N;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    int64_t gx = base[0] + k, gy = base[1] + k, gz = base[2] + k;
+    if (periodic) {
+      gx = gx < 0 ? gx + N : (gx >= N ? gx - N : gx);
+      gy = gy < 0 ? gy + N : (gy >= N ? gy - N : gy);
+      gz = gz < 0 ? gz + N : (gz >= N ? gz - N : gz);
+    }
+    s.ix[k] = gx;
+    s.iy[k] = gy * N;
+    s.iz[k] = gz * NN;
+  }
+  return true;
+}
+
+// sum_{j2} wz sum_{j1} wy sum_{j0} wx v : separable form of the reference's
+// 64-term sum (same terms, grouped per axis).
+__device__ __forceinline__ double apply_stencil(const double* __restrict__ g, const Stencil& s) {
+  double u = 0.0;
+#pragma unroll
+  for (int j2 = 0; j2 < 4; ++j2) {
+    double v = 0.0;
+#pragma unroll
+    for (int j1 = 0; j1 < 4; ++j1) {
+      const double* row = g + s.iz[j2] + s.iy[j1];
+      double w = 0.0;
+#pragma unroll
+      for (int j0 = 0; j0 < 4; ++j0) w = fma(s.wx[j0], __ldg(row + s.ix[j0]), w);
+      v = fma(s.wy[j1], w, v);
+    }
+    u = fma(s.wz[j2], v, u);
+  }
+  return u;
+}
+
+__global__ void __launch_bounds__(256) k_fast_interp(const double* __restrict__ grid, int dof,
+                                                     int N, const double* __restrict__ pts,
+                                                     int64_t n, double* __restrict__ out,
+                                                     int periodic) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+  Stencil s;
+  const int64_t N3 = (int64_t)N * N * N;
+  if (!make_stencil(x, y, z, N, periodic != 0, s)) {
+    for (int k = 0; k < dof; ++k) out[i * dof + k] = 0.0;
+    return;
+  }
+  for (int k = 0; k < dof; ++k) out[i * dof + k] = apply_stencil(grid + k * N3, s);
+}
+
+// Fused grid SL step, one thread per node (x fastest: coalesced node reads
+// and output writes).  On a periodic power-of-two grid the first velocity
+// evaluation of the first sub-step sits exactly on the node (the Lagrange
+// weights there are exactly 0,1,0,0), so it is read, not interpolated.
+__global__ void __launch_bounds__(256) k_semilag_grid(const double* __restrict__ vel,
+                                                      const double* __restrict__ con,
+                                                      double* __restrict__ cout, int N,
+                                                      double tau, int nrk, int periodic,
+                                                      int node_read) {
+  const int64_t N3 = (int64_t)N * N * N;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= N3) return;
+  const bool per = periodic != 0;
+  const double h = per ? 1.0 / N : 1.0 / (N - 1);
+  const int64_t ix = t % N, iy = (t / N) % N, iz = t / ((int64_t)N * N);
+  double x = (double)ix * h, y = (double)iy * h, z = (double)iz * h;
+  const double half_tau = 0.5 * tau;
+  double px = x, py = y, pz = z;
+#pragma unroll 1
+  for (int st = 0; st < 2 * nrk; ++st) {
+    double v[3];
+    if (st == 0 && node_read) {
+      v[0] = __ldg(vel + t);
+      v[1] = __ldg(vel + N3 + t);
+      v[2] = __ldg(vel + 2 * N3 + t);
+    } else {
+      Stencil s;
+      if (make_stencil(px, py, pz, N, per, s)) {
+        v[0] = apply_stencil(vel, s);
+        v[1] = apply_stencil(vel + N3, s);
+        v[2] = apply_stencil(vel + 2 * N3, s);
+      } else {
+        v[0] = v[1] = v[2] = 0.0;
+      }
+    }
+    if ((st & 1) == 0) {
+      x = px;
+      y = py;
+      z = pz;
+      px = x + half_tau * v[0];
+      py = y + half_tau * v[1];
+      pz = z + half_tau * v[2];
+    } else {
+      x = x + tau * v[0];
+      y = y + tau * v[1];
+      z = z + tau * v[2];
+      px = x;
+      py = y;
+      pz = z;
+    }
+  }
+  Stencil s;
+  cout[t] = make_stencil(x, y, z, N, per, s) ? apply_stencil(con, s) : 0.0;
+}
+
+void launch_fast_interp(const double* grid, int dof, int nreg, const double* pts, int64_t n,
+                        double* out, int periodic, cudaStream_t s) {
+  if (n <= 0) return;
+  k_fast_interp<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(grid, dof, nreg, pts, n, out,
+                                                            periodic);
+}
+
+void launch_semilag_grid(const double* vel, const double* con, double* cout, int nreg,
+                         double tau, int nrk, int periodic, cudaStream_t s) {
+  const int64_t n = (int64_t)nreg * nreg * nreg;
+  const bool pow2 = (nreg & (nreg - 1)) == 0;
+  const int node_read = (periodic && pow2) ? 1 : 0;
+  k_semilag_grid<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(vel, con, cout, nreg, tau, nrk,
+                                                             periodic, node_read);
+}
+
+}  // namespace tbg

@@ -1,0 +1,86 @@
+// Declarations shared by the translation units of libtbslas_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace tbg {
+
+// One tile of the bucketed functor evaluation: `count` (<= kTile) points of
+// one leaf, stored at perm[start, start+count).
+struct Tile {
+  int64_t start;
+  int32_t leaf;
+  int32_t count;
+};
+constexpr int kTile = 128;
+
+struct SemilagTreeArgs {
+  TreeView vel;       // dof 3
+  TreeView con;       // dof 1, same degree as vel
+  Nodes1D nodes;      // 1-D nodes of con's degree
+  double tau;         // -dt / nrk
+  int nrk;
+  int periodic;
+  double* vals;       // [Lc * Np] node values at the departure points
+};
+
+struct TrajArgs {
+  TreeView vel;
+  const double* x;
+  int64_t n;
+  double tau;
+  int nrk;
+  int periodic;
+  double* xdep;
+};
+
+struct EvalTilesArgs {
+  TreeView tree;
+  const double* pos;
+  const int64_t* perm;
+  const Tile* tiles;
+  const int64_t* ntiles;  // device scalar
+  int periodic;
+  double* out;
+  uint32_t* err;
+  int grid;
+};
+
+typedef void (*SemilagTreeFn)(const SemilagTreeArgs&, cudaStream_t);
+typedef void (*TrajFn)(const TrajArgs&, cudaStream_t);
+typedef void (*EvalTilesFn)(const EvalTilesArgs&, cudaStream_t);
+
+struct DegreeKernels {
+  SemilagTreeFn semilag = nullptr;
+  TrajFn traj = nullptr;
+  EvalTilesFn eval_tiles = nullptr;
+  int eval_tiles_max_threads_hint = 0;
+};
+
+// Filled by the per-degree translation units (index = Chebyshev degree q).
+void register_degrees_a(DegreeKernels* table);
+void register_degrees_b(DegreeKernels* table);
+void register_degrees_c(DegreeKernels* table);
+void register_degrees_d(DegreeKernels* table);
+void register_degrees_e(DegreeKernels* table);
+void register_degrees_f(DegreeKernels* table);
+void register_degrees_g(DegreeKernels* table);
+void register_degrees_h(DegreeKernels* table);
+
+// refit.cu: coeff[(r/dof)*stride + (r%dof)*nc + n] = sum_p vals[r*np+p] M[p*nc+n]
+void launch_refit(const double* vals, const double* M, int64_t rows, int np, int nc, int dof,
+                  int64_t stride, double* coeff, cudaStream_t s);
+
+// misc kernels (capi.cu)
+void launch_collect(const TreeView& t, const Nodes1D& nodes, double* out, cudaStream_t s);
+
+// grid.cu
+void launch_fast_interp(const double* grid, int dof, int nreg, const double* pts, int64_t n,
+                        double* out, int periodic, cudaStream_t s);
+void launch_semilag_grid(const double* vel, const double* con, double* cout, int nreg,
+                         double tau, int nrk, int periodic, cudaStream_t s);
+
+}  // namespace tbg

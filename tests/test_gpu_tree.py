@@ -1,0 +1,204 @@
+"""GPU parity of the tree path (C ABI -> CUDA) against the oracle.
+
+Tolerance: FP64, max |gpu - oracle| <= 1e-12 * max |oracle| (L-infinity
+relative) on node values, point values and coefficients; the integer work
+(leaf buckets, collected node coordinates) is compared exactly."""
+import math
+
+import numpy as np
+import pytest
+
+import tbslas_gb300 as tb
+from tbslas_gb300 import capi, fields, trees
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+
+def _tree_case(kind, q, dof, seed=0):
+    rng = np.random.default_rng(seed)
+    if kind == "uniform":
+        anchor, depth = trees.uniform_tree(2)
+    else:
+        g = fields.gaussian((0.35, 0.6, 0.45), 0.07)
+        anchor, depth = trees.adaptive_tree(g, 4, 1, 1e-3, 1, 4)
+    coeff = rng.standard_normal((len(depth), dof, tb.n_coeff(q)))
+    coeff /= (1 + np.arange(tb.n_coeff(q)))[None, None, :]
+    return anchor, depth, coeff
+
+
+def _points(rng, n):
+    pts = rng.uniform(-0.05, 1.05, size=(n, 3))
+    special = np.array([[1.0, 0.5, 0.5], [0.0, 0.0, 0.0], [1.0, 1.0, 1.0], [0.5, 0.5, 0.5],
+                        [0.25, 0.75, 1.0], [np.nan, 0.5, 0.5], [0.5, -0.0, 0.5],
+                        [1.0 - 2 ** -53, 0.5, 0.5], [0.125, 0.125, 0.125]])
+    pts[:len(special)] = special
+    return pts
+
+
+@pytest.mark.parametrize("kind", ["uniform", "adaptive"])
+@pytest.mark.parametrize("q,dof", [(2, 1), (5, 3), (8, 1), (8, 3), (14, 1)])
+@pytest.mark.parametrize("bc", [0, 1])
+def test_eval_tree_matches_oracle(ctx, ora, kind, q, dof, bc):
+    anchor, depth, coeff = _tree_case(kind, q, dof, seed=q)
+    rng = np.random.default_rng(10 + q)
+    pts = _points(rng, 20000)
+    t = tb.Tree(ctx, anchor, depth, q, dof, coeff)
+    f = tb.NodeFieldFunctor(t, bc)
+    out = f(_dev(pts)).cpu().numpy()
+    ref = ora.eval_tree(anchor, depth, q, dof, coeff, pts, periodic=bool(bc))
+    assert rel_err(out, ref) <= TOL
+    assert np.array_equal(out == 0, ref == 0)
+    host = f(pts)
+    assert np.array_equal(host, out)
+
+
+def test_eval_tree_empty_and_errors(ctx):
+    import torch
+    anchor, depth = trees.uniform_tree(1)
+    t = tb.Tree(ctx, anchor, depth, 3, 1)
+    out = tb.NodeFieldFunctor(t)(torch.empty((0, 3), dtype=torch.float64, device="cuda"))
+    assert out.shape == (0, 1)
+    with pytest.raises(capi.TbslasError) as e:
+        tb.Tree(ctx, anchor[:-1], depth[:-1], 3, 1)
+    assert e.value.status == 2
+    with pytest.raises(capi.TbslasError) as e:
+        tb.Tree(ctx, anchor[::-1], depth[::-1], 3, 1)
+    assert e.value.status == 2
+    bad = anchor.copy()
+    bad[0, 0] = 0.1
+    with pytest.raises(capi.TbslasError) as e:
+        tb.Tree(ctx, bad, depth, 3, 1)
+    assert e.value.status == 2
+    with pytest.raises(capi.TbslasError) as e:
+        tb.Tree(ctx, anchor, depth, 17, 1)
+    assert e.value.status == 4
+    with pytest.raises(capi.TbslasError) as e:
+        tb.NodeFieldFunctor(t, bc=7)(np.zeros((4, 3)))
+    assert e.value.status == 1
+
+
+def test_collect_grid_points_exact(ctx, ora):
+    g = fields.gaussian((0.5, 0.4, 0.6), 0.06)
+    anchor, depth = trees.adaptive_tree(g, 3, 1, 1e-3, 1, 4)
+    for q in (3, 8):
+        t = tb.Tree(ctx, anchor, depth, q, 1)
+        out = tb.collect_cheb_tree_grid_points(t).cpu().numpy()
+        assert np.array_equal(out, ora.collect_grid_points(anchor, depth, q))
+
+
+@pytest.mark.parametrize("q,dof", [(4, 1), (8, 3), (14, 1)])
+def test_set_tree_grid_values_matches_oracle(ctx, ora, q, dof):
+    rng = np.random.default_rng(q)
+    anchor, depth = trees.uniform_tree(2)
+    L, np_ = len(depth), (q + 1) ** 3
+    vals = rng.standard_normal((L, dof, np_))
+    t = tb.Tree(ctx, anchor, depth, q, dof)
+    tb.set_tree_grid_values(t, _dev(vals))
+    ref = ora.set_tree_grid_values(L, q, dof, vals)
+    assert rel_err(t.get_coeffs(), ref) <= TOL
+
+
+@pytest.mark.parametrize("bc,nrk", [(0, 1), (1, 1), (0, 3)])
+def test_traj_rk2_matches_oracle(ctx, ora, bc, nrk):
+    q = 8
+    anchor, depth = trees.uniform_tree(2)
+    vc = trees.fit(fields.taylor_green(), anchor, depth, q, 3)
+    t = tb.Tree(ctx, anchor, depth, q, 3, vc)
+    rng = np.random.default_rng(3)
+    x = rng.uniform(0, 1, size=(5000, 3))
+    out = tb.compute_traj_rk2(tb.NodeFieldFunctor(t, bc), _dev(x), 0.3, 0.3 - 0.05, nrk)
+    ref = ora.traj_rk2(anchor, depth, q, vc, x, 0.3, 0.3 - 0.05, nrk, periodic=bool(bc))
+    assert np.abs(out.cpu().numpy() - ref).max() <= 1e-14
+
+
+def _sl_case(kind, qv, qc, dofc, rng):
+    if kind == "uniform":
+        av, dv = trees.uniform_tree(2)
+        ac, dc = trees.uniform_tree(2)
+    else:
+        av, dv = trees.adaptive_tree(fields.taylor_green(), 4, 3, 1e-2, 1, 3)
+        g = fields.gaussian_blobs(rng, 3, (0.05, 0.1))
+        ac, dc = trees.adaptive_tree(g, 4, 1, 1e-3, 1, 4)
+    vc = trees.fit(fields.taylor_green(), av, dv, qv, 3)
+    blobs = fields.gaussian_blobs(rng, 2, (0.08, 0.12))
+    cc = trees.fit(lambda p: np.repeat(blobs(p), dofc, axis=1) * (1 + np.arange(dofc)),
+                   ac, dc, qc, dofc)
+    return (av, dv, vc), (ac, dc, cc)
+
+
+@pytest.mark.parametrize("kind", ["uniform", "adaptive"])
+@pytest.mark.parametrize("qv,qc,dofc", [(8, 8, 1), (5, 5, 1), (6, 4, 1), (4, 4, 2)])
+@pytest.mark.parametrize("bc,nrk", [(0, 1), (1, 2)])
+def test_semilag_in_situ_matches_oracle(ctx, ora, kind, qv, qc, dofc, bc, nrk):
+    rng = np.random.default_rng(qv * 10 + qc)
+    (av, dv, vc), (ac, dc, cc) = _sl_case(kind, qv, qc, dofc, rng)
+    tv = tb.Tree(ctx, av, dv, qv, 3, vc)
+    tc = tb.Tree(ctx, ac, dc, qc, dofc, cc)
+    vel = tb.NodeFieldFunctor(tv, bc)
+    ref_con = dict(anchor=ac, depth=dc, q=qc, dof=dofc, coeff=cc.copy())
+    ref_vel = dict(anchor=av, depth=dv, q=qv, dof=3, coeff=vc)
+    dt = 0.02
+    for step in (1, 2):
+        tb.solve_semilag_in_situ(vel, tc, step, dt, nrk)
+        ref_con["coeff"] = ora.semilag_in_situ(ref_vel, ref_con, step, dt, nrk, periodic=bool(bc))
+        assert rel_err(tc.get_coeffs(), ref_con["coeff"]) <= TOL, step
+
+
+def test_semilag_in_situ_host_equals_device(ctx):
+    rng = np.random.default_rng(5)
+    (av, dv, vc), (ac, dc, cc) = _sl_case("uniform", 6, 6, 1, rng)
+    tv = tb.Tree(ctx, av, dv, 6, 3, vc)
+    tc = tb.Tree(ctx, ac, dc, 6, 1, cc)
+    vel = tb.NodeFieldFunctor(tv)
+    tb.solve_semilag_in_situ(vel, tc, 1, 0.01)
+    dev = tc.get_coeffs()
+    host = cc.copy()
+    tb.solve_semilag_in_situ(vel, tc, 1, 0.01, coeff_host=host)
+    assert np.array_equal(host, dev)
+
+
+def test_config1_full_size_one_step_matches_oracle(ctx, ora):
+    """Depth-4 uniform tree (4096 leaves), q=8, rotation omega=2pi, Gaussian
+    sigma=0.05 at (0.7,0.5,0.5), dt=0.01: one full SL step (2,985,984
+    departure points) against the oracle."""
+    q = 8
+    anchor, depth = trees.uniform_tree(4)
+    vc = trees.fit(fields.rotation(2 * math.pi), anchor, depth, q, 3)
+    cc = trees.fit(fields.gaussian((0.7, 0.5, 0.5), 0.05), anchor, depth, q, 1)
+    tv = tb.Tree(ctx, anchor, depth, q, 3, vc)
+    tc = tb.Tree(ctx, anchor, depth, q, 1, cc)
+    tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv), tc, 1, 0.01)
+    ref = ora.semilag_in_situ(dict(anchor=anchor, depth=depth, q=q, dof=3, coeff=vc),
+                              dict(anchor=anchor, depth=depth, q=q, dof=1, coeff=cc), 1, 0.01)
+    assert rel_err(tc.get_coeffs(), ref) <= TOL
+
+
+def test_config1_full_size_translation_exact(ctx):
+    """Size-independent property at full size: constant velocity and a
+    polynomial of total degree <= q are advected exactly wherever the
+    departure points stay inside the domain."""
+    q = 8
+    anchor, depth = trees.uniform_tree(4)
+    v = np.array([0.4, -0.3, 0.2])
+    dt = 0.03
+    poly = lambda p: (1 + p[:, 0] ** 3 * p[:, 1] ** 2 - 2 * p[:, 2] ** 8 + p[:, 0] * p[:, 1] * p[:, 2] ** 6)[:, None]
+    tv = tb.Tree(ctx, anchor, depth, q, 3, trees.fit(lambda p: np.tile(v, (len(p), 1)), anchor, depth, q, 3))
+    tc = tb.Tree(ctx, anchor, depth, q, 1, trees.fit(poly, anchor, depth, q, 1))
+    tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv), tc, 1, dt)
+    exact = trees.fit(lambda p: poly(p - dt * v), anchor, depth, q, 1)
+    h = 1.0 / 16
+    safe = np.all((anchor - dt * v >= 0) & (anchor + h - dt * v <= 1), axis=1)
+    got = tc.get_coeffs()
+    assert safe.sum() > 3000
+    assert rel_err(got[safe], exact[safe]) <= 1e-11
