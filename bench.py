@@ -1,0 +1,434 @@
+#!/usr/bin/env python
+"""Throughput of the semi-Lagrangian advection step on GB300.
+
+One step = one in-situ SL step of the whole concentration tree: every
+Chebyshev node is backtraced (RK2) through the velocity tree, the
+concentration is evaluated at the departure points and every leaf is refitted
+(SolveSemilagInSitu, src/tree/tree_semilag.h:92-135).  Metric: departure
+points per second.  Default workload: the adaptive q=14 configuration
+(Taylor-Green velocity, 4 Gaussians, tolerance 1e-6, depths 3..8, CFL 1).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+  python bench.py --impl reference ...   # the reference algorithm on the host cores
+
+With N > 1 (torchrun, one rank per GPU) every rank advances its own replica
+(the path is replicated, not partitioned: no collective on the data path);
+value = all ranks' departure points / the slowest rank's time.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "SL departure-points/s on 1 GB300 at ≤1e-10 rel err; batched vs plain; adj/fwd"
+UNIT = "departure points/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def flops_per_point_tree(q, nrk=1):
+    """Algorithmic FLOPs of one SL step per departure point, counted as the
+    reference counts them: per evaluation 3*d*3 + 2*Nc*dof
+    (src/tree/tree_functor.h:389-394), 2*3*3 per RK2 sub-step
+    (src/semilag/traj.inc:44), and 2*Nc per node for the refit GEMM
+    (src/tree/tree_utils.h:538-551).  Returns (step total, fused-kernel part)."""
+    d = q + 1
+    nc = d * (d + 1) * (d + 2) // 6
+    ev = lambda dof: 9 * d + 2 * nc * dof
+    kernel = nrk * (2 * ev(3) + 18) + ev(1)
+    return kernel + 2 * nc, kernel
+
+
+def bytes_per_point_tree(q, vel_leaves, con_leaves):
+    """Compulsory HBM bytes per departure point: each velocity and
+    concentration coefficient read once, one node value written and read back
+    by the refit, each new coefficient written once."""
+    d = q + 1
+    nc = d * (d + 1) * (d + 2) // 6
+    npt = con_leaves * d ** 3
+    coeff_reads = 8.0 * nc * (3 * vel_leaves + con_leaves) / npt
+    kernel = coeff_reads + 8.0
+    step = kernel + 8.0 + 8.0 * nc * con_leaves / npt
+    return step, kernel
+
+
+# FLOPs per point of the grid step: midpoint velocity (weights 3x12 + 3
+# components x 144) + departure concentration (36 + 144) + RK updates 18; the
+# first velocity sits on a node (exact read).
+GRID_FLOPS_PER_POINT = (36 + 3 * 144) + (36 + 144) + 18
+GRID_BYTES_PER_POINT = 40  # 3 velocity + 1 concentration read, 1 written (FP64)
+
+
+# ---------------------------------------------------------------------------
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def aggregate(points, seconds, world):
+    """Whole-job throughput: sum of points over ranks / max time over ranks."""
+    if world == 1:
+        return points, seconds
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=dev)
+    p = torch.tensor([float(points)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(p, op=dist.ReduceOp.SUM)
+    return p.item(), t.item()
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            return json.load(open(path)), "measured"
+        except ValueError:
+            pass
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline_tree(wl, budget_s=12.0, steps=1):
+    """The oracle (OpenMP C++ restatement of the reference CPU path) on a
+    bounded sample of the workload: the targets of the first k leaves of the
+    concentration tree, k sized for ~budget_s of CPU work."""
+    from oracle import oracle as ora
+    cores = ora.num_threads()
+    vel = dict(anchor=wl.va, depth=wl.vd, q=wl.q, dof=3, coeff=wl.vc)
+    con = dict(anchor=wl.ca, depth=wl.cd, q=wl.q, dof=1, coeff=wl.cc)
+    ora.pt2coeff(wl.q)
+    npl = (wl.q + 1) ** 3
+    probe = min(4, len(wl.cd))
+    t0 = time.perf_counter()
+    ora.semilag_in_situ(vel, con, 1, wl.dt, 1, bool(wl.bc), leaf_begin=0, leaf_end=probe)
+    per_leaf = max((time.perf_counter() - t0) / probe, 1e-6)
+    k = int(max(probe, min(len(wl.cd), budget_s / per_leaf / max(steps, 1))))
+    out = None
+    t0 = time.perf_counter()
+    for s in range(steps):
+        out = ora.semilag_in_situ(vel, con, 1, wl.dt, 1, bool(wl.bc), leaf_begin=0, leaf_end=k)
+    sec = time.perf_counter() - t0
+    return {"value": k * npl * steps / sec, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d of %d concentration leaves (%d departure points) x %d step(s), "
+                      "one SL step from the initial state" % (k, len(wl.cd), k * npl, steps),
+            "seconds": sec}, out, k
+
+
+def cpu_baseline_grid(wl, budget_s=12.0):
+    from oracle import oracle as ora
+    cores = ora.num_threads()
+    probe = 20000
+    t0 = time.perf_counter()
+    ora.semilag_grid(wl.vel, wl.con, wl.n, wl.dt, 1, True, 0, probe)
+    per = (time.perf_counter() - t0) / probe
+    k = int(min(wl.n ** 3, max(probe, budget_s / per)))
+    t0 = time.perf_counter()
+    out = ora.semilag_grid(wl.vel, wl.con, wl.n, wl.dt, 1, True, 0, k)
+    sec = time.perf_counter() - t0
+    return {"value": k / sec, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "first %d of %d grid nodes, one SL step" % (k, wl.n ** 3),
+            "seconds": sec}, out, k
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, wl):
+    """--impl reference: the reference algorithm (oracle port, all host
+    threads) timed on bounded samples of the same workload, K steps."""
+    total_budget = 150.0
+    per_step = total_budget / max(1, args.steps + args.warmup)
+    if isinstance(wl, GridWorkloadType()):
+        for _ in range(args.warmup):
+            cpu_baseline_grid(wl, per_step)
+        vals, secs, pts = [], 0.0, 0
+        for _ in range(args.steps):
+            cb, _, k = cpu_baseline_grid(wl, per_step)
+            secs += cb["seconds"]
+            pts += k
+        cb["sample"] = "per step: " + cb["sample"]
+    else:
+        for _ in range(args.warmup):
+            cpu_baseline_tree(wl, per_step)
+        secs, pts = 0.0, 0
+        for _ in range(args.steps):
+            cb, _, k = cpu_baseline_tree(wl, per_step)
+            secs += cb["seconds"]
+            pts += k * (wl.q + 1) ** 3
+        cb["sample"] = "per step: " + cb["sample"]
+    value = pts / secs
+    cb["value"] = value
+    cb.pop("seconds", None)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded analytic fields)", "config": wl.describe(),
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def GridWorkloadType():
+    from tbslas_gb300.workloads import GridWorkload
+    return GridWorkload
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args, wl, rank, world, local_rank):
+    import torch
+    import tbslas_gb300 as tb
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = tb.Context(local_rank)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    is_grid = isinstance(wl, GridWorkloadType())
+
+    if is_grid:
+        N = wl.n
+        vel = torch.from_numpy(wl.vel).to(dev)
+        con0 = torch.from_numpy(wl.con).to(dev)
+        bufs = [con0.clone(), torch.empty_like(con0)]
+
+        def step(i):
+            tb.semilag_grid(ctx, vel, bufs[i % 2], N, wl.dt, 1, wl.bc, out=bufs[(i + 1) % 2])
+        flops_kernel = GRID_FLOPS_PER_POINT
+        bytes_kernel = GRID_BYTES_PER_POINT
+        dominant = "semilag_grid"
+        kernel_points = wl.points_per_step
+    else:
+        tv = tb.Tree(ctx, wl.va, wl.vd, wl.q, 3, wl.vc)
+        tc = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
+        vf = tb.NodeFieldFunctor(tv, wl.bc)
+
+        def step(i):
+            tb.solve_semilag_in_situ(vf, tc, i + 1, wl.dt, 1)
+        _, flops_kernel = flops_per_point_tree(wl.q)
+        _, bytes_kernel = bytes_per_point_tree(wl.q, len(wl.vd), len(wl.cd))
+        dominant = "semilag_tree"
+        kernel_points = wl.points_per_step
+
+    # one step from the initial state, kept for the in-run parity check
+    step(0)
+    torch.cuda.synchronize()
+    first = (bufs[1].cpu().numpy().ravel() if is_grid else tc.get_coeffs())
+    for i in range(args.warmup):
+        step(i + 1)
+    torch.cuda.synchronize()
+
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for i in range(args.steps):
+            flush.fill_(float(i))  # L2 flush: the step's working set fits in L2
+            step(args.warmup + 1 + i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+
+    # per-kernel breakdown from a separate pass with the library's event
+    # profiler on (same steps, same L2 flushes), so the timed loop carries no
+    # profiling events
+    ctx.profile(True)
+    ctx.profile_reset()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        step(args.warmup + 1 + args.steps + i)
+    torch.cuda.synchronize()
+    prof = ctx.profile_totals()
+    ctx.profile(False)
+    points = wl.points_per_step * args.steps
+    tot_points, tot_sec = aggregate(points, ms * 1e-3, world)
+    value = tot_points / tot_sec
+    gpu_launches = int(sum(v[1] for v in prof.values()))  # same step sequence as the timed loop
+
+    # end-to-end through the host-buffer C-ABI entry point: host->device copy of
+    # the step's input state and device->host copy of its result every step
+    if is_grid:
+        vel_h = torch.from_numpy(wl.vel).pin_memory().numpy()
+        con_h = torch.from_numpy(wl.con).pin_memory().numpy()
+        out_h = torch.empty(wl.con.shape, dtype=torch.float64).pin_memory().numpy()
+        h2d = vel_h.nbytes + con_h.nbytes
+        d2h = out_h.nbytes
+
+        def e2e_step(i):
+            tb.semilag_grid(ctx, vel_h, con_h, N, wl.dt, 1, wl.bc, out=out_h)
+    else:
+        coeff_h = torch.from_numpy(np.ascontiguousarray(wl.cc)).pin_memory().numpy()
+        h2d = d2h = coeff_h.nbytes
+
+        def e2e_step(i):
+            tb.solve_semilag_in_situ(vf, tc, i + 1, wl.dt, 1, coeff_host=coeff_h)
+    e2e_step(0)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        e2e_step(i + 1)
+    torch.cuda.synchronize()
+    e2e_sec = time.perf_counter() - t0
+    e_points, e_sec = aggregate(points, e2e_sec, world)
+
+    if rank != 0:
+        return
+    peaks, peak_src = measured_peaks()
+    fp64_peak = ctx.fp64_fma_peak()
+    groups, kernels, kms = prof.get(dominant, (0, 0, 0.0))
+    launch_ms = kms / max(groups, 1)
+    achieved_tflops = flops_kernel * kernel_points / (launch_ms * 1e-3) / 1e12
+    achieved_gbs = bytes_kernel * kernel_points / (launch_ms * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(wl.name, {}).get(dominant)
+    roofline = {
+        "kernel": dominant,
+        "bound": "fp64",
+        "achieved": achieved_tflops, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+        "frac": achieved_tflops / (fp64_peak / 1e12),
+        "peak_source": "FP64 FMA throughput measured in this run (tbslas_fp64_fma_peak)",
+        "algorithmic_flops_per_point": flops_kernel, "algorithmic_bytes_per_point": bytes_kernel,
+        "launch_ms": launch_ms, "traffic": traffic,
+        "hbm": {"achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved_gbs / peaks["hbm_gbs"], "peak_source": peak_src},
+        "kernels_ms_per_step": {k: v[2] / args.steps for k, v in prof.items()},
+    }
+
+    cpu = None
+    accuracy = None
+    if world == 1:
+        if is_grid:
+            cpu, ref, k = cpu_baseline_grid(wl)
+            got = first[:k]
+        else:
+            cpu, ref, k = cpu_baseline_tree(wl)
+            got = first[:k]
+        accuracy = {"rel_err_vs_oracle": float(np.abs(got - ref).max() / np.abs(ref).max()),
+                    "compared": "first GPU step vs the oracle on the CPU-baseline sample"}
+        cpu.pop("seconds", None)
+
+    cfg = wl.describe()
+    cfg.update({"l2": "flushed between timed steps (256 MiB write inside the timed loop)",
+                "parallelism": "replicas x%d" % world, "nrk": 1})
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded analytic fields)", "config": cfg,
+            "e2e": {"value": e_points / e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
+            "clocks": clk.summary(), "gpu_launches": gpu_launches}
+    print(json.dumps(line))
+    assert ctx.check() == 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="tree_adaptive_q14")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from tbslas_gb300.workloads import make
+        run_reference(args, make(args.workload))
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    from tbslas_gb300 import build
+    build.build()
+    from tbslas_gb300.workloads import make
+    wl = make(args.workload)
+    try:
+        run_gpu(args, wl, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -79,6 +79,24 @@ int tbslas_ctx_destroy(tbslas_ctx ctx);
  * Synchronises the context's device; clears the word. */
 int tbslas_ctx_check(tbslas_ctx ctx, uint32_t* device_error);
 
+/* ---- profiling --------------------------------------------------------------- */
+/* Per-kernel CUDA-event timing, accumulated per kernel name.  Replaces
+ * pvfmm::Profile::Enable / Tic / Toc / print as the reference uses them
+ * (src/applications/src/advection.cpp:77, :400; src/semilag/traj.inc:53).
+ * When enabled, every launch group is bracketed by a pair of events on its
+ * stream; reading the totals waits for those events. */
+int tbslas_profile_enable(tbslas_ctx ctx, int enable);
+int tbslas_profile_reset(tbslas_ctx ctx);
+int tbslas_profile_count(tbslas_ctx ctx, int* n);
+/* launches: bracketed launch groups; kernels: kernel launches inside them.
+ * name: valid until the next reset or destroy of ctx. */
+int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launches,
+                       int64_t* kernels, double* total_ms);
+/* Measured FP64 FMA throughput of the device (FLOP/s, 2 per FMA): the
+ * roofline denominator of the FP64-pipe-bound kernels.  Diagnostic; no
+ * reference counterpart. */
+int tbslas_fp64_fma_peak(tbslas_ctx ctx, double* flops_per_s);
+
 /* ---- Chebyshev helpers (host) ---------------------------------------------- */
 /* new_nodes(q,3): (q+1)^3 x 3 nodes in [0,1], x fastest.
  * Replaces tbslas::new_nodes, src/utils/cheb.h:41-67. */
@@ -126,6 +144,10 @@ int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_ho
 int tbslas_traj_rk2(tbslas_ctx ctx, tbslas_tree vel, const double* x_dev, int64_t n,
                     double tinit, double tfinal, int nrk, int bc, double* xdep_dev,
                     void* stream);
+
+/* Synchronous host-buffer form of tbslas_traj_rk2. */
+int tbslas_traj_rk2_host(tbslas_ctx ctx, tbslas_tree vel, const double* x_host, int64_t n,
+                         double tinit, double tfinal, int nrk, int bc, double* xdep_host);
 
 /* Node values -> coefficients of every leaf: vals_dev[L][dof][(q+1)^3].
  * Replaces SetTreeGridValues, src/tree/tree_utils.h:500-552. */

@@ -56,6 +56,11 @@ static std::vector<Real> new_nodes(int deg, int dim) {
 // Chebyshev polynomials T_0..T_q at n points, row k = T_k.  Points with
 // |x| > 1 (or NaN) get all-zero rows.  Restates pvfmm::cheb_poly as called at
 // src/tree/tree_functor.h:328-330 (three-term recurrence, 2x*T_{k-1}-T_{k-2}).
+//
+// Multiply-adds are written as explicit fused multiply-adds (std::fma)
+// wherever a contracting compiler fuses them in the reference's build (the
+// recurrence, vec_eval's accumulations, the RK2 updates), so the oracle's
+// rounding is fixed and the same on every host.
 static void cheb_poly(int q, const Real* in, int n, Real* out) {
   for (int j = 0; j < n; j++) {
     const bool ok = std::fabs(in[j]) <= 1;
@@ -67,7 +72,7 @@ static void cheb_poly(int q, const Real* in, int n, Real* out) {
     Real y1 = x;
     x *= 2;
     for (int i = 2; i <= q; i++) {
-      Real y2 = x * y1 - y0;
+      Real y2 = std::fma(x, y1, -y0);
       out[i * n + j] = y2;
       y0 = y1;
       y1 = y2;
@@ -143,7 +148,7 @@ struct Tree {
 // out[l][p] = sum_i pz_i sum_{j<d-i} py_j sum_{k<d-i-j} c[l][i][j][k] px_k.
 // Restates pvfmm::vec_eval, src/tree/tree_functor.h:27-84 (coefficients in a
 // padded d0^3 cube, points processed 16 at a time as in the 4xVecLen AVX
-// unroll, same i/j/k summation order, separate multiply and add).
+// unroll, same i/j/k summation order, fused multiply-add accumulation).
 static void vec_eval(int n, int d0, int d, int dof, const Real* px, const Real* py,
                      const Real* pz, const Real* coeff, Real* tmp_out) {
   const int B = 16;
@@ -162,11 +167,11 @@ static void vec_eval(int n, int d0, int d, int dof, const Real* px, const Real* 
           for (int k = 0; i + j + k < d; k++) {
             const Real* px_ = px + k * n + l1;
             const Real c = coeff[k + d0 * (j + d0 * (i + d0 * l0))];
-            for (int p = 0; p < B; p++) w[p] = w[p] + px_[p] * c;
+            for (int p = 0; p < B; p++) w[p] = std::fma(px_[p], c, w[p]);
           }
-          for (int p = 0; p < B; p++) v[p] = v[p] + py_[p] * w[p];
+          for (int p = 0; p < B; p++) v[p] = std::fma(py_[p], w[p], v[p]);
         }
-        for (int p = 0; p < B; p++) u[p] = u[p] + pz_[p] * v[p];
+        for (int p = 0; p < B; p++) u[p] = std::fma(pz_[p], v[p], u[p]);
       }
       for (int p = 0; p < B; p++) tmp_out[l0 * n + l1 + p] = u[p];
     }
@@ -296,10 +301,10 @@ static void integrate_rk2(Functor& fn, Real* x, size_t N, Real tau) {
   std::vector<Real> xtmp(N * 3), vtmp(N * 3);
   fn(x, N, vtmp.data());
 #pragma omp parallel for
-  for (size_t i = 0; i < N * 3; i++) xtmp[i] = x[i] + 0.5 * tau * vtmp[i];
+  for (size_t i = 0; i < N * 3; i++) xtmp[i] = std::fma(0.5 * tau, vtmp[i], x[i]);
   fn(xtmp.data(), N, vtmp.data());
 #pragma omp parallel for
-  for (size_t i = 0; i < N * 3; i++) x[i] = x[i] + tau * vtmp[i];
+  for (size_t i = 0; i < N * 3; i++) x[i] = std::fma(tau, vtmp[i], x[i]);
 }
 
 template <class Functor>
@@ -521,29 +526,38 @@ int orc_set_tree_grid_values(long L, int q, int dof, const double* M, const doub
 // Restates SolveSemilagInSitu, src/tree/tree_semilag.h:92-135, with
 // SolveSemilagRK2, src/semilag/semilag.inc:26-45.  For dof > 1 the point-major
 // values are transposed to the dof-major layout SetTreeGridValues reads.
-// coeff_out may alias con_coeff.
+// Only the target nodes of leaves [leaf_begin, leaf_end) are advected and
+// refitted when leaf_end > leaf_begin (bounded CPU samples); coeff_out then
+// holds those leaves only.  coeff_out may alias con_coeff only for a full
+// step.
 int orc_semilag_in_situ(long Lv, const double* av, const int* dv, int qv, const double* cv,
                         long Lc, const double* ac, const int* dc, int qc, int dofc,
                         const double* cc, const double* M, int timestep, double dt, int nrk,
-                        int periodic, double* coeff_out) {
+                        int periodic, long leaf_begin, long leaf_end, double* coeff_out) {
   Tree tv = make_tree(Lv, av, dv, qv, 3, cv);
   Tree tc = make_tree(Lc, ac, dc, qc, dofc, cc);
+  if (leaf_end <= leaf_begin) {
+    leaf_begin = 0;
+    leaf_end = Lc;
+  }
+  const long Ls = leaf_end - leaf_begin;
+  Tree ts = make_tree(Ls, ac + 3 * leaf_begin, dc + leaf_begin, qc, dofc, nullptr);
   const int d = qc + 1;
   const long np = (long)d * d * d;
-  const size_t N = (size_t)Lc * np;
+  const size_t N = (size_t)Ls * np;
   std::vector<Real> pts(N * 3), xdep(N * 3), vals(N * dofc);
-  collect_grid_points(tc, pts.data());
+  collect_grid_points(ts, pts.data());
   Real tinit = timestep * dt;
   Real tfinal = tinit - dt;
   TreeFunctor fv{&tv, periodic != 0};
   traj_rk2(fv, pts.data(), N, tinit, tfinal, nrk, xdep.data());
   eval_tree(tc, xdep.data(), N, vals.data(), periodic != 0);
   std::vector<Real> vdm(N * dofc);
-  for (long l = 0; l < Lc; l++)
+  for (long l = 0; l < Ls; l++)
     for (long p = 0; p < np; p++)
       for (int k = 0; k < dofc; k++)
         vdm[((size_t)l * dofc + k) * np + p] = vals[((size_t)l * np + p) * dofc + k];
-  set_tree_grid_values(Lc, dofc, np, (long)d * (d + 1) * (d + 2) / 6, M, vdm.data(), coeff_out);
+  set_tree_grid_values(Ls, dofc, np, (long)d * (d + 1) * (d + 2) / 6, M, vdm.data(), coeff_out);
   return 0;
 }
 

@@ -37,7 +37,7 @@ def lib():
     L.orc_set_tree_grid_values.argtypes = [i64, i32, i32, _f64p, _f64p, _f64p]
     L.orc_semilag_in_situ.argtypes = [i64, _f64p, _i32p, i32, _f64p,
                                       i64, _f64p, _i32p, i32, i32, _f64p,
-                                      _f64p, i32, f64, i32, i32, _f64p]
+                                      _f64p, i32, f64, i32, i32, i64, i64, _f64p]
     L.orc_fast_interp.argtypes = [_f64p, i32, i32, _f64p, i64, _f64p, i32]
     L.orc_semilag_grid.argtypes = [_f64p, _f64p, i32, f64, i32, i32, i64, i64, _f64p]
     return L
@@ -131,16 +131,22 @@ def set_tree_grid_values(L, q, dof, vals, M=None):
     return out
 
 
-def semilag_in_situ(vel, con, timestep, dt, nrk=1, periodic=False, M=None):
-    """One in-situ SL step.  vel/con: dicts with anchor, depth, q, dof, coeff."""
+def semilag_in_situ(vel, con, timestep, dt, nrk=1, periodic=False, M=None, leaf_begin=0,
+                    leaf_end=0):
+    """One in-situ SL step.  vel/con: dicts with anchor, depth, q, dof, coeff.
+
+    With leaf_end > leaf_begin only those leaves' targets are advected and
+    their new coefficients returned (a bounded sample of the step)."""
     qc = con["q"]
     M = pt2coeff(qc) if M is None else _f64(M)
     av, dv, cv = _f64(vel["anchor"]), _i32(vel["depth"]), _f64(vel["coeff"])
     ac, dc, cc = _f64(con["anchor"]), _i32(con["depth"]), _f64(con["coeff"])
-    out = np.empty((dc.size, con["dof"], n_coeff(qc)))
+    nl = dc.size if leaf_end <= leaf_begin else leaf_end - leaf_begin
+    out = np.empty((nl, con["dof"], n_coeff(qc)))
     lib().orc_semilag_in_situ(dv.size, _d(av), _i(dv), vel["q"], _d(cv),
                               dc.size, _d(ac), _i(dc), qc, con["dof"], _d(cc),
-                              _d(M), int(timestep), float(dt), int(nrk), int(periodic), _d(out))
+                              _d(M), int(timestep), float(dt), int(nrk), int(periodic),
+                              int(leaf_begin), int(leaf_end), _d(out))
     return out
 
 

@@ -89,6 +89,31 @@ class Context:
         except Exception:
             pass
 
+    def profile(self, enable=True):
+        call("tbslas_profile_enable", self.handle, int(bool(enable)))
+
+    def profile_reset(self):
+        call("tbslas_profile_reset", self.handle)
+
+    def profile_totals(self):
+        """{name: (launch groups, kernel launches, total ms)} of the profiled launches."""
+        n = ctypes.c_int(0)
+        call("tbslas_profile_count", self.handle, ctypes.byref(n))
+        out = {}
+        for i in range(n.value):
+            name, cnt, ker, ms = (ctypes.c_char_p(), ctypes.c_int64(), ctypes.c_int64(),
+                                  ctypes.c_double())
+            call("tbslas_profile_get", self.handle, i, ctypes.byref(name), ctypes.byref(cnt),
+                 ctypes.byref(ker), ctypes.byref(ms))
+            out[name.value.decode()] = (cnt.value, ker.value, ms.value)
+        return out
+
+    def fp64_fma_peak(self):
+        """Measured FP64 FMA throughput, FLOP/s."""
+        f = ctypes.c_double(0)
+        call("tbslas_fp64_fma_peak", self.handle, ctypes.byref(f))
+        return f.value
+
     def check(self):
         """Synchronise and return the device error word (raises if non-zero)."""
         w = ctypes.c_uint32(0)

@@ -30,6 +30,11 @@ SIGNATURES = {
     "tbslas_ctx_create": [_i32, _c.POINTER(_vp)],
     "tbslas_ctx_destroy": [_vp],
     "tbslas_ctx_check": [_vp, _u32p],
+    "tbslas_profile_enable": [_vp, _i32],
+    "tbslas_profile_reset": [_vp],
+    "tbslas_profile_count": [_vp, _i32p],
+    "tbslas_profile_get": [_vp, _i32, _c.POINTER(_c.c_char_p), _i64p, _i64p, _c.POINTER(_f64)],
+    "tbslas_fp64_fma_peak": [_vp, _c.POINTER(_f64)],
     "tbslas_cheb_nodes": [_i32, _vp],
     "tbslas_pt2coeff_matrix": [_i32, _vp],
     "tbslas_tree_create": [_vp, _i64, _vp, _vp, _i32, _i32, _c.POINTER(_vp)],
@@ -43,6 +48,7 @@ SIGNATURES = {
     "tbslas_eval_tree": [_vp, _vp, _vp, _i64, _vp, _i32, _vp],
     "tbslas_eval_tree_host": [_vp, _vp, _vp, _i64, _vp, _i32],
     "tbslas_traj_rk2": [_vp, _vp, _vp, _i64, _f64, _f64, _i32, _i32, _vp, _vp],
+    "tbslas_traj_rk2_host": [_vp, _vp, _vp, _i64, _f64, _f64, _i32, _i32, _vp],
     "tbslas_set_tree_grid_values": [_vp, _vp, _vp, _vp],
     "tbslas_semilag_in_situ": [_vp, _vp, _vp, _i32, _f64, _i32, _i32, _vp],
     "tbslas_semilag_in_situ_host": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _i32],

@@ -98,6 +98,20 @@ inline bool bc_ok(int bc) { return bc == TBSLAS_BC_FREESPACE || bc == TBSLAS_BC_
 
 }  // namespace
 
+// Per-kernel CUDA-event timing (the role of pvfmm::Profile::Tic/Toc in the
+// reference, e.g. src/semilag/traj.inc:53, src/tree/tree_functor.h:389-394).
+struct ProfRecord {
+  const char* name;
+  int kernels;
+  cudaEvent_t start, stop;
+};
+struct ProfTotal {
+  std::string name;
+  int64_t launches = 0;
+  int64_t kernels = 0;
+  double ms = 0.0;
+};
+
 struct tbslas_ctx_s {
   int device = 0;
   int num_sms = 0;
@@ -105,6 +119,10 @@ struct tbslas_ctx_s {
   uint32_t* d_err = nullptr;
   DevBuf slots[kNumSlots];
   double* d_M[TBSLAS_MAX_DEGREE + 1] = {};
+  bool profile = false;
+  std::vector<ProfRecord> prof_pending;
+  std::vector<cudaEvent_t> prof_pool;
+  std::vector<ProfTotal> prof_totals;
 };
 
 struct tbslas_tree_s {
@@ -133,6 +151,63 @@ struct tbslas_tree_s {
 };
 
 namespace {
+
+cudaEvent_t prof_event(tbslas_ctx ctx) {
+  if (!ctx->prof_pool.empty()) {
+    cudaEvent_t e = ctx->prof_pool.back();
+    ctx->prof_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Brackets the launches of one named kernel on a stream with events when
+// profiling is on; a no-op otherwise.
+struct ProfScope {
+  tbslas_ctx ctx;
+  const char* name;
+  cudaStream_t s;
+  int kernels;
+  cudaEvent_t start = nullptr;
+  ProfScope(tbslas_ctx c, const char* n, cudaStream_t st, int nkernels = 1)
+      : ctx(c), name(n), s(st), kernels(nkernels) {
+    if (ctx->profile) {
+      start = prof_event(ctx);
+      cudaEventRecord(start, s);
+    }
+  }
+  ~ProfScope() {
+    if (start) {
+      cudaEvent_t stop = prof_event(ctx);
+      cudaEventRecord(stop, s);
+      ctx->prof_pending.push_back(ProfRecord{name, kernels, start, stop});
+    }
+  }
+};
+
+// Folds finished event pairs into the per-name totals.
+void prof_collect(tbslas_ctx ctx) {
+  for (ProfRecord& r : ctx->prof_pending) {
+    cudaEventSynchronize(r.stop);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.start, r.stop);
+    ProfTotal* t = nullptr;
+    for (ProfTotal& x : ctx->prof_totals)
+      if (x.name == r.name) t = &x;
+    if (!t) {
+      ctx->prof_totals.push_back(ProfTotal{r.name});
+      t = &ctx->prof_totals.back();
+    }
+    t->launches += 1;
+    t->kernels += r.kernels;
+    t->ms += ms;
+    ctx->prof_pool.push_back(r.start);
+    ctx->prof_pool.push_back(r.stop);
+  }
+  ctx->prof_pending.clear();
+}
 
 int bind(tbslas_ctx ctx) {
   if (!ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null context");
@@ -325,6 +400,27 @@ __global__ void k_point_to_dof_major(const double* __restrict__ in, int64_t L, i
   out[(leaf * dof + l) * np + p] = in[i];
 }
 
+// FP64 FMA throughput probe: 8 independent dependency chains per thread,
+// 64 FMAs per iteration; one store per thread.
+__global__ void __launch_bounds__(256) k_fp64_fma(double* out, double b, double c, int iters) {
+  double a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5,
+         a6 = a0 + 6, a7 = a0 + 7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      a0 = fma(a0, b, c);
+      a1 = fma(a1, b, c);
+      a2 = fma(a2, b, c);
+      a3 = fma(a3, b, c);
+      a4 = fma(a4, b, c);
+      a5 = fma(a5, b, c);
+      a6 = fma(a6, b, c);
+      a7 = fma(a7, b, c);
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 // The bucketed tree functor on device buffers.
@@ -348,13 +444,16 @@ int eval_tree_dev(tbslas_ctx ctx, tbslas_tree tree, const double* pos, int64_t n
   TRY(scratch_t(ctx, kTiles, max_tiles, &tiles));
   CUDA_TRY(cudaMemsetAsync(count, 0, L * sizeof(*count), s));
   CUDA_TRY(cudaMemsetAsync(cursor, 0, L * sizeof(*cursor), s));
-  k_classify<<<blocks_for(n, 256), 256, 0, s>>>(tv, pos, n, bc, leaf_of, count, out);
-  k_ntiles<<<blocks_for(L, 256), 256, 0, s>>>(count, L, ntile);
-  k_scan_excl<<<1, 1024, 0, s>>>(reinterpret_cast<const int64_t*>(count), start, L);
-  k_scan_excl<<<1, 1024, 0, s>>>(ntile, tileoff, L);
-  k_scatter<<<blocks_for(n, 256), 256, 0, s>>>(leaf_of, n, start, cursor, perm);
-  k_make_tiles<<<blocks_for(L, 256), 256, 0, s>>>(start, tileoff, L, tiles);
-  TRY(check_launch("bucketing"));
+  {
+    ProfScope p(ctx, "bucket_points", s, 6);
+    k_classify<<<blocks_for(n, 256), 256, 0, s>>>(tv, pos, n, bc, leaf_of, count, out);
+    k_ntiles<<<blocks_for(L, 256), 256, 0, s>>>(count, L, ntile);
+    k_scan_excl<<<1, 1024, 0, s>>>(reinterpret_cast<const int64_t*>(count), start, L);
+    k_scan_excl<<<1, 1024, 0, s>>>(ntile, tileoff, L);
+    k_scatter<<<blocks_for(n, 256), 256, 0, s>>>(leaf_of, n, start, cursor, perm);
+    k_make_tiles<<<blocks_for(L, 256), 256, 0, s>>>(start, tileoff, L, tiles);
+    TRY(check_launch("bucketing"));
+  }
   EvalTilesArgs a;
   a.tree = tv;
   a.pos = pos;
@@ -365,6 +464,7 @@ int eval_tree_dev(tbslas_ctx ctx, tbslas_tree tree, const double* pos, int64_t n
   a.out = out;
   a.err = ctx->d_err;
   a.grid = (int)std::min<int64_t>(max_tiles, (int64_t)ctx->num_sms * 8);
+  ProfScope p(ctx, "eval_tiles", s);
   g_kernels[tree->q].eval_tiles(a, s);
   return check_launch("eval_tiles");
 }
@@ -380,6 +480,7 @@ int traj_dev(tbslas_ctx ctx, tbslas_tree vel, const double* x, int64_t n, double
   a.nrk = nrk;
   a.periodic = bc;
   a.xdep = xdep;
+  ProfScope p(ctx, "traj_rk2", s);
   g_kernels[vel->q].traj(a, s);
   return check_launch("traj");
 }
@@ -387,6 +488,7 @@ int traj_dev(tbslas_ctx ctx, tbslas_tree vel, const double* x, int64_t n, double
 int refit_dev(tbslas_ctx ctx, tbslas_tree tree, const double* vals, cudaStream_t s) {
   const double* M = nullptr;
   TRY(device_M(ctx, tree->q, &M));
+  ProfScope p(ctx, "refit", s);
   launch_refit(vals, M, tree->L * tree->dof, (int)n_points(tree->q), (int)n_coeff(tree->q),
                tree->dof, tree->stride, tree->d_coeff, s);
   return check_launch("refit");
@@ -395,6 +497,7 @@ int refit_dev(tbslas_ctx ctx, tbslas_tree tree, const double* vals, cudaStream_t
 int collect_dev(tbslas_tree tree, double* out, cudaStream_t s) {
   const int64_t n = tree->L * n_points(tree->q);
   if (n == 0) return TBSLAS_OK;
+  ProfScope p(tree->ctx, "collect", s);
   k_collect<<<blocks_for(n, 256), 256, 0, s>>>(tree->view(), nodes_1d(tree->q), tree->q + 1, out);
   return check_launch("collect");
 }
@@ -428,6 +531,7 @@ int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int ti
     a.nrk = nrk;
     a.periodic = bc;
     a.vals = vals;
+    ProfScope p(ctx, "semilag_tree", s);
     g_kernels[con->q].semilag(a, s);
     TRY(check_launch("semilag_tree"));
   } else {
@@ -438,6 +542,7 @@ int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int ti
     TRY(collect_dev(con, X, s));
     TRY(traj_dev(ctx, vel, X, N, tau, nrk, bc, Xdep, s));
     TRY(eval_tree_dev(ctx, con, Xdep, N, vt, bc, s));
+    ProfScope p(ctx, "to_dof_major", s);
     k_point_to_dof_major<<<blocks_for(N * con->dof, 256), 256, 0, s>>>(vt, con->L, (int)np,
                                                                       con->dof, vals);
     TRY(check_launch("transpose"));
@@ -572,6 +677,8 @@ int tbslas_ctx_destroy(tbslas_ctx ctx) {
     if (b.p) cudaFree(b.p);
   for (auto p : ctx->d_M)
     if (p) cudaFree(p);
+  prof_collect(ctx);
+  for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -586,6 +693,64 @@ int tbslas_ctx_check(tbslas_ctx ctx, uint32_t* device_error) {
   CUDA_TRY(cudaMemset(ctx->d_err, 0, sizeof(uint32_t)));
   if (device_error) *device_error = e;
   if (e) return fail(TBSLAS_ERR_DEVICE, "device error word 0x%x", e);
+  return TBSLAS_OK;
+}
+
+int tbslas_profile_enable(tbslas_ctx ctx, int enable) {
+  TRY(bind(ctx));
+  ctx->profile = enable != 0;
+  return TBSLAS_OK;
+}
+
+int tbslas_profile_reset(tbslas_ctx ctx) {
+  TRY(bind(ctx));
+  prof_collect(ctx);
+  ctx->prof_totals.clear();
+  return TBSLAS_OK;
+}
+
+int tbslas_profile_count(tbslas_ctx ctx, int* n) {
+  TRY(bind(ctx));
+  if (!n) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
+  prof_collect(ctx);
+  *n = (int)ctx->prof_totals.size();
+  return TBSLAS_OK;
+}
+
+int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launches,
+                       int64_t* kernels, double* total_ms) {
+  TRY(bind(ctx));
+  prof_collect(ctx);
+  if (i < 0 || i >= (int)ctx->prof_totals.size())
+    return fail(TBSLAS_ERR_INVALID_ARG, "profile index %d", i);
+  const ProfTotal& t = ctx->prof_totals[i];
+  if (name) *name = t.name.c_str();
+  if (launches) *launches = t.launches;
+  if (kernels) *kernels = t.kernels;
+  if (total_ms) *total_ms = t.ms;
+  return TBSLAS_OK;
+}
+
+int tbslas_fp64_fma_peak(tbslas_ctx ctx, double* flops_per_s) {
+  TRY(bind(ctx));
+  if (!flops_per_s) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
+  const int blocks = ctx->num_sms * 8, threads = 256, iters = 2000;
+  double* out;
+  TRY(scratch_t(ctx, kHostOut, (size_t)blocks * threads, &out));
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  k_fp64_fma<<<blocks, threads, 0, ctx->stream>>>(out, 1.0, 0.0, 10);
+  cudaEventRecord(e0, ctx->stream);
+  k_fp64_fma<<<blocks, threads, 0, ctx->stream>>>(out, 1.0, 0.0, iters);
+  cudaEventRecord(e1, ctx->stream);
+  CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  TRY(check_launch("fp64_fma"));
+  *flops_per_s = 2.0 * 64.0 * iters * (double)blocks * threads / (ms * 1e-3);
   return TBSLAS_OK;
 }
 
@@ -740,6 +905,26 @@ int tbslas_traj_rk2(tbslas_ctx ctx, tbslas_tree vel, const double* x_dev, int64_
   return traj_dev(ctx, vel, x_dev, n, tau, nrk, bc, xdep_dev, (cudaStream_t)stream);
 }
 
+int tbslas_traj_rk2_host(tbslas_ctx ctx, tbslas_tree vel, const double* x_host, int64_t n,
+                         double tinit, double tfinal, int nrk, int bc, double* xdep_host) {
+  TRY(check_tree(vel));
+  TRY(bind(ctx));
+  if (vel->dof != 3) return fail(TBSLAS_ERR_INVALID_ARG, "velocity tree has dof %d, not 3", vel->dof);
+  if (n < 0 || nrk < 1) return fail(TBSLAS_ERR_INVALID_ARG, "n=%lld nrk=%d", (long long)n, nrk);
+  if (n == 0) return TBSLAS_OK;
+  if (!x_host || !xdep_host) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  double *x, *xd;
+  TRY(scratch_t(ctx, kHostIn, n * 3, &x));
+  TRY(scratch_t(ctx, kHostOut, n * 3, &xd));
+  cudaStream_t s = ctx->stream;
+  CUDA_TRY(cudaMemcpyAsync(x, x_host, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
+  TRY(traj_dev(ctx, vel, x, n, (tfinal - tinit) / nrk, nrk, bc, xd, s));
+  CUDA_TRY(cudaMemcpyAsync(xdep_host, xd, n * 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return TBSLAS_OK;
+}
+
 int tbslas_set_tree_grid_values(tbslas_ctx ctx, tbslas_tree tree, const double* vals_dev,
                                 void* stream) {
   TRY(check_tree(tree));
@@ -791,6 +976,7 @@ int tbslas_fast_interp(tbslas_ctx ctx, const double* grid_dev, int dof, int n_re
   if (n > 0 && (!grid_dev || !pts_dev || !out_dev))
     return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
   if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  ProfScope p(ctx, "fast_interp", (cudaStream_t)stream);
   launch_fast_interp(grid_dev, dof, n_reg, pts_dev, n, out_dev, bc, (cudaStream_t)stream);
   return check_launch("fast_interp");
 }
@@ -814,6 +1000,7 @@ int tbslas_semilag_grid(tbslas_ctx ctx, const double* vel_dev, const double* con
                         void* stream) {
   TRY(check_grid_args(ctx, vel_dev, con_dev, con_out_dev, n_reg, dt, nrk, bc));
   const double tau = (-dt - 0.0) / nrk;
+  ProfScope p(ctx, "semilag_grid", (cudaStream_t)stream);
   launch_semilag_grid(vel_dev, con_dev, con_out_dev, n_reg, tau, nrk, bc, (cudaStream_t)stream);
   return check_launch("semilag_grid");
 }
@@ -830,8 +1017,11 @@ int tbslas_semilag_grid_host(tbslas_ctx ctx, const double* vel_host, const doubl
   CUDA_TRY(cudaMemcpyAsync(vel, vel_host, n3 * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemcpyAsync(con, con_host, n3 * sizeof(double), cudaMemcpyHostToDevice, s));
   const double tau = (-dt - 0.0) / nrk;
-  launch_semilag_grid(vel, con, cout, n_reg, tau, nrk, bc, s);
-  TRY(check_launch("semilag_grid"));
+  {
+    ProfScope p(ctx, "semilag_grid", s);
+    launch_semilag_grid(vel, con, cout, n_reg, tau, nrk, bc, s);
+    TRY(check_launch("semilag_grid"));
+  }
   CUDA_TRY(cudaMemcpyAsync(con_out_host, cout, n3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   return TBSLAS_OK;

@@ -104,7 +104,7 @@ __device__ __forceinline__ void cheb_T(double xi, double (&T)[D]) {
   if (D > 1) T[1] = x;
   const double x2 = 2.0 * x;
 #pragma unroll
-  for (int k = 2; k < D; ++k) T[k] = x2 * T[k - 1] - T[k - 2];
+  for (int k = 2; k < D; ++k) T[k] = fma(x2, T[k - 1], -T[k - 2]);
 }
 
 // Triangular tensor Chebyshev sum of one dof:

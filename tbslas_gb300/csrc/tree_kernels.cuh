@@ -62,7 +62,9 @@ constexpr uint32_t kWaitLimit = 1u << 22;
 // (IntegrateRK2 / ComputeTrajRK2, src/semilag/traj.inc:20-68).  The first
 // evaluation of each sub-step wraps X in place under periodic boundaries and
 // the update uses the wrapped X, as the reference's aliasing of xinit and
-// xsol does.  One evaluation site serves both stages (smaller code).
+// xsol does.  One evaluation site serves both stages (smaller code).  The
+// updates are fused multiply-adds, matching the oracle operation for
+// operation, so departure points are bit-identical to it.
 template <int D>
 __device__ __forceinline__ void rk2_backtrace(const TreeView& vel, double& x, double& y,
                                               double& z, double tau, int nrk, bool per) {
@@ -76,13 +78,13 @@ __device__ __forceinline__ void rk2_backtrace(const TreeView& vel, double& x, do
       x = px;
       y = py;
       z = pz;
-      px = x + half_tau * v[0];
-      py = y + half_tau * v[1];
-      pz = z + half_tau * v[2];
+      px = fma(half_tau, v[0], x);
+      py = fma(half_tau, v[1], y);
+      pz = fma(half_tau, v[2], z);
     } else {
-      x = x + tau * v[0];
-      y = y + tau * v[1];
-      z = z + tau * v[2];
+      x = fma(tau, v[0], x);
+      y = fma(tau, v[1], y);
+      z = fma(tau, v[2], z);
       px = x;
       py = y;
       pz = z;

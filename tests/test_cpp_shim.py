@@ -1,0 +1,54 @@
+"""The C++ drop-in layer (include/tbslas_gb300.hpp): it compiles against the
+header and links against the library on any host; on the GPU a driver-shaped
+program (tests/cpp/shim_demo.cpp) reproduces the oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from tbslas_gb300 import fields, trees
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _compile(built, tmp_path):
+    exe = str(tmp_path / "shim_demo")
+    pkg = os.path.join(ROOT, "tbslas_gb300")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+                           os.path.join(HERE, "cpp", "shim_demo.cpp"), "-L" + pkg,
+                           "-ltbslas_gb300", "-Wl,-rpath," + pkg, "-o", exe])
+    return exe
+
+
+def test_shim_compiles_and_links(built, tmp_path):
+    assert os.path.exists(_compile(built, tmp_path))
+
+
+@pytest.mark.gpu
+def test_shim_program_matches_oracle(built, ora, tmp_path):
+    q, dt, steps = 6, 0.02, 2
+    anchor, depth = trees.uniform_tree(2)
+    vc = trees.fit(fields.taylor_green(), anchor, depth, q, 3)
+    cc = trees.fit(fields.gaussian((0.4, 0.55, 0.5), 0.1), anchor, depth, q, 1)
+    rng = np.random.default_rng(0)
+    pts = rng.uniform(0, 1, size=(777, 3))
+    inp = tmp_path / "in.bin"
+    hdr = np.array([len(depth), q, len(pts), dt, 0, steps], dtype=np.float64)
+    with open(inp, "wb") as f:
+        for a in (hdr, anchor, depth.astype(np.float64), vc, cc, pts):
+            f.write(np.ascontiguousarray(a, dtype=np.float64).tobytes())
+    out = tmp_path / "out.bin"
+    subprocess.check_call([_compile(built, tmp_path), str(inp), str(out)])
+    res = np.fromfile(out, dtype=np.float64)
+    n = len(pts)
+    v, xdep, coeff = res[:3 * n], res[3 * n:6 * n], res[6 * n:]
+    assert np.array_equal(v, ora.eval_tree(anchor, depth, q, 3, vc, pts).ravel())
+    assert np.array_equal(xdep, ora.traj_rk2(anchor, depth, q, vc, pts, 0.0, -dt, 1).ravel())
+    con = dict(anchor=anchor, depth=depth, q=q, dof=1, coeff=cc)
+    vel = dict(anchor=anchor, depth=depth, q=q, dof=3, coeff=vc)
+    for s in range(1, steps + 1):
+        con["coeff"] = ora.semilag_in_situ(vel, con, s, dt)
+    ref = con["coeff"].ravel()
+    assert np.abs(coeff - ref).max() <= 1e-12 * np.abs(ref).max()
