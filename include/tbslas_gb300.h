@@ -138,6 +138,34 @@ int tbslas_eval_tree(tbslas_ctx ctx, tbslas_tree tree, const double* pos_dev, in
 int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_host, int64_t n,
                           double* out_host, int bc);
 
+/* Allocation-free form of tbslas_eval_tree, for callers that cannot allocate
+ * device memory while they evaluate: a solver loop running under a memory
+ * budget fixed up front, a host application whose own pool owns every device
+ * allocation (library-side cudaMalloc/cudaFree would synchronise the device
+ * and fragment that pool), or code that records its work into a stream
+ * capture, where a cudaMalloc breaks the capture.  No counterpart in the
+ * reference (it allocates freely: static grow-on-demand buffers in
+ * EvalTree).  Same inputs, outputs and results as tbslas_eval_tree; the call
+ * itself makes no cudaMalloc, cudaFree or allocating library call.
+ *  - Scratch lives in one static device array of TBSLAS_NOALLOC_SCRATCH_BYTES
+ *    (about 5 MiB) that every GPU which loads this library holds until the
+ *    process exits.
+ *  - Limits: n <= TBSLAS_NOALLOC_MAX_POINTS points per call and trees of at
+ *    most TBSLAS_NOALLOC_MAX_LEAVES leaves; larger requests return
+ *    TBSLAS_ERR_SIZE (split the points over several calls).
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - Every call on a device shares the one array: calls whose work overlaps
+ *    on the GPU (other streams, other host threads) race and corrupt each
+ *    other.  Serialise them (one stream, or events).  The parts that must
+ *    start at zero are cleared by each call. */
+#define TBSLAS_NOALLOC_MAX_POINTS (1 << 18)
+#define TBSLAS_NOALLOC_MAX_LEAVES (1 << 15)
+#define TBSLAS_NOALLOC_SCRATCH_BYTES (5u << 20)
+int tbslas_eval_tree_noalloc(tbslas_tree tree, const double* pos_dev, int64_t n, double* out_dev,
+                             int bc, void* stream);
+
 /* RK2 backtrace of n points through a dof-3 velocity tree from tinit to tfinal
  * in nrk sub-steps: xdep_dev[n*3].  Replaces ComputeTrajRK2 with a
  * NodeFieldFunctor velocity, src/semilag/traj.inc:20-68. */

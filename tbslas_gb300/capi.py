@@ -15,6 +15,8 @@ BC_FREESPACE = 0
 BC_PERIODIC = 1
 MAX_DEGREE = 16
 MAX_DEPTH = 21
+NOALLOC_MAX_POINTS = 1 << 18
+NOALLOC_MAX_LEAVES = 1 << 15
 
 _c = ctypes
 _vp, _i64, _i32, _f64 = _c.c_void_p, _c.c_int64, _c.c_int, _c.c_double
@@ -47,6 +49,7 @@ SIGNATURES = {
     "tbslas_collect_grid_points": [_vp, _vp, _vp, _vp],
     "tbslas_eval_tree": [_vp, _vp, _vp, _i64, _vp, _i32, _vp],
     "tbslas_eval_tree_host": [_vp, _vp, _vp, _i64, _vp, _i32],
+    "tbslas_eval_tree_noalloc": [_vp, _vp, _i64, _vp, _i32, _vp],
     "tbslas_traj_rk2": [_vp, _vp, _vp, _i64, _f64, _f64, _i32, _i32, _vp, _vp],
     "tbslas_traj_rk2_host": [_vp, _vp, _vp, _i64, _f64, _f64, _i32, _i32, _vp],
     "tbslas_set_tree_grid_values": [_vp, _vp, _vp, _vp],

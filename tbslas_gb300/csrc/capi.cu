@@ -625,6 +625,53 @@ int copy_coeffs(tbslas_tree t, double* dst, const double* src, bool to_tree, cud
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Used only by the allocation-free entry point (noalloc.cu): the bucketed
+// functor evaluation on scratch the caller has carved out.  Same kernels and
+// launch sequence as eval_tree_dev.
+namespace tbg {
+
+int tree_shape(tbslas_tree t, int64_t* L, int* device, int* dof) {
+  if (!t || !t->ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null tree");
+  *L = t->L;
+  *device = t->ctx->device;
+  *dof = t->dof;
+  return TBSLAS_OK;
+}
+
+int bucketed_eval_on(const BucketScratch& b, tbslas_tree tree, const double* pos, int64_t n,
+                     double* out, int bc, cudaStream_t s) {
+  if (n == 0) return TBSLAS_OK;
+  const TreeView tv = tree->view();
+  const int64_t L = tree->L;
+  const int64_t max_tiles = (n + kTile - 1) / kTile + L;
+  CUDA_TRY(cudaMemsetAsync(b.count, 0, L * sizeof(*b.count), s));
+  CUDA_TRY(cudaMemsetAsync(b.cursor, 0, L * sizeof(*b.cursor), s));
+  k_classify<<<blocks_for(n, 256), 256, 0, s>>>(tv, pos, n, bc, b.leaf_of, b.count, out);
+  k_ntiles<<<blocks_for(L, 256), 256, 0, s>>>(b.count, L, b.ntile);
+  k_scan_excl<<<1, 1024, 0, s>>>(reinterpret_cast<const int64_t*>(b.count), b.start, L);
+  k_scan_excl<<<1, 1024, 0, s>>>(b.ntile, b.tileoff, L);
+  k_scatter<<<blocks_for(n, 256), 256, 0, s>>>(b.leaf_of, n, b.start, b.cursor, b.perm);
+  k_make_tiles<<<blocks_for(L, 256), 256, 0, s>>>(b.start, b.tileoff, L, b.tiles);
+  TRY(check_launch("bucketing"));
+  EvalTilesArgs a;
+  a.tree = tv;
+  a.pos = pos;
+  a.perm = b.perm;
+  a.tiles = b.tiles;
+  a.ntiles = b.tileoff + L;
+  a.periodic = bc;
+  a.out = out;
+  a.err = tree->ctx->d_err;
+  a.grid = (int)std::min<int64_t>(max_tiles, (int64_t)tree->ctx->num_sms * 8);
+  g_kernels[tree->q].eval_tiles(a, s);
+  return check_launch("eval_tiles");
+}
+
+int fail_status(int code, const char* msg) { return fail(code, "%s", msg); }
+
+}  // namespace tbg
+
 // ===========================================================================
 extern "C" {
 

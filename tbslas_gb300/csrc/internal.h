@@ -49,6 +49,18 @@ struct EvalTilesArgs {
   int grid;
 };
 
+// Scratch of one bucketed tree evaluation, carved by the caller.
+struct BucketScratch {
+  int32_t* leaf_of;             // [n]
+  unsigned long long* count;    // [L], zeroed by the launcher
+  unsigned long long* cursor;   // [L], zeroed by the launcher
+  int64_t* start;               // [L + 1]
+  int64_t* ntile;               // [L]
+  int64_t* tileoff;             // [L + 1]
+  int64_t* perm;                // [n]
+  Tile* tiles;                  // [n / kTile + 1 + L]
+};
+
 typedef void (*SemilagTreeFn)(const SemilagTreeArgs&, cudaStream_t);
 typedef void (*TrajFn)(const TrajArgs&, cudaStream_t);
 typedef void (*EvalTilesFn)(const EvalTilesArgs&, cudaStream_t);
@@ -69,6 +81,12 @@ void register_degrees_e(DegreeKernels* table);
 void register_degrees_f(DegreeKernels* table);
 void register_degrees_g(DegreeKernels* table);
 void register_degrees_h(DegreeKernels* table);
+
+// capi.cu, for the allocation-free entry point (noalloc.cu)
+int tree_shape(tbslas_tree t, int64_t* L, int* device, int* dof);
+int bucketed_eval_on(const BucketScratch& b, tbslas_tree tree, const double* pos,
+                     int64_t n, double* out, int bc, cudaStream_t s);
+int fail_status(int code, const char* msg);
 
 // refit.cu: coeff[(r/dof)*stride + (r%dof)*nc + n] = sum_p vals[r*np+p] M[p*nc+n]
 void launch_refit(const double* vals, const double* M, int64_t rows, int np, int nc, int dof,
