@@ -396,6 +396,105 @@ def run_gpu(args, wl, rank, world, local_rank):
     assert ctx.check() == 0
 
 
+def run_batched(args, wl, rank, world, local_rank):
+    """Config 4: the batched, graph-captured step vs the plain per-problem
+    loop of in-situ steps on the same problems, from the same state."""
+    import torch
+    import tbslas_gb300 as tb
+
+    torch.cuda.set_device(local_rank)
+    ctx = tb.Context(local_rank)
+    stream = torch.cuda.current_stream()
+    probs = [(tb.Tree(ctx, p["va"], p["vd"], p["q"], 3, p["vc"]),
+              tb.Tree(ctx, p["ca"], p["cd"], p["q"], 1, p["cc"]), p["dt"]) for p in wl.problems]
+    funcs = [tb.NodeFieldFunctor(tv, wl.bc) for tv, _, _ in probs]
+
+    def reset():
+        for (tv, tc, _), p in zip(probs, wl.problems):
+            tc.set_coeffs(p["cc"])
+
+    def plain(ts0, k):
+        for i in range(k):
+            for f, (tv, tc, dt) in zip(funcs, probs):
+                tb.solve_semilag_in_situ(f, tc, ts0 + i, dt)
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # plain per-problem loop
+    reset()
+    plain(1, args.warmup)
+    reset()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    plain(1, args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    plain_state = [tc.get_coeffs() for _, tc, _ in probs]
+
+    batch = tb.Batch(ctx, probs, 1, wl.bc)
+    reset()
+    tune = batch.autotune()
+    reset()
+    batch.run(1, args.steps, True)          # capture + warm replay
+    reset()
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        batch.run(1, args.steps, True)      # the captured K-step graph
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    same = all(np.array_equal(tc.get_coeffs(), ref) for (_, tc, _), ref in zip(probs, plain_state))
+
+    # e2e: host coefficients in, one graph step, host coefficients out, per step
+    pinned = [torch.from_numpy(np.ascontiguousarray(p["cc"])).pin_memory().numpy()
+              for p in wl.problems]
+    h2d = sum(a.nbytes for a in pinned)
+    batch.run(1, 1, True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        for (_, tc, _), a in zip(probs, pinned):
+            tc.set_coeffs(a)
+        batch.run(1 + i, 1, True)
+        for (_, tc, _), a in zip(probs, pinned):
+            tc.get_coeffs(a)
+    torch.cuda.synchronize()
+    e2e_sec = time.perf_counter() - t0
+
+    points = wl.points_per_step * args.steps
+    tot_points, tot_sec = aggregate(points, ms * 1e-3, world)
+    e_points, e_sec = aggregate(points, e2e_sec, world)
+    if rank != 0:
+        return
+    cfg = wl.describe()
+    cfg.update({"l2": "inputs larger than L2 (all problems' trees)",
+                "parallelism": "replicas x%d" % world, "nrk": 1,
+                "autotuned": {"block": tune[0], "targets_per_item": tune[1], "ctas_per_sm": tune[2]},
+                "graph": "the K-step run is one captured CUDA graph"})
+    line = {"metric": METRIC, "value": tot_points / tot_sec, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded analytic fields)", "config": cfg,
+            "batched_vs_plain": plain_ms / ms,
+            "plain_loop": {"value": points / (plain_ms * 1e-3), "ms_per_step": plain_ms / args.steps,
+                           "launches_per_step": 2 * len(probs)},
+            "accuracy": {"batched_equals_plain_bitwise": bool(same)},
+            "e2e": {"value": e_points / e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(h2d)},
+            "clocks": clk.summary(),
+            "gpu_launches": int(args.steps * (1 + sum(
+                1 for band in range(3) if any(_band(p["q"]) == band for p in wl.problems))))}
+    print(json.dumps(line))
+    assert ctx.check() == 0
+
+
+def _band(q):
+    return 0 if q <= 8 else (1 if q <= 12 else 2)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -423,7 +522,10 @@ def main():
     from tbslas_gb300.workloads import make
     wl = make(args.workload)
     try:
-        run_gpu(args, wl, rank, world, local_rank)
+        if args.workload.startswith("batched"):
+            run_batched(args, wl, rank, world, local_rank)
+        else:
+            run_gpu(args, wl, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as dist

@@ -18,7 +18,8 @@
  *  - Pointers named *_dev are device pointers owned by the caller; *_host are
  *    host pointers.  `stream` is a cudaStream_t (NULL = legacy default stream).
  *    Device entry points are asynchronous on `stream`; *_host entry points are
- *    synchronous.
+ *    synchronous: they first wait for all work queued on the device, then copy,
+ *    compute and copy back on the context's own stream.
  *  - All arithmetic is IEEE FP64.
  *  - Boundary condition `bc`: TBSLAS_BC_FREESPACE or TBSLAS_BC_PERIODIC, the
  *    reference's pvfmm::FreeSpace / pvfmm::Periodic (sim_config->bc).
@@ -63,6 +64,7 @@ enum { TBSLAS_BC_FREESPACE = 0, TBSLAS_BC_PERIODIC = 1 };
 
 typedef struct tbslas_ctx_s* tbslas_ctx;
 typedef struct tbslas_tree_s* tbslas_tree;
+typedef struct tbslas_batch_s* tbslas_batch;
 
 /* ---- errors / version ---------------------------------------------------- */
 const char* tbslas_status_string(int status);
@@ -195,6 +197,36 @@ int tbslas_semilag_in_situ(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int
 int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
                                 double* con_coeff_host, int timestep, double dt, int nrk,
                                 int bc);
+
+/* ---- batched in-situ SL --------------------------------------------------------- */
+/* Many independent in-situ SL problems advanced together: problem i is
+ * (vel[i] (dof 3), con[i] (dof 1, same degree), dt[i]); all share nrk and bc.
+ * Each step is one persistent kernel over a flattened worklist of target
+ * chunks of every problem plus one batched refit kernel; results equal a
+ * loop of tbslas_semilag_in_situ calls over the problems, bit for bit.  No
+ * single-call counterpart in the reference (a driver loops over
+ * SolveSemilagInSitu, src/tree/tree_semilag.h:92-135).  The batch keeps
+ * pointers to the trees: they must outlive it and keep their shapes. */
+int tbslas_batch_create(tbslas_ctx ctx, int n_problems, const tbslas_tree* vel,
+                        const tbslas_tree* con, const double* dt, int nrk, int bc,
+                        tbslas_batch* out);
+int tbslas_batch_destroy(tbslas_batch batch);
+int tbslas_batch_info(tbslas_batch batch, int64_t* total_targets, int64_t* work_items);
+/* Launch parameters: threads per CTA (64/128/256), targets per work chunk,
+ * CTAs per SM of the persistent grid. */
+int tbslas_batch_set_params(tbslas_batch batch, int block, int targets_per_item,
+                            int ctas_per_sm);
+int tbslas_batch_get_params(tbslas_batch batch, int* block, int* targets_per_item,
+                            int* ctas_per_sm);
+/* Times candidate parameter sets on this batch (one step each; the
+ * concentration coefficients are saved and restored) and keeps the fastest. */
+int tbslas_batch_autotune(tbslas_batch batch, int* block, int* targets_per_item,
+                          int* ctas_per_sm);
+/* Advance every problem by nsteps steps, timesteps timestep0 .. timestep0 +
+ * nsteps - 1.  use_graph != 0: the nsteps-step sequence is captured once as a
+ * CUDA graph (re-captured when nsteps or the parameters change) and replayed
+ * on `stream`. */
+int tbslas_batch_run(tbslas_batch batch, int timestep0, int nsteps, int use_graph, void* stream);
 
 /* ---- tricubic regular grid --------------------------------------------------- */
 /* out_dev[n*dof] = tricubic Lagrange interpolant of grid_dev (SoA,

@@ -251,6 +251,59 @@ def solve_semilag_in_situ(vel_functor, tree, timestep, dt, num_rk_step=1, stream
     return None
 
 
+class Batch:
+    """Many independent in-situ SL problems advanced by one kernel per step.
+
+    problems: list of (velocity Tree, concentration Tree, dt)."""
+
+    def __init__(self, ctx, problems, num_rk_step=1, bc=FreeSpace):
+        n = len(problems)
+        vel = (ctypes.c_void_p * n)(*[p[0].handle.value for p in problems])
+        con = (ctypes.c_void_p * n)(*[p[1].handle.value for p in problems])
+        dt = (ctypes.c_double * n)(*[float(p[2]) for p in problems])
+        h = ctypes.c_void_p()
+        call("tbslas_batch_create", ctx.handle, n, ctypes.cast(vel, ctypes.c_void_p),
+             ctypes.cast(con, ctypes.c_void_p), ctypes.cast(dt, ctypes.c_void_p),
+             int(num_rk_step), int(bc), ctypes.byref(h))
+        self.ctx, self.handle, self.problems = ctx, h, list(problems)
+
+    def close(self):
+        if self.handle:
+            capi.lib().tbslas_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        t, w = ctypes.c_int64(), ctypes.c_int64()
+        call("tbslas_batch_info", self.handle, ctypes.byref(t), ctypes.byref(w))
+        return t.value, w.value
+
+    def params(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        call("tbslas_batch_get_params", self.handle, ctypes.byref(a), ctypes.byref(b),
+             ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def set_params(self, block, targets_per_item, ctas_per_sm):
+        call("tbslas_batch_set_params", self.handle, int(block), int(targets_per_item),
+             int(ctas_per_sm))
+
+    def autotune(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        call("tbslas_batch_autotune", self.handle, ctypes.byref(a), ctypes.byref(b),
+             ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def run(self, timestep0, nsteps, use_graph=True, stream=None):
+        call("tbslas_batch_run", self.handle, int(timestep0), int(nsteps), int(bool(use_graph)),
+             _stream(stream))
+
+
 def fast_interp(ctx, grid, dof, n_reg, pts, bc=FreeSpace, out=None, stream=None):
     import torch
     n = pts.numel() // 3

@@ -55,6 +55,13 @@ SIGNATURES = {
     "tbslas_set_tree_grid_values": [_vp, _vp, _vp, _vp],
     "tbslas_semilag_in_situ": [_vp, _vp, _vp, _i32, _f64, _i32, _i32, _vp],
     "tbslas_semilag_in_situ_host": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _i32],
+    "tbslas_batch_create": [_vp, _i32, _vp, _vp, _vp, _i32, _i32, _c.POINTER(_vp)],
+    "tbslas_batch_destroy": [_vp],
+    "tbslas_batch_info": [_vp, _i64p, _i64p],
+    "tbslas_batch_set_params": [_vp, _i32, _i32, _i32],
+    "tbslas_batch_get_params": [_vp, _i32p, _i32p, _i32p],
+    "tbslas_batch_autotune": [_vp, _i32p, _i32p, _i32p],
+    "tbslas_batch_run": [_vp, _i32, _i32, _i32, _vp],
     "tbslas_fast_interp": [_vp, _vp, _i32, _i32, _vp, _i64, _vp, _i32, _vp],
     "tbslas_semilag_grid": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _i32, _vp],
     "tbslas_semilag_grid_host": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _i32],

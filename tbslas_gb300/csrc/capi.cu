@@ -670,6 +670,33 @@ int bucketed_eval_on(const BucketScratch& b, tbslas_tree tree, const double* pos
 
 int fail_status(int code, const char* msg) { return fail(code, "%s", msg); }
 
+// Accessors for batch.cu.
+int tree_view(tbslas_tree t, TreeView* v, tbslas_ctx* ctx) {
+  if (!t || !t->ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null tree");
+  *v = t->view();
+  *ctx = t->ctx;
+  return TBSLAS_OK;
+}
+
+int tree_coeff(tbslas_tree t, double** coeff, int64_t* n_doubles) {
+  if (!t || !t->ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null tree");
+  *coeff = t->d_coeff;
+  *n_doubles = t->L * t->stride;
+  return TBSLAS_OK;
+}
+
+int ctx_info(tbslas_ctx ctx, int* device, int* num_sms) {
+  if (!ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null context");
+  *device = ctx->device;
+  *num_sms = ctx->num_sms;
+  return TBSLAS_OK;
+}
+
+int ctx_M(tbslas_ctx ctx, int q, const double** M) {
+  TRY(bind(ctx));
+  return device_M(ctx, q, M);
+}
+
 }  // namespace tbg
 
 // ===========================================================================
@@ -870,6 +897,7 @@ int tbslas_tree_set_coeffs_host(tbslas_tree t, const double* coeff_host) {
   TRY(check_tree(t));
   TRY(bind(t->ctx));
   if (!coeff_host) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
+  CUDA_TRY(cudaDeviceSynchronize());  // queued work on any stream may still use the tree
   TRY(copy_coeffs(t, t->d_coeff, coeff_host, true, cudaMemcpyHostToDevice, t->ctx->stream));
   CUDA_TRY(cudaStreamSynchronize(t->ctx->stream));
   return TBSLAS_OK;
@@ -926,6 +954,7 @@ int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_ho
   if (n == 0) return TBSLAS_OK;
   if (!pos_host || !out_host) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
   if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  CUDA_TRY(cudaDeviceSynchronize());  // the tree may still be written by queued work
   double *pos, *out;
   TRY(scratch_t(ctx, kHostIn, n * 3, &pos));
   TRY(scratch_t(ctx, kHostOut, n * tree->dof, &out));
@@ -961,6 +990,7 @@ int tbslas_traj_rk2_host(tbslas_ctx ctx, tbslas_tree vel, const double* x_host, 
   if (n == 0) return TBSLAS_OK;
   if (!x_host || !xdep_host) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
   if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  CUDA_TRY(cudaDeviceSynchronize());  // the tree may still be written by queued work
   double *x, *xd;
   TRY(scratch_t(ctx, kHostIn, n * 3, &x));
   TRY(scratch_t(ctx, kHostOut, n * 3, &xd));
@@ -1005,6 +1035,7 @@ int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con
                                 int bc) {
   TRY(check_step_args(ctx, vel, con, dt, nrk, bc));
   if (!con_coeff_host) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
+  CUDA_TRY(cudaDeviceSynchronize());  // queued work on any stream may still use the trees
   cudaStream_t s = ctx->stream;
   TRY(copy_coeffs(con, con->d_coeff, con_coeff_host, true, cudaMemcpyHostToDevice, s));
   TRY(semilag_in_situ_dev(ctx, vel, con, timestep, dt, nrk, bc, s));
@@ -1055,6 +1086,7 @@ int tbslas_semilag_grid(tbslas_ctx ctx, const double* vel_dev, const double* con
 int tbslas_semilag_grid_host(tbslas_ctx ctx, const double* vel_host, const double* con_host,
                              double* con_out_host, int n_reg, double dt, int nrk, int bc) {
   TRY(check_grid_args(ctx, vel_host, con_host, con_out_host, n_reg, dt, nrk, bc));
+  CUDA_TRY(cudaDeviceSynchronize());  // earlier queued work may still use the scratch
   const int64_t n3 = (int64_t)n_reg * n_reg * n_reg;
   double *vel, *con, *cout;
   TRY(scratch_t(ctx, kHostIn, n3 * 3, &vel));

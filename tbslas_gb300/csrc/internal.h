@@ -87,6 +87,26 @@ int tree_shape(tbslas_tree t, int64_t* L, int* device, int* dof);
 int bucketed_eval_on(const BucketScratch& b, tbslas_tree tree, const double* pos,
                      int64_t n, double* out, int bc, cudaStream_t s);
 int fail_status(int code, const char* msg);
+int tree_view(tbslas_tree t, TreeView* v, tbslas_ctx* ctx);
+int tree_coeff(tbslas_tree t, double** coeff, int64_t* n_doubles);
+int ctx_info(tbslas_ctx ctx, int* device, int* num_sms);
+int ctx_M(tbslas_ctx ctx, int q, const double** M);
+
+// Batched refit: one job per problem, one item per 64x64 output tile.
+constexpr int kRefitBM = 64, kRefitBN = 64, kRefitBK = 16;
+struct RefitJob {
+  const double* vals;
+  const double* M;
+  double* coeff;
+  int64_t rows;
+  int64_t stride;
+  int np, nc, dof, pad;
+};
+struct RefitItem {
+  int32_t job, row_tile, col_tile, pad;
+};
+void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_items,
+                        cudaStream_t s);
 
 // refit.cu: coeff[(r/dof)*stride + (r%dof)*nc + n] = sum_p vals[r*np+p] M[p*nc+n]
 void launch_refit(const double* vals, const double* M, int64_t rows, int np, int nc, int dof,

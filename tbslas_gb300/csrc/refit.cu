@@ -9,40 +9,38 @@
 
 namespace tbg {
 
-constexpr int kBM = 64, kBN = 64, kBK = 16;
-
-__global__ void __launch_bounds__(256) k_refit(const double* __restrict__ V,
-                                               const double* __restrict__ M, int64_t rows,
-                                               int np, int nc, int dof, int64_t stride,
-                                               double* __restrict__ C) {
-  __shared__ double As[kBK][kBM];
-  __shared__ double Bs[kBK][kBN];
+// One 64x64 output tile of C = V M (rows x nc), written into the padded
+// per-leaf coefficient layout.  Shared by the single-tree and batched kernels.
+__device__ __forceinline__ void refit_tile(const double* __restrict__ V,
+                                           const double* __restrict__ M, int64_t rows, int np,
+                                           int nc, int dof, int64_t stride, double* __restrict__ C,
+                                           int64_t row0, int col0) {
+  __shared__ double As[kRefitBK][kRefitBM];
+  __shared__ double Bs[kRefitBK][kRefitBN];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int64_t row0 = (int64_t)blockIdx.x * kBM;
-  const int col0 = blockIdx.y * kBN;
   double acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
 
-  for (int k0 = 0; k0 < np; k0 += kBK) {
+  for (int k0 = 0; k0 < np; k0 += kRefitBK) {
 #pragma unroll
-    for (int e = threadIdx.x; e < kBM * kBK; e += 256) {
-      const int r = e / kBK, k = e % kBK;
+    for (int e = threadIdx.x; e < kRefitBM * kRefitBK; e += 256) {
+      const int r = e / kRefitBK, k = e % kRefitBK;
       const int64_t row = row0 + r;
       const int kk = k0 + k;
       As[k][r] = (row < rows && kk < np) ? __ldg(V + row * np + kk) : 0.0;
     }
 #pragma unroll
-    for (int e = threadIdx.x; e < kBK * kBN; e += 256) {
-      const int k = e / kBN, c = e % kBN;
+    for (int e = threadIdx.x; e < kRefitBK * kRefitBN; e += 256) {
+      const int k = e / kRefitBN, c = e % kRefitBN;
       const int kk = k0 + k, col = col0 + c;
       Bs[k][c] = (kk < np && col < nc) ? __ldg(M + (int64_t)kk * nc + col) : 0.0;
     }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < kBK; ++k) {
+    for (int k = 0; k < kRefitBK; ++k) {
       double a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = As[k][ty + 16 * i];
@@ -70,10 +68,32 @@ __global__ void __launch_bounds__(256) k_refit(const double* __restrict__ V,
   }
 }
 
+__global__ void __launch_bounds__(256) k_refit(const double* __restrict__ V,
+                                               const double* __restrict__ M, int64_t rows,
+                                               int np, int nc, int dof, int64_t stride,
+                                               double* __restrict__ C) {
+  refit_tile(V, M, rows, np, nc, dof, stride, C, (int64_t)blockIdx.x * kRefitBM,
+             blockIdx.y * kRefitBN);
+}
+
+// Batched refit: one CTA per (problem, row tile, column tile) work item.
+__global__ void __launch_bounds__(256) k_batch_refit(const RefitJob* __restrict__ jobs,
+                                                     const RefitItem* __restrict__ items) {
+  const RefitItem it = items[blockIdx.x];
+  const RefitJob j = jobs[it.job];
+  refit_tile(j.vals, j.M, j.rows, j.np, j.nc, j.dof, j.stride, j.coeff,
+             (int64_t)it.row_tile * kRefitBM, it.col_tile * kRefitBN);
+}
+
+void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_items,
+                        cudaStream_t s) {
+  if (n_items > 0) k_batch_refit<<<(unsigned)n_items, 256, 0, s>>>(jobs, items);
+}
+
 void launch_refit(const double* vals, const double* M, int64_t rows, int np, int nc, int dof,
                   int64_t stride, double* coeff, cudaStream_t s) {
   if (rows <= 0) return;
-  dim3 grid((unsigned)((rows + kBM - 1) / kBM), (unsigned)((nc + kBN - 1) / kBN));
+  dim3 grid((unsigned)((rows + kRefitBM - 1) / kRefitBM), (unsigned)((nc + kRefitBN - 1) / kRefitBN));
   k_refit<<<grid, 256, 0, s>>>(vals, M, rows, np, nc, dof, stride, coeff);
 }
 

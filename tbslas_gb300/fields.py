@@ -95,13 +95,31 @@ def fourier_modes(rng, kmax=4):
 def fourier_velocity(rng, kmax=4):
     """v(x) = sum_k A_k cos(2pi k.x) + B_k sin(2pi k.x) as a point function."""
     ks, A, B = fourier_modes(rng, kmax)
+    return fourier_velocity_from_modes(ks, A, B, kmax)
+
+
+def fourier_velocity_from_modes(ks, A, B, kmax=4):
+    """Evaluated as Re sum_k (A_k - i B_k) e_x[k_x] e_y[k_y] e_z[k_z] with the
+    per-axis exponentials tabulated once per call."""
+    ki = ks.astype(int)
+    r = int(kmax)
+    coef = A - 1j * B
 
     def fn(p):
-        p = np.asarray(p).reshape(-1, 3)
+        p = np.asarray(p, dtype=np.float64).reshape(-1, 3)
+        kk = np.arange(-r, r + 1)
+        E = [np.exp(2j * math.pi * np.outer(p[:, a], kk)) for a in range(3)]  # [n, 2r+1]
         out = np.zeros((len(p), 3))
-        ph = 2 * math.pi * (p @ ks.T)
-        out += np.cos(ph) @ A
-        out += np.sin(ph) @ B
+        # group modes by (k_y, k_z): sum over k_x first
+        groups = {}
+        for m, (kx, ky, kz) in enumerate(ki):
+            groups.setdefault((ky, kz), []).append(m)
+        for (ky, kz), ms in groups.items():
+            eyz = E[1][:, ky + r] * E[2][:, kz + r]
+            acc = np.zeros((len(p), 3), dtype=np.complex128)
+            for m in ms:
+                acc += E[0][:, ki[m, 0] + r, None] * coef[m][None, :]
+            out += (acc * eyz[:, None]).real
         return out
     fn.modes = (ks, A, B)
     return fn

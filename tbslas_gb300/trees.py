@@ -117,12 +117,15 @@ def balance21(anchor, depth, periodic=False):
         depth = np.concatenate([depth[~refine], cd])
 
 
-def adaptive_tree(fn, q, dof, tol, min_depth, max_depth, balance=True, periodic=False, M=None):
-    """Leaves refined by the coefficient-tail rule; returns (anchor, depth)."""
+def adaptive_tree(fn, q, dof, tol, min_depth, max_depth, balance=True, periodic=False, M=None,
+                  fitter=None):
+    """Leaves refined by the coefficient-tail rule; returns (anchor, depth).
+
+    fitter(anchor, depth) -> [L, dof, Nc] replaces fit(fn, ...) when given."""
     M = api.get_pt2coeff_matrix(q) if M is None else M
     anchor, depth = uniform_tree(min_depth)
     while True:
-        c = fit(fn, anchor, depth, q, dof, M)
+        c = fitter(anchor, depth) if fitter is not None else fit(fn, anchor, depth, q, dof, M)
         refine = (tail(c, q) > tol) & (depth < max_depth)
         if not refine.any():
             break

@@ -85,11 +85,104 @@ class GridWorkload:
                         "Fourier velocity |k|<=4, Gaussian blob"}
 
 
+def fourier_fitter(modes, q, M):
+    """Fits the Fourier velocity on every leaf: torch on the GPU when one is
+    present (the point count runs into the millions), numpy otherwise."""
+    ks, A, B = modes
+    coef = A - 1j * B
+
+    try:
+        import torch
+        use_gpu = torch.cuda.is_available()
+    except ImportError:
+        use_gpu = False
+
+    def fit_gpu(anchor, depth):
+        import torch
+        dev = "cuda"
+        nodes = torch.from_numpy(api_nodes(q)).to(dev)                      # [Np, 3]
+        a = torch.from_numpy(anchor).to(dev)
+        h = torch.from_numpy(np.ldexp(1.0, -depth.astype(np.int64))).to(dev)
+        L, Np = len(depth), nodes.shape[0]
+        out = torch.empty((L, 3, M.shape[1]), dtype=torch.float64, device=dev)
+        Mt = torch.from_numpy(M).to(dev)
+        kt = torch.from_numpy(ks).to(dev)
+        ct = torch.from_numpy(coef).to(dev)                                # [m, 3]
+        step = max(1, (1 << 21) // Np)
+        for l0 in range(0, L, step):
+            l1 = min(L, l0 + step)
+            pts = (a[l0:l1, None, :] + h[l0:l1, None, None] * nodes[None]).reshape(-1, 3)
+            ph = 2 * math.pi * (pts @ kt.T)                                  # [n, m]
+            v = torch.cos(ph) @ ct.real + torch.sin(ph) @ (-ct.imag)        # [n, 3]
+            vals = v.reshape(l1 - l0, Np, 3).permute(0, 2, 1).reshape(-1, Np)
+            out[l0:l1] = (vals @ Mt).reshape(l1 - l0, 3, -1)
+        return out.cpu().numpy()
+
+    def fit_cpu(anchor, depth):
+        fn = fields.fourier_velocity_from_modes(ks, A, B)
+        return trees.fit(fn, anchor, depth, q, 3, M)
+
+    return fit_gpu if use_gpu else fit_cpu
+
+
+def api_nodes(q):
+    from . import api
+    return api.new_nodes(q)
+
+
+class BatchWorkload:
+    """Independent problems of uneven size: degree q ~ U{qlo..qhi}, maximum
+    depth ~ U{dlo..dhi}; velocity = random divergence-free Fourier field
+    (|k| <= 4, amplitudes N(0,1)/|k|^2), concentration = 1..8 Gaussian blobs;
+    both trees refined by the coefficient-tail rule at tolerance `tol`
+    (minimum depth 2); periodic; dt for Chebyshev CFL 1 on the finest leaf."""
+
+    def __init__(self, n=64, seed=SEED, qs=(8, 14), depths=(4, 7), tol=1e-5, min_depth=2,
+                 name="batched_64", qlist=None):
+        from . import api
+        rng = np.random.default_rng(seed)
+        self.name, self.bc, self.problems = name, 1, []
+        Ms = {}
+        for i in range(n):
+            q = int(rng.integers(qs[0], qs[1] + 1))
+            if qlist is not None:
+                q = int(qlist[i % len(qlist)])
+            dmax = int(rng.integers(depths[0], depths[1] + 1))
+            M = Ms.setdefault(q, api.get_pt2coeff_matrix(q))
+            modes = fields.fourier_modes(rng)
+            blobs = fields.gaussian_blobs(rng, int(rng.integers(1, 9)))
+            vfit = fourier_fitter(modes, q, M)
+            va, vd = trees.adaptive_tree(None, q, 3, tol, min_depth, dmax, periodic=True, M=M,
+                                         fitter=vfit)
+            ca, cd = trees.adaptive_tree(blobs, q, 1, tol, min_depth, dmax, periodic=True, M=M)
+            vc = vfit(va, vd)
+            cc = trees.fit(blobs, ca, cd, q, 1, M)
+            finest = int(max(vd.max(), cd.max()))
+            dt = 1.0 / (2.0 ** finest * q * q)
+            self.problems.append(dict(q=q, dmax=dmax, va=va, vd=vd, vc=vc, ca=ca, cd=cd, cc=cc,
+                                      dt=dt))
+
+    @property
+    def points_per_step(self):
+        return sum(len(p["cd"]) * (p["q"] + 1) ** 3 for p in self.problems)
+
+    def describe(self):
+        qs = [p["q"] for p in self.problems]
+        return {"workload": self.name, "problems": len(self.problems),
+                "q_range": [min(qs), max(qs)],
+                "con_leaves": int(sum(len(p["cd"]) for p in self.problems)),
+                "vel_leaves": int(sum(len(p["vd"]) for p in self.problems)),
+                "departure_points_per_step": int(self.points_per_step),
+                "bc": "periodic", "note": self.__doc__.split("\n")[0]}
+
+
 def make(name):
     if name == "tree_uniform_q8":
         return tree_uniform_q8()
     if name == "tree_adaptive_q14":
         return tree_adaptive_q14()
+    if name == "batched_64":
+        return BatchWorkload()
     if name.startswith("grid_periodic_"):
         return GridWorkload(int(name.rsplit("_", 1)[1]))
     raise ValueError("unknown workload %r" % name)
