@@ -491,6 +491,108 @@ def run_batched(args, wl, rank, world, local_rank):
     assert ctx.check() == 0
 
 
+def run_adjoint(args, wl, rank, world, local_rank):
+    """Config 5: forward (plain and checkpointed) and adjoint passes of the
+    T-step advection, timed; gradients checked by central differences."""
+    import torch
+    import tbslas_gb300 as tb
+    from tbslas_gb300 import adjoint
+
+    torch.cuda.set_device(local_rank)
+    ctx = tb.Context(local_rank)
+    stream = torch.cuda.current_stream()
+    dev = torch.device("cuda", local_rank)
+    tv = tb.Tree(ctx, wl.a, wl.d, wl.q, 3, wl.vc)
+    tc = tb.Tree(ctx, wl.a, wl.d, wl.q, 1, wl.c0)
+    V = torch.from_numpy(adjoint.basis_at_nodes(wl.q)).to(dev)
+    vct = torch.from_numpy(wl.vc).to(dev)
+    c0 = torch.from_numpy(wl.c0).to(dev)
+    T = wl.steps
+    with torch.no_grad():
+        cobs = adjoint.advect(torch.from_numpy(wl.c0_obs).to(dev), vct, tv, tc, wl.dt, 1, T,
+                              wl.bc, False)
+
+    def J(c):
+        vals = torch.einsum("ln,pn->lp", c[:, 0, :], V)
+        ovals = torch.einsum("ln,pn->lp", cobs[:, 0, :], V)
+        return 0.5 * ((vals - ovals) ** 2).sum()
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    def fwd_plain():
+        with torch.no_grad():
+            return adjoint.advect(c0, vct, tv, tc, wl.dt, 1, T, wl.bc, False)
+
+    def grad(checkpoint):
+        c = c0.clone().requires_grad_(True)
+        v = vct.clone().requires_grad_(True)
+        cT = adjoint.advect(c, v, tv, tc, wl.dt, 1, T, wl.bc, checkpoint)
+        j = J(cT)
+        torch.cuda.synchronize()
+        return c, v, j
+
+    for _ in range(args.warmup if args.warmup < 3 else 1):
+        fwd_plain()
+    fwd_ms, _ = timed(fwd_plain)
+    res = {}
+    for ck in (True, False):
+        fms, (c, v, j) = timed(lambda: grad(ck))
+        bms, _ = timed(lambda: j.backward())
+        res[ck] = (fms, bms, c.grad.clone(), v.grad.clone(), j.item())
+    gc, gv = res[True][2], res[True][3]
+    rng = np.random.default_rng(123)
+    eps = 1e-6
+    errs_c, errs_v = [], []
+
+    def J_at(cc, vv):
+        with torch.no_grad():
+            return J(adjoint.advect(cc, vv, tv, tc, wl.dt, 1, T, wl.bc, False)).item()
+
+    for k in range(16):
+        if k % 2 == 0:
+            d = torch.from_numpy(rng.standard_normal(wl.c0.shape)).to(dev)
+            fd = (J_at(c0 + eps * d, vct) - J_at(c0 - eps * d, vct)) / (2 * eps)
+            an = (gc * d).sum().item()
+            errs_c.append(abs(fd - an) / abs(an))
+        else:
+            d = torch.from_numpy(rng.standard_normal(wl.vc.shape)).to(dev)
+            fd = (J_at(c0, vct + eps * d) - J_at(c0, vct - eps * d)) / (2 * eps)
+            an = (gv * d).sum().item()
+            errs_v.append(abs(fd - an) / abs(an))
+    ck_fms, ck_bms = res[True][0], res[True][1]
+    rc_fms, rc_bms = res[False][0], res[False][1]
+    ck_gap = max(float((res[True][2] - res[False][2]).abs().max() / res[False][2].abs().max()),
+                 float((res[True][3] - res[False][3]).abs().max() / res[False][3].abs().max()))
+    points = wl.points_per_step * T
+    if rank != 0:
+        return
+    cfg = wl.describe()
+    line = {"metric": METRIC, "value": points / (ck_bms * 1e-3), "unit": UNIT + " (adjoint pass)",
+            "n_gpus": world, "steps": T, "warmup": 1, "ms_per_step": ck_bms / T,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded analytic fields)", "config": cfg,
+            "forward": {"ms": fwd_ms, "points_per_s": points / (fwd_ms * 1e-3)},
+            "checkpoint": {"forward_ms": ck_fms, "adjoint_ms": ck_bms,
+                           "adj_over_fwd": ck_bms / fwd_ms,
+                           "grad_over_fwd": (ck_fms + ck_bms) / fwd_ms,
+                           "stored_bytes": int(points * 48)},
+            "recompute": {"forward_ms": rc_fms, "adjoint_ms": rc_bms,
+                          "adj_over_fwd": rc_bms / fwd_ms,
+                          "grad_over_fwd": (rc_fms + rc_bms) / fwd_ms, "stored_bytes": 0},
+            "fd_check": {"eps": eps, "directions": 16,
+                         "max_rel_err_dJ_dc0": max(errs_c), "max_rel_err_dJ_dV": max(errs_v)},
+            "checkpoint_vs_recompute_rel_diff": ck_gap, "J": res[True][4]}
+    print(json.dumps(line))
+    assert ctx.check() == 0
+
+
 def _band(q):
     return 0 if q <= 8 else (1 if q <= 12 else 2)
 
@@ -524,6 +626,8 @@ def main():
     try:
         if args.workload.startswith("batched"):
             run_batched(args, wl, rank, world, local_rank)
+        elif args.workload.startswith("adjoint"):
+            run_adjoint(args, wl, rank, world, local_rank)
         else:
             run_gpu(args, wl, rank, world, local_rank)
     finally:

@@ -198,6 +198,29 @@ int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con
                                 double* con_coeff_host, int timestep, double dt, int nrk,
                                 int bc);
 
+/* ---- differentiation (adjoint of the in-situ step, nrk = 1) ------------------ */
+/* No counterpart in the reference.  The forward map of one step is
+ * C^{k+1} = refit(c^k(Xd(V))), Xd = X + tau v(X + tau/2 v(X)), for every node
+ * X of `con`; the adjoint gives dJ/dC^k and dJ/dV from dJ/dC^{k+1}.  Both
+ * support Chebyshev degree 1..10, a dof-3 velocity and a dof-1 concentration
+ * tree of the same degree. */
+/* tbslas_semilag_in_situ with nrk = 1 that also stores, per target node
+ * (leaf-major, node order of CollectChebTreeGridPoints), the RK2 midpoint
+ * xmid_dev[N*3] and departure point xdep_dev[N*3], N = L (q+1)^3. */
+int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
+                                double dt, int bc, double* xmid_dev, double* xdep_dev,
+                                void* stream);
+/* Adjoint of step `timestep`: con_coeff_k_dev [L][Nc] = the concentration
+ * coefficients the step started from; lambda_next_dev [L][Nc] = dJ/dC^{k+1};
+ * writes lambda_k_dev [L][Nc] = dJ/dC^k and ADDS the step's dJ/dV to
+ * grad_vel_dev [Lv][3][Nc].  xmid/xdep: the step's checkpoints, or both NULL
+ * to recompute them.  Velocity coefficients are read from `vel`. */
+int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                           const double* con_coeff_k_dev, int timestep, double dt, int bc,
+                           const double* lambda_next_dev, double* lambda_k_dev,
+                           double* grad_vel_dev, const double* xmid_dev, const double* xdep_dev,
+                           void* stream);
+
 /* ---- batched in-situ SL --------------------------------------------------------- */
 /* Many independent in-situ SL problems advanced together: problem i is
  * (vel[i] (dof 3), con[i] (dof 1, same degree), dt[i]); all share nrk and bc.

@@ -31,6 +31,37 @@ namespace orc {
 
 typedef double Real;
 
+// Forward-mode dual number (value, directional derivative) for the
+// dual-number gradient of the SL step: the tree path below is templated on
+// its number type R, and R = Dual carries d/ds of every quantity along one
+// input direction.  Value parts are computed with exactly the operations of
+// R = double, so they reproduce the double oracle bit for bit; leaf choices
+// and the |x|>1 rule use value parts only (the derivative of the discrete
+// map with leaf assignment held fixed).
+struct Dual {
+  double v, d;
+};
+static inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+static inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+static inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
+static inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.v * b.d + a.d * b.v}; }
+static inline Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
+static inline Dual operator-(Dual a, double b) { return {a.v - b, a.d}; }
+static inline Dual operator*(Dual a, double b) { return {a.v * b, a.d * b}; }
+static inline Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
+static inline Dual& operator*=(Dual& a, double b) { a = a * b; return a; }
+static inline double val(double x) { return x; }
+static inline double val(Dual x) { return x.v; }
+template <class R> static inline R mk(double v) { return R(v); }
+template <> inline Dual mk<Dual>(double v) { return Dual{v, 0.0}; }
+static inline double fmaR(double a, double b, double c) { return std::fma(a, b, c); }
+static inline Dual fmaR(Dual a, Dual b, Dual c) {
+  return {std::fma(a.v, b.v, c.v), a.v * b.d + a.d * b.v + c.d};
+}
+static inline Dual fmaR(double a, Dual b, Dual c) {
+  return {std::fma(a, b.v, c.v), a * b.d + c.d};
+}
+
 // ---------------------------------------------------------------------------
 // Chebyshev nodes stretched onto [0,1], x fastest.
 // Restates tbslas::new_nodes, src/utils/cheb.h:41-67.
@@ -61,18 +92,19 @@ static std::vector<Real> new_nodes(int deg, int dim) {
 // wherever a contracting compiler fuses them in the reference's build (the
 // recurrence, vec_eval's accumulations, the RK2 updates), so the oracle's
 // rounding is fixed and the same on every host.
-static void cheb_poly(int q, const Real* in, int n, Real* out) {
+template <class R>
+static void cheb_poly(int q, const R* in, int n, R* out) {
   for (int j = 0; j < n; j++) {
-    const bool ok = std::fabs(in[j]) <= 1;
-    Real x = ok ? in[j] : 0;
-    Real y0 = ok ? 1.0 : 0;
+    const bool ok = std::fabs(val(in[j])) <= 1;
+    R x = ok ? in[j] : mk<R>(0);
+    R y0 = mk<R>(ok ? 1.0 : 0.0);
     out[j] = y0;
     if (q == 0) continue;
     out[j + n] = x;
-    Real y1 = x;
+    R y1 = x;
     x *= 2;
     for (int i = 2; i <= q; i++) {
-      Real y2 = std::fma(x, y1, -y0);
+      R y2 = fmaR(x, y1, -y0);
       out[i * n + j] = y2;
       y0 = y1;
       y1 = y2;
@@ -109,11 +141,12 @@ static const unsigned __int128 kKeyMax = ~(unsigned __int128)0;
 // after every leaf, i.e. it is handed to the last leaf, where cheb_poly's
 // |x|>1 rule evaluates it to 0 (the reference reaches the same leaf through
 // the wrap-around of its unsigned cast).
-static Mid point_mid(const Real* c, bool periodic) {
+template <class R>
+static Mid point_mid(const R* c, bool periodic) {
   const Real shift = 1.0 / (Real)(1UL << kMaxDepth);
   uint64_t q[3];
   for (int k = 0; k < 3; k++) {
-    Real v = c[k];
+    Real v = val(c[k]);
     if (v == 1.0 && !periodic) v = v - shift;
     if (!(v >= 0.0 && v < 1.0)) return Mid{kKeyMax, kMaxDepth};
     q[k] = (uint64_t)std::floor(v * (Real)(1UL << kMaxDepth));
@@ -124,12 +157,13 @@ static Mid point_mid(const Real* c, bool periodic) {
 // ---------------------------------------------------------------------------
 // A linear octree given by its leaves (anchor, depth) in Morton order with
 // per-leaf triangular Chebyshev coefficients [leaf][dof][Nc].
-struct Tree {
+template <class R>
+struct TreeT {
   long L;
   const Real* anchor;  // L x 3
   const int* depth;    // L
   int q, dof;
-  const Real* coeff;   // L x dof x Nc
+  const R* coeff;      // L x dof x Nc
   std::vector<Mid> mid;
   long nc() const { return (long)(q + 1) * (q + 2) * (q + 3) / 6; }
   void init() {
@@ -149,29 +183,30 @@ struct Tree {
 // Restates pvfmm::vec_eval, src/tree/tree_functor.h:27-84 (coefficients in a
 // padded d0^3 cube, points processed 16 at a time as in the 4xVecLen AVX
 // unroll, same i/j/k summation order, fused multiply-add accumulation).
-static void vec_eval(int n, int d0, int d, int dof, const Real* px, const Real* py,
-                     const Real* pz, const Real* coeff, Real* tmp_out) {
+template <class R>
+static void vec_eval(int n, int d0, int d, int dof, const R* px, const R* py, const R* pz,
+                     const R* coeff, R* tmp_out) {
   const int B = 16;
   for (int l0 = 0; l0 < dof; l0++) {
     for (int l1 = 0; l1 < n; l1 += B) {
-      Real u[B];
-      for (int p = 0; p < B; p++) u[p] = 0;
+      R u[B];
+      for (int p = 0; p < B; p++) u[p] = mk<R>(0);
       for (int i = 0; i < d; i++) {
-        Real v[B];
-        for (int p = 0; p < B; p++) v[p] = 0;
-        const Real* pz_ = pz + i * n + l1;
+        R v[B];
+        for (int p = 0; p < B; p++) v[p] = mk<R>(0);
+        const R* pz_ = pz + i * n + l1;
         for (int j = 0; i + j < d; j++) {
-          Real w[B];
-          for (int p = 0; p < B; p++) w[p] = 0;
-          const Real* py_ = py + j * n + l1;
+          R w[B];
+          for (int p = 0; p < B; p++) w[p] = mk<R>(0);
+          const R* py_ = py + j * n + l1;
           for (int k = 0; i + j + k < d; k++) {
-            const Real* px_ = px + k * n + l1;
-            const Real c = coeff[k + d0 * (j + d0 * (i + d0 * l0))];
-            for (int p = 0; p < B; p++) w[p] = std::fma(px_[p], c, w[p]);
+            const R* px_ = px + k * n + l1;
+            const R c = coeff[k + d0 * (j + d0 * (i + d0 * l0))];
+            for (int p = 0; p < B; p++) w[p] = fmaR(px_[p], c, w[p]);
           }
-          for (int p = 0; p < B; p++) v[p] = std::fma(py_[p], w[p], v[p]);
+          for (int p = 0; p < B; p++) v[p] = fmaR(py_[p], w[p], v[p]);
         }
-        for (int p = 0; p < B; p++) u[p] = std::fma(pz_[p], v[p], u[p]);
+        for (int p = 0; p < B; p++) u[p] = fmaR(pz_[p], v[p], u[p]);
       }
       for (int p = 0; p < B; p++) tmp_out[l0 * n + l1 + p] = u[p];
     }
@@ -185,8 +220,9 @@ static void vec_eval(int n, int d0, int d, int dof, const Real* px, const Real* 
 // contiguous point range (:212-243); coefficients repacked into a padded cube
 // (:248-268); blocks of 288 points mapped to [-1,1] (:270-295); cheb_poly and
 // vec_eval (:303-366); transpose to point-major (:376-383).
-static void eval_nodes_local(const Tree& t, const Real* coord, const Mid* trg_mid, size_t N,
-                             Real* value) {
+template <class R>
+static void eval_nodes_local(const TreeT<R>& t, const R* coord, const Mid* trg_mid, size_t N,
+                             R* value) {
   const int dof = t.dof;
   const long L = t.L;
   std::vector<size_t> part(L + 1);
@@ -201,8 +237,8 @@ static void eval_nodes_local(const Tree& t, const Real* coord, const Mid* trg_mi
     const int d = t.q + 1;
     int d0 = d;
     while (d0 % 4) d0++;
-    std::vector<Real> coeff_((size_t)d0 * d0 * d0 * dof, 0.0);
-    std::vector<Real> cx, cy, cz, px, py, pz, tmp_out;
+    std::vector<R> coeff_((size_t)d0 * d0 * d0 * dof, mk<R>(0));
+    std::vector<R> cx, cy, cz, px, py, pz, tmp_out;
 
     size_t pt_start0 = (size_t)pid * N / omp_p;
     size_t pt_end0 = (size_t)(pid + 1) * N / omp_p;
@@ -215,7 +251,7 @@ static void eval_nodes_local(const Tree& t, const Real* coord, const Mid* trg_mi
       size_t b = std::min(pt_end0, part[j + 1]);
       if (a >= b) continue;
       {  // repack the triangular coefficients into the padded cube
-        const Real* c = t.coeff + (size_t)j * dof * t.nc();
+        const R* c = t.coeff + (size_t)j * dof * t.nc();
         long indx = 0;
         for (int l0 = 0; l0 < dof; l0++)
           for (int i = 0; i < d; i++)
@@ -231,24 +267,24 @@ static void eval_nodes_local(const Tree& t, const Real* coord, const Mid* trg_mi
         const int npts = (int)(pe - ps);
         int n = npts;
         while (n % 16) n++;
-        cx.assign(n, 0.0);
-        cy.assign(n, 0.0);
-        cz.assign(n, 0.0);
+        cx.assign(n, mk<R>(0));
+        cy.assign(n, mk<R>(0));
+        cz.assign(n, mk<R>(0));
         for (int i = 0; i < npts; i++) {
-          const Real* p = coord + (ps + i) * 3;
+          const R* p = coord + (ps + i) * 3;
           cx[i] = (p[0] - anc[0]) * 2.0 * s - 1.0;
           cy[i] = (p[1] - anc[1]) * 2.0 * s - 1.0;
           cz[i] = (p[2] - anc[2]) * 2.0 * s - 1.0;
         }
-        px.assign((size_t)d0 * n, 0.0);
-        py.assign((size_t)d0 * n, 0.0);
-        pz.assign((size_t)d0 * n, 0.0);
+        px.assign((size_t)d0 * n, mk<R>(0));
+        py.assign((size_t)d0 * n, mk<R>(0));
+        pz.assign((size_t)d0 * n, mk<R>(0));
         cheb_poly(t.q, cx.data(), n, px.data());
         cheb_poly(t.q, cy.data(), n, py.data());
         cheb_poly(t.q, cz.data(), n, pz.data());
         tmp_out.resize((size_t)n * dof);
         vec_eval(n, d0, d, dof, px.data(), py.data(), pz.data(), coeff_.data(), tmp_out.data());
-        Real* out = value + ps * dof;
+        R* out = value + ps * dof;
         for (int i = 0; i < npts; i++)
           for (int l = 0; l < dof; l++) out[i * dof + l] = tmp_out[l * n + i];
       }
@@ -261,13 +297,14 @@ static void eval_nodes_local(const Tree& t, const Real* coord, const Mid* trg_mi
 // on one rank (lcl_start = 0, lcl_end = N): periodic wrap of the caller's
 // array IN PLACE (:442-448), Morton sort with index tracking (:463-489),
 // evaluation of the sorted points (:656-677), un-permutation (:683-690).
-static void eval_tree(const Tree& t, Real* pos, size_t N, Real* value, bool periodic) {
+template <class R>
+static void eval_tree(const TreeT<R>& t, R* pos, size_t N, R* value, bool periodic) {
   if (periodic) {
 #pragma omp parallel for
     for (size_t i = 0; i < N * 3; i++) {
-      Real& c = pos[i];
-      if (c < 0.0) c = c + 1.0;
-      if (c >= 1.0) c = c - 1.0;
+      R& c = pos[i];
+      if (val(c) < 0.0) c = c + 1.0;
+      if (val(c) >= 1.0) c = c - 1.0;
     }
   }
   struct Pair {
@@ -279,51 +316,55 @@ static void eval_tree(const Tree& t, Real* pos, size_t N, Real* value, bool peri
   for (size_t i = 0; i < N; i++) pr[i] = Pair{point_mid(pos + 3 * i, periodic), i};
   std::stable_sort(pr.begin(), pr.end(), [](const Pair& a, const Pair& b) { return a.key < b.key; });
 
-  std::vector<Real> coord(N * 3), val(N * t.dof);
+  std::vector<R> coord(N * 3), vals(N * t.dof);
   std::vector<Mid> mids(N);
 #pragma omp parallel for
   for (size_t i = 0; i < N; i++) {
     for (int k = 0; k < 3; k++) coord[3 * i + k] = pos[3 * pr[i].data + k];
     mids[i] = pr[i].key;
   }
-  eval_nodes_local(t, coord.data(), mids.data(), N, val.data());
+  eval_nodes_local(t, coord.data(), mids.data(), N, vals.data());
 #pragma omp parallel for
   for (size_t i = 0; i < N; i++)
-    for (int l = 0; l < t.dof; l++) value[pr[i].data * t.dof + l] = val[i * t.dof + l];
+    for (int l = 0; l < t.dof; l++) value[pr[i].data * t.dof + l] = vals[i * t.dof + l];
 }
 
 // ---------------------------------------------------------------------------
 // Midpoint RK2.  Restates IntegrateRK2 / ComputeTrajRK2,
 // src/semilag/traj.inc:20-68: xsol aliases xinit, so the functor's in-place
 // periodic wrap of xinit is seen by the final update.
-template <class Functor>
-static void integrate_rk2(Functor& fn, Real* x, size_t N, Real tau) {
-  std::vector<Real> xtmp(N * 3), vtmp(N * 3);
+template <class R, class Functor>
+static void integrate_rk2(Functor& fn, R* x, size_t N, Real tau) {
+  std::vector<R> xtmp(N * 3), vtmp(N * 3);
   fn(x, N, vtmp.data());
 #pragma omp parallel for
-  for (size_t i = 0; i < N * 3; i++) xtmp[i] = std::fma(0.5 * tau, vtmp[i], x[i]);
+  for (size_t i = 0; i < N * 3; i++) xtmp[i] = fmaR(0.5 * tau, vtmp[i], x[i]);
   fn(xtmp.data(), N, vtmp.data());
 #pragma omp parallel for
-  for (size_t i = 0; i < N * 3; i++) x[i] = std::fma(tau, vtmp[i], x[i]);
+  for (size_t i = 0; i < N * 3; i++) x[i] = fmaR(tau, vtmp[i], x[i]);
 }
 
-template <class Functor>
-static void traj_rk2(Functor& fn, const Real* xinit, size_t N, Real tinit, Real tfinal, int nrk,
-                     Real* xsol) {
+template <class R, class Functor>
+static void traj_rk2(Functor& fn, const R* xinit, size_t N, Real tinit, Real tfinal, int nrk,
+                     R* xsol) {
   Real tau = (tfinal - tinit) / nrk;
-  std::memcpy(xsol, xinit, sizeof(Real) * N * 3);
-  for (int s = 0; s < nrk; s++) integrate_rk2(fn, xsol, N, tau);
+  std::memcpy(xsol, xinit, sizeof(R) * N * 3);
+  for (int s = 0; s < nrk; s++) integrate_rk2<R>(fn, xsol, N, tau);
 }
 
-struct TreeFunctor {
-  const Tree* t;
+template <class R>
+struct TreeFunctorT {
+  const TreeT<R>* t;
   bool periodic;
-  void operator()(Real* pos, size_t n, Real* out) { eval_tree(*t, pos, n, out, periodic); }
+  void operator()(R* pos, size_t n, R* out) { eval_tree(*t, pos, n, out, periodic); }
 };
+typedef TreeT<Real> Tree;
+typedef TreeFunctorT<Real> TreeFunctor;
 
 // Leaf Chebyshev nodes of every leaf, leaves in order.  Restates
 // CollectChebTreeGridPoints, src/tree/tree_utils.h:442-498.
-static void collect_grid_points(const Tree& t, Real* out) {
+template <class R>
+static void collect_grid_points(const TreeT<R>& t, Real* out) {
   std::vector<Real> nodes = new_nodes(t.q, 3);
   const long np = (long)nodes.size() / 3;
 #pragma omp parallel for
@@ -339,24 +380,25 @@ static void collect_grid_points(const Tree& t, Real* out) {
 // Node values -> coefficients, coeff[row][n] = sum_p vals[row][p] M[p][n] with
 // row = leaf*dof + l.  Restates SetTreeGridValues, src/tree/tree_utils.h:500-552
 // (per-thread row blocks, GEMM against the point-to-coefficient matrix).
+template <class R>
 static void set_tree_grid_values(long L, int dof, long np, long nc, const Real* M,
-                                 const Real* vals, Real* coeff) {
-  const long R = L * dof;
+                                 const R* vals, R* coeff) {
+  const long rows = L * dof;
   const int RB = 4;
 #pragma omp parallel for schedule(static)
-  for (long r0 = 0; r0 < R; r0 += RB) {
-    const int rb = (int)std::min<long>(RB, R - r0);
-    std::vector<Real> acc((size_t)RB * nc, 0.0);
+  for (long r0 = 0; r0 < rows; r0 += RB) {
+    const int rb = (int)std::min<long>(RB, rows - r0);
+    std::vector<R> acc((size_t)RB * nc, mk<R>(0));
     for (long p = 0; p < np; p++) {
       const Real* m = M + p * nc;
       for (int rr = 0; rr < rb; rr++) {
-        const Real v = vals[(r0 + rr) * np + p];
-        Real* a = acc.data() + rr * nc;
+        const R v = vals[(r0 + rr) * np + p];
+        R* a = acc.data() + rr * nc;
         for (long n = 0; n < nc; n++) a[n] = a[n] + v * m[n];
       }
     }
     for (int rr = 0; rr < rb; rr++)
-      std::memcpy(coeff + (r0 + rr) * nc, acc.data() + rr * nc, sizeof(Real) * nc);
+      std::memcpy(coeff + (r0 + rr) * nc, acc.data() + rr * nc, sizeof(R) * nc);
   }
 }
 
@@ -453,6 +495,56 @@ static Tree make_tree(long L, const double* anchor, const int* depth, int q, int
   return t;
 }
 
+template <class R>
+static TreeT<R> make_tree_t(long L, const double* anchor, const int* depth, int q, int dof,
+                            const R* coeff) {
+  TreeT<R> t{L, anchor, depth, q, dof, coeff, {}};
+  t.init();
+  return t;
+}
+
+// One in-situ SL step of a concentration tree through a velocity tree.
+// Restates SolveSemilagInSitu, src/tree/tree_semilag.h:92-135, with
+// SolveSemilagRK2, src/semilag/semilag.inc:26-45.  For dof > 1 the point-major
+// values are transposed to the dof-major layout SetTreeGridValues reads.
+// Only the target nodes of leaves [leaf_begin, leaf_end) are advected and
+// refitted when leaf_end > leaf_begin (bounded CPU samples); coeff_out then
+// holds those leaves only.  coeff_out may alias con_coeff only for a full
+// step.
+template <class R>
+static void semilag_in_situ_T(long Lv, const double* av, const int* dv, int qv, const R* cv,
+                              long Lc, const double* ac, const int* dc, int qc, int dofc,
+                              const R* cc, const double* M, int timestep, double dt, int nrk,
+                              int periodic, long leaf_begin, long leaf_end, R* coeff_out) {
+  TreeT<R> tv = make_tree_t<R>(Lv, av, dv, qv, 3, cv);
+  TreeT<R> tc = make_tree_t<R>(Lc, ac, dc, qc, dofc, cc);
+  if (leaf_end <= leaf_begin) {
+    leaf_begin = 0;
+    leaf_end = Lc;
+  }
+  const long Ls = leaf_end - leaf_begin;
+  TreeT<R> ts = make_tree_t<R>(Ls, ac + 3 * leaf_begin, dc + leaf_begin, qc, dofc, nullptr);
+  const int d = qc + 1;
+  const long np = (long)d * d * d;
+  const size_t N = (size_t)Ls * np;
+  std::vector<Real> pts(N * 3);
+  std::vector<R> x0(N * 3), xdep(N * 3), vals(N * dofc);
+  collect_grid_points(ts, pts.data());
+  for (size_t i = 0; i < N * 3; i++) x0[i] = mk<R>(pts[i]);
+  Real tinit = timestep * dt;
+  Real tfinal = tinit - dt;
+  TreeFunctorT<R> fv{&tv, periodic != 0};
+  traj_rk2<R>(fv, x0.data(), N, tinit, tfinal, nrk, xdep.data());
+  eval_tree(tc, xdep.data(), N, vals.data(), periodic != 0);
+  std::vector<R> vdm(N * dofc);
+  for (long l = 0; l < Ls; l++)
+    for (long p = 0; p < np; p++)
+      for (int k = 0; k < dofc; k++)
+        vdm[((size_t)l * dofc + k) * np + p] = vals[((size_t)l * np + p) * dofc + k];
+  set_tree_grid_values<R>(Ls, dofc, np, (long)d * (d + 1) * (d + 2) / 6, M, vdm.data(),
+                          coeff_out);
+}
+
 extern "C" {
 
 int orc_num_threads(int n) {
@@ -534,30 +626,29 @@ int orc_semilag_in_situ(long Lv, const double* av, const int* dv, int qv, const 
                         long Lc, const double* ac, const int* dc, int qc, int dofc,
                         const double* cc, const double* M, int timestep, double dt, int nrk,
                         int periodic, long leaf_begin, long leaf_end, double* coeff_out) {
-  Tree tv = make_tree(Lv, av, dv, qv, 3, cv);
-  Tree tc = make_tree(Lc, ac, dc, qc, dofc, cc);
-  if (leaf_end <= leaf_begin) {
-    leaf_begin = 0;
-    leaf_end = Lc;
+  semilag_in_situ_T<Real>(Lv, av, dv, qv, cv, Lc, ac, dc, qc, dofc, cc, M, timestep, dt, nrk,
+                          periodic, leaf_begin, leaf_end, coeff_out);
+  return 0;
+}
+
+// The same step on dual numbers: cv_d / cc_d are the directional
+// derivatives of the velocity / concentration coefficients, out_d receives
+// the derivative of the new concentration coefficients (whole tree).
+int orc_semilag_in_situ_dual(long Lv, const double* av, const int* dv, int qv, const double* cv,
+                             const double* cv_d, long Lc, const double* ac, const int* dc, int qc,
+                             const double* cc, const double* cc_d, const double* M, int timestep,
+                             double dt, int nrk, int periodic, double* out, double* out_d) {
+  const long ncv = (long)(qv + 1) * (qv + 2) * (qv + 3) / 6 * 3 * Lv;
+  const long ncc = (long)(qc + 1) * (qc + 2) * (qc + 3) / 6 * Lc;
+  std::vector<Dual> v(ncv), c(ncc), o(ncc);
+  for (long i = 0; i < ncv; i++) v[i] = Dual{cv[i], cv_d[i]};
+  for (long i = 0; i < ncc; i++) c[i] = Dual{cc[i], cc_d[i]};
+  semilag_in_situ_T<Dual>(Lv, av, dv, qv, v.data(), Lc, ac, dc, qc, 1, c.data(), M, timestep, dt,
+                          nrk, periodic, 0, 0, o.data());
+  for (long i = 0; i < ncc; i++) {
+    out[i] = o[i].v;
+    out_d[i] = o[i].d;
   }
-  const long Ls = leaf_end - leaf_begin;
-  Tree ts = make_tree(Ls, ac + 3 * leaf_begin, dc + leaf_begin, qc, dofc, nullptr);
-  const int d = qc + 1;
-  const long np = (long)d * d * d;
-  const size_t N = (size_t)Ls * np;
-  std::vector<Real> pts(N * 3), xdep(N * 3), vals(N * dofc);
-  collect_grid_points(ts, pts.data());
-  Real tinit = timestep * dt;
-  Real tfinal = tinit - dt;
-  TreeFunctor fv{&tv, periodic != 0};
-  traj_rk2(fv, pts.data(), N, tinit, tfinal, nrk, xdep.data());
-  eval_tree(tc, xdep.data(), N, vals.data(), periodic != 0);
-  std::vector<Real> vdm(N * dofc);
-  for (long l = 0; l < Ls; l++)
-    for (long p = 0; p < np; p++)
-      for (int k = 0; k < dofc; k++)
-        vdm[((size_t)l * dofc + k) * np + p] = vals[((size_t)l * np + p) * dofc + k];
-  set_tree_grid_values(Ls, dofc, np, (long)d * (d + 1) * (d + 2) / 6, M, vdm.data(), coeff_out);
   return 0;
 }
 

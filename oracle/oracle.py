@@ -38,6 +38,9 @@ def lib():
     L.orc_semilag_in_situ.argtypes = [i64, _f64p, _i32p, i32, _f64p,
                                       i64, _f64p, _i32p, i32, i32, _f64p,
                                       _f64p, i32, f64, i32, i32, i64, i64, _f64p]
+    L.orc_semilag_in_situ_dual.argtypes = [i64, _f64p, _i32p, i32, _f64p, _f64p,
+                                           i64, _f64p, _i32p, i32, _f64p, _f64p,
+                                           _f64p, i32, f64, i32, i32, _f64p, _f64p]
     L.orc_fast_interp.argtypes = [_f64p, i32, i32, _f64p, i64, _f64p, i32]
     L.orc_semilag_grid.argtypes = [_f64p, _f64p, i32, f64, i32, i32, i64, i64, _f64p]
     return L
@@ -148,6 +151,22 @@ def semilag_in_situ(vel, con, timestep, dt, nrk=1, periodic=False, M=None, leaf_
                               _d(M), int(timestep), float(dt), int(nrk), int(periodic),
                               int(leaf_begin), int(leaf_end), _d(out))
     return out
+
+
+def semilag_in_situ_dual(vel, vel_d, con, con_d, timestep, dt, nrk=1, periodic=False, M=None):
+    """One SL step on forward-mode dual numbers: returns (new coefficients,
+    their derivative along the input direction (vel_d, con_d))."""
+    qc = con["q"]
+    M = pt2coeff(qc) if M is None else _f64(M)
+    av, dv, cv, cvd = (_f64(vel["anchor"]), _i32(vel["depth"]), _f64(vel["coeff"]), _f64(vel_d))
+    ac, dc, cc, ccd = (_f64(con["anchor"]), _i32(con["depth"]), _f64(con["coeff"]), _f64(con_d))
+    out = np.empty((dc.size, 1, n_coeff(qc)))
+    outd = np.empty_like(out)
+    lib().orc_semilag_in_situ_dual(dv.size, _d(av), _i(dv), vel["q"], _d(cv), _d(cvd),
+                                   dc.size, _d(ac), _i(dc), qc, _d(cc), _d(ccd), _d(M),
+                                   int(timestep), float(dt), int(nrk), int(periodic), _d(out),
+                                   _d(outd))
+    return out, outd
 
 
 def fast_interp(grid, dof, nreg, pts, periodic=False):

@@ -1,0 +1,106 @@
+"""Differentiable T-step SL advection: torch.autograd.Function over the
+checkpointed forward step and the hand-written adjoint kernels.
+
+    cT = advect(c0, vcoeff, vel_tree, con_tree, dt, timestep0, nsteps, bc, checkpoint)
+
+c0 [L, 1, Nc] and vcoeff [Lv, 3, Nc] are CUDA float64 tensors (the
+concentration and velocity Chebyshev coefficients); the result is the
+concentration coefficients after nsteps in-situ SL steps (nrk = 1).  Backward
+gives dJ/dc0 and dJ/dvcoeff.  checkpoint=True stores every step's RK2
+midpoints and departure points (48 bytes per node per step); False
+recomputes them in the backward pass.
+"""
+import numpy as np
+
+from . import api
+from .capi import call
+
+
+def basis_at_nodes(q):
+    """V[p][n] = T_i(z_p) T_j(y_p) T_k(x_p) at the leaf's nodes mapped to [-1,1]
+    (the matrix whose pseudo-inverse is the point-to-coefficient matrix):
+    node values of a leaf = coefficients @ V^T."""
+    pts = 2.0 * api.new_nodes(q) - 1.0
+    d = q + 1
+    T = []
+    for a in range(3):
+        x = pts[:, a]
+        t = [np.ones_like(x), x]
+        for k in range(2, d):
+            t.append(2 * x * t[-1] - t[-2])
+        T.append(t[:d])
+    cols = []
+    for i in range(d):
+        for j in range(d - i):
+            for k in range(d - i - j):
+                cols.append(T[2][i] * T[1][j] * T[0][k])
+    return np.stack(cols, axis=1)
+
+
+def step_ckpt(vel_functor, tree, timestep, dt, xmid, xdep, stream=None):
+    call("tbslas_semilag_in_situ_ckpt", tree.ctx.handle, vel_functor.tree.handle, tree.handle,
+         int(timestep), float(dt), vel_functor.bc, api._ptr(xmid), api._ptr(xdep),
+         api._stream(stream))
+
+
+def step_adjoint(vel_functor, tree, coeff_k, timestep, dt, lam_next, lam_k, grad_vel, xmid=None,
+                 xdep=None, stream=None):
+    call("tbslas_semilag_adjoint", tree.ctx.handle, vel_functor.tree.handle, tree.handle,
+         api._ptr(coeff_k), int(timestep), float(dt), vel_functor.bc, api._ptr(lam_next),
+         api._ptr(lam_k), api._ptr(grad_vel), api._ptr(xmid), api._ptr(xdep), api._stream(stream))
+
+
+def _function():
+    import torch
+
+    class SemilagAdvect(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, c0, vcoeff, vel_tree, con_tree, dt, timestep0, nsteps, bc, checkpoint):
+            vel_tree.set_coeffs(vcoeff.contiguous())
+            con_tree.set_coeffs(c0.contiguous())
+            vf = api.NodeFieldFunctor(vel_tree, bc)
+            n = con_tree.n_leaves * api.n_points(con_tree.q)
+            states, ckpts = [], []
+            for k in range(nsteps):
+                states.append(con_tree.get_coeffs(torch.empty_like(c0)))
+                if checkpoint:
+                    xm = torch.empty((n, 3), dtype=torch.float64, device=c0.device)
+                    xd = torch.empty_like(xm)
+                    step_ckpt(vf, con_tree, timestep0 + k, dt, xm, xd)
+                    ckpts.append((xm, xd))
+                else:
+                    api.solve_semilag_in_situ(vf, con_tree, timestep0 + k, dt, 1)
+            cT = con_tree.get_coeffs(torch.empty_like(c0))
+            ctx.vel_tree, ctx.con_tree, ctx.dt, ctx.ts0, ctx.bc = vel_tree, con_tree, dt, timestep0, bc
+            ctx.states, ctx.ckpts, ctx.vshape = states, ckpts, vcoeff.shape
+            ctx.vcoeff = vcoeff
+            return cT
+
+        @staticmethod
+        def backward(ctx, grad_cT):
+            vel_tree, con_tree = ctx.vel_tree, ctx.con_tree
+            vel_tree.set_coeffs(ctx.vcoeff.detach().contiguous())
+            vf = api.NodeFieldFunctor(vel_tree, ctx.bc)
+            lam = grad_cT.contiguous().clone()
+            gv = torch.zeros(ctx.vshape, dtype=torch.float64, device=grad_cT.device)
+            for k in reversed(range(len(ctx.states))):
+                lam_k = torch.empty_like(lam)
+                xm, xd = ctx.ckpts[k] if ctx.ckpts else (None, None)
+                step_adjoint(vf, con_tree, ctx.states[k], ctx.ts0 + k, ctx.dt, lam, lam_k, gv,
+                             xm, xd)
+                lam = lam_k
+            return lam, gv, None, None, None, None, None, None, None
+
+    return SemilagAdvect
+
+
+_FN = None
+
+
+def advect(c0, vcoeff, vel_tree, con_tree, dt, timestep0=1, nsteps=1, bc=api.FreeSpace,
+           checkpoint=True):
+    global _FN
+    if _FN is None:
+        _FN = _function()
+    return _FN.apply(c0, vcoeff, vel_tree, con_tree, float(dt), int(timestep0), int(nsteps),
+                     int(bc), bool(checkpoint))

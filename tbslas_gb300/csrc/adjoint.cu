@@ -1,0 +1,139 @@
+// Entry points of the checkpointed forward step and its adjoint (the
+// differentiation pattern of the SL step; no reference counterpart).
+#include <cmath>
+
+#include "adjoint_kernels.cuh"
+
+namespace tbg {
+
+constexpr int kAdjMaxDegree = 10;
+
+
+struct AdjTable {
+  CkptFn ckpt[kAdjMaxDegree + 1] = {};
+  AdjFn adj[kAdjMaxDegree + 1] = {};
+  AdjTable() {
+    register_adjoint_a(ckpt, adj);
+    register_adjoint_b(ckpt, adj);
+    register_adjoint_c(ckpt, adj);
+  }
+};
+const AdjTable g_adj;
+
+int check_pair(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, double dt, int bc, TreeView* tv,
+               TreeView* tc) {
+  tbslas_ctx cv = nullptr, cc = nullptr;
+  int st = tree_view(vel, tv, &cv);
+  if (st != TBSLAS_OK) return st;
+  st = tree_view(con, tc, &cc);
+  if (st != TBSLAS_OK) return st;
+  if (cv != ctx || cc != ctx) return fail_status(TBSLAS_ERR_INVALID_ARG, "trees of another context");
+  if (tv->dof != 3 || tc->dof != 1 || tv->q != tc->q)
+    return fail_status(TBSLAS_ERR_UNSUPPORTED,
+                       "adjoint step needs a dof-3 velocity and a dof-1 concentration tree of one degree");
+  if (tc->q < 1 || tc->q > kAdjMaxDegree)
+    return fail_status(TBSLAS_ERR_UNSUPPORTED, "adjoint step supports Chebyshev degree 1..10");
+  if (!std::isfinite(dt)) return fail_status(TBSLAS_ERR_INVALID_ARG, "dt is not finite");
+  if (bc != TBSLAS_BC_FREESPACE && bc != TBSLAS_BC_PERIODIC)
+    return fail_status(TBSLAS_ERR_INVALID_ARG, "invalid boundary condition");
+  int dev = 0, sms = 0;
+  st = ctx_info(ctx, &dev, &sms);
+  if (st != TBSLAS_OK) return st;
+  if (cudaSetDevice(dev) != cudaSuccess) return fail_status(TBSLAS_ERR_CUDA, "cudaSetDevice");
+  return TBSLAS_OK;
+}
+
+double step_tau_host(int timestep, double dt) {
+  const double tinit = timestep * dt;
+  const double tfinal = tinit - dt;
+  return (tfinal - tinit) / 1;
+}
+
+int launched(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail_status(TBSLAS_ERR_CUDA, what);
+  return TBSLAS_OK;
+}
+
+}  // namespace tbg
+
+using namespace tbg;
+
+extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                           int timestep, double dt, int bc, double* xmid_dev,
+                                           double* xdep_dev, void* stream) {
+  TreeView tv, tc;
+  int st = check_pair(ctx, vel, con, dt, bc, &tv, &tc);
+  if (st != TBSLAS_OK) return st;
+  if (!xmid_dev || !xdep_dev) return fail_status(TBSLAS_ERR_INVALID_ARG, "null checkpoint buffer");
+  const int q = tc.q, d = q + 1;
+  const int64_t np = (int64_t)d * d * d, nc = (int64_t)d * (d + 1) * (d + 2) / 6;
+  double* vals = nullptr;
+  st = ctx_vals_scratch(ctx, tc.L * np, &vals);
+  if (st != TBSLAS_OK) return st;
+  const double* M = nullptr;
+  st = ctx_M(ctx, q, &M);
+  if (st != TBSLAS_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  CkptArgs a;
+  a.vel = tv;
+  a.con = tc;
+  a.nodes = ctx_nodes(q);
+  a.tau = step_tau_host(timestep, dt);
+  a.periodic = bc;
+  a.vals = vals;
+  a.xmid = xmid_dev;
+  a.xdep = xdep_dev;
+  g_adj.ckpt[q](a, s);
+  st = launched("checkpointed SL step launch");
+  if (st != TBSLAS_OK) return st;
+  double* coeff = nullptr;
+  int64_t ncf = 0;
+  tree_coeff(con, &coeff, &ncf);
+  launch_refit(vals, M, tc.L, (int)np, (int)nc, 1, tc.stride, coeff, s);
+  return launched("refit launch");
+}
+
+extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                      const double* con_coeff_k_dev, int timestep, double dt,
+                                      int bc, const double* lambda_next_dev, double* lambda_k_dev,
+                                      double* grad_vel_dev, const double* xmid_dev,
+                                      const double* xdep_dev, void* stream) {
+  TreeView tv, tc;
+  int st = check_pair(ctx, vel, con, dt, bc, &tv, &tc);
+  if (st != TBSLAS_OK) return st;
+  if (!con_coeff_k_dev || !lambda_next_dev || !lambda_k_dev || !grad_vel_dev)
+    return fail_status(TBSLAS_ERR_INVALID_ARG, "null buffer");
+  if ((xmid_dev == nullptr) != (xdep_dev == nullptr))
+    return fail_status(TBSLAS_ERR_INVALID_ARG, "give both checkpoint buffers or neither");
+  const int q = tc.q, d = q + 1;
+  const int64_t np = (int64_t)d * d * d, nc = (int64_t)d * (d + 1) * (d + 2) / 6;
+  double* mu = nullptr;
+  st = ctx_mu_scratch(ctx, tc.L * np, &mu);
+  if (st != TBSLAS_OK) return st;
+  const double* Mt = nullptr;
+  st = ctx_Mt(ctx, q, &Mt);
+  if (st != TBSLAS_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  // mu = lambda^{k+1} M^T: rows = leaves, K = Nc, N = Np.
+  launch_refit(lambda_next_dev, Mt, tc.L, (int)nc, (int)np, 1, np, mu, s);
+  st = launched("transposed refit launch");
+  if (st != TBSLAS_OK) return st;
+  if (cudaMemsetAsync(lambda_k_dev, 0, sizeof(double) * tc.L * nc, s) != cudaSuccess)
+    return fail_status(TBSLAS_ERR_CUDA, "cudaMemsetAsync");
+  AdjArgs a;
+  a.vel = tv;
+  a.con = tc;
+  a.con.coeff = con_coeff_k_dev;
+  a.con.stride = nc;
+  a.nodes = ctx_nodes(q);
+  a.tau = step_tau_host(timestep, dt);
+  a.periodic = bc;
+  a.mu = mu;
+  a.xmid = xmid_dev;
+  a.xdep = xdep_dev;
+  a.lambda = lambda_k_dev;
+  a.grad_vel = grad_vel_dev;
+  g_adj.adj[q](a, s);
+  return launched("adjoint step launch");
+}

@@ -84,6 +84,7 @@ enum Slot {
   kHostIn,
   kHostIn2,
   kHostOut,
+  kMu,
   kNumSlots
 };
 
@@ -119,6 +120,7 @@ struct tbslas_ctx_s {
   uint32_t* d_err = nullptr;
   DevBuf slots[kNumSlots];
   double* d_M[TBSLAS_MAX_DEGREE + 1] = {};
+  double* d_Mt[TBSLAS_MAX_DEGREE + 1] = {};
   bool profile = false;
   std::vector<ProfRecord> prof_pending;
   std::vector<cudaEvent_t> prof_pool;
@@ -697,6 +699,31 @@ int ctx_M(tbslas_ctx ctx, int q, const double** M) {
   return device_M(ctx, q, M);
 }
 
+// M^T (Nc x Np) on the device, for the transposed refit of the adjoint.
+int ctx_Mt(tbslas_ctx ctx, int q, const double** Mt) {
+  TRY(bind(ctx));
+  if (!ctx->d_Mt[q]) {
+    const std::vector<double>& M = host_M(q);
+    const int64_t np = n_points(q), nc = n_coeff(q);
+    std::vector<double> T(M.size());
+    for (int64_t p = 0; p < np; ++p)
+      for (int64_t n = 0; n < nc; ++n) T[n * np + p] = M[p * nc + n];
+    double* d = nullptr;
+    CUDA_TRY(cudaMalloc(&d, T.size() * sizeof(double)));
+    CUDA_TRY(cudaMemcpy(d, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice));
+    ctx->d_Mt[q] = d;
+  }
+  *Mt = ctx->d_Mt[q];
+  return TBSLAS_OK;
+}
+
+int ctx_mu_scratch(tbslas_ctx ctx, size_t n, double** out) { return scratch_t(ctx, kMu, n, out); }
+int ctx_vals_scratch(tbslas_ctx ctx, size_t n, double** out) {
+  return scratch_t(ctx, kVals, n, out);
+}
+
+Nodes1D ctx_nodes(int q) { return nodes_1d(q); }
+
 }  // namespace tbg
 
 // ===========================================================================
@@ -750,6 +777,8 @@ int tbslas_ctx_destroy(tbslas_ctx ctx) {
   for (auto& b : ctx->slots)
     if (b.p) cudaFree(b.p);
   for (auto p : ctx->d_M)
+    if (p) cudaFree(p);
+  for (auto p : ctx->d_Mt)
     if (p) cudaFree(p);
   prof_collect(ctx);
   for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);

@@ -91,6 +91,10 @@ int tree_view(tbslas_tree t, TreeView* v, tbslas_ctx* ctx);
 int tree_coeff(tbslas_tree t, double** coeff, int64_t* n_doubles);
 int ctx_info(tbslas_ctx ctx, int* device, int* num_sms);
 int ctx_M(tbslas_ctx ctx, int q, const double** M);
+int ctx_Mt(tbslas_ctx ctx, int q, const double** Mt);
+int ctx_mu_scratch(tbslas_ctx ctx, size_t n, double** out);
+int ctx_vals_scratch(tbslas_ctx ctx, size_t n, double** out);
+Nodes1D ctx_nodes(int q);
 
 // Batched refit: one job per problem, one item per 64x64 output tile.
 constexpr int kRefitBM = 64, kRefitBN = 64, kRefitBK = 16;

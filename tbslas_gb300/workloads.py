@@ -176,11 +176,41 @@ class BatchWorkload:
                 "bc": "periodic", "note": self.__doc__.split("\n")[0]}
 
 
+class AdjointWorkload:
+    """Uniform depth-5 octree (32768 leaves), q = 8, stationary Taylor-Green
+    velocity, Gaussian c0 (sigma 0.08 at (0.45, 0.5, 0.5)), 20 SL steps of dt
+    0.004; the observation is the advected field of a seeded perturbed Gaussian;
+    J = 1/2 sum over leaf nodes (c(T) - c_obs)^2."""
+
+    def __init__(self, depth=5, q=8, steps=20, dt=0.004, seed=SEED, name="adjoint_q8"):
+        rng = np.random.default_rng(seed)
+        self.name, self.q, self.steps, self.dt, self.bc = name, q, steps, dt, 0
+        self.a, self.d = trees.uniform_tree(depth)
+        self.vc = trees.fit(fields.taylor_green(), self.a, self.d, q, 3)
+        self.c0 = trees.fit(fields.gaussian((0.45, 0.5, 0.5), 0.08), self.a, self.d, q, 1)
+        shift = rng.uniform(-0.02, 0.02, size=3)
+        self.c0_obs = trees.fit(fields.gaussian((0.45 + shift[0], 0.5 + shift[1], 0.5 + shift[2]),
+                                                0.08 * (1 + rng.uniform(-0.1, 0.1))),
+                                self.a, self.d, q, 1)
+
+    @property
+    def points_per_step(self):
+        return len(self.d) * (self.q + 1) ** 3
+
+    def describe(self):
+        return {"workload": self.name, "q": self.q, "leaves": int(len(self.d)), "steps": self.steps,
+                "dt": self.dt, "bc": "freespace",
+                "departure_points_per_step": int(self.points_per_step),
+                "note": self.__doc__.split("\n")[0]}
+
+
 def make(name):
     if name == "tree_uniform_q8":
         return tree_uniform_q8()
     if name == "tree_adaptive_q14":
         return tree_adaptive_q14()
+    if name == "adjoint_q8":
+        return AdjointWorkload()
     if name == "batched_64":
         return BatchWorkload()
     if name.startswith("grid_periodic_"):

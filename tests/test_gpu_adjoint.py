@@ -1,0 +1,136 @@
+"""Adjoint of the in-situ SL step: the checkpointed forward step reproduces
+the plain step and the oracle's departure points bit for bit; dJ/dc0 and
+dJ/dV from the hand-written adjoint (behind torch.autograd) match central
+finite differences (eps = 1e-6) along seeded random directions to 1e-6
+relative; checkpointing and recomputation give the same gradients."""
+import numpy as np
+import pytest
+
+import tbslas_gb300 as tb
+from tbslas_gb300 import adjoint, fields, trees
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(ctx, q=5, depth=2, seed=3):
+    rng = np.random.default_rng(seed)
+    a, d = trees.uniform_tree(depth)
+    vel_fn = fields.fourier_velocity(rng)
+    vc = trees.fit(lambda p: 0.5 * vel_fn(p), a, d, q, 3)
+    c0 = trees.fit(fields.gaussian((0.5, 0.45, 0.55), 0.12), a, d, q, 1)
+    cobs = trees.fit(fields.gaussian((0.52, 0.47, 0.5), 0.11), a, d, q, 1)
+    tv = tb.Tree(ctx, a, d, q, 3, vc)
+    tc = tb.Tree(ctx, a, d, q, 1, c0)
+    return a, d, q, vc, c0, cobs, tv, tc
+
+
+def test_ckpt_step_matches_plain_step_and_oracle(ctx, ora):
+    import torch
+    a, d, q, vc, c0, _, tv, tc = _problem(ctx)
+    vf = tb.NodeFieldFunctor(tv, tb.Periodic)
+    n = len(d) * (q + 1) ** 3
+    xm = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    xd = torch.empty_like(xm)
+    adjoint.step_ckpt(vf, tc, 1, 0.03, xm, xd)
+    got = tc.get_coeffs()
+    tc.set_coeffs(c0)
+    tb.solve_semilag_in_situ(vf, tc, 1, 0.03)
+    assert np.array_equal(got, tc.get_coeffs())
+    pts = ora.collect_grid_points(a, d, q)
+    ref = ora.traj_rk2(a, d, q, vc, pts, 0.03, 0.0, 1, periodic=True)
+    assert np.array_equal(xd.cpu().numpy(), ref)
+
+
+def _J(c, V, cobs):
+    import torch
+    vals = torch.einsum("ln,pn->lp", c[:, 0, :], V)
+    ovals = torch.einsum("ln,pn->lp", cobs[:, 0, :], V)
+    return 0.5 * ((vals - ovals) ** 2).sum()
+
+
+@pytest.mark.parametrize("checkpoint", [True, False])
+def test_adjoint_matches_central_differences(ctx, checkpoint):
+    import torch
+    a, d, q, vc, c0, cobs, tv, tc = _problem(ctx)
+    V = torch.from_numpy(adjoint.basis_at_nodes(q)).cuda()
+    co = torch.from_numpy(cobs).cuda()
+    c0t = torch.from_numpy(c0).cuda().requires_grad_(True)
+    vct = torch.from_numpy(vc).cuda().requires_grad_(True)
+    dt, steps = 0.03, 3
+    cT = adjoint.advect(c0t, vct, tv, tc, dt, 1, steps, tb.Periodic, checkpoint)
+    J = _J(cT, V, co)
+    J.backward()
+    gc, gv = c0t.grad.clone(), vct.grad.clone()
+
+    def J_at(c, v):
+        with torch.no_grad():
+            return _J(adjoint.advect(c, v, tv, tc, dt, 1, steps, tb.Periodic, False), V, co).item()
+
+    rng = np.random.default_rng(11)
+    eps = 1e-6
+    for _ in range(4):
+        dc = torch.from_numpy(rng.standard_normal(c0.shape)).cuda()
+        fd = (J_at(c0t.detach() + eps * dc, vct.detach()) -
+              J_at(c0t.detach() - eps * dc, vct.detach())) / (2 * eps)
+        an = (gc * dc).sum().item()
+        assert abs(fd - an) <= 1e-6 * abs(an), (fd, an)
+        dv = torch.from_numpy(rng.standard_normal(vc.shape)).cuda()
+        fd = (J_at(c0t.detach(), vct.detach() + eps * dv) -
+              J_at(c0t.detach(), vct.detach() - eps * dv)) / (2 * eps)
+        an = (gv * dv).sum().item()
+        assert abs(fd - an) <= 1e-6 * abs(an), (fd, an)
+
+
+def test_adjoint_checkpoint_equals_recompute(ctx):
+    import torch
+    a, d, q, vc, c0, cobs, tv, tc = _problem(ctx, q=4, seed=5)
+    V = torch.from_numpy(adjoint.basis_at_nodes(q)).cuda()
+    co = torch.from_numpy(cobs).cuda()
+    grads = []
+    for ck in (True, False):
+        c0t = torch.from_numpy(c0).cuda().requires_grad_(True)
+        vct = torch.from_numpy(vc).cuda().requires_grad_(True)
+        _J(adjoint.advect(c0t, vct, tv, tc, 0.02, 1, 4, tb.Periodic, ck), V, co).backward()
+        grads.append((c0t.grad.cpu().numpy(), vct.grad.cpu().numpy()))
+    for x, y in zip(grads[0], grads[1]):
+        assert np.abs(x - y).max() <= 1e-12 * np.abs(y).max()
+
+
+@pytest.mark.parametrize("vel_kind", ["fourier", "taylor_green"])
+def test_adjoint_matches_dual_number_oracle(ctx, ora, vel_kind):
+    """Exact directional derivative of the discrete T-step map (forward-mode
+    dual numbers through the oracle, leaf choices held fixed) against the
+    adjoint's gradient."""
+    import torch
+    q, steps, dt = 4, 3, 0.03
+    a, d = trees.uniform_tree(2)
+    if vel_kind == "fourier":
+        fn = fields.fourier_velocity(np.random.default_rng(3))
+        vc = trees.fit(lambda p: 0.5 * fn(p), a, d, q, 3)
+        bc = tb.Periodic
+    else:
+        vc = trees.fit(fields.taylor_green(), a, d, q, 3)
+        bc = tb.FreeSpace
+    c0 = trees.fit(fields.gaussian((0.5, 0.45, 0.55), 0.12), a, d, q, 1)
+    cobs = trees.fit(fields.gaussian((0.52, 0.47, 0.5), 0.11), a, d, q, 1)
+    tv = tb.Tree(ctx, a, d, q, 3, vc)
+    tc = tb.Tree(ctx, a, d, q, 1, c0)
+    Vb = adjoint.basis_at_nodes(q)
+    c0t = torch.from_numpy(c0).cuda().requires_grad_(True)
+    vct = torch.from_numpy(vc).cuda().requires_grad_(True)
+    J = _J(adjoint.advect(c0t, vct, tv, tc, dt, 1, steps, bc, True),
+           torch.from_numpy(Vb).cuda(), torch.from_numpy(cobs).cuda())
+    J.backward()
+    gc, gv = c0t.grad.cpu().numpy(), vct.grad.cpu().numpy()
+    rng = np.random.default_rng(17)
+    for _ in range(3):
+        dc0, dvc = rng.standard_normal(c0.shape), rng.standard_normal(vc.shape)
+        vel = dict(anchor=a, depth=d, q=q, dof=3, coeff=vc)
+        c, dcur = c0, dc0
+        for s in range(1, steps + 1):
+            c, dcur = ora.semilag_in_situ_dual(vel, dvc, dict(anchor=a, depth=d, q=q, dof=1, coeff=c),
+                                               dcur, s, dt, 1, bc == tb.Periodic)
+        resid = c[:, 0, :] @ Vb.T - cobs[:, 0, :] @ Vb.T
+        dJ = float((resid * (dcur[:, 0, :] @ Vb.T)).sum())
+        an = float((gc * dc0).sum() + (gv * dvc).sum())
+        assert abs(dJ - an) <= 1e-10 * abs(dJ), (dJ, an)
