@@ -562,7 +562,11 @@ def run_adjoint(args, wl, rank, world, local_rank):
             an = (gc * d).sum().item()
             errs_c.append(abs(fd - an) / abs(an))
         else:
-            d = torch.from_numpy(rng.standard_normal(wl.vc.shape)).to(dev)
+            # smooth directions keeping the flow tangent on the Taylor-Green
+            # stagnation planes, which are leaf faces (see the tests)
+            from tbslas_gb300 import fields, trees
+            d = torch.from_numpy(trees.fit(fields.wall_tangent_perturbation(rng), wl.a, wl.d,
+                                           wl.q, 3)).to(dev)
             fd = (J_at(c0, vct + eps * d) - J_at(c0, vct - eps * d)) / (2 * eps)
             an = (gv * d).sum().item()
             errs_v.append(abs(fd - an) / abs(an))
@@ -587,6 +591,8 @@ def run_adjoint(args, wl, rank, world, local_rank):
                           "adj_over_fwd": rc_bms / fwd_ms,
                           "grad_over_fwd": (rc_fms + rc_bms) / fwd_ms, "stored_bytes": 0},
             "fd_check": {"eps": eps, "directions": 16,
+                         "directions_kind": "c0: N(0,1) coefficients; V: smooth random fields "
+                                            "tangent on the stagnation planes",
                          "max_rel_err_dJ_dc0": max(errs_c), "max_rel_err_dJ_dV": max(errs_v)},
             "checkpoint_vs_recompute_rel_diff": ck_gap, "J": res[True][4]}
     print(json.dumps(line))

@@ -64,9 +64,24 @@ __device__ __forceinline__ void cheb_TdT(double xi, double (&T)[D], double (&dT)
   }
 }
 
-// Gradient (d/dxi) of one dof of the triangular expansion.
-template <int D>
-__device__ __forceinline__ void tri_grad(const double* __restrict__ c, const double (&tx)[D],
+// Coefficient loaders for tri_grad: one dof, or sum_a g_a c^a over the three
+// velocity components (the gradient of g . v in one sweep).
+struct OneDof {
+  const double* __restrict__ p;
+  __device__ __forceinline__ double operator()(int i) const { return __ldg(p + i); }
+};
+struct Weighted3 {
+  const double* __restrict__ p;
+  int nc;
+  double g0, g1, g2;
+  __device__ __forceinline__ double operator()(int i) const {
+    return fma(g2, __ldg(p + 2 * nc + i), fma(g1, __ldg(p + nc + i), g0 * __ldg(p + i)));
+  }
+};
+
+// Gradient (d/dxi) of the triangular expansion with coefficients c(idx).
+template <int D, class Load>
+__device__ __forceinline__ void tri_grad(Load c, const double (&tx)[D],
                                          const double (&ty)[D], const double (&tz)[D],
                                          const double (&dx)[D], const double (&dy)[D],
                                          const double (&dz)[D], double (&g)[3]) {
@@ -80,7 +95,7 @@ __device__ __forceinline__ void tri_grad(const double* __restrict__ c, const dou
       double w = 0.0, wd = 0.0;
 #pragma unroll
       for (int k = 0; k < D - i - j; ++k) {
-        const double ck = __ldg(c + idx);
+        const double ck = c(idx);
         w = fma(ck, tx[k], w);
         wd = fma(ck, dx[k], wd);
         ++idx;
@@ -295,7 +310,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const AdjArgs a) {
       cheb_TdT<D>((yd - g.y) * g.w - 1.0, ty, dy);
       cheb_TdT<D>((zd - g.z) * g.w - 1.0, tz, dz);
       double gr[3];
-      tri_grad<D>(a.con.coeff + lf * a.con.stride, tx, ty, tz, dx, dy, dz, gr);
+      tri_grad<D>(OneDof{a.con.coeff + lf * a.con.stride}, tx, ty, tz, dx, dy, dz, gr);
       gvec[0] = mu * gr[0] * g.w;
       gvec[1] = mu * gr[1] * g.w;
       gvec[2] = mu * gr[2] * g.w;
@@ -317,14 +332,13 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const AdjArgs a) {
       cheb_TdT<D>((xs - g.x) * g.w - 1.0, tx, dx);
       cheb_TdT<D>((ys - g.y) * g.w - 1.0, ty, dy);
       cheb_TdT<D>((zs - g.z) * g.w - 1.0, tz, dz);
-#pragma unroll
-      for (int comp = 0; comp < 3; ++comp) {
-        double gr[3];
-        tri_grad<D>(a.vel.coeff + lf * a.vel.stride + comp * NC, tx, ty, tz, dx, dy, dz, gr);
-        jtg[0] = fma(gvec[comp], gr[0] * g.w, jtg[0]);
-        jtg[1] = fma(gvec[comp], gr[1] * g.w, jtg[1]);
-        jtg[2] = fma(gvec[comp], gr[2] * g.w, jtg[2]);
-      }
+      // J_v^T g = grad (g . v) at X*
+      double gr[3];
+      tri_grad<D>(Weighted3{a.vel.coeff + lf * a.vel.stride, NC, gvec[0], gvec[1], gvec[2]}, tx,
+                  ty, tz, dx, dy, dz, gr);
+      jtg[0] = gr[0] * g.w;
+      jtg[1] = gr[1] * g.w;
+      jtg[2] = gr[2] * g.w;
     } else {
 #pragma unroll
       for (int k = 0; k < D; ++k) tx[k] = ty[k] = tz[k] = 0.0;

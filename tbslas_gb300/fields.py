@@ -151,3 +151,26 @@ def periodic_blob_grid(n, centre=(0.5, 0.5, 0.5), sigma=0.1):
     x = np.arange(n) / n
     g = [np.exp(-(x - c) ** 2 / (2 * sigma * sigma)) for c in centre]
     return np.ascontiguousarray(g[2][:, None, None] * g[1][None, :, None] * g[0][None, None, :])
+
+
+def wall_tangent_perturbation(rng, nmodes=4):
+    """Random smooth velocity perturbation whose x-component vanishes on the
+    planes x = 0, 1/2, 1 (likewise y, z): it keeps every plane on which a
+    Taylor-Green-type flow is tangent, so the perturbed flow moves no node
+    across those planes (the SL step is smooth along such directions)."""
+    amp = rng.standard_normal((3, nmodes))
+    kk = rng.integers(1, 4, size=(3, nmodes, 2))
+    ph = rng.uniform(0, 2 * math.pi, size=(3, nmodes, 2))
+
+    def fn(p):
+        p = np.asarray(p).reshape(-1, 3)
+        out = np.zeros((len(p), 3))
+        for a in range(3):
+            o1, o2 = [b for b in range(3) if b != a]
+            g = np.zeros(len(p))
+            for m in range(nmodes):
+                g += amp[a, m] * np.cos(2 * math.pi * kk[a, m, 0] * p[:, o1] + ph[a, m, 0]) * \
+                    np.cos(2 * math.pi * kk[a, m, 1] * p[:, o2] + ph[a, m, 1])
+            out[:, a] = np.sin(2 * math.pi * p[:, a]) * g
+        return out
+    return fn

@@ -211,6 +211,8 @@ def make(name):
         return tree_adaptive_q14()
     if name == "adjoint_q8":
         return AdjointWorkload()
+    if name == "adjoint_q8_d4":
+        return AdjointWorkload(depth=4, steps=4, name=name)
     if name == "batched_64":
         return BatchWorkload()
     if name.startswith("grid_periodic_"):
