@@ -570,6 +570,7 @@ def run_adjoint(args, wl, rank, world, local_rank):
             fd = (J_at(c0, vct + eps * d) - J_at(c0, vct - eps * d)) / (2 * eps)
             an = (gv * d).sum().item()
             errs_v.append(abs(fd - an) / abs(an))
+    dual = dual_check_adjoint(wl, ctx, dev)
     ck_fms, ck_bms = res[True][0], res[True][1]
     rc_fms, rc_bms = res[False][0], res[False][1]
     ck_gap = max(float((res[True][2] - res[False][2]).abs().max() / res[False][2].abs().max()),
@@ -594,9 +595,55 @@ def run_adjoint(args, wl, rank, world, local_rank):
                          "directions_kind": "c0: N(0,1) coefficients; V: smooth random fields "
                                             "tangent on the stagnation planes",
                          "max_rel_err_dJ_dc0": max(errs_c), "max_rel_err_dJ_dV": max(errs_v)},
+            "dual_number_check": dual,
             "checkpoint_vs_recompute_rel_diff": ck_gap, "J": res[True][4]}
     print(json.dumps(line))
     assert ctx.check() == 0
+
+
+def dual_check_adjoint(wl, ctx, dev, depth=3, ndir=2):
+    """Exact check of the adjoint on the same configuration at a reduced tree
+    depth: directional derivative of J through the oracle on forward-mode dual
+    numbers (leaf choices held fixed) vs the adjoint gradient, along seeded
+    N(0,1) directions in (c0, V) jointly."""
+    import torch
+    import tbslas_gb300 as tb
+    from oracle import oracle as ora
+    from tbslas_gb300 import adjoint, workloads
+    small = workloads.AdjointWorkload(depth=depth, q=wl.q, steps=wl.steps, dt=wl.dt)
+    tv = tb.Tree(ctx, small.a, small.d, small.q, 3, small.vc)
+    tc = tb.Tree(ctx, small.a, small.d, small.q, 1, small.c0)
+    Vb = adjoint.basis_at_nodes(small.q)
+    with torch.no_grad():
+        cobs = adjoint.advect(torch.from_numpy(small.c0_obs).to(dev),
+                              torch.from_numpy(small.vc).to(dev), tv, tc, small.dt, 1,
+                              small.steps, small.bc, False).cpu().numpy()
+    c = torch.from_numpy(small.c0).to(dev).requires_grad_(True)
+    v = torch.from_numpy(small.vc).to(dev).requires_grad_(True)
+    cT = adjoint.advect(c, v, tv, tc, small.dt, 1, small.steps, small.bc, True)
+    Vt = torch.from_numpy(Vb).to(dev)
+    J = 0.5 * ((torch.einsum("ln,pn->lp", cT[:, 0, :], Vt) -
+                torch.einsum("ln,pn->lp", torch.from_numpy(cobs).to(dev)[:, 0, :], Vt)) ** 2).sum()
+    J.backward()
+    gc, gv = c.grad.cpu().numpy(), v.grad.cpu().numpy()
+    rng = np.random.default_rng(5)
+    errs = []
+    t0 = time.perf_counter()
+    for _ in range(ndir):
+        dc, dv = rng.standard_normal(small.c0.shape), rng.standard_normal(small.vc.shape)
+        vel = dict(anchor=small.a, depth=small.d, q=small.q, dof=3, coeff=small.vc)
+        cc, dcc = small.c0, dc
+        for s in range(1, small.steps + 1):
+            cc, dcc = ora.semilag_in_situ_dual(
+                vel, dv, dict(anchor=small.a, depth=small.d, q=small.q, dof=1, coeff=cc), dcc,
+                s, small.dt, 1, bool(small.bc))
+        resid = cc[:, 0, :] @ Vb.T - cobs[:, 0, :] @ Vb.T
+        dJ = float((resid * (dcc[:, 0, :] @ Vb.T)).sum())
+        an = float((gc * dc).sum() + (gv * dv).sum())
+        errs.append(abs(dJ - an) / abs(dJ))
+    return {"tree": "uniform depth %d (%d leaves), same q/velocity/steps" % (depth, len(small.d)),
+            "directions": ndir, "max_rel_err": max(errs),
+            "seconds": time.perf_counter() - t0}
 
 
 def _band(q):
