@@ -485,8 +485,7 @@ def run_batched(args, wl, rank, world, local_rank):
             "e2e": {"value": e_points / e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(h2d)},
             "clocks": clk.summary(),
-            "gpu_launches": int(args.steps * (1 + sum(
-                1 for band in range(3) if any(_band(p["q"]) == band for p in wl.problems))))}
+            "gpu_launches": int(args.steps * (1 + 2 * len({_band(p["q"]) for p in wl.problems})))}
     print(json.dumps(line))
     assert ctx.check() == 0
 
@@ -647,7 +646,8 @@ def dual_check_adjoint(wl, ctx, dev, depth=3, ndir=2):
 
 
 def _band(q):
-    return 0 if q <= 8 else (1 if q <= 12 else 2)
+    """Degree band of the batched kernels (band_of in csrc/batch_kernels.cuh)."""
+    return 0 if q <= 8 else (1 if q <= 11 else (2 if q <= 13 else q - 11))
 
 
 def main():

@@ -88,9 +88,11 @@ extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbsl
   st = launched("checkpointed SL step launch");
   if (st != TBSLAS_OK) return st;
   double* coeff = nullptr;
+  float2* coeff2 = nullptr;
   int64_t ncf = 0;
   tree_coeff(con, &coeff, &ncf);
-  launch_refit(vals, M, tc.L, (int)np, (int)nc, 1, tc.stride, coeff, s);
+  tree_coeff2(con, &coeff2);
+  launch_refit(vals, M, tc.L, (int)np, (int)nc, 1, tc.stride, coeff, coeff2, s);
   return launched("refit launch");
 }
 
@@ -116,7 +118,7 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   if (st != TBSLAS_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
   // mu = lambda^{k+1} M^T: rows = leaves, K = Nc, N = Np.
-  launch_refit(lambda_next_dev, Mt, tc.L, (int)nc, (int)np, 1, np, mu, s);
+  launch_refit(lambda_next_dev, Mt, tc.L, (int)nc, (int)np, 1, np, mu, nullptr, s);
   st = launched("transposed refit launch");
   if (st != TBSLAS_OK) return st;
   if (cudaMemsetAsync(lambda_k_dev, 0, sizeof(double) * tc.L * nc, s) != cudaSuccess)

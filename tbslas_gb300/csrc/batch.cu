@@ -44,8 +44,9 @@ struct tbslas_batch_s {
   int64_t n_items = 0, items_cap = 0;
   int64_t band_begin[kBands + 1] = {};
   double* d_vals = nullptr;
-  unsigned long long* d_counters = nullptr;
+  unsigned long long* d_counters = nullptr;  // per step: kBands chunk counters + 1 fix count
   int counters_cap = 0;
+  int64_t* d_fix = nullptr;                  // fix list (total_targets entries)
   int* d_ts0 = nullptr;
   int block = 128, tpi = 256, cps = 4;
   cudaStream_t cap = nullptr;
@@ -105,15 +106,23 @@ int build_items(tbslas_batch b) {
 }
 
 int enqueue_steps(tbslas_batch b, int nsteps, cudaStream_t s) {
-  BCUDA(cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned long long) * nsteps * kBands, s));
+  constexpr int kPer = kBands + 1;
+  BCUDA(cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned long long) * nsteps * kPer, s));
   const int grid = b->num_sms * b->cps;
   for (int i = 0; i < nsteps; ++i) {
+    unsigned long long* fix_count = b->d_counters + (int64_t)i * kPer + kBands;
     for (int band = 0; band < kBands; ++band) {
       const int64_t n = b->band_begin[band + 1] - b->band_begin[band];
       if (n == 0) continue;
       BatchLaunch a{b->d_probs, b->d_items + b->band_begin[band], n,
-                    b->d_counters + (int64_t)i * kBands + band, b->d_ts0, i, b->bc};
-      launch_batch_band(band, a, (int)std::min<int64_t>(grid, n), b->block, s);
+                    b->d_counters + (int64_t)i * kPer + band, b->d_ts0, i, b->bc,
+                    b->d_fix, fix_count};
+      launch_batch_band(band, a, (int)std::min<int64_t>(grid, n), b->block, s, false);
+    }
+    for (int band = 0; band < kBands; ++band) {
+      if (b->band_begin[band + 1] == b->band_begin[band]) continue;
+      BatchLaunch a{b->d_probs, nullptr, 0, nullptr, b->d_ts0, i, b->bc, b->d_fix, fix_count};
+      launch_batch_band(band, a, b->num_sms * 4, 128, s, true);
     }
     launch_batch_refit(b->d_jobs, b->d_ritems, b->n_ritems, s);
   }
@@ -132,7 +141,7 @@ int ensure_counters(tbslas_batch b, int nsteps) {
   if (nsteps > b->counters_cap) {
     if (b->d_counters) BCUDA(cudaFree(b->d_counters));
     b->d_counters = nullptr;
-    BCUDA(cudaMalloc(&b->d_counters, sizeof(unsigned long long) * nsteps * kBands));
+    BCUDA(cudaMalloc(&b->d_counters, sizeof(unsigned long long) * nsteps * (kBands + 1)));
     b->counters_cap = nsteps;
     drop_graph(b);
   }
@@ -239,7 +248,9 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     const double* M = nullptr;
     st = ctx_M(ctx, p.q, &M);
     if (st != TBSLAS_OK) break;
-    jobs.push_back(RefitJob{nullptr, M, coeff, p.con.L, p.con.stride, np, nc, 1, 0});
+    float2* coeff2 = nullptr;
+    tree_coeff2(con[i], &coeff2);
+    jobs.push_back(RefitJob{nullptr, M, coeff, coeff2, p.con.L, p.con.stride, np, nc, 1, 0});
     for (int64_t r = 0; r < (p.con.L + kRefitBM - 1) / kRefitBM; ++r)
       for (int c = 0; c < (nc + kRefitBN - 1) / kRefitBN; ++c)
         ritems.push_back(RefitItem{i, (int32_t)r, c, 0});
@@ -267,6 +278,7 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
                      cudaMemcpyHostToDevice);
     b->n_ritems = (int64_t)ritems.size();
     if (e == cudaSuccess) e = cudaMalloc(&b->d_ts0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_fix, sizeof(int64_t) * std::max<int64_t>(off, 1));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
     if (e != cudaSuccess) st = cuda_fail(e, "batch setup");
     if (st == TBSLAS_OK) st = build_items(b);
@@ -286,7 +298,7 @@ int tbslas_batch_destroy(tbslas_batch b) {
   drop_graph(b);
   if (b->cap) cudaStreamDestroy(b->cap);
   for (void* p : {(void*)b->d_probs, (void*)b->d_jobs, (void*)b->d_ritems, (void*)b->d_items,
-                  (void*)b->d_vals, (void*)b->d_counters, (void*)b->d_ts0})
+                  (void*)b->d_vals, (void*)b->d_counters, (void*)b->d_ts0, (void*)b->d_fix})
     if (p) cudaFree(p);
   delete b;
   return TBSLAS_OK;

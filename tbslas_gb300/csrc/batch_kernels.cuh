@@ -31,11 +31,17 @@ struct BatchLaunch {
   const int* ts0;  // device scalar: first timestep of the run
   int step;        // step index inside the run
   int periodic;
+  int64_t* fix_list;              // (problem << 40 | target) handed to the FP64 pass
+  unsigned long long* fix_count;  // shared by the bands of one step
 };
+constexpr int kFixShift = 40;
 
-// Degree bands: q 1..8, 9..12, 13..16.
-constexpr int kBands = 3;
-__host__ __device__ inline int band_of(int q) { return q <= 8 ? 0 : (q <= 12 ? 1 : 2); }
+// Degree bands, one translation unit each (the unrolled sums of the high
+// degrees dominate compile time): q 1..8, 9..11, 12..13, 14, 15, 16.
+constexpr int kBands = 6;
+__host__ __device__ inline int band_of(int q) {
+  return q <= 8 ? 0 : (q <= 11 ? 1 : (q <= 13 ? 2 : q - 11));
+}
 
 
 
@@ -47,7 +53,56 @@ __device__ __forceinline__ double step_tau(int ts, double dt, int nrk) {
   return __ddiv_rn(__dsub_rn(tfinal, tinit), (double)nrk);
 }
 
-// One target of one problem: the arithmetic of k_semilag_tree<D>.
+// One target of one problem: the arithmetic of k_semilag_tree_df<D>
+// (double-float sums, FP64 coordinates, near-face targets listed for the
+// FP64 pass).
+template <int D>
+__device__ __forceinline__ void batch_target_df(const BatchProblem& p, int64_t t, double tau,
+                                                bool per, const BatchLaunch& a, int prob) {
+  constexpr int NP = D * D * D;
+  const int64_t leaf = t / NP;
+  const int pi = (int)(t - leaf * NP);
+  const Geom g = load_geom(p.con.geom + leaf);
+  const double h = 2.0 / g.w;
+  double x = g.x + h * p.nodes.x[pi % D];
+  double y = g.y + h * p.nodes.x[(pi / D) % D];
+  double z = g.z + h * p.nodes.x[pi / (D * D)];
+  const double half_tau = 0.5 * tau, atau = fabs(tau);
+  double px = x, py = y, pz = z;
+  double m0 = 0.0, mp = 0.0;
+  bool amb = false;
+#pragma unroll 1
+  for (int st = 0; st < 2 * p.nrk; ++st) {
+    double v[3];
+    amb |= eval_point_df<D, 3>(p.vel, px, py, pz, per, mp, v) && mp > 0.0;
+    const double vn = fabs(v[0]) + fabs(v[1]) + fabs(v[2]);
+    const double ev = kDfSumErr * (vn + 1.0) + kDfLipschitz * mp;
+    if ((st & 1) == 0) {
+      x = px;
+      y = py;
+      z = pz;
+      px = fma(half_tau, v[0], x);
+      py = fma(half_tau, v[1], y);
+      pz = fma(half_tau, v[2], z);
+      mp = m0 + 0.5 * atau * ev;
+    } else {
+      x = fma(tau, v[0], x);
+      y = fma(tau, v[1], y);
+      z = fma(tau, v[2], z);
+      px = x;
+      py = y;
+      pz = z;
+      m0 = m0 + atau * ev;
+      mp = m0;
+    }
+  }
+  double c[1];
+  amb |= eval_point_df<D, 1>(p.con, x, y, z, per, m0, c) && m0 > 0.0;
+  p.vals[t] = c[0];
+  if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = ((int64_t)prob << kFixShift) | t;
+}
+
+// One target of one problem in FP64: the arithmetic of k_semilag_tree<D>.
 template <int D>
 __device__ __forceinline__ void batch_target(const BatchProblem& p, int64_t t, double tau,
                                              bool per) {
@@ -67,12 +122,23 @@ __device__ __forceinline__ void batch_target(const BatchProblem& p, int64_t t, d
 
 template <int QLO, int QHI>
 __device__ __forceinline__ void batch_dispatch(int q, const BatchProblem& p, int64_t t, double tau,
-                                               bool per) {
+                                               bool per, const BatchLaunch& a, int prob) {
+  if constexpr (QLO <= QHI) {
+    if (q == QLO)
+      batch_target_df<QLO + 1>(p, t, tau, per, a, prob);
+    else
+      batch_dispatch<QLO + 1, QHI>(q, p, t, tau, per, a, prob);
+  }
+}
+
+template <int QLO, int QHI>
+__device__ __forceinline__ void batch_dispatch_fp64(int q, const BatchProblem& p, int64_t t,
+                                                    double tau, bool per) {
   if constexpr (QLO <= QHI) {
     if (q == QLO)
       batch_target<QLO + 1>(p, t, tau, per);
     else
-      batch_dispatch<QLO + 1, QHI>(q, p, t, tau, per);
+      batch_dispatch_fp64<QLO + 1, QHI>(q, p, t, tau, per);
   }
 }
 
@@ -95,21 +161,46 @@ __global__ void __launch_bounds__(256) k_batch_semilag(const BatchLaunch a) {
     const double tau = step_tau(ts, sp.dt, sp.nrk);
     const int q = sp.q;
     for (int k = threadIdx.x; k < w.count; k += blockDim.x)
-      batch_dispatch<QLO, QHI>(q, sp, w.start + k, tau, per);
+      batch_dispatch<QLO, QHI>(q, sp, w.start + k, tau, per, a, w.problem);
     __syncthreads();  // s_item and sp are rewritten for the next chunk
+  }
+}
+
+// FP64 pass over the listed targets whose problem's degree is in this band.
+template <int QLO, int QHI>
+__global__ void __launch_bounds__(128) k_batch_fix(const BatchLaunch a) {
+  const bool per = a.periodic != 0;
+  const int ts = *a.ts0 + a.step;
+  const int64_t n = (int64_t)*a.fix_count;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = a.fix_list[i];
+    const int prob = (int)(e >> kFixShift);
+    const int64_t t = e & ((1ll << kFixShift) - 1);
+    const BatchProblem& p = a.probs[prob];
+    if (p.q < QLO || p.q > QHI) continue;
+    batch_dispatch_fp64<QLO, QHI>(p.q, p, t, step_tau(ts, p.dt, p.nrk), per);
   }
 }
 
 }  // namespace tbg
 
 namespace tbg {
-void launch_batch_band_0(const BatchLaunch& a, int grid, int block, cudaStream_t s);
-void launch_batch_band_1(const BatchLaunch& a, int grid, int block, cudaStream_t s);
-void launch_batch_band_2(const BatchLaunch& a, int grid, int block, cudaStream_t s);
+void launch_batch_band_0(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
+void launch_batch_band_1(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
+void launch_batch_band_2(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
+void launch_batch_band_3(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
+void launch_batch_band_4(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
+void launch_batch_band_5(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
 inline void launch_batch_band(int band, const BatchLaunch& a, int grid, int block,
-                              cudaStream_t s) {
-  if (band == 0) launch_batch_band_0(a, grid, block, s);
-  else if (band == 1) launch_batch_band_1(a, grid, block, s);
-  else launch_batch_band_2(a, grid, block, s);
+                              cudaStream_t s, bool fix) {
+  switch (band) {
+    case 0: launch_batch_band_0(a, grid, block, s, fix); break;
+    case 1: launch_batch_band_1(a, grid, block, s, fix); break;
+    case 2: launch_batch_band_2(a, grid, block, s, fix); break;
+    case 3: launch_batch_band_3(a, grid, block, s, fix); break;
+    case 4: launch_batch_band_4(a, grid, block, s, fix); break;
+    default: launch_batch_band_5(a, grid, block, s, fix); break;
+  }
 }
 }  // namespace tbg

@@ -85,6 +85,8 @@ enum Slot {
   kHostIn2,
   kHostOut,
   kMu,
+  kFixList,
+  kFixCount,
   kNumSlots
 };
 
@@ -135,6 +137,7 @@ struct tbslas_tree_s {
   uint64_t* d_keys = nullptr;
   Geom* d_geom = nullptr;
   double* d_coeff = nullptr;
+  float2* d_coeff2 = nullptr;  // double-float split of d_coeff, kept in sync
   int32_t* d_table = nullptr;
 
   TreeView view() const {
@@ -142,6 +145,7 @@ struct tbslas_tree_s {
     v.keys = d_keys;
     v.geom = d_geom;
     v.coeff = d_coeff;
+    v.coeff2 = d_coeff2;
     v.table = d_table;
     v.L = L;
     v.stride = stride;
@@ -492,7 +496,7 @@ int refit_dev(tbslas_ctx ctx, tbslas_tree tree, const double* vals, cudaStream_t
   TRY(device_M(ctx, tree->q, &M));
   ProfScope p(ctx, "refit", s);
   launch_refit(vals, M, tree->L * tree->dof, (int)n_points(tree->q), (int)n_coeff(tree->q),
-               tree->dof, tree->stride, tree->d_coeff, s);
+               tree->dof, tree->stride, tree->d_coeff, tree->d_coeff2, s);
   return check_launch("refit");
 }
 
@@ -533,8 +537,11 @@ int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int ti
     a.nrk = nrk;
     a.periodic = bc;
     a.vals = vals;
-    ProfScope p(ctx, "semilag_tree", s);
-    g_kernels[con->q].semilag(a, s);
+    TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
+    TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
+    a.fix_grid = ctx->num_sms * 8;
+    ProfScope p(ctx, "semilag_tree", s, 3);
+    g_kernels[con->q].semilag_df(a, s);
     TRY(check_launch("semilag_tree"));
   } else {
     double *X, *Xdep, *vt;
@@ -606,6 +613,8 @@ int build_tree(tbslas_tree t, const double* anchor, const int32_t* depth) {
   CUDA_TRY(cudaMalloc(&t->d_geom, L * sizeof(Geom)));
   CUDA_TRY(cudaMalloc(&t->d_table, (ncell + 1) * sizeof(int32_t)));
   CUDA_TRY(cudaMalloc(&t->d_coeff, L * t->stride * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&t->d_coeff2, L * t->stride * sizeof(float2)));
+  CUDA_TRY(cudaMemset(t->d_coeff2, 0, L * t->stride * sizeof(float2)));
   CUDA_TRY(cudaMemcpy(t->d_keys, keys.data(), L * sizeof(uint64_t), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(t->d_geom, geom.data(), L * sizeof(Geom), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(t->d_table, table.data(), (ncell + 1) * sizeof(int32_t),
@@ -618,10 +627,12 @@ int copy_coeffs(tbslas_tree t, double* dst, const double* src, bool to_tree, cud
                 cudaStream_t s) {
   const size_t w = (size_t)t->dof * n_coeff(t->q) * sizeof(double);
   const size_t pitch = (size_t)t->stride * sizeof(double);
-  if (to_tree)
+  if (to_tree) {
     CUDA_TRY(cudaMemcpy2DAsync(dst, pitch, src, w, w, t->L, kind, s));
-  else
-    CUDA_TRY(cudaMemcpy2DAsync(dst, w, src, pitch, w, t->L, kind, s));
+    launch_split(t->d_coeff, t->d_coeff2, t->L * t->stride, s);
+    return check_launch("split");
+  }
+  CUDA_TRY(cudaMemcpy2DAsync(dst, w, src, pitch, w, t->L, kind, s));
   return TBSLAS_OK;
 }
 
@@ -677,6 +688,12 @@ int tree_view(tbslas_tree t, TreeView* v, tbslas_ctx* ctx) {
   if (!t || !t->ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null tree");
   *v = t->view();
   *ctx = t->ctx;
+  return TBSLAS_OK;
+}
+
+int tree_coeff2(tbslas_tree t, float2** coeff2) {
+  if (!t || !t->ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null tree");
+  *coeff2 = t->d_coeff2;
   return TBSLAS_OK;
 }
 
@@ -908,6 +925,7 @@ int tbslas_tree_destroy(tbslas_tree t) {
   if (t->d_keys) cudaFree(t->d_keys);
   if (t->d_geom) cudaFree(t->d_geom);
   if (t->d_coeff) cudaFree(t->d_coeff);
+  if (t->d_coeff2) cudaFree(t->d_coeff2);
   if (t->d_table) cudaFree(t->d_table);
   delete t;
   return TBSLAS_OK;

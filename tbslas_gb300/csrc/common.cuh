@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "df64.cuh"
 #include "tbslas_gb300.h"
 
 namespace tbg {
@@ -71,6 +72,7 @@ struct TreeView {
   const uint64_t* __restrict__ keys;   // [L] anchor keys, strictly increasing
   const Geom* __restrict__ geom;       // [L]
   const double* __restrict__ coeff;    // [L * stride]
+  const float2* __restrict__ coeff2;   // [L * stride] the same, split hi + lo
   const int32_t* __restrict__ table;   // [8^T + 1] coarse-cell -> first leaf
   int64_t L;
   int64_t stride;  // doubles per leaf (dof*Nc rounded up to an even count)
@@ -171,6 +173,51 @@ __device__ __forceinline__ void eval_point(const TreeView& t, double& x, double&
   const double* c = t.coeff + leaf * t.stride;
 #pragma unroll
   for (int l = 0; l < DOF; ++l) out[l] = tri_sum<D>(GlobalLoad{c + l * NC}, tx, ty, tz);
+}
+
+// Double-float evaluation of DOF components at one point, for the fused
+// step.  Returns true when the lookup is ambiguous: the point lies within
+// `margin` (a physical distance bounding the difference between this
+// point and the one an all-FP64 computation would have produced) of a face of
+// its leaf, or just outside the domain -- then the caller recomputes the
+// point in FP64 so that leaf choices always agree with the FP64 path.
+template <int D, int DOF>
+__device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, double& y, double& z,
+                                              bool periodic, double margin, double (&out)[DOF]) {
+  constexpr int NC = D * (D + 1) * (D + 2) / 6;
+  if (periodic) {
+    x = wrap1(x);
+    y = wrap1(y);
+    z = wrap1(z);
+  }
+  if (!inside(x, y, z, periodic)) {
+#pragma unroll
+    for (int l = 0; l < DOF; ++l) out[l] = 0.0;
+    const double lo = -margin, hi = 1.0 + margin;
+    return x >= lo && x <= hi && y >= lo && y <= hi && z >= lo && z <= hi;
+  }
+  const uint64_t key = morton3(quantise(x), quantise(y), quantise(z));
+  const int64_t leaf = find_leaf(t, key);
+  const Geom g = load_geom(t.geom + leaf);
+  const double xi = (x - g.x) * g.w - 1.0, yi = (y - g.y) * g.w - 1.0, zi = (z - g.z) * g.w - 1.0;
+  const double edge = 1.0 - margin * g.w;
+  const bool amb = fabs(xi) >= edge || fabs(yi) >= edge || fabs(zi) >= edge;
+  double T[D];
+  df tx[D], ty[D], tz[D];
+  cheb_T<D>(xi, T);
+#pragma unroll
+  for (int k = 0; k < D; ++k) tx[k] = df_from_double(T[k]);
+  cheb_T<D>(yi, T);
+#pragma unroll
+  for (int k = 0; k < D; ++k) ty[k] = df_from_double(T[k]);
+  cheb_T<D>(zi, T);
+#pragma unroll
+  for (int k = 0; k < D; ++k) tz[k] = df_from_double(T[k]);
+  const float2* c = t.coeff2 + leaf * t.stride;
+#pragma unroll
+  for (int l = 0; l < DOF; ++l)
+    out[l] = df_to_double(tri_sum_df<D>(GlobalLoadDF{c + l * NC}, tx, ty, tz));
+  return amb;
 }
 
 // 1-D Chebyshev nodes on [0,1] (new_nodes, src/utils/cheb.h:50-58) passed by

@@ -25,6 +25,9 @@ struct SemilagTreeArgs {
   int nrk;
   int periodic;
   double* vals;       // [Lc * Np] node values at the departure points
+  int64_t* fix_list;  // targets the double-float kernel hands to the FP64 pass
+  unsigned long long* fix_count;
+  int fix_grid;       // CTAs of the FP64 pass (persistent)
 };
 
 struct TrajArgs {
@@ -66,7 +69,8 @@ typedef void (*TrajFn)(const TrajArgs&, cudaStream_t);
 typedef void (*EvalTilesFn)(const EvalTilesArgs&, cudaStream_t);
 
 struct DegreeKernels {
-  SemilagTreeFn semilag = nullptr;
+  SemilagTreeFn semilag = nullptr;     // FP64 fused step
+  SemilagTreeFn semilag_df = nullptr;  // double-float fused step + FP64 pass over near-face targets
   TrajFn traj = nullptr;
   EvalTilesFn eval_tiles = nullptr;
   int eval_tiles_max_threads_hint = 0;
@@ -89,6 +93,7 @@ int bucketed_eval_on(const BucketScratch& b, tbslas_tree tree, const double* pos
 int fail_status(int code, const char* msg);
 int tree_view(tbslas_tree t, TreeView* v, tbslas_ctx* ctx);
 int tree_coeff(tbslas_tree t, double** coeff, int64_t* n_doubles);
+int tree_coeff2(tbslas_tree t, float2** coeff2);
 int ctx_info(tbslas_ctx ctx, int* device, int* num_sms);
 int ctx_M(tbslas_ctx ctx, int q, const double** M);
 int ctx_Mt(tbslas_ctx ctx, int q, const double** Mt);
@@ -102,6 +107,7 @@ struct RefitJob {
   const double* vals;
   const double* M;
   double* coeff;
+  float2* coeff2;
   int64_t rows;
   int64_t stride;
   int np, nc, dof, pad;
@@ -114,7 +120,8 @@ void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_
 
 // refit.cu: coeff[(r/dof)*stride + (r%dof)*nc + n] = sum_p vals[r*np+p] M[p*nc+n]
 void launch_refit(const double* vals, const double* M, int64_t rows, int np, int nc, int dof,
-                  int64_t stride, double* coeff, cudaStream_t s);
+                  int64_t stride, double* coeff, float2* coeff2, cudaStream_t s);
+void launch_split(const double* c, float2* c2, int64_t n, cudaStream_t s);
 
 // misc kernels (capi.cu)
 void launch_collect(const TreeView& t, const Nodes1D& nodes, double* out, cudaStream_t s);

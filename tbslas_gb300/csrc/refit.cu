@@ -14,7 +14,7 @@ namespace tbg {
 __device__ __forceinline__ void refit_tile(const double* __restrict__ V,
                                            const double* __restrict__ M, int64_t rows, int np,
                                            int nc, int dof, int64_t stride, double* __restrict__ C,
-                                           int64_t row0, int col0) {
+                                           float2* __restrict__ C2, int64_t row0, int col0) {
   __shared__ double As[kRefitBK][kRefitBM];
   __shared__ double Bs[kRefitBK][kRefitBN];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -59,11 +59,17 @@ __device__ __forceinline__ void refit_tile(const double* __restrict__ V,
     if (row >= rows) continue;
     const int64_t leaf = row / dof;
     const int l = (int)(row - leaf * dof);
-    double* out = C + leaf * stride + (int64_t)l * nc;
+    const int64_t base = leaf * stride + (int64_t)l * nc;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int col = col0 + tx + 16 * j;
-      if (col < nc) out[col] = acc[i][j];
+      if (col < nc) {
+        C[base + col] = acc[i][j];
+        if (C2) {
+          const df v = df_from_double(acc[i][j]);
+          C2[base + col] = make_float2(v.hi, v.lo);
+        }
+      }
     }
   }
 }
@@ -71,8 +77,8 @@ __device__ __forceinline__ void refit_tile(const double* __restrict__ V,
 __global__ void __launch_bounds__(256) k_refit(const double* __restrict__ V,
                                                const double* __restrict__ M, int64_t rows,
                                                int np, int nc, int dof, int64_t stride,
-                                               double* __restrict__ C) {
-  refit_tile(V, M, rows, np, nc, dof, stride, C, (int64_t)blockIdx.x * kRefitBM,
+                                               double* __restrict__ C, float2* __restrict__ C2) {
+  refit_tile(V, M, rows, np, nc, dof, stride, C, C2, (int64_t)blockIdx.x * kRefitBM,
              blockIdx.y * kRefitBN);
 }
 
@@ -81,7 +87,7 @@ __global__ void __launch_bounds__(256) k_batch_refit(const RefitJob* __restrict_
                                                      const RefitItem* __restrict__ items) {
   const RefitItem it = items[blockIdx.x];
   const RefitJob j = jobs[it.job];
-  refit_tile(j.vals, j.M, j.rows, j.np, j.nc, j.dof, j.stride, j.coeff,
+  refit_tile(j.vals, j.M, j.rows, j.np, j.nc, j.dof, j.stride, j.coeff, j.coeff2,
              (int64_t)it.row_tile * kRefitBM, it.col_tile * kRefitBN);
 }
 
@@ -91,10 +97,23 @@ void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_
 }
 
 void launch_refit(const double* vals, const double* M, int64_t rows, int np, int nc, int dof,
-                  int64_t stride, double* coeff, cudaStream_t s) {
+                  int64_t stride, double* coeff, float2* coeff2, cudaStream_t s) {
   if (rows <= 0) return;
   dim3 grid((unsigned)((rows + kRefitBM - 1) / kRefitBM), (unsigned)((nc + kRefitBN - 1) / kRefitBN));
-  k_refit<<<grid, 256, 0, s>>>(vals, M, rows, np, nc, dof, stride, coeff);
+  k_refit<<<grid, 256, 0, s>>>(vals, M, rows, np, nc, dof, stride, coeff, coeff2);
+}
+
+// Split FP64 coefficients into their double-float form.
+__global__ void k_split(const double* __restrict__ c, float2* __restrict__ c2, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) {
+    const df v = df_from_double(c[i]);
+    c2[i] = make_float2(v.hi, v.lo);
+  }
+}
+
+void launch_split(const double* c, float2* c2, int64_t n, cudaStream_t s) {
+  if (n > 0) k_split<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c, c2, n);
 }
 
 }  // namespace tbg

@@ -128,6 +128,102 @@ void launch_semilag_tree(const SemilagTreeArgs& a, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
+// The fused step with the Chebyshev sums in double-float (df64.cuh) and
+// everything else -- targets, T_k recurrences, RK2 updates, Morton keys, leaf
+// search, local coordinates -- in FP64.  Each position carries a bound on its
+// distance from the all-FP64 position (sum-error bound 1e-12 (|v| + 1) per
+// evaluation, Lipschitz constant 1e3 for the dependence of v on the
+// position); a target whose midpoint or departure point falls within that
+// bound of a face of its leaf is appended to fix_list and recomputed by
+// k_semilag_fix with the FP64 kernel body, so every leaf choice is the FP64
+// path's.  Values differ from the FP64 path by the sums' rounding (~1e-14).
+constexpr double kDfSumErr = 1e-12;
+constexpr double kDfLipschitz = 1e3;
+
+template <int D>
+__global__ void __launch_bounds__(128) k_semilag_tree_df(const SemilagTreeArgs a) {
+  constexpr int NP = D * D * D;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= a.con.L * NP) return;
+  const int64_t leaf = t / NP;
+  const int p = (int)(t - leaf * NP);
+  const Geom g = load_geom(a.con.geom + leaf);
+  const double h = 2.0 / g.w;
+  double x = g.x + h * a.nodes.x[p % D];
+  double y = g.y + h * a.nodes.x[(p / D) % D];
+  double z = g.z + h * a.nodes.x[p / (D * D)];
+  const bool per = a.periodic != 0;
+  const double half_tau = 0.5 * a.tau, atau = fabs(a.tau);
+  double px = x, py = y, pz = z;
+  double m0 = 0.0, mp = 0.0;  // bounds at the sub-step start and at the point being evaluated
+  bool amb = false;
+#pragma unroll 1
+  for (int st = 0; st < 2 * a.nrk; ++st) {
+    double v[3];
+    amb |= eval_point_df<D, 3>(a.vel, px, py, pz, per, mp, v) && mp > 0.0;
+    const double vn = fabs(v[0]) + fabs(v[1]) + fabs(v[2]);
+    const double ev = kDfSumErr * (vn + 1.0) + kDfLipschitz * mp;
+    if ((st & 1) == 0) {
+      x = px;
+      y = py;
+      z = pz;
+      px = fma(half_tau, v[0], x);
+      py = fma(half_tau, v[1], y);
+      pz = fma(half_tau, v[2], z);
+      mp = m0 + 0.5 * atau * ev;
+    } else {
+      x = fma(a.tau, v[0], x);
+      y = fma(a.tau, v[1], y);
+      z = fma(a.tau, v[2], z);
+      px = x;
+      py = y;
+      pz = z;
+      m0 = m0 + atau * ev;
+      mp = m0;
+    }
+  }
+  double c[1];
+  amb |= eval_point_df<D, 1>(a.con, x, y, z, per, m0, c) && m0 > 0.0;
+  a.vals[t] = c[0];
+  if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = t;
+}
+
+// FP64 recomputation of the listed targets (the body of k_semilag_tree).
+template <int D>
+__global__ void __launch_bounds__(128) k_semilag_fix(const SemilagTreeArgs a) {
+  constexpr int NP = D * D * D;
+  const int64_t n = (int64_t)*a.fix_count;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = a.fix_list[i];
+    const int64_t leaf = t / NP;
+    const int p = (int)(t - leaf * NP);
+    const Geom g = load_geom(a.con.geom + leaf);
+    const double h = 2.0 / g.w;
+    double x = g.x + h * a.nodes.x[p % D];
+    double y = g.y + h * a.nodes.x[(p / D) % D];
+    double z = g.z + h * a.nodes.x[p / (D * D)];
+    const bool per = a.periodic != 0;
+    rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
+    double c[1];
+    eval_point<D, 1>(a.con, x, y, z, per, c);
+    a.vals[t] = c[0];
+  }
+}
+
+template <int D>
+void launch_semilag_tree_df(const SemilagTreeArgs& a, cudaStream_t s) {
+  constexpr int NP = D * D * D;
+  const int64_t n = a.con.L * NP;
+  const int threads = 128;
+  const int64_t blocks = (n + threads - 1) / threads;
+  if (blocks == 0) return;
+  cudaMemsetAsync(a.fix_count, 0, sizeof(unsigned long long), s);
+  k_semilag_tree_df<D><<<(unsigned)blocks, threads, 0, s>>>(a);
+  k_semilag_fix<D><<<a.fix_grid, threads, 0, s>>>(a);
+}
+
+// ---------------------------------------------------------------------------
 // RK2 backtrace of arbitrary points (ComputeTrajRK2, traj.inc:48-68), one
 // thread per point, direct leaf lookup per stage.
 template <int D>
@@ -221,6 +317,7 @@ void launch_eval_tiles(const EvalTilesArgs& a, cudaStream_t s) {
 template <int D>
 void register_degree(DegreeKernels* table) {
   table[D - 1].semilag = &launch_semilag_tree<D>;
+  table[D - 1].semilag_df = &launch_semilag_tree_df<D>;
   table[D - 1].traj = &launch_traj<D>;
   table[D - 1].eval_tiles = &launch_eval_tiles<D>;
 }

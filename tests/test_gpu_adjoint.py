@@ -1,5 +1,6 @@
-"""Adjoint of the in-situ SL step: the checkpointed forward step reproduces
-the plain step and the oracle's departure points bit for bit; dJ/dc0 and
+"""Adjoint of the in-situ SL step: the checkpointed (all-FP64) forward step
+reproduces the oracle's departure points bit for bit and the plain step to
+1e-12; dJ/dc0 and
 dJ/dV from the hand-written adjoint (behind torch.autograd) match central
 finite differences (eps = 1e-6) along seeded random directions to 1e-6
 relative; checkpointing and recomputation give the same gradients."""
@@ -34,8 +35,9 @@ def test_ckpt_step_matches_plain_step_and_oracle(ctx, ora):
     adjoint.step_ckpt(vf, tc, 1, 0.03, xm, xd)
     got = tc.get_coeffs()
     tc.set_coeffs(c0)
-    tb.solve_semilag_in_situ(vf, tc, 1, 0.03)
-    assert np.array_equal(got, tc.get_coeffs())
+    tb.solve_semilag_in_situ(vf, tc, 1, 0.03)  # double-float sums: equal to ~1e-14
+    ref_c = tc.get_coeffs()
+    assert np.abs(got - ref_c).max() <= 1e-12 * np.abs(ref_c).max()
     pts = ora.collect_grid_points(a, d, q)
     ref = ora.traj_rk2(a, d, q, vc, pts, 0.03, 0.0, 1, periodic=True)
     assert np.array_equal(xd.cpu().numpy(), ref)
