@@ -35,6 +35,7 @@ struct tbslas_batch_s {
   int n = 0, nrk = 1, bc = 0;
   std::vector<BatchProblem> h_probs;
   std::vector<double*> con_coeff;
+  std::vector<float2*> con_coeff2;
   std::vector<int64_t> con_coeff_n;
   BatchProblem* d_probs = nullptr;
   RefitJob* d_jobs = nullptr;
@@ -245,6 +246,11 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     tree_coeff(con[i], &coeff, &ncf);
     b->con_coeff.push_back(coeff);
     b->con_coeff_n.push_back(ncf);
+    {
+      float2* c2 = nullptr;
+      tree_coeff2(con[i], &c2);
+      b->con_coeff2.push_back(c2);
+    }
     const double* M = nullptr;
     st = ctx_M(ctx, p.q, &M);
     if (st != TBSLAS_OK) break;
@@ -362,6 +368,7 @@ int tbslas_batch_autotune(tbslas_batch b, int* block, int* targets_per_item, int
                            : cudaMemcpyAsync(b->con_coeff[i], backup + o, bytes,
                                              cudaMemcpyDeviceToDevice, s);
       if (e != cudaSuccess) return e;
+      if (!save) launch_split(b->con_coeff[i], b->con_coeff2[i], b->con_coeff_n[i], s);
       o += b->con_coeff_n[i];
     }
     return cudaSuccess;

@@ -67,37 +67,32 @@ __device__ __forceinline__ void batch_target_df(const BatchProblem& p, int64_t t
   double x = g.x + h * p.nodes.x[pi % D];
   double y = g.y + h * p.nodes.x[(pi / D) % D];
   double z = g.z + h * p.nodes.x[pi / (D * D)];
-  const double half_tau = 0.5 * tau, atau = fabs(tau);
-  double px = x, py = y, pz = z;
-  double m0 = 0.0, mp = 0.0;
+  const double half_tau = 0.5 * tau;
+  double xx[3] = {x, y, z};
+  double px[3] = {x, y, z};
+  double m0[3] = {0.0, 0.0, 0.0}, mp[3] = {0.0, 0.0, 0.0};
   bool amb = false;
 #pragma unroll 1
   for (int st = 0; st < 2 * p.nrk; ++st) {
-    double v[3];
-    amb |= eval_point_df<D, 3>(p.vel, px, py, pz, per, mp, v) && mp > 0.0;
-    const double vn = fabs(v[0]) + fabs(v[1]) + fabs(v[2]);
-    const double ev = kDfSumErr * (vn + 1.0) + kDfLipschitz * mp;
+    double v[3], ev[3];
+    amb |= eval_point_df<D, 3, true>(p.vel, px[0], px[1], px[2], per, mp, v, ev);
     if ((st & 1) == 0) {
-      x = px;
-      y = py;
-      z = pz;
-      px = fma(half_tau, v[0], x);
-      py = fma(half_tau, v[1], y);
-      pz = fma(half_tau, v[2], z);
-      mp = m0 + 0.5 * atau * ev;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        xx[k] = px[k];
+        df_update(half_tau, v[k], ev[k], xx[k], m0[k], px[k], mp[k]);
+      }
     } else {
-      x = fma(tau, v[0], x);
-      y = fma(tau, v[1], y);
-      z = fma(tau, v[2], z);
-      px = x;
-      py = y;
-      pz = z;
-      m0 = m0 + atau * ev;
-      mp = m0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        df_update(tau, v[k], ev[k], xx[k], m0[k], xx[k], m0[k]);
+        px[k] = xx[k];
+        mp[k] = m0[k];
+      }
     }
   }
-  double c[1];
-  amb |= eval_point_df<D, 1>(p.con, x, y, z, per, m0, c) && m0 > 0.0;
+  double c[1], ce[1];
+  amb |= eval_point_df<D, 1, false>(p.con, xx[0], xx[1], xx[2], per, m0, c, ce);
   p.vals[t] = c[0];
   if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = ((int64_t)prob << kFixShift) | t;
 }

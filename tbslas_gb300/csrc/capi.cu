@@ -138,6 +138,7 @@ struct tbslas_tree_s {
   Geom* d_geom = nullptr;
   double* d_coeff = nullptr;
   float2* d_coeff2 = nullptr;  // double-float split of d_coeff, kept in sync
+  double* d_cnorm = nullptr;   // [L * dof] sum |c| per leaf and component, kept in sync
   int32_t* d_table = nullptr;
 
   TreeView view() const {
@@ -146,6 +147,7 @@ struct tbslas_tree_s {
     v.geom = d_geom;
     v.coeff = d_coeff;
     v.coeff2 = d_coeff2;
+    v.cnorm = d_cnorm;
     v.table = d_table;
     v.L = L;
     v.stride = stride;
@@ -427,6 +429,19 @@ __global__ void __launch_bounds__(256) k_fp64_fma(double* out, double b, double 
   out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+// Per leaf and component: sum of |c| (bounds the double-float sums' error).
+__global__ void k_cnorm(const double* __restrict__ c, int64_t L, int dof, int nc, int64_t stride,
+                        double* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= L * dof) return;
+  const int64_t leaf = i / dof;
+  const int l = (int)(i - leaf * dof);
+  const double* p = c + leaf * stride + (int64_t)l * nc;
+  double s = 0.0;
+  for (int n = 0; n < nc; ++n) s += fabs(p[n]);
+  out[i] = s;
+}
+
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 // The bucketed tree functor on device buffers.
@@ -494,10 +509,17 @@ int traj_dev(tbslas_ctx ctx, tbslas_tree vel, const double* x, int64_t n, double
 int refit_dev(tbslas_ctx ctx, tbslas_tree tree, const double* vals, cudaStream_t s) {
   const double* M = nullptr;
   TRY(device_M(ctx, tree->q, &M));
-  ProfScope p(ctx, "refit", s);
+  ProfScope p(ctx, "refit", s, tree->dof == 3 ? 2 : 1);
   launch_refit(vals, M, tree->L * tree->dof, (int)n_points(tree->q), (int)n_coeff(tree->q),
                tree->dof, tree->stride, tree->d_coeff, tree->d_coeff2, s);
-  return check_launch("refit");
+  TRY(check_launch("refit"));
+  if (tree->dof == 3) {  // a velocity-shaped tree: its norms feed the double-float bounds
+    k_cnorm<<<blocks_for(tree->L * 3, 128), 128, 0, s>>>(tree->d_coeff, tree->L, 3,
+                                                         (int)n_coeff(tree->q), tree->stride,
+                                                         tree->d_cnorm);
+    return check_launch("norms");
+  }
+  return TBSLAS_OK;
 }
 
 int collect_dev(tbslas_tree tree, double* out, cudaStream_t s) {
@@ -540,7 +562,7 @@ int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int ti
     TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
     TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
     a.fix_grid = ctx->num_sms * 8;
-    ProfScope p(ctx, "semilag_tree", s, 3);
+    ProfScope p(ctx, "semilag_tree", s, 2);
     g_kernels[con->q].semilag_df(a, s);
     TRY(check_launch("semilag_tree"));
   } else {
@@ -615,6 +637,8 @@ int build_tree(tbslas_tree t, const double* anchor, const int32_t* depth) {
   CUDA_TRY(cudaMalloc(&t->d_coeff, L * t->stride * sizeof(double)));
   CUDA_TRY(cudaMalloc(&t->d_coeff2, L * t->stride * sizeof(float2)));
   CUDA_TRY(cudaMemset(t->d_coeff2, 0, L * t->stride * sizeof(float2)));
+  CUDA_TRY(cudaMalloc(&t->d_cnorm, L * t->dof * sizeof(double)));
+  CUDA_TRY(cudaMemset(t->d_cnorm, 0, L * t->dof * sizeof(double)));
   CUDA_TRY(cudaMemcpy(t->d_keys, keys.data(), L * sizeof(uint64_t), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(t->d_geom, geom.data(), L * sizeof(Geom), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(t->d_table, table.data(), (ncell + 1) * sizeof(int32_t),
@@ -623,14 +647,23 @@ int build_tree(tbslas_tree t, const double* anchor, const int32_t* depth) {
   return TBSLAS_OK;
 }
 
+// Refresh what is derived from a tree's coefficients: the double-float split
+// and the per-leaf coefficient norms.
+int derived_coeffs(tbslas_tree t, cudaStream_t s) {
+  launch_split(t->d_coeff, t->d_coeff2, t->L * t->stride, s);
+  const int64_t n = t->L * t->dof;
+  k_cnorm<<<blocks_for(n, 128), 128, 0, s>>>(t->d_coeff, t->L, t->dof, (int)n_coeff(t->q),
+                                             t->stride, t->d_cnorm);
+  return check_launch("coefficient split / norms");
+}
+
 int copy_coeffs(tbslas_tree t, double* dst, const double* src, bool to_tree, cudaMemcpyKind kind,
                 cudaStream_t s) {
   const size_t w = (size_t)t->dof * n_coeff(t->q) * sizeof(double);
   const size_t pitch = (size_t)t->stride * sizeof(double);
   if (to_tree) {
     CUDA_TRY(cudaMemcpy2DAsync(dst, pitch, src, w, w, t->L, kind, s));
-    launch_split(t->d_coeff, t->d_coeff2, t->L * t->stride, s);
-    return check_launch("split");
+    return derived_coeffs(t, s);
   }
   CUDA_TRY(cudaMemcpy2DAsync(dst, w, src, pitch, w, t->L, kind, s));
   return TBSLAS_OK;
@@ -926,6 +959,7 @@ int tbslas_tree_destroy(tbslas_tree t) {
   if (t->d_geom) cudaFree(t->d_geom);
   if (t->d_coeff) cudaFree(t->d_coeff);
   if (t->d_coeff2) cudaFree(t->d_coeff2);
+  if (t->d_cnorm) cudaFree(t->d_cnorm);
   if (t->d_table) cudaFree(t->d_table);
   delete t;
   return TBSLAS_OK;

@@ -73,6 +73,7 @@ struct TreeView {
   const Geom* __restrict__ geom;       // [L]
   const double* __restrict__ coeff;    // [L * stride]
   const float2* __restrict__ coeff2;   // [L * stride] the same, split hi + lo
+  const double* __restrict__ cnorm;    // [L * dof] sum of |c| per leaf and component
   const int32_t* __restrict__ table;   // [8^T + 1] coarse-cell -> first leaf
   int64_t L;
   int64_t stride;  // doubles per leaf (dof*Nc rounded up to an even count)
@@ -176,32 +177,40 @@ __device__ __forceinline__ void eval_point(const TreeView& t, double& x, double&
 }
 
 // Double-float evaluation of DOF components at one point, for the fused
-// step.  Returns true when the lookup is ambiguous: the point lies within
-// `margin` (a physical distance bounding the difference between this
-// point and the one an all-FP64 computation would have produced) of a face of
-// its leaf, or just outside the domain -- then the caller recomputes the
-// point in FP64 so that leaf choices always agree with the FP64 path.
-template <int D, int DOF>
+// step.  m[a] bounds, per axis, the distance between this point and the one
+// an all-FP64 computation would have produced (0: identical).  Returns true
+// when the lookup is ambiguous -- within m[a] of a face of the leaf on some
+// axis, or just outside the domain -- so the caller must recompute the target
+// in FP64.  With ERR, err[l] receives a bound on |out[l] - out_fp64[l]|: the
+// sums' rounding (1e-13 sum|c|, |T_k| <= 1) plus the change of the expansion
+// over the position uncertainty (|dT_k/dxi| <= k^2 on [-1,1]).
+constexpr double kDfSumErr = 1e-13;
+
+template <int D, int DOF, bool ERR>
 __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, double& y, double& z,
-                                              bool periodic, double margin, double (&out)[DOF]) {
+                                              bool periodic, const double (&m)[3],
+                                              double (&out)[DOF], double (&err)[DOF]) {
   constexpr int NC = D * (D + 1) * (D + 2) / 6;
   if (periodic) {
     x = wrap1(x);
     y = wrap1(y);
     z = wrap1(z);
   }
+  const double mmax = fmax(m[0], fmax(m[1], m[2]));
   if (!inside(x, y, z, periodic)) {
 #pragma unroll
-    for (int l = 0; l < DOF; ++l) out[l] = 0.0;
-    const double lo = -margin, hi = 1.0 + margin;
-    return x >= lo && x <= hi && y >= lo && y <= hi && z >= lo && z <= hi;
+    for (int l = 0; l < DOF; ++l) out[l] = err[l] = 0.0;
+    if (mmax == 0.0) return false;
+    return x >= -m[0] && x <= 1.0 + m[0] && y >= -m[1] && y <= 1.0 + m[1] && z >= -m[2] &&
+           z <= 1.0 + m[2];
   }
   const uint64_t key = morton3(quantise(x), quantise(y), quantise(z));
   const int64_t leaf = find_leaf(t, key);
   const Geom g = load_geom(t.geom + leaf);
   const double xi = (x - g.x) * g.w - 1.0, yi = (y - g.y) * g.w - 1.0, zi = (z - g.z) * g.w - 1.0;
-  const double edge = 1.0 - margin * g.w;
-  const bool amb = fabs(xi) >= edge || fabs(yi) >= edge || fabs(zi) >= edge;
+  const bool amb = (m[0] > 0.0 && fabs(xi) >= 1.0 - m[0] * g.w) ||
+                   (m[1] > 0.0 && fabs(yi) >= 1.0 - m[1] * g.w) ||
+                   (m[2] > 0.0 && fabs(zi) >= 1.0 - m[2] * g.w);
   double T[D];
   df tx[D], ty[D], tz[D];
   cheb_T<D>(xi, T);
@@ -215,9 +224,29 @@ __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, doub
   for (int k = 0; k < D; ++k) tz[k] = df_from_double(T[k]);
   const float2* c = t.coeff2 + leaf * t.stride;
 #pragma unroll
-  for (int l = 0; l < DOF; ++l)
+  for (int l = 0; l < DOF; ++l) {
     out[l] = df_to_double(tri_sum_df<D>(GlobalLoadDF{c + l * NC}, tx, ty, tz));
+    if (ERR) {
+      const double cn = __ldg(t.cnorm + leaf * DOF + l);
+      err[l] = cn * (kDfSumErr + (double)((D - 1) * (D - 1)) * g.w * mmax);
+    }
+  }
   return amb;
+}
+
+// Position update p = x + s*v of one axis in the double-float step, with its
+// uncertainty: mx bounds x's distance from the FP64 path, ev bounds v's.  When
+// x is exact and the whole step (plus its uncertainty) is below half an ulp
+// of x, both paths round back to x exactly and the result stays exact.
+__device__ __forceinline__ void df_update(double s, double v, double ev, double x, double mx,
+                                          double& p, double& mp) {
+  p = fma(s, v, x);
+  const double step = fabs(s) * (fabs(v) + ev);
+  if (mx == 0.0 && p == x && step < fabs(x) * 0x1p-54) {
+    mp = 0.0;
+  } else {
+    mp = mx + fabs(s) * ev;
+  }
 }
 
 // 1-D Chebyshev nodes on [0,1] (new_nodes, src/utils/cheb.h:50-58) passed by

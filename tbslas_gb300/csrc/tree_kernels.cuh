@@ -130,16 +130,12 @@ void launch_semilag_tree(const SemilagTreeArgs& a, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // The fused step with the Chebyshev sums in double-float (df64.cuh) and
 // everything else -- targets, T_k recurrences, RK2 updates, Morton keys, leaf
-// search, local coordinates -- in FP64.  Each position carries a bound on its
-// distance from the all-FP64 position (sum-error bound 1e-12 (|v| + 1) per
-// evaluation, Lipschitz constant 1e3 for the dependence of v on the
-// position); a target whose midpoint or departure point falls within that
-// bound of a face of its leaf is appended to fix_list and recomputed by
-// k_semilag_fix with the FP64 kernel body, so every leaf choice is the FP64
-// path's.  Values differ from the FP64 path by the sums' rounding (~1e-14).
-constexpr double kDfSumErr = 1e-12;
-constexpr double kDfLipschitz = 1e3;
-
+// search, local coordinates -- in FP64.  Each coordinate carries a bound on
+// its distance from the all-FP64 coordinate (eval_point_df / df_update); a
+// target whose midpoint or departure point falls within that bound of a face
+// of its leaf is appended to fix_list and recomputed by k_semilag_fix with
+// the FP64 kernel body, so every leaf choice is the FP64 path's.  Values
+// differ from the FP64 path by the sums' rounding (~1e-14).
 template <int D>
 __global__ void __launch_bounds__(128) k_semilag_tree_df(const SemilagTreeArgs a) {
   constexpr int NP = D * D * D;
@@ -149,41 +145,34 @@ __global__ void __launch_bounds__(128) k_semilag_tree_df(const SemilagTreeArgs a
   const int p = (int)(t - leaf * NP);
   const Geom g = load_geom(a.con.geom + leaf);
   const double h = 2.0 / g.w;
-  double x = g.x + h * a.nodes.x[p % D];
-  double y = g.y + h * a.nodes.x[(p / D) % D];
-  double z = g.z + h * a.nodes.x[p / (D * D)];
+  double x[3] = {g.x + h * a.nodes.x[p % D], g.y + h * a.nodes.x[(p / D) % D],
+                 g.z + h * a.nodes.x[p / (D * D)]};
   const bool per = a.periodic != 0;
-  const double half_tau = 0.5 * a.tau, atau = fabs(a.tau);
-  double px = x, py = y, pz = z;
-  double m0 = 0.0, mp = 0.0;  // bounds at the sub-step start and at the point being evaluated
+  const double half_tau = 0.5 * a.tau;
+  double px[3] = {x[0], x[1], x[2]};
+  double m0[3] = {0.0, 0.0, 0.0}, mp[3] = {0.0, 0.0, 0.0};
   bool amb = false;
 #pragma unroll 1
   for (int st = 0; st < 2 * a.nrk; ++st) {
-    double v[3];
-    amb |= eval_point_df<D, 3>(a.vel, px, py, pz, per, mp, v) && mp > 0.0;
-    const double vn = fabs(v[0]) + fabs(v[1]) + fabs(v[2]);
-    const double ev = kDfSumErr * (vn + 1.0) + kDfLipschitz * mp;
+    double v[3], ev[3];
+    amb |= eval_point_df<D, 3, true>(a.vel, px[0], px[1], px[2], per, mp, v, ev);
     if ((st & 1) == 0) {
-      x = px;
-      y = py;
-      z = pz;
-      px = fma(half_tau, v[0], x);
-      py = fma(half_tau, v[1], y);
-      pz = fma(half_tau, v[2], z);
-      mp = m0 + 0.5 * atau * ev;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        x[k] = px[k];
+        df_update(half_tau, v[k], ev[k], x[k], m0[k], px[k], mp[k]);
+      }
     } else {
-      x = fma(a.tau, v[0], x);
-      y = fma(a.tau, v[1], y);
-      z = fma(a.tau, v[2], z);
-      px = x;
-      py = y;
-      pz = z;
-      m0 = m0 + atau * ev;
-      mp = m0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        df_update(a.tau, v[k], ev[k], x[k], m0[k], x[k], m0[k]);
+        px[k] = x[k];
+        mp[k] = m0[k];
+      }
     }
   }
-  double c[1];
-  amb |= eval_point_df<D, 1>(a.con, x, y, z, per, m0, c) && m0 > 0.0;
+  double c[1], ce[1];
+  amb |= eval_point_df<D, 1, false>(a.con, x[0], x[1], x[2], per, m0, c, ce);
   a.vals[t] = c[0];
   if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = t;
 }
