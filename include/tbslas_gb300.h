@@ -98,6 +98,10 @@ int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launch
  * roofline denominator of the FP64-pipe-bound kernels.  Diagnostic; no
  * reference counterpart. */
 int tbslas_fp64_fma_peak(tbslas_ctx ctx, double* flops_per_s);
+/* Measured FP32 FMA throughput (FLOP/s, 2 per FMA): the denominator of the
+ * double-float sums, which run on the FP32 pipe.  Diagnostic; no reference
+ * counterpart. */
+int tbslas_fp32_fma_peak(tbslas_ctx ctx, double* flops_per_s);
 
 /* ---- Chebyshev helpers (host) ---------------------------------------------- */
 /* new_nodes(q,3): (q+1)^3 x 3 nodes in [0,1], x fastest.

@@ -114,6 +114,12 @@ class Context:
         call("tbslas_fp64_fma_peak", self.handle, ctypes.byref(f))
         return f.value
 
+    def fp32_fma_peak(self):
+        """Measured FP32 FMA throughput, FLOP/s."""
+        f = ctypes.c_double(0)
+        call("tbslas_fp32_fma_peak", self.handle, ctypes.byref(f))
+        return f.value
+
     def check(self):
         """Synchronise and return the device error word (raises if non-zero)."""
         w = ctypes.c_uint32(0)

@@ -71,8 +71,8 @@ extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbsl
   double* vals = nullptr;
   st = ctx_vals_scratch(ctx, tc.L * np, &vals);
   if (st != TBSLAS_OK) return st;
-  const double* M = nullptr;
-  st = ctx_M(ctx, q, &M);
+  const double* F = nullptr;
+  st = ctx_F(ctx, q, &F);
   if (st != TBSLAS_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
   CkptArgs a;
@@ -92,7 +92,7 @@ extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbsl
   int64_t ncf = 0;
   tree_coeff(con, &coeff, &ncf);
   tree_coeff2(con, &coeff2);
-  launch_refit(vals, M, tc.L, (int)np, (int)nc, 1, tc.stride, coeff, coeff2, s);
+  launch_refit(vals, F, q, tc.L, 1, tc.stride, coeff, coeff2, s);
   return launched("refit launch");
 }
 
@@ -113,12 +113,12 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   double* mu = nullptr;
   st = ctx_mu_scratch(ctx, tc.L * np, &mu);
   if (st != TBSLAS_OK) return st;
-  const double* Mt = nullptr;
-  st = ctx_Mt(ctx, q, &Mt);
+  const double* F = nullptr;
+  st = ctx_F(ctx, q, &F);
   if (st != TBSLAS_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  // mu = lambda^{k+1} M^T: rows = leaves, K = Nc, N = Np.
-  launch_refit(lambda_next_dev, Mt, tc.L, (int)nc, (int)np, 1, np, mu, nullptr, s);
+  // mu = lambda^{k+1} M^T, one row of Np node weights per leaf
+  launch_refit_t(lambda_next_dev, F, q, tc.L, mu, s);
   st = launched("transposed refit launch");
   if (st != TBSLAS_OK) return st;
   if (cudaMemsetAsync(lambda_k_dev, 0, sizeof(double) * tc.L * nc, s) != cudaSuccess)

@@ -41,6 +41,7 @@ struct tbslas_batch_s {
   RefitJob* d_jobs = nullptr;
   RefitItem* d_ritems = nullptr;
   int64_t n_ritems = 0;
+  int max_q = 0;
   BatchItem* d_items = nullptr;
   int64_t n_items = 0, items_cap = 0;
   int64_t band_begin[kBands + 1] = {};
@@ -125,7 +126,7 @@ int enqueue_steps(tbslas_batch b, int nsteps, cudaStream_t s) {
       BatchLaunch a{b->d_probs, nullptr, 0, nullptr, b->d_ts0, i, b->bc, b->d_fix, fix_count};
       launch_batch_band(band, a, b->num_sms * 4, 128, s, true);
     }
-    launch_batch_refit(b->d_jobs, b->d_ritems, b->n_ritems, s);
+    launch_batch_refit(b->d_jobs, b->d_ritems, b->n_ritems, b->max_q, s);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch step launch");
@@ -251,15 +252,14 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
       tree_coeff2(con[i], &c2);
       b->con_coeff2.push_back(c2);
     }
-    const double* M = nullptr;
-    st = ctx_M(ctx, p.q, &M);
+    const double* F = nullptr;
+    st = ctx_F(ctx, p.q, &F);
     if (st != TBSLAS_OK) break;
     float2* coeff2 = nullptr;
     tree_coeff2(con[i], &coeff2);
-    jobs.push_back(RefitJob{nullptr, M, coeff, coeff2, p.con.L, p.con.stride, np, nc, 1, 0});
-    for (int64_t r = 0; r < (p.con.L + kRefitBM - 1) / kRefitBM; ++r)
-      for (int c = 0; c < (nc + kRefitBN - 1) / kRefitBN; ++c)
-        ritems.push_back(RefitItem{i, (int32_t)r, c, 0});
+    jobs.push_back(RefitJob{nullptr, F, coeff, coeff2, p.con.L, p.con.stride, p.q, 1});
+    b->max_q = std::max(b->max_q, p.q);
+    for (int64_t r = 0; r < p.con.L; ++r) ritems.push_back(RefitItem{i, 0, r});
   }
   cudaError_t e = cudaSuccess;
   if (st == TBSLAS_OK) {

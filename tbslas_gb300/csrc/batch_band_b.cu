@@ -3,9 +3,6 @@
 
 namespace tbg {
 void launch_batch_band_1(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix) {
-  if (fix)
-    k_batch_fix<9, 11><<<grid, 128, 0, s>>>(a);
-  else
-    k_batch_semilag<9, 11><<<grid, block, 0, s>>>(a);
+  launch_band<9, 11>(a, grid, block, s, fix);
 }
 }  // namespace tbg

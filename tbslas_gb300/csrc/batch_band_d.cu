@@ -3,9 +3,6 @@
 
 namespace tbg {
 void launch_batch_band_3(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix) {
-  if (fix)
-    k_batch_fix<14, 14><<<grid, 128, 0, s>>>(a);
-  else
-    k_batch_semilag<14, 14><<<grid, block, 0, s>>>(a);
+  launch_band<14, 14>(a, grid, block, s, fix);
 }
 }  // namespace tbg

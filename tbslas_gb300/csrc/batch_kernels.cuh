@@ -2,6 +2,8 @@
 // batch_band_*.cu translation units (so the bands compile in parallel).
 #pragma once
 
+#include <atomic>
+
 #include "tree_kernels.cuh"
 
 namespace tbg {
@@ -58,7 +60,8 @@ __device__ __forceinline__ double step_tau(int ts, double dt, int nrk) {
 // FP64 pass).
 template <int D>
 __device__ __forceinline__ void batch_target_df(const BatchProblem& p, int64_t t, double tau,
-                                                bool per, const BatchLaunch& a, int prob) {
+                                                bool per, const BatchLaunch& a, int prob,
+                                                ThreadSlots slots) {
   constexpr int NP = D * D * D;
   const int64_t leaf = t / NP;
   const int pi = (int)(t - leaf * NP);
@@ -75,7 +78,7 @@ __device__ __forceinline__ void batch_target_df(const BatchProblem& p, int64_t t
 #pragma unroll 1
   for (int st = 0; st < 2 * p.nrk; ++st) {
     double v[3], ev[3];
-    amb |= eval_point_df<D, 3, true>(p.vel, px[0], px[1], px[2], per, mp, v, ev);
+    amb |= eval_point_df<D, 3, true>(p.vel, px[0], px[1], px[2], per, mp, v, ev, slots);
     if ((st & 1) == 0) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -92,7 +95,7 @@ __device__ __forceinline__ void batch_target_df(const BatchProblem& p, int64_t t
     }
   }
   double c[1], ce[1];
-  amb |= eval_point_df<D, 1, false>(p.con, xx[0], xx[1], xx[2], per, m0, c, ce);
+  amb |= eval_point_df<D, 1, false>(p.con, xx[0], xx[1], xx[2], per, m0, c, ce, slots);
   p.vals[t] = c[0];
   if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = ((int64_t)prob << kFixShift) | t;
 }
@@ -117,12 +120,13 @@ __device__ __forceinline__ void batch_target(const BatchProblem& p, int64_t t, d
 
 template <int QLO, int QHI>
 __device__ __forceinline__ void batch_dispatch(int q, const BatchProblem& p, int64_t t, double tau,
-                                               bool per, const BatchLaunch& a, int prob) {
+                                               bool per, const BatchLaunch& a, int prob,
+                                               ThreadSlots slots) {
   if constexpr (QLO <= QHI) {
     if (q == QLO)
-      batch_target_df<QLO + 1>(p, t, tau, per, a, prob);
+      batch_target_df<QLO + 1>(p, t, tau, per, a, prob, slots);
     else
-      batch_dispatch<QLO + 1, QHI>(q, p, t, tau, per, a, prob);
+      batch_dispatch<QLO + 1, QHI>(q, p, t, tau, per, a, prob, slots);
   }
 }
 
@@ -143,6 +147,8 @@ template <int QLO, int QHI>
 __global__ void __launch_bounds__(256) k_batch_semilag(const BatchLaunch a) {
   __shared__ BatchProblem sp;
   __shared__ int64_t s_item;
+  extern __shared__ float2 s_slots[];  // 2 * (QHI + 1) elements per thread
+  const ThreadSlots slots{s_slots + threadIdx.x, (int)blockDim.x};
   const bool per = a.periodic != 0;
   const int ts = *a.ts0 + a.step;
   for (;;) {
@@ -156,7 +162,7 @@ __global__ void __launch_bounds__(256) k_batch_semilag(const BatchLaunch a) {
     const double tau = step_tau(ts, sp.dt, sp.nrk);
     const int q = sp.q;
     for (int k = threadIdx.x; k < w.count; k += blockDim.x)
-      batch_dispatch<QLO, QHI>(q, sp, w.start + k, tau, per, a, w.problem);
+      batch_dispatch<QLO, QHI>(q, sp, w.start + k, tau, per, a, w.problem, slots);
     __syncthreads();  // s_item and sp are rewritten for the next chunk
   }
 }
@@ -176,6 +182,30 @@ __global__ void __launch_bounds__(128) k_batch_fix(const BatchLaunch a) {
     if (p.q < QLO || p.q > QHI) continue;
     batch_dispatch_fp64<QLO, QHI>(p.q, p, t, step_tau(ts, p.dt, p.nrk), per);
   }
+}
+
+// Launch of one band: the step kernel with 2 * (QHI + 1) shared-memory
+// elements per thread (its dynamic shared-memory limit raised once per
+// device: with the static descriptor, 48 KB of slots already exceeds the
+// default), or the FP64 pass.
+template <int QLO, int QHI>
+void launch_band(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix) {
+  if (fix) {
+    k_batch_fix<QLO, QHI><<<grid, 128, 0, s>>>(a);
+    return;
+  }
+  constexpr size_t kMaxSmem = 2 * (size_t)(QHI + 1) * 256 * sizeof(float2);
+  const size_t smem = 2 * (size_t)(QHI + 1) * block * sizeof(float2);
+  static std::atomic<uint64_t> done{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t bit = 1ull << (dev & 63);
+  if (!(done.load() & bit)) {
+    cudaFuncSetAttribute(k_batch_semilag<QLO, QHI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kMaxSmem);
+    done.fetch_or(bit);
+  }
+  k_batch_semilag<QLO, QHI><<<grid, block, smem, s>>>(a);
 }
 
 }  // namespace tbg

@@ -121,8 +121,7 @@ struct tbslas_ctx_s {
   cudaStream_t stream = nullptr;  // used by the synchronous *_host entry points
   uint32_t* d_err = nullptr;
   DevBuf slots[kNumSlots];
-  double* d_M[TBSLAS_MAX_DEGREE + 1] = {};
-  double* d_Mt[TBSLAS_MAX_DEGREE + 1] = {};
+  double* d_F[TBSLAS_MAX_DEGREE + 1] = {};  // separable refit factors per degree
   bool profile = false;
   std::vector<ProfRecord> prof_pending;
   std::vector<cudaEvent_t> prof_pool;
@@ -251,15 +250,15 @@ int scratch_t(tbslas_ctx ctx, Slot s, size_t count, T** out) {
   return TBSLAS_OK;
 }
 
-int device_M(tbslas_ctx ctx, int q, const double** out) {
-  if (!ctx->d_M[q]) {
-    const std::vector<double>& M = host_M(q);
+int device_F(tbslas_ctx ctx, int q, const double** out) {
+  if (!ctx->d_F[q]) {
+    const std::vector<double> F = refit_factors(q);
     double* d = nullptr;
-    CUDA_TRY(cudaMalloc(&d, M.size() * sizeof(double)));
-    CUDA_TRY(cudaMemcpy(d, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice));
-    ctx->d_M[q] = d;
+    CUDA_TRY(cudaMalloc(&d, F.size() * sizeof(double)));
+    CUDA_TRY(cudaMemcpy(d, F.data(), F.size() * sizeof(double), cudaMemcpyHostToDevice));
+    ctx->d_F[q] = d;
   }
-  *out = ctx->d_M[q];
+  *out = ctx->d_F[q];
   return TBSLAS_OK;
 }
 
@@ -408,11 +407,13 @@ __global__ void k_point_to_dof_major(const double* __restrict__ in, int64_t L, i
   out[(leaf * dof + l) * np + p] = in[i];
 }
 
-// FP64 FMA throughput probe: 8 independent dependency chains per thread,
-// 64 FMAs per iteration; one store per thread.
-__global__ void __launch_bounds__(256) k_fp64_fma(double* out, double b, double c, int iters) {
-  double a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5,
-         a6 = a0 + 6, a7 = a0 + 7;
+// FMA throughput probe (T = double: FP64 pipe, T = float: FP32 pipe): 8
+// independent dependency chains per thread, 64 FMAs per iteration; one store
+// per thread.
+template <class T>
+__global__ void __launch_bounds__(256) k_fma_probe(T* out, T b, T c, int iters) {
+  T a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5,
+    a6 = a0 + 6, a7 = a0 + 7;
   for (int i = 0; i < iters; ++i) {
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -507,11 +508,11 @@ int traj_dev(tbslas_ctx ctx, tbslas_tree vel, const double* x, int64_t n, double
 }
 
 int refit_dev(tbslas_ctx ctx, tbslas_tree tree, const double* vals, cudaStream_t s) {
-  const double* M = nullptr;
-  TRY(device_M(ctx, tree->q, &M));
+  const double* F = nullptr;
+  TRY(device_F(ctx, tree->q, &F));
   ProfScope p(ctx, "refit", s, tree->dof == 3 ? 2 : 1);
-  launch_refit(vals, M, tree->L * tree->dof, (int)n_points(tree->q), (int)n_coeff(tree->q),
-               tree->dof, tree->stride, tree->d_coeff, tree->d_coeff2, s);
+  launch_refit(vals, F, tree->q, tree->L * tree->dof, tree->dof, tree->stride, tree->d_coeff,
+               tree->d_coeff2, s);
   TRY(check_launch("refit"));
   if (tree->dof == 3) {  // a velocity-shaped tree: its norms feed the double-float bounds
     k_cnorm<<<blocks_for(tree->L * 3, 128), 128, 0, s>>>(tree->d_coeff, tree->L, 3,
@@ -669,6 +670,31 @@ int copy_coeffs(tbslas_tree t, double* dst, const double* src, bool to_tree, cud
   return TBSLAS_OK;
 }
 
+template <class T>
+int fma_peak(tbslas_ctx ctx, int iters, double* flops_per_s) {
+  TRY(bind(ctx));
+  if (!flops_per_s) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
+  const int blocks = ctx->num_sms * 8, threads = 256;
+  double* out;
+  TRY(scratch_t(ctx, kHostOut, (size_t)blocks * threads, &out));
+  T* o = reinterpret_cast<T*>(out);
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  k_fma_probe<T><<<blocks, threads, 0, ctx->stream>>>(o, T(1), T(0), 10);
+  cudaEventRecord(e0, ctx->stream);
+  k_fma_probe<T><<<blocks, threads, 0, ctx->stream>>>(o, T(1), T(0), iters);
+  cudaEventRecord(e1, ctx->stream);
+  CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  TRY(check_launch("fma_probe"));
+  *flops_per_s = 2.0 * 64.0 * iters * (double)blocks * threads / (ms * 1e-3);
+  return TBSLAS_OK;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -744,27 +770,9 @@ int ctx_info(tbslas_ctx ctx, int* device, int* num_sms) {
   return TBSLAS_OK;
 }
 
-int ctx_M(tbslas_ctx ctx, int q, const double** M) {
+int ctx_F(tbslas_ctx ctx, int q, const double** F) {
   TRY(bind(ctx));
-  return device_M(ctx, q, M);
-}
-
-// M^T (Nc x Np) on the device, for the transposed refit of the adjoint.
-int ctx_Mt(tbslas_ctx ctx, int q, const double** Mt) {
-  TRY(bind(ctx));
-  if (!ctx->d_Mt[q]) {
-    const std::vector<double>& M = host_M(q);
-    const int64_t np = n_points(q), nc = n_coeff(q);
-    std::vector<double> T(M.size());
-    for (int64_t p = 0; p < np; ++p)
-      for (int64_t n = 0; n < nc; ++n) T[n * np + p] = M[p * nc + n];
-    double* d = nullptr;
-    CUDA_TRY(cudaMalloc(&d, T.size() * sizeof(double)));
-    CUDA_TRY(cudaMemcpy(d, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice));
-    ctx->d_Mt[q] = d;
-  }
-  *Mt = ctx->d_Mt[q];
-  return TBSLAS_OK;
+  return device_F(ctx, q, F);
 }
 
 int ctx_mu_scratch(tbslas_ctx ctx, size_t n, double** out) { return scratch_t(ctx, kMu, n, out); }
@@ -826,9 +834,7 @@ int tbslas_ctx_destroy(tbslas_ctx ctx) {
   cudaDeviceSynchronize();
   for (auto& b : ctx->slots)
     if (b.p) cudaFree(b.p);
-  for (auto p : ctx->d_M)
-    if (p) cudaFree(p);
-  for (auto p : ctx->d_Mt)
+  for (auto p : ctx->d_F)
     if (p) cudaFree(p);
   prof_collect(ctx);
   for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
@@ -885,26 +891,11 @@ int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launch
 }
 
 int tbslas_fp64_fma_peak(tbslas_ctx ctx, double* flops_per_s) {
-  TRY(bind(ctx));
-  if (!flops_per_s) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
-  const int blocks = ctx->num_sms * 8, threads = 256, iters = 2000;
-  double* out;
-  TRY(scratch_t(ctx, kHostOut, (size_t)blocks * threads, &out));
-  cudaEvent_t e0, e1;
-  CUDA_TRY(cudaEventCreate(&e0));
-  CUDA_TRY(cudaEventCreate(&e1));
-  k_fp64_fma<<<blocks, threads, 0, ctx->stream>>>(out, 1.0, 0.0, 10);
-  cudaEventRecord(e0, ctx->stream);
-  k_fp64_fma<<<blocks, threads, 0, ctx->stream>>>(out, 1.0, 0.0, iters);
-  cudaEventRecord(e1, ctx->stream);
-  CUDA_TRY(cudaEventSynchronize(e1));
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  TRY(check_launch("fp64_fma"));
-  *flops_per_s = 2.0 * 64.0 * iters * (double)blocks * threads / (ms * 1e-3);
-  return TBSLAS_OK;
+  return fma_peak<double>(ctx, 2000, flops_per_s);
+}
+
+int tbslas_fp32_fma_peak(tbslas_ctx ctx, double* flops_per_s) {
+  return fma_peak<float>(ctx, 40000, flops_per_s);
 }
 
 int tbslas_cheb_nodes(int q, double* out_host) {

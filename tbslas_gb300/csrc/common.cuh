@@ -177,7 +177,8 @@ __device__ __forceinline__ void eval_point(const TreeView& t, double& x, double&
 }
 
 // Double-float evaluation of DOF components at one point, for the fused
-// step.  m[a] bounds, per axis, the distance between this point and the one
+// step; `slots` holds 2*D shared-memory elements of this thread (the y and z
+// Chebyshev values of tri_sum_df_rows).  m[a] bounds, per axis, the distance between this point and the one
 // an all-FP64 computation would have produced (0: identical).  Returns true
 // when the lookup is ambiguous -- within m[a] of a face of the leaf on some
 // axis, or just outside the domain -- so the caller must recompute the target
@@ -189,8 +190,8 @@ constexpr double kDfSumErr = 1e-13;
 template <int D, int DOF, bool ERR>
 __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, double& y, double& z,
                                               bool periodic, const double (&m)[3],
-                                              double (&out)[DOF], double (&err)[DOF]) {
-  constexpr int NC = D * (D + 1) * (D + 2) / 6;
+                                              double (&out)[DOF], double (&err)[DOF],
+                                              ThreadSlots slots) {
   if (periodic) {
     x = wrap1(x);
     y = wrap1(y);
@@ -212,20 +213,22 @@ __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, doub
                    (m[1] > 0.0 && fabs(yi) >= 1.0 - m[1] * g.w) ||
                    (m[2] > 0.0 && fabs(zi) >= 1.0 - m[2] * g.w);
   double T[D];
-  df tx[D], ty[D], tz[D];
+  df tx[D];
+  const ThreadSlots ty = slots, tz{slots.s + D * slots.bs, slots.bs};
+  cheb_T<D>(yi, T);
+#pragma unroll
+  for (int k = 0; k < D; ++k) ty.put(k, df_from_double(T[k]));
+  cheb_T<D>(zi, T);
+#pragma unroll
+  for (int k = 0; k < D; ++k) tz.put(k, df_from_double(T[k]));
   cheb_T<D>(xi, T);
 #pragma unroll
   for (int k = 0; k < D; ++k) tx[k] = df_from_double(T[k]);
-  cheb_T<D>(yi, T);
-#pragma unroll
-  for (int k = 0; k < D; ++k) ty[k] = df_from_double(T[k]);
-  cheb_T<D>(zi, T);
-#pragma unroll
-  for (int k = 0; k < D; ++k) tz[k] = df_from_double(T[k]);
-  const float2* c = t.coeff2 + leaf * t.stride;
+  df r[DOF];
+  tri_sum_df_rows<D, DOF>(t.coeff2 + leaf * t.stride, tx, ty, tz, r);
 #pragma unroll
   for (int l = 0; l < DOF; ++l) {
-    out[l] = df_to_double(tri_sum_df<D>(GlobalLoadDF{c + l * NC}, tx, ty, tz));
+    out[l] = df_to_double(r[l]);
     if (ERR) {
       const double cn = __ldg(t.cnorm + leaf * DOF + l);
       err[l] = cn * (kDfSumErr + (double)((D - 1) * (D - 1)) * g.w * mmax);

@@ -84,4 +84,88 @@ __device__ __forceinline__ df tri_sum_df(Load c, const df (&tx)[D], const df (&t
   return df_norm(u);
 }
 
+// One thread's array in shared memory: element k at s[k * bs] (bs = the
+// block size), so a warp's accesses to one element are conflict-free.
+struct ThreadSlots {
+  float2* s;
+  int bs;
+  __device__ __forceinline__ df get(int k) const {
+    const float2 v = s[k * bs];
+    return df{v.x, v.y};
+  }
+  __device__ __forceinline__ void put(int k, df a) const { s[k * bs] = make_float2(a.hi, a.lo); }
+};
+
+// The triangular sum with the i and j loops rolled: the unrolled form is
+// ~13 instructions per term x Nc terms per component (35K instructions for a
+// velocity and a concentration evaluation at q = 14), far beyond the
+// instruction caches, so warps stalled on instruction fetch.  Here the code
+// is one row of at most D terms: each (i, j) row of n = D-i-j coefficients
+// enters the unrolled sequence k = n-1 .. 0 through a switch (one indexed
+// jump), tx stays in registers, ty_j and tz_i come from shared memory.  The
+// DOF components share the row's T values and form independent chains.
+#define TBG_DF_TERM(K)                                                           \
+  case (K) + 1:                                                                  \
+    if constexpr ((K) < D) {                                                     \
+      _Pragma("unroll") for (int l = 0; l < DOF; ++l)                            \
+          df_fma_acc(w[l], ld(l * NC + idx + (K)), tx[(K) < D ? (K) : 0]);       \
+    }                                                                            \
+    [[fallthrough]];
+
+template <int D, int DOF>
+__device__ __forceinline__ void tri_sum_df_rows(const float2* __restrict__ c, const df (&tx)[D],
+                                                ThreadSlots ty, ThreadSlots tz, df (&out)[DOF]) {
+  static_assert(D >= 1 && D <= 17, "degree above 16");
+  constexpr int NC = D * (D + 1) * (D + 2) / 6;
+  const GlobalLoadDF ld{c};
+  df u[DOF];
+#pragma unroll
+  for (int l = 0; l < DOF; ++l) u[l] = df{0.f, 0.f};
+  int idx = 0;
+#pragma unroll 1
+  for (int i = 0; i < D; ++i) {
+    df v[DOF];
+#pragma unroll
+    for (int l = 0; l < DOF; ++l) v[l] = df{0.f, 0.f};
+#pragma unroll 1
+    for (int j = 0; j < D - i; ++j) {
+      const int n = D - i - j;
+      df w[DOF];
+#pragma unroll
+      for (int l = 0; l < DOF; ++l) w[l] = df{0.f, 0.f};
+      switch (n) {
+        TBG_DF_TERM(16)
+        TBG_DF_TERM(15)
+        TBG_DF_TERM(14)
+        TBG_DF_TERM(13)
+        TBG_DF_TERM(12)
+        TBG_DF_TERM(11)
+        TBG_DF_TERM(10)
+        TBG_DF_TERM(9)
+        TBG_DF_TERM(8)
+        TBG_DF_TERM(7)
+        TBG_DF_TERM(6)
+        TBG_DF_TERM(5)
+        TBG_DF_TERM(4)
+        TBG_DF_TERM(3)
+        TBG_DF_TERM(2)
+        TBG_DF_TERM(1)
+        TBG_DF_TERM(0)
+        default:
+          break;
+      }
+      idx += n;
+      const df yj = ty.get(j);
+#pragma unroll
+      for (int l = 0; l < DOF; ++l) df_fma_acc(v[l], yj, df_norm(w[l]));
+    }
+    const df zi = tz.get(i);
+#pragma unroll
+    for (int l = 0; l < DOF; ++l) df_fma_acc(u[l], zi, df_norm(v[l]));
+  }
+#pragma unroll
+  for (int l = 0; l < DOF; ++l) out[l] = df_norm(u[l]);
+}
+#undef TBG_DF_TERM
+
 }  // namespace tbg

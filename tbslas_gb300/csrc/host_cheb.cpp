@@ -130,4 +130,85 @@ std::vector<double> pt2coeff_matrix(int q) {
   return M;
 }
 
+// Factors of the separable refit.  A[a][k] = T_k(xi_a) at the D = q+1
+// stretched nodes (xi_a = 2 x_a - 1, as pt2coeff_matrix maps them) has the QR
+// factorisation A = Q R.  The 3-D tensor basis on the tensor grid is
+// A (x) A (x) A, so the least-squares fit onto the total-degree triangle T =
+// {i+j+k < D} that M = pinv(V)^T computes is
+//   c = [ (R^-1)^(x)3 ext_T( [ (Q^T)^(x)3 f ]_T ) ]_T :
+// with U = R (x) R (x) R the objective is |U (S c - c_full)|^2; U is upper
+// triangular on every axis and T is closed downwards, so U's rows outside T
+// see only coefficients outside T and the rows in T are solved exactly.
+// Returned row-major, 4 D x D blocks: Q[a][k], Q^T, R^-1[k'][k], R^-T.
+// Householder QR in long double.
+std::vector<double> refit_factors(int q) {
+  const int d = q + 1;
+  std::vector<double> x = cheb_nodes_1d(q);
+  std::vector<long double> A((size_t)d * d), Q((size_t)d * d, 0.0L);
+  for (int a = 0; a < d; a++) {
+    const long double xi = (long double)(x[a] * 2.0 - 1.0);
+    long double t0 = 1.0L, t1 = xi;
+    for (int k = 0; k < d; k++) {
+      long double t;
+      if (k == 0) {
+        t = t0;
+      } else if (k == 1) {
+        t = t1;
+      } else {
+        t = 2.0L * xi * t1 - t0;
+        t0 = t1;
+        t1 = t;
+      }
+      A[(size_t)a * d + k] = t;
+    }
+  }
+  for (int i = 0; i < d; i++) Q[(size_t)i * d + i] = 1.0L;
+  // A <- H_{d-1} ... H_0 A = R, Q <- Q H_0 ... H_{d-1}
+  std::vector<long double> v(d);
+  for (int j = 0; j < d; j++) {
+    long double norm2 = 0.0L;
+    for (int i = j; i < d; i++) norm2 += A[(size_t)i * d + j] * A[(size_t)i * d + j];
+    const long double norm = std::sqrt(norm2);
+    if (norm == 0.0L) continue;
+    const long double ajj = A[(size_t)j * d + j];
+    const long double alpha = ajj >= 0 ? -norm : norm;
+    long double vn2 = 0.0L;
+    for (int i = 0; i < d; i++) v[i] = i < j ? 0.0L : A[(size_t)i * d + j];
+    v[j] -= alpha;
+    for (int i = j; i < d; i++) vn2 += v[i] * v[i];
+    if (vn2 == 0.0L) continue;
+    for (int c = 0; c < d; c++) {  // A = (I - 2 v v^T / vn2) A
+      long double s = 0.0L;
+      for (int i = j; i < d; i++) s += v[i] * A[(size_t)i * d + c];
+      s *= 2.0L / vn2;
+      for (int i = j; i < d; i++) A[(size_t)i * d + c] -= s * v[i];
+    }
+    for (int r = 0; r < d; r++) {  // Q = Q (I - 2 v v^T / vn2)
+      long double s = 0.0L;
+      for (int i = j; i < d; i++) s += Q[(size_t)r * d + i] * v[i];
+      s *= 2.0L / vn2;
+      for (int i = j; i < d; i++) Q[(size_t)r * d + i] -= s * v[i];
+    }
+  }
+  // R^-1 by back substitution (R = upper triangle of A)
+  std::vector<long double> Ri((size_t)d * d, 0.0L);
+  for (int c = 0; c < d; c++) {
+    for (int r = c; r >= 0; r--) {
+      long double s = r == c ? 1.0L : 0.0L;
+      for (int k = r + 1; k <= c; k++) s -= A[(size_t)r * d + k] * Ri[(size_t)k * d + c];
+      Ri[(size_t)r * d + c] = s / A[(size_t)r * d + r];
+    }
+  }
+  const size_t dd = (size_t)d * d;
+  std::vector<double> out(4 * dd);
+  for (int r = 0; r < d; r++)
+    for (int c = 0; c < d; c++) {
+      out[0 * dd + (size_t)r * d + c] = (double)Q[(size_t)r * d + c];
+      out[1 * dd + (size_t)r * d + c] = (double)Q[(size_t)c * d + r];
+      out[2 * dd + (size_t)r * d + c] = (double)Ri[(size_t)r * d + c];
+      out[3 * dd + (size_t)r * d + c] = (double)Ri[(size_t)c * d + r];
+    }
+  return out;
+}
+
 }  // namespace tbg

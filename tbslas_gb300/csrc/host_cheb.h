@@ -7,4 +7,5 @@ namespace tbg {
 std::vector<double> cheb_nodes_1d(int q);
 std::vector<double> cheb_nodes_3d(int q);
 std::vector<double> pt2coeff_matrix(int q);
+std::vector<double> refit_factors(int q);
 }  // namespace tbg

@@ -95,32 +95,35 @@ int tree_view(tbslas_tree t, TreeView* v, tbslas_ctx* ctx);
 int tree_coeff(tbslas_tree t, double** coeff, int64_t* n_doubles);
 int tree_coeff2(tbslas_tree t, float2** coeff2);
 int ctx_info(tbslas_ctx ctx, int* device, int* num_sms);
-int ctx_M(tbslas_ctx ctx, int q, const double** M);
-int ctx_Mt(tbslas_ctx ctx, int q, const double** Mt);
+int ctx_F(tbslas_ctx ctx, int q, const double** F);
 int ctx_mu_scratch(tbslas_ctx ctx, size_t n, double** out);
 int ctx_vals_scratch(tbslas_ctx ctx, size_t n, double** out);
 Nodes1D ctx_nodes(int q);
 
-// Batched refit: one job per problem, one item per 64x64 output tile.
-constexpr int kRefitBM = 64, kRefitBN = 64, kRefitBK = 16;
+// Refit (refit.cu): node values -> coefficients through the separable
+// factors F = refit_factors(q) (4 D x D blocks on the device).
+//   coeff[(r/dof)*stride + (r%dof)*nc + t] = sum_p vals[r*np + p] M[p][t]
+void launch_refit(const double* vals, const double* F, int q, int64_t rows, int dof,
+                  int64_t stride, double* coeff, float2* coeff2, cudaStream_t s);
+// mu[r*np + p] = sum_t M[p][t] lam[r*nc + t] (the adjoint's transposed refit)
+void launch_refit_t(const double* lam, const double* F, int q, int64_t rows, double* mu,
+                    cudaStream_t s);
+// Batched refit: one job per problem, one CTA per (job, row) item.
 struct RefitJob {
   const double* vals;
-  const double* M;
+  const double* F;
   double* coeff;
   float2* coeff2;
   int64_t rows;
   int64_t stride;
-  int np, nc, dof, pad;
+  int q, dof;
 };
 struct RefitItem {
-  int32_t job, row_tile, col_tile, pad;
+  int32_t job, pad;
+  int64_t row;
 };
-void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_items,
+void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_items, int max_q,
                         cudaStream_t s);
-
-// refit.cu: coeff[(r/dof)*stride + (r%dof)*nc + n] = sum_p vals[r*np+p] M[p*nc+n]
-void launch_refit(const double* vals, const double* M, int64_t rows, int np, int nc, int dof,
-                  int64_t stride, double* coeff, float2* coeff2, cudaStream_t s);
 void launch_split(const double* c, float2* c2, int64_t n, cudaStream_t s);
 
 // misc kernels (capi.cu)

@@ -1,106 +1,303 @@
 // Node values -> Chebyshev coefficients of every leaf (SetTreeGridValues,
-// src/tree/tree_utils.h:500-552): one batched dense contraction
-//   C[r][n] = sum_p V[r][p] M[p][n],  r = leaf*dof + l,
-// V: rows x np node values (row-major), M: np x nc point-to-coefficient
-// matrix, C written into the tree's padded per-leaf coefficient layout.
-// FP64; 64x64 output tile per CTA, 16-deep K slices staged in shared memory,
-// 4x4 outputs per thread (16 FMAs per 8 shared loads).
+// src/tree/tree_utils.h:500-552), which the reference computes as one dense
+// product with the Np x Nc matrix M = pinv(V)^T (GetPt2CoeffMatrix,
+// src/utils/cheb.h:166-196).  The same linear map factors through the 1-D
+// QR A = Q R of the Chebyshev-Vandermonde matrix at the stretched nodes
+// (refit_factors, host_cheb.cpp):
+//   c = [ (R^-1)^(x)3 ext_T( [ (Q^T)^(x)3 f ]_T ) ]_T ,  T = {i+j+k < D},
+// three 1-D passes with Q^T over the box (D^4 + D^4/2 + D^4/6 multiply-adds)
+// and three triangular passes with R^-1 inside T (~D^4/24 each): ~1.8 D^4
+// per leaf and component instead of D^3 Nc (D^6/6) -- 25x fewer at q = 14.
+// One CTA per (leaf, component) row; the row and its intermediates live in
+// shared memory (two D^3 buffers), FP64 throughout.
+#include <atomic>
+
 #include "internal.h"
 
 namespace tbg {
 
-// One 64x64 output tile of C = V M (rows x nc), written into the padded
-// per-leaf coefficient layout.  Shared by the single-tree and batched kernels.
-__device__ __forceinline__ void refit_tile(const double* __restrict__ V,
-                                           const double* __restrict__ M, int64_t rows, int np,
-                                           int nc, int dof, int64_t stride, double* __restrict__ C,
-                                           float2* __restrict__ C2, int64_t row0, int col0) {
-  __shared__ double As[kRefitBK][kRefitBM];
-  __shared__ double Bs[kRefitBK][kRefitBN];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  double acc[4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+namespace {
 
-  for (int k0 = 0; k0 < np; k0 += kRefitBK) {
-#pragma unroll
-    for (int e = threadIdx.x; e < kRefitBM * kRefitBK; e += 256) {
-      const int r = e / kRefitBK, k = e % kRefitBK;
-      const int64_t row = row0 + r;
-      const int kk = k0 + k;
-      As[k][r] = (row < rows && kk < np) ? __ldg(V + row * np + kk) : 0.0;
-    }
-#pragma unroll
-    for (int e = threadIdx.x; e < kRefitBK * kRefitBN; e += 256) {
-      const int k = e / kRefitBN, c = e % kRefitBN;
-      const int kk = k0 + k, col = col0 + c;
-      Bs[k][c] = (kk < np && col < nc) ? __ldg(M + (int64_t)kk * nc + col) : 0.0;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < kRefitBK; ++k) {
-      double a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[k][ty + 16 * i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[k][tx + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int64_t row = row0 + ty + 16 * i;
-    if (row >= rows) continue;
-    const int64_t leaf = row / dof;
-    const int l = (int)(row - leaf * dof);
-    const int64_t base = leaf * stride + (int64_t)l * nc;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int col = col0 + tx + 16 * j;
-      if (col < nc) {
-        C[base + col] = acc[i][j];
-        if (C2) {
-          const df v = df_from_double(acc[i][j]);
-          C2[base + col] = make_float2(v.hi, v.lo);
-        }
-      }
-    }
-  }
+constexpr int kRefitThreads = 256;
+
+__host__ __device__ constexpr int nc_of(int n) { return n * (n + 1) * (n + 2) / 6; }
+
+// Position of coefficient (i, j, k) (z, y, x degrees) in the triangular order
+// i outer, j, k inner.
+__device__ __forceinline__ int tri_index(int D, int i, int j, int k) {
+  const int m = D - i;
+  return nc_of(D) - nc_of(m) + j * m - (j * (j - 1)) / 2 + k;
 }
 
-__global__ void __launch_bounds__(256) k_refit(const double* __restrict__ V,
-                                               const double* __restrict__ M, int64_t rows,
-                                               int np, int nc, int dof, int64_t stride,
-                                               double* __restrict__ C, float2* __restrict__ C2) {
-  refit_tile(V, M, rows, np, nc, dof, stride, C, C2, (int64_t)blockIdx.x * kRefitBM,
-             blockIdx.y * kRefitBN);
+struct Factors {  // shared-memory views of the 4 D x D blocks
+  const double *Q, *QT, *Ri, *RiT;
+};
+
+__device__ __forceinline__ Factors stage_factors(const double* __restrict__ F, int D,
+                                                 double* sm) {
+  const int n = 4 * D * D;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) sm[e] = __ldg(F + e);
+  const int dd = D * D;
+  return Factors{sm, sm + dd, sm + 2 * dd, sm + 3 * dd};
 }
 
-// Batched refit: one CTA per (problem, row tile, column tile) work item.
-__global__ void __launch_bounds__(256) k_batch_refit(const RefitJob* __restrict__ jobs,
-                                                     const RefitItem* __restrict__ items) {
+// f (D^3 values, x fastest) in S0 -> coefficients, handed to `emit(t, c)`
+// with t the triangular index.  Ends with the block synchronised.
+template <class Emit>
+__device__ __forceinline__ void refit_row(const Factors& f, int D, double* S0, double* S1,
+                                          Emit emit) {
+  const int D2 = D * D, D3 = D2 * D;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  // x: S1[c][b][k] = sum_a Q[a][k] S0[c][b][a]
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D;
+    const double* row = S0 + (o - k);
+    double s = 0.0;
+    for (int a = 0; a < D; ++a) s = fma(f.Q[a * D + k], row[a], s);
+    S1[o] = s;
+  }
+  __syncthreads();
+  // y: S0[c][j][k] = sum_b Q[b][j] S1[c][b][k],  j + k < D
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, j = (o / D) % D, c = o / D2;
+    if (j + k >= D) continue;
+    const double* col = S1 + c * D2 + k;
+    double s = 0.0;
+    for (int b = 0; b < D; ++b) s = fma(f.Q[b * D + j], col[b * D], s);
+    S0[o] = s;
+  }
+  __syncthreads();
+  // z: S1[i][j][k] = sum_c Q[c][i] S0[c][j][k],  i + j + k < D
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, j = (o / D) % D, i = o / D2;
+    if (i + j + k >= D) continue;
+    const double* col = S0 + j * D + k;
+    double s = 0.0;
+    for (int c = 0; c < D; ++c) s = fma(f.Q[c * D + i], col[c * D2], s);
+    S1[o] = s;
+  }
+  __syncthreads();
+  // R^-1 along x: S0[i][j][k'] = sum_{k >= k'} R^-1[k'][k] S1[i][j][k]
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, j = (o / D) % D, i = o / D2;
+    const int n = D - i - j;
+    if (k >= n) continue;
+    const double* row = S1 + (o - k);
+    double s = 0.0;
+    for (int kk = k; kk < n; ++kk) s = fma(f.RiT[kk * D + k], row[kk], s);
+    S0[o] = s;
+  }
+  __syncthreads();
+  // R^-1 along y: S1[i][j'][k] = sum_{j >= j'} R^-1[j'][j] S0[i][j][k]
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, j = (o / D) % D, i = o / D2;
+    const int n = D - i - k;
+    if (j >= n) continue;
+    const double* col = S0 + i * D2 + k;
+    double s = 0.0;
+    for (int jj = j; jj < n; ++jj) s = fma(f.Ri[j * D + jj], col[jj * D], s);
+    S1[o] = s;
+  }
+  __syncthreads();
+  // R^-1 along z: c[i'][j][k] = sum_{i >= i'} R^-1[i'][i] S1[i][j][k]
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, j = (o / D) % D, i = o / D2;
+    const int n = D - j - k;
+    if (i >= n) continue;
+    const double* col = S1 + j * D + k;
+    double s = 0.0;
+    for (int ii = i; ii < n; ++ii) s = fma(f.Ri[i * D + ii], col[ii * D2], s);
+    emit(tri_index(D, i, j, k), s);
+  }
+  __syncthreads();
+}
+
+// The transposed map, f = M c (M: Np x Nc): c (triangular order) in S0 at
+// the box positions of T ->
+//   f = (Q)^(x)3 ext_T( [ (R^-T)^(x)3 c ]_T ),
+// handed to `emit(p, value)` with p the node index (x fastest).
+template <class Emit>
+__device__ __forceinline__ void refit_row_t(const Factors& f, int D, double* S0, double* S1,
+                                            Emit emit) {
+  const int D2 = D * D, D3 = D2 * D;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  // R^-T along z: S1[i][j][k] = sum_{i' <= i} R^-1[i'][i] S0[i'][j][k]
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, j = (o / D) % D, i = o / D2;
+    if (i + j + k >= D) continue;
+    const double* col = S0 + j * D + k;
+    double s = 0.0;
+    for (int ii = 0; ii <= i; ++ii) s = fma(f.RiT[i * D + ii], col[ii * D2], s);
+    S1[o] = s;
+  }
+  __syncthreads();
+  // R^-T along y
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, j = (o / D) % D, i = o / D2;
+    if (i + j + k >= D) continue;
+    const double* col = S1 + i * D2 + k;
+    double s = 0.0;
+    for (int jj = 0; jj <= j; ++jj) s = fma(f.RiT[j * D + jj], col[jj * D], s);
+    S0[o] = s;
+  }
+  __syncthreads();
+  // R^-T along x
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, j = (o / D) % D, i = o / D2;
+    if (i + j + k >= D) continue;
+    const double* row = S0 + (o - k);
+    double s = 0.0;
+    for (int kk = 0; kk <= k; ++kk) s = fma(f.Ri[kk * D + k], row[kk], s);
+    S1[o] = s;
+  }
+  __syncthreads();
+  // Q along z: S0[c][j][k] = sum_{i < D-j-k} Q[c][i] S1[i][j][k],  j + k < D
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, j = (o / D) % D, c = o / D2;
+    const int n = D - j - k;
+    if (n <= 0) continue;
+    const double* col = S1 + j * D + k;
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = fma(f.Q[c * D + i], col[i * D2], s);
+    S0[o] = s;
+  }
+  __syncthreads();
+  // Q along y: S1[c][b][k] = sum_{j < D-k} Q[b][j] S0[c][j][k]
+  for (int o = tid; o < D3; o += bs) {
+    const int k = o % D, b = (o / D) % D, c = o / D2;
+    const int n = D - k;
+    const double* col = S0 + c * D2 + k;
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) s = fma(f.Q[b * D + j], col[j * D], s);
+    S1[o] = s;
+  }
+  __syncthreads();
+  // Q along x: f[c][b][a] = sum_k Q[a][k] S1[c][b][k]
+  for (int o = tid; o < D3; o += bs) {
+    const int a = o % D;
+    const double* row = S1 + (o - a);
+    double s = 0.0;
+    for (int k = 0; k < D; ++k) s = fma(f.QT[k * D + a], row[k], s);
+    emit(o, s);
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void load_row(const double* __restrict__ v, int n, double* S0) {
+  for (int e = threadIdx.x; e < n; e += blockDim.x) S0[e] = __ldg(v + e);
+  __syncthreads();
+}
+
+struct CoeffOut {
+  double* c;
+  float2* c2;
+  __device__ __forceinline__ void operator()(int t, double s) const {
+    c[t] = s;
+    if (c2) {
+      const df v = df_from_double(s);
+      c2[t] = make_float2(v.hi, v.lo);
+    }
+  }
+};
+
+// Dynamic shared memory of the refit kernels at degree q.
+__host__ __device__ constexpr size_t refit_smem(int q) {
+  return (size_t)(4 * (q + 1) * (q + 1) + 2 * (q + 1) * (q + 1) * (q + 1)) * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kRefitThreads) k_refit(const double* __restrict__ vals,
+                                                         const double* __restrict__ F, int q,
+                                                         int dof, int64_t stride,
+                                                         double* __restrict__ coeff,
+                                                         float2* __restrict__ coeff2) {
+  extern __shared__ __align__(16) double sm[];
+  const int D = q + 1, D3 = D * D * D;
+  const Factors f = stage_factors(F, D, sm);
+  double* S0 = sm + 4 * D * D;
+  double* S1 = S0 + D3;
+  const int64_t r = blockIdx.x;
+  const int64_t leaf = r / dof;
+  const int l = (int)(r - leaf * dof);
+  load_row(vals + r * D3, D3, S0);
+  const int64_t base = leaf * stride + (int64_t)l * nc_of(D);
+  refit_row(f, D, S0, S1, CoeffOut{coeff + base, coeff2 ? coeff2 + base : nullptr});
+}
+
+// mu[r][p] = sum_n M[p][n] lam[r][n] (the adjoint's transposed refit).
+__global__ void __launch_bounds__(kRefitThreads) k_refit_t(const double* __restrict__ lam,
+                                                           const double* __restrict__ F, int q,
+                                                           double* __restrict__ mu) {
+  extern __shared__ __align__(16) double sm[];
+  const int D = q + 1, D2 = D * D, D3 = D2 * D, NC = nc_of(D);
+  const Factors f = stage_factors(F, D, sm);
+  double* S0 = sm + 4 * D2;
+  double* S1 = S0 + D3;
+  const int64_t r = blockIdx.x;
+  const double* c = lam + r * NC;
+  for (int o = threadIdx.x; o < D3; o += blockDim.x) {
+    const int k = o % D, j = (o / D) % D, i = o / D2;
+    if (i + j + k < D) S0[o] = __ldg(c + tri_index(D, i, j, k));
+  }
+  __syncthreads();
+  double* out = mu + r * D3;
+  refit_row_t(f, D, S0, S1, [out](int p, double s) { out[p] = s; });
+}
+
+// Batched refit: one CTA per (problem, row) item.
+__global__ void __launch_bounds__(kRefitThreads) k_batch_refit(const RefitJob* __restrict__ jobs,
+                                                               const RefitItem* __restrict__ items) {
+  extern __shared__ __align__(16) double sm[];
   const RefitItem it = items[blockIdx.x];
   const RefitJob j = jobs[it.job];
-  refit_tile(j.vals, j.M, j.rows, j.np, j.nc, j.dof, j.stride, j.coeff, j.coeff2,
-             (int64_t)it.row_tile * kRefitBM, it.col_tile * kRefitBN);
+  const int D = j.q + 1, D3 = D * D * D;
+  const Factors f = stage_factors(j.F, D, sm);
+  double* S0 = sm + 4 * D * D;
+  double* S1 = S0 + D3;
+  const int64_t leaf = it.row / j.dof;
+  const int l = (int)(it.row - leaf * j.dof);
+  load_row(j.vals + it.row * D3, D3, S0);
+  const int64_t base = leaf * j.stride + (int64_t)l * nc_of(D);
+  refit_row(f, D, S0, S1, CoeffOut{j.coeff + base, j.coeff2 ? j.coeff2 + base : nullptr});
 }
 
-void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_items,
-                        cudaStream_t s) {
-  if (n_items > 0) k_batch_refit<<<(unsigned)n_items, 256, 0, s>>>(jobs, items);
+// Raise a kernel's dynamic shared-memory limit to the degree-16 size, once
+// per device.
+template <class K>
+void allow_smem(K kernel, std::atomic<uint64_t>& done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t bit = 1ull << (dev & 63);
+  if (!(done.load() & bit)) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)refit_smem(TBSLAS_MAX_DEGREE));
+    done.fetch_or(bit);
+  }
 }
 
-void launch_refit(const double* vals, const double* M, int64_t rows, int np, int nc, int dof,
+std::atomic<uint64_t> g_smem_refit{0}, g_smem_refit_t{0}, g_smem_batch{0};
+
+}  // namespace
+
+void launch_refit(const double* vals, const double* F, int q, int64_t rows, int dof,
                   int64_t stride, double* coeff, float2* coeff2, cudaStream_t s) {
   if (rows <= 0) return;
-  dim3 grid((unsigned)((rows + kRefitBM - 1) / kRefitBM), (unsigned)((nc + kRefitBN - 1) / kRefitBN));
-  k_refit<<<grid, 256, 0, s>>>(vals, M, rows, np, nc, dof, stride, coeff, coeff2);
+  allow_smem(k_refit, g_smem_refit);
+  k_refit<<<(unsigned)rows, kRefitThreads, refit_smem(q), s>>>(vals, F, q, dof, stride, coeff,
+                                                               coeff2);
+}
+
+void launch_refit_t(const double* lam, const double* F, int q, int64_t rows, double* mu,
+                    cudaStream_t s) {
+  if (rows <= 0) return;
+  allow_smem(k_refit_t, g_smem_refit_t);
+  k_refit_t<<<(unsigned)rows, kRefitThreads, refit_smem(q), s>>>(lam, F, q, mu);
+}
+
+void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_items, int max_q,
+                        cudaStream_t s) {
+  if (n_items <= 0) return;
+  allow_smem(k_batch_refit, g_smem_batch);
+  k_batch_refit<<<(unsigned)n_items, kRefitThreads, refit_smem(max_q), s>>>(jobs, items);
 }
 
 // Split FP64 coefficients into their double-float form.

@@ -139,6 +139,8 @@ void launch_semilag_tree(const SemilagTreeArgs& a, cudaStream_t s) {
 template <int D>
 __global__ void __launch_bounds__(128) k_semilag_tree_df(const SemilagTreeArgs a) {
   constexpr int NP = D * D * D;
+  extern __shared__ float2 s_slots[];
+  const ThreadSlots slots{s_slots + threadIdx.x, (int)blockDim.x};
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= a.con.L * NP) return;
   const int64_t leaf = t / NP;
@@ -155,7 +157,7 @@ __global__ void __launch_bounds__(128) k_semilag_tree_df(const SemilagTreeArgs a
 #pragma unroll 1
   for (int st = 0; st < 2 * a.nrk; ++st) {
     double v[3], ev[3];
-    amb |= eval_point_df<D, 3, true>(a.vel, px[0], px[1], px[2], per, mp, v, ev);
+    amb |= eval_point_df<D, 3, true>(a.vel, px[0], px[1], px[2], per, mp, v, ev, slots);
     if ((st & 1) == 0) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -172,7 +174,7 @@ __global__ void __launch_bounds__(128) k_semilag_tree_df(const SemilagTreeArgs a
     }
   }
   double c[1], ce[1];
-  amb |= eval_point_df<D, 1, false>(a.con, x[0], x[1], x[2], per, m0, c, ce);
+  amb |= eval_point_df<D, 1, false>(a.con, x[0], x[1], x[2], per, m0, c, ce, slots);
   a.vals[t] = c[0];
   if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = t;
 }
@@ -208,7 +210,8 @@ void launch_semilag_tree_df(const SemilagTreeArgs& a, cudaStream_t s) {
   const int64_t blocks = (n + threads - 1) / threads;
   if (blocks == 0) return;
   cudaMemsetAsync(a.fix_count, 0, sizeof(unsigned long long), s);
-  k_semilag_tree_df<D><<<(unsigned)blocks, threads, 0, s>>>(a);
+  const size_t smem = 2 * D * threads * sizeof(float2);
+  k_semilag_tree_df<D><<<(unsigned)blocks, threads, smem, s>>>(a);
   k_semilag_fix<D><<<a.fix_grid, threads, 0, s>>>(a);
 }
 

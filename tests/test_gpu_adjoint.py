@@ -54,12 +54,14 @@ def _J(c, V, cobs):
 def test_adjoint_matches_central_differences(ctx, checkpoint):
     """Central differences, eps = 1e-6, along seeded random directions: N(0,1)
     coefficients for c0 (J is quadratic in c0), smooth random velocity fields
-    for V.  J is only piecewise smooth in V (a node pushed across a leaf face
-    changes polynomial), so the velocity is a generic periodic Fourier field
-    that pins no node on a face; the exact check along arbitrary directions is
-    the dual-number test below."""
+    for V.  J is only piecewise smooth in V: the per-leaf fits differ across a
+    leaf face, so a departure point that the eps-perturbation pushes across a
+    face makes the quotient jump.  At q = 4 on this seeded problem no point
+    lies within that distance of a face (the quotients at eps = 1e-4 .. 1e-7
+    agree to 1e-8); at q = 5 some do, and there the exact check is the
+    dual-number test below, which holds leaf choices fixed."""
     import torch
-    a, d, q, vc, c0, cobs, tv, tc = _problem(ctx)
+    a, d, q, vc, c0, cobs, tv, tc = _problem(ctx, q=4)
     V = torch.from_numpy(adjoint.basis_at_nodes(q)).cuda()
     co = torch.from_numpy(cobs).cuda()
     c0t = torch.from_numpy(c0).cuda().requires_grad_(True)
@@ -104,13 +106,14 @@ def test_adjoint_checkpoint_equals_recompute(ctx):
         assert np.abs(x - y).max() <= 1e-12 * np.abs(y).max()
 
 
-@pytest.mark.parametrize("vel_kind", ["fourier", "taylor_green"])
-def test_adjoint_matches_dual_number_oracle(ctx, ora, vel_kind):
+@pytest.mark.parametrize("vel_kind,q", [("fourier", 4), ("taylor_green", 4), ("fourier", 5),
+                                        ("fourier", 7)])
+def test_adjoint_matches_dual_number_oracle(ctx, ora, vel_kind, q):
     """Exact directional derivative of the discrete T-step map (forward-mode
     dual numbers through the oracle, leaf choices held fixed) against the
     adjoint's gradient."""
     import torch
-    q, steps, dt = 4, 3, 0.03
+    steps, dt = 3, 0.03
     a, d = trees.uniform_tree(2)
     if vel_kind == "fourier":
         fn = fields.fourier_velocity(np.random.default_rng(3))
