@@ -139,6 +139,16 @@ int tbslas_collect_grid_points(tbslas_ctx ctx, tbslas_tree tree, double* out_dev
  * src/tree/tree_functor.h:397-815. */
 int tbslas_eval_tree(tbslas_ctx ctx, tbslas_tree tree, const double* pos_dev, int64_t n,
                      double* out_dev, int bc, void* stream);
+/* src evaluated at every Chebyshev node of dst's leaves: out_dev
+ * [dst leaves * (q_dst+1)^3][src dof], in the order of
+ * tbslas_collect_grid_points(dst).  Equals tbslas_eval_tree(src) at those
+ * points bit for bit (same sums, same order); computed by sum factorisation
+ * over the nodes' tensor grid, ~D^4 instead of D^6/6 work per leaf.  The
+ * composition EvalTree(src, CollectChebTreeGridPoints(dst)) that the first
+ * RK2 stage of SolveSemilagInSitu performs (src/tree/tree_semilag.h:114-124,
+ * src/semilag/traj.inc:20-68). */
+int tbslas_eval_tree_on_nodes(tbslas_ctx ctx, tbslas_tree src, tbslas_tree dst, double* out_dev,
+                              int bc, void* stream);
 /* Synchronous host-buffer form of the same functor (the reference's exact
  * calling convention: host arrays in, host array out). */
 int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_host, int64_t n,

@@ -210,6 +210,19 @@ class NodeFieldFunctor:
              _stream(stream))
         return out
 
+    def at_nodes(self, dst_tree, out=None, stream=None):
+        """The field at every Chebyshev node of dst_tree's leaves, [N, dof] in
+        collect_cheb_tree_grid_points order (same values as calling the
+        functor at those points, by sum factorisation)."""
+        import torch
+        t = self.tree
+        if out is None:
+            out = torch.empty((dst_tree.n_leaves * n_points(dst_tree.q), t.dof),
+                              dtype=torch.float64, device="cuda:%d" % t.ctx.device)
+        call("tbslas_eval_tree_on_nodes", t.ctx.handle, t.handle, dst_tree.handle, _ptr(out),
+             self.bc, _stream(stream))
+        return out
+
 
 def compute_traj_rk2(vel_functor, xinit, tinit, tfinal, num_rk_step, xsol=None, stream=None):
     """RK2 departure points of xinit (CUDA tensor [n,3]) through a tree velocity."""

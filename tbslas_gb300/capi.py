@@ -50,6 +50,7 @@ SIGNATURES = {
     "tbslas_collect_grid_points": [_vp, _vp, _vp, _vp],
     "tbslas_eval_tree": [_vp, _vp, _vp, _i64, _vp, _i32, _vp],
     "tbslas_eval_tree_host": [_vp, _vp, _vp, _i64, _vp, _i32],
+    "tbslas_eval_tree_on_nodes": [_vp, _vp, _vp, _vp, _i32, _vp],
     "tbslas_eval_tree_noalloc": [_vp, _vp, _i64, _vp, _i32, _vp],
     "tbslas_traj_rk2": [_vp, _vp, _vp, _i64, _f64, _f64, _i32, _i32, _vp, _vp],
     "tbslas_traj_rk2_host": [_vp, _vp, _vp, _i64, _f64, _f64, _i32, _i32, _vp],

@@ -4,7 +4,9 @@
 // One persistent kernel per step walks a flattened worklist of target
 // chunks across all problems (CTAs take chunks from an atomic counter, so
 // problems of uneven size and degree balance across SMs); one batched refit
-// kernel per step walks all problems' 64x64 coefficient tiles.  A run of
+// kernel per step walks all problems' leaves; before them one kernel
+// evaluates each problem's velocity on its concentration nodes (the first RK
+// stage, by sum factorisation).  A run of
 // nsteps steps is captured once as a CUDA graph and replayed.  Launch
 // parameters (threads per CTA, targets per chunk, CTAs per SM) come from the
 // autotuner below, which times candidates on the batch itself.
@@ -40,6 +42,10 @@ struct tbslas_batch_s {
   BatchProblem* d_probs = nullptr;
   RefitJob* d_jobs = nullptr;
   RefitItem* d_ritems = nullptr;
+  NodeEvalJob* d_njobs = nullptr;
+  NodeEvalItem* d_nitems = nullptr;
+  int64_t n_nitems = 0;
+  double* d_vn = nullptr;
   int64_t n_ritems = 0;
   int max_q = 0;
   BatchItem* d_items = nullptr;
@@ -113,6 +119,7 @@ int enqueue_steps(tbslas_batch b, int nsteps, cudaStream_t s) {
   const int grid = b->num_sms * b->cps;
   for (int i = 0; i < nsteps; ++i) {
     unsigned long long* fix_count = b->d_counters + (int64_t)i * kPer + kBands;
+    launch_batch_eval_on_nodes(b->d_njobs, b->d_nitems, b->n_nitems, b->max_q, b->bc, s);
     for (int band = 0; band < kBands; ++band) {
       const int64_t n = b->band_begin[band + 1] - b->band_begin[band];
       if (n == 0) continue;
@@ -207,6 +214,8 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
   cudaSetDevice(b->device);
   std::vector<RefitJob> jobs;
   std::vector<RefitItem> ritems;
+  std::vector<NodeEvalJob> njobs;
+  std::vector<NodeEvalItem> nitems;
   int64_t off = 0;
   for (int i = 0; i < n && st == TBSLAS_OK; ++i) {
     BatchProblem p;
@@ -260,15 +269,26 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     jobs.push_back(RefitJob{nullptr, F, coeff, coeff2, p.con.L, p.con.stride, p.q, 1});
     b->max_q = std::max(b->max_q, p.q);
     for (int64_t r = 0; r < p.con.L; ++r) ritems.push_back(RefitItem{i, 0, r});
+    NodeEvalJob nj;
+    nj.src = p.vel;
+    nj.dst = p.con;
+    nj.nodes = p.nodes;
+    nj.out = nullptr;  // rebased below
+    njobs.push_back(nj);
+    for (int64_t r = 0; r < p.con.L; ++r) nitems.push_back(NodeEvalItem{i, 0, r});
   }
   cudaError_t e = cudaSuccess;
   if (st == TBSLAS_OK) {
     b->total_targets = off;
     e = cudaMalloc(&b->d_vals, sizeof(double) * std::max<int64_t>(off, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_vn, sizeof(double) * 3 * std::max<int64_t>(off, 1));
     if (e == cudaSuccess) {
       for (size_t i = 0; i < b->h_probs.size(); ++i) {
-        b->h_probs[i].vals = b->d_vals + reinterpret_cast<int64_t>(b->h_probs[i].vals);
+        const int64_t o = reinterpret_cast<int64_t>(b->h_probs[i].vals);
+        b->h_probs[i].vals = b->d_vals + o;
+        b->h_probs[i].vn = b->d_vn + 3 * o;
         jobs[i].vals = b->h_probs[i].vals;
+        njobs[i].out = b->d_vn + 3 * o;
       }
       e = cudaMalloc(&b->d_probs, sizeof(BatchProblem) * n);
     }
@@ -283,6 +303,14 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
       e = cudaMemcpy(b->d_ritems, ritems.data(), sizeof(RefitItem) * ritems.size(),
                      cudaMemcpyHostToDevice);
     b->n_ritems = (int64_t)ritems.size();
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_njobs, sizeof(NodeEvalJob) * n);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_njobs, njobs.data(), sizeof(NodeEvalJob) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_nitems, sizeof(NodeEvalItem) * nitems.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_nitems, nitems.data(), sizeof(NodeEvalItem) * nitems.size(),
+                     cudaMemcpyHostToDevice);
+    b->n_nitems = (int64_t)nitems.size();
     if (e == cudaSuccess) e = cudaMalloc(&b->d_ts0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_fix, sizeof(int64_t) * std::max<int64_t>(off, 1));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
@@ -304,7 +332,8 @@ int tbslas_batch_destroy(tbslas_batch b) {
   drop_graph(b);
   if (b->cap) cudaStreamDestroy(b->cap);
   for (void* p : {(void*)b->d_probs, (void*)b->d_jobs, (void*)b->d_ritems, (void*)b->d_items,
-                  (void*)b->d_vals, (void*)b->d_counters, (void*)b->d_ts0, (void*)b->d_fix})
+                  (void*)b->d_vals, (void*)b->d_counters, (void*)b->d_ts0, (void*)b->d_fix,
+                  (void*)b->d_njobs, (void*)b->d_nitems, (void*)b->d_vn})
     if (p) cudaFree(p);
   delete b;
   return TBSLAS_OK;

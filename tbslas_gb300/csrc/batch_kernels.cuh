@@ -13,6 +13,7 @@ struct BatchProblem {
   TreeView con;   // dof 1, same degree
   Nodes1D nodes;  // 1-D Chebyshev nodes of degree q
   double* vals;   // [n_targets] node values of this problem
+  const double* vn;  // [n_targets][3] velocity at the targets (first RK stage)
   double dt;
   int64_t n_targets;
   int q;
@@ -75,8 +76,14 @@ __device__ __forceinline__ void batch_target_df(const BatchProblem& p, int64_t t
   double px[3] = {x, y, z};
   double m0[3] = {0.0, 0.0, 0.0}, mp[3] = {0.0, 0.0, 0.0};
   bool amb = false;
+  // first stage from the velocity at the nodes (as k_semilag_tree_df)
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (per) xx[k] = wrap1(xx[k]);
+    px[k] = fma(half_tau, __ldg(p.vn + 3 * t + k), xx[k]);
+  }
 #pragma unroll 1
-  for (int st = 0; st < 2 * p.nrk; ++st) {
+  for (int st = 1; st < 2 * p.nrk; ++st) {
     double v[3], ev[3];
     amb |= eval_point_df<D, 3, true>(p.vel, px[0], px[1], px[2], per, mp, v, ev, slots);
     if ((st & 1) == 0) {

@@ -87,6 +87,7 @@ enum Slot {
   kMu,
   kFixList,
   kFixCount,
+  kVN,
   kNumSlots
 };
 
@@ -560,6 +561,15 @@ int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int ti
     a.nrk = nrk;
     a.periodic = bc;
     a.vals = vals;
+    {
+      // first RK stage: the velocity at the targets by sum factorisation
+      double* vn = nullptr;
+      TRY(scratch_t(ctx, kVN, N * 3, &vn));
+      ProfScope pv(ctx, "vel_at_nodes", s);
+      launch_eval_on_nodes(a.vel, a.con, bc, vn, s);
+      TRY(check_launch("velocity at nodes"));
+      a.vn = vn;
+    }
     TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
     TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
     a.fix_grid = ctx->num_sms * 8;
@@ -1016,6 +1026,21 @@ int tbslas_eval_tree(tbslas_ctx ctx, tbslas_tree tree, const double* pos_dev, in
   if (n > 0 && (!pos_dev || !out_dev)) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
   if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
   return eval_tree_dev(ctx, tree, pos_dev, n, out_dev, bc, (cudaStream_t)stream);
+}
+
+int tbslas_eval_tree_on_nodes(tbslas_ctx ctx, tbslas_tree src, tbslas_tree dst, double* out_dev,
+                              int bc, void* stream) {
+  TRY(check_tree(src));
+  TRY(check_tree(dst));
+  TRY(bind(ctx));
+  if (src->ctx != ctx || dst->ctx != ctx)
+    return fail(TBSLAS_ERR_INVALID_ARG, "trees belong to another context");
+  if (!out_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  cudaStream_t s = (cudaStream_t)stream;
+  ProfScope p(ctx, "eval_on_nodes", s);
+  launch_eval_on_nodes(src->view(), dst->view(), bc, out_dev, s);
+  return check_launch("eval on nodes");
 }
 
 int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_host, int64_t n,

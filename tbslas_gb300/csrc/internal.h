@@ -25,6 +25,7 @@ struct SemilagTreeArgs {
   int nrk;
   int periodic;
   double* vals;       // [Lc * Np] node values at the departure points
+  const double* vn;   // [Lc * Np][3] velocity at the targets (first RK stage) or null
   int64_t* fix_list;  // targets the double-float kernel hands to the FP64 pass
   unsigned long long* fix_count;
   int fix_grid;       // CTAs of the FP64 pass (persistent)
@@ -99,6 +100,25 @@ int ctx_F(tbslas_ctx ctx, int q, const double** F);
 int ctx_mu_scratch(tbslas_ctx ctx, size_t n, double** out);
 int ctx_vals_scratch(tbslas_ctx ctx, size_t n, double** out);
 Nodes1D ctx_nodes(int q);
+
+// node_eval.cu: src evaluated at every node of dst's leaves, [dst.L * Np][src.dof]
+// (bit-identical to the pointwise FP64 evaluation)
+void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic, double* out,
+                          cudaStream_t s);
+// Batched: one item per (job, destination leaf); max_q bounds both trees'
+// degrees over all jobs.
+struct NodeEvalJob {
+  TreeView src;
+  TreeView dst;
+  Nodes1D nodes;  // 1-D nodes of dst's degree
+  double* out;
+};
+struct NodeEvalItem {
+  int32_t job, pad;
+  int64_t leaf;
+};
+void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* items,
+                                int64_t n_items, int max_q, int periodic, cudaStream_t s);
 
 // Refit (refit.cu): node values -> coefficients through the separable
 // factors F = refit_factors(q) (4 D x D blocks on the device).

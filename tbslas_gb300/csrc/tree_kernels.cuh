@@ -154,8 +154,19 @@ __global__ void __launch_bounds__(128) k_semilag_tree_df(const SemilagTreeArgs a
   double px[3] = {x[0], x[1], x[2]};
   double m0[3] = {0.0, 0.0, 0.0}, mp[3] = {0.0, 0.0, 0.0};
   bool amb = false;
+  int st0 = 0;
+  if (a.vn) {
+    // first stage from the velocity at the nodes, bit-identical to the FP64
+    // path's v(X): X wrapped in place as eval_point does, the midpoint exact
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (per) x[k] = wrap1(x[k]);
+      px[k] = fma(half_tau, __ldg(a.vn + 3 * t + k), x[k]);
+    }
+    st0 = 1;
+  }
 #pragma unroll 1
-  for (int st = 0; st < 2 * a.nrk; ++st) {
+  for (int st = st0; st < 2 * a.nrk; ++st) {
     double v[3], ev[3];
     amb |= eval_point_df<D, 3, true>(a.vel, px[0], px[1], px[2], per, mp, v, ev, slots);
     if ((st & 1) == 0) {
