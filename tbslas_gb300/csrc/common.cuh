@@ -217,13 +217,13 @@ __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, doub
   const ThreadSlots ty = slots, tz{slots.s + D * slots.bs, slots.bs};
   cheb_T<D>(yi, T);
 #pragma unroll
-  for (int k = 0; k < D; ++k) ty.put(k, df_from_double(T[k]));
+  for (int k = 0; k < D; ++k) ty.put(k, df_split_bits(T[k]));
   cheb_T<D>(zi, T);
 #pragma unroll
-  for (int k = 0; k < D; ++k) tz.put(k, df_from_double(T[k]));
+  for (int k = 0; k < D; ++k) tz.put(k, df_split_bits(T[k]));
   cheb_T<D>(xi, T);
 #pragma unroll
-  for (int k = 0; k < D; ++k) tx[k] = df_from_double(T[k]);
+  for (int k = 0; k < D; ++k) tx[k] = df_split_bits(T[k]);
   df r[DOF];
   tri_sum_df_rows<D, DOF>(t.coeff2 + leaf * t.stride, tx, ty, tz, r);
 #pragma unroll

@@ -32,6 +32,28 @@ __device__ __forceinline__ df df_from_double(double x) {
 
 __device__ __forceinline__ double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
 
+// Split of an FP64 value into hi + lo with integer operations only (no FP64
+// pipe, which runs at 1/72 of the FP32 rate): hi = x with its significand
+// truncated to 24 bits, lo = the remaining 29 significand bits rounded to a
+// float.  |x - hi - lo| <= 2^-48 |x|; values below 2^-74 lose lo and values
+// below 2^-126 become 0 (absolute error < 2^-97, resp. 2^-126 -- far below
+// the sums' error bound).  For |x| < 2^128 (the callers pass Chebyshev values
+// in [-1, 1]).
+__device__ __forceinline__ df df_split_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  if (e < 897u) return df{0.f, 0.f};
+  const float hi = __uint_as_float(sign | ((e - 896u) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+  float lo = 0.f;
+  if (e >= 949u) {
+    const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e - 1075)
+    lo = __uint_as_float(__float_as_uint(__fmul_rn(__uint2float_rn((unsigned)(b & 0x1fffffffu)),
+                                                   scale)) | sign);
+  }
+  return df{hi, lo};
+}
+
 __device__ __forceinline__ df df_norm(df a) {
   const float s = __fadd_rn(a.hi, a.lo);
   return df{s, __fsub_rn(a.lo, __fsub_rn(s, a.hi))};
