@@ -44,7 +44,7 @@ struct tbslas_batch_s {
   RefitItem* d_ritems = nullptr;
   NodeEvalJob* d_njobs = nullptr;
   NodeEvalItem* d_nitems = nullptr;
-  int64_t n_nitems = 0;
+  int64_t nitem_begin[TBSLAS_MAX_DEGREE + 2] = {};  // items grouped by degree
   double* d_vn = nullptr;
   int64_t n_ritems = 0;
   int max_q = 0;
@@ -119,7 +119,11 @@ int enqueue_steps(tbslas_batch b, int nsteps, cudaStream_t s) {
   const int grid = b->num_sms * b->cps;
   for (int i = 0; i < nsteps; ++i) {
     unsigned long long* fix_count = b->d_counters + (int64_t)i * kPer + kBands;
-    launch_batch_eval_on_nodes(b->d_njobs, b->d_nitems, b->n_nitems, b->max_q, b->bc, s);
+    for (int q = 0; q <= TBSLAS_MAX_DEGREE; ++q) {
+      const int64_t n = b->nitem_begin[q + 1] - b->nitem_begin[q];
+      if (n > 0)
+        launch_batch_eval_on_nodes(b->d_njobs, b->d_nitems + b->nitem_begin[q], n, q, q, b->bc, s);
+    }
     for (int band = 0; band < kBands; ++band) {
       const int64_t n = b->band_begin[band + 1] - b->band_begin[band];
       if (n == 0) continue;
@@ -306,11 +310,22 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     if (e == cudaSuccess) e = cudaMalloc(&b->d_njobs, sizeof(NodeEvalJob) * n);
     if (e == cudaSuccess)
       e = cudaMemcpy(b->d_njobs, njobs.data(), sizeof(NodeEvalJob) * n, cudaMemcpyHostToDevice);
+    {
+      // group the items by degree (one launch per degree)
+      std::stable_sort(nitems.begin(), nitems.end(), [&](const NodeEvalItem& x, const NodeEvalItem& y) {
+        return b->h_probs[x.job].q < b->h_probs[y.job].q;
+      });
+      int64_t k = 0;
+      for (int q = 0; q <= TBSLAS_MAX_DEGREE + 1; ++q) {
+        while (k < (int64_t)nitems.size() && b->h_probs[nitems[k].job].q < q) ++k;
+        b->nitem_begin[q] = k;
+      }
+    }
     if (e == cudaSuccess) e = cudaMalloc(&b->d_nitems, sizeof(NodeEvalItem) * nitems.size());
     if (e == cudaSuccess)
       e = cudaMemcpy(b->d_nitems, nitems.data(), sizeof(NodeEvalItem) * nitems.size(),
                      cudaMemcpyHostToDevice);
-    b->n_nitems = (int64_t)nitems.size();
+
     if (e == cudaSuccess) e = cudaMalloc(&b->d_ts0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_fix, sizeof(int64_t) * std::max<int64_t>(off, 1));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);

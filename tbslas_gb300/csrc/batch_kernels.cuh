@@ -151,7 +151,7 @@ __device__ __forceinline__ void batch_dispatch_fp64(int q, const BatchProblem& p
 // Persistent CTAs take chunks of targets from an atomic counter; the chunk's
 // problem descriptor is staged in shared memory.
 template <int QLO, int QHI>
-__global__ void __launch_bounds__(256) k_batch_semilag(const BatchLaunch a) {
+__global__ void __launch_bounds__(256, 3) k_batch_semilag(const BatchLaunch a) {
   __shared__ BatchProblem sp;
   __shared__ int64_t s_item;
   extern __shared__ float2 s_slots[];  // 2 * (QHI + 1) elements per thread

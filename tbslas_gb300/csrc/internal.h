@@ -105,8 +105,8 @@ Nodes1D ctx_nodes(int q);
 // (bit-identical to the pointwise FP64 evaluation)
 void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic, double* out,
                           cudaStream_t s);
-// Batched: one item per (job, destination leaf); max_q bounds both trees'
-// degrees over all jobs.
+// Batched: one item per (job, destination leaf); the jobs of one launch
+// share the source degree q_src, max_q_dst bounds their destination degrees.
 struct NodeEvalJob {
   TreeView src;
   TreeView dst;
@@ -118,7 +118,8 @@ struct NodeEvalItem {
   int64_t leaf;
 };
 void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* items,
-                                int64_t n_items, int max_q, int periodic, cudaStream_t s);
+                                int64_t n_items, int q_src, int max_q_dst, int periodic,
+                                cudaStream_t s);
 
 // Refit (refit.cu): node values -> coefficients through the separable
 // factors F = refit_factors(q) (4 D x D blocks on the device).

@@ -16,17 +16,19 @@
 // and the same node and local coordinates, so every value is bit-identical to
 // the pointwise FP64 evaluation (eval_point).
 //
-// One CTA per destination leaf: each node's source leaf is found by the
-// usual key search (points outside the domain evaluate to 0); then, source
-// leaf by source leaf, the sub-grid of nodes it holds is evaluated with the
-// three passes in shared memory.  Runtime degree; FP64 (FP64 pipe).
+// One CTA per destination leaf.  Leaves tile the unit cube (tree_create
+// checks it), so the nodes a source leaf holds are those inside its box:
+// starting from the first node not yet evaluated, one key search finds its
+// source leaf, per-axis box tests give the sub-grid, and the three passes
+// evaluate it -- w in shared memory, then per (b, a) column v(., b, a) in
+// registers and every u of the column.  FP64 (FP64 pipe); templated on the
+// source degree (register arrays), runtime destination degree.
 #include <atomic>
 #include <climits>
 #include <cstring>
 #include <vector>
 
 #include "host_cheb.h"
-
 #include "internal.h"
 
 namespace tbg {
@@ -35,16 +37,18 @@ namespace {
 
 constexpr int kNodeEvalThreads = 256;
 
-__device__ __forceinline__ void cheb_T_rt(double xi, int D, double* T, int stride) {
-  // the operations of cheb_T<D>, with a runtime length
+template <int Ds>
+__device__ __forceinline__ void cheb_T_col(double xi, double* T, int stride) {
+  // the operations of cheb_T<Ds>, written to a strided column
   const bool ok = fabs(xi) <= 1.0;
   const double x = ok ? xi : 0.0;
   const double t0 = ok ? 1.0 : 0.0;
   T[0] = t0;
-  if (D > 1) T[stride] = x;
+  if (Ds > 1) T[stride] = x;
   const double x2 = 2.0 * x;
   double a = t0, b = x;
-  for (int k = 2; k < D; ++k) {
+#pragma unroll
+  for (int k = 2; k < Ds; ++k) {
     const double t = fma(x2, b, -a);
     T[k * stride] = t;
     a = b;
@@ -52,31 +56,32 @@ __device__ __forceinline__ void cheb_T_rt(double xi, int D, double* T, int strid
   }
 }
 
-__host__ __device__ constexpr size_t node_eval_smem(int Ds, int Dd) {
-  // doubles: coordinates 3*Dd, T tables 3*Ds*Dd, w: Ds(Ds+1)/2*Dd, v: Ds*Dd*Dd;
-  // ints: leaf per node Dd^3, index lists 3*Dd
-  return (size_t)(3 * Dd + 3 * Ds * Dd + Ds * (Ds + 1) / 2 * Dd + Ds * Dd * Dd) * 8 +
-         (size_t)(Dd * Dd * Dd + 3 * Dd) * 4;
+__host__ __device__ constexpr size_t node_eval_smem(int Ds, int Dd, int dof) {
+  // doubles: coordinates 3*Dd, T tables 3*Ds*Dd, w: dof*Ds(Ds+1)/2*Dd;
+  // ints: quantised coordinates 3*Dd, index lists 3*Dd; bytes: node state Dd^3
+  return (size_t)(3 * Dd + 3 * Ds * Dd + dof * Ds * (Ds + 1) / 2 * Dd) * 8 +
+         (size_t)(6 * Dd) * 4 + (size_t)(Dd * Dd * Dd + 15) / 16 * 16;
 }
 
 // One destination leaf (the whole CTA).  out: the destination tree's
 // [L * Dd^3][src.dof] array.
+template <int Ds>
 __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const TreeView& dst,
                                                    const Nodes1D& nodes, bool per, int64_t leaf,
                                                    double* __restrict__ out_all, double* sm) {
+  constexpr int NCs = Ds * (Ds + 1) * (Ds + 2) / 6, npair = Ds * (Ds + 1) / 2;
   __shared__ int s_first;
-  __shared__ unsigned s_mask[3];
   __shared__ int s_n[3];
-  const int Ds = S.q + 1, Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
-  const int NCs = Ds * (Ds + 1) * (Ds + 2) / 6, dof = S.dof;
+  const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
+  const int dof = S.dof;
   const int tid = threadIdx.x, bs = blockDim.x;
 
   double* sx = sm;                       // [3][Dd] wrapped node coordinates
   double* sT = sx + 3 * Dd;              // [3][Ds][Dd]: T_k of the listed indices
-  double* sw = sT + 3 * Ds * Dd;         // [pair(i,j)][Dd]
-  double* sv = sw + Ds * (Ds + 1) / 2 * Dd;  // [i][Dd][Dd]
-  int* sleaf = reinterpret_cast<int*>(sv + Ds * Dd * Dd);  // [Dd^3]
-  int* sidx = sleaf + Dd3;               // [3][Dd] index lists
+  double* sw = sT + 3 * Ds * Dd;         // [dof][pair(i,j)][Dd]
+  uint32_t* sq = reinterpret_cast<uint32_t*>(sw + dof * npair * Dd);  // [3][Dd] keys, ~0 outside
+  int* sidx = reinterpret_cast<int*>(sq + 3 * Dd);                     // [3][Dd] index lists
+  uint8_t* sdone = reinterpret_cast<uint8_t*>(sidx + 3 * Dd);          // [Dd^3]
 
   const Geom g = load_geom(dst.geom + leaf);
   const double h = 2.0 / g.w;
@@ -86,118 +91,124 @@ __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const Tree
     double c = o + h * nodes.x[i];
     if (per) c = wrap1(c);
     sx[tid] = c;
+    // the per-axis part of inside(); a point is inside iff all three are
+    const bool in = per ? (c >= 0.0 && c < 1.0) : (c >= 0.0 && c <= 1.0);
+    sq[tid] = in ? (uint32_t)quantise(c) : 0xffffffffu;
   }
   __syncthreads();
   double* out = out_all + leaf * (int64_t)Dd3 * dof;
   for (int p = tid; p < Dd3; p += bs) {
-    const double x = sx[p % Dd], y = sx[Dd + (p / Dd) % Dd], z = sx[2 * Dd + p / Dd2];
-    if (inside(x, y, z, per)) {
-      sleaf[p] = (int)find_leaf(S, morton3(quantise(x), quantise(y), quantise(z)));
-    } else {
-      sleaf[p] = -1;
+    const bool in = sq[p % Dd] != 0xffffffffu && sq[Dd + (p / Dd) % Dd] != 0xffffffffu &&
+                    sq[2 * Dd + p / Dd2] != 0xffffffffu;
+    sdone[p] = in ? 0 : 1;
+    if (!in)
       for (int l = 0; l < dof; ++l) out[(int64_t)p * dof + l] = 0.0;
-    }
   }
   __syncthreads();
 
   for (;;) {
     if (tid == 0) s_first = INT_MAX;
-    if (tid < 3) s_mask[tid] = 0u;
     __syncthreads();
     int first = INT_MAX;
     for (int p = tid; p < Dd3; p += bs)
-      if (sleaf[p] >= 0) {
+      if (!sdone[p]) {
         first = p;
         break;
       }
     if (first != INT_MAX) atomicMin(&s_first, first);
     __syncthreads();
-    if (s_first == INT_MAX) break;
-    const int V = sleaf[s_first];
-    for (int p = tid; p < Dd3; p += bs)
-      if (sleaf[p] == V) {
-        atomicOr(&s_mask[0], 1u << (p % Dd));
-        atomicOr(&s_mask[1], 1u << ((p / Dd) % Dd));
-        atomicOr(&s_mask[2], 1u << (p / Dd2));
-      }
-    __syncthreads();
+    const int p0 = s_first;
+    if (p0 == INT_MAX) break;
+    const int64_t V = find_leaf(S, morton3(sq[p0 % Dd], sq[Dd + (p0 / Dd) % Dd],
+                                           sq[2 * Dd + p0 / Dd2]));
+    const Geom vg = load_geom(S.geom + V);
+    // the box of V in key units: anchor * 2^21, side 2^21 / 2^depth = 2^22 / w
+    const uint32_t side = (uint32_t)(4194304.0 / vg.w);
     if (tid < 3) {
+      const double o = tid == 0 ? vg.x : (tid == 1 ? vg.y : vg.z);
+      const uint32_t lo = (uint32_t)(o * (double)kKeyScale);
       int n = 0;
-      for (int i = 0; i < Dd; ++i)
-        if (s_mask[tid] >> i & 1u) sidx[tid * Dd + n++] = i;
+      for (int i = 0; i < Dd; ++i) {
+        const uint32_t k = sq[tid * Dd + i];
+        if (k != 0xffffffffu && k >= lo && k - lo < side) sidx[tid * Dd + n++] = i;
+      }
       s_n[tid] = n;
     }
     __syncthreads();
     const int na = s_n[0], nb = s_n[1], nz = s_n[2];
-    const Geom vg = load_geom(S.geom + V);
-    // T tables of the listed indices: sT[ax][k][i'] (the local coordinate
-    // and recurrence of eval_point)
+    // T tables of the listed indices: sT[ax][k][i'] (local coordinate and
+    // recurrence of eval_point)
     if (tid < 3 * Dd) {
       const int ax = tid / Dd, i = tid - ax * Dd;
       const int n = ax == 0 ? na : (ax == 1 ? nb : nz);
       if (i < n) {
         const double c = sx[ax * Dd + sidx[ax * Dd + i]];
         const double o = ax == 0 ? vg.x : (ax == 1 ? vg.y : vg.z);
-        cheb_T_rt((c - o) * vg.w - 1.0, Ds, sT + ax * Ds * Dd + i, Dd);
+        cheb_T_col<Ds>((c - o) * vg.w - 1.0, sT + ax * Ds * Dd + i, Dd);
       }
     }
     __syncthreads();
     const double* Tx = sT;
     const double* Ty = sT + Ds * Dd;
     const double* Tz = sT + 2 * Ds * Dd;
-    const int npair = Ds * (Ds + 1) / 2;
-    for (int l = 0; l < dof; ++l) {
-      const double* c = S.coeff + (int64_t)V * S.stride + (int64_t)l * NCs;
-      // w(i,j,a') = sum_k c[i][j][k] T_k(x_a')
-      for (int o = tid; o < npair * na; o += bs) {
-        const int pr = o / na, ai = o - pr * na;
-        // pair index pr -> (i, j): rows of length Ds - i
-        int i = 0, rem = pr;
-        while (rem >= Ds - i) {
-          rem -= Ds - i;
-          ++i;
-        }
-        const int j = rem;
-        const int m = Ds - i;
-        const int base = NCs - m * (m + 1) * (m + 2) / 6 + j * m - (j * (j - 1)) / 2;
-        double w = 0.0;
-        for (int k = 0; k < m - j; ++k) w = fma(__ldg(c + base + k), Tx[k * Dd + ai], w);
-        sw[pr * Dd + ai] = w;
+    const double* cV = S.coeff + V * S.stride;
+    // w(l; i,j,a') = sum_k c[l][i][j][k] T_k(x_a')
+    for (int o = tid; o < dof * npair * na; o += bs) {
+      const int ai = o % na, r = o / na, pr = r % npair, l = r / npair;
+      int i = 0, rem = pr;  // pair index -> (i, j): rows of length Ds - i
+      while (rem >= Ds - i) {
+        rem -= Ds - i;
+        ++i;
       }
-      __syncthreads();
-      // v(i,b',a') = sum_j T_j(y_b') w(i,j,a')
-      for (int o = tid; o < Ds * nb * na; o += bs) {
-        const int ai = o % na, bi = (o / na) % nb, i = o / (na * nb);
-        const int prow = i * Ds - (i * (i - 1)) / 2;  // pair index of (i, 0)
-        double v = 0.0;
-        for (int j = 0; j < Ds - i; ++j) v = fma(Ty[j * Dd + bi], sw[(prow + j) * Dd + ai], v);
-        sv[(i * Dd + bi) * Dd + ai] = v;
-      }
-      __syncthreads();
-      // u(c',b',a') = sum_i T_i(z_c') v(i,b',a'), kept where the node's leaf is V
-      for (int o = tid; o < nz * nb * na; o += bs) {
-        const int ai = o % na, bi = (o / na) % nb, ci = o / (na * nb);
-        const int p = sidx[ai] + Dd * (sidx[Dd + bi] + Dd * sidx[2 * Dd + ci]);
-        if (sleaf[p] != V) continue;
-        double u = 0.0;
-        for (int i = 0; i < Ds; ++i) u = fma(Tz[i * Dd + ci], sv[(i * Dd + bi) * Dd + ai], u);
-        out[(int64_t)p * dof + l] = u;
-      }
-      __syncthreads();
+      const int j = rem, m = Ds - i;
+      const double* c =
+          cV + l * NCs + (NCs - m * (m + 1) * (m + 2) / 6 + j * m - (j * (j - 1)) / 2);
+      double w = 0.0;
+      for (int k = 0; k < m - j; ++k) w = fma(__ldg(c + k), Tx[k * Dd + ai], w);
+      sw[(l * npair + pr) * Dd + ai] = w;
     }
-    for (int p = tid; p < Dd3; p += bs)
-      if (sleaf[p] == V) sleaf[p] = -2;
+    __syncthreads();
+    // per column (l, b', a'): v(i) = sum_j T_j(y_b') w(l; i,j,a'), then
+    // u(c') = sum_i T_i(z_c') v(i) for every listed c'
+    for (int o = tid; o < dof * nb * na; o += bs) {
+      const int ai = o % na, r = o / na, bi = r % nb, l = r / nb;
+      const double* wl = sw + l * npair * Dd + ai;
+      double v[Ds];
+      int prow = 0;
+#pragma unroll
+      for (int i = 0; i < Ds; ++i) {
+        double s = 0.0;
+#pragma unroll
+        for (int j = 0; j < Ds - i; ++j) s = fma(Ty[j * Dd + bi], wl[(prow + j) * Dd], s);
+        v[i] = s;
+        prow += Ds - i;
+      }
+      const int pab = sidx[ai] + Dd * sidx[Dd + bi];
+      for (int ci = 0; ci < nz; ++ci) {
+        double u = 0.0;
+#pragma unroll
+        for (int i = 0; i < Ds; ++i) u = fma(Tz[i * Dd + ci], v[i], u);
+        out[(int64_t)(pab + Dd2 * sidx[2 * Dd + ci]) * dof + l] = u;
+      }
+    }
+    for (int o = tid; o < nz * nb * na; o += bs) {
+      const int ai = o % na, r = o / na, bi = r % nb, ci = r / nb;
+      sdone[sidx[ai] + Dd * (sidx[Dd + bi] + Dd * sidx[2 * Dd + ci])] = 1;
+    }
     __syncthreads();
   }
 }
 
+template <int Ds>
 __global__ void __launch_bounds__(kNodeEvalThreads) k_eval_on_nodes(const NodeEvalJob j,
                                                                     int periodic) {
   extern __shared__ __align__(16) double sm[];
-  eval_on_nodes_leaf(j.src, j.dst, j.nodes, periodic != 0, blockIdx.x, j.out, sm);
+  eval_on_nodes_leaf<Ds>(j.src, j.dst, j.nodes, periodic != 0, blockIdx.x, j.out, sm);
 }
 
-// Batched: one CTA per (job, destination leaf) item.
+// Batched: one CTA per (job, destination leaf) item; the jobs of one launch
+// share the source degree Ds.
+template <int Ds>
 __global__ void __launch_bounds__(kNodeEvalThreads) k_batch_eval_on_nodes(
     const NodeEvalJob* __restrict__ jobs, const NodeEvalItem* __restrict__ items, int periodic) {
   extern __shared__ __align__(16) double sm[];
@@ -205,21 +216,60 @@ __global__ void __launch_bounds__(kNodeEvalThreads) k_batch_eval_on_nodes(
   const NodeEvalItem it = items[blockIdx.x];
   if (threadIdx.x == 0) sj = jobs[it.job];
   __syncthreads();
-  eval_on_nodes_leaf(sj.src, sj.dst, sj.nodes, periodic != 0, it.leaf, sj.out, sm);
+  eval_on_nodes_leaf<Ds>(sj.src, sj.dst, sj.nodes, periodic != 0, it.leaf, sj.out, sm);
 }
 
-void allow_node_smem(const void* kernel, std::atomic<uint64_t>& done) {
+constexpr int kMaxD = TBSLAS_MAX_DEGREE + 1;
+
+// Raise a kernel's dynamic shared-memory limit to its largest launch, once
+// per device.
+void allow_smem(const void* kernel, size_t bytes, std::atomic<uint64_t>& done) {
   int dev = 0;
   cudaGetDevice(&dev);
   const uint64_t bit = 1ull << (dev & 63);
   if (!(done.load() & bit)) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)node_eval_smem(TBSLAS_MAX_DEGREE + 1, TBSLAS_MAX_DEGREE + 1));
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     done.fetch_or(bit);
   }
 }
 
-std::atomic<uint64_t> g_smem_nodes{0}, g_smem_batch_nodes{0};
+template <int Ds>
+void launch_single(const NodeEvalJob& j, int64_t L, int periodic, cudaStream_t s) {
+  static std::atomic<uint64_t> done{0};
+  allow_smem((const void*)k_eval_on_nodes<Ds>, node_eval_smem(Ds, kMaxD, 3), done);
+  k_eval_on_nodes<Ds><<<(unsigned)L, kNodeEvalThreads,
+                        node_eval_smem(Ds, j.dst.q + 1, j.src.dof), s>>>(j, periodic);
+}
+
+template <int Ds>
+void launch_batched(const NodeEvalJob* jobs, const NodeEvalItem* items, int64_t n, int max_qd,
+                    int periodic, cudaStream_t s) {
+  static std::atomic<uint64_t> done{0};
+  allow_smem((const void*)k_batch_eval_on_nodes<Ds>, node_eval_smem(Ds, kMaxD, 3), done);
+  k_batch_eval_on_nodes<Ds><<<(unsigned)n, kNodeEvalThreads, node_eval_smem(Ds, max_qd + 1, 3),
+                              s>>>(jobs, items, periodic);
+}
+
+template <int Ds>
+void dispatch_single(int ds, const NodeEvalJob& j, int64_t L, int periodic, cudaStream_t s) {
+  if constexpr (Ds <= kMaxD) {
+    if (ds == Ds)
+      launch_single<Ds>(j, L, periodic, s);
+    else
+      dispatch_single<Ds + 1>(ds, j, L, periodic, s);
+  }
+}
+
+template <int Ds>
+void dispatch_batched(int ds, const NodeEvalJob* jobs, const NodeEvalItem* items, int64_t n,
+                      int max_qd, int periodic, cudaStream_t s) {
+  if constexpr (Ds <= kMaxD) {
+    if (ds == Ds)
+      launch_batched<Ds>(jobs, items, n, max_qd, periodic, s);
+    else
+      dispatch_batched<Ds + 1>(ds, jobs, items, n, max_qd, periodic, s);
+  }
+}
 
 }  // namespace
 
@@ -233,17 +283,14 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
   const std::vector<double> x = cheb_nodes_1d(dst.q);
   for (int i = 0; i <= dst.q; ++i) j.nodes.x[i] = x[i];
   j.out = out;
-  allow_node_smem((const void*)k_eval_on_nodes, g_smem_nodes);
-  k_eval_on_nodes<<<(unsigned)dst.L, kNodeEvalThreads, node_eval_smem(src.q + 1, dst.q + 1),
-                    s>>>(j, periodic);
+  dispatch_single<1>(src.q + 1, j, dst.L, periodic, s);
 }
 
 void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* items,
-                                int64_t n_items, int max_q, int periodic, cudaStream_t s) {
+                                int64_t n_items, int q_src, int max_q_dst, int periodic,
+                                cudaStream_t s) {
   if (n_items <= 0) return;
-  allow_node_smem((const void*)k_batch_eval_on_nodes, g_smem_batch_nodes);
-  k_batch_eval_on_nodes<<<(unsigned)n_items, kNodeEvalThreads,
-                          node_eval_smem(max_q + 1, max_q + 1), s>>>(jobs, items, periodic);
+  dispatch_batched<1>(q_src + 1, jobs, items, n_items, max_q_dst, periodic, s);
 }
 
 }  // namespace tbg

@@ -136,12 +136,13 @@ void launch_semilag_tree(const SemilagTreeArgs& a, cudaStream_t s) {
 // of its leaf is appended to fix_list and recomputed by k_semilag_fix with
 // the FP64 kernel body, so every leaf choice is the FP64 path's.  Values
 // differ from the FP64 path by the sums' rounding (~1e-14).
-// Six 128-thread CTAs per SM (<= 80 registers): the row loads of the sums
-// wait on L1, and 24 resident warps hide that better than 16 warps without
-// spills (measured on GB300: +11% at q = 14, +5% at q = 8; five CTAs per SM
-// was slower than four).
+// Seven (degree > 9) or eight 128-thread CTAs per SM (<= 72 / 64
+// registers): the row loads of the sums wait on L1, and 28-32 resident warps
+// hide that better than 16 warps without spills (measured on GB300: q = 14
+// 309 -> 354 M points/s, q = 8 787 -> 879 M; five CTAs per SM was slower
+// than four).
 template <int D>
-__global__ void __launch_bounds__(128, 6) k_semilag_tree_df(const SemilagTreeArgs a) {
+__global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(const SemilagTreeArgs a) {
   constexpr int NP = D * D * D;
   extern __shared__ float2 s_slots[];
   const ThreadSlots slots{s_slots + threadIdx.x, (int)blockDim.x};
