@@ -81,6 +81,10 @@ def bytes_per_point_tree(q, vel_leaves, con_leaves):
 # first velocity sits on a node (exact read).
 GRID_FLOPS_PER_POINT = (36 + 3 * 144) + (36 + 144) + 18
 GRID_BYTES_PER_POINT = 40  # 3 velocity + 1 concentration read, 1 written (FP64)
+# double-float multiply-adds per node of the periodic grid step: 84 per
+# component (64 + 16 + 4) at the midpoint (3 components) and the departure
+# point (1)
+GRID_DF_MACS_PER_POINT = 4 * 84
 
 
 # ---------------------------------------------------------------------------
@@ -326,6 +330,67 @@ def run_gpu(args, wl, rank, world, local_rank):
     prof = ctx.profile_totals()
     ctx.profile(False)
     points = wl.points_per_step * args.steps
+
+    fp64_targets = None if is_grid else ctx.last_fp64_targets()
+    # the same step with every Chebyshev sum in FP64 (TBSLAS_SUMS_FP64), timed
+    # the same way on a copy of the initial state, plus its distance from the
+    # default double-float step after one step
+    fp64, first64 = None, None
+    if is_grid and wl.bc == 1:
+        # the periodic grid step with FP64 stencil sums (TBSLAS_SUMS_FP64)
+        gb = [con0.clone(), torch.empty_like(con0)]
+        ctx.sums = tb.SUMS_FP64
+        try:
+            tb.semilag_grid(ctx, vel, gb[0], N, wl.dt, 1, wl.bc, out=gb[1])
+            torch.cuda.synchronize()
+            g64 = gb[1].cpu().numpy().ravel()
+            n64 = max(3, min(args.steps, 10))
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for i in range(n64):
+                flush.fill_(float(i))
+                tb.semilag_grid(ctx, vel, gb[i % 2], N, wl.dt, 1, wl.bc, out=gb[(i + 1) % 2])
+            f1.record(stream)
+            torch.cuda.synchronize()
+        finally:
+            ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        ms64 = f0.elapsed_time(f1) / n64
+        fp64 = {"value": wl.points_per_step / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64,
+                "steps": n64,
+                "rel_diff_vs_default_first_step": float(np.abs(g64 - first).max()
+                                                        / np.abs(g64).max()),
+                "note": "TBSLAS_SUMS_FP64: the stencil sums in FP64"}
+        del gb
+    if not is_grid:
+        tc64 = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
+        ctx.sums = tb.SUMS_FP64
+        try:
+            tb.solve_semilag_in_situ(vf, tc64, 1, wl.dt, 1)
+            torch.cuda.synchronize()
+            first64 = tc64.get_coeffs()
+            n64 = max(3, min(args.steps, 10))
+            for i in range(3):
+                tb.solve_semilag_in_situ(vf, tc64, i + 2, wl.dt, 1)
+            torch.cuda.synchronize()
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for i in range(n64):
+                flush.fill_(float(i))
+                tb.solve_semilag_in_situ(vf, tc64, i + 5, wl.dt, 1)
+            f1.record(stream)
+            torch.cuda.synchronize()
+        finally:
+            ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        ms64 = f0.elapsed_time(f1) / n64
+        fp64 = {"value": wl.points_per_step / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64,
+                "steps": n64,
+                "rel_diff_vs_default_first_step": float(np.abs(first64 - first).max()
+                                                        / np.abs(first64).max()),
+                "note": "TBSLAS_SUMS_FP64: every Chebyshev sum in FP64 (departure points and "
+                        "node values bit-identical to the oracle)"}
+        del tc64
     tot_points, tot_sec = aggregate(points, ms * 1e-3, world)
     value = tot_points / tot_sec
     gpu_launches = int(sum(v[1] for v in prof.values()))  # same step sequence as the timed loop
@@ -373,7 +438,28 @@ def run_gpu(args, wl, rank, world, local_rank):
     hbm = {"achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
            "frac": achieved_gbs / peaks["hbm_gbs"], "peak_source": peak_src}
     per_kernel = {k: v[2] / args.steps for k, v in prof.items()}
-    if is_grid:
+    if is_grid and wl.bc == 1:
+        # periodic grid step: stencil sums in double-float on the FP32 pipe
+        fp32_peak = ctx.fp32_fma_peak()
+        macs = GRID_DF_MACS_PER_POINT
+        fp32_flops = 2 * DF_FP32_INSTR_PER_MAC * macs
+        achieved32 = fp32_flops * kernel_points / (launch_ms * 1e-3) / 1e12
+        roofline = {
+            "kernel": dominant + " (hi/lo split of the grids + double-float stencil sums)",
+            "bound": "fp32",
+            "achieved": achieved32, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+            "frac": achieved32 / (fp32_peak / 1e12),
+            "peak_source": "FP32 FMA throughput measured in this run (tbslas_fp32_fma_peak)",
+            "counting": "%d double-float multiply-adds per point x %d FP32 instructions, "
+                        "each counted as 2 FLOP" % (macs, DF_FP32_INSTR_PER_MAC),
+            "fp64_equivalent": {
+                "achieved": achieved_tflops, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                "frac": achieved_tflops / (fp64_peak / 1e12),
+                "algorithmic_flops_per_point": flops_kernel},
+            "algorithmic_bytes_per_point": bytes_kernel,
+            "launch_ms": launch_ms, "traffic": traffic, "hbm": hbm,
+            "kernels_ms_per_step": per_kernel}
+    elif is_grid:
         roofline = {
             "kernel": dominant, "bound": "fp64",
             "achieved": achieved_tflops, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
@@ -420,6 +506,10 @@ def run_gpu(args, wl, rank, world, local_rank):
             got = first[:k]
         accuracy = {"rel_err_vs_oracle": float(np.abs(got - ref).max() / np.abs(ref).max()),
                     "compared": "first GPU step vs the oracle on the CPU-baseline sample"}
+        if first64 is not None:
+            g64 = first64[:k]
+            accuracy["fp64_sums_rel_err_vs_oracle"] = float(np.abs(g64 - ref).max()
+                                                            / np.abs(ref).max())
         cpu.pop("seconds", None)
 
     cfg = wl.describe()
@@ -432,7 +522,9 @@ def run_gpu(args, wl, rank, world, local_rank):
             "e2e": {"value": e_points / e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
-            "clocks": clk.summary(), "gpu_launches": gpu_launches}
+            "fp64_sums": fp64, "clocks": clk.summary(), "gpu_launches": gpu_launches}
+    if fp64_targets is not None:
+        line["fp64_recomputed_targets_last_step"] = int(fp64_targets)
     print(json.dumps(line))
     assert ctx.check() == 0
 

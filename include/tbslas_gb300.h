@@ -94,6 +94,26 @@ int tbslas_profile_count(tbslas_ctx ctx, int* n);
  * name: valid until the next reset or destroy of ctx. */
 int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launches,
                        int64_t* kernels, double* total_ms);
+/* Arithmetic of the in-situ step's Chebyshev sums (targets, RK2 updates,
+ * Morton keys, leaf search and leaf-local coordinates are FP64 either way):
+ *  - TBSLAS_SUMS_DOUBLE_FLOAT (default): the sums at the midpoint and the
+ *    departure point run as double-float (hi + lo float pairs, 48-bit
+ *    significand, error-free products and sums) on the FP32 pipe -- GB300
+ *    runs FP64 at 1/72 of its FP32 rate.  Every coordinate carries a
+ *    rigorous bound on its distance from the all-FP64 one; targets whose
+ *    lookup that bound makes ambiguous are recomputed in FP64, so every leaf
+ *    choice equals the FP64 path's.  Values agree with the FP64 path to
+ *    ~1e-14 relative (the parity tolerance is 1e-12).
+ *  - TBSLAS_SUMS_FP64: every sum in FP64 in the reference's order; departure
+ *    points and node values bit-identical to the oracle.
+ * The first RK2 stage (the velocity at the nodes) is FP64 and exact in both. */
+enum { TBSLAS_SUMS_DOUBLE_FLOAT = 0, TBSLAS_SUMS_FP64 = 1 };
+int tbslas_ctx_set_sums(tbslas_ctx ctx, int mode);
+int tbslas_ctx_get_sums(tbslas_ctx ctx, int* mode);
+/* Targets of the last double-float in-situ step on ctx that were recomputed
+ * in FP64 (ambiguous lookups); synchronises the device.  Diagnostic. */
+int tbslas_ctx_last_fp64_targets(tbslas_ctx ctx, int64_t* n);
+
 /* Measured FP64 FMA throughput of the device (FLOP/s, 2 per FMA): the
  * roofline denominator of the FP64-pipe-bound kernels.  Diagnostic; no
  * reference counterpart. */

@@ -20,6 +20,7 @@ from .capi import BC_FREESPACE, BC_PERIODIC, call
 
 FreeSpace = BC_FREESPACE
 Periodic = BC_PERIODIC
+SUMS_DOUBLE_FLOAT, SUMS_FP64 = 0, 1
 
 
 def n_coeff(q):
@@ -113,6 +114,24 @@ class Context:
         f = ctypes.c_double(0)
         call("tbslas_fp64_fma_peak", self.handle, ctypes.byref(f))
         return f.value
+
+    @property
+    def sums(self):
+        """Arithmetic of the in-situ step's Chebyshev sums: SUMS_DOUBLE_FLOAT
+        (default) or SUMS_FP64 (bit-identical to the oracle)."""
+        m = ctypes.c_int(0)
+        call("tbslas_ctx_get_sums", self.handle, ctypes.byref(m))
+        return m.value
+
+    @sums.setter
+    def sums(self, mode):
+        call("tbslas_ctx_set_sums", self.handle, int(mode))
+
+    def last_fp64_targets(self):
+        """Targets of the last double-float in-situ step recomputed in FP64."""
+        n = ctypes.c_int64(0)
+        call("tbslas_ctx_last_fp64_targets", self.handle, ctypes.byref(n))
+        return n.value
 
     def fp32_fma_peak(self):
         """Measured FP32 FMA throughput, FLOP/s."""

@@ -38,6 +38,9 @@ SIGNATURES = {
     "tbslas_profile_get": [_vp, _i32, _c.POINTER(_c.c_char_p), _i64p, _i64p, _c.POINTER(_f64)],
     "tbslas_fp64_fma_peak": [_vp, _c.POINTER(_f64)],
     "tbslas_fp32_fma_peak": [_vp, _c.POINTER(_f64)],
+    "tbslas_ctx_set_sums": [_vp, _i32],
+    "tbslas_ctx_get_sums": [_vp, _c.POINTER(_i32)],
+    "tbslas_ctx_last_fp64_targets": [_vp, _c.POINTER(_i64)],
     "tbslas_cheb_nodes": [_i32, _vp],
     "tbslas_pt2coeff_matrix": [_i32, _vp],
     "tbslas_tree_create": [_vp, _i64, _vp, _vp, _i32, _i32, _c.POINTER(_vp)],

@@ -92,7 +92,7 @@ extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbsl
   int64_t ncf = 0;
   tree_coeff(con, &coeff, &ncf);
   tree_coeff2(con, &coeff2);
-  launch_refit(vals, F, q, tc.L, 1, tc.stride, coeff, coeff2, s);
+  launch_refit(vals, F, q, tc.L, 1, tc.stride, coeff, coeff2, ctx_err(ctx), s);
   return launched("refit launch");
 }
 

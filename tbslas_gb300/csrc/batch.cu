@@ -270,7 +270,7 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     if (st != TBSLAS_OK) break;
     float2* coeff2 = nullptr;
     tree_coeff2(con[i], &coeff2);
-    jobs.push_back(RefitJob{nullptr, F, coeff, coeff2, p.con.L, p.con.stride, p.q, 1});
+    jobs.push_back(RefitJob{nullptr, F, coeff, coeff2, ctx_err(ctx), p.con.L, p.con.stride, p.q, 1});
     b->max_q = std::max(b->max_q, p.q);
     for (int64_t r = 0; r < p.con.L; ++r) ritems.push_back(RefitItem{i, 0, r});
     NodeEvalJob nj;
@@ -412,7 +412,8 @@ int tbslas_batch_autotune(tbslas_batch b, int* block, int* targets_per_item, int
                            : cudaMemcpyAsync(b->con_coeff[i], backup + o, bytes,
                                              cudaMemcpyDeviceToDevice, s);
       if (e != cudaSuccess) return e;
-      if (!save) launch_split(b->con_coeff[i], b->con_coeff2[i], b->con_coeff_n[i], s);
+      if (!save)
+        launch_split(b->con_coeff[i], b->con_coeff2[i], b->con_coeff_n[i], ctx_err(b->ctx), s);
       o += b->con_coeff_n[i];
     }
     return cudaSuccess;

@@ -107,7 +107,8 @@ __device__ __forceinline__ void batch_target_df(const BatchProblem& p, int64_t t
   if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = ((int64_t)prob << kFixShift) | t;
 }
 
-// One target of one problem in FP64: the arithmetic of k_semilag_tree<D>.
+// One target of one problem in FP64: the arithmetic of k_semilag_tree<D>
+// (first stage from the node grid).
 template <int D>
 __device__ __forceinline__ void batch_target(const BatchProblem& p, int64_t t, double tau,
                                              bool per) {
@@ -119,7 +120,7 @@ __device__ __forceinline__ void batch_target(const BatchProblem& p, int64_t t, d
   double x = g.x + h * p.nodes.x[pi % D];
   double y = g.y + h * p.nodes.x[(pi / D) % D];
   double z = g.z + h * p.nodes.x[pi / (D * D)];
-  rk2_backtrace<D>(p.vel, x, y, z, tau, p.nrk, per);
+  rk2_backtrace_from_node<D>(p.vel, p.vn + 3 * t, x, y, z, tau, p.nrk, per);
   double c[1];
   eval_point<D, 1>(p.con, x, y, z, per, c);
   p.vals[t] = c[0];

@@ -88,6 +88,8 @@ enum Slot {
   kFixList,
   kFixCount,
   kVN,
+  kGridV2,
+  kGridC2,
   kNumSlots
 };
 
@@ -123,6 +125,7 @@ struct tbslas_ctx_s {
   uint32_t* d_err = nullptr;
   DevBuf slots[kNumSlots];
   double* d_F[TBSLAS_MAX_DEGREE + 1] = {};  // separable refit factors per degree
+  int sums = TBSLAS_SUMS_DOUBLE_FLOAT;       // arithmetic of the in-situ step's sums
   bool profile = false;
   std::vector<ProfRecord> prof_pending;
   std::vector<cudaEvent_t> prof_pool;
@@ -513,7 +516,7 @@ int refit_dev(tbslas_ctx ctx, tbslas_tree tree, const double* vals, cudaStream_t
   TRY(device_F(ctx, tree->q, &F));
   ProfScope p(ctx, "refit", s, tree->dof == 3 ? 2 : 1);
   launch_refit(vals, F, tree->q, tree->L * tree->dof, tree->dof, tree->stride, tree->d_coeff,
-               tree->d_coeff2, s);
+               tree->d_coeff2, ctx->d_err, s);
   TRY(check_launch("refit"));
   if (tree->dof == 3) {  // a velocity-shaped tree: its norms feed the double-float bounds
     k_cnorm<<<blocks_for(tree->L * 3, 128), 128, 0, s>>>(tree->d_coeff, tree->L, 3,
@@ -530,6 +533,24 @@ int collect_dev(tbslas_tree tree, double* out, cudaStream_t s) {
   ProfScope p(tree->ctx, "collect", s);
   k_collect<<<blocks_for(n, 256), 256, 0, s>>>(tree->view(), nodes_1d(tree->q), tree->q + 1, out);
   return check_launch("collect");
+}
+
+// The grid step: double-float stencil sums on periodic grids (unless the
+// context asks for FP64 sums), FP64 otherwise.
+int semilag_grid_dev(tbslas_ctx ctx, const double* vel, const double* con, double* cout,
+                     int n_reg, double tau, int nrk, int bc, cudaStream_t s) {
+  if (bc == TBSLAS_BC_PERIODIC && ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT) {
+    const int64_t n3 = (int64_t)n_reg * n_reg * n_reg;
+    float2 *v2, *c2;
+    TRY(scratch_t(ctx, kGridV2, n3 * 3, &v2));
+    TRY(scratch_t(ctx, kGridC2, n3, &c2));
+    ProfScope p(ctx, "semilag_grid", s, 3);
+    launch_semilag_grid_df(vel, con, cout, n_reg, tau, nrk, v2, c2, ctx->d_err, ctx->num_sms, s);
+    return check_launch("semilag_grid");
+  }
+  ProfScope p(ctx, "semilag_grid", s);
+  launch_semilag_grid(vel, con, cout, n_reg, tau, nrk, bc, s);
+  return check_launch("semilag_grid");
 }
 
 int check_tree(tbslas_tree t) {
@@ -573,8 +594,13 @@ int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int ti
     TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
     TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
     a.fix_grid = ctx->num_sms * 8;
-    ProfScope p(ctx, "semilag_tree", s, 2);
-    g_kernels[con->q].semilag_df(a, s);
+    if (ctx->sums == TBSLAS_SUMS_FP64) {
+      ProfScope p(ctx, "semilag_tree", s, 1);
+      g_kernels[con->q].semilag(a, s);
+    } else {
+      ProfScope p(ctx, "semilag_tree", s, 2);
+      g_kernels[con->q].semilag_df(a, s);
+    }
     TRY(check_launch("semilag_tree"));
   } else {
     double *X, *Xdep, *vt;
@@ -661,7 +687,7 @@ int build_tree(tbslas_tree t, const double* anchor, const int32_t* depth) {
 // Refresh what is derived from a tree's coefficients: the double-float split
 // and the per-leaf coefficient norms.
 int derived_coeffs(tbslas_tree t, cudaStream_t s) {
-  launch_split(t->d_coeff, t->d_coeff2, t->L * t->stride, s);
+  launch_split(t->d_coeff, t->d_coeff2, t->L * t->stride, t->ctx->d_err, s);
   const int64_t n = t->L * t->dof;
   k_cnorm<<<blocks_for(n, 128), 128, 0, s>>>(t->d_coeff, t->L, t->dof, (int)n_coeff(t->q),
                                              t->stride, t->d_cnorm);
@@ -780,6 +806,8 @@ int ctx_info(tbslas_ctx ctx, int* device, int* num_sms) {
   return TBSLAS_OK;
 }
 
+uint32_t* ctx_err(tbslas_ctx ctx) { return ctx ? ctx->d_err : nullptr; }
+
 int ctx_F(tbslas_ctx ctx, int q, const double** F) {
   TRY(bind(ctx));
   return device_F(ctx, q, F);
@@ -897,6 +925,33 @@ int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launch
   if (launches) *launches = t.launches;
   if (kernels) *kernels = t.kernels;
   if (total_ms) *total_ms = t.ms;
+  return TBSLAS_OK;
+}
+
+int tbslas_ctx_set_sums(tbslas_ctx ctx, int mode) {
+  TRY(bind(ctx));
+  if (mode != TBSLAS_SUMS_DOUBLE_FLOAT && mode != TBSLAS_SUMS_FP64)
+    return fail(TBSLAS_ERR_INVALID_ARG, "sums mode %d", mode);
+  ctx->sums = mode;
+  return TBSLAS_OK;
+}
+
+int tbslas_ctx_get_sums(tbslas_ctx ctx, int* mode) {
+  TRY(bind(ctx));
+  if (!mode) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
+  *mode = ctx->sums;
+  return TBSLAS_OK;
+}
+
+int tbslas_ctx_last_fp64_targets(tbslas_ctx ctx, int64_t* n) {
+  TRY(bind(ctx));
+  if (!n) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
+  *n = 0;
+  if (!ctx->slots[kFixCount].p) return TBSLAS_OK;
+  unsigned long long c = 0;
+  CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(&c, ctx->slots[kFixCount].p, sizeof(c), cudaMemcpyDeviceToHost));
+  *n = (int64_t)c;
   return TBSLAS_OK;
 }
 
@@ -1175,9 +1230,8 @@ int tbslas_semilag_grid(tbslas_ctx ctx, const double* vel_dev, const double* con
                         void* stream) {
   TRY(check_grid_args(ctx, vel_dev, con_dev, con_out_dev, n_reg, dt, nrk, bc));
   const double tau = (-dt - 0.0) / nrk;
-  ProfScope p(ctx, "semilag_grid", (cudaStream_t)stream);
-  launch_semilag_grid(vel_dev, con_dev, con_out_dev, n_reg, tau, nrk, bc, (cudaStream_t)stream);
-  return check_launch("semilag_grid");
+  return semilag_grid_dev(ctx, vel_dev, con_dev, con_out_dev, n_reg, tau, nrk, bc,
+                          (cudaStream_t)stream);
 }
 
 int tbslas_semilag_grid_host(tbslas_ctx ctx, const double* vel_host, const double* con_host,
@@ -1193,11 +1247,7 @@ int tbslas_semilag_grid_host(tbslas_ctx ctx, const double* vel_host, const doubl
   CUDA_TRY(cudaMemcpyAsync(vel, vel_host, n3 * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemcpyAsync(con, con_host, n3 * sizeof(double), cudaMemcpyHostToDevice, s));
   const double tau = (-dt - 0.0) / nrk;
-  {
-    ProfScope p(ctx, "semilag_grid", s);
-    launch_semilag_grid(vel, con, cout, n_reg, tau, nrk, bc, s);
-    TRY(check_launch("semilag_grid"));
-  }
+  TRY(semilag_grid_dev(ctx, vel, con, cout, n_reg, tau, nrk, bc, s));
   CUDA_TRY(cudaMemcpyAsync(con_out_host, cout, n3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   return TBSLAS_OK;

@@ -178,14 +178,31 @@ __device__ __forceinline__ void eval_point(const TreeView& t, double& x, double&
 
 // Double-float evaluation of DOF components at one point, for the fused
 // step; `slots` holds 2*D shared-memory elements of this thread (the y and z
-// Chebyshev values of tri_sum_df_rows).  m[a] bounds, per axis, the distance between this point and the one
-// an all-FP64 computation would have produced (0: identical).  Returns true
-// when the lookup is ambiguous -- within m[a] of a face of the leaf on some
-// axis, or just outside the domain -- so the caller must recompute the target
-// in FP64.  With ERR, err[l] receives a bound on |out[l] - out_fp64[l]|: the
-// sums' rounding (1e-13 sum|c|, |T_k| <= 1) plus the change of the expansion
-// over the position uncertainty (|dT_k/dxi| <= k^2 on [-1,1]).
-constexpr double kDfSumErr = 1e-13;
+// Chebyshev values of tri_sum_df_rows).  m[a] bounds, per axis, the distance
+// between this point and the one an all-FP64 computation would have produced
+// (0: identical).  Returns true when the lookup is ambiguous -- within m[a] of
+// a face of the leaf on some axis, or just outside the domain -- so the caller
+// must recompute the target in FP64.  With ERR, err[l] receives a bound on
+// |out[l] - out_fp64[l]|: the sums' rounding (df_sum_err<D>() sum|c|, since
+// |T_k| <= 1) plus the change of the expansion over the position uncertainty
+// (|dT_k/dxi| <= k^2 on [-1,1]).
+//
+// df_sum_err: worst-case error of the three nested double-float sums relative
+// to S = sum |c T T T|, with u = 2^-24.  One df_fma_acc of a row of n terms
+// forms each product to 9 u^2 |c t| (two FMA roundings at <= 3u|ct| and 4u|ct|,
+// the dropped lo*lo term, the operands' splits) and adds it with an exact
+// TwoSum; the low word collects the product and TwoSum errors (|lo_k| <=
+// (k+4) u S) and each of its two additions rounds at <= u |lo|, so a row
+// carries <= (n^2/2 + 4.5 n + 13) u^2 S, df_norm included.  The i, j, k
+// levels add one such term each (the inner errors enter the outer sums with
+// weights |T| <= 1), and the FP64 path's own rounding (<= 3 D 2^-53 S) and the
+// splits of T and c add < 10 u^2 S.  So |df - fp64| <= (3 (D^2/2 + 4.5 D + 13)
+// + 10) 2^-48 S: 2.1e-12 at q = 14.  (Observed errors are ~1e-16 S; the bound
+// only sizes the ambiguity margins.)
+template <int D>
+__host__ __device__ constexpr double df_sum_err() {
+  return (3.0 * (0.5 * D * D + 4.5 * D + 13.0) + 10.0) * 0x1p-48;
+}
 
 template <int D, int DOF, bool ERR>
 __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, double& y, double& z,
@@ -231,7 +248,7 @@ __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, doub
     out[l] = df_to_double(r[l]);
     if (ERR) {
       const double cn = __ldg(t.cnorm + leaf * DOF + l);
-      err[l] = cn * (kDfSumErr + (double)((D - 1) * (D - 1)) * g.w * mmax);
+      err[l] = cn * (df_sum_err<D>() + (double)((D - 1) * (D - 1)) * g.w * mmax);
     }
   }
   return amb;
@@ -262,6 +279,14 @@ struct Nodes1D {
 enum : uint32_t {
   kErrBarrierTimeout = 1u << 0,
   kErrBadLeaf = 1u << 1,
+  // a coefficient or grid value with |x| >= 2^100 (or not finite) met a
+  // double-float split; the double-float results are then meaningless (use
+  // TBSLAS_SUMS_FP64)
+  kErrDfRange = 1u << 2,
 };
+
+__device__ __forceinline__ void check_df_range(double x, uint32_t* err) {
+  if (err && !(fabs(x) < 0x1p100)) atomicOr(err, kErrDfRange);
+}
 
 }  // namespace tbg

@@ -8,6 +8,10 @@
 //             [0, N-4]; points outside [0,1]^3 give 0 (the reference's form).
 //  PERIODIC:  nodes i/N on [0,1); the query is wrapped once (as EvalTree
 //             wraps), stencil base floor(xN)-1, indices taken mod N.
+// The periodic step runs its stencil sums in double-float unless the
+// context asks for FP64 sums (TBSLAS_SUMS_FP64); the free-space step is FP64
+// (its interpolant jumps to 0 at the domain boundary, so a departure point
+// must not move by a rounding).
 #include "internal.h"
 
 namespace tbg {
@@ -168,6 +172,111 @@ __global__ void __launch_bounds__(256) k_semilag_grid(const double* __restrict__
   cout[t] = make_stencil(x, y, z, N, per, s) ? apply_stencil(con, s) : 0.0;
 }
 
+// Double-float form of apply_stencil: the same 64 terms and grouping, the
+// sums on the FP32 pipe (df64.cuh) over a hi/lo split copy of the grid.
+__device__ __forceinline__ df apply_stencil_df(const float2* __restrict__ g, const Stencil& s,
+                                               const df (&wx)[4], const df (&wy)[4],
+                                               const df (&wz)[4]) {
+  df u{0.f, 0.f};
+#pragma unroll
+  for (int j2 = 0; j2 < 4; ++j2) {
+    df v{0.f, 0.f};
+#pragma unroll
+    for (int j1 = 0; j1 < 4; ++j1) {
+      const float2* row = g + s.iz[j2] + s.iy[j1];
+      df w{0.f, 0.f};
+#pragma unroll
+      for (int j0 = 0; j0 < 4; ++j0) {
+        const float2 c = __ldg(row + s.ix[j0]);
+        df_fma_acc(w, df{c.x, c.y}, wx[j0]);
+      }
+      df_fma_acc(v, wy[j1], df_norm(w));
+    }
+    df_fma_acc(u, wz[j2], df_norm(v));
+  }
+  return df_norm(u);
+}
+
+__device__ __forceinline__ void split_weights(const Stencil& s, df (&wx)[4], df (&wy)[4],
+                                              df (&wz)[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    wx[k] = df_split_bits(s.wx[k]);
+    wy[k] = df_split_bits(s.wy[k]);
+    wz[k] = df_split_bits(s.wz[k]);
+  }
+}
+
+// The periodic grid step with the stencil sums in double-float: coordinates,
+// stencil bases, Lagrange weights and the RK2 updates stay FP64.  The
+// periodic tricubic interpolant is continuous everywhere, so the ~1e-17
+// difference of a departure point from the FP64 one cannot move a value by
+// more than the sums' own rounding (~1e-14 relative).  vel2/con2: hi/lo
+// copies of the FP64 grids.
+__global__ void __launch_bounds__(256) k_semilag_grid_df(const double* __restrict__ vel,
+                                                         const float2* __restrict__ vel2,
+                                                         const float2* __restrict__ con2,
+                                                         double* __restrict__ cout, int N,
+                                                         double tau, int nrk, int node_read) {
+  const int64_t N3 = (int64_t)N * N * N;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= N3) return;
+  const double h = 1.0 / N;
+  const int64_t ix = t % N, iy = (t / N) % N, iz = t / ((int64_t)N * N);
+  double x = (double)ix * h, y = (double)iy * h, z = (double)iz * h;
+  const double half_tau = 0.5 * tau;
+  double px = x, py = y, pz = z;
+#pragma unroll 1
+  for (int st = 0; st < 2 * nrk; ++st) {
+    double v[3];
+    if (st == 0 && node_read) {
+      v[0] = __ldg(vel + t);
+      v[1] = __ldg(vel + N3 + t);
+      v[2] = __ldg(vel + 2 * N3 + t);
+    } else {
+      Stencil s;
+      make_stencil(px, py, pz, N, true, s);  // always inside under periodic wrap
+      df wx[4], wy[4], wz[4];
+      split_weights(s, wx, wy, wz);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[c] = df_to_double(apply_stencil_df(vel2 + c * N3, s, wx, wy, wz));
+    }
+    if ((st & 1) == 0) {
+      x = px;
+      y = py;
+      z = pz;
+      px = x + half_tau * v[0];
+      py = y + half_tau * v[1];
+      pz = z + half_tau * v[2];
+    } else {
+      x = x + tau * v[0];
+      y = y + tau * v[1];
+      z = z + tau * v[2];
+      px = x;
+      py = y;
+      pz = z;
+    }
+  }
+  Stencil s;
+  make_stencil(x, y, z, N, true, s);
+  df wx[4], wy[4], wz[4];
+  split_weights(s, wx, wy, wz);
+  cout[t] = df_to_double(apply_stencil_df(con2, s, wx, wy, wz));
+}
+
+// hi/lo split of an FP64 grid (integer operations), flagging values outside
+// the double-float range.
+__global__ void k_split_grid(const double* __restrict__ g, float2* __restrict__ g2, int64_t n,
+                             uint32_t* err) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = g[i];
+    check_df_range(x, err);
+    const df v = df_split_bits(x);
+    g2[i] = make_float2(v.hi, v.lo);
+  }
+}
+
 void launch_fast_interp(const double* grid, int dof, int nreg, const double* pts, int64_t n,
                         double* out, int periodic, cudaStream_t s) {
   if (n <= 0) return;
@@ -182,6 +291,18 @@ void launch_semilag_grid(const double* vel, const double* con, double* cout, int
   const int node_read = (periodic && pow2) ? 1 : 0;
   k_semilag_grid<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(vel, con, cout, nreg, tau, nrk,
                                                              periodic, node_read);
+}
+
+void launch_semilag_grid_df(const double* vel, const double* con, double* cout, int nreg,
+                            double tau, int nrk, float2* vel2, float2* con2, uint32_t* err,
+                            int num_sms, cudaStream_t s) {
+  const int64_t n = (int64_t)nreg * nreg * nreg;
+  const bool pow2 = (nreg & (nreg - 1)) == 0;
+  const int split_grid = num_sms * 8;
+  k_split_grid<<<split_grid, 256, 0, s>>>(vel, vel2, 3 * n, err);
+  k_split_grid<<<split_grid, 256, 0, s>>>(con, con2, n, err);
+  k_semilag_grid_df<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(vel, vel2, con2, cout, nreg, tau,
+                                                                nrk, pow2 ? 1 : 0);
 }
 
 }  // namespace tbg

@@ -125,7 +125,7 @@ void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* ite
 // factors F = refit_factors(q) (4 D x D blocks on the device).
 //   coeff[(r/dof)*stride + (r%dof)*nc + t] = sum_p vals[r*np + p] M[p][t]
 void launch_refit(const double* vals, const double* F, int q, int64_t rows, int dof,
-                  int64_t stride, double* coeff, float2* coeff2, cudaStream_t s);
+                  int64_t stride, double* coeff, float2* coeff2, uint32_t* err, cudaStream_t s);
 // mu[r*np + p] = sum_t M[p][t] lam[r*nc + t] (the adjoint's transposed refit)
 void launch_refit_t(const double* lam, const double* F, int q, int64_t rows, double* mu,
                     cudaStream_t s);
@@ -135,6 +135,7 @@ struct RefitJob {
   const double* F;
   double* coeff;
   float2* coeff2;
+  uint32_t* err;
   int64_t rows;
   int64_t stride;
   int q, dof;
@@ -145,7 +146,8 @@ struct RefitItem {
 };
 void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_items, int max_q,
                         cudaStream_t s);
-void launch_split(const double* c, float2* c2, int64_t n, cudaStream_t s);
+void launch_split(const double* c, float2* c2, int64_t n, uint32_t* err, cudaStream_t s);
+uint32_t* ctx_err(tbslas_ctx ctx);
 
 // misc kernels (capi.cu)
 void launch_collect(const TreeView& t, const Nodes1D& nodes, double* out, cudaStream_t s);
@@ -155,5 +157,10 @@ void launch_fast_interp(const double* grid, int dof, int nreg, const double* pts
                         double* out, int periodic, cudaStream_t s);
 void launch_semilag_grid(const double* vel, const double* con, double* cout, int nreg,
                          double tau, int nrk, int periodic, cudaStream_t s);
+// periodic grids, stencil sums in double-float over hi/lo copies of the grids
+// (vel2: 3 n^3, con2: n^3 float2 scratch)
+void launch_semilag_grid_df(const double* vel, const double* con, double* cout, int nreg,
+                            double tau, int nrk, float2* vel2, float2* con2, uint32_t* err,
+                            int num_sms, cudaStream_t s);
 
 }  // namespace tbg

@@ -191,9 +191,11 @@ __device__ __forceinline__ void load_row(const double* __restrict__ v, int n, do
 struct CoeffOut {
   double* c;
   float2* c2;
+  uint32_t* err;
   __device__ __forceinline__ void operator()(int t, double s) const {
     c[t] = s;
     if (c2) {
+      check_df_range(s, err);
       const df v = df_from_double(s);
       c2[t] = make_float2(v.hi, v.lo);
     }
@@ -209,7 +211,8 @@ __global__ void __launch_bounds__(kRefitThreads) k_refit(const double* __restric
                                                          const double* __restrict__ F, int q,
                                                          int dof, int64_t stride,
                                                          double* __restrict__ coeff,
-                                                         float2* __restrict__ coeff2) {
+                                                         float2* __restrict__ coeff2,
+                                                         uint32_t* err) {
   extern __shared__ __align__(16) double sm[];
   const int D = q + 1, D3 = D * D * D;
   const Factors f = stage_factors(F, D, sm);
@@ -220,7 +223,7 @@ __global__ void __launch_bounds__(kRefitThreads) k_refit(const double* __restric
   const int l = (int)(r - leaf * dof);
   load_row(vals + r * D3, D3, S0);
   const int64_t base = leaf * stride + (int64_t)l * nc_of(D);
-  refit_row(f, D, S0, S1, CoeffOut{coeff + base, coeff2 ? coeff2 + base : nullptr});
+  refit_row(f, D, S0, S1, CoeffOut{coeff + base, coeff2 ? coeff2 + base : nullptr, err});
 }
 
 // mu[r][p] = sum_n M[p][n] lam[r][n] (the adjoint's transposed refit).
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(kRefitThreads) k_batch_refit(const RefitJob* _
   const int l = (int)(it.row - leaf * j.dof);
   load_row(j.vals + it.row * D3, D3, S0);
   const int64_t base = leaf * j.stride + (int64_t)l * nc_of(D);
-  refit_row(f, D, S0, S1, CoeffOut{j.coeff + base, j.coeff2 ? j.coeff2 + base : nullptr});
+  refit_row(f, D, S0, S1, CoeffOut{j.coeff + base, j.coeff2 ? j.coeff2 + base : nullptr, j.err});
 }
 
 // Raise a kernel's dynamic shared-memory limit to the degree-16 size, once
@@ -279,11 +282,11 @@ std::atomic<uint64_t> g_smem_refit{0}, g_smem_refit_t{0}, g_smem_batch{0};
 }  // namespace
 
 void launch_refit(const double* vals, const double* F, int q, int64_t rows, int dof,
-                  int64_t stride, double* coeff, float2* coeff2, cudaStream_t s) {
+                  int64_t stride, double* coeff, float2* coeff2, uint32_t* err, cudaStream_t s) {
   if (rows <= 0) return;
   allow_smem(k_refit, g_smem_refit);
   k_refit<<<(unsigned)rows, kRefitThreads, refit_smem(q), s>>>(vals, F, q, dof, stride, coeff,
-                                                               coeff2);
+                                                               coeff2, err);
 }
 
 void launch_refit_t(const double* lam, const double* F, int q, int64_t rows, double* mu,
@@ -301,16 +304,19 @@ void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_
 }
 
 // Split FP64 coefficients into their double-float form.
-__global__ void k_split(const double* __restrict__ c, float2* __restrict__ c2, int64_t n) {
+__global__ void k_split(const double* __restrict__ c, float2* __restrict__ c2, int64_t n,
+                        uint32_t* err) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) {
-    const df v = df_from_double(c[i]);
+    const double x = c[i];
+    check_df_range(x, err);
+    const df v = df_from_double(x);
     c2[i] = make_float2(v.hi, v.lo);
   }
 }
 
-void launch_split(const double* c, float2* c2, int64_t n, cudaStream_t s) {
-  if (n > 0) k_split<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c, c2, n);
+void launch_split(const double* c, float2* c2, int64_t n, uint32_t* err, cudaStream_t s) {
+  if (n > 0) k_split<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c, c2, n, err);
 }
 
 }  // namespace tbg

@@ -92,6 +92,31 @@ __device__ __forceinline__ void rk2_backtrace(const TreeView& vel, double& x, do
   }
 }
 
+// rk2_backtrace of a target node whose first-stage velocity vn (3 values) is
+// known -- the node-grid evaluation, bit-identical to eval_point at X: X is
+// wrapped in place as eval_point would, then the sub-steps continue as
+// rk2_backtrace.
+template <int D>
+__device__ __forceinline__ void rk2_backtrace_from_node(const TreeView& vel, const double* vn,
+                                                        double& x, double& y, double& z,
+                                                        double tau, int nrk, bool per) {
+  if (per) {
+    x = wrap1(x);
+    y = wrap1(y);
+    z = wrap1(z);
+  }
+  const double half_tau = 0.5 * tau;
+  double px = fma(half_tau, __ldg(vn + 0), x);
+  double py = fma(half_tau, __ldg(vn + 1), y);
+  double pz = fma(half_tau, __ldg(vn + 2), z);
+  double v[3];
+  eval_point<D, 3>(vel, px, py, pz, per, v);
+  x = fma(tau, v[0], x);
+  y = fma(tau, v[1], y);
+  z = fma(tau, v[2], z);
+  if (nrk > 1) rk2_backtrace<D>(vel, x, y, z, tau, nrk - 1, per);
+}
+
 // ---------------------------------------------------------------------------
 // Fused in-situ SL step, one thread per target node of `con`:
 //   target  = leaf anchor + 2^-depth * node           (tree_utils.h:484-491)
@@ -112,7 +137,10 @@ __global__ void __launch_bounds__(128) k_semilag_tree(const SemilagTreeArgs a) {
   double y = g.y + h * a.nodes.x[(p / D) % D];
   double z = g.z + h * a.nodes.x[p / (D * D)];
   const bool per = a.periodic != 0;
-  rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
+  if (a.vn)
+    rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * t, x, y, z, a.tau, a.nrk, per);
+  else
+    rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
   double c[1];
   eval_point<D, 1>(a.con, x, y, z, per, c);
   a.vals[t] = c[0];
@@ -195,7 +223,9 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(cons
   if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = t;
 }
 
-// FP64 recomputation of the listed targets (the body of k_semilag_tree).
+// FP64 recomputation of the listed targets (the arithmetic of
+// k_semilag_tree, with the first-stage velocity from the node grid when
+// given -- it is bit-identical to eval_point there).
 template <int D>
 __global__ void __launch_bounds__(128) k_semilag_fix(const SemilagTreeArgs a) {
   constexpr int NP = D * D * D;
@@ -211,7 +241,10 @@ __global__ void __launch_bounds__(128) k_semilag_fix(const SemilagTreeArgs a) {
     double y = g.y + h * a.nodes.x[(p / D) % D];
     double z = g.z + h * a.nodes.x[p / (D * D)];
     const bool per = a.periodic != 0;
-    rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
+    if (a.vn)
+      rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * t, x, y, z, a.tau, a.nrk, per);
+    else
+      rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
     double c[1];
     eval_point<D, 1>(a.con, x, y, z, per, c);
     a.vals[t] = c[0];

@@ -54,16 +54,25 @@ def test_semilag_grid_matches_oracle(ctx, ora, bc, nrk, N):
 
 def test_semilag_grid_full_size_shift_and_sample(ctx, ora):
     """256^3 periodic: (1) a velocity that moves every departure point one
-    node reproduces the shifted field exactly; (2) one step of the config's
-    random Fourier field matches the oracle on a sample of nodes."""
+    node reproduces the shifted field -- exactly with FP64 stencil sums, to
+    the double-float split (2^-48 relative per value) with the default
+    sums; (2) one step of the config's random Fourier field matches the
+    oracle on a sample of nodes."""
     import torch
     N = 256
     rng = np.random.default_rng(11)
     con = fields.periodic_blob_grid(N, (0.45, 0.5, 0.55), 0.1)
     vel = np.zeros((3, N, N, N))
     vel[1] = -0.5
+    shifted = np.roll(con, -1, axis=1)
+    try:
+        ctx.sums = tb.SUMS_FP64
+        out = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, 2.0 / N, 1, 1).cpu().numpy()
+    finally:
+        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+    assert np.array_equal(out, shifted)
     out = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, 2.0 / N, 1, 1).cpu().numpy()
-    assert np.array_equal(out, np.roll(con, -1, axis=1))
+    assert np.all(np.abs(out - shifted) <= 2.0 ** -47 * np.abs(shifted))
     vel = fields.fourier_velocity_grid(rng, N)
     dt = 2.0 / N / np.abs(vel).max()
     out = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, dt, 1, 1).cpu().numpy().ravel()

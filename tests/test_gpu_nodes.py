@@ -55,3 +55,32 @@ def test_in_situ_step_first_stage_is_exact(ctx, ora):
     ref = ora.semilag_in_situ(dict(anchor=a, depth=d, q=q, dof=3, coeff=vc),
                               dict(anchor=a, depth=d, q=q, dof=1, coeff=cc), 1, 0.02, 1, False)
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("bc", [0, 1])
+def test_in_situ_fp64_sums_mode(ctx, ora, bc):
+    """TBSLAS_SUMS_FP64: every sum in FP64 -- matches the oracle to 1e-12 (the
+    refit's summation order is the only difference) and the default
+    double-float mode to 1e-12; the mode is a context setting."""
+    q = 8
+    a, d = trees.adaptive_tree(fields.gaussian((0.45, 0.5, 0.52), 0.08), q, 1, 1e-4, 1, 3)
+    vc = trees.fit(fields.taylor_green(), a, d, q, 3)
+    cc = trees.fit(fields.gaussian((0.45, 0.5, 0.52), 0.08), a, d, q, 1)
+    tv = tb.Tree(ctx, a, d, q, 3, vc)
+    ref = ora.semilag_in_situ(dict(anchor=a, depth=d, q=q, dof=3, coeff=vc),
+                              dict(anchor=a, depth=d, q=q, dof=1, coeff=cc), 2, 0.01, 1, bool(bc))
+    got = {}
+    assert ctx.sums == tb.SUMS_DOUBLE_FLOAT
+    try:
+        for mode in (tb.SUMS_FP64, tb.SUMS_DOUBLE_FLOAT):
+            ctx.sums = mode
+            tc = tb.Tree(ctx, a, d, q, 1, cc)
+            tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv, bc), tc, 2, 0.01, 1)
+            got[mode] = tc.get_coeffs()
+    finally:
+        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+    scale = np.abs(ref).max()
+    assert np.abs(got[tb.SUMS_FP64] - ref).max() <= 1e-12 * scale
+    assert np.abs(got[tb.SUMS_DOUBLE_FLOAT] - ref).max() <= 1e-12 * scale
+    with pytest.raises(tb.capi.TbslasError):
+        ctx.sums = 7
