@@ -2,7 +2,7 @@
 // differentiation pattern of the SL step; no reference counterpart).
 #include <cmath>
 
-#include "adjoint_kernels.cuh"
+#include "adjoint_df.cuh"
 
 namespace tbg {
 
@@ -12,10 +12,11 @@ constexpr int kAdjMaxDegree = 10;
 struct AdjTable {
   CkptFn ckpt[kAdjMaxDegree + 1] = {};
   AdjFn adj[kAdjMaxDegree + 1] = {};
+  AdjDfFn adj_df[kAdjMaxDegree + 1] = {};
   AdjTable() {
-    register_adjoint_a(ckpt, adj);
-    register_adjoint_b(ckpt, adj);
-    register_adjoint_c(ckpt, adj);
+    register_adjoint_a(ckpt, adj, adj_df);
+    register_adjoint_b(ckpt, adj, adj_df);
+    register_adjoint_c(ckpt, adj, adj_df);
   }
 };
 const AdjTable g_adj;
@@ -136,6 +137,15 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   a.xdep = xdep_dev;
   a.lambda = lambda_k_dev;
   a.grad_vel = grad_vel_dev;
-  g_adj.adj[q](a, s);
+  if (ctx_sums(ctx) == TBSLAS_SUMS_FP64) {
+    g_adj.adj[q](a, s);
+  } else {
+    // the sums in double-float over a hi/lo split of c^k
+    float2* c2 = nullptr;
+    st = ctx_c2_scratch(ctx, tc.L * nc, &c2);
+    if (st != TBSLAS_OK) return st;
+    launch_split(con_coeff_k_dev, c2, tc.L * nc, ctx_err(ctx), s);
+    g_adj.adj_df[q](a, c2, s);
+  }
   return launched("adjoint step launch");
 }

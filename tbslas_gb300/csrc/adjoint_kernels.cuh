@@ -368,9 +368,10 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const AdjArgs a) {
 
 typedef void (*CkptFn)(const CkptArgs&, cudaStream_t);
 typedef void (*AdjFn)(const AdjArgs&, cudaStream_t);
-void register_adjoint_a(CkptFn* c, AdjFn* a);
-void register_adjoint_b(CkptFn* c, AdjFn* a);
-void register_adjoint_c(CkptFn* c, AdjFn* a);
+typedef void (*AdjDfFn)(const AdjArgs&, const float2*, cudaStream_t);
+void register_adjoint_a(CkptFn* c, AdjFn* a, AdjDfFn* d);
+void register_adjoint_b(CkptFn* c, AdjFn* a, AdjDfFn* d);
+void register_adjoint_c(CkptFn* c, AdjFn* a, AdjDfFn* d);
 
 template <int D>
 void launch_ckpt(const CkptArgs& a, cudaStream_t s) {
@@ -391,10 +392,6 @@ void launch_adjoint(const AdjArgs& a, cudaStream_t s) {
     k_adjoint<D><<<(unsigned)((n + kAdjThreads - 1) / kAdjThreads), kAdjThreads, smem, s>>>(a);
 }
 
-template <int D>
-void register_adjoint_degree(CkptFn* c, AdjFn* a) {
-  c[D - 1] = &launch_ckpt<D>;
-  a[D - 1] = &launch_adjoint<D>;
-}
+
 
 }  // namespace tbg

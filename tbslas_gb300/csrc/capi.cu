@@ -90,6 +90,7 @@ enum Slot {
   kVN,
   kGridV2,
   kGridC2,
+  kAdjC2,
   kNumSlots
 };
 
@@ -807,6 +808,10 @@ int ctx_info(tbslas_ctx ctx, int* device, int* num_sms) {
 }
 
 uint32_t* ctx_err(tbslas_ctx ctx) { return ctx ? ctx->d_err : nullptr; }
+int ctx_sums(tbslas_ctx ctx) { return ctx->sums; }
+int ctx_c2_scratch(tbslas_ctx ctx, size_t n, float2** out) {
+  return scratch_t(ctx, kAdjC2, n, out);
+}
 
 int ctx_F(tbslas_ctx ctx, int q, const double** F) {
   TRY(bind(ctx));

@@ -172,22 +172,29 @@ __global__ void __launch_bounds__(256) k_semilag_grid(const double* __restrict__
   cout[t] = make_stencil(x, y, z, N, per, s) ? apply_stencil(con, s) : 0.0;
 }
 
+// Stencil of the double-float path: grid indices per axis (32-bit; the
+// addresses are formed per row), weights in double-float.
+struct StencilDF {
+  int gx[4], gy[4], gz[4];
+};
+
 // Double-float form of apply_stencil: the same 64 terms and grouping, the
 // sums on the FP32 pipe (df64.cuh) over a hi/lo split copy of the grid.
-__device__ __forceinline__ df apply_stencil_df(const float2* __restrict__ g, const Stencil& s,
-                                               const df (&wx)[4], const df (&wy)[4],
+__device__ __forceinline__ df apply_stencil_df(const float2* __restrict__ g, const StencilDF& s,
+                                               int N, const df (&wx)[4], const df (&wy)[4],
                                                const df (&wz)[4]) {
+  const int64_t NN = (int64_t)N * N;
   df u{0.f, 0.f};
-#pragma unroll
+#pragma unroll 1
   for (int j2 = 0; j2 < 4; ++j2) {
     df v{0.f, 0.f};
 #pragma unroll
     for (int j1 = 0; j1 < 4; ++j1) {
-      const float2* row = g + s.iz[j2] + s.iy[j1];
+      const float2* row = g + (int64_t)s.gz[j2] * NN + (int64_t)s.gy[j1] * N;
       df w{0.f, 0.f};
 #pragma unroll
       for (int j0 = 0; j0 < 4; ++j0) {
-        const float2 c = __ldg(row + s.ix[j0]);
+        const float2 c = __ldg(row + s.gx[j0]);
         df_fma_acc(w, df{c.x, c.y}, wx[j0]);
       }
       df_fma_acc(v, wy[j1], df_norm(w));
@@ -197,23 +204,80 @@ __device__ __forceinline__ df apply_stencil_df(const float2* __restrict__ g, con
   return df_norm(u);
 }
 
-__device__ __forceinline__ void split_weights(const Stencil& s, df (&wx)[4], df (&wy)[4],
-                                              df (&wz)[4]) {
+// a - l for a small integer l, as an unnormalised double-float (TwoSum of
+// the high word, exact)
+__device__ __forceinline__ df df_sub_small(df a, float l) {
+  const float s = __fsub_rn(a.hi, l);
+  const float v = __fsub_rn(s, a.hi);
+  const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(-l, v));
+  return df{s, __fadd_rn(err, a.lo)};
+}
+
+__device__ __forceinline__ df df_mul_n(df a, df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df{p, e};
+}
+
+// The four cubic Lagrange weights at offset t (the products of lagrange4) in
+// double-float, from the hi/lo split of the FP64 offset: ~25 FP32
+// instructions a weight instead of FP64 products (relative error ~2^-46).
+__device__ __forceinline__ void lagrange4_df(double t, df (&w)[4]) {
+  const df td = df_split_bits(t);
+  const df d0 = td, d1 = df_sub_small(td, 1.f), d2 = df_sub_small(td, 2.f),
+           d3 = df_sub_small(td, 3.f);
+  // den = -1/6, 1/2, -1/2, 1/6; 1/6 as a hi/lo pair
+  const df sixth{0x1.555556p-3f, -0x1.555556p-28f};
+  const df m6{-sixth.hi, -sixth.lo};
+  w[0] = df_norm(df_mul_n(df_mul_n(df_mul_n(m6, d1), d2), d3));
+  w[1] = df_norm(df_mul_n(df_mul_n(df_mul_n(df{0.5f, 0.f}, d0), d2), d3));
+  w[2] = df_norm(df_mul_n(df_mul_n(df_mul_n(df{-0.5f, 0.f}, d0), d1), d3));
+  w[3] = df_norm(df_mul_n(df_mul_n(df_mul_n(sixth, d0), d1), d2));
+}
+
+// Stencil of a point on the periodic grid for the double-float sums: the
+// indices of make_stencil, the weights from lagrange4_df.
+__device__ __forceinline__ void make_stencil_df(double& x, double& y, double& z, int N,
+                                                StencilDF& s, df (&wx)[4], df (&wy)[4],
+                                                df (&wz)[4]) {
+  x = wrap1(x);
+  y = wrap1(y);
+  z = wrap1(z);
+  const double c[3] = {x, y, z};
+  int64_t base[3];
+  double t[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double p = c[j] * (double)N;
+    const int64_t g = (int64_t)p - 1;
+    base[j] = g;
+    t[j] = p - (double)g;
+  }
+  lagrange4_df(t[0], wx);
+  lagrange4_df(t[1], wy);
+  lagrange4_df(t[2], wz);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    wx[k] = df_split_bits(s.wx[k]);
-    wy[k] = df_split_bits(s.wy[k]);
-    wz[k] = df_split_bits(s.wz[k]);
+    int64_t gx = base[0] + k, gy = base[1] + k, gz = base[2] + k;
+    gx = gx < 0 ? gx + N : (gx >= N ? gx - N : gx);
+    gy = gy < 0 ? gy + N : (gy >= N ? gy - N : gy);
+    gz = gz < 0 ? gz + N : (gz >= N ? gz - N : gz);
+    s.gx[k] = (int)gx;
+    s.gy[k] = (int)gy;
+    s.gz[k] = (int)gz;
   }
 }
 
 // The periodic grid step with the stencil sums in double-float: coordinates,
-// stencil bases, Lagrange weights and the RK2 updates stay FP64.  The
+// stencil bases, the offsets t and the RK2 updates stay FP64; the Lagrange
+// weights are formed from t in double-float.  The
 // periodic tricubic interpolant is continuous everywhere, so the ~1e-17
 // difference of a departure point from the FP64 one cannot move a value by
 // more than the sums' own rounding (~1e-14 relative).  vel2/con2: hi/lo
 // copies of the FP64 grids.
-__global__ void __launch_bounds__(256) k_semilag_grid_df(const double* __restrict__ vel,
+__global__ void __launch_bounds__(256, 3) k_semilag_grid_df(const double* __restrict__ vel,
                                                          const float2* __restrict__ vel2,
                                                          const float2* __restrict__ con2,
                                                          double* __restrict__ cout, int N,
@@ -234,12 +298,12 @@ __global__ void __launch_bounds__(256) k_semilag_grid_df(const double* __restric
       v[1] = __ldg(vel + N3 + t);
       v[2] = __ldg(vel + 2 * N3 + t);
     } else {
-      Stencil s;
-      make_stencil(px, py, pz, N, true, s);  // always inside under periodic wrap
+      StencilDF s;
       df wx[4], wy[4], wz[4];
-      split_weights(s, wx, wy, wz);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) v[c] = df_to_double(apply_stencil_df(vel2 + c * N3, s, wx, wy, wz));
+      make_stencil_df(px, py, pz, N, s, wx, wy, wz);  // inside after the periodic wrap
+      v[0] = df_to_double(apply_stencil_df(vel2, s, N, wx, wy, wz));
+      v[1] = df_to_double(apply_stencil_df(vel2 + N3, s, N, wx, wy, wz));
+      v[2] = df_to_double(apply_stencil_df(vel2 + 2 * N3, s, N, wx, wy, wz));
     }
     if ((st & 1) == 0) {
       x = px;
@@ -257,11 +321,10 @@ __global__ void __launch_bounds__(256) k_semilag_grid_df(const double* __restric
       pz = z;
     }
   }
-  Stencil s;
-  make_stencil(x, y, z, N, true, s);
+  StencilDF s;
   df wx[4], wy[4], wz[4];
-  split_weights(s, wx, wy, wz);
-  cout[t] = df_to_double(apply_stencil_df(con2, s, wx, wy, wz));
+  make_stencil_df(x, y, z, N, s, wx, wy, wz);
+  cout[t] = df_to_double(apply_stencil_df(con2, s, N, wx, wy, wz));
 }
 
 // hi/lo split of an FP64 grid (integer operations), flagging values outside

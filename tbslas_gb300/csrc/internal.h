@@ -148,6 +148,8 @@ void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_
                         cudaStream_t s);
 void launch_split(const double* c, float2* c2, int64_t n, uint32_t* err, cudaStream_t s);
 uint32_t* ctx_err(tbslas_ctx ctx);
+int ctx_sums(tbslas_ctx ctx);
+int ctx_c2_scratch(tbslas_ctx ctx, size_t n, float2** out);
 
 // misc kernels (capi.cu)
 void launch_collect(const TreeView& t, const Nodes1D& nodes, double* out, cudaStream_t s);
