@@ -234,14 +234,26 @@ def run_reference(args, wl):
             pts += k
         cb["sample"] = "per step: " + cb["sample"]
     else:
-        for _ in range(args.warmup):
-            cpu_baseline_tree(wl, per_step)
+        note = None
+        tw = wl
+        if hasattr(wl, "problems"):
+            # batched: the reference advances the problems one by one; its
+            # CPU path is timed on the problems in turn (a bounded sample each)
+            note = "batched: the reference's per-problem CPU step, problems in turn"
+        elif not hasattr(wl, "va"):
+            # adjoint: the reference has no adjoint; its forward SL step on the
+            # same tree and fields is timed
+            tw = _TreeView(wl.a, wl.d, wl.vc, wl.a, wl.d, wl.c0, wl.q, wl.dt, wl.bc)
+            note = "adjoint: the reference has no adjoint; its forward SL step is timed"
+        for i in range(args.warmup):
+            cpu_baseline_tree(_pick(tw, i), per_step)
         secs, pts = 0.0, 0
-        for _ in range(args.steps):
-            cb, _, k = cpu_baseline_tree(wl, per_step)
+        for i in range(args.steps):
+            t = _pick(tw, i)
+            cb, _, k = cpu_baseline_tree(t, per_step)
             secs += cb["seconds"]
-            pts += k * (wl.q + 1) ** 3
-        cb["sample"] = "per step: " + cb["sample"]
+            pts += k * (t.q + 1) ** 3
+        cb["sample"] = "per step: " + cb["sample"] + ("; " + note if note else "")
     value = pts / secs
     cb["value"] = value
     cb.pop("seconds", None)
@@ -253,6 +265,23 @@ def run_reference(args, wl):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+class _TreeView:
+    """The tree-workload fields cpu_baseline_tree reads."""
+
+    def __init__(self, va, vd, vc, ca, cd, cc, q, dt, bc):
+        self.va, self.vd, self.vc, self.ca, self.cd, self.cc = va, vd, vc, ca, cd, cc
+        self.q, self.dt, self.bc = q, dt, bc
+
+
+def _pick(wl, i):
+    """A batch's i-th problem (cyclically) as a tree workload; else wl."""
+    if not hasattr(wl, "problems"):
+        return wl
+    p = wl.problems[i % len(wl.problems)]
+    return _TreeView(p["va"], p["vd"], p["vc"], p["ca"], p["cd"], p["cc"], p["q"], p["dt"],
+                     wl.bc)
 
 
 def GridWorkloadType():
@@ -301,6 +330,7 @@ def run_gpu(args, wl, rank, world, local_rank):
     torch.cuda.synchronize()
     first = (bufs[1].cpu().numpy().ravel() if is_grid else tc.get_coeffs())
     for i in range(args.warmup):
+        flush.fill_(float(i))  # the flush's own first launch stays out of the timed loop
         step(i + 1)
     torch.cuda.synchronize()
 
@@ -683,6 +713,12 @@ def run_adjoint(args, wl, rank, world, local_rank):
         fwd_default()
     fwd_ms, _ = timed(fwd_plain)
     fwd_df_ms, _ = timed(fwd_default)
+    # one untimed gradient each way: the first autograd pass of a process
+    # carries one-time setup
+    for ck in (True, False):
+        _, _, j0 = grad(ck)
+        j0.backward()
+    torch.cuda.synchronize()
     res = {}
     for ck in (True, False):
         fms, (c, v, j) = timed(lambda: grad(ck))

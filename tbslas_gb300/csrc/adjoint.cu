@@ -137,15 +137,22 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   a.xdep = xdep_dev;
   a.lambda = lambda_k_dev;
   a.grad_vel = grad_vel_dev;
+  a.wnode = nullptr;
   if (ctx_sums(ctx) == TBSLAS_SUMS_FP64) {
     g_adj.adj[q](a, s);
   } else {
-    // the sums in double-float over a hi/lo split of c^k
+    // the sums in double-float over a hi/lo split of c^k; the node term by
+    // the transposed node-grid passes
     float2* c2 = nullptr;
     st = ctx_c2_scratch(ctx, tc.L * nc, &c2);
     if (st != TBSLAS_OK) return st;
+    st = ctx_wnode_scratch(ctx, tc.L * np * 3, &a.wnode);
+    if (st != TBSLAS_OK) return st;
     launch_split(con_coeff_k_dev, c2, tc.L * nc, ctx_err(ctx), s);
     g_adj.adj_df[q](a, c2, s);
+    st = launched("adjoint step launch");
+    if (st != TBSLAS_OK) return st;
+    launch_scatter_on_nodes(tv, tc, bc, a.wnode, grad_vel_dev, 3 * nc, s);
   }
   return launched("adjoint step launch");
 }

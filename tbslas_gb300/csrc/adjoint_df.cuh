@@ -253,8 +253,11 @@ __device__ __forceinline__ void cta_scatter_df(AdjStageDF<D>& sm, double* __rest
   }
 }
 
+// Five (q <= 8) or four 128-thread CTAs per SM: with the register cap the
+// kernel spills a little but keeps 16-20 warps resident (measured on GB300,
+// q = 8: 43.1 -> 35.9 ms per adjoint pass of a 4096-leaf tree).
 template <int D>
-__global__ void __launch_bounds__(kAdjThreads) k_adjoint_df(const AdjArgs a,
+__global__ void __launch_bounds__(kAdjThreads, (D <= 9 ? 5 : 4)) k_adjoint_df(const AdjArgs a,
                                                             const float2* __restrict__ con2) {
   constexpr int NP = D * D * D;
   constexpr int NC = D * (D + 1) * (D + 2) / 6;
@@ -347,7 +350,17 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint_df(const AdjArgs a,
     const double w[3] = {a.tau * gvec[0], a.tau * gvec[1], a.tau * gvec[2]};
     cta_scatter_df<D, 3>(sm, a.grad_vel, 3 * NC, lf, w, tx, ty, tz);
   }
-  // tau^2/2 J_v(X*)^T g (x) phi(X)
+  // tau^2/2 J_v(X*)^T g (x) phi(X): X is a node, so the weights go to the
+  // node-grid scatter when a buffer is given
+  if (a.wnode) {
+    const double c2 = 0.5 * a.tau * a.tau;
+    if (active) {
+      a.wnode[3 * t + 0] = c2 * jtg[0];
+      a.wnode[3 * t + 1] = c2 * jtg[1];
+      a.wnode[3 * t + 2] = c2 * jtg[2];
+    }
+    return;
+  }
   {
     Geom g;
     int64_t lf = locate<D>(a.vel, x, y, z, per, g);

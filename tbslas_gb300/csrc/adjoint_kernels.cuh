@@ -43,6 +43,8 @@ struct AdjArgs {
   const double* xdep;  // checkpointed Xd or null (recompute)
   double* lambda;      // [Lc][Nc] accumulated
   double* grad_vel;    // [Lv][3][Nc] accumulated
+  double* wnode;       // [Lc * Np][3]: weights of the tau^2/2 term at the nodes for
+                       // the node-grid scatter (launch_scatter_on_nodes), or null
 };
 
 // T_k and dT_k/dxi for k < D; zero outside [-1,1] like cheb_T.

@@ -91,6 +91,7 @@ enum Slot {
   kGridV2,
   kGridC2,
   kAdjC2,
+  kAdjW,
   kNumSlots
 };
 
@@ -811,6 +812,9 @@ uint32_t* ctx_err(tbslas_ctx ctx) { return ctx ? ctx->d_err : nullptr; }
 int ctx_sums(tbslas_ctx ctx) { return ctx->sums; }
 int ctx_c2_scratch(tbslas_ctx ctx, size_t n, float2** out) {
   return scratch_t(ctx, kAdjC2, n, out);
+}
+int ctx_wnode_scratch(tbslas_ctx ctx, size_t n, double** out) {
+  return scratch_t(ctx, kAdjW, n, out);
 }
 
 int ctx_F(tbslas_ctx ctx, int q, const double** F) {

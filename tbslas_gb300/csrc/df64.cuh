@@ -37,13 +37,15 @@ __device__ __forceinline__ double df_to_double(df a) { return (double)a.hi + (do
 // truncated to 24 bits, lo = the remaining 29 significand bits rounded to a
 // float.  |x - hi - lo| <= 2^-48 |x|; values below 2^-74 lose lo and values
 // below 2^-126 become 0 (absolute error < 2^-97, resp. 2^-126 -- far below
-// the sums' error bound).  For |x| < 2^128 (the callers pass Chebyshev values
-// in [-1, 1]).
+// the sums' error bound).  |x| >= 2^127, inf and NaN take the float
+// conversion (inf / NaN as in FP64; callers flag |x| >= 2^100 as outside the
+// double-float range).
 __device__ __forceinline__ df df_split_bits(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
   const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
   if (e < 897u) return df{0.f, 0.f};
+  if (e > 1149u) return df{__double2float_rn(x), 0.f};  // exponent field 254 at most
   const float hi = __uint_as_float(sign | ((e - 896u) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
   float lo = 0.f;
   if (e >= 949u) {

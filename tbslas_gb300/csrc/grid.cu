@@ -237,37 +237,63 @@ __device__ __forceinline__ void lagrange4_df(double t, df (&w)[4]) {
   w[3] = df_norm(df_mul_n(df_mul_n(df_mul_n(sixth, d0), d1), d2));
 }
 
+// Stencil base and offset of one coordinate on a periodic grid of N = 2^nl
+// nodes, with integer operations on the bits of x in [0, 1): p = x N,
+// g = floor(p) - 1, t = p - g in [1, 2) -- the values make_stencil computes
+// in FP64 (x N is exact: a power-of-two scaling).
+__device__ __forceinline__ void grid_split_pow2(double x, int nl, int& g, double& t) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int s = 1075 - nl - (int)(b >> 52);  // p = M 2^-s, M = 2^52 + mantissa
+  if (x == 0.0 || s > 52) {                  // p < 1 (first cell): FP64
+    g = -1;
+    t = fma(x, (double)(1 << nl), 1.0);
+    return;
+  }
+  const unsigned long long M = (b & ((1ull << 52) - 1)) | (1ull << 52);
+  g = (int)(M >> s) - 1;
+  const unsigned long long frac = s > 0 ? (M & ((1ull << s) - 1)) : 0ull;
+  t = __longlong_as_double((long long)((1023ull << 52) | (frac << (52 - s))));
+}
+
 // Stencil of a point on the periodic grid for the double-float sums: the
-// indices of make_stencil, the weights from lagrange4_df.
-__device__ __forceinline__ void make_stencil_df(double& x, double& y, double& z, int N,
+// indices of make_stencil, the weights from lagrange4_df.  Returns false for
+// a coordinate that is not a number (the FP64 path's "outside": value 0).
+// nl >= 0: N = 2^nl (integer stencil bases), else FP64 bases.
+__device__ __forceinline__ bool make_stencil_df(double& x, double& y, double& z, int N, int nl,
                                                 StencilDF& s, df (&wx)[4], df (&wy)[4],
                                                 df (&wz)[4]) {
   x = wrap1(x);
   y = wrap1(y);
   z = wrap1(z);
+  if (!inside(x, y, z, true)) return false;
   const double c[3] = {x, y, z};
-  int64_t base[3];
+  int base[3];
   double t[3];
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    const double p = c[j] * (double)N;
-    const int64_t g = (int64_t)p - 1;
-    base[j] = g;
-    t[j] = p - (double)g;
+    if (nl >= 0) {
+      grid_split_pow2(c[j], nl, base[j], t[j]);
+    } else {
+      const double p = c[j] * (double)N;
+      const int64_t g = (int64_t)p - 1;
+      base[j] = (int)g;
+      t[j] = p - (double)g;
+    }
   }
   lagrange4_df(t[0], wx);
   lagrange4_df(t[1], wy);
   lagrange4_df(t[2], wz);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    int64_t gx = base[0] + k, gy = base[1] + k, gz = base[2] + k;
+    int gx = base[0] + k, gy = base[1] + k, gz = base[2] + k;
     gx = gx < 0 ? gx + N : (gx >= N ? gx - N : gx);
     gy = gy < 0 ? gy + N : (gy >= N ? gy - N : gy);
     gz = gz < 0 ? gz + N : (gz >= N ? gz - N : gz);
-    s.gx[k] = (int)gx;
-    s.gy[k] = (int)gy;
-    s.gz[k] = (int)gz;
+    s.gx[k] = gx;
+    s.gy[k] = gy;
+    s.gz[k] = gz;
   }
+  return true;
 }
 
 // The periodic grid step with the stencil sums in double-float: coordinates,
@@ -277,11 +303,12 @@ __device__ __forceinline__ void make_stencil_df(double& x, double& y, double& z,
 // difference of a departure point from the FP64 one cannot move a value by
 // more than the sums' own rounding (~1e-14 relative).  vel2/con2: hi/lo
 // copies of the FP64 grids.
-__global__ void __launch_bounds__(256, 3) k_semilag_grid_df(const double* __restrict__ vel,
+__global__ void __launch_bounds__(256, 4) k_semilag_grid_df(const double* __restrict__ vel,
                                                          const float2* __restrict__ vel2,
                                                          const float2* __restrict__ con2,
                                                          double* __restrict__ cout, int N,
-                                                         double tau, int nrk, int node_read) {
+                                                         double tau, int nrk, int nl) {
+  const int node_read = nl >= 0;  // power-of-two grid: the first stage sits on the node
   const int64_t N3 = (int64_t)N * N * N;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= N3) return;
@@ -300,10 +327,13 @@ __global__ void __launch_bounds__(256, 3) k_semilag_grid_df(const double* __rest
     } else {
       StencilDF s;
       df wx[4], wy[4], wz[4];
-      make_stencil_df(px, py, pz, N, s, wx, wy, wz);  // inside after the periodic wrap
-      v[0] = df_to_double(apply_stencil_df(vel2, s, N, wx, wy, wz));
-      v[1] = df_to_double(apply_stencil_df(vel2 + N3, s, N, wx, wy, wz));
-      v[2] = df_to_double(apply_stencil_df(vel2 + 2 * N3, s, N, wx, wy, wz));
+      if (make_stencil_df(px, py, pz, N, nl, s, wx, wy, wz)) {
+        v[0] = df_to_double(apply_stencil_df(vel2, s, N, wx, wy, wz));
+        v[1] = df_to_double(apply_stencil_df(vel2 + N3, s, N, wx, wy, wz));
+        v[2] = df_to_double(apply_stencil_df(vel2 + 2 * N3, s, N, wx, wy, wz));
+      } else {
+        v[0] = v[1] = v[2] = 0.0;
+      }
     }
     if ((st & 1) == 0) {
       x = px;
@@ -323,8 +353,9 @@ __global__ void __launch_bounds__(256, 3) k_semilag_grid_df(const double* __rest
   }
   StencilDF s;
   df wx[4], wy[4], wz[4];
-  make_stencil_df(x, y, z, N, s, wx, wy, wz);
-  cout[t] = df_to_double(apply_stencil_df(con2, s, N, wx, wy, wz));
+  cout[t] = make_stencil_df(x, y, z, N, nl, s, wx, wy, wz)
+                ? df_to_double(apply_stencil_df(con2, s, N, wx, wy, wz))
+                : 0.0;
 }
 
 // hi/lo split of an FP64 grid (integer operations), flagging values outside
@@ -364,8 +395,12 @@ void launch_semilag_grid_df(const double* vel, const double* con, double* cout, 
   const int split_grid = num_sms * 8;
   k_split_grid<<<split_grid, 256, 0, s>>>(vel, vel2, 3 * n, err);
   k_split_grid<<<split_grid, 256, 0, s>>>(con, con2, n, err);
+  int nl = -1;
+  if (pow2)
+    for (nl = 0; (1 << nl) < nreg; ++nl) {
+    }
   k_semilag_grid_df<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(vel, vel2, con2, cout, nreg, tau,
-                                                                nrk, pow2 ? 1 : 0);
+                                                                nrk, nl);
 }
 
 }  // namespace tbg

@@ -105,6 +105,10 @@ Nodes1D ctx_nodes(int q);
 // (bit-identical to the pointwise FP64 evaluation)
 void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic, double* out,
                           cudaStream_t s);
+// Transposed: out[V * out_stride + l * Nc + n] += sum over dst's nodes p in
+// leaf V of W[p][l] phi_n(X_p) (FP64 atomics); W: [dst.L * Np][src.dof].
+void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int periodic,
+                             const double* W, double* out, int64_t out_stride, cudaStream_t s);
 // Batched: one item per (job, destination leaf); the jobs of one launch
 // share the source degree q_src, max_q_dst bounds their destination degrees.
 struct NodeEvalJob {
@@ -150,6 +154,7 @@ void launch_split(const double* c, float2* c2, int64_t n, uint32_t* err, cudaStr
 uint32_t* ctx_err(tbslas_ctx ctx);
 int ctx_sums(tbslas_ctx ctx);
 int ctx_c2_scratch(tbslas_ctx ctx, size_t n, float2** out);
+int ctx_wnode_scratch(tbslas_ctx ctx, size_t n, double** out);
 
 // misc kernels (capi.cu)
 void launch_collect(const TreeView& t, const Nodes1D& nodes, double* out, cudaStream_t s);

@@ -56,32 +56,52 @@ __device__ __forceinline__ void cheb_T_col(double xi, double* T, int stride) {
   }
 }
 
+// Shared memory of the sub-grid walk: coordinates 3*Dd and T tables
+// 3*Ds*Dd (doubles), quantised coordinates and index lists 6*Dd (ints), the
+// node state Dd^3 (bytes); then the pass buffers of the caller.
+__host__ __device__ constexpr size_t walk_smem(int Ds, int Dd) {
+  return (size_t)(3 * Dd + 3 * Ds * Dd) * 8 + (size_t)(6 * Dd) * 4 +
+         (size_t)(Dd * Dd * Dd + 15) / 16 * 16;
+}
 __host__ __device__ constexpr size_t node_eval_smem(int Ds, int Dd, int dof) {
-  // doubles: coordinates 3*Dd, T tables 3*Ds*Dd, w: dof*Ds(Ds+1)/2*Dd;
-  // ints: quantised coordinates 3*Dd, index lists 3*Dd; bytes: node state Dd^3
-  return (size_t)(3 * Dd + 3 * Ds * Dd + dof * Ds * (Ds + 1) / 2 * Dd) * 8 +
-         (size_t)(6 * Dd) * 4 + (size_t)(Dd * Dd * Dd + 15) / 16 * 16;
+  return walk_smem(Ds, Dd) + (size_t)dof * Ds * (Ds + 1) / 2 * Dd * 8;  // w
+}
+__host__ __device__ constexpr size_t node_scatter_smem(int Ds, int Dd, int dof) {
+  (void)dof;
+  return walk_smem(Ds, Dd) +
+         (size_t)(Dd * Dd * Dd + Ds * Dd * Dd + Ds * (Ds + 1) / 2 * Dd) * 8;  // W, H, G
 }
 
-// One destination leaf (the whole CTA).  out: the destination tree's
-// [L * Dd^3][src.dof] array.
-template <int Ds>
-__device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const TreeView& dst,
-                                                   const Nodes1D& nodes, bool per, int64_t leaf,
-                                                   double* __restrict__ out_all, double* sm) {
-  constexpr int NCs = Ds * (Ds + 1) * (Ds + 2) / 6, npair = Ds * (Ds + 1) / 2;
+// The part of a destination leaf's node grid inside one source leaf: leaf
+// V, the listed node indices per axis (sidx[ax*Dd + i'], i' < n[ax]) and
+// T_k of their local coordinates in V (T[ax][k][i'], stride Dd).
+struct SubGrid {
+  int64_t V;
+  int na, nb, nz;
+  const int* sidx;
+  const double *Tx, *Ty, *Tz;
+};
+
+// Walks the destination leaf's nodes source leaf by source leaf.  Leaves
+// tile the unit cube (tree_create checks it), so the nodes a source leaf
+// holds are those inside its box: starting from the first node not yet
+// visited, one key search finds its source leaf and per-axis box tests give
+// the sub-grid.  outside(p) is called for nodes outside the domain, fn(sub)
+// for every sub-grid (all threads, block-synchronised around it).  The
+// walk's shared memory is the first walk_smem(Ds, Dd) bytes of sm.
+template <int Ds, class Outside, class Fn>
+__device__ __forceinline__ void for_each_subgrid(const TreeView& S, const TreeView& dst,
+                                                 const Nodes1D& nodes, bool per, int64_t leaf,
+                                                 double* sm, Outside outside, Fn fn) {
   __shared__ int s_first;
   __shared__ int s_n[3];
   const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
-  const int dof = S.dof;
   const int tid = threadIdx.x, bs = blockDim.x;
-
-  double* sx = sm;                       // [3][Dd] wrapped node coordinates
-  double* sT = sx + 3 * Dd;              // [3][Ds][Dd]: T_k of the listed indices
-  double* sw = sT + 3 * Ds * Dd;         // [dof][pair(i,j)][Dd]
-  uint32_t* sq = reinterpret_cast<uint32_t*>(sw + dof * npair * Dd);  // [3][Dd] keys, ~0 outside
-  int* sidx = reinterpret_cast<int*>(sq + 3 * Dd);                     // [3][Dd] index lists
-  uint8_t* sdone = reinterpret_cast<uint8_t*>(sidx + 3 * Dd);          // [Dd^3]
+  double* sx = sm;                                              // [3][Dd]
+  double* sT = sx + 3 * Dd;                                     // [3][Ds][Dd]
+  uint32_t* sq = reinterpret_cast<uint32_t*>(sT + 3 * Ds * Dd);  // [3][Dd] keys, ~0 outside
+  int* sidx = reinterpret_cast<int*>(sq + 3 * Dd);              // [3][Dd]
+  uint8_t* sdone = reinterpret_cast<uint8_t*>(sidx + 3 * Dd);   // [Dd^3]
 
   const Geom g = load_geom(dst.geom + leaf);
   const double h = 2.0 / g.w;
@@ -96,13 +116,11 @@ __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const Tree
     sq[tid] = in ? (uint32_t)quantise(c) : 0xffffffffu;
   }
   __syncthreads();
-  double* out = out_all + leaf * (int64_t)Dd3 * dof;
   for (int p = tid; p < Dd3; p += bs) {
     const bool in = sq[p % Dd] != 0xffffffffu && sq[Dd + (p / Dd) % Dd] != 0xffffffffu &&
                     sq[2 * Dd + p / Dd2] != 0xffffffffu;
     sdone[p] = in ? 0 : 1;
-    if (!in)
-      for (int l = 0; l < dof; ++l) out[(int64_t)p * dof + l] = 0.0;
+    if (!in) outside(p);
   }
   __syncthreads();
 
@@ -136,8 +154,8 @@ __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const Tree
     }
     __syncthreads();
     const int na = s_n[0], nb = s_n[1], nz = s_n[2];
-    // T tables of the listed indices: sT[ax][k][i'] (local coordinate and
-    // recurrence of eval_point)
+    // T tables of the listed indices (local coordinate and recurrence of
+    // eval_point)
     if (tid < 3 * Dd) {
       const int ax = tid / Dd, i = tid - ax * Dd;
       const int n = ax == 0 ? na : (ax == 1 ? nb : nz);
@@ -148,55 +166,155 @@ __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const Tree
       }
     }
     __syncthreads();
-    const double* Tx = sT;
-    const double* Ty = sT + Ds * Dd;
-    const double* Tz = sT + 2 * Ds * Dd;
-    const double* cV = S.coeff + V * S.stride;
-    // w(l; i,j,a') = sum_k c[l][i][j][k] T_k(x_a')
-    for (int o = tid; o < dof * npair * na; o += bs) {
-      const int ai = o % na, r = o / na, pr = r % npair, l = r / npair;
-      int i = 0, rem = pr;  // pair index -> (i, j): rows of length Ds - i
-      while (rem >= Ds - i) {
-        rem -= Ds - i;
-        ++i;
-      }
-      const int j = rem, m = Ds - i;
-      const double* c =
-          cV + l * NCs + (NCs - m * (m + 1) * (m + 2) / 6 + j * m - (j * (j - 1)) / 2);
-      double w = 0.0;
-      for (int k = 0; k < m - j; ++k) w = fma(__ldg(c + k), Tx[k * Dd + ai], w);
-      sw[(l * npair + pr) * Dd + ai] = w;
-    }
-    __syncthreads();
-    // per column (l, b', a'): v(i) = sum_j T_j(y_b') w(l; i,j,a'), then
-    // u(c') = sum_i T_i(z_c') v(i) for every listed c'
-    for (int o = tid; o < dof * nb * na; o += bs) {
-      const int ai = o % na, r = o / na, bi = r % nb, l = r / nb;
-      const double* wl = sw + l * npair * Dd + ai;
-      double v[Ds];
-      int prow = 0;
-#pragma unroll
-      for (int i = 0; i < Ds; ++i) {
-        double s = 0.0;
-#pragma unroll
-        for (int j = 0; j < Ds - i; ++j) s = fma(Ty[j * Dd + bi], wl[(prow + j) * Dd], s);
-        v[i] = s;
-        prow += Ds - i;
-      }
-      const int pab = sidx[ai] + Dd * sidx[Dd + bi];
-      for (int ci = 0; ci < nz; ++ci) {
-        double u = 0.0;
-#pragma unroll
-        for (int i = 0; i < Ds; ++i) u = fma(Tz[i * Dd + ci], v[i], u);
-        out[(int64_t)(pab + Dd2 * sidx[2 * Dd + ci]) * dof + l] = u;
-      }
-    }
+    fn(SubGrid{V, na, nb, nz, sidx, sT, sT + Ds * Dd, sT + 2 * Ds * Dd});
     for (int o = tid; o < nz * nb * na; o += bs) {
       const int ai = o % na, r = o / na, bi = r % nb, ci = r / nb;
       sdone[sidx[ai] + Dd * (sidx[Dd + bi] + Dd * sidx[2 * Dd + ci])] = 1;
     }
     __syncthreads();
   }
+}
+
+// One destination leaf (the whole CTA) of the evaluation.  out: the
+// destination tree's [L * Dd^3][src.dof] array.
+template <int Ds>
+__device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const TreeView& dst,
+                                                   const Nodes1D& nodes, bool per, int64_t leaf,
+                                                   double* __restrict__ out_all, double* sm) {
+  constexpr int NCs = Ds * (Ds + 1) * (Ds + 2) / 6, npair = Ds * (Ds + 1) / 2;
+  const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
+  const int dof = S.dof;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  double* sw = sm + walk_smem(Ds, Dd) / 8;  // [dof][pair(i,j)][Dd]
+  double* out = out_all + leaf * (int64_t)Dd3 * dof;
+  for_each_subgrid<Ds>(
+      S, dst, nodes, per, leaf, sm,
+      [&](int p) {
+        for (int l = 0; l < dof; ++l) out[(int64_t)p * dof + l] = 0.0;
+      },
+      [&](const SubGrid& sg) {
+        const int na = sg.na, nb = sg.nb, nz = sg.nz;
+        const int* sidx = sg.sidx;
+        const double* cV = S.coeff + sg.V * S.stride;
+        // w(l; i,j,a') = sum_k c[l][i][j][k] T_k(x_a')
+        for (int o = tid; o < dof * npair * na; o += bs) {
+          const int ai = o % na, r = o / na, pr = r % npair, l = r / npair;
+          int i = 0, rem = pr;  // pair index -> (i, j): rows of length Ds - i
+          while (rem >= Ds - i) {
+            rem -= Ds - i;
+            ++i;
+          }
+          const int j = rem, m = Ds - i;
+          const double* c =
+              cV + l * NCs + (NCs - m * (m + 1) * (m + 2) / 6 + j * m - (j * (j - 1)) / 2);
+          double w = 0.0;
+          for (int k = 0; k < m - j; ++k) w = fma(__ldg(c + k), sg.Tx[k * Dd + ai], w);
+          sw[(l * npair + pr) * Dd + ai] = w;
+        }
+        __syncthreads();
+        // per column (l, b', a'): v(i) = sum_j T_j(y_b') w(l; i,j,a'), then
+        // u(c') = sum_i T_i(z_c') v(i) for every listed c'
+        for (int o = tid; o < dof * nb * na; o += bs) {
+          const int ai = o % na, r = o / na, bi = r % nb, l = r / nb;
+          const double* wl = sw + l * npair * Dd + ai;
+          double v[Ds];
+          int prow = 0;
+#pragma unroll
+          for (int i = 0; i < Ds; ++i) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < Ds - i; ++j) s = fma(sg.Ty[j * Dd + bi], wl[(prow + j) * Dd], s);
+            v[i] = s;
+            prow += Ds - i;
+          }
+          const int pab = sidx[ai] + Dd * sidx[Dd + bi];
+          for (int ci = 0; ci < nz; ++ci) {
+            double u = 0.0;
+#pragma unroll
+            for (int i = 0; i < Ds; ++i) u = fma(sg.Tz[i * Dd + ci], v[i], u);
+            out[(int64_t)(pab + Dd2 * sidx[2 * Dd + ci]) * dof + l] = u;
+          }
+        }
+      });
+}
+
+// The transposed map (adjoint of the evaluation): for one destination leaf,
+// out[V * out_stride + l * Nc + n] += sum over its nodes p inside V of
+// W[p][l] phi_n(X_p), the basis of V at the node -- the same passes in
+// reverse (z, then y, then x), one FP64 atomic per coefficient and sub-grid.
+// W: [dst.L * Dd^3][dof].
+template <int Ds>
+__device__ __forceinline__ void scatter_on_nodes_leaf(const TreeView& S, const TreeView& dst,
+                                                      const Nodes1D& nodes, bool per,
+                                                      int64_t leaf, const double* __restrict__ W,
+                                                      double* __restrict__ out,
+                                                      int64_t out_stride, double* sm) {
+  constexpr int NCs = Ds * (Ds + 1) * (Ds + 2) / 6, npair = Ds * (Ds + 1) / 2;
+  const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
+  const int dof = S.dof;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  double* sW = sm + walk_smem(Ds, Dd) / 8;  // [c'][b'][a'] weights of one component
+  double* sH = sW + Dd3;                    // [i][b'][a']
+  double* sG = sH + Ds * Dd2;               // [pair(i,j)][a']
+  const double* Wl = W + leaf * (int64_t)Dd3 * dof;
+  for_each_subgrid<Ds>(
+      S, dst, nodes, per, leaf, sm, [](int) {},
+      [&](const SubGrid& sg) {
+        const int na = sg.na, nb = sg.nb, nz = sg.nz;
+        const int* sidx = sg.sidx;
+        double* oV = out + sg.V * out_stride;
+        for (int l = 0; l < dof; ++l) {
+          for (int o = tid; o < nz * nb * na; o += bs) {
+            const int ai = o % na, r = o / na, bi = r % nb, ci = r / nb;
+            const int p = sidx[ai] + Dd * (sidx[Dd + bi] + Dd * sidx[2 * Dd + ci]);
+            sW[o] = __ldg(Wl + (int64_t)p * dof + l);
+          }
+          __syncthreads();
+          // H(i, b', a') = sum_c' T_i(z_c') W(c', b', a')
+          for (int o = tid; o < Ds * nb * na; o += bs) {
+            const int ai = o % na, r = o / na, bi = r % nb, i = r / nb;
+            double s = 0.0;
+            for (int ci = 0; ci < nz; ++ci)
+              s = fma(sg.Tz[i * Dd + ci], sW[(ci * nb + bi) * na + ai], s);
+            sH[(i * nb + bi) * na + ai] = s;
+          }
+          __syncthreads();
+          // G(pair(i,j), a') = sum_b' T_j(y_b') H(i, b', a')
+          for (int o = tid; o < npair * na; o += bs) {
+            const int ai = o % na, pr = o / na;
+            int i = 0, rem = pr;
+            while (rem >= Ds - i) {
+              rem -= Ds - i;
+              ++i;
+            }
+            const int j = rem;
+            double s = 0.0;
+            for (int bi = 0; bi < nb; ++bi)
+              s = fma(sg.Ty[j * Dd + bi], sH[(i * nb + bi) * na + ai], s);
+            sG[pr * na + ai] = s;
+          }
+          __syncthreads();
+          // coefficient (i,j,k): sum_a' T_k(x_a') G(pair(i,j), a')
+          for (int n = tid; n < NCs; n += bs) {
+            int i = 0, rem = n;  // triangular index -> (i, j, k)
+            while (rem >= (Ds - i) * (Ds - i + 1) / 2) {
+              rem -= (Ds - i) * (Ds - i + 1) / 2;
+              ++i;
+            }
+            int j = 0;
+            while (rem >= Ds - i - j) {
+              rem -= Ds - i - j;
+              ++j;
+            }
+            const int k = rem;
+            const int pr = i * Ds - (i * (i - 1)) / 2 + j;
+            double s = 0.0;
+            for (int ai = 0; ai < na; ++ai) s = fma(sg.Tx[k * Dd + ai], sG[pr * na + ai], s);
+            if (s != 0.0) atomicAdd(oV + l * NCs + n, s);
+          }
+          __syncthreads();
+        }
+      });
 }
 
 template <int Ds>
@@ -217,6 +335,16 @@ __global__ void __launch_bounds__(kNodeEvalThreads) k_batch_eval_on_nodes(
   if (threadIdx.x == 0) sj = jobs[it.job];
   __syncthreads();
   eval_on_nodes_leaf<Ds>(sj.src, sj.dst, sj.nodes, periodic != 0, it.leaf, sj.out, sm);
+}
+
+template <int Ds>
+__global__ void __launch_bounds__(kNodeEvalThreads) k_scatter_on_nodes(const NodeEvalJob j,
+                                                                       const double* W,
+                                                                       int64_t out_stride,
+                                                                       int periodic) {
+  extern __shared__ __align__(16) double sm[];
+  scatter_on_nodes_leaf<Ds>(j.src, j.dst, j.nodes, periodic != 0, blockIdx.x, W, j.out,
+                            out_stride, sm);
 }
 
 constexpr int kMaxD = TBSLAS_MAX_DEGREE + 1;
@@ -248,6 +376,27 @@ void launch_batched(const NodeEvalJob* jobs, const NodeEvalItem* items, int64_t 
   allow_smem((const void*)k_batch_eval_on_nodes<Ds>, node_eval_smem(Ds, kMaxD, 3), done);
   k_batch_eval_on_nodes<Ds><<<(unsigned)n, kNodeEvalThreads, node_eval_smem(Ds, max_qd + 1, 3),
                               s>>>(jobs, items, periodic);
+}
+
+template <int Ds>
+void launch_scatter(const NodeEvalJob& j, const double* W, int64_t out_stride, int64_t L,
+                    int periodic, cudaStream_t s) {
+  static std::atomic<uint64_t> done{0};
+  allow_smem((const void*)k_scatter_on_nodes<Ds>, node_scatter_smem(Ds, kMaxD, 3), done);
+  k_scatter_on_nodes<Ds><<<(unsigned)L, kNodeEvalThreads,
+                           node_scatter_smem(Ds, j.dst.q + 1, j.src.dof), s>>>(j, W, out_stride,
+                                                                               periodic);
+}
+
+template <int Ds>
+void dispatch_scatter(int ds, const NodeEvalJob& j, const double* W, int64_t out_stride,
+                      int64_t L, int periodic, cudaStream_t s) {
+  if constexpr (Ds <= kMaxD) {
+    if (ds == Ds)
+      launch_scatter<Ds>(j, W, out_stride, L, periodic, s);
+    else
+      dispatch_scatter<Ds + 1>(ds, j, W, out_stride, L, periodic, s);
+  }
 }
 
 template <int Ds>
@@ -284,6 +433,19 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
   for (int i = 0; i <= dst.q; ++i) j.nodes.x[i] = x[i];
   j.out = out;
   dispatch_single<1>(src.q + 1, j, dst.L, periodic, s);
+}
+
+void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int periodic,
+                             const double* W, double* out, int64_t out_stride, cudaStream_t s) {
+  if (dst.L <= 0) return;
+  NodeEvalJob j;
+  j.src = src;
+  j.dst = dst;
+  std::memset(&j.nodes, 0, sizeof(j.nodes));
+  const std::vector<double> x = cheb_nodes_1d(dst.q);
+  for (int i = 0; i <= dst.q; ++i) j.nodes.x[i] = x[i];
+  j.out = out;
+  dispatch_scatter<1>(src.q + 1, j, W, out_stride, dst.L, periodic, s);
 }
 
 void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* items,

@@ -49,3 +49,34 @@ def test_aggregate_two_ranks_gloo():
         assert p.exitcode == 0
     for rank, pts, sec in res:
         assert pts == 3000 and sec == 1.5
+
+
+def _tiny_tree_workload():
+    from tbslas_gb300 import fields, trees, workloads
+    a, d = trees.uniform_tree(1)
+    q = 3
+    vc = trees.fit(fields.rotation(1.0), a, d, q, 3)
+    cc = trees.fit(fields.gaussian((0.5, 0.5, 0.5), 0.2), a, d, q, 1)
+    return workloads.TreeWorkload("tiny", (a, d, vc), (a, d, cc), q, 0.01, 0, "tiny")
+
+
+class _Args:
+    steps, warmup = 1, 0
+
+
+def test_reference_arm_tree_and_adapters(capsys):
+    """--impl reference on a tree workload prints the contract line; the
+    batch and adjoint adapters hand cpu_baseline_tree the fields it reads."""
+    import json
+    wl = _tiny_tree_workload()
+    bench.run_reference(_Args(), wl)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
+    batch = type("B", (), {})()
+    batch.bc = 1
+    batch.problems = [dict(va=wl.va, vd=wl.vd, vc=wl.vc, ca=wl.ca, cd=wl.cd, cc=wl.cc, q=wl.q,
+                           dt=wl.dt)]
+    t = bench._pick(batch, 3)
+    assert t.q == wl.q and t.bc == 1 and t.cc is wl.cc
+    assert bench._pick(wl, 0) is wl

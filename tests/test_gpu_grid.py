@@ -80,3 +80,29 @@ def test_semilag_grid_full_size_shift_and_sample(ctx, ora):
         ref = ora.semilag_grid(vel, con, N, dt, 1, True, lo, lo + 40000)
         assert rel_err(out[lo:lo + 40000], ref) <= TOL
     del torch
+
+
+@pytest.mark.parametrize("N", [16, 24])
+def test_semilag_grid_nan_velocity_matches_fp64_sums(ctx, N):
+    """A non-finite velocity value (NaN, inf) gives the FP64 path's result in
+    the double-float path too: the point it moves is 'outside' (value 0, no
+    stencil read), exactly as make_stencil treats it."""
+    rng = np.random.default_rng(N)
+    vel = fields.fourier_velocity_grid(rng, N)
+    con = fields.periodic_blob_grid(N, (0.4, 0.55, 0.5), 0.12)
+    vel[0, 3, 4, 5] = np.nan
+    vel[2, 1, 7, 2] = np.inf
+    dt = 1.5 / N
+    out = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, dt, 1, 1).cpu().numpy()
+    try:
+        ctx.sums = tb.SUMS_FP64
+        ref = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, dt, 1, 1).cpu().numpy()
+    finally:
+        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+    assert np.array_equal(np.isnan(out), np.isnan(ref))
+    ok = ~np.isnan(ref)
+    assert np.abs(out[ok] - ref[ok]).max() <= 1e-13 * np.abs(ref[ok]).max()
+    # the double-float split reported the non-finite values (kErrDfRange)
+    with pytest.raises(tb.capi.TbslasError) as e:
+        ctx.check()
+    assert e.value.status == 7  # TBSLAS_ERR_DEVICE
