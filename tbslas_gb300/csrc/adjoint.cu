@@ -93,7 +93,7 @@ extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbsl
   int64_t ncf = 0;
   tree_coeff(con, &coeff, &ncf);
   tree_coeff2(con, &coeff2);
-  launch_refit(vals, F, q, tc.L, 1, tc.stride, coeff, coeff2, ctx_err(ctx), s);
+  launch_refit(vals, F, q, tc.L, 1, tc.stride, coeff, coeff2, ctx_err(ctx), false, s);
   return launched("refit launch");
 }
 
@@ -119,7 +119,7 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   if (st != TBSLAS_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
   // mu = lambda^{k+1} M^T, one row of Np node weights per leaf
-  launch_refit_t(lambda_next_dev, F, q, tc.L, mu, s);
+  launch_refit_t(lambda_next_dev, F, q, tc.L, mu, ctx_sums(ctx) == TBSLAS_SUMS_DOUBLE_FLOAT, s);
   st = launched("transposed refit launch");
   if (st != TBSLAS_OK) return st;
   if (cudaMemsetAsync(lambda_k_dev, 0, sizeof(double) * tc.L * nc, s) != cudaSuccess)
@@ -138,6 +138,7 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   a.lambda = lambda_k_dev;
   a.grad_vel = grad_vel_dev;
   a.wnode = nullptr;
+  a.vn = nullptr;
   if (ctx_sums(ctx) == TBSLAS_SUMS_FP64) {
     g_adj.adj[q](a, s);
   } else {
@@ -148,11 +149,19 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
     if (st != TBSLAS_OK) return st;
     st = ctx_wnode_scratch(ctx, tc.L * np * 3, &a.wnode);
     if (st != TBSLAS_OK) return st;
+    if (!xmid_dev) {
+      // recompute: the first stage from the node grid
+      double* vn = nullptr;
+      st = ctx_vn_scratch(ctx, tc.L * np * 3, &vn);
+      if (st != TBSLAS_OK) return st;
+      launch_eval_on_nodes(tv, tc, bc, vn, s);
+      a.vn = vn;
+    }
     launch_split(con_coeff_k_dev, c2, tc.L * nc, ctx_err(ctx), s);
     g_adj.adj_df[q](a, c2, s);
     st = launched("adjoint step launch");
     if (st != TBSLAS_OK) return st;
-    launch_scatter_on_nodes(tv, tc, bc, a.wnode, grad_vel_dev, 3 * nc, s);
+    launch_scatter_on_nodes(tv, tc, bc, a.wnode, grad_vel_dev, 3 * nc, true, s);
   }
   return launched("adjoint step launch");
 }

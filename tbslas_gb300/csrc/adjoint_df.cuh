@@ -11,6 +11,12 @@
 
 namespace tbg {
 
+// Targets (threads) per CTA of the double-float adjoint: 192 gives every warp
+// one coefficient per scatter pass at q = 8 (Nc = 165); with 128 threads two
+// warps carried a second coefficient and set the pace (measured on GB300,
+// q = 8: 36.0 -> 34.0 ms per 4-step adjoint pass of a 4096-leaf tree).
+constexpr int kAdjDfThreads = 192;
+
 // Per-thread shared-memory slots of the gradient sums, 4*D elements: T_j(y),
 // dT_j(y), T_i(z), dT_i(z) (ThreadSlots: element k at s[k * blockDim]).
 // The gradient's coefficients: one component, or sum_a g_a c_a over the three
@@ -140,18 +146,18 @@ __device__ __forceinline__ df df_mul(df a, df b) {
 // x, y, z Chebyshev values, up to three weights and the leaf.
 template <int D>
 struct AdjStageDF {
-  float2 tx[kAdjThreads][D];
-  float2 ty[kAdjThreads][D];
-  float2 tz[kAdjThreads][D];
-  float2 w[kAdjThreads][3];
-  long long leaf[kAdjThreads];
+  float2 tx[kAdjDfThreads][D];
+  float2 ty[kAdjDfThreads][D];
+  float2 tz[kAdjDfThreads][D];
+  float2 w[kAdjDfThreads][3];
+  long long leaf[kAdjDfThreads];
   long long cur;
 };
 
 template <int D>
 constexpr size_t adj_df_smem() {
   const size_t stage = sizeof(AdjStageDF<D>);
-  const size_t slots = (size_t)4 * D * kAdjThreads * sizeof(float2);
+  const size_t slots = (size_t)4 * D * kAdjDfThreads * sizeof(float2);
   return stage > slots ? stage : slots;
 }
 
@@ -164,7 +170,7 @@ __device__ __forceinline__ void cta_scatter_df(AdjStageDF<D>& sm, double* __rest
                                                const double (&w)[DOF], const double (&tx)[D],
                                                const double (&ty)[D], const double (&tz)[D]) {
   constexpr int NC = D * (D + 1) * (D + 2) / 6;
-  constexpr int PER = (NC + kAdjThreads - 1) / kAdjThreads;
+  constexpr int PER = (NC + kAdjDfThreads - 1) / kAdjDfThreads;
   const int tid = threadIdx.x;
   __syncthreads();  // the staging area is free
   sm.leaf[tid] = leaf;
@@ -185,7 +191,7 @@ __device__ __forceinline__ void cta_scatter_df(AdjStageDF<D>& sm, double* __rest
   int mi[PER], mj[PER], mk[PER];
 #pragma unroll
   for (int c = 0; c < PER; ++c) {
-    const int n = tid + c * kAdjThreads;
+    const int n = tid + c * kAdjDfThreads;
     int idx = 0;
     mi[c] = -1;
     mj[c] = mk[c] = 0;
@@ -205,7 +211,7 @@ __device__ __forceinline__ void cta_scatter_df(AdjStageDF<D>& sm, double* __rest
     if (tid < 32) {
       long long first = -1;
 #pragma unroll
-      for (int chunk = 0; chunk < kAdjThreads / 32; ++chunk) {
+      for (int chunk = 0; chunk < kAdjDfThreads / 32; ++chunk) {
         const long long v = sm.leaf[chunk * 32 + tid];
         const unsigned m = __ballot_sync(0xffffffffu, v >= 0);
         if (m) {
@@ -223,7 +229,7 @@ __device__ __forceinline__ void cta_scatter_df(AdjStageDF<D>& sm, double* __rest
     for (int c = 0; c < PER; ++c)
 #pragma unroll
       for (int l = 0; l < DOF; ++l) acc[c][l] = df{0.f, 0.f};
-    for (int p = 0; p < kAdjThreads; ++p) {
+    for (int p = 0; p < kAdjDfThreads; ++p) {
       if (sm.leaf[p] != cur) continue;
       df wp[DOF];
 #pragma unroll
@@ -240,7 +246,7 @@ __device__ __forceinline__ void cta_scatter_df(AdjStageDF<D>& sm, double* __rest
 #pragma unroll
     for (int c = 0; c < PER; ++c) {
       if (mi[c] < 0) continue;
-      const int n = tid + c * kAdjThreads;
+      const int n = tid + c * kAdjDfThreads;
 #pragma unroll
       for (int l = 0; l < DOF; ++l) {
         const double v = df_to_double(df_norm(acc[c][l]));
@@ -253,17 +259,16 @@ __device__ __forceinline__ void cta_scatter_df(AdjStageDF<D>& sm, double* __rest
   }
 }
 
-// Five (q <= 8) or four 128-thread CTAs per SM: with the register cap the
-// kernel spills a little but keeps 16-20 warps resident (measured on GB300,
-// q = 8: 43.1 -> 35.9 ms per adjoint pass of a 4096-leaf tree).
+// Four (q <= 8) or three CTAs per SM: with the register cap the kernel
+// spills a little but keeps 24 or 18 warps resident.
 template <int D>
-__global__ void __launch_bounds__(kAdjThreads, (D <= 9 ? 5 : 4)) k_adjoint_df(const AdjArgs a,
+__global__ void __launch_bounds__(kAdjDfThreads, (D <= 9 ? 4 : 3)) k_adjoint_df(const AdjArgs a,
                                                             const float2* __restrict__ con2) {
   constexpr int NP = D * D * D;
   constexpr int NC = D * (D + 1) * (D + 2) / 6;
   extern __shared__ __align__(16) unsigned char adj_df_raw[];
   AdjStageDF<D>& sm = *reinterpret_cast<AdjStageDF<D>*>(adj_df_raw);
-  const ThreadSlots slots{reinterpret_cast<float2*>(adj_df_raw) + threadIdx.x, kAdjThreads};
+  const ThreadSlots slots{reinterpret_cast<float2*>(adj_df_raw) + threadIdx.x, kAdjDfThreads};
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool active = t < a.con.L * NP;
   const bool per = a.periodic != 0;
@@ -283,6 +288,23 @@ __global__ void __launch_bounds__(kAdjThreads, (D <= 9 ? 5 : 4)) k_adjoint_df(co
     xd = a.xdep[3 * tt];
     yd = a.xdep[3 * tt + 1];
     zd = a.xdep[3 * tt + 2];
+  } else if (a.vn) {
+    // recompute from the node-grid velocity (bit-identical to eval_point at X)
+    double v[3];
+    double px = x, py = y, pz = z;
+    if (per) {
+      px = wrap1(px);
+      py = wrap1(py);
+      pz = wrap1(pz);
+    }
+    xs = fma(0.5 * a.tau, __ldg(a.vn + 3 * tt + 0), px);
+    ys = fma(0.5 * a.tau, __ldg(a.vn + 3 * tt + 1), py);
+    zs = fma(0.5 * a.tau, __ldg(a.vn + 3 * tt + 2), pz);
+    double qx = xs, qy = ys, qz = zs;
+    eval_point<D, 3>(a.vel, qx, qy, qz, per, v);
+    xd = fma(a.tau, v[0], px);
+    yd = fma(a.tau, v[1], py);
+    zd = fma(a.tau, v[2], pz);
   } else {
     double v[3];
     double px = x, py = y, pz = z;
@@ -390,7 +412,7 @@ void launch_adjoint_df(const AdjArgs& a, const float2* con2, cudaStream_t s) {
     attr = true;
   }
   if (n > 0)
-    k_adjoint_df<D><<<(unsigned)((n + kAdjThreads - 1) / kAdjThreads), kAdjThreads, smem, s>>>(
+    k_adjoint_df<D><<<(unsigned)((n + kAdjDfThreads - 1) / kAdjDfThreads), kAdjDfThreads, smem, s>>>(
         a, con2);
 }
 

@@ -45,6 +45,8 @@ struct AdjArgs {
   double* grad_vel;    // [Lv][3][Nc] accumulated
   double* wnode;       // [Lc * Np][3]: weights of the tau^2/2 term at the nodes for
                        // the node-grid scatter (launch_scatter_on_nodes), or null
+  const double* vn;    // [Lc * Np][3]: v(X) from the node grid for the recompute
+                       // (bit-identical to eval_point at X), or null
 };
 
 // T_k and dT_k/dxi for k < D; zero outside [-1,1] like cheb_T.

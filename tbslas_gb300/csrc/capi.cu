@@ -518,7 +518,7 @@ int refit_dev(tbslas_ctx ctx, tbslas_tree tree, const double* vals, cudaStream_t
   TRY(device_F(ctx, tree->q, &F));
   ProfScope p(ctx, "refit", s, tree->dof == 3 ? 2 : 1);
   launch_refit(vals, F, tree->q, tree->L * tree->dof, tree->dof, tree->stride, tree->d_coeff,
-               tree->d_coeff2, ctx->d_err, s);
+               tree->d_coeff2, ctx->d_err, ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT, s);
   TRY(check_launch("refit"));
   if (tree->dof == 3) {  // a velocity-shaped tree: its norms feed the double-float bounds
     k_cnorm<<<blocks_for(tree->L * 3, 128), 128, 0, s>>>(tree->d_coeff, tree->L, 3,
@@ -816,6 +816,7 @@ int ctx_c2_scratch(tbslas_ctx ctx, size_t n, float2** out) {
 int ctx_wnode_scratch(tbslas_ctx ctx, size_t n, double** out) {
   return scratch_t(ctx, kAdjW, n, out);
 }
+int ctx_vn_scratch(tbslas_ctx ctx, size_t n, double** out) { return scratch_t(ctx, kVN, n, out); }
 
 int ctx_F(tbslas_ctx ctx, int q, const double** F) {
   TRY(bind(ctx));

@@ -108,7 +108,8 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
 // Transposed: out[V * out_stride + l * Nc + n] += sum over dst's nodes p in
 // leaf V of W[p][l] phi_n(X_p) (FP64 atomics); W: [dst.L * Np][src.dof].
 void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int periodic,
-                             const double* W, double* out, int64_t out_stride, cudaStream_t s);
+                             const double* W, double* out, int64_t out_stride, bool df_sums,
+                             cudaStream_t s);
 // Batched: one item per (job, destination leaf); the jobs of one launch
 // share the source degree q_src, max_q_dst bounds their destination degrees.
 struct NodeEvalJob {
@@ -128,11 +129,13 @@ void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* ite
 // Refit (refit.cu): node values -> coefficients through the separable
 // factors F = refit_factors(q) (4 D x D blocks on the device).
 //   coeff[(r/dof)*stride + (r%dof)*nc + t] = sum_p vals[r*np + p] M[p][t]
+// df_sums: the passes in double-float (the default step), else FP64
 void launch_refit(const double* vals, const double* F, int q, int64_t rows, int dof,
-                  int64_t stride, double* coeff, float2* coeff2, uint32_t* err, cudaStream_t s);
+                  int64_t stride, double* coeff, float2* coeff2, uint32_t* err, bool df_sums,
+                  cudaStream_t s);
 // mu[r*np + p] = sum_t M[p][t] lam[r*nc + t] (the adjoint's transposed refit)
 void launch_refit_t(const double* lam, const double* F, int q, int64_t rows, double* mu,
-                    cudaStream_t s);
+                    bool df_sums, cudaStream_t s);
 // Batched refit: one job per problem, one CTA per (job, row) item.
 struct RefitJob {
   const double* vals;
@@ -155,6 +158,7 @@ uint32_t* ctx_err(tbslas_ctx ctx);
 int ctx_sums(tbslas_ctx ctx);
 int ctx_c2_scratch(tbslas_ctx ctx, size_t n, float2** out);
 int ctx_wnode_scratch(tbslas_ctx ctx, size_t n, double** out);
+int ctx_vn_scratch(tbslas_ctx ctx, size_t n, double** out);
 
 // misc kernels (capi.cu)
 void launch_collect(const TreeView& t, const Nodes1D& nodes, double* out, cudaStream_t s);

@@ -16,6 +16,10 @@
 // and the same node and local coordinates, so every value is bit-identical to
 // the pointwise FP64 evaluation (eval_point).
 //
+// Neighbouring leaves of one depth share their face nodes (the stretched end
+// nodes are exactly 0 and 1 at most degrees): a leaf's shared upper-face
+// nodes are not evaluated but copied from the neighbour afterwards.
+//
 // One CTA per destination leaf.  Leaves tile the unit cube (tree_create
 // checks it), so the nodes a source leaf holds are those inside its box:
 // starting from the first node not yet evaluated, one key search finds its
@@ -56,6 +60,35 @@ __device__ __forceinline__ void cheb_T_col(double xi, double* T, int stride) {
   }
 }
 
+// Arithmetic of the transposed passes: FP64, or double-float pairs
+// accumulated with df_fma_acc (df64.cuh).
+struct NodeF64 {
+  typedef double T;
+  __device__ static T zero() { return 0.0; }
+  __device__ static void mac(T& acc, T a, T b) { acc = fma(a, b, acc); }
+  __device__ static T done(T acc) { return acc; }
+  __device__ static T from(double x) { return x; }
+  __device__ static double value(T v) { return v; }
+};
+struct NodeDF {
+  typedef float2 T;
+  __device__ static T zero() { return make_float2(0.f, 0.f); }
+  __device__ static void mac(T& acc, T a, T b) {
+    df s{acc.x, acc.y};
+    df_fma_acc(s, df{a.x, a.y}, df{b.x, b.y});
+    acc = make_float2(s.hi, s.lo);
+  }
+  __device__ static T done(T acc) {
+    const df v = df_norm(df{acc.x, acc.y});
+    return make_float2(v.hi, v.lo);
+  }
+  __device__ static T from(double x) {
+    const df v = df_from_double(x);
+    return make_float2(v.hi, v.lo);
+  }
+  __device__ static double value(T v) { return df_to_double(df_norm(df{v.x, v.y})); }
+};
+
 // Shared memory of the sub-grid walk: coordinates 3*Dd and T tables
 // 3*Ds*Dd (doubles), quantised coordinates and index lists 6*Dd (ints), the
 // node state Dd^3 (bytes); then the pass buffers of the caller.
@@ -69,7 +102,8 @@ __host__ __device__ constexpr size_t node_eval_smem(int Ds, int Dd, int dof) {
 __host__ __device__ constexpr size_t node_scatter_smem(int Ds, int Dd, int dof) {
   (void)dof;
   return walk_smem(Ds, Dd) +
-         (size_t)(Dd * Dd * Dd + Ds * Dd * Dd + Ds * (Ds + 1) / 2 * Dd) * 8;  // W, H, G
+         (size_t)(3 * Ds * Dd + Dd * Dd * Dd + Ds * Dd * Dd + Ds * (Ds + 1) / 2 * Dd) *
+             8;  // T (pass arithmetic), W, H, G
 }
 
 // The part of a destination leaf's node grid inside one source leaf: leaf
@@ -82,17 +116,65 @@ struct SubGrid {
   const double *Tx, *Ty, *Tz;
 };
 
+// Node (a, b, c) of destination leaf `leaf` on an upper face, where its
+// point is also a node of the neighbouring destination leaf of the same
+// depth that contains it (the stretched end nodes are exactly 0 and 1, so
+// neighbours share face nodes): returns that node's target index -- the
+// neighbour's node with the upper-face indices set to 0, which is not itself
+// on an upper face -- or -1.  The point is the same double, so its source
+// leaf and value are the same.
+__device__ __forceinline__ int64_t face_source(const TreeView& dst, const Nodes1D& nodes, bool per,
+                                               int64_t leaf, const Geom& g, int a, int b, int c) {
+  const int Dd = dst.q + 1;
+  if (a != Dd - 1 && b != Dd - 1 && c != Dd - 1) return -1;
+  if (nodes.x[0] != 0.0 || nodes.x[Dd - 1] != 1.0) return -1;
+  const double h = 2.0 / g.w;
+  double x = g.x + h * nodes.x[a], y = g.y + h * nodes.x[b], z = g.z + h * nodes.x[c];
+  if (per) {
+    x = wrap1(x);
+    y = wrap1(y);
+    z = wrap1(z);
+  }
+  if (!inside(x, y, z, per)) return -1;
+  const int64_t B = find_leaf(dst, morton3(quantise(x), quantise(y), quantise(z)));
+  if (B == leaf) return -1;
+  const Geom gb = load_geom(dst.geom + B);
+  if (gb.w != g.w) return -1;
+  int ia = a, ib = b, ic = c;
+  if (a == Dd - 1) {
+    if (gb.x != x) return -1;
+    ia = 0;
+  } else if (gb.x != g.x) {
+    return -1;
+  }
+  if (b == Dd - 1) {
+    if (gb.y != y) return -1;
+    ib = 0;
+  } else if (gb.y != g.y) {
+    return -1;
+  }
+  if (c == Dd - 1) {
+    if (gb.z != z) return -1;
+    ic = 0;
+  } else if (gb.z != g.z) {
+    return -1;
+  }
+  return B * (int64_t)Dd * Dd * Dd + ia + Dd * (ib + Dd * ic);
+}
+
 // Walks the destination leaf's nodes source leaf by source leaf.  Leaves
 // tile the unit cube (tree_create checks it), so the nodes a source leaf
 // holds are those inside its box: starting from the first node not yet
 // visited, one key search finds its source leaf and per-axis box tests give
 // the sub-grid.  outside(p) is called for nodes outside the domain, fn(sub)
-// for every sub-grid (all threads, block-synchronised around it).  The
+// for every sub-grid (all threads, block-synchronised around it); with
+// dedup, nodes that face_source maps to a neighbour's node are skipped.  The
 // walk's shared memory is the first walk_smem(Ds, Dd) bytes of sm.
 template <int Ds, class Outside, class Fn>
 __device__ __forceinline__ void for_each_subgrid(const TreeView& S, const TreeView& dst,
                                                  const Nodes1D& nodes, bool per, int64_t leaf,
-                                                 double* sm, Outside outside, Fn fn) {
+                                                 bool dedup, double* sm, Outside outside,
+                                                 Fn fn) {
   __shared__ int s_first;
   __shared__ int s_n[3];
   const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
@@ -119,7 +201,10 @@ __device__ __forceinline__ void for_each_subgrid(const TreeView& S, const TreeVi
   for (int p = tid; p < Dd3; p += bs) {
     const bool in = sq[p % Dd] != 0xffffffffu && sq[Dd + (p / Dd) % Dd] != 0xffffffffu &&
                     sq[2 * Dd + p / Dd2] != 0xffffffffu;
-    sdone[p] = in ? 0 : 1;
+    // with dedup, shared upper-face nodes are left to copy_face_nodes
+    const bool skip =
+        !in || (dedup && face_source(dst, nodes, per, leaf, g, p % Dd, (p / Dd) % Dd, p / Dd2) >= 0);
+    sdone[p] = skip ? 1 : 0;
     if (!in) outside(p);
   }
   __syncthreads();
@@ -188,7 +273,7 @@ __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const Tree
   double* sw = sm + walk_smem(Ds, Dd) / 8;  // [dof][pair(i,j)][Dd]
   double* out = out_all + leaf * (int64_t)Dd3 * dof;
   for_each_subgrid<Ds>(
-      S, dst, nodes, per, leaf, sm,
+      S, dst, nodes, per, leaf, true, sm,
       [&](int p) {
         for (int l = 0; l < dof; ++l) out[(int64_t)p * dof + l] = 0.0;
       },
@@ -243,40 +328,46 @@ __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const Tree
 // W[p][l] phi_n(X_p), the basis of V at the node -- the same passes in
 // reverse (z, then y, then x), one FP64 atomic per coefficient and sub-grid.
 // W: [dst.L * Dd^3][dof].
-template <int Ds>
+template <int Ds, class A>
 __device__ __forceinline__ void scatter_on_nodes_leaf(const TreeView& S, const TreeView& dst,
                                                       const Nodes1D& nodes, bool per,
                                                       int64_t leaf, const double* __restrict__ W,
                                                       double* __restrict__ out,
                                                       int64_t out_stride, double* sm) {
+  typedef typename A::T T;
   constexpr int NCs = Ds * (Ds + 1) * (Ds + 2) / 6, npair = Ds * (Ds + 1) / 2;
   const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
   const int dof = S.dof;
   const int tid = threadIdx.x, bs = blockDim.x;
-  double* sW = sm + walk_smem(Ds, Dd) / 8;  // [c'][b'][a'] weights of one component
-  double* sH = sW + Dd3;                    // [i][b'][a']
-  double* sG = sH + Ds * Dd2;               // [pair(i,j)][a']
+  T* sTT = reinterpret_cast<T*>(sm + walk_smem(Ds, Dd) / 8);  // [3][Ds][Dd] T in A
+  T* sW = sTT + 3 * Ds * Dd;  // [c'][b'][a'] weights of one component
+  T* sH = sW + Dd3;           // [i][b'][a']
+  T* sG = sH + Ds * Dd2;      // [pair(i,j)][a']
   const double* Wl = W + leaf * (int64_t)Dd3 * dof;
   for_each_subgrid<Ds>(
-      S, dst, nodes, per, leaf, sm, [](int) {},
+      S, dst, nodes, per, leaf, false, sm, [](int) {},
       [&](const SubGrid& sg) {
         const int na = sg.na, nb = sg.nb, nz = sg.nz;
         const int* sidx = sg.sidx;
         double* oV = out + sg.V * out_stride;
+        for (int o = tid; o < 3 * Ds * Dd; o += bs) sTT[o] = A::from(sg.Tx[o]);
+        __syncthreads();
+        const T* Tx = sTT;
+        const T* Ty = sTT + Ds * Dd;
+        const T* Tz = sTT + 2 * Ds * Dd;
         for (int l = 0; l < dof; ++l) {
           for (int o = tid; o < nz * nb * na; o += bs) {
             const int ai = o % na, r = o / na, bi = r % nb, ci = r / nb;
             const int p = sidx[ai] + Dd * (sidx[Dd + bi] + Dd * sidx[2 * Dd + ci]);
-            sW[o] = __ldg(Wl + (int64_t)p * dof + l);
+            sW[o] = A::from(__ldg(Wl + (int64_t)p * dof + l));
           }
           __syncthreads();
           // H(i, b', a') = sum_c' T_i(z_c') W(c', b', a')
           for (int o = tid; o < Ds * nb * na; o += bs) {
             const int ai = o % na, r = o / na, bi = r % nb, i = r / nb;
-            double s = 0.0;
-            for (int ci = 0; ci < nz; ++ci)
-              s = fma(sg.Tz[i * Dd + ci], sW[(ci * nb + bi) * na + ai], s);
-            sH[(i * nb + bi) * na + ai] = s;
+            T s = A::zero();
+            for (int ci = 0; ci < nz; ++ci) A::mac(s, Tz[i * Dd + ci], sW[(ci * nb + bi) * na + ai]);
+            sH[(i * nb + bi) * na + ai] = A::done(s);
           }
           __syncthreads();
           // G(pair(i,j), a') = sum_b' T_j(y_b') H(i, b', a')
@@ -288,10 +379,9 @@ __device__ __forceinline__ void scatter_on_nodes_leaf(const TreeView& S, const T
               ++i;
             }
             const int j = rem;
-            double s = 0.0;
-            for (int bi = 0; bi < nb; ++bi)
-              s = fma(sg.Ty[j * Dd + bi], sH[(i * nb + bi) * na + ai], s);
-            sG[pr * na + ai] = s;
+            T s = A::zero();
+            for (int bi = 0; bi < nb; ++bi) A::mac(s, Ty[j * Dd + bi], sH[(i * nb + bi) * na + ai]);
+            sG[pr * na + ai] = A::done(s);
           }
           __syncthreads();
           // coefficient (i,j,k): sum_a' T_k(x_a') G(pair(i,j), a')
@@ -308,13 +398,45 @@ __device__ __forceinline__ void scatter_on_nodes_leaf(const TreeView& S, const T
             }
             const int k = rem;
             const int pr = i * Ds - (i * (i - 1)) / 2 + j;
-            double s = 0.0;
-            for (int ai = 0; ai < na; ++ai) s = fma(sg.Tx[k * Dd + ai], sG[pr * na + ai], s);
-            if (s != 0.0) atomicAdd(oV + l * NCs + n, s);
+            T s = A::zero();
+            for (int ai = 0; ai < na; ++ai) A::mac(s, Tx[k * Dd + ai], sG[pr * na + ai]);
+            const double v = A::value(s);
+            if (v != 0.0) atomicAdd(oV + l * NCs + n, v);
           }
           __syncthreads();
         }
       });
+}
+
+// The values the walk left to copy: every shared upper-face node of the
+// leaf takes its neighbour's value (run after the evaluation).
+__device__ __forceinline__ void copy_face_nodes_leaf(const TreeView& dst, const Nodes1D& nodes,
+                                                     bool per, int64_t leaf, int dof,
+                                                     double* __restrict__ out) {
+  const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
+  const Geom g = load_geom(dst.geom + leaf);
+  for (int p = threadIdx.x; p < Dd3; p += blockDim.x) {
+    const int a = p % Dd, b = (p / Dd) % Dd, c = p / Dd2;
+    if (a != Dd - 1 && b != Dd - 1 && c != Dd - 1) continue;
+    const int64_t src = face_source(dst, nodes, per, leaf, g, a, b, c);
+    if (src < 0) continue;
+    const int64_t t = leaf * Dd3 + p;
+    for (int l = 0; l < dof; ++l) out[t * dof + l] = out[src * dof + l];
+  }
+}
+
+__global__ void __launch_bounds__(kNodeEvalThreads) k_copy_face_nodes(const NodeEvalJob j,
+                                                                      int periodic) {
+  copy_face_nodes_leaf(j.dst, j.nodes, periodic != 0, blockIdx.x, j.src.dof, j.out);
+}
+
+__global__ void __launch_bounds__(kNodeEvalThreads) k_batch_copy_face_nodes(
+    const NodeEvalJob* __restrict__ jobs, const NodeEvalItem* __restrict__ items, int periodic) {
+  __shared__ NodeEvalJob sj;
+  const NodeEvalItem it = items[blockIdx.x];
+  if (threadIdx.x == 0) sj = jobs[it.job];
+  __syncthreads();
+  copy_face_nodes_leaf(sj.dst, sj.nodes, periodic != 0, it.leaf, sj.src.dof, sj.out);
 }
 
 template <int Ds>
@@ -337,14 +459,14 @@ __global__ void __launch_bounds__(kNodeEvalThreads) k_batch_eval_on_nodes(
   eval_on_nodes_leaf<Ds>(sj.src, sj.dst, sj.nodes, periodic != 0, it.leaf, sj.out, sm);
 }
 
-template <int Ds>
+template <int Ds, class A>
 __global__ void __launch_bounds__(kNodeEvalThreads) k_scatter_on_nodes(const NodeEvalJob j,
                                                                        const double* W,
                                                                        int64_t out_stride,
                                                                        int periodic) {
   extern __shared__ __align__(16) double sm[];
-  scatter_on_nodes_leaf<Ds>(j.src, j.dst, j.nodes, periodic != 0, blockIdx.x, W, j.out,
-                            out_stride, sm);
+  scatter_on_nodes_leaf<Ds, A>(j.src, j.dst, j.nodes, periodic != 0, blockIdx.x, W, j.out,
+                               out_stride, sm);
 }
 
 constexpr int kMaxD = TBSLAS_MAX_DEGREE + 1;
@@ -378,24 +500,28 @@ void launch_batched(const NodeEvalJob* jobs, const NodeEvalItem* items, int64_t 
                               s>>>(jobs, items, periodic);
 }
 
-template <int Ds>
+template <int Ds, class A>
 void launch_scatter(const NodeEvalJob& j, const double* W, int64_t out_stride, int64_t L,
                     int periodic, cudaStream_t s) {
   static std::atomic<uint64_t> done{0};
-  allow_smem((const void*)k_scatter_on_nodes<Ds>, node_scatter_smem(Ds, kMaxD, 3), done);
-  k_scatter_on_nodes<Ds><<<(unsigned)L, kNodeEvalThreads,
-                           node_scatter_smem(Ds, j.dst.q + 1, j.src.dof), s>>>(j, W, out_stride,
-                                                                               periodic);
+  allow_smem((const void*)k_scatter_on_nodes<Ds, A>, node_scatter_smem(Ds, kMaxD, 3), done);
+  k_scatter_on_nodes<Ds, A><<<(unsigned)L, kNodeEvalThreads,
+                              node_scatter_smem(Ds, j.dst.q + 1, j.src.dof), s>>>(j, W, out_stride,
+                                                                                  periodic);
 }
 
 template <int Ds>
 void dispatch_scatter(int ds, const NodeEvalJob& j, const double* W, int64_t out_stride,
-                      int64_t L, int periodic, cudaStream_t s) {
+                      int64_t L, int periodic, bool df_sums, cudaStream_t s) {
   if constexpr (Ds <= kMaxD) {
-    if (ds == Ds)
-      launch_scatter<Ds>(j, W, out_stride, L, periodic, s);
-    else
-      dispatch_scatter<Ds + 1>(ds, j, W, out_stride, L, periodic, s);
+    if (ds == Ds) {
+      if (df_sums)
+        launch_scatter<Ds, NodeDF>(j, W, out_stride, L, periodic, s);
+      else
+        launch_scatter<Ds, NodeF64>(j, W, out_stride, L, periodic, s);
+    } else {
+      dispatch_scatter<Ds + 1>(ds, j, W, out_stride, L, periodic, df_sums, s);
+    }
   }
 }
 
@@ -433,10 +559,12 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
   for (int i = 0; i <= dst.q; ++i) j.nodes.x[i] = x[i];
   j.out = out;
   dispatch_single<1>(src.q + 1, j, dst.L, periodic, s);
+  k_copy_face_nodes<<<(unsigned)dst.L, kNodeEvalThreads, 0, s>>>(j, periodic);
 }
 
 void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int periodic,
-                             const double* W, double* out, int64_t out_stride, cudaStream_t s) {
+                             const double* W, double* out, int64_t out_stride, bool df_sums,
+                             cudaStream_t s) {
   if (dst.L <= 0) return;
   NodeEvalJob j;
   j.src = src;
@@ -445,7 +573,7 @@ void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int perio
   const std::vector<double> x = cheb_nodes_1d(dst.q);
   for (int i = 0; i <= dst.q; ++i) j.nodes.x[i] = x[i];
   j.out = out;
-  dispatch_scatter<1>(src.q + 1, j, W, out_stride, dst.L, periodic, s);
+  dispatch_scatter<1>(src.q + 1, j, W, out_stride, dst.L, periodic, df_sums, s);
 }
 
 void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* items,
@@ -453,6 +581,7 @@ void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* ite
                                 cudaStream_t s) {
   if (n_items <= 0) return;
   dispatch_batched<1>(q_src + 1, jobs, items, n_items, max_q_dst, periodic, s);
+  k_batch_copy_face_nodes<<<(unsigned)n_items, kNodeEvalThreads, 0, s>>>(jobs, items, periodic);
 }
 
 }  // namespace tbg

@@ -145,3 +145,26 @@ def test_adjoint_matches_dual_number_oracle(ctx, ora, vel_kind, q):
         dJ = float((resid * (dcur[:, 0, :] @ Vb.T)).sum())
         an = float((gc * dc0).sum() + (gv * dvc).sum())
         assert abs(dJ - an) <= 1e-10 * abs(dJ), (dJ, an)
+
+
+@pytest.mark.parametrize("checkpoint", [True, False])
+def test_adjoint_fp64_sums_matches_double_float(ctx, checkpoint):
+    """The all-FP64 adjoint kernel (TBSLAS_SUMS_FP64) and the default
+    double-float one give the same gradients to 1e-12."""
+    import torch
+    a, d, q, vc, c0, cobs, tv, tc = _problem(ctx, q=6, seed=9)
+    V = torch.from_numpy(adjoint.basis_at_nodes(q)).cuda()
+    co = torch.from_numpy(cobs).cuda()
+    grads = []
+    try:
+        for mode in (tb.SUMS_DOUBLE_FLOAT, tb.SUMS_FP64):
+            ctx.sums = mode
+            c0t = torch.from_numpy(c0).cuda().requires_grad_(True)
+            vct = torch.from_numpy(vc).cuda().requires_grad_(True)
+            _J(adjoint.advect(c0t, vct, tv, tc, 0.02, 1, 3, tb.Periodic, checkpoint), V,
+               co).backward()
+            grads.append((c0t.grad.cpu().numpy(), vct.grad.cpu().numpy()))
+    finally:
+        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+    for x, y in zip(grads[0], grads[1]):
+        assert np.abs(x - y).max() <= 1e-12 * np.abs(y).max()
