@@ -724,6 +724,18 @@ def run_adjoint(args, wl, rank, world, local_rank):
         fms, (c, v, j) = timed(lambda: grad(ck))
         bms, _ = timed(lambda: j.backward())
         res[ck] = (fms, bms, c.grad.clone(), v.grad.clone(), j.item())
+    # per-kernel breakdown of one more adjoint pass each way (profiler on,
+    # outside the timed passes)
+    by_kernel = {}
+    for ck in (True, False):
+        _, _, j1 = grad(ck)
+        ctx.profile(True)
+        ctx.profile_reset()
+        j1.backward()
+        torch.cuda.synchronize()
+        by_kernel["checkpoint" if ck else "recompute"] = {
+            k: round(v[2] / T, 3) for k, v in sorted(ctx.profile_totals().items())}
+        ctx.profile(False)
     gc = res[True][2]
     rng = np.random.default_rng(123)
     eps = 1e-6
@@ -753,8 +765,8 @@ def run_adjoint(args, wl, rank, world, local_rank):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded analytic fields)", "config": cfg,
             "forward": {"ms": fwd_ms, "points_per_s": points / (fwd_ms * 1e-3),
-                        "kind": "FP64 step (the differentiable forward, departure points "
-                                "bit-identical to the oracle)"},
+                        "kind": "the differentiable forward without checkpoints (the "
+                                "in-situ step, double-float sums)"},
             "forward_default": {"ms": fwd_df_ms, "points_per_s": points / (fwd_df_ms * 1e-3),
                                 "kind": "tbslas_semilag_in_situ (double-float sums)"},
             "checkpoint": {"forward_ms": ck_fms, "adjoint_ms": ck_bms,
@@ -776,6 +788,7 @@ def run_adjoint(args, wl, rank, world, local_rank):
                                             "check below is the exact test)",
                          "max_rel_err_dJ_dc0": max(errs_c), "max_rel_err_dJ_dV": max(errs_v)},
             "dual_number_check": dual,
+            "adjoint_ms_per_step_by_kernel": by_kernel,
             "checkpoint_vs_recompute_rel_diff": ck_gap, "J": res[True][4]}
     print(json.dumps(line))
     assert ctx.check() == 0

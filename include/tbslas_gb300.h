@@ -238,9 +238,12 @@ int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con
  * X of `con`; the adjoint gives dJ/dC^k and dJ/dV from dJ/dC^{k+1}.  Both
  * support Chebyshev degree 1..10, a dof-3 velocity and a dof-1 concentration
  * tree of the same degree. */
-/* tbslas_semilag_in_situ with nrk = 1 that also stores, per target node
- * (leaf-major, node order of CollectChebTreeGridPoints), the RK2 midpoint
- * xmid_dev[N*3] and departure point xdep_dev[N*3], N = L (q+1)^3. */
+/* tbslas_semilag_in_situ with nrk = 1 (same kernels, same result, the
+ * context's sum mode) that also stores, per target node (leaf-major, node
+ * order of CollectChebTreeGridPoints), the RK2 midpoint xmid_dev[N*3] and
+ * departure point xdep_dev[N*3], N = L (q+1)^3.  In the double-float mode the
+ * points lie in the FP64 step's leaves (targets near a face are recomputed in
+ * FP64) and within ~1e-15 of its points. */
 int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
                                 double dt, int bc, double* xmid_dev, double* xdep_dev,
                                 void* stream);

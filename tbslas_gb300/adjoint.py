@@ -1,7 +1,11 @@
 """Differentiable T-step SL advection: torch.autograd.Function over the
-checkpointed forward step and the hand-written adjoint kernels.  The forward
-pass runs the all-FP64 step (bit-identical departure points to the oracle),
-i.e. exactly the map the adjoint differentiates.
+in-situ SL step and the hand-written adjoint kernels.  The forward pass is
+the production step (tbslas_semilag_in_situ, in the context's sum mode).  In
+the double-float mode its leaf choices are the FP64 step's (targets near a
+face are recomputed in FP64) and its values differ from the FP64 step's by
+the sums' rounding (~1e-14), so the adjoint -- the derivative of that
+piecewise-polynomial map with the leaf choices held fixed -- is its
+derivative to the same accuracy.
 
     cT = advect(c0, vcoeff, vel_tree, con_tree, dt, timestep0, nsteps, bc, checkpoint)
 
@@ -63,7 +67,6 @@ def _function():
             vf = api.NodeFieldFunctor(vel_tree, bc)
             n = con_tree.n_leaves * api.n_points(con_tree.q)
             states, ckpts = [], []
-            tmp = None
             for k in range(nsteps):
                 states.append(con_tree.get_coeffs(torch.empty_like(c0)))
                 if checkpoint:
@@ -72,10 +75,7 @@ def _function():
                     step_ckpt(vf, con_tree, timestep0 + k, dt, xm, xd)
                     ckpts.append((xm, xd))
                 else:
-                    if tmp is None:
-                        tmp = (torch.empty((n, 3), dtype=torch.float64, device=c0.device),
-                               torch.empty((n, 3), dtype=torch.float64, device=c0.device))
-                    step_ckpt(vf, con_tree, timestep0 + k, dt, tmp[0], tmp[1])
+                    api.solve_semilag_in_situ(vf, con_tree, timestep0 + k, dt, 1)
             cT = con_tree.get_coeffs(torch.empty_like(c0))
             ctx.vel_tree, ctx.con_tree, ctx.dt, ctx.ts0, ctx.bc = vel_tree, con_tree, dt, timestep0, bc
             ctx.states, ctx.ckpts, ctx.vshape = states, ckpts, vcoeff.shape

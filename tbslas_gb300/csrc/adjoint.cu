@@ -10,13 +10,12 @@ constexpr int kAdjMaxDegree = 10;
 
 
 struct AdjTable {
-  CkptFn ckpt[kAdjMaxDegree + 1] = {};
   AdjFn adj[kAdjMaxDegree + 1] = {};
   AdjDfFn adj_df[kAdjMaxDegree + 1] = {};
   AdjTable() {
-    register_adjoint_a(ckpt, adj, adj_df);
-    register_adjoint_b(ckpt, adj, adj_df);
-    register_adjoint_c(ckpt, adj, adj_df);
+    register_adjoint_a(adj, adj_df);
+    register_adjoint_b(adj, adj_df);
+    register_adjoint_c(adj, adj_df);
   }
 };
 const AdjTable g_adj;
@@ -63,38 +62,13 @@ using namespace tbg;
 extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
                                            int timestep, double dt, int bc, double* xmid_dev,
                                            double* xdep_dev, void* stream) {
+  // the in-situ step itself (the context's sum mode), storing the points
   TreeView tv, tc;
   int st = check_pair(ctx, vel, con, dt, bc, &tv, &tc);
   if (st != TBSLAS_OK) return st;
   if (!xmid_dev || !xdep_dev) return fail_status(TBSLAS_ERR_INVALID_ARG, "null checkpoint buffer");
-  const int q = tc.q, d = q + 1;
-  const int64_t np = (int64_t)d * d * d, nc = (int64_t)d * (d + 1) * (d + 2) / 6;
-  double* vals = nullptr;
-  st = ctx_vals_scratch(ctx, tc.L * np, &vals);
-  if (st != TBSLAS_OK) return st;
-  const double* F = nullptr;
-  st = ctx_F(ctx, q, &F);
-  if (st != TBSLAS_OK) return st;
-  cudaStream_t s = (cudaStream_t)stream;
-  CkptArgs a;
-  a.vel = tv;
-  a.con = tc;
-  a.nodes = ctx_nodes(q);
-  a.tau = step_tau_host(timestep, dt);
-  a.periodic = bc;
-  a.vals = vals;
-  a.xmid = xmid_dev;
-  a.xdep = xdep_dev;
-  g_adj.ckpt[q](a, s);
-  st = launched("checkpointed SL step launch");
-  if (st != TBSLAS_OK) return st;
-  double* coeff = nullptr;
-  float2* coeff2 = nullptr;
-  int64_t ncf = 0;
-  tree_coeff(con, &coeff, &ncf);
-  tree_coeff2(con, &coeff2);
-  launch_refit(vals, F, q, tc.L, 1, tc.stride, coeff, coeff2, ctx_err(ctx), false, s);
-  return launched("refit launch");
+  return semilag_in_situ_points(ctx, vel, con, timestep, dt, bc, xmid_dev, xdep_dev,
+                                (cudaStream_t)stream);
 }
 
 extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
@@ -119,7 +93,10 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   if (st != TBSLAS_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
   // mu = lambda^{k+1} M^T, one row of Np node weights per leaf
-  launch_refit_t(lambda_next_dev, F, q, tc.L, mu, ctx_sums(ctx) == TBSLAS_SUMS_DOUBLE_FLOAT, s);
+  {
+    ProfBracket pb(ctx, "adjoint_refit_t", s);
+    launch_refit_t(lambda_next_dev, F, q, tc.L, mu, ctx_sums(ctx) == TBSLAS_SUMS_DOUBLE_FLOAT, s);
+  }
   st = launched("transposed refit launch");
   if (st != TBSLAS_OK) return st;
   if (cudaMemsetAsync(lambda_k_dev, 0, sizeof(double) * tc.L * nc, s) != cudaSuccess)
@@ -138,8 +115,8 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   a.lambda = lambda_k_dev;
   a.grad_vel = grad_vel_dev;
   a.wnode = nullptr;
-  a.vn = nullptr;
   if (ctx_sums(ctx) == TBSLAS_SUMS_FP64) {
+    ProfBracket pb(ctx, "adjoint_fp64", s);
     g_adj.adj[q](a, s);
   } else {
     // the sums in double-float over a hi/lo split of c^k; the node term by
@@ -150,17 +127,25 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
     st = ctx_wnode_scratch(ctx, tc.L * np * 3, &a.wnode);
     if (st != TBSLAS_OK) return st;
     if (!xmid_dev) {
-      // recompute: the first stage from the node grid
-      double* vn = nullptr;
-      st = ctx_vn_scratch(ctx, tc.L * np * 3, &vn);
+      // recompute: the step's points by its double-float kernels (FP64 for
+      // the ambiguous targets)
+      double *xm = nullptr, *xd = nullptr;
+      st = step_points_df(ctx, vel, con, timestep, dt, bc, &xm, &xd, s);
       if (st != TBSLAS_OK) return st;
-      launch_eval_on_nodes(tv, tc, bc, vn, s);
-      a.vn = vn;
+      a.xmid = xm;
+      a.xdep = xd;
     }
-    launch_split(con_coeff_k_dev, c2, tc.L * nc, ctx_err(ctx), s);
-    g_adj.adj_df[q](a, c2, s);
+    {
+      ProfBracket pb(ctx, "adjoint_split", s);
+      launch_split(con_coeff_k_dev, c2, tc.L * nc, ctx_err(ctx), s);
+    }
+    {
+      ProfBracket pb(ctx, "adjoint_df", s);
+      g_adj.adj_df[q](a, c2, s);
+    }
     st = launched("adjoint step launch");
     if (st != TBSLAS_OK) return st;
+    ProfBracket pb(ctx, "adjoint_node_scatter", s);
     launch_scatter_on_nodes(tv, tc, bc, a.wnode, grad_vel_dev, 3 * nc, true, s);
   }
   return launched("adjoint step launch");

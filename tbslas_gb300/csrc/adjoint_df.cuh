@@ -1,10 +1,12 @@
 // The adjoint step of adjoint_kernels.cuh with its sums in double-float
 // (df64.cuh): the two gradient sums (grad c^k at Xd, grad(g . v) at X*) and
-// the three CTA-cooperative scatters run as hi/lo float pairs on the FP32
-// pipe; point locations, T_k and dT_k recurrences, the weights and the global
-// accumulation (FP64 atomics) stay FP64.  The checkpointed points are the
-// FP64 forward's, so every leaf choice is the FP64 adjoint's and results
-// differ from it by the sums' rounding (~1e-15 relative).
+// the two CTA-cooperative scatters at those points run as hi/lo float pairs
+// on the FP32 pipe; point locations, T_k and dT_k recurrences, the weights
+// and the global accumulation (FP64 atomics) stay FP64, and the third
+// scatter (at the node X) is the transposed node-grid pass.  The points are
+// the step's own (checkpointed by the forward, whose leaf choices are the
+// FP64 step's, or recomputed in FP64), so results differ from the FP64
+// adjoint by the sums' rounding (~1e-15 relative).
 #pragma once
 
 #include "adjoint_kernels.cuh"
@@ -17,8 +19,6 @@ namespace tbg {
 // q = 8: 36.0 -> 34.0 ms per 4-step adjoint pass of a 4096-leaf tree).
 constexpr int kAdjDfThreads = 192;
 
-// Per-thread shared-memory slots of the gradient sums, 4*D elements: T_j(y),
-// dT_j(y), T_i(z), dT_i(z) (ThreadSlots: element k at s[k * blockDim]).
 // The gradient's coefficients: one component, or sum_a g_a c_a over the three
 // velocity components.
 struct GradOne {
@@ -142,102 +142,137 @@ __device__ __forceinline__ df df_mul(df a, df b) {
   return df{p, e};
 }
 
-// Staging of one block's points for a double-float scatter: per point the
-// x, y, z Chebyshev values, up to three weights and the leaf.
+// Shared memory of the double-float adjoint.  Every thread owns NS slots of
+// one double-float each (ThreadSlots: element e of thread t at
+// slots[e * BS + t]); the stride BS is odd, so that a warp reading element
+// e_lane of one point's column -- the scatters, one coefficient per lane --
+// touches distinct banks for distinct e.  Slot map of a point:
+//   [0, D)    T_j(y)
+//   [D, 2D)   dT_j(y) for the gradient, then T_k(x) for the scatter
+//   [2D, 3D)  T_i(z)
+//   [3D, 4D)  dT_i(z) for the gradient, then the scatter's weights
 template <int D>
-struct AdjStageDF {
-  float2 tx[kAdjDfThreads][D];
-  float2 ty[kAdjDfThreads][D];
-  float2 tz[kAdjDfThreads][D];
-  float2 w[kAdjDfThreads][3];
-  long long leaf[kAdjDfThreads];
-  long long cur;
+struct AdjDfShared {
+  static constexpr int BS = kAdjDfThreads + 1;
+  static constexpr int NS = 4 * D > 3 * D + 3 ? 4 * D : 3 * D + 3;
+  float2 slots[NS * BS];
+  int leaf[kAdjDfThreads];            // scatter leaf of each point (-1: none / done)
+  unsigned char list[kAdjDfThreads];  // points of the leaf in progress
+  int wcount[kAdjDfThreads / 32];
+  int cur;
 };
 
 template <int D>
 constexpr size_t adj_df_smem() {
-  const size_t stage = sizeof(AdjStageDF<D>);
-  const size_t slots = (size_t)4 * D * kAdjDfThreads * sizeof(float2);
-  return stage > slots ? stage : slots;
+  return sizeof(AdjDfShared<D>);
 }
 
-// out[leaf*stride + l*NC + n] += w[l] * phi_n(point) for every thread's point
-// (leaf < 0: none); the thread's coefficients n = tid + c*blockDim are
-// carried together through one pass over the block's points of each leaf.
-template <int D, int DOF>
-__device__ __forceinline__ void cta_scatter_df(AdjStageDF<D>& sm, double* __restrict__ out,
-                                               int64_t stride, int64_t leaf,
-                                               const double (&w)[DOF], const double (&tx)[D],
-                                               const double (&ty)[D], const double (&tz)[D]) {
-  constexpr int NC = D * (D + 1) * (D + 2) / 6;
-  constexpr int PER = (NC + kAdjDfThreads - 1) / kAdjDfThreads;
-  const int tid = threadIdx.x;
-  __syncthreads();  // the staging area is free
-  sm.leaf[tid] = leaf;
-  if (leaf >= 0) {
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-      const df a = df_split_bits(tx[k]), b = df_split_bits(ty[k]), c = df_split_bits(tz[k]);
-      sm.tx[tid][k] = make_float2(a.hi, a.lo);
-      sm.ty[tid][k] = make_float2(b.hi, b.lo);
-      sm.tz[tid][k] = make_float2(c.hi, c.lo);
-    }
-#pragma unroll
-    for (int l = 0; l < DOF; ++l) {
-      const df v = df_from_double(w[l]);
-      sm.w[tid][l] = make_float2(v.hi, v.lo);
-    }
-  }
-  int mi[PER], mj[PER], mk[PER];
+// Slot offsets of T_i(z), T_j(y), T_k(x) for this thread's scatter
+// coefficients n = tid + c * blockDim (triangular order; oz < 0: none).
+template <int D, int PER>
+__device__ __forceinline__ void scatter_offsets(int (&oz)[PER], int (&oy)[PER], int (&ox)[PER]) {
+  constexpr int BS = AdjDfShared<D>::BS;
 #pragma unroll
   for (int c = 0; c < PER; ++c) {
-    const int n = tid + c * kAdjDfThreads;
+    const int n = threadIdx.x + c * kAdjDfThreads;
     int idx = 0;
-    mi[c] = -1;
-    mj[c] = mk[c] = 0;
+    oz[c] = -1;
+    oy[c] = ox[c] = 0;
     for (int i = 0; i < D; ++i)
       for (int j = 0; j < D - i; ++j) {
         const int len = D - i - j;
         if (n >= idx && n < idx + len) {
-          mi[c] = i;
-          mj[c] = j;
-          mk[c] = n - idx;
+          oz[c] = (2 * D + i) * BS;
+          oy[c] = j * BS;
+          ox[c] = (D + n - idx) * BS;
         }
         idx += len;
       }
   }
+}
+
+// out[leaf*stride + l*NC + n] += w[l] * phi_n(point) for every thread's point
+// (lf < 0: none).  The point's T_j(y) and T_i(z) are in its slots (from
+// grad_tables), T_k(x) in tx.  For each distinct leaf among the block's
+// points, in order of first appearance, the points of that leaf are listed
+// (ballot compaction, in thread order) and every thread sums its
+// coefficients over the list, adding each to global memory with one FP64
+// atomic.  All threads of the block call it; it ends after a barrier that
+// every thread passes once it has finished reading the slots.
+template <int D, int DOF, int PER>
+__device__ __forceinline__ void scatter_df(AdjDfShared<D>& sm, double* __restrict__ out,
+                                           int64_t stride, int64_t lf, const df (&tx)[D],
+                                           const double (&w)[DOF], const int (&oz)[PER],
+                                           const int (&oy)[PER], const int (&ox)[PER]) {
+  constexpr int NC = D * (D + 1) * (D + 2) / 6;
+  constexpr int BS = AdjDfShared<D>::BS;
+  constexpr int NW = kAdjDfThreads / 32;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (lf >= 0) {
+    float2* const col = sm.slots + tid;
+#pragma unroll
+    for (int k = 0; k < D; ++k) col[(D + k) * BS] = make_float2(tx[k].hi, tx[k].lo);
+#pragma unroll
+    for (int l = 0; l < DOF; ++l) {
+      const df v = df_from_double(w[l]);
+      col[(3 * D + l) * BS] = make_float2(v.hi, v.lo);
+    }
+  }
+  const int my_leaf = lf >= 0 ? (int)lf : -1;
+  sm.leaf[tid] = my_leaf;
+  bool pending = my_leaf >= 0;
   __syncthreads();
   for (;;) {
-    if (tid < 32) {
-      long long first = -1;
+    if (warp == 0) {
+      int first = -1;
 #pragma unroll
-      for (int chunk = 0; chunk < kAdjDfThreads / 32; ++chunk) {
-        const long long v = sm.leaf[chunk * 32 + tid];
+      for (int chunk = 0; chunk < NW; ++chunk) {
+        const int v = sm.leaf[chunk * 32 + lane];
         const unsigned m = __ballot_sync(0xffffffffu, v >= 0);
         if (m) {
           first = __shfl_sync(0xffffffffu, v, __ffs(m) - 1);
           break;
         }
       }
-      if (tid == 0) sm.cur = first;
+      if (lane == 0) sm.cur = first;
     }
     __syncthreads();
-    const long long cur = sm.cur;
+    const int cur = sm.cur;
     if (cur < 0) break;
+    const bool mine = pending && my_leaf == cur;
+    const unsigned m = __ballot_sync(0xffffffffu, mine);
+    if (lane == 0) sm.wcount[warp] = __popc(m);
+    __syncthreads();
+    int base = 0, total = 0;
+#pragma unroll
+    for (int w2 = 0; w2 < NW; ++w2) {
+      const int c = sm.wcount[w2];
+      base += w2 < warp ? c : 0;
+      total += c;
+    }
+    if (mine) {
+      sm.list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned char)tid;
+      sm.leaf[tid] = -1;
+      pending = false;
+    }
+    __syncthreads();
     df acc[PER][DOF];
 #pragma unroll
     for (int c = 0; c < PER; ++c)
 #pragma unroll
       for (int l = 0; l < DOF; ++l) acc[c][l] = df{0.f, 0.f};
-    for (int p = 0; p < kAdjDfThreads; ++p) {
-      if (sm.leaf[p] != cur) continue;
+    for (int k = 0; k < total; ++k) {
+      const float2* const pc = sm.slots + sm.list[k];
       df wp[DOF];
 #pragma unroll
-      for (int l = 0; l < DOF; ++l) wp[l] = df{sm.w[p][l].x, sm.w[p][l].y};
+      for (int l = 0; l < DOF; ++l) {
+        const float2 v = pc[(3 * D + l) * BS];
+        wp[l] = df{v.x, v.y};
+      }
 #pragma unroll
       for (int c = 0; c < PER; ++c) {
-        if (mi[c] < 0) continue;
-        const float2 a = sm.tz[p][mi[c]], b = sm.ty[p][mj[c]], e = sm.tx[p][mk[c]];
+        if (oz[c] < 0) continue;
+        const float2 a = pc[oz[c]], b = pc[oy[c]], e = pc[ox[c]];
         const df t = df_mul(df_mul(df{a.x, a.y}, df{b.x, b.y}), df{e.x, e.y});
 #pragma unroll
         for (int l = 0; l < DOF; ++l) df_fma_acc(acc[c][l], wp[l], t);
@@ -245,80 +280,39 @@ __device__ __forceinline__ void cta_scatter_df(AdjStageDF<D>& sm, double* __rest
     }
 #pragma unroll
     for (int c = 0; c < PER; ++c) {
-      if (mi[c] < 0) continue;
+      if (oz[c] < 0) continue;
       const int n = tid + c * kAdjDfThreads;
 #pragma unroll
       for (int l = 0; l < DOF; ++l) {
         const double v = df_to_double(df_norm(acc[c][l]));
-        if (v != 0.0) atomicAdd(out + cur * stride + l * NC + n, v);
+        if (v != 0.0) atomicAdd(out + (int64_t)cur * stride + l * NC + n, v);
       }
     }
-    __syncthreads();
-    if (sm.leaf[tid] == cur) sm.leaf[tid] = -1;
-    __syncthreads();
   }
 }
 
-// Four (q <= 8) or three CTAs per SM: with the register cap the kernel
-// spills a little but keeps 24 or 18 warps resident.
+// One thread per target node, its X* and Xd from a.xmid / a.xdep (required:
+// the forward's checkpoints or the recompute's).  The tau^2/2 J_v(X*)^T g (x)
+// phi(X) term goes to a.wnode (required) for the node-grid scatter.  Four
+// (q <= 8) or three CTAs per SM.
 template <int D>
 __global__ void __launch_bounds__(kAdjDfThreads, (D <= 9 ? 4 : 3)) k_adjoint_df(const AdjArgs a,
                                                             const float2* __restrict__ con2) {
   constexpr int NP = D * D * D;
   constexpr int NC = D * (D + 1) * (D + 2) / 6;
+  constexpr int PER = (NC + kAdjDfThreads - 1) / kAdjDfThreads;
   extern __shared__ __align__(16) unsigned char adj_df_raw[];
-  AdjStageDF<D>& sm = *reinterpret_cast<AdjStageDF<D>*>(adj_df_raw);
-  const ThreadSlots slots{reinterpret_cast<float2*>(adj_df_raw) + threadIdx.x, kAdjDfThreads};
+  AdjDfShared<D>& sm = *reinterpret_cast<AdjDfShared<D>*>(adj_df_raw);
+  const ThreadSlots slots{sm.slots + threadIdx.x, AdjDfShared<D>::BS};
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool active = t < a.con.L * NP;
   const bool per = a.periodic != 0;
   const int64_t tt = active ? t : 0;
-  const int64_t leaf = tt / NP;
-  const int p = (int)(tt - leaf * NP);
-  const Geom gl = load_geom(a.con.geom + leaf);
-  const double h = 2.0 / gl.w;
-  double x = gl.x + h * a.nodes.x[p % D];
-  double y = gl.y + h * a.nodes.x[(p / D) % D];
-  double z = gl.z + h * a.nodes.x[p / (D * D)];
-  double xs, ys, zs, xd, yd, zd;
-  if (a.xmid) {
-    xs = a.xmid[3 * tt];
-    ys = a.xmid[3 * tt + 1];
-    zs = a.xmid[3 * tt + 2];
-    xd = a.xdep[3 * tt];
-    yd = a.xdep[3 * tt + 1];
-    zd = a.xdep[3 * tt + 2];
-  } else if (a.vn) {
-    // recompute from the node-grid velocity (bit-identical to eval_point at X)
-    double v[3];
-    double px = x, py = y, pz = z;
-    if (per) {
-      px = wrap1(px);
-      py = wrap1(py);
-      pz = wrap1(pz);
-    }
-    xs = fma(0.5 * a.tau, __ldg(a.vn + 3 * tt + 0), px);
-    ys = fma(0.5 * a.tau, __ldg(a.vn + 3 * tt + 1), py);
-    zs = fma(0.5 * a.tau, __ldg(a.vn + 3 * tt + 2), pz);
-    double qx = xs, qy = ys, qz = zs;
-    eval_point<D, 3>(a.vel, qx, qy, qz, per, v);
-    xd = fma(a.tau, v[0], px);
-    yd = fma(a.tau, v[1], py);
-    zd = fma(a.tau, v[2], pz);
-  } else {
-    double v[3];
-    double px = x, py = y, pz = z;
-    eval_point<D, 3>(a.vel, px, py, pz, per, v);
-    xs = fma(0.5 * a.tau, v[0], px);
-    ys = fma(0.5 * a.tau, v[1], py);
-    zs = fma(0.5 * a.tau, v[2], pz);
-    double qx = xs, qy = ys, qz = zs;
-    eval_point<D, 3>(a.vel, qx, qy, qz, per, v);
-    xd = fma(a.tau, v[0], px);
-    yd = fma(a.tau, v[1], py);
-    zd = fma(a.tau, v[2], pz);
-  }
+  double xs = a.xmid[3 * tt], ys = a.xmid[3 * tt + 1], zs = a.xmid[3 * tt + 2];
+  double xd = a.xdep[3 * tt], yd = a.xdep[3 * tt + 1], zd = a.xdep[3 * tt + 2];
   const double mu = active ? a.mu[tt] : 0.0;
+  int oz[PER], oy[PER], ox[PER];
+  scatter_offsets<D, PER>(oz, oy, ox);
 
   // g = mu grad c^k(Xd); lambda^k += mu phi(Xd)
   double gvec[3] = {0.0, 0.0, 0.0};
@@ -326,24 +320,18 @@ __global__ void __launch_bounds__(kAdjDfThreads, (D <= 9 ? 4 : 3)) k_adjoint_df(
     Geom g;
     int64_t lf = locate<D>(a.con, xd, yd, zd, per, g);
     if (!active) lf = -1;
-    double tx[D], ty[D], tz[D];
+    df tx[D];
     if (lf >= 0) {
-      df dtx[D], ddx[D];
-      grad_tables<D>(g, xd, yd, zd, dtx, ddx, slots);
+      df dx[D];
+      grad_tables<D>(g, xd, yd, zd, tx, dx, slots);
       double gr[3];
-      tri_grad_df<D>(GradOne{con2 + lf * NC}, dtx, ddx, slots, gr);
+      tri_grad_df<D>(GradOne{con2 + lf * NC}, tx, dx, slots, gr);
       gvec[0] = mu * gr[0] * g.w;
       gvec[1] = mu * gr[1] * g.w;
       gvec[2] = mu * gr[2] * g.w;
-      cheb_T<D>((xd - g.x) * g.w - 1.0, tx);
-      cheb_T<D>((yd - g.y) * g.w - 1.0, ty);
-      cheb_T<D>((zd - g.z) * g.w - 1.0, tz);
-    } else {
-#pragma unroll
-      for (int k = 0; k < D; ++k) tx[k] = ty[k] = tz[k] = 0.0;
     }
     const double w[1] = {mu};
-    cta_scatter_df<D, 1>(sm, a.lambda, NC, lf, w, tx, ty, tz);
+    scatter_df<D, 1, PER>(sm, a.lambda, NC, lf, tx, w, oz, oy, ox);
   }
   // tau g (x) phi(X*) and J_v(X*)^T g = grad(g . v)(X*)
   double jtg[3] = {0.0, 0.0, 0.0};
@@ -351,54 +339,27 @@ __global__ void __launch_bounds__(kAdjDfThreads, (D <= 9 ? 4 : 3)) k_adjoint_df(
     Geom g;
     int64_t lf = locate<D>(a.vel, xs, ys, zs, per, g);
     if (!active) lf = -1;
-    double tx[D], ty[D], tz[D];
+    df tx[D];
     if (lf >= 0) {
-      df dtx[D], ddx[D];
-      grad_tables<D>(g, xs, ys, zs, dtx, ddx, slots);
+      df dx[D];
+      grad_tables<D>(g, xs, ys, zs, tx, dx, slots);
       double gr[3];
       tri_grad_df<D>(GradW3{a.vel.coeff2 + lf * a.vel.stride, NC, df_from_double(gvec[0]),
                             df_from_double(gvec[1]), df_from_double(gvec[2])},
-                     dtx, ddx, slots, gr);
+                     tx, dx, slots, gr);
       jtg[0] = gr[0] * g.w;
       jtg[1] = gr[1] * g.w;
       jtg[2] = gr[2] * g.w;
-      cheb_T<D>((xs - g.x) * g.w - 1.0, tx);
-      cheb_T<D>((ys - g.y) * g.w - 1.0, ty);
-      cheb_T<D>((zs - g.z) * g.w - 1.0, tz);
-    } else {
-#pragma unroll
-      for (int k = 0; k < D; ++k) tx[k] = ty[k] = tz[k] = 0.0;
     }
     const double w[3] = {a.tau * gvec[0], a.tau * gvec[1], a.tau * gvec[2]};
-    cta_scatter_df<D, 3>(sm, a.grad_vel, 3 * NC, lf, w, tx, ty, tz);
+    scatter_df<D, 3, PER>(sm, a.grad_vel, 3 * NC, lf, tx, w, oz, oy, ox);
   }
-  // tau^2/2 J_v(X*)^T g (x) phi(X): X is a node, so the weights go to the
-  // node-grid scatter when a buffer is given
-  if (a.wnode) {
+  // tau^2/2 J_v(X*)^T g (x) phi(X): X is a node, the node-grid scatter adds it
+  if (active) {
     const double c2 = 0.5 * a.tau * a.tau;
-    if (active) {
-      a.wnode[3 * t + 0] = c2 * jtg[0];
-      a.wnode[3 * t + 1] = c2 * jtg[1];
-      a.wnode[3 * t + 2] = c2 * jtg[2];
-    }
-    return;
-  }
-  {
-    Geom g;
-    int64_t lf = locate<D>(a.vel, x, y, z, per, g);
-    if (!active) lf = -1;
-    double tx[D], ty[D], tz[D];
-    if (lf >= 0) {
-      cheb_T<D>((x - g.x) * g.w - 1.0, tx);
-      cheb_T<D>((y - g.y) * g.w - 1.0, ty);
-      cheb_T<D>((z - g.z) * g.w - 1.0, tz);
-    } else {
-#pragma unroll
-      for (int k = 0; k < D; ++k) tx[k] = ty[k] = tz[k] = 0.0;
-    }
-    const double c2 = 0.5 * a.tau * a.tau;
-    const double w[3] = {c2 * jtg[0], c2 * jtg[1], c2 * jtg[2]};
-    cta_scatter_df<D, 3>(sm, a.grad_vel, 3 * NC, lf, w, tx, ty, tz);
+    a.wnode[3 * t + 0] = c2 * jtg[0];
+    a.wnode[3 * t + 1] = c2 * jtg[1];
+    a.wnode[3 * t + 2] = c2 * jtg[2];
   }
 }
 
@@ -417,8 +378,7 @@ void launch_adjoint_df(const AdjArgs& a, const float2* con2, cudaStream_t s) {
 }
 
 template <int D>
-void register_adjoint_degree(CkptFn* c, AdjFn* a, AdjDfFn* d) {
-  c[D - 1] = &launch_ckpt<D>;
+void register_adjoint_degree(AdjFn* a, AdjDfFn* d) {
   a[D - 1] = &launch_adjoint<D>;
   d[D - 1] = &launch_adjoint_df<D>;
 }

@@ -1,5 +1,5 @@
-// Forward-with-checkpoint and adjoint kernels of the in-situ SL step
-// (nrk = 1), instantiated per Chebyshev degree by adjoint_*.cu.
+// Adjoint kernels of the in-situ SL step (nrk = 1), instantiated per
+// Chebyshev degree by adjoint_*.cu.
 //
 // Forward, per target node X of the concentration tree (c^k -> c^{k+1}):
 //   X* = X + tau/2 v(X),  Xd = X + tau v(X*),  u = c^k(Xd),  C^{k+1} = refit(u).
@@ -22,16 +22,6 @@
 
 namespace tbg {
 
-struct CkptArgs {
-  TreeView vel, con;
-  Nodes1D nodes;
-  double tau;
-  int periodic;
-  double* vals;  // [Lc * Np]
-  double* xmid;  // [Lc * Np * 3]
-  double* xdep;  // [Lc * Np * 3]
-};
-
 struct AdjArgs {
   TreeView vel;        // velocity coefficients (read)
   TreeView con;        // geometry of the concentration tree, coefficients = c^k
@@ -45,8 +35,6 @@ struct AdjArgs {
   double* grad_vel;    // [Lv][3][Nc] accumulated
   double* wnode;       // [Lc * Np][3]: weights of the tau^2/2 term at the nodes for
                        // the node-grid scatter (launch_scatter_on_nodes), or null
-  const double* vn;    // [Lc * Np][3]: v(X) from the node grid for the recompute
-                       // (bit-identical to eval_point at X), or null
 };
 
 // T_k and dT_k/dxi for k < D; zero outside [-1,1] like cheb_T.
@@ -228,40 +216,6 @@ __device__ __forceinline__ void cta_scatter(AdjSmem<D>& sm, double* __restrict__
   }
 }
 
-// Forward step storing X* and Xd (unwrapped, as computed) per target.
-template <int D>
-__global__ void __launch_bounds__(128) k_semilag_ckpt(const CkptArgs a) {
-  constexpr int NP = D * D * D;
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= a.con.L * NP) return;
-  const int64_t leaf = t / NP;
-  const int p = (int)(t - leaf * NP);
-  const Geom g = load_geom(a.con.geom + leaf);
-  const double h = 2.0 / g.w;
-  double x = g.x + h * a.nodes.x[p % D];
-  double y = g.y + h * a.nodes.x[(p / D) % D];
-  double z = g.z + h * a.nodes.x[p / (D * D)];
-  const bool per = a.periodic != 0;
-  double v[3];
-  eval_point<D, 3>(a.vel, x, y, z, per, v);
-  double xs = fma(0.5 * a.tau, v[0], x);
-  double ys = fma(0.5 * a.tau, v[1], y);
-  double zs = fma(0.5 * a.tau, v[2], z);
-  a.xmid[3 * t + 0] = xs;
-  a.xmid[3 * t + 1] = ys;
-  a.xmid[3 * t + 2] = zs;
-  eval_point<D, 3>(a.vel, xs, ys, zs, per, v);
-  x = fma(a.tau, v[0], x);
-  y = fma(a.tau, v[1], y);
-  z = fma(a.tau, v[2], z);
-  a.xdep[3 * t + 0] = x;
-  a.xdep[3 * t + 1] = y;
-  a.xdep[3 * t + 2] = z;
-  double c[1];
-  eval_point<D, 1>(a.con, x, y, z, per, c);
-  a.vals[t] = c[0];
-}
-
 template <int D>
 __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const AdjArgs a) {
   constexpr int NP = D * D * D;
@@ -370,18 +324,11 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const AdjArgs a) {
   }
 }
 
-typedef void (*CkptFn)(const CkptArgs&, cudaStream_t);
 typedef void (*AdjFn)(const AdjArgs&, cudaStream_t);
 typedef void (*AdjDfFn)(const AdjArgs&, const float2*, cudaStream_t);
-void register_adjoint_a(CkptFn* c, AdjFn* a, AdjDfFn* d);
-void register_adjoint_b(CkptFn* c, AdjFn* a, AdjDfFn* d);
-void register_adjoint_c(CkptFn* c, AdjFn* a, AdjDfFn* d);
-
-template <int D>
-void launch_ckpt(const CkptArgs& a, cudaStream_t s) {
-  const int64_t n = a.con.L * D * D * D;
-  if (n > 0) k_semilag_ckpt<D><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
-}
+void register_adjoint_a(AdjFn* a, AdjDfFn* d);
+void register_adjoint_b(AdjFn* a, AdjDfFn* d);
+void register_adjoint_c(AdjFn* a, AdjDfFn* d);
 
 template <int D>
 void launch_adjoint(const AdjArgs& a, cudaStream_t s) {
@@ -395,7 +342,5 @@ void launch_adjoint(const AdjArgs& a, cudaStream_t s) {
   if (n > 0)
     k_adjoint<D><<<(unsigned)((n + kAdjThreads - 1) / kAdjThreads), kAdjThreads, smem, s>>>(a);
 }
-
-
 
 }  // namespace tbg

@@ -569,7 +569,8 @@ double sl_tau(int timestep, double dt, int nrk) {
 }
 
 int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
-                        int nrk, int bc, cudaStream_t s) {
+                        int nrk, int bc, cudaStream_t s, double* xmid = nullptr,
+                        double* xdep = nullptr) {
   const double tau = sl_tau(timestep, dt, nrk);
   const int64_t np = n_points(con->q);
   const int64_t N = con->L * np;
@@ -584,6 +585,8 @@ int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int ti
     a.nrk = nrk;
     a.periodic = bc;
     a.vals = vals;
+    a.xmid = xmid;
+    a.xdep = xdep;
     {
       // first RK stage: the velocity at the targets by sum factorisation
       double* vn = nullptr;
@@ -1191,6 +1194,76 @@ int tbslas_semilag_in_situ(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int
   TRY(check_step_args(ctx, vel, con, dt, nrk, bc));
   return semilag_in_situ_dev(ctx, vel, con, timestep, dt, nrk, bc, (cudaStream_t)stream);
 }
+
+}  // extern "C"
+
+// For the adjoint's checkpointed forward (adjoint.cu).
+namespace tbg {
+int semilag_in_situ_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
+                           double dt, int bc, double* xmid, double* xdep, cudaStream_t s) {
+  TRY(check_step_args(ctx, vel, con, dt, 1, bc));
+  if (vel->q != con->q || vel->dof != 3 || con->dof != 1)
+    return fail(TBSLAS_ERR_UNSUPPORTED, "points of the step need a dof-3 velocity and a dof-1 "
+                                        "concentration tree of one degree");
+  if (!xmid || !xdep) return fail(TBSLAS_ERR_INVALID_ARG, "null point buffer");
+  return semilag_in_situ_dev(ctx, vel, con, timestep, dt, 1, bc, s, xmid, xdep);
+}
+
+ProfBracket::ProfBracket(tbslas_ctx ctx, const char* name, cudaStream_t s, int kernels)
+    : ctx_(ctx), name_(name), s_(s), kernels_(kernels) {
+  if (ctx_->profile) {
+    start_ = prof_event(ctx_);
+    cudaEventRecord(start_, s_);
+  }
+}
+ProfBracket::~ProfBracket() {
+  if (start_) {
+    cudaEvent_t stop = prof_event(ctx_);
+    cudaEventRecord(stop, s_);
+    ctx_->prof_pending.push_back(ProfRecord{name_, kernels_, start_, stop});
+  }
+}
+
+int step_points_df(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
+                   int bc, double** xmid, double** xdep, cudaStream_t s) {
+  TRY(check_step_args(ctx, vel, con, dt, 1, bc));
+  const int q = con->q;
+  if (vel->q != q || con->dof != 1 || !g_kernels[q].points_df)
+    return fail(TBSLAS_ERR_UNSUPPORTED, "step points: degree %d", q);
+  const int64_t N = con->L * n_points(q);
+  SemilagTreeArgs a;
+  a.vel = vel->view();
+  a.con = con->view();
+  a.nodes = nodes_1d(q);
+  a.tau = sl_tau(timestep, dt, 1);
+  a.nrk = 1;
+  a.periodic = bc;
+  a.vals = nullptr;
+  double* vn = nullptr;
+  TRY(scratch_t(ctx, kVN, N * 3, &vn));
+  {
+    ProfScope pv(ctx, "adjoint_vel_at_nodes", s, 2);
+    launch_eval_on_nodes(a.vel, a.con, bc, vn, s);
+  }
+  TRY(check_launch("velocity at nodes"));
+  a.vn = vn;
+  TRY(scratch_t(ctx, kXA, N * 3, &a.xmid));
+  TRY(scratch_t(ctx, kXB, N * 3, &a.xdep));
+  TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
+  TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
+  a.fix_grid = ctx->num_sms * 8;
+  {
+    ProfScope pp(ctx, "adjoint_points", s, 2);
+    g_kernels[q].points_df(a, s);
+  }
+  TRY(check_launch("step points"));
+  *xmid = a.xmid;
+  *xdep = a.xdep;
+  return TBSLAS_OK;
+}
+}  // namespace tbg
+
+extern "C" {
 
 int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
                                 double* con_coeff_host, int timestep, double dt, int nrk,

@@ -254,6 +254,30 @@ __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, doub
   return amb;
 }
 
+// The leaf lookup of eval_point_df without the sums: true when (x, y, z) --
+// wrapped under periodic boundaries -- lies within m[a] of a face of its leaf
+// on some axis, or just outside the domain, so that the FP64 path's lookup
+// could differ.
+__device__ __forceinline__ bool lookup_ambiguous(const TreeView& t, double x, double y, double z,
+                                                 bool periodic, const double (&m)[3]) {
+  if (periodic) {
+    x = wrap1(x);
+    y = wrap1(y);
+    z = wrap1(z);
+  }
+  if (!inside(x, y, z, periodic)) {
+    if (fmax(m[0], fmax(m[1], m[2])) == 0.0) return false;
+    return x >= -m[0] && x <= 1.0 + m[0] && y >= -m[1] && y <= 1.0 + m[1] && z >= -m[2] &&
+           z <= 1.0 + m[2];
+  }
+  const int64_t leaf = find_leaf(t, morton3(quantise(x), quantise(y), quantise(z)));
+  const Geom g = load_geom(t.geom + leaf);
+  const double xi = (x - g.x) * g.w - 1.0, yi = (y - g.y) * g.w - 1.0, zi = (z - g.z) * g.w - 1.0;
+  return (m[0] > 0.0 && fabs(xi) >= 1.0 - m[0] * g.w) ||
+         (m[1] > 0.0 && fabs(yi) >= 1.0 - m[1] * g.w) ||
+         (m[2] > 0.0 && fabs(zi) >= 1.0 - m[2] * g.w);
+}
+
 // Position update p = x + s*v of one axis in the double-float step, with its
 // uncertainty: mx bounds x's distance from the FP64 path, ev bounds v's.  When
 // x is exact and the whole step (plus its uncertainty) is below half an ulp

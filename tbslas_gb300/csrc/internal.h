@@ -29,6 +29,11 @@ struct SemilagTreeArgs {
   int64_t* fix_list;  // targets the double-float kernel hands to the FP64 pass
   unsigned long long* fix_count;
   int fix_grid;       // CTAs of the FP64 pass (persistent)
+  // nrk = 1 with vn given: every target's RK2 midpoint X* and departure point
+  // Xd ([Lc * Np][3], unwrapped, as computed -- the FP64 path's points for the
+  // targets the FP64 pass recomputes), or null
+  double* xmid = nullptr;
+  double* xdep = nullptr;
 };
 
 struct TrajArgs {
@@ -72,6 +77,7 @@ typedef void (*EvalTilesFn)(const EvalTilesArgs&, cudaStream_t);
 struct DegreeKernels {
   SemilagTreeFn semilag = nullptr;     // FP64 fused step
   SemilagTreeFn semilag_df = nullptr;  // double-float fused step + FP64 pass over near-face targets
+  SemilagTreeFn points_df = nullptr;   // its midpoints and departure points only (q <= 10)
   TrajFn traj = nullptr;
   EvalTilesFn eval_tiles = nullptr;
   int eval_tiles_max_threads_hint = 0;
@@ -100,6 +106,32 @@ int ctx_F(tbslas_ctx ctx, int q, const double** F);
 int ctx_mu_scratch(tbslas_ctx ctx, size_t n, double** out);
 int ctx_vals_scratch(tbslas_ctx ctx, size_t n, double** out);
 Nodes1D ctx_nodes(int q);
+// The in-situ step (nrk = 1, fused path: dof-3 velocity and dof-1
+// concentration of one degree) writing every target's RK2 midpoint and
+// departure point to xmid / xdep ([Lc * Np][3]).
+int semilag_in_situ_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
+                           double dt, int bc, double* xmid, double* xdep, cudaStream_t s);
+// Profiling bracket for launch groups of other translation units (the
+// context's per-name CUDA-event timing; nothing when profiling is off).
+class ProfBracket {
+ public:
+  ProfBracket(tbslas_ctx ctx, const char* name, cudaStream_t s, int kernels = 1);
+  ~ProfBracket();
+  ProfBracket(const ProfBracket&) = delete;
+  ProfBracket& operator=(const ProfBracket&) = delete;
+
+ private:
+  tbslas_ctx ctx_;
+  const char* name_;
+  cudaStream_t s_;
+  int kernels_;
+  cudaEvent_t start_ = nullptr;
+};
+// The midpoints and departure points of that step only, into scratch of the
+// context (*xmid, *xdep: [Lc * Np][3]), for the double-float adjoint's
+// recompute: the double-float step's kernels, FP64 for ambiguous targets.
+int step_points_df(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
+                   int bc, double** xmid, double** xdep, cudaStream_t s);
 
 // node_eval.cu: src evaluated at every node of dst's leaves, [dst.L * Np][src.dof]
 // (bit-identical to the pointwise FP64 evaluation)

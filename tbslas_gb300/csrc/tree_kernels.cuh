@@ -95,11 +95,12 @@ __device__ __forceinline__ void rk2_backtrace(const TreeView& vel, double& x, do
 // rk2_backtrace of a target node whose first-stage velocity vn (3 values) is
 // known -- the node-grid evaluation, bit-identical to eval_point at X: X is
 // wrapped in place as eval_point would, then the sub-steps continue as
-// rk2_backtrace.
+// rk2_backtrace.  mid (or null) receives the first sub-step's midpoint.
 template <int D>
 __device__ __forceinline__ void rk2_backtrace_from_node(const TreeView& vel, const double* vn,
                                                         double& x, double& y, double& z,
-                                                        double tau, int nrk, bool per) {
+                                                        double tau, int nrk, bool per,
+                                                        double* mid = nullptr) {
   if (per) {
     x = wrap1(x);
     y = wrap1(y);
@@ -109,12 +110,26 @@ __device__ __forceinline__ void rk2_backtrace_from_node(const TreeView& vel, con
   double px = fma(half_tau, __ldg(vn + 0), x);
   double py = fma(half_tau, __ldg(vn + 1), y);
   double pz = fma(half_tau, __ldg(vn + 2), z);
+  if (mid) {
+    mid[0] = px;
+    mid[1] = py;
+    mid[2] = pz;
+  }
   double v[3];
   eval_point<D, 3>(vel, px, py, pz, per, v);
   x = fma(tau, v[0], x);
   y = fma(tau, v[1], y);
   z = fma(tau, v[2], z);
   if (nrk > 1) rk2_backtrace<D>(vel, x, y, z, tau, nrk - 1, per);
+}
+
+// p[3t .. 3t+2] = (x, y, z) unless p is null.
+__device__ __forceinline__ void store_point(double* p, int64_t t, double x, double y, double z) {
+  if (p) {
+    p[3 * t + 0] = x;
+    p[3 * t + 1] = y;
+    p[3 * t + 2] = z;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -138,9 +153,11 @@ __global__ void __launch_bounds__(128) k_semilag_tree(const SemilagTreeArgs a) {
   double z = g.z + h * a.nodes.x[p / (D * D)];
   const bool per = a.periodic != 0;
   if (a.vn)
-    rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * t, x, y, z, a.tau, a.nrk, per);
+    rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * t, x, y, z, a.tau, a.nrk, per,
+                               a.xmid ? a.xmid + 3 * t : nullptr);
   else
     rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
+  store_point(a.xdep, t, x, y, z);
   double c[1];
   eval_point<D, 1>(a.con, x, y, z, per, c);
   a.vals[t] = c[0];
@@ -169,7 +186,10 @@ void launch_semilag_tree(const SemilagTreeArgs& a, cudaStream_t s) {
 // hide that better than 16 warps without spills (measured on GB300: q = 14
 // 309 -> 354 M points/s, q = 8 787 -> 879 M; five CTAs per SM was slower
 // than four).
-template <int D>
+// POINTS: only the midpoints and departure points (xmid, xdep required,
+// nrk = 1) -- the departure point's lookup in con is checked for ambiguity
+// but not summed, and no value is written.
+template <int D, bool POINTS = false>
 __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(const SemilagTreeArgs a) {
   constexpr int NP = D * D * D;
   extern __shared__ float2 s_slots[];
@@ -197,6 +217,7 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(cons
       px[k] = fma(half_tau, __ldg(a.vn + 3 * t + k), x[k]);
     }
     st0 = 1;
+    store_point(a.xmid, t, px[0], px[1], px[2]);
   }
 #pragma unroll 1
   for (int st = st0; st < 2 * a.nrk; ++st) {
@@ -208,6 +229,7 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(cons
         x[k] = px[k];
         df_update(half_tau, v[k], ev[k], x[k], m0[k], px[k], mp[k]);
       }
+      store_point(a.xmid, t, px[0], px[1], px[2]);
     } else {
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -217,16 +239,22 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(cons
       }
     }
   }
-  double c[1], ce[1];
-  amb |= eval_point_df<D, 1, false>(a.con, x[0], x[1], x[2], per, m0, c, ce, slots);
-  a.vals[t] = c[0];
+  store_point(a.xdep, t, x[0], x[1], x[2]);
+  if (POINTS) {
+    amb |= lookup_ambiguous(a.con, x[0], x[1], x[2], per, m0);
+  } else {
+    double c[1], ce[1];
+    amb |= eval_point_df<D, 1, false>(a.con, x[0], x[1], x[2], per, m0, c, ce, slots);
+    a.vals[t] = c[0];
+  }
   if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = t;
 }
 
 // FP64 recomputation of the listed targets (the arithmetic of
 // k_semilag_tree, with the first-stage velocity from the node grid when
-// given -- it is bit-identical to eval_point there).
-template <int D>
+// given -- it is bit-identical to eval_point there); stored midpoints and
+// departure points of those targets become the FP64 path's.
+template <int D, bool POINTS = false>
 __global__ void __launch_bounds__(128) k_semilag_fix(const SemilagTreeArgs a) {
   constexpr int NP = D * D * D;
   const int64_t n = (int64_t)*a.fix_count;
@@ -242,12 +270,16 @@ __global__ void __launch_bounds__(128) k_semilag_fix(const SemilagTreeArgs a) {
     double z = g.z + h * a.nodes.x[p / (D * D)];
     const bool per = a.periodic != 0;
     if (a.vn)
-      rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * t, x, y, z, a.tau, a.nrk, per);
+      rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * t, x, y, z, a.tau, a.nrk, per,
+                                 a.xmid ? a.xmid + 3 * t : nullptr);
     else
       rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
-    double c[1];
-    eval_point<D, 1>(a.con, x, y, z, per, c);
-    a.vals[t] = c[0];
+    store_point(a.xdep, t, x, y, z);
+    if (!POINTS) {
+      double c[1];
+      eval_point<D, 1>(a.con, x, y, z, per, c);
+      a.vals[t] = c[0];
+    }
   }
 }
 
@@ -262,6 +294,20 @@ void launch_semilag_tree_df(const SemilagTreeArgs& a, cudaStream_t s) {
   const size_t smem = 2 * D * threads * sizeof(float2);
   k_semilag_tree_df<D><<<(unsigned)blocks, threads, smem, s>>>(a);
   k_semilag_fix<D><<<a.fix_grid, threads, 0, s>>>(a);
+}
+
+// Midpoints and departure points only (the double-float adjoint's recompute).
+template <int D>
+void launch_points_df(const SemilagTreeArgs& a, cudaStream_t s) {
+  constexpr int NP = D * D * D;
+  const int64_t n = a.con.L * NP;
+  const int threads = 128;
+  const int64_t blocks = (n + threads - 1) / threads;
+  if (blocks == 0) return;
+  cudaMemsetAsync(a.fix_count, 0, sizeof(unsigned long long), s);
+  const size_t smem = 2 * D * threads * sizeof(float2);
+  k_semilag_tree_df<D, true><<<(unsigned)blocks, threads, smem, s>>>(a);
+  k_semilag_fix<D, true><<<a.fix_grid, threads, 0, s>>>(a);
 }
 
 // ---------------------------------------------------------------------------
@@ -361,6 +407,7 @@ void register_degree(DegreeKernels* table) {
   table[D - 1].semilag_df = &launch_semilag_tree_df<D>;
   table[D - 1].traj = &launch_traj<D>;
   table[D - 1].eval_tiles = &launch_eval_tiles<D>;
+  if constexpr (D <= 11) table[D - 1].points_df = &launch_points_df<D>;  // the adjoint's degrees
 }
 
 }  // namespace tbg

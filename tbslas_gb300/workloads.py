@@ -185,6 +185,7 @@ class AdjointWorkload:
     def __init__(self, depth=5, q=8, steps=20, dt=0.004, seed=SEED, name="adjoint_q8"):
         rng = np.random.default_rng(seed)
         self.name, self.q, self.steps, self.dt, self.bc = name, q, steps, dt, 0
+        self.depth = depth
         self.a, self.d = trees.uniform_tree(depth)
         self.vc = trees.fit(fields.taylor_green(), self.a, self.d, q, 3)
         self.c0 = trees.fit(fields.gaussian((0.45, 0.5, 0.5), 0.08), self.a, self.d, q, 1)
@@ -201,7 +202,8 @@ class AdjointWorkload:
         return {"workload": self.name, "q": self.q, "leaves": int(len(self.d)), "steps": self.steps,
                 "dt": self.dt, "bc": "freespace",
                 "departure_points_per_step": int(self.points_per_step),
-                "note": self.__doc__.split("\n")[0]}
+                "note": "uniform depth-%d octree, q = %d, stationary Taylor-Green velocity, "
+                        "%d SL steps of dt %g" % (self.depth, self.q, self.steps, self.dt)}
 
 
 def make(name):

@@ -1,9 +1,10 @@
-"""Adjoint of the in-situ SL step: the checkpointed (all-FP64) forward step
-reproduces the oracle's departure points bit for bit and the plain step to
-1e-12; dJ/dc0 and
-dJ/dV from the hand-written adjoint (behind torch.autograd) match central
-finite differences (eps = 1e-6) along seeded random directions to 1e-6
-relative; checkpointing and recomputation give the same gradients."""
+"""Adjoint of the in-situ SL step: the checkpointed forward is the in-situ
+step storing its points (the oracle's departure points bit for bit in the
+FP64 mode, the same leaves in the double-float mode); dJ/dc0 and dJ/dV from
+the hand-written adjoint (behind torch.autograd) match central finite
+differences (eps = 1e-6) along seeded random directions to 1e-6 relative and
+forward-mode dual numbers through the oracle to 1e-10; checkpointing and
+recomputation give the same gradients."""
 import numpy as np
 import pytest
 
@@ -26,21 +27,45 @@ def _problem(ctx, q=5, depth=2, seed=3):
 
 
 def test_ckpt_step_matches_plain_step_and_oracle(ctx, ora):
+    """The checkpointed step is the in-situ step of the context's sum mode
+    (same coefficients, bit for bit) storing its points.  FP64 mode: the
+    departure points are the oracle's bit for bit.  Double-float mode: they are
+    within 1e-13 of the oracle's (the velocity sums' rounding times tau) and in
+    the same leaves (targets near a face are recomputed in FP64)."""
     import torch
     a, d, q, vc, c0, _, tv, tc = _problem(ctx)
     vf = tb.NodeFieldFunctor(tv, tb.Periodic)
     n = len(d) * (q + 1) ** 3
-    xm = torch.empty((n, 3), dtype=torch.float64, device="cuda")
-    xd = torch.empty_like(xm)
-    adjoint.step_ckpt(vf, tc, 1, 0.03, xm, xd)
-    got = tc.get_coeffs()
-    tc.set_coeffs(c0)
-    tb.solve_semilag_in_situ(vf, tc, 1, 0.03)  # double-float sums: equal to ~1e-14
-    ref_c = tc.get_coeffs()
-    assert np.abs(got - ref_c).max() <= 1e-12 * np.abs(ref_c).max()
     pts = ora.collect_grid_points(a, d, q)
     ref = ora.traj_rk2(a, d, q, vc, pts, 0.03, 0.0, 1, periodic=True)
-    assert np.array_equal(xd.cpu().numpy(), ref)
+    xw = np.mod(pts, 1.0)
+    ref_mid = xw + (-0.015) * ora.eval_tree(a, d, q, 3, vc, xw, periodic=True)
+    cells = 2 ** int(d.max())
+
+    def leaf_of(x):
+        return np.floor(np.mod(x, 1.0) * cells)
+
+    try:
+        for mode in (tb.SUMS_FP64, tb.SUMS_DOUBLE_FLOAT):
+            ctx.sums = mode
+            xm = torch.full((n, 3), np.nan, dtype=torch.float64, device="cuda")
+            xd = torch.full_like(xm, np.nan)
+            tc.set_coeffs(c0)
+            adjoint.step_ckpt(vf, tc, 1, 0.03, xm, xd)
+            got = tc.get_coeffs()
+            tc.set_coeffs(c0)
+            tb.solve_semilag_in_situ(vf, tc, 1, 0.03)
+            assert np.array_equal(got, tc.get_coeffs())
+            xd, xm = xd.cpu().numpy(), xm.cpu().numpy()
+            assert np.abs(xm - ref_mid).max() <= 1e-15
+            assert np.array_equal(leaf_of(xm), leaf_of(ref_mid))
+            if mode == tb.SUMS_FP64:
+                assert np.array_equal(xd, ref)
+            else:
+                assert np.abs(xd - ref).max() <= 1e-13
+                assert np.array_equal(leaf_of(xd), leaf_of(ref))
+    finally:
+        ctx.sums = tb.SUMS_DOUBLE_FLOAT
 
 
 def _J(c, V, cobs):
