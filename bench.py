@@ -224,7 +224,37 @@ def run_reference(args, wl):
     threads) timed on bounded samples of the same workload, K steps."""
     total_budget = 150.0
     per_step = total_budget / max(1, args.steps + args.warmup)
-    if isinstance(wl, GridWorkloadType()):
+    timed_steps = args.steps
+    if hasattr(wl, "remesh"):
+        # the driver's loop on the CPU: oracle step + oracle re-mesh, advancing
+        # the state, as many of the K steps as fit the time budget
+        from oracle import oracle as ora
+        from oracle import remesh as rm
+        tol, lo, hi = wl.remesh
+        npl = (wl.q + 1) ** 3
+        vel = dict(anchor=wl.va, depth=wl.vd, q=wl.q, dof=3, coeff=wl.vc)
+        a, d, c = wl.ca, wl.cd, wl.cc
+        ora.pt2coeff(wl.q)
+        secs, pts, n = 0.0, 0, 0
+        t_start = time.perf_counter()
+        for i in range(args.warmup + args.steps):
+            if i > args.warmup and time.perf_counter() - t_start > total_budget:
+                break
+            t0 = time.perf_counter()
+            L = d.size
+            c1 = ora.semilag_in_situ(vel, dict(anchor=a, depth=d, q=wl.q, dof=1, coeff=c), i + 1,
+                                     wl.dt, 1, bool(wl.bc))
+            a, d, c = rm.remesh(a, d, wl.q, c1, tol, lo, hi, bool(wl.bc))
+            if i >= args.warmup:
+                secs += time.perf_counter() - t0
+                pts += L * npl
+                n += 1
+        cb = {"unit": UNIT, "cores": ora.num_threads(), "kind": "port",
+              "sample": "%d of the %d timed steps (step + re-mesh, whole tree, state advanced; "
+                        "the rest did not fit the %.0f s budget)" % (n, args.steps, total_budget)
+              if n < args.steps else "all %d timed steps (step + re-mesh, whole tree)" % n}
+        timed_steps = max(n, 1)
+    elif isinstance(wl, GridWorkloadType()):
         for _ in range(args.warmup):
             cpu_baseline_grid(wl, per_step)
         vals, secs, pts = [], 0.0, 0
@@ -258,7 +288,7 @@ def run_reference(args, wl):
     cb["value"] = value
     cb.pop("seconds", None)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / timed_steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded analytic fields)", "config": wl.describe(),
             "cpu_baseline": cb,
@@ -555,6 +585,164 @@ def run_gpu(args, wl, rank, world, local_rank):
             "fp64_sums": fp64, "clocks": clk.summary(), "gpu_launches": gpu_launches}
     if fp64_targets is not None:
         line["fp64_recomputed_targets_last_step"] = int(fp64_targets)
+    print(json.dumps(line))
+    assert ctx.check() == 0
+
+
+def run_remesh(args, wl, rank, world, local_rank):
+    """The adaptive advection loop of the reference's driver: an in-situ SL
+    step, then RefineTree and Balance21 (src/applications/src/advection.cpp:
+    296-311) -- here tbslas_semilag_in_situ + tbslas_tree_remesh -- every step.
+    value: departure points over the K timed steps / their time, re-meshing
+    included.  One step + re-mesh from the initial state is checked against
+    the oracle (same leaves, coefficients within 1e-12), which is also the
+    CPU baseline."""
+    import torch
+    import tbslas_gb300 as tb
+    from oracle import oracle as ora
+    from oracle import remesh as rm
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = tb.Context(local_rank)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    tol, lo, hi = wl.remesh
+    npl = (wl.q + 1) ** 3
+    tv = tb.Tree(ctx, wl.va, wl.vd, wl.q, 3, wl.vc)
+    vf = tb.NodeFieldFunctor(tv, wl.bc)
+
+    def advance(tc, ts):
+        tb.solve_semilag_in_situ(vf, tc, ts, wl.dt, 1)
+        return tc.remesh(tol, lo, hi, wl.bc)
+
+    # one step + re-mesh from the initial state, for the parity check
+    tc = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
+    advance(tc, 1)
+    ga, gd = tc.leaves()
+    gc = tc.get_coeffs()
+    tc.close()
+
+    tc = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
+    for i in range(args.warmup):
+        flush.fill_(float(i))
+        advance(tc, i + 1)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    points, rm_sec, stats, leaves = 0, 0.0, [], []
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            points += tc.n_leaves * npl
+            tb.solve_semilag_in_situ(vf, tc, args.warmup + 1 + i, wl.dt, 1)
+            torch.cuda.synchronize()  # the re-meshing waits for the step anyway
+            t0 = time.perf_counter()
+            stats.append(tc.remesh(tol, lo, hi, wl.bc))
+            rm_sec += time.perf_counter() - t0
+            leaves.append(tc.n_leaves)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    state_after = (tc.leaves(), tc.get_coeffs())
+
+    # the same K steps again from the same state with the library's event
+    # profiler on: the per-kernel split of the SL steps
+    tc2 = tb.Tree(ctx, state_after[0][0], state_after[0][1], wl.q, 1, state_after[1])
+    ctx.profile(True)
+    ctx.profile_reset()
+    pts2 = 0
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        pts2 += tc2.n_leaves * npl
+        advance(tc2, args.warmup + args.steps + 1 + i)
+    torch.cuda.synchronize()
+    prof = ctx.profile_totals()
+    ctx.profile(False)
+    tc2.close()
+
+    # end to end: the field comes from pinned host memory and goes back every
+    # step (host-buffer step entry point, re-mesh, coefficients read back)
+    tc3 = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
+    host = torch.from_numpy(np.ascontiguousarray(wl.cc)).pin_memory().numpy()
+    e_points, h2d, d2h = 0, 0, 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        e_points += tc3.n_leaves * npl
+        h2d += host.nbytes
+        tb.solve_semilag_in_situ(vf, tc3, i + 1, wl.dt, 1, coeff_host=host)
+        tc3.remesh(tol, lo, hi, wl.bc)
+        host = torch.empty(tc3.coeff_shape, dtype=torch.float64).pin_memory().numpy()
+        tc3.get_coeffs(host)
+        d2h += host.nbytes
+    torch.cuda.synchronize()
+    e2e_sec = time.perf_counter() - t0
+    tc3.close()
+    if rank != 0:
+        return
+
+    # the oracle: one step + re-mesh from the initial state (parity and the
+    # CPU baseline)
+    vel = dict(anchor=wl.va, depth=wl.vd, q=wl.q, dof=3, coeff=wl.vc)
+    con = dict(anchor=wl.ca, depth=wl.cd, q=wl.q, dof=1, coeff=wl.cc)
+    ora.pt2coeff(wl.q)
+    t0 = time.perf_counter()
+    c1 = ora.semilag_in_situ(vel, con, 1, wl.dt, 1, bool(wl.bc))
+    t_step = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ra, rd, rc = rm.remesh(wl.ca, wl.cd, wl.q, c1, tol, lo, hi, bool(wl.bc))
+    t_rm = time.perf_counter() - t0
+    same = bool(np.array_equal(ga, ra) and np.array_equal(gd, rd))
+    accuracy = {"same_leaves_as_oracle": same,
+                "rel_err_vs_oracle": (float(np.abs(gc - rc).max() / np.abs(rc).max())
+                                      if same else None),
+                "compared": "one SL step + re-mesh from the initial state"}
+    cpu = {"value": len(wl.cd) * npl / (t_step + t_rm), "unit": UNIT,
+           "cores": ora.num_threads(), "kind": "port",
+           "sample": "one step + re-mesh of the whole initial tree (%d leaves, %d departure "
+                     "points): oracle step %.2f s (OpenMP C++), re-mesh %.2f s (numpy)"
+                     % (len(wl.cd), len(wl.cd) * npl, t_step, t_rm)}
+
+    sl = prof.get("semilag_tree", (0, 0, 0.0))
+    launch_ms = sl[2] / max(sl[0], 1)
+    fp32_peak = ctx.fp32_fma_peak()
+    macs = df_macs_per_point_tree(wl.q)
+    achieved32 = 2 * DF_FP32_INSTR_PER_MAC * macs * (pts2 / args.steps) / (launch_ms * 1e-3) / 1e12
+    roofline = {
+        "kernel": "semilag_tree (double-float sums + FP64 near-face pass)", "bound": "fp32",
+        "achieved": achieved32, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+        "frac": achieved32 / (fp32_peak / 1e12),
+        "peak_source": "FP32 FMA throughput measured in this run (tbslas_fp32_fma_peak)",
+        "counting": "%d double-float multiply-adds per point x %d FP32 instructions, each "
+                    "counted as 2 FLOP; points per launch = the mean leaf count x (q+1)^3"
+                    % (macs, DF_FP32_INSTR_PER_MAC),
+        "launch_ms": launch_ms, "traffic": None,
+        "kernels_ms_per_step": {k: v[2] / args.steps for k, v in prof.items()}}
+    step_launches = int(sum(v[1] for v in prof.values()))
+    remesh_launches = int(sum(st["kernels"] for st in stats))
+    cfg = wl.describe()
+    cfg.update({"remesh": {"tol": tol, "min_depth": lo, "max_depth": hi},
+                "l2": "flushed between timed steps (256 MiB write inside the timed loop)",
+                "parallelism": "replicas x%d" % world, "nrk": 1,
+                "departure_points_per_step": "varies with the leaf count"})
+    line = {"metric": METRIC, "value": points / (ms * 1e-3), "unit": UNIT + " (step + re-mesh)",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded analytic fields)",
+            "config": cfg,
+            "e2e": {"value": e_points / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps},
+            "remesh": {"ms_per_step": rm_sec * 1e3 / args.steps,
+                       "share_of_step": rm_sec * 1e3 / ms,
+                       "leaves": {"initial": int(len(wl.cd)), "final": leaves[-1],
+                                  "min": min(leaves), "max": max(leaves)},
+                       "merged_groups": int(sum(st["merged"] for st in stats)),
+                       "split_by_refinement": int(sum(st["split"] for st in stats)),
+                       "split_by_balance": int(sum(st["balanced"] for st in stats))},
+            "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
+            "clocks": clk.summary(), "gpu_launches": step_launches + remesh_launches}
     print(json.dumps(line))
     assert ctx.check() == 0
 
@@ -917,6 +1105,8 @@ def main():
             run_batched(args, wl, rank, world, local_rank)
         elif args.workload.startswith("adjoint"):
             run_adjoint(args, wl, rank, world, local_rank)
+        elif hasattr(wl, "remesh"):
+            run_remesh(args, wl, rank, world, local_rank)
         else:
             run_gpu(args, wl, rank, world, local_rank)
     finally:

@@ -146,6 +146,28 @@ int tbslas_tree_set_coeffs_host(tbslas_tree tree, const double* coeff_host);
 int tbslas_tree_get_coeffs_host(tbslas_tree tree, double* coeff_host);
 int tbslas_tree_set_coeffs(tbslas_tree tree, const double* coeff_dev, void* stream);
 int tbslas_tree_get_coeffs(tbslas_tree tree, double* coeff_dev, void* stream);
+/* The current leaves: anchor_host[L*3], depth_host[L] (L from tbslas_tree_info). */
+int tbslas_tree_get_leaves(tbslas_tree tree, double* anchor_host, int32_t* depth_host);
+
+/* Adaptive re-meshing after a step, on the device: the reference's
+ * tcon.RefineTree(); tcon.Balance21(bc) (src/applications/src/advection.cpp:
+ * 305-311).  Both live in PVFMM (not vendored); this is the project's
+ * restatement of their rule, with tail(leaf) = sum over dofs of |c| over the
+ * coefficients of total degree q:
+ *  1. coarsen, one level: each complete group of 8 sibling leaves deeper than
+ *     min_depth becomes its parent when the parent's tail <= tol (the parent
+ *     fitted at its nodes from the sibling whose closed half holds each node);
+ *  2. refine: while a leaf has tail > tol and depth < max_depth, it is split
+ *     into its 8 children (the restriction of its expansion, fitted at the
+ *     children's nodes);
+ *  3. balance: while a leaf has a face, edge or corner neighbour more than one
+ *     level deeper (periodic images under TBSLAS_BC_PERIODIC), it is split.
+ * Leaves no rule touches keep their coefficients bit for bit.  The tree's
+ * leaf count changes (tbslas_tree_info, tbslas_tree_get_leaves).  stats
+ * (optional, 5 values): new leaf count, groups merged, leaves split by
+ * refinement, leaves split by balancing, kernels launched.  Synchronous. */
+int tbslas_tree_remesh(tbslas_ctx ctx, tbslas_tree tree, double tol, int min_depth,
+                       int max_depth, int bc, int64_t* stats);
 
 /* ---- the SL path --------------------------------------------------------------- */
 /* Chebyshev nodes of every leaf, leaves in order: out_dev[L*(q+1)^3*3].

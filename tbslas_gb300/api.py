@@ -200,6 +200,26 @@ class Tree:
             call("tbslas_tree_get_coeffs", self.handle, _ptr(out), _stream(stream))
         return out
 
+    def leaves(self):
+        """(anchor [L,3], depth [L]) of the current leaves."""
+        a = np.empty((self.n_leaves, 3))
+        d = np.empty(self.n_leaves, dtype=np.int32)
+        call("tbslas_tree_get_leaves", self.handle, a.ctypes.data, d.ctypes.data)
+        return a, d
+
+    def remesh(self, tol, min_depth, max_depth, bc=0):
+        """Adaptive re-meshing on the device (coarsen one level, refine,
+        2:1 balance; tbslas_tree_remesh).  Returns {"leaves", "merged",
+        "split", "balanced", "kernels"}; the tree's leaves and n_leaves
+        change."""
+        st = np.zeros(5, dtype=np.int64)
+        call("tbslas_tree_remesh", self.ctx.handle, self.handle, float(tol), int(min_depth),
+             int(max_depth), int(bc), st.ctypes.data)
+        self.n_leaves = int(st[0])
+        self.anchor, self.depth = self.leaves()
+        return {"leaves": int(st[0]), "merged": int(st[1]), "split": int(st[2]),
+                "balanced": int(st[3]), "kernels": int(st[4])}
+
 
 class NodeFieldFunctor:
     """Field functor of a tree: f(pos[n,3]) -> values[n,dof].

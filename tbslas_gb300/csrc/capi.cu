@@ -92,6 +92,28 @@ enum Slot {
   kGridC2,
   kAdjC2,
   kAdjW,
+  // re-meshing: two sets of leaf arrays (ping-pong) and the temporaries
+  kRmKeys0,
+  kRmGeom0,
+  kRmCoeff0,
+  kRmKeys1,
+  kRmGeom1,
+  kRmCoeff1,
+  kRmI64a,
+  kRmI64b,
+  kRmI64c,
+  kRmI64d,
+  kRmSrc,
+  kRmItems,
+  kRmVals,
+  kRmSplitC,
+  kRmMergeC,
+  kRmTail,
+  kRmAct,
+  kRmAux,
+  kRmGroup,
+  kRmTable,
+  kRmScalars,
   kNumSlots
 };
 
@@ -129,6 +151,7 @@ struct tbslas_ctx_s {
   double* d_F[TBSLAS_MAX_DEGREE + 1] = {};  // separable refit factors per degree
   int sums = TBSLAS_SUMS_DOUBLE_FLOAT;       // arithmetic of the in-situ step's sums
   bool profile = false;
+  int64_t* h_pinned = nullptr;  // small pinned host buffer for scalar read-backs
   std::vector<ProfRecord> prof_pending;
   std::vector<cudaEvent_t> prof_pool;
   std::vector<ProfTotal> prof_totals;
@@ -145,6 +168,8 @@ struct tbslas_tree_s {
   float2* d_coeff2 = nullptr;  // double-float split of d_coeff, kept in sync
   double* d_cnorm = nullptr;   // [L * dof] sum |c| per leaf and component, kept in sync
   int32_t* d_table = nullptr;
+  int64_t cap_L = 0;      // leaves the per-leaf arrays hold (>= L after a re-meshing)
+  int64_t cap_table = 0;  // entries d_table holds
 
   TreeView view() const {
     TreeView v;
@@ -686,6 +711,8 @@ int build_tree(tbslas_tree t, const double* anchor, const int32_t* depth) {
   CUDA_TRY(cudaMemcpy(t->d_table, table.data(), (ncell + 1) * sizeof(int32_t),
                       cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemset(t->d_coeff, 0, L * t->stride * sizeof(double)));
+  t->cap_L = L;
+  t->cap_table = ncell + 1;
   return TBSLAS_OK;
 }
 
@@ -708,6 +735,276 @@ int copy_coeffs(tbslas_tree t, double* dst, const double* src, bool to_tree, cud
     return derived_coeffs(t, s);
   }
   CUDA_TRY(cudaMemcpy2DAsync(dst, w, src, pitch, w, t->L, kind, s));
+  return TBSLAS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adaptive re-meshing (tbslas_tree_remesh): host sequence over the kernels of
+// remesh.cu.  Leaf arrays ping-pong between two sets of the context's
+// grow-only scratch; the host reads back one or two scalars per phase.
+constexpr Slot kMeshKeys[2] = {kRmKeys0, kRmKeys1};
+constexpr Slot kMeshGeom[2] = {kRmGeom0, kRmGeom1};
+constexpr Slot kMeshCoeff[2] = {kRmCoeff0, kRmCoeff1};
+
+struct MeshState {
+  int64_t L = 0;
+  int set = 0;  // scratch set holding the current leaves
+  uint64_t* keys = nullptr;
+  Geom* geom = nullptr;
+  double* coeff = nullptr;
+};
+
+// n (<= 2) int64 device scalars -> host, one synchronisation.
+int read_scalars(tbslas_ctx ctx, const int64_t* const* dev, int n, int64_t* host, cudaStream_t s) {
+  if (!ctx->h_pinned) CUDA_TRY(cudaMallocHost(&ctx->h_pinned, 4 * sizeof(int64_t)));
+  for (int i = 0; i < n; ++i)
+    CUDA_TRY(cudaMemcpyAsync(ctx->h_pinned + i, dev[i], sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  for (int i = 0; i < n; ++i) host[i] = ctx->h_pinned[i];
+  return TBSLAS_OK;
+}
+
+TreeView mesh_view(const tbslas_tree t, const MeshState& m, const int32_t* table, int T) {
+  TreeView v;
+  v.keys = m.keys;
+  v.geom = m.geom;
+  v.coeff = m.coeff;
+  v.coeff2 = nullptr;
+  v.cnorm = nullptr;
+  v.table = table;
+  v.L = m.L;
+  v.stride = t->stride;
+  v.T = T;
+  v.q = t->q;
+  v.dof = t->dof;
+  return v;
+}
+
+// New leaves from per-leaf actions (keep, split into 8, merge 8 siblings
+// into their parent, drop), into the other scratch set: split children get
+// the restriction of their parent (transfer + FP64 refit), merged parents the
+// rows of merge_c.
+int apply_actions(tbslas_ctx ctx, tbslas_tree t, MeshState& m, const int8_t* act,
+                  const int64_t* aux, const double* merge_c, cudaStream_t s, int64_t* launches) {
+  const int q = t->q, dof = t->dof;
+  const int64_t L = m.L, np = n_points(q), stride = t->stride;
+  int64_t *nleaf, *nxfer, *pos, *xpos;
+  TRY(scratch_t(ctx, kRmI64a, L, &nleaf));
+  TRY(scratch_t(ctx, kRmI64b, L, &nxfer));
+  TRY(scratch_t(ctx, kRmI64c, L + 1, &pos));
+  TRY(scratch_t(ctx, kRmI64d, L + 1, &xpos));
+  launch_action_counts(act, L, nleaf, nxfer, s);
+  k_scan_excl<<<1, 1024, 0, s>>>(nleaf, pos, L);
+  k_scan_excl<<<1, 1024, 0, s>>>(nxfer, xpos, L);
+  *launches += 3;
+  TRY(check_launch("re-meshing counts"));
+  const int64_t* ends[2] = {pos + L, xpos + L};
+  int64_t sz[2];
+  TRY(read_scalars(ctx, ends, 2, sz, s));
+  const int64_t Lnew = sz[0], nx = sz[1];
+  const int o = 1 - m.set;
+  MeshState n;
+  n.L = Lnew;
+  n.set = o;
+  int64_t* src_of;
+  XferItem* items;
+  TRY(scratch_t(ctx, kMeshKeys[o], Lnew, &n.keys));
+  TRY(scratch_t(ctx, kMeshGeom[o], Lnew, &n.geom));
+  TRY(scratch_t(ctx, kMeshCoeff[o], Lnew * stride, &n.coeff));
+  TRY(scratch_t(ctx, kRmSrc, Lnew, &src_of));
+  TRY(scratch_t(ctx, kRmItems, nx > 0 ? nx : 1, &items));
+  launch_rebuild(m.keys, m.geom, act, aux, pos, xpos, L, n.keys, n.geom, src_of, items, s);
+  *launches += 1;
+  TRY(check_launch("re-meshing leaves"));
+  double* split_c = nullptr;
+  if (nx > 0) {
+    const double* F = nullptr;
+    double* vals;
+    TRY(device_F(ctx, q, &F));
+    TRY(scratch_t(ctx, kRmVals, nx * dof * np, &vals));
+    TRY(scratch_t(ctx, kRmSplitC, nx * stride, &split_c));
+    CUDA_TRY(cudaMemsetAsync(split_c, 0, nx * stride * sizeof(double), s));  // row padding
+    launch_transfer(mesh_view(t, m, nullptr, 0), items, nx, nodes_1d(q), vals, s);
+    launch_refit(vals, F, q, nx * dof, dof, stride, split_c, nullptr, ctx->d_err, false, s);
+    *launches += 2;
+    TRY(check_launch("re-meshing transfer"));
+  }
+  launch_place_coeffs(src_of, Lnew, stride, m.coeff, merge_c, split_c, n.coeff, s);
+  *launches += 1;
+  TRY(check_launch("re-meshing coefficients"));
+  m = n;
+  return TBSLAS_OK;
+}
+
+int tree_remesh(tbslas_ctx ctx, tbslas_tree t, double tol, int min_depth, int max_depth, int bc,
+                int64_t* stats) {
+  cudaStream_t s = ctx->stream;
+  const int q = t->q, dof = t->dof;
+  const int64_t stride = t->stride;
+  CUDA_TRY(cudaDeviceSynchronize());  // queued work on any stream may still use the tree
+  MeshState m;
+  m.L = t->L;
+  TRY(scratch_t(ctx, kMeshKeys[0], m.L, &m.keys));
+  TRY(scratch_t(ctx, kMeshGeom[0], m.L, &m.geom));
+  TRY(scratch_t(ctx, kMeshCoeff[0], m.L * stride, &m.coeff));
+  CUDA_TRY(cudaMemcpyAsync(m.keys, t->d_keys, m.L * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(m.geom, t->d_geom, m.L * sizeof(Geom), cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(m.coeff, t->d_coeff, m.L * stride * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s));
+  int64_t merged = 0, split = 0, balanced = 0, launches = 0;
+  int64_t* sc;  // device scalars: [0] a count, [1] a maximum depth
+  TRY(scratch_t(ctx, kRmScalars, 2, &sc));
+  // 1. coarsen one level
+  {
+    const int64_t L = m.L;
+    int64_t *first, *gpos;
+    TRY(scratch_t(ctx, kRmI64a, L, &first));
+    TRY(scratch_t(ctx, kRmI64c, L + 1, &gpos));
+    launch_sibling_groups(m.keys, m.geom, L, min_depth, first, s);
+    k_scan_excl<<<1, 1024, 0, s>>>(first, gpos, L);
+    launches += 2;
+    TRY(check_launch("sibling groups"));
+    int64_t G = 0;
+    const int64_t* gend = gpos + L;
+    TRY(read_scalars(ctx, &gend, 1, &G, s));
+    if (G > 0) {
+      const double* F = nullptr;
+      TRY(device_F(ctx, q, &F));
+      XferItem* items;
+      int64_t *group_leaf, *aux;
+      double *vals, *merge_c, *tail;
+      int8_t* act;
+      TRY(scratch_t(ctx, kRmItems, G, &items));
+      TRY(scratch_t(ctx, kRmGroup, G, &group_leaf));
+      TRY(scratch_t(ctx, kRmVals, G * dof * n_points(q), &vals));
+      TRY(scratch_t(ctx, kRmMergeC, G * stride, &merge_c));
+      TRY(scratch_t(ctx, kRmTail, G, &tail));
+      TRY(scratch_t(ctx, kRmAct, L, &act));
+      TRY(scratch_t(ctx, kRmAux, L, &aux));
+      CUDA_TRY(cudaMemsetAsync(merge_c, 0, G * stride * sizeof(double), s));  // row padding
+      launch_group_items(first, gpos, m.geom, L, items, group_leaf, s);
+      launch_transfer(mesh_view(t, m, nullptr, 0), items, G, nodes_1d(q), vals, s);
+      launch_refit(vals, F, q, G * dof, dof, stride, merge_c, nullptr, ctx->d_err, false, s);
+      launch_leaf_tails(merge_c, G, dof, q, stride, tail, s);
+      CUDA_TRY(cudaMemsetAsync(act, kActKeep, L, s));
+      launch_merge_actions(group_leaf, G, tail, tol, act, aux, s);
+      launches += 5;
+      TRY(check_launch("coarsening"));
+      TRY(apply_actions(ctx, t, m, act, aux, merge_c, s, &launches));
+      merged = (L - m.L) / 7;
+    }
+  }
+  // 2. refine
+  for (int it = 0; it <= TBSLAS_MAX_DEPTH; ++it) {
+    double* tail;
+    int8_t* act;
+    TRY(scratch_t(ctx, kRmTail, m.L, &tail));
+    TRY(scratch_t(ctx, kRmAct, m.L, &act));
+    CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(int64_t), s));
+    launch_leaf_tails(m.coeff, m.L, dof, q, stride, tail, s);
+    launch_split_actions(tail, m.geom, m.L, tol, max_depth, act,
+                         reinterpret_cast<unsigned long long*>(sc), s);
+    launches += 2;
+    TRY(check_launch("refinement flags"));
+    int64_t n = 0;
+    TRY(read_scalars(ctx, &sc, 1, &n, s));
+    if (n == 0) break;
+    split += n;
+    TRY(apply_actions(ctx, t, m, act, nullptr, nullptr, s, &launches));
+  }
+  // 3. balance 2:1 (the lookup table at level 7, which find_leaf accepts at
+  // any maximum depth)
+  for (int it = 0; it <= TBSLAS_MAX_DEPTH; ++it) {
+    int32_t* table;
+    int8_t* act;
+    TRY(scratch_t(ctx, kRmTable, (1ll << 21) + 1, &table));
+    TRY(scratch_t(ctx, kRmAct, m.L, &act));
+    launch_build_table(m.keys, m.L, 7, table, s);
+    CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(int64_t), s));
+    launch_balance_flags(mesh_view(t, m, table, 7), bc, act,
+                         reinterpret_cast<unsigned long long*>(sc), s);
+    launches += 2;
+    TRY(check_launch("balance flags"));
+    int64_t n = 0;
+    TRY(read_scalars(ctx, &sc, 1, &n, s));
+    if (n == 0) break;
+    balanced += n;
+    TRY(apply_actions(ctx, t, m, act, nullptr, nullptr, s, &launches));
+  }
+  // install into the tree's arrays (grown when the leaf count outgrows them)
+  CUDA_TRY(cudaMemsetAsync(sc + 1, 0, sizeof(int64_t), s));
+  launch_max_depth(m.geom, m.L, reinterpret_cast<int*>(sc + 1), s);
+  launches += 1;
+  int64_t md = 0;
+  const int64_t* mdp = sc + 1;
+  TRY(read_scalars(ctx, &mdp, 1, &md, s));
+  const int maxd = (int)(md & 0xffffffff);
+  const int T = std::min(maxd, 7);
+  const int64_t ntab = (1ll << (3 * T)) + 1;
+  if (m.L > t->cap_L) {
+    const int64_t cap = m.L + m.L / 4;
+    uint64_t* k = nullptr;
+    Geom* g = nullptr;
+    double *c = nullptr, *cn = nullptr;
+    float2* c2 = nullptr;
+    if (cudaMalloc(&k, cap * sizeof(uint64_t)) != cudaSuccess ||
+        cudaMalloc(&g, cap * sizeof(Geom)) != cudaSuccess ||
+        cudaMalloc(&c, cap * stride * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c2, cap * stride * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&cn, cap * dof * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(k);
+      cudaFree(g);
+      cudaFree(c);
+      cudaFree(c2);
+      cudaFree(cn);
+      return fail(TBSLAS_ERR_ALLOC, "re-meshing: growing the tree to %lld leaves failed",
+                  (long long)cap);
+    }
+    CUDA_TRY(cudaMemsetAsync(c2, 0, cap * stride * sizeof(float2), s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    cudaFree(t->d_keys);
+    cudaFree(t->d_geom);
+    cudaFree(t->d_coeff);
+    cudaFree(t->d_coeff2);
+    cudaFree(t->d_cnorm);
+    t->d_keys = k;
+    t->d_geom = g;
+    t->d_coeff = c;
+    t->d_coeff2 = c2;
+    t->d_cnorm = cn;
+    t->cap_L = cap;
+  }
+  if (ntab > t->cap_table) {
+    int32_t* tab = nullptr;
+    if (cudaMalloc(&tab, ntab * sizeof(int32_t)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(TBSLAS_ERR_ALLOC, "re-meshing: lookup table allocation failed");
+    }
+    CUDA_TRY(cudaStreamSynchronize(s));
+    cudaFree(t->d_table);
+    t->d_table = tab;
+    t->cap_table = ntab;
+  }
+  CUDA_TRY(cudaMemcpyAsync(t->d_keys, m.keys, m.L * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(t->d_geom, m.geom, m.L * sizeof(Geom), cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(t->d_coeff, m.coeff, m.L * stride * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s));
+  t->L = m.L;
+  t->max_depth = maxd;
+  t->T = T;
+  launch_build_table(t->d_keys, t->L, T, t->d_table, s);
+  launches += 3;  // the table, then the split and norms of derived_coeffs
+  TRY(check_launch("lookup table"));
+  TRY(derived_coeffs(t, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (stats) {
+    stats[0] = t->L;
+    stats[1] = merged;
+    stats[2] = split;
+    stats[3] = balanced;
+    stats[4] = launches;
+  }
   return TBSLAS_OK;
 }
 
@@ -887,6 +1184,7 @@ int tbslas_ctx_destroy(tbslas_ctx ctx) {
     if (b.p) cudaFree(b.p);
   for (auto p : ctx->d_F)
     if (p) cudaFree(p);
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   prof_collect(ctx);
   for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
   if (ctx->d_err) cudaFree(ctx->d_err);
@@ -1031,6 +1329,36 @@ int tbslas_tree_destroy(tbslas_tree t) {
   if (t->d_cnorm) cudaFree(t->d_cnorm);
   if (t->d_table) cudaFree(t->d_table);
   delete t;
+  return TBSLAS_OK;
+}
+
+int tbslas_tree_remesh(tbslas_ctx ctx, tbslas_tree tree, double tol, int min_depth,
+                       int max_depth, int bc, int64_t* stats) {
+  TRY(check_tree(tree));
+  TRY(bind(ctx));
+  if (tree->ctx != ctx) return fail(TBSLAS_ERR_INVALID_ARG, "tree belongs to another context");
+  if (!(tol >= 0.0))  // +inf: refine nothing
+    return fail(TBSLAS_ERR_INVALID_ARG, "tolerance %g is negative or NaN", tol);
+  if (min_depth < 0 || max_depth < min_depth || max_depth > TBSLAS_MAX_DEPTH)
+    return fail(TBSLAS_ERR_INVALID_ARG, "depth range [%d, %d] outside [0, %d]", min_depth,
+                max_depth, TBSLAS_MAX_DEPTH);
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  return tree_remesh(ctx, tree, tol, min_depth, max_depth, bc, stats);
+}
+
+int tbslas_tree_get_leaves(tbslas_tree t, double* anchor_host, int32_t* depth_host) {
+  TRY(check_tree(t));
+  TRY(bind(t->ctx));
+  if (!anchor_host || !depth_host) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
+  CUDA_TRY(cudaDeviceSynchronize());  // queued work may still change the leaves
+  std::vector<Geom> g(t->L);
+  CUDA_TRY(cudaMemcpy(g.data(), t->d_geom, t->L * sizeof(Geom), cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < t->L; ++i) {
+    anchor_host[3 * i + 0] = g[i].x;
+    anchor_host[3 * i + 1] = g[i].y;
+    anchor_host[3 * i + 2] = g[i].z;
+    depth_host[i] = std::ilogb(g[i].w) - 1;
+  }
   return TBSLAS_OK;
 }
 

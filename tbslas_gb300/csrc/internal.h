@@ -192,6 +192,44 @@ int ctx_c2_scratch(tbslas_ctx ctx, size_t n, float2** out);
 int ctx_wnode_scratch(tbslas_ctx ctx, size_t n, double** out);
 int ctx_vn_scratch(tbslas_ctx ctx, size_t n, double** out);
 
+// Re-meshing (remesh.cu; the host sequence is tree_remesh in capi.cu).
+// Transfer item: node values of a new leaf with geometry g, from the old
+// tree's leaf src (kXferChild: its parent) or leaves src..src+7 (kXferParent:
+// its 8 children, child index x + 2y + 4z).
+enum : int32_t { kXferChild = 0, kXferParent = 1 };
+struct XferItem {
+  Geom g;
+  int64_t src;
+  int32_t mode, pad;
+};
+// Per-leaf re-meshing actions.
+enum : int8_t { kActKeep = 0, kActSplit = 1, kActMerge = 2, kActDrop = 3 };
+// out: [n][S.dof][(q+1)^3] node values (the refit's row layout)
+void launch_transfer(const TreeView& S, const XferItem* items, int64_t n, const Nodes1D& nodes,
+                     double* out, cudaStream_t s);
+void launch_leaf_tails(const double* coeff, int64_t L, int dof, int q, int64_t stride,
+                       double* tail, cudaStream_t s);
+void launch_sibling_groups(const uint64_t* keys, const Geom* geom, int64_t L, int min_depth,
+                           int64_t* first, cudaStream_t s);
+void launch_group_items(const int64_t* first, const int64_t* pos, const Geom* geom, int64_t L,
+                        XferItem* items, int64_t* group_leaf, cudaStream_t s);
+void launch_merge_actions(const int64_t* group_leaf, int64_t G, const double* tail, double tol,
+                          int8_t* act, int64_t* aux, cudaStream_t s);
+void launch_split_actions(const double* tail, const Geom* geom, int64_t L, double tol,
+                          int max_depth, int8_t* act, unsigned long long* count, cudaStream_t s);
+void launch_action_counts(const int8_t* act, int64_t L, int64_t* nleaf, int64_t* nxfer,
+                          cudaStream_t s);
+void launch_rebuild(const uint64_t* keys, const Geom* geom, const int8_t* act, const int64_t* aux,
+                    const int64_t* pos, const int64_t* xpos, int64_t L, uint64_t* nkeys,
+                    Geom* ngeom, int64_t* src_of, XferItem* items, cudaStream_t s);
+void launch_place_coeffs(const int64_t* src_of, int64_t Lnew, int64_t stride, const double* old_c,
+                         const double* merge_c, const double* split_c, double* out,
+                         cudaStream_t s);
+void launch_balance_flags(const TreeView& t, int periodic, int8_t* act, unsigned long long* count,
+                          cudaStream_t s);
+void launch_build_table(const uint64_t* keys, int64_t L, int T, int32_t* table, cudaStream_t s);
+void launch_max_depth(const Geom* geom, int64_t L, int* out, cudaStream_t s);
+
 // misc kernels (capi.cu)
 void launch_collect(const TreeView& t, const Nodes1D& nodes, double* out, cudaStream_t s);
 

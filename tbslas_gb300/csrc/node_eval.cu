@@ -34,31 +34,13 @@
 
 #include "host_cheb.h"
 #include "internal.h"
+#include "node_passes.cuh"
 
 namespace tbg {
 
 namespace {
 
 constexpr int kNodeEvalThreads = 256;
-
-template <int Ds>
-__device__ __forceinline__ void cheb_T_col(double xi, double* T, int stride) {
-  // the operations of cheb_T<Ds>, written to a strided column
-  const bool ok = fabs(xi) <= 1.0;
-  const double x = ok ? xi : 0.0;
-  const double t0 = ok ? 1.0 : 0.0;
-  T[0] = t0;
-  if (Ds > 1) T[stride] = x;
-  const double x2 = 2.0 * x;
-  double a = t0, b = x;
-#pragma unroll
-  for (int k = 2; k < Ds; ++k) {
-    const double t = fma(x2, b, -a);
-    T[k * stride] = t;
-    a = b;
-    b = t;
-  }
-}
 
 // Arithmetic of the transposed passes: FP64, or double-float pairs
 // accumulated with df_fma_acc (df64.cuh).
@@ -105,16 +87,6 @@ __host__ __device__ constexpr size_t node_scatter_smem(int Ds, int Dd, int dof) 
          (size_t)(3 * Ds * Dd + Dd * Dd * Dd + Ds * Dd * Dd + Ds * (Ds + 1) / 2 * Dd) *
              8;  // T (pass arithmetic), W, H, G
 }
-
-// The part of a destination leaf's node grid inside one source leaf: leaf
-// V, the listed node indices per axis (sidx[ax*Dd + i'], i' < n[ax]) and
-// T_k of their local coordinates in V (T[ax][k][i'], stride Dd).
-struct SubGrid {
-  int64_t V;
-  int na, nb, nz;
-  const int* sidx;
-  const double *Tx, *Ty, *Tz;
-};
 
 // Node (a, b, c) of destination leaf `leaf` on an upper face, where its
 // point is also a node of the neighbouring destination leaf of the same
@@ -266,10 +238,8 @@ template <int Ds>
 __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const TreeView& dst,
                                                    const Nodes1D& nodes, bool per, int64_t leaf,
                                                    double* __restrict__ out_all, double* sm) {
-  constexpr int NCs = Ds * (Ds + 1) * (Ds + 2) / 6, npair = Ds * (Ds + 1) / 2;
-  const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
+  const int Dd = dst.q + 1, Dd3 = Dd * Dd * Dd;
   const int dof = S.dof;
-  const int tid = threadIdx.x, bs = blockDim.x;
   double* sw = sm + walk_smem(Ds, Dd) / 8;  // [dof][pair(i,j)][Dd]
   double* out = out_all + leaf * (int64_t)Dd3 * dof;
   for_each_subgrid<Ds>(
@@ -277,50 +247,7 @@ __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const Tree
       [&](int p) {
         for (int l = 0; l < dof; ++l) out[(int64_t)p * dof + l] = 0.0;
       },
-      [&](const SubGrid& sg) {
-        const int na = sg.na, nb = sg.nb, nz = sg.nz;
-        const int* sidx = sg.sidx;
-        const double* cV = S.coeff + sg.V * S.stride;
-        // w(l; i,j,a') = sum_k c[l][i][j][k] T_k(x_a')
-        for (int o = tid; o < dof * npair * na; o += bs) {
-          const int ai = o % na, r = o / na, pr = r % npair, l = r / npair;
-          int i = 0, rem = pr;  // pair index -> (i, j): rows of length Ds - i
-          while (rem >= Ds - i) {
-            rem -= Ds - i;
-            ++i;
-          }
-          const int j = rem, m = Ds - i;
-          const double* c =
-              cV + l * NCs + (NCs - m * (m + 1) * (m + 2) / 6 + j * m - (j * (j - 1)) / 2);
-          double w = 0.0;
-          for (int k = 0; k < m - j; ++k) w = fma(__ldg(c + k), sg.Tx[k * Dd + ai], w);
-          sw[(l * npair + pr) * Dd + ai] = w;
-        }
-        __syncthreads();
-        // per column (l, b', a'): v(i) = sum_j T_j(y_b') w(l; i,j,a'), then
-        // u(c') = sum_i T_i(z_c') v(i) for every listed c'
-        for (int o = tid; o < dof * nb * na; o += bs) {
-          const int ai = o % na, r = o / na, bi = r % nb, l = r / nb;
-          const double* wl = sw + l * npair * Dd + ai;
-          double v[Ds];
-          int prow = 0;
-#pragma unroll
-          for (int i = 0; i < Ds; ++i) {
-            double s = 0.0;
-#pragma unroll
-            for (int j = 0; j < Ds - i; ++j) s = fma(sg.Ty[j * Dd + bi], wl[(prow + j) * Dd], s);
-            v[i] = s;
-            prow += Ds - i;
-          }
-          const int pab = sidx[ai] + Dd * sidx[Dd + bi];
-          for (int ci = 0; ci < nz; ++ci) {
-            double u = 0.0;
-#pragma unroll
-            for (int i = 0; i < Ds; ++i) u = fma(sg.Tz[i * Dd + ci], v[i], u);
-            out[(int64_t)(pab + Dd2 * sidx[2 * Dd + ci]) * dof + l] = u;
-          }
-        }
-      });
+      [&](const SubGrid& sg) { eval_subgrid<Ds>(S, sg, Dd, out, dof, 1, sw); });
 }
 
 // The transposed map (adjoint of the evaluation): for one destination leaf,

@@ -64,6 +64,27 @@ def tree_adaptive_q14(seed=SEED):
                         "Gaussians, CFL=1 on the finest leaf")
 
 
+def tree_adaptive_q8_remesh():
+    """The adaptive advection loop of the reference's driver
+    (SolveSemilagInSitu, then RefineTree and Balance21 after every step,
+    src/applications/src/advection.cpp:296-311) on the rotating Gaussian of
+    the uniform q = 8 configuration: the concentration tree starts refined for
+    the blob (tol 1e-5, depths 3..6) and is re-meshed with the same rule after
+    every step while the blob moves through it."""
+    q, tol = 8, 1e-5
+    va, vd = trees.uniform_tree(4)
+    vc = trees.fit(fields.rotation(2 * math.pi), va, vd, q, 3)
+    blob = fields.gaussian((0.7, 0.5, 0.5), 0.05)
+    ca, cd = trees.adaptive_tree(blob, q, 1, tol, 3, 6)
+    cc = trees.fit(blob, ca, cd, q, 1)
+    wl = TreeWorkload("tree_adaptive_q8_remesh", (va, vd, vc), (ca, cd, cc), q, 0.01, 0,
+                      "rotating Gaussian (sigma 0.05) on an adaptive q=8 concentration tree "
+                      "(tol 1e-5, depths 3..6) re-meshed after every step (coarsen, refine, "
+                      "2:1 balance); velocity: rotation on the uniform depth-4 tree")
+    wl.remesh = (tol, 3, 6)
+    return wl
+
+
 class GridWorkload:
     def __init__(self, n, seed=SEED):
         rng = np.random.default_rng(seed)
@@ -211,6 +232,8 @@ def make(name):
         return tree_uniform_q8()
     if name == "tree_adaptive_q14":
         return tree_adaptive_q14()
+    if name == "tree_adaptive_q8_remesh":
+        return tree_adaptive_q8_remesh()
     if name == "adjoint_q8":
         return AdjointWorkload()
     if name == "adjoint_q8_d4":
