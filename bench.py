@@ -254,6 +254,15 @@ def run_reference(args, wl):
                         "the rest did not fit the %.0f s budget)" % (n, args.steps, total_budget)
               if n < args.steps else "all %d timed steps (step + re-mesh, whole tree)" % n}
         timed_steps = max(n, 1)
+    elif hasattr(wl, "c_prev"):
+        for _ in range(args.warmup):
+            cpu_baseline_bdf2(wl, per_step)
+        secs, pts = 0.0, 0
+        for _ in range(args.steps):
+            cb, _, k = cpu_baseline_bdf2(wl, per_step)
+            secs += cb["seconds"]
+            pts += 2 * k * (wl.q + 1) ** 3
+        cb["sample"] = "per step: " + cb["sample"]
     elif isinstance(wl, GridWorkloadType()):
         for _ in range(args.warmup):
             cpu_baseline_grid(wl, per_step)
@@ -747,6 +756,132 @@ def run_remesh(args, wl, rank, world, local_rank):
     assert ctx.check() == 0
 
 
+def cpu_baseline_bdf2(wl, budget_s=12.0):
+    """The oracle's BDF2 step on the first k leaves' targets, k sized for about
+    budget_s of CPU work."""
+    from oracle import oracle as ora
+    vel = dict(anchor=wl.a, depth=wl.d, q=wl.q, dof=3, coeff=wl.vc)
+    prev = dict(anchor=wl.a, depth=wl.d, q=wl.q, dof=1, coeff=wl.c_prev)
+    cur = dict(anchor=wl.a, depth=wl.d, q=wl.q, dof=1, coeff=wl.c_cur)
+    ora.pt2coeff(wl.q)
+
+    def run(k):
+        return ora.semilag_bdf2(vel, prev, cur, dict(anchor=wl.a[:k], depth=wl.d[:k], q=wl.q),
+                                wl.t0, wl.dt)
+    probe = 8
+    t0 = time.perf_counter()
+    run(probe)
+    per_leaf = max((time.perf_counter() - t0) / probe, 1e-6)
+    k = int(max(probe, min(len(wl.d), budget_s / per_leaf)))
+    t0 = time.perf_counter()
+    out = run(k)
+    sec = time.perf_counter() - t0
+    npl = (wl.q + 1) ** 3
+    return {"value": 2 * k * npl / sec, "unit": UNIT, "cores": ora.num_threads(), "kind": "port",
+            "sample": "targets of the first %d of %d leaves (%d departure points: two per "
+                      "target), one BDF2 step" % (k, len(wl.d), 2 * k * npl),
+            "seconds": sec}, out, k
+
+
+def run_bdf2(args, wl, rank, world, local_rank):
+    """BDF2 two-backtrace steps (tbslas_semilag_bdf2), three concentration
+    trees rotating roles (next <- 4/3 cur(X1) - 1/3 prev(X2)); value counts
+    both departure points of every target."""
+    import torch
+    import tbslas_gb300 as tb
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = tb.Context(local_rank)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    tv = tb.Tree(ctx, wl.a, wl.d, wl.q, 3, wl.vc)
+    vf = tb.NodeFieldFunctor(tv, wl.bc)
+    ts = [tb.Tree(ctx, wl.a, wl.d, wl.q, 1, wl.c_prev), tb.Tree(ctx, wl.a, wl.d, wl.q, 1, wl.c_cur),
+          tb.Tree(ctx, wl.a, wl.d, wl.q, 1)]
+
+    def step(i):
+        # after i steps: prev = ts[i % 3], cur = ts[(i + 1) % 3], next = ts[(i + 2) % 3]
+        tb.solve_semilag_bdf2(vf, ts[i % 3], ts[(i + 1) % 3], ts[(i + 2) % 3],
+                              wl.t0 + i * wl.dt, wl.dt)
+    step(0)
+    torch.cuda.synchronize()
+    first = ts[2].get_coeffs()
+    for i in range(args.warmup):
+        flush.fill_(float(i))
+        step(i + 1)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            step(args.warmup + 1 + i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ctx.profile(True)
+    ctx.profile_reset()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        step(args.warmup + args.steps + 1 + i)
+    torch.cuda.synchronize()
+    prof = ctx.profile_totals()
+    ctx.profile(False)
+    # end to end: c_{n-1} and c_n from pinned host memory, c_{n+1} back, every step
+    hp = torch.from_numpy(np.ascontiguousarray(wl.c_prev)).pin_memory().numpy()
+    hc = torch.from_numpy(np.ascontiguousarray(wl.c_cur)).pin_memory().numpy()
+    hn = torch.empty(hc.shape, dtype=torch.float64).pin_memory().numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        ts[0].set_coeffs(hp)
+        ts[1].set_coeffs(hc)
+        tb.solve_semilag_bdf2(vf, ts[0], ts[1], ts[2], wl.t0, wl.dt)
+        ts[2].get_coeffs(hn)
+    torch.cuda.synchronize()
+    e2e_sec = time.perf_counter() - t0
+    points = wl.points_per_step * args.steps
+    if rank != 0:
+        return
+    cpu, ref, k = cpu_baseline_bdf2(wl)
+    cpu.pop("seconds", None)
+    accuracy = {"rel_err_vs_oracle": float(np.abs(first[:k] - ref).max() / np.abs(ref).max()),
+                "compared": "first GPU step vs the oracle on the CPU-baseline sample"}
+    groups, kernels, kms = prof.get("semilag_bdf2", (0, 0, 0.0))
+    launch_ms = kms / max(groups, 1)
+    fp32_peak = ctx.fp32_fma_peak()
+    macs = 2 * df_macs_per_point_tree(wl.q)  # both backtraces and both evaluations
+    targets = wl.points_per_step // 2
+    achieved32 = 2 * DF_FP32_INSTR_PER_MAC * macs * targets / (launch_ms * 1e-3) / 1e12
+    roofline = {
+        "kernel": "semilag_bdf2 (double-float sums + FP64 near-face pass)", "bound": "fp32",
+        "achieved": achieved32, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+        "frac": achieved32 / (fp32_peak / 1e12),
+        "peak_source": "FP32 FMA throughput measured in this run (tbslas_fp32_fma_peak)",
+        "counting": "%d double-float multiply-adds per target (both backtraces and both "
+                    "evaluations; the first stage from the node grid) x %d FP32 instructions, "
+                    "each counted as 2 FLOP" % (macs, DF_FP32_INSTR_PER_MAC),
+        "launch_ms": launch_ms, "traffic": None,
+        "kernels_ms_per_step": {k2: v[2] / args.steps for k2, v in prof.items()}}
+    cfg = wl.describe()
+    cfg.update({"l2": "flushed between timed steps (256 MiB write inside the timed loop)",
+                "parallelism": "replicas x%d" % world, "nrk": 1})
+    line = {"metric": METRIC, "value": points / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded analytic fields)", "config": cfg,
+            "e2e": {"value": points / e2e_sec, "unit": UNIT,
+                    "h2d_bytes_per_step": int(hp.nbytes + hc.nbytes),
+                    "d2h_bytes_per_step": int(hn.nbytes)},
+            "targets_per_s": points / 2 / (ms * 1e-3),
+            "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
+            "clocks": clk.summary(), "gpu_launches": int(sum(v[1] for v in prof.values()))}
+    print(json.dumps(line))
+    assert ctx.check() == 0
+
+
 def run_batched(args, wl, rank, world, local_rank):
     """Config 4: the batched, graph-captured step vs the plain per-problem
     loop of in-situ steps on the same problems, from the same state."""
@@ -1107,6 +1242,8 @@ def main():
             run_adjoint(args, wl, rank, world, local_rank)
         elif hasattr(wl, "remesh"):
             run_remesh(args, wl, rank, world, local_rank)
+        elif hasattr(wl, "c_prev"):
+            run_bdf2(args, wl, rank, world, local_rank)
         else:
             run_gpu(args, wl, rank, world, local_rank)
     finally:

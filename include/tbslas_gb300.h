@@ -254,6 +254,46 @@ int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con
                                 double* con_coeff_host, int timestep, double dt, int nrk,
                                 int bc);
 
+/* In-situ step through a time-dependent velocity: m (1..4) velocity trees
+ * blended per RK2 stage, the velocity at stage j (two per sub-step: at X,
+ * then at X*) being sum_k w[j*m + k] v_k; w: host [2*nrk][m].  The
+ * reference's time-dependent functors map to weights:
+ *  - FieldSetFunctor (src/tree/tree_set_functor.h:49-72): four trees at times
+ *    T[4], cubic in time (CubicInterpPolicy::InterpCubic1D, src/utils/cubic.h:
+ *    42-56), queried by IntegrateRK2 at tinit and tinit + tau/2 of each
+ *    sub-step (src/semilag/traj.inc:20-45): w[2s*4 + k] and w[(2s+1)*4 + k]
+ *    from tbslas_cubic_time_weights;
+ *  - FieldExtrapFunctor (src/tree/tree_extrap_functor.h:47-78) with the
+ *    current field as the first-stage functor (the two-functor
+ *    SolveSemilagInSitu, src/tree/tree_semilag.h:137-180, traj.inc:71-93):
+ *    trees {v_n, v_{n-1}}, w = {1, 0, 1.5, -0.5} per sub-step.
+ * Trees of one leaf structure with nrk = 1 run the fused step on the
+ * per-stage blends of their coefficients (the context's sum mode); otherwise
+ * every tree is evaluated at every stage point in FP64.  Velocity trees share
+ * the concentration's degree; the concentration has dof 1. */
+int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, const double* w,
+                              tbslas_tree con, int timestep, double dt, int nrk, int bc,
+                              void* stream);
+/* w[4] with InterpCubic1D(t, times, p) = sum_k w[k] p[k] for every p (the
+ * interpolant is linear in p); times strictly increasing.  Host only. */
+int tbslas_cubic_time_weights(const double* times, double t, double* w);
+
+/* Second-order (BDF2) semi-Lagrangian step with two backtraces, the step of
+ * the reference's advection-diffusion driver (src/applications/src/
+ * advdiff-ss.cpp:485-521): for every Chebyshev node X of con_next,
+ *   X1 = ComputeTrajRK2(vel, X, t, t - dt, nrk),
+ *   X2 = ComputeTrajRK2(vel, X1, t - dt, t - 2 dt, nrk),
+ *   value = 4/3 con_cur(X1) - 1/3 con_prev(X2),
+ * refitted into con_next (SetTreeGridValues).  t is the driver's current
+ * time (its running tcurr); the sub-steps are computed from it as the
+ * reference does.  The four trees share one Chebyshev degree (vel dof 3, the
+ * others dof 1); con_next may be con_cur or con_prev itself (it is only
+ * written after both are read).  The context's sum mode applies as in
+ * tbslas_semilag_in_situ. */
+int tbslas_semilag_bdf2(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con_prev,
+                        tbslas_tree con_cur, tbslas_tree con_next, double t, double dt, int nrk,
+                        int bc, void* stream);
+
 /* ---- differentiation (adjoint of the in-situ step, nrk = 1) ------------------ */
 /* No counterpart in the reference.  The forward map of one step is
  * C^{k+1} = refit(c^k(Xd(V))), Xd = X + tau v(X + tau/2 v(X)), for every node

@@ -153,6 +153,84 @@ def semilag_in_situ(vel, con, timestep, dt, nrk=1, periodic=False, M=None, leaf_
     return out
 
 
+def semilag_bdf2(vel, prev, cur, nxt, t, dt, nrk=1, periodic=False, M=None):
+    """BDF2 two-backtrace step of the advection-diffusion driver
+    (src/applications/src/advdiff-ss.cpp:485-521), composed from the oracle's
+    ComputeTrajRK2 / EvalTree / SetTreeGridValues restatements: for every node
+    X of nxt (anchor, depth, q), X1 = traj(X, t -> t - dt), X2 = traj(X1,
+    t - dt -> t - 2 dt), value = 4/3 cur(X1) - 1/3 prev(X2); returns nxt's new
+    coefficients.  vel / prev / cur: dicts with anchor, depth, q, dof, coeff."""
+    q = nxt["q"]
+    pts = collect_grid_points(nxt["anchor"], nxt["depth"], q)
+    x1 = traj_rk2(vel["anchor"], vel["depth"], vel["q"], vel["coeff"], pts, t, t - dt, nrk,
+                  periodic)
+    a = eval_tree(cur["anchor"], cur["depth"], cur["q"], 1, cur["coeff"], x1, periodic)
+    x2 = traj_rk2(vel["anchor"], vel["depth"], vel["q"], vel["coeff"], x1, t - dt, t - dt * 2,
+                  nrk, periodic)
+    b = eval_tree(prev["anchor"], prev["depth"], prev["q"], 1, prev["coeff"], x2, periodic)
+    vals = (4.0 / 3) * a - (1.0 / 3) * b
+    return set_tree_grid_values(len(nxt["depth"]), q, 1, vals.reshape(-1), M)
+
+
+def interp_cubic_1d(x, xx, pp):
+    """CubicInterpPolicy::InterpCubic1D (src/utils/cubic.h:42-56), elementwise
+    over the value arrays pp[0..3]."""
+    def tangent(tk_1, tk, tk1, pk_1, pk, pk1):
+        return (pk1 - pk) * 0.5 / (tk1 - tk) + (pk - pk_1) * 0.5 / (tk - tk_1)
+    mk = tangent(xx[0], xx[1], xx[2], pp[0], pp[1], pp[2])
+    mk1 = tangent(xx[1], xx[2], xx[3], pp[1], pp[2], pp[3])
+    t = (x - xx[1]) / (xx[2] - xx[1])
+    h00 = 2 * t * t * t - 3 * t * t + 1
+    h10 = t * t * t - 2 * t * t + t
+    h01 = -2 * t * t * t + 3 * t * t
+    h11 = t * t * t - t * t
+    return h00 * pp[1] + h10 * (xx[2] - xx[1]) * mk + h01 * pp[2] + h11 * (xx[2] - xx[1]) * mk1
+
+
+def semilag_in_situ_tv(vels, con, timestep, dt, nrk=1, periodic=False, times=None, M=None):
+    """In-situ step through a time-dependent velocity (SolveSemilagInSitu ->
+    SolveSemilagRK2 -> ComputeTrajRK2 -> IntegrateRK2, src/tree/tree_semilag.h:
+    92-180, src/semilag/semilag.inc:26-80, src/semilag/traj.inc:20-93):
+    with `times`, vels are the four trees of a FieldSetFunctor
+    (tree_set_functor.h:49-72: every tree evaluated, then InterpCubic1D at the
+    stage's time); without, vels = [v_n, v_{n-1}] of the two-functor form
+    (v_n at X, FieldExtrapFunctor's 1.5 v_n - 0.5 v_{n-1} at X*,
+    tree_extrap_functor.h:47-78).  Each evaluation wraps the point array in
+    place under periodic boundaries (EvalTree's aliasing)."""
+    q = con["q"]
+    x = collect_grid_points(con["anchor"], con["depth"], q)
+    tinit = timestep * dt
+    tfinal = tinit - dt
+    tau = (tfinal - tinit) / nrk
+
+    def wrap(p):
+        if periodic:
+            p = np.where(p < 0.0, p + 1.0, p)
+            p = np.where(p >= 1.0, p - 1.0, p)
+        return p
+
+    def ev(tr, p):
+        return eval_tree(tr["anchor"], tr["depth"], tr["q"], 3, tr["coeff"], p, periodic)
+
+    cur = tinit
+    for _ in range(nrk):
+        x = wrap(x)
+        if times is not None:
+            v = interp_cubic_1d(cur, times, [ev(tr, x) for tr in vels])
+        else:
+            v = ev(vels[0], x)
+        xt = x + 0.5 * tau * v
+        xt = wrap(xt)
+        if times is not None:
+            v = interp_cubic_1d(cur + 0.5 * tau, times, [ev(tr, xt) for tr in vels])
+        else:
+            v = 1.5 * ev(vels[0], xt) - 0.5 * ev(vels[1], xt)
+        x = x + tau * v
+        cur = cur + tau
+    c = eval_tree(con["anchor"], con["depth"], q, 1, con["coeff"], x, periodic)
+    return set_tree_grid_values(len(con["depth"]), q, 1, c.reshape(-1), M)
+
+
 def semilag_in_situ_dual(vel, vel_d, con, con_d, timestep, dt, nrk=1, periodic=False, M=None):
     """One SL step on forward-mode dual numbers: returns (new coefficients,
     their derivative along the input direction (vel_d, con_d))."""

@@ -309,6 +309,86 @@ def solve_semilag_in_situ(vel_functor, tree, timestep, dt, num_rk_step=1, stream
     return None
 
 
+def cubic_time_weights(times, t):
+    """w[4] with CubicInterpPolicy::InterpCubic1D(t, times, p) = w . p."""
+    tm = np.ascontiguousarray(times, dtype=np.float64)
+    w = np.empty(4)
+    call("tbslas_cubic_time_weights", tm.ctypes.data, float(t), w.ctypes.data)
+    return w
+
+
+def _stage_times(timestep, dt, nrk):
+    """(time at X, time at X*) of each RK2 sub-step as ComputeTrajRK2 /
+    IntegrateRK2 pass them (src/semilag/traj.inc:20-68)."""
+    tinit = timestep * dt
+    tfinal = tinit - dt
+    tau = (tfinal - tinit) / nrk
+    out, cur = [], tinit
+    for _ in range(nrk):
+        out.append((cur, cur + 0.5 * tau))
+        cur = cur + tau
+    return out
+
+
+class FieldSetFunctor:
+    """Velocity interpolated cubically in time between four trees
+    (tbslas::FieldSetFunctor, src/tree/tree_set_functor.h:28-103)."""
+
+    def __init__(self, trees, times, bc=FreeSpace):
+        if len(trees) != 4 or len(times) != 4:
+            raise ValueError("four trees and four times")
+        self.trees, self.times, self.bc = list(trees), [float(x) for x in times], int(bc)
+
+    def update(self, new_tree, time):
+        """Drop the oldest tree, append new_tree at `time` (as the reference)."""
+        self.trees = self.trees[1:] + [new_tree]
+        self.times = self.times[1:] + [float(time)]
+
+    def stage_weights(self, timestep, dt, nrk):
+        w = []
+        for t0, t1 in _stage_times(timestep, dt, nrk):
+            w.extend(cubic_time_weights(self.times, t0))
+            w.extend(cubic_time_weights(self.times, t1))
+        return self.trees, np.asarray(w)
+
+
+class FieldExtrapFunctor:
+    """1.5 v_n - 0.5 v_{n-1} (tbslas::FieldExtrapFunctor,
+    src/tree/tree_extrap_functor.h:27-95), used at the midpoint stage while
+    the first stage takes v_n (the two-functor SolveSemilagInSitu)."""
+
+    def __init__(self, tree_prev, tree_cur, bc=FreeSpace):
+        self.tp, self.tc, self.bc = tree_prev, tree_cur, int(bc)
+
+    def update(self, new_tree, time=None):
+        self.tp, self.tc = self.tc, new_tree
+
+    def stage_weights(self, timestep, dt, nrk):
+        return [self.tc, self.tp], np.tile([1.0, 0.0, 1.5, -0.5], nrk)
+
+
+def solve_semilag_in_situ_tv(vel_functor, tree, timestep, dt, num_rk_step=1, stream=None):
+    """In-situ SL step through a FieldSetFunctor or FieldExtrapFunctor
+    velocity (tbslas_semilag_in_situ_tv)."""
+    trees, w = vel_functor.stage_weights(timestep, dt, int(num_rk_step))
+    handles = (ctypes.c_void_p * len(trees))(*[t.handle.value for t in trees])
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    call("tbslas_semilag_in_situ_tv", tree.ctx.handle, len(trees), ctypes.addressof(handles),
+         w.ctypes.data, tree.handle, int(timestep), float(dt), int(num_rk_step), vel_functor.bc,
+         _stream(stream))
+
+
+def solve_semilag_bdf2(vel_functor, tree_prev, tree_cur, tree_next, t, dt, num_rk_step=1,
+                       stream=None):
+    """BDF2 two-backtrace SL step (the advection-diffusion driver's step,
+    src/applications/src/advdiff-ss.cpp:485-521): tree_next's coefficients
+    become the fit of 4/3 tree_cur(X1) - 1/3 tree_prev(X2) at its nodes, X1 /
+    X2 the RK2 backtraces from t over one and two steps of dt."""
+    call("tbslas_semilag_bdf2", tree_next.ctx.handle, vel_functor.tree.handle, tree_prev.handle,
+         tree_cur.handle, tree_next.handle, float(t), float(dt), int(num_rk_step),
+         vel_functor.bc, _stream(stream))
+
+
 class Batch:
     """Many independent in-situ SL problems advanced by one kernel per step.
 

@@ -45,9 +45,15 @@ int fail(int code, const char* fmt, ...) {
   } while (0)
 
 DegreeKernels g_kernels[TBSLAS_MAX_DEGREE + 1];
+Bdf2Fn g_bdf2[TBSLAS_MAX_DEGREE + 1] = {};
+TvFn g_tv[TBSLAS_MAX_DEGREE + 1] = {};
 std::once_flag g_kernels_once;
 
 void init_kernels() {
+  register_tv_a(g_tv);
+  register_tv_b(g_tv);
+  register_bdf2_a(g_bdf2);
+  register_bdf2_b(g_bdf2);
   register_degrees_a(g_kernels);
   register_degrees_b(g_kernels);
   register_degrees_c(g_kernels);
@@ -114,6 +120,12 @@ enum Slot {
   kRmGroup,
   kRmTable,
   kRmScalars,
+  // time-dependent velocity: the two stage blends of a velocity set
+  kTvC1,
+  kTvC2,
+  kTvC2s,
+  kTvN2,
+  kTvFlag,
   kNumSlots
 };
 
@@ -593,46 +605,82 @@ double sl_tau(int timestep, double dt, int nrk) {
   return (tfinal - tinit) / nrk;
 }
 
+// Do two key arrays differ?  (*flag set to 1 if so)
+__global__ void k_keys_differ(const uint64_t* __restrict__ a, const uint64_t* __restrict__ b,
+                              int64_t n, int* __restrict__ flag) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n && a[i] != b[i]) *flag = 1;
+}
+
+// CubicInterpPolicy::InterpCubic1D (src/utils/cubic.h:42-56): Hermite
+// interpolation on [xx1, xx2] with tangents from the neighbouring
+// differences, at x, of the values pp.
+double interp_cubic_1d(double x, const double* xx, const double* pp) {
+  auto tangent = [](double tk_1, double tk, double tk1, double pk_1, double pk, double pk1) {
+    return (pk1 - pk) * 0.5 / (tk1 - tk) + (pk - pk_1) * 0.5 / (tk - tk_1);
+  };
+  const double mk = tangent(xx[0], xx[1], xx[2], pp[0], pp[1], pp[2]);
+  const double mk1 = tangent(xx[1], xx[2], xx[3], pp[1], pp[2], pp[3]);
+  const double t = (x - xx[1]) / (xx[2] - xx[1]);
+  const double h00 = 2 * t * t * t - 3 * t * t + 1, h10 = t * t * t - 2 * t * t + t;
+  const double h01 = -2 * t * t * t + 3 * t * t, h11 = t * t * t - t * t;
+  return h00 * pp[1] + h10 * (xx[2] - xx[1]) * mk + h01 * pp[2] + h11 * (xx[2] - xx[1]) * mk1;
+}
+
+// The fused step of a dof-1 concentration through a velocity of its degree:
+// the first RK stage from v1 at the nodes, the others from v2 (one tree for
+// the plain step; two blends of a velocity set for the time-dependent one).
+int fused_step(tbslas_ctx ctx, const TreeView& v1, const TreeView& v2, tbslas_tree con,
+               double tau, int nrk, int bc, cudaStream_t s, double* xmid, double* xdep) {
+  const int64_t N = con->L * n_points(con->q);
+  double* vals;
+  TRY(scratch_t(ctx, kVals, N, &vals));
+  SemilagTreeArgs a;
+  a.vel = v2;
+  a.con = con->view();
+  a.nodes = nodes_1d(con->q);
+  a.tau = tau;
+  a.nrk = nrk;
+  a.periodic = bc;
+  a.vals = vals;
+  a.xmid = xmid;
+  a.xdep = xdep;
+  {
+    // first RK stage: the velocity at the targets by sum factorisation
+    double* vn = nullptr;
+    TRY(scratch_t(ctx, kVN, N * 3, &vn));
+    ProfScope pv(ctx, "vel_at_nodes", s);
+    launch_eval_on_nodes(v1, a.con, bc, vn, s);
+    TRY(check_launch("velocity at nodes"));
+    a.vn = vn;
+  }
+  TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
+  TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
+  a.fix_grid = ctx->num_sms * 8;
+  if (ctx->sums == TBSLAS_SUMS_FP64) {
+    ProfScope p(ctx, "semilag_tree", s, 1);
+    g_kernels[con->q].semilag(a, s);
+  } else {
+    ProfScope p(ctx, "semilag_tree", s, 2);
+    g_kernels[con->q].semilag_df(a, s);
+  }
+  TRY(check_launch("semilag_tree"));
+  return refit_dev(ctx, con, vals, s);
+}
+
 int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
                         int nrk, int bc, cudaStream_t s, double* xmid = nullptr,
                         double* xdep = nullptr) {
   const double tau = sl_tau(timestep, dt, nrk);
   const int64_t np = n_points(con->q);
   const int64_t N = con->L * np;
+  if (vel->q == con->q && con->dof == 1) {
+    const TreeView v = vel->view();
+    return fused_step(ctx, v, v, con, tau, nrk, bc, s, xmid, xdep);
+  }
   double* vals;
   TRY(scratch_t(ctx, kVals, N * con->dof, &vals));
-  if (vel->q == con->q && con->dof == 1) {
-    SemilagTreeArgs a;
-    a.vel = vel->view();
-    a.con = con->view();
-    a.nodes = nodes_1d(con->q);
-    a.tau = tau;
-    a.nrk = nrk;
-    a.periodic = bc;
-    a.vals = vals;
-    a.xmid = xmid;
-    a.xdep = xdep;
-    {
-      // first RK stage: the velocity at the targets by sum factorisation
-      double* vn = nullptr;
-      TRY(scratch_t(ctx, kVN, N * 3, &vn));
-      ProfScope pv(ctx, "vel_at_nodes", s);
-      launch_eval_on_nodes(a.vel, a.con, bc, vn, s);
-      TRY(check_launch("velocity at nodes"));
-      a.vn = vn;
-    }
-    TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
-    TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
-    a.fix_grid = ctx->num_sms * 8;
-    if (ctx->sums == TBSLAS_SUMS_FP64) {
-      ProfScope p(ctx, "semilag_tree", s, 1);
-      g_kernels[con->q].semilag(a, s);
-    } else {
-      ProfScope p(ctx, "semilag_tree", s, 2);
-      g_kernels[con->q].semilag_df(a, s);
-    }
-    TRY(check_launch("semilag_tree"));
-  } else {
+  {
     double *X, *Xdep, *vt;
     TRY(scratch_t(ctx, kXA, N * 3, &X));
     TRY(scratch_t(ctx, kXB, N * 3, &Xdep));
@@ -1524,6 +1572,150 @@ int tbslas_semilag_in_situ(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int
 }
 
 }  // extern "C"
+
+int tbslas_semilag_bdf2(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con_prev,
+                        tbslas_tree con_cur, tbslas_tree con_next, double t, double dt, int nrk,
+                        int bc, void* stream) {
+  TRY(check_step_args(ctx, vel, con_cur, dt, nrk, bc));
+  TRY(check_tree(con_prev));
+  TRY(check_tree(con_next));
+  if (con_prev->ctx != ctx || con_next->ctx != ctx)
+    return fail(TBSLAS_ERR_INVALID_ARG, "trees belong to another context");
+  if (!std::isfinite(t)) return fail(TBSLAS_ERR_INVALID_ARG, "t is not finite");
+  const int q = con_next->q;
+  if (vel->q != q || con_cur->q != q || con_prev->q != q || con_cur->dof != 1 ||
+      con_prev->dof != 1 || con_next->dof != 1 || !g_bdf2[q])
+    return fail(TBSLAS_ERR_UNSUPPORTED, "BDF2 step needs a dof-3 velocity and dof-1 "
+                                        "concentration trees of one degree");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t N = con_next->L * n_points(q);
+  Bdf2Args a;
+  a.vel = vel->view();
+  a.prev = con_prev->view();
+  a.cur = con_cur->view();
+  a.next = con_next->view();
+  a.nodes = nodes_1d(q);
+  // the two backtraces' sub-steps as the driver computes them: from t to
+  // t - dt, then from t - dt to t - 2 dt (ComputeTrajRK2's (tfinal - tinit) / nrk)
+  a.tau1 = ((t - dt) - t) / nrk;
+  a.tau2 = ((t - dt * 2) - (t - dt)) / nrk;
+  a.nrk = nrk;
+  a.periodic = bc;
+  double* vn = nullptr;
+  TRY(scratch_t(ctx, kVals, N, &a.vals));
+  TRY(scratch_t(ctx, kVN, N * 3, &vn));
+  TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
+  TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
+  a.fix_grid = ctx->num_sms * 8;
+  {
+    ProfScope pv(ctx, "vel_at_nodes", s, 2);
+    launch_eval_on_nodes(a.vel, a.next, bc, vn, s);
+  }
+  TRY(check_launch("velocity at nodes"));
+  a.vn = vn;
+  {
+    const bool df = ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT;
+    ProfScope p(ctx, "semilag_bdf2", s, df ? 2 : 1);
+    g_bdf2[q](a, df, s);
+  }
+  TRY(check_launch("semilag_bdf2"));
+  return refit_dev(ctx, con_next, a.vals, s);
+}
+
+int tbslas_cubic_time_weights(const double* times, double t, double* w) {
+  if (!times || !w) return fail(TBSLAS_ERR_INVALID_ARG, "null pointer");
+  if (!(times[0] < times[1] && times[1] < times[2] && times[2] < times[3]) ||
+      !std::isfinite(times[0]) || !std::isfinite(times[3]) || !std::isfinite(t))
+    return fail(TBSLAS_ERR_INVALID_ARG, "times must be finite and increasing");
+  for (int k = 0; k < 4; ++k) {
+    double e[4] = {0.0, 0.0, 0.0, 0.0};
+    e[k] = 1.0;
+    w[k] = interp_cubic_1d(t, times, e);  // the interpolant is linear in the values
+  }
+  return TBSLAS_OK;
+}
+
+int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, const double* w,
+                              tbslas_tree con, int timestep, double dt, int nrk, int bc,
+                              void* stream) {
+  if (m < 1 || m > kTvMaxTrees)
+    return fail(TBSLAS_ERR_INVALID_ARG, "%d velocity trees (1..%d)", m, kTvMaxTrees);
+  if (!vel || !w) return fail(TBSLAS_ERR_INVALID_ARG, "null pointer");
+  if (nrk > kTvMaxSubsteps)
+    return fail(TBSLAS_ERR_UNSUPPORTED, "nrk %d > %d with a velocity set", nrk, kTvMaxSubsteps);
+  for (int k = 0; k < m; ++k) {
+    TRY(check_step_args(ctx, vel[k], con, dt, nrk, bc));
+    if (vel[k]->q != con->q)
+      return fail(TBSLAS_ERR_UNSUPPORTED, "velocity set: degree %d vs the concentration's %d",
+                  vel[k]->q, con->q);
+  }
+  if (con->dof != 1) return fail(TBSLAS_ERR_UNSUPPORTED, "velocity set: dof-1 concentration only");
+  for (int j = 0; j < 2 * nrk * m; ++j)
+    if (!std::isfinite(w[j])) return fail(TBSLAS_ERR_INVALID_ARG, "weight %d is not finite", j);
+  cudaStream_t s = (cudaStream_t)stream;
+  const double tau = sl_tau(timestep, dt, nrk);
+  // one leaf structure (and nrk = 1): blend the coefficients per stage and run
+  // the fused step
+  bool same = nrk == 1;
+  for (int k = 1; k < m && same; ++k) same = vel[k]->L == vel[0]->L;
+  if (same && m > 1) {
+    int* flag;
+    TRY(scratch_t(ctx, kTvFlag, 1, &flag));
+    CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    for (int k = 1; k < m; ++k)
+      k_keys_differ<<<blocks_for(vel[0]->L, 256), 256, 0, s>>>(vel[0]->d_keys, vel[k]->d_keys,
+                                                              vel[0]->L, flag);
+    TRY(check_launch("velocity set structure"));
+    int h = 0;
+    CUDA_TRY(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    same = h == 0;
+  }
+  if (same) {
+    const tbslas_tree v0 = vel[0];
+    const int64_t n = v0->L * v0->stride;
+    const double* c[kTvMaxTrees];
+    for (int k = 0; k < m; ++k) c[k] = vel[k]->d_coeff;
+    double *c1, *c2, *n2;
+    float2* c2s;
+    TRY(scratch_t(ctx, kTvC1, n, &c1));
+    TRY(scratch_t(ctx, kTvC2, n, &c2));
+    TRY(scratch_t(ctx, kTvC2s, n, &c2s));
+    TRY(scratch_t(ctx, kTvN2, v0->L * 3, &n2));
+    {
+      ProfScope pb(ctx, "velocity_blend", s, 4);
+      launch_blend_coeffs(c, w, m, n, c1, s);
+      launch_blend_coeffs(c, w + m, m, n, c2, s);
+      launch_split(c2, c2s, n, ctx->d_err, s);
+      k_cnorm<<<blocks_for(v0->L * 3, 128), 128, 0, s>>>(c2, v0->L, 3, (int)n_coeff(v0->q),
+                                                         v0->stride, n2);
+    }
+    TRY(check_launch("velocity blend"));
+    TreeView b1 = v0->view(), b2 = v0->view();
+    b1.coeff = c1;
+    b2.coeff = c2;
+    b2.coeff2 = c2s;
+    b2.cnorm = n2;
+    return fused_step(ctx, b1, b2, con, tau, 1, bc, s, nullptr, nullptr);
+  }
+  // general: every tree evaluated at every stage point (FP64)
+  TvArgs a;
+  for (int k = 0; k < m; ++k) a.vel[k] = vel[k]->view();
+  a.m = m;
+  a.con = con->view();
+  a.nodes = nodes_1d(con->q);
+  a.tau = tau;
+  a.nrk = nrk;
+  a.periodic = bc;
+  for (int j = 0; j < 2 * nrk * m; ++j) a.w[j] = w[j];
+  TRY(scratch_t(ctx, kVals, con->L * n_points(con->q), &a.vals));
+  {
+    ProfScope p(ctx, "semilag_tv", s);
+    g_tv[con->q](a, s);
+  }
+  TRY(check_launch("semilag_tv"));
+  return refit_dev(ctx, con, a.vals, s);
+}
 
 // For the adjoint's checkpointed forward (adjoint.cu).
 namespace tbg {

@@ -70,6 +70,52 @@ struct BucketScratch {
   Tile* tiles;                  // [n / kTile + 1 + L]
 };
 
+// The BDF2 two-backtrace step (bdf2_kernels.cuh): value at every node X of
+// `next` = 4/3 cur(X1) - 1/3 prev(X2), X1 and X2 the RK2 backtraces over one
+// and two steps.
+struct Bdf2Args {
+  TreeView vel;       // dof 3
+  TreeView prev;      // c_{n-1}, dof 1
+  TreeView cur;       // c_n, dof 1
+  TreeView next;      // the target tree (its nodes); same degree as the others
+  Nodes1D nodes;      // 1-D nodes of the degree
+  double tau1, tau2;  // sub-step of the first / second backtrace
+  int nrk;
+  int periodic;
+  double* vals;       // [next.L * Np]
+  const double* vn;   // [next.L * Np][3] velocity at the targets
+  int64_t* fix_list;  // targets the double-float kernel hands to the FP64 pass
+  unsigned long long* fix_count;
+  int fix_grid;
+};
+
+typedef void (*Bdf2Fn)(const Bdf2Args&, bool df_sums, cudaStream_t);
+void register_bdf2_a(Bdf2Fn* table);  // index = Chebyshev degree q
+void register_bdf2_b(Bdf2Fn* table);
+
+// The in-situ step through a blended set of velocity trees (tv_kernels.cuh):
+// the velocity at the stage point of RK2 stage j (2 per sub-step: at X, then
+// at X*) is sum_k w[j * m + k] v_k.
+constexpr int kTvMaxTrees = 4;
+constexpr int kTvMaxSubsteps = 8;
+struct TvArgs {
+  TreeView vel[kTvMaxTrees];  // dof 3, same degree as con
+  int m;                      // trees in use
+  TreeView con;               // dof 1
+  Nodes1D nodes;
+  double tau;
+  int nrk;
+  int periodic;
+  double* vals;  // [con.L * Np]
+  double w[2 * kTvMaxSubsteps * kTvMaxTrees];
+};
+typedef void (*TvFn)(const TvArgs&, cudaStream_t);
+void register_tv_a(TvFn* table);  // index = Chebyshev degree q
+void register_tv_b(TvFn* table);
+// out[i] = sum_k w[k] c_k[i], i < n (tv_deg_a.cu)
+void launch_blend_coeffs(const double* const* c, const double* w, int m, int64_t n, double* out,
+                         cudaStream_t s);
+
 typedef void (*SemilagTreeFn)(const SemilagTreeArgs&, cudaStream_t);
 typedef void (*TrajFn)(const TrajArgs&, cudaStream_t);
 typedef void (*EvalTilesFn)(const EvalTilesArgs&, cudaStream_t);

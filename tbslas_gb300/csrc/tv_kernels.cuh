@@ -1,0 +1,68 @@
+// In-situ SL step through a time-dependent velocity: a set of up to four
+// velocity trees blended with per-stage weights -- the reference's
+// FieldSetFunctor (cubic interpolation in time of four trees,
+// src/tree/tree_set_functor.h:49-72, src/utils/cubic.h:42-56) and
+// FieldExtrapFunctor (1.5 v_n - 0.5 v_{n-1}, src/tree/tree_extrap_functor.h:
+// 47-78) as IntegrateRK2 calls them at each stage (src/semilag/traj.inc:
+// 20-45, :71-93).  This is the general kernel, instantiated per degree by
+// tv_deg_*.cu: every tree is evaluated at every stage point in FP64 and the
+// values blended, so the trees may have different leaf structures.  Trees of
+// one structure take the fast path in capi.cu instead (blended coefficients
+// through the fused step).
+#pragma once
+
+#include "tree_kernels.cuh"
+
+namespace tbg {
+
+template <int D>
+__device__ __forceinline__ void tv_velocity(const TvArgs& a, int stage, double& x, double& y,
+                                            double& z, bool per, double (&v)[3]) {
+  const double* w = a.w + stage * a.m;
+  v[0] = v[1] = v[2] = 0.0;
+  for (int k = 0; k < a.m; ++k) {
+    double u[3];
+    eval_point<D, 3>(a.vel[k], x, y, z, per, u);  // wraps the point in place
+    v[0] = fma(w[k], u[0], v[0]);
+    v[1] = fma(w[k], u[1], v[1]);
+    v[2] = fma(w[k], u[2], v[2]);
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_semilag_tv(const TvArgs a) {
+  constexpr int NP = D * D * D;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= a.con.L * NP) return;
+  const int64_t leaf = t / NP;
+  const int p = (int)(t - leaf * NP);
+  const Geom g = load_geom(a.con.geom + leaf);
+  const double h = 2.0 / g.w;
+  double x = g.x + h * a.nodes.x[p % D];
+  double y = g.y + h * a.nodes.x[(p / D) % D];
+  double z = g.z + h * a.nodes.x[p / (D * D)];
+  const bool per = a.periodic != 0;
+  const double half_tau = 0.5 * a.tau;
+#pragma unroll 1
+  for (int s = 0; s < a.nrk; ++s) {
+    double v[3];
+    tv_velocity<D>(a, 2 * s, x, y, z, per, v);  // at X (wrapped in place)
+    double px = fma(half_tau, v[0], x), py = fma(half_tau, v[1], y),
+           pz = fma(half_tau, v[2], z);
+    tv_velocity<D>(a, 2 * s + 1, px, py, pz, per, v);  // at X*
+    x = fma(a.tau, v[0], x);
+    y = fma(a.tau, v[1], y);
+    z = fma(a.tau, v[2], z);
+  }
+  double c[1];
+  eval_point<D, 1>(a.con, x, y, z, per, c);
+  a.vals[t] = c[0];
+}
+
+template <int D>
+void launch_semilag_tv(const TvArgs& a, cudaStream_t s) {
+  const int64_t n = a.con.L * D * D * D;
+  if (n > 0) k_semilag_tv<D><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+}
+
+}  // namespace tbg

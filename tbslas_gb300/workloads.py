@@ -85,6 +85,36 @@ def tree_adaptive_q8_remesh():
     return wl
 
 
+class Bdf2Workload:
+    """The BDF2 two-backtrace step (the advection-diffusion driver's step,
+    src/applications/src/advdiff-ss.cpp:485-521) on the uniform q = 8
+    configuration: rotation on the depth-4 tree, the Gaussian at t - dt and
+    t - 2 dt as c_n and c_{n-1}, the three concentration trees of one shape."""
+
+    def __init__(self, q=8, depth=4, dt=0.01, name="bdf2_q8"):
+        self.name, self.q, self.dt, self.bc = name, q, dt, 0
+        self.a, self.d = trees.uniform_tree(depth)
+        self.vc = trees.fit(fields.rotation(2 * math.pi), self.a, self.d, q, 3)
+        self.t0 = 2 * dt  # the time of the first step's result
+
+        def blob(time):
+            return fields.rotated_gaussian((0.7, 0.5, 0.5), 0.05, 2 * math.pi, time)
+        self.c_prev = trees.fit(blob(0.0), self.a, self.d, q, 1)
+        self.c_cur = trees.fit(blob(dt), self.a, self.d, q, 1)
+
+    @property
+    def points_per_step(self):
+        return 2 * len(self.d) * (self.q + 1) ** 3  # two backtraces per target
+
+    def describe(self):
+        return {"workload": self.name, "q": self.q, "dt": self.dt, "bc": "freespace",
+                "leaves": int(len(self.d)),
+                "targets_per_step": int(len(self.d) * (self.q + 1) ** 3),
+                "departure_points_per_step": int(self.points_per_step),
+                "note": "BDF2 step 4/3 c_n(X1) - 1/3 c_{n-1}(X2), two RK2 backtraces per "
+                        "target; uniform depth-4 octree, q=8, rotation + Gaussian"}
+
+
 class GridWorkload:
     def __init__(self, n, seed=SEED):
         rng = np.random.default_rng(seed)
@@ -234,6 +264,8 @@ def make(name):
         return tree_adaptive_q14()
     if name == "tree_adaptive_q8_remesh":
         return tree_adaptive_q8_remesh()
+    if name == "bdf2_q8":
+        return Bdf2Workload()
     if name == "adjoint_q8":
         return AdjointWorkload()
     if name == "adjoint_q8_d4":

@@ -219,3 +219,25 @@ def test_fast_interp_periodic_and_grid_shift(ora):
     a = ora.fast_interp(con.ravel(), 1, N, pts, periodic=True)
     b = ora.fast_interp(con.ravel(), 1, N, pts - 1.0, periodic=True)
     assert np.allclose(a, b, atol=1e-12)
+
+
+def test_bdf2_translation_exact(ora):
+    """BDF2 two-backtrace step (advdiff-ss.cpp:485-521) under a constant
+    velocity with exact c_n, c_{n-1} of a translated polynomial: 4/3 - 1/3 = 1
+    times the exact value, on the leaves whose departure points stay inside."""
+    q, dt, t = 4, 0.01, 0.05
+    a, d = trees.uniform_tree(2)
+    v = np.array([0.7, -0.4, 0.3])
+    vc = trees.fit(lambda p: np.tile(v, (len(np.asarray(p).reshape(-1, 3)), 1)), a, d, q, 3)
+    P = _poly(np.random.default_rng(5), q)
+
+    def at(time):
+        return lambda p: P(np.asarray(p).reshape(-1, 3) - v * time)
+    vel = dict(anchor=a, depth=d, q=q, dof=3, coeff=vc)
+    prev = dict(anchor=a, depth=d, q=q, dof=1, coeff=trees.fit(at(t - 2 * dt), a, d, q, 1))
+    cur = dict(anchor=a, depth=d, q=q, dof=1, coeff=trees.fit(at(t - dt), a, d, q, 1))
+    out = ora.semilag_bdf2(vel, prev, cur, dict(anchor=a, depth=d, q=q), t, dt)
+    pts = np.random.default_rng(6).uniform(0.3, 0.7, (500, 3))
+    got = ora.eval_tree(a, d, q, 1, out, pts)
+    ref = at(t)(pts)
+    assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max()
