@@ -254,6 +254,15 @@ def run_reference(args, wl):
                         "the rest did not fit the %.0f s budget)" % (n, args.steps, total_budget)
               if n < args.steps else "all %d timed steps (step + re-mesh, whole tree)" % n}
         timed_steps = max(n, 1)
+    elif hasattr(wl, "vcs"):
+        for _ in range(args.warmup):
+            cpu_baseline_tv(wl, per_step)
+        secs, pts = 0.0, 0
+        for _ in range(args.steps):
+            cb, _, k = cpu_baseline_tv(wl, per_step)
+            secs += cb["seconds"]
+            pts += k * (wl.q + 1) ** 3
+        cb["sample"] = "per step: " + cb["sample"]
     elif hasattr(wl, "c_prev"):
         for _ in range(args.warmup):
             cpu_baseline_bdf2(wl, per_step)
@@ -882,6 +891,121 @@ def run_bdf2(args, wl, rank, world, local_rank):
     assert ctx.check() == 0
 
 
+def cpu_baseline_tv(wl, budget_s=12.0):
+    """The oracle's time-dependent step (every tree evaluated, cubic in time)
+    on the first k leaves' targets."""
+    from oracle import oracle as ora
+    vels = [dict(anchor=wl.a, depth=wl.d, q=wl.q, dof=3, coeff=c) for c in wl.vcs]
+    con = dict(anchor=wl.a, depth=wl.d, q=wl.q, dof=1, coeff=wl.cc)
+    ora.pt2coeff(wl.q)
+
+    def run(k):
+        return ora.semilag_in_situ_tv(vels, con, wl.timestep, wl.dt, 1, False, times=wl.times,
+                                      leaf_end=k)
+    probe = 8
+    t0 = time.perf_counter()
+    run(probe)
+    per_leaf = max((time.perf_counter() - t0) / probe, 1e-6)
+    k = int(max(probe, min(len(wl.d), budget_s / per_leaf)))
+    t0 = time.perf_counter()
+    out = run(k)
+    sec = time.perf_counter() - t0
+    npl = (wl.q + 1) ** 3
+    return {"value": k * npl / sec, "unit": UNIT, "cores": ora.num_threads(), "kind": "port",
+            "sample": "targets of the first %d of %d leaves, one step (four velocity trees "
+                      "evaluated per stage, numpy composition of the oracle's EvalTree)"
+                      % (k, len(wl.d)), "seconds": sec}, out, k
+
+
+def run_tv(args, wl, rank, world, local_rank):
+    """In-situ steps through a FieldSetFunctor velocity (four trees, cubic in
+    time; tbslas_semilag_in_situ_tv's blended fused step)."""
+    import torch
+    import tbslas_gb300 as tb
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = tb.Context(local_rank)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    vt = [tb.Tree(ctx, wl.a, wl.d, wl.q, 3, c) for c in wl.vcs]
+    f = tb.FieldSetFunctor(vt, wl.times, wl.bc)
+    tc = tb.Tree(ctx, wl.a, wl.d, wl.q, 1, wl.cc)
+
+    def step(i):
+        tb.solve_semilag_in_situ_tv(f, tc, wl.timestep, wl.dt)
+    step(0)
+    torch.cuda.synchronize()
+    first = tc.get_coeffs()
+    for i in range(args.warmup):
+        flush.fill_(float(i))
+        step(i + 1)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            step(i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ctx.profile(True)
+    ctx.profile_reset()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        step(i)
+    torch.cuda.synchronize()
+    prof = ctx.profile_totals()
+    ctx.profile(False)
+    host = torch.from_numpy(np.ascontiguousarray(wl.cc)).pin_memory().numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        tc.set_coeffs(host)
+        step(i)
+        tc.get_coeffs(host)
+    torch.cuda.synchronize()
+    e2e_sec = time.perf_counter() - t0
+    points = wl.points_per_step * args.steps
+    if rank != 0:
+        return
+    cpu, ref, k = cpu_baseline_tv(wl)
+    cpu.pop("seconds", None)
+    accuracy = {"rel_err_vs_oracle": float(np.abs(first[:k] - ref).max() / np.abs(ref).max()),
+                "compared": "first GPU step vs the oracle on the CPU-baseline sample"}
+    groups, kernels, kms = prof.get("semilag_tree", (0, 0, 0.0))
+    launch_ms = kms / max(groups, 1)
+    fp32_peak = ctx.fp32_fma_peak()
+    macs = df_macs_per_point_tree(wl.q)
+    achieved32 = (2 * DF_FP32_INSTR_PER_MAC * macs * wl.points_per_step / (launch_ms * 1e-3)
+                  / 1e12)
+    roofline = {
+        "kernel": "semilag_tree on the blended velocity (double-float sums + FP64 near-face "
+                  "pass)", "bound": "fp32",
+        "achieved": achieved32, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+        "frac": achieved32 / (fp32_peak / 1e12),
+        "peak_source": "FP32 FMA throughput measured in this run (tbslas_fp32_fma_peak)",
+        "counting": "%d double-float multiply-adds per point x %d FP32 instructions, each "
+                    "counted as 2 FLOP" % (macs, DF_FP32_INSTR_PER_MAC),
+        "launch_ms": launch_ms, "traffic": None,
+        "kernels_ms_per_step": {k2: v[2] / args.steps for k2, v in prof.items()}}
+    cfg = wl.describe()
+    cfg.update({"l2": "flushed between timed steps (256 MiB write inside the timed loop)",
+                "parallelism": "replicas x%d" % world, "nrk": 1})
+    line = {"metric": METRIC, "value": points / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded analytic fields)", "config": cfg,
+            "e2e": {"value": points / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(host.nbytes),
+                    "d2h_bytes_per_step": int(host.nbytes)},
+            "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
+            "clocks": clk.summary(), "gpu_launches": int(sum(v[1] for v in prof.values()))}
+    print(json.dumps(line))
+    assert ctx.check() == 0
+
+
 def run_batched(args, wl, rank, world, local_rank):
     """Config 4: the batched, graph-captured step vs the plain per-problem
     loop of in-situ steps on the same problems, from the same state."""
@@ -1244,6 +1368,8 @@ def main():
             run_remesh(args, wl, rank, world, local_rank)
         elif hasattr(wl, "c_prev"):
             run_bdf2(args, wl, rank, world, local_rank)
+        elif hasattr(wl, "vcs"):
+            run_tv(args, wl, rank, world, local_rank)
         else:
             run_gpu(args, wl, rank, world, local_rank)
     finally:

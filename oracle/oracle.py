@@ -187,7 +187,8 @@ def interp_cubic_1d(x, xx, pp):
     return h00 * pp[1] + h10 * (xx[2] - xx[1]) * mk + h01 * pp[2] + h11 * (xx[2] - xx[1]) * mk1
 
 
-def semilag_in_situ_tv(vels, con, timestep, dt, nrk=1, periodic=False, times=None, M=None):
+def semilag_in_situ_tv(vels, con, timestep, dt, nrk=1, periodic=False, times=None, M=None,
+                       leaf_end=0):
     """In-situ step through a time-dependent velocity (SolveSemilagInSitu ->
     SolveSemilagRK2 -> ComputeTrajRK2 -> IntegrateRK2, src/tree/tree_semilag.h:
     92-180, src/semilag/semilag.inc:26-80, src/semilag/traj.inc:20-93):
@@ -196,9 +197,11 @@ def semilag_in_situ_tv(vels, con, timestep, dt, nrk=1, periodic=False, times=Non
     stage's time); without, vels = [v_n, v_{n-1}] of the two-functor form
     (v_n at X, FieldExtrapFunctor's 1.5 v_n - 0.5 v_{n-1} at X*,
     tree_extrap_functor.h:47-78).  Each evaluation wraps the point array in
-    place under periodic boundaries (EvalTree's aliasing)."""
+    place under periodic boundaries (EvalTree's aliasing).  With leaf_end,
+    only the first leaf_end leaves' targets (a bounded sample)."""
     q = con["q"]
-    x = collect_grid_points(con["anchor"], con["depth"], q)
+    nl = len(con["depth"]) if leaf_end <= 0 else leaf_end
+    x = collect_grid_points(con["anchor"][:nl], con["depth"][:nl], q)
     tinit = timestep * dt
     tfinal = tinit - dt
     tau = (tfinal - tinit) / nrk
@@ -228,7 +231,7 @@ def semilag_in_situ_tv(vels, con, timestep, dt, nrk=1, periodic=False, times=Non
         x = x + tau * v
         cur = cur + tau
     c = eval_tree(con["anchor"], con["depth"], q, 1, con["coeff"], x, periodic)
-    return set_tree_grid_values(len(con["depth"]), q, 1, c.reshape(-1), M)
+    return set_tree_grid_values(nl, q, 1, c.reshape(-1), M)
 
 
 def semilag_in_situ_dual(vel, vel_d, con, con_d, timestep, dt, nrk=1, periodic=False, M=None):

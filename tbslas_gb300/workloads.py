@@ -115,6 +115,33 @@ class Bdf2Workload:
                         "target; uniform depth-4 octree, q=8, rotation + Gaussian"}
 
 
+class TvWorkload:
+    """The uniform q = 8 configuration advected through a time-dependent
+    velocity: four rotation trees (omega = 2 pi (1 + k / 4) at times k dt),
+    cubic in time (the reference's FieldSetFunctor), one leaf structure -- the
+    blended fused step."""
+
+    def __init__(self, q=8, depth=4, dt=0.01, name="tree_uniform_q8_tv"):
+        self.name, self.q, self.dt, self.bc = name, q, dt, 0
+        self.a, self.d = trees.uniform_tree(depth)
+        self.times = [k * dt for k in range(4)]
+        self.vcs = [trees.fit(fields.rotation(2 * math.pi * (1 + k / 4)), self.a, self.d, q, 3)
+                    for k in range(4)]
+        self.cc = trees.fit(fields.gaussian((0.7, 0.5, 0.5), 0.05), self.a, self.d, q, 1)
+        self.timestep = 2  # steps query t in [times[1], times[2]]
+
+    @property
+    def points_per_step(self):
+        return len(self.d) * (self.q + 1) ** 3
+
+    def describe(self):
+        return {"workload": self.name, "q": self.q, "dt": self.dt, "bc": "freespace",
+                "leaves": int(len(self.d)), "velocity_trees": 4,
+                "departure_points_per_step": int(self.points_per_step),
+                "note": "uniform depth-4 octree, q=8, Gaussian; velocity cubic in time over four "
+                        "rotation trees (FieldSetFunctor), blended per RK2 stage"}
+
+
 class GridWorkload:
     def __init__(self, n, seed=SEED):
         rng = np.random.default_rng(seed)
@@ -266,6 +293,8 @@ def make(name):
         return tree_adaptive_q8_remesh()
     if name == "bdf2_q8":
         return Bdf2Workload()
+    if name == "tree_uniform_q8_tv":
+        return TvWorkload()
     if name == "adjoint_q8":
         return AdjointWorkload()
     if name == "adjoint_q8_d4":
