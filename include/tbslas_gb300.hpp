@@ -10,6 +10,11 @@
 //   tbslas::SetTreeGridValues                src/tree/tree_utils.h:500-552
 //   tbslas::new_nodes / GetPt2CoeffMatrix    src/utils/cheb.h:41-196
 //   tbslas::fast_interp                      src/tree/tree_functor.h:89-153
+//   tbslas::FieldSetFunctor                  src/tree/tree_set_functor.h:28-103
+//   tbslas::FieldExtrapFunctor               src/tree/tree_extrap_functor.h:27-95
+//   the two-functor SolveSemilagInSitu       src/tree/tree_semilag.h:137-180
+//   Tree::RefineTree + Balance21 after a step src/applications/src/advection.cpp:305-311
+//   the BDF2 step of the driver              src/applications/src/advdiff-ss.cpp:485-521
 //
 // Differences a caller sees: errors throw tbslas_gb300::Error (the reference
 // asserts); the boundary condition is an argument, not the SimConfig
@@ -94,6 +99,20 @@ class Tree {
   tbslas_tree get() const { return t_; }
   Context& ctx() const { return *ctx_; }
 
+  // The driver's `tree.RefineTree(); tree.Balance21(bc);` after a step, on the
+  // device (tbslas_tree_remesh: coarsen one level, refine, 2:1 balance by the
+  // Chebyshev tail against tol).  The leaf list changes.
+  void Remesh(double tol, int min_depth, int max_depth, BoundaryType bc) {
+    check(tbslas_tree_remesh(ctx_->get(), t_, tol, min_depth, max_depth, bc, nullptr),
+          "tbslas_tree_remesh");
+    check(tbslas_tree_info(t_, &n_, nullptr, nullptr, nullptr), "tbslas_tree_info");
+  }
+  void Leaves(std::vector<double>& anchor, std::vector<int32_t>& depth) const {
+    anchor.resize(static_cast<size_t>(3 * n_));
+    depth.resize(static_cast<size_t>(n_));
+    check(tbslas_tree_get_leaves(t_, anchor.data(), depth.data()), "tbslas_tree_get_leaves");
+  }
+
  private:
   Context* ctx_;
   tbslas_tree t_ = nullptr;
@@ -161,6 +180,108 @@ void SolveSemilagInSitu(TreeFunc& tvel_func, Tree& tree_curr, const int timestep
                                timestep, dt, num_rk_step, tvel_func.bc(), nullptr),
         "tbslas_semilag_in_situ");
   check(tbslas_ctx_check(tree_curr.ctx().get(), nullptr), "tbslas_ctx_check");
+}
+
+// tbslas::FieldSetFunctor: the velocity cubic in time over four trees at
+// increasing times; update() drops the oldest and appends a tree, as the
+// reference's does.  Used through SolveSemilagInSitu below.
+template <typename real_t, class Tree_t = Tree>
+class FieldSetFunctor {
+ public:
+  FieldSetFunctor(std::vector<Tree_t*> field_set_elems, std::vector<real_t> field_set_times,
+                  BoundaryType bc = FreeSpace)
+      : elems_(field_set_elems), times_(field_set_times), bc_(bc) {
+    if (elems_.size() != 4 || times_.size() != 4)
+      throw std::invalid_argument("FieldSetFunctor: four trees and four times");
+  }
+  void update(Tree_t* new_tree, real_t time) {
+    elems_.erase(elems_.begin());
+    times_.erase(times_.begin());
+    elems_.push_back(new_tree);
+    times_.push_back(time);
+  }
+  const std::vector<Tree_t*>& elems() const { return elems_; }
+  const std::vector<real_t>& times() const { return times_; }
+  BoundaryType bc() const { return bc_; }
+
+ private:
+  std::vector<Tree_t*> elems_;
+  std::vector<real_t> times_;
+  BoundaryType bc_;
+};
+
+// tbslas::FieldExtrapFunctor: 1.5 v_n - 0.5 v_{n-1}; update() shifts in a tree.
+template <typename real_t, class Tree_t = Tree>
+class FieldExtrapFunctor {
+ public:
+  FieldExtrapFunctor(Tree_t* tp, Tree_t* tc, BoundaryType bc = FreeSpace)
+      : tp_(tp), tc_(tc), bc_(bc) {}
+  void update(Tree_t* new_tree, real_t) {
+    tp_ = tc_;
+    tc_ = new_tree;
+  }
+  Tree_t* tp() const { return tp_; }
+  Tree_t* tc() const { return tc_; }
+  BoundaryType bc() const { return bc_; }
+
+ private:
+  Tree_t *tp_, *tc_;
+  BoundaryType bc_;
+};
+
+// SolveSemilagInSitu with a FieldSetFunctor velocity: the cubic's weights at
+// the times IntegrateRK2 queries (tinit and tinit + tau/2 of each sub-step,
+// src/semilag/traj.inc:20-68), one tbslas_semilag_in_situ_tv call.
+template <typename real_t>
+void SolveSemilagInSitu(FieldSetFunctor<real_t, Tree>& f, Tree& tree_curr, const int timestep,
+                        const double dt, int num_rk_step = 1) {
+  std::vector<double> w(static_cast<size_t>(8 * num_rk_step));
+  const double tinit = timestep * dt, tfinal = tinit - dt;
+  const double tau = (tfinal - tinit) / num_rk_step;
+  const double times[4] = {f.times()[0], f.times()[1], f.times()[2], f.times()[3]};
+  double cur = tinit;
+  for (int s = 0; s < num_rk_step; ++s) {
+    check(tbslas_cubic_time_weights(times, cur, &w[8 * s]), "tbslas_cubic_time_weights");
+    check(tbslas_cubic_time_weights(times, cur + 0.5 * tau, &w[8 * s + 4]),
+          "tbslas_cubic_time_weights");
+    cur = cur + tau;
+  }
+  tbslas_tree v[4];
+  for (int k = 0; k < 4; ++k) v[k] = f.elems()[k]->get();
+  check(tbslas_semilag_in_situ_tv(tree_curr.ctx().get(), 4, v, w.data(), tree_curr.get(), timestep,
+                                  dt, num_rk_step, f.bc(), nullptr),
+        "tbslas_semilag_in_situ_tv");
+}
+
+// The two-functor SolveSemilagInSitu: tvel_func at X, tvel_extrap at X*.
+template <typename real_t>
+void SolveSemilagInSitu(NodeFieldFunctor<real_t, Tree>& tvel_func,
+                        FieldExtrapFunctor<real_t, Tree>& tvel_extrap, Tree& tree_curr,
+                        const int timestep, const double dt, int num_rk_step = 1) {
+  tbslas_tree v[3] = {tvel_extrap.tc()->get(), tvel_extrap.tp()->get(), tvel_func.node()->get()};
+  const bool same = tvel_func.node() == tvel_extrap.tc();
+  const int m = same ? 2 : 3;
+  std::vector<double> w;
+  for (int s = 0; s < num_rk_step; ++s) {
+    const double first[3] = {same ? 1.0 : 0.0, 0.0, same ? 0.0 : 1.0};
+    const double second[3] = {1.5, -0.5, 0.0};
+    w.insert(w.end(), first, first + m);
+    w.insert(w.end(), second, second + m);
+  }
+  check(tbslas_semilag_in_situ_tv(tree_curr.ctx().get(), m, v, w.data(), tree_curr.get(), timestep,
+                                  dt, num_rk_step, tvel_extrap.bc(), nullptr),
+        "tbslas_semilag_in_situ_tv");
+}
+
+// The advection-diffusion driver's BDF2 step at its running time tcurr:
+// treen <- fit of 4/3 treec(X1) - 1/3 treep(X2).
+template <typename real_t>
+void SemilagBDF2(NodeFieldFunctor<real_t, Tree>& vel_evaluator, Tree& treep, Tree& treec,
+                 Tree& treen, const double tcurr, const double dt, int num_rk_step = 1) {
+  check(tbslas_semilag_bdf2(treen.ctx().get(), vel_evaluator.node()->get(), treep.get(),
+                            treec.get(), treen.get(), tcurr, dt, num_rk_step, vel_evaluator.bc(),
+                            nullptr),
+        "tbslas_semilag_bdf2");
 }
 
 inline std::vector<double> new_nodes(int deg, int dim = 3) {
