@@ -1006,6 +1006,79 @@ def run_tv(args, wl, rank, world, local_rank):
     assert ctx.check() == 0
 
 
+def run_construct(args, wl, rank, world, local_rank):
+    """ConstructTree on the device (tbslas_tree_construct) for the two trees of
+    the adaptive q=14 configuration (4 Gaussians; Taylor-Green; tol 1e-6,
+    depths 3..8): the trees must equal the host construction the other
+    workloads use; value = Chebyshev nodes of the final trees fitted per
+    second, K constructions timed."""
+    import torch
+    import tbslas_gb300 as tb
+    from oracle import construct as oc
+
+    torch.cuda.set_device(local_rank)
+    ctx = tb.Context(local_rank)
+    tol, lo, hi = wl.construct
+    fc = tb.Field.gaussians(wl.blobs.centres, wl.blobs.sigmas)
+    fv = tb.Field.taylor_green()
+
+    def build():
+        return (tb.construct_tree(ctx, fc, wl.q, tol, lo, hi),
+                tb.construct_tree(ctx, fv, wl.q, tol, lo, hi))
+    tcon, tvel = build()
+    check = {}
+    for name, t, (a, d, c) in (("concentration", tcon, (wl.ca, wl.cd, wl.cc)),
+                               ("velocity", tvel, (wl.va, wl.vd, wl.vc))):
+        ga, gd = t.leaves()
+        same = bool(np.array_equal(ga, a) and np.array_equal(gd, d))
+        check[name] = {"leaves": int(len(gd)), "same_leaves_as_host_construction": same,
+                       "coeff_rel_diff_vs_host_fit": (float(np.abs(t.get_coeffs() - c).max()
+                                                            / np.abs(c).max()) if same else None)}
+        t.close()
+    nodes = (len(wl.cd) + len(wl.vd)) * (wl.q + 1) ** 3
+    for _ in range(args.warmup):
+        for t in build():
+            t.close()
+    torch.cuda.synchronize()
+    sec = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ts = build()
+        torch.cuda.synchronize()
+        sec.append(time.perf_counter() - t0)
+        for t in ts:
+            t.close()
+    ms = 1e3 * float(np.median(sec))
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    oc.construct(fc.kind, fc.n, fc.params, wl.q, tol, lo, hi)
+    oc.construct(fv.kind, fv.n, fv.params, wl.q, tol, lo, hi)
+    cpu_sec = time.perf_counter() - t0
+    from oracle import oracle as ora
+    cfg = {"workload": wl.name, "q": wl.q, "tol": tol, "depths": [lo, hi],
+           "trees": "4 Gaussians (concentration), Taylor-Green (velocity)",
+           "note": "ConstructTree on the device: fit, refine by the Chebyshev tail, "
+                   "2:1 balance, final fit"}
+    line = {"metric": METRIC, "value": nodes / (ms * 1e-3),
+            "unit": "Chebyshev nodes of the final trees fitted per second (tree construction)",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded analytic fields)", "config": cfg,
+            "timing": "wall clock around each synchronous construction of both trees (median "
+                      "of K)",
+            "e2e": {"value": nodes / (ms * 1e-3), "unit": "fitted nodes/s",
+                    "h2d_bytes_per_step": 8 * (fc.params.size + fv.params.size),
+                    "d2h_bytes_per_step": 0},
+            "cpu_baseline": {"value": nodes / cpu_sec, "unit": "fitted nodes/s",
+                             "cores": ora.num_threads(), "kind": "port",
+                             "sample": "the oracle's construction of both trees (numpy, the C "
+                                       "oracle's fit), once: %.2f s" % cpu_sec},
+            "accuracy": check}
+    print(json.dumps(line))
+    assert ctx.check() == 0
+
+
 def run_batched(args, wl, rank, world, local_rank):
     """Config 4: the batched, graph-captured step vs the plain per-problem
     loop of in-situ steps on the same problems, from the same state."""
@@ -1370,6 +1443,8 @@ def main():
             run_bdf2(args, wl, rank, world, local_rank)
         elif hasattr(wl, "vcs"):
             run_tv(args, wl, rank, world, local_rank)
+        elif hasattr(wl, "construct"):
+            run_construct(args, wl, rank, world, local_rank)
         else:
             run_gpu(args, wl, rank, world, local_rank)
     finally:

@@ -146,6 +146,50 @@ int tbslas_tree_set_coeffs_host(tbslas_tree tree, const double* coeff_host);
 int tbslas_tree_get_coeffs_host(tbslas_tree tree, double* coeff_host);
 int tbslas_tree_set_coeffs(tbslas_tree tree, const double* coeff_dev, void* stream);
 int tbslas_tree_get_coeffs(tbslas_tree tree, double* coeff_dev, void* stream);
+/* Analytic input fields for tree construction and fitting (the input
+ * functions of the reference's drivers, src/utils/fields.h).  p: host array
+ * of the kind's parameters (copied by the call).
+ *   GAUSSIANS        dof 1, sum of n terms amp exp(-|x-c|^2 / (2 sigma^2)),
+ *                    p[5i..5i+4] = cx, cy, cz, sigma, amp
+ *   GAUSSIAN_3D      dof 1, get_gaussian_field_3d: xc, yc, zc, A, sx, sy, sz
+ *   EXP_ALPHA        dof 1, get_exp_alpha_field: xc, yc, zc, R, alpha
+ *   ROTATION         dof 3, get_vorticity_field with omega = p[0]
+ *   TAYLOR_GREEN     dof 3, (sin 2pi x cos 2pi y cos 2pi z,
+ *                    -cos 2pi x sin 2pi y cos 2pi z, 0); no parameters
+ *   TAYLOR_GREEN_ABC dof 3, get_taylor_green_field: A, B, C, a, b, c
+ *   HOPF             dof 3, get_hopf_field: xc, yc, zc, A, r
+ *   FOURIER          dof 3, sum of n modes A cos(2pi k.x) + B sin(2pi k.x),
+ *                    p[9i..9i+8] = kx, ky, kz, Ax, Ay, Az, Bx, By, Bz */
+enum {
+  TBSLAS_FIELD_GAUSSIANS = 0,
+  TBSLAS_FIELD_GAUSSIAN_3D = 1,
+  TBSLAS_FIELD_EXP_ALPHA = 2,
+  TBSLAS_FIELD_ROTATION = 3,
+  TBSLAS_FIELD_TAYLOR_GREEN = 4,
+  TBSLAS_FIELD_TAYLOR_GREEN_ABC = 5,
+  TBSLAS_FIELD_HOPF = 6,
+  TBSLAS_FIELD_FOURIER = 7
+};
+typedef struct {
+  int kind;
+  int n;
+  const double* p;
+} tbslas_field;
+/* InitTree (src/tree/tree_utils.h:128-178) on the device: the field at every
+ * leaf's Chebyshev nodes (new_nodes), fitted as SetTreeGridValues does.  The
+ * field's dof must be the tree's. */
+int tbslas_tree_fit_field(tbslas_ctx ctx, tbslas_tree tree, const tbslas_field* field,
+                          void* stream);
+/* ConstructTree (src/tree/tree_utils.h:83-126) on the device: from the
+ * uniform tree of min_depth (<= 6), every leaf whose fit of the field has
+ * tail > tol (sum over dofs of |c| over the total-degree-q coefficients) and
+ * depth < max_depth is split, its children fitted afresh, until none is; then
+ * 2:1 balance (periodic images under TBSLAS_BC_PERIODIC) and the final fit.
+ * The refinement rule is PVFMM's (not vendored); this is the project's
+ * restatement, the one tbslas_tree_remesh applies.  Synchronous. */
+int tbslas_tree_construct(tbslas_ctx ctx, const tbslas_field* field, int q, double tol,
+                          int min_depth, int max_depth, int bc, tbslas_tree* out);
+
 /* The current leaves: anchor_host[L*3], depth_host[L] (L from tbslas_tree_info). */
 int tbslas_tree_get_leaves(tbslas_tree tree, double* anchor_host, int32_t* depth_host);
 

@@ -207,6 +207,12 @@ class Tree:
         call("tbslas_tree_get_leaves", self.handle, a.ctypes.data, d.ctypes.data)
         return a, d
 
+    def fit_field(self, field, stream=None):
+        """InitTree on the device: the analytic field fitted on every leaf."""
+        f = field._c()
+        call("tbslas_tree_fit_field", self.ctx.handle, self.handle, ctypes.byref(f),
+             _stream(stream))
+
     def remesh(self, tol, min_depth, max_depth, bc=0):
         """Adaptive re-meshing on the device (coarsen one level, refine,
         2:1 balance; tbslas_tree_remesh).  Returns {"leaves", "merged",
@@ -219,6 +225,67 @@ class Tree:
         self.anchor, self.depth = self.leaves()
         return {"leaves": int(st[0]), "merged": int(st[1]), "split": int(st[2]),
                 "balanced": int(st[3]), "kernels": int(st[4])}
+
+
+class _CField(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("n", ctypes.c_int),
+                ("p", ctypes.POINTER(ctypes.c_double))]
+
+
+class Field:
+    """An analytic input field evaluated on the device (tbslas_field; the
+    closed forms of the reference's src/utils/fields.h)."""
+    GAUSSIANS, GAUSSIAN_3D, EXP_ALPHA, ROTATION = 0, 1, 2, 3
+    TAYLOR_GREEN, TAYLOR_GREEN_ABC, HOPF, FOURIER = 4, 5, 6, 7
+
+    def __init__(self, kind, params=(), n=0):
+        self.kind, self.n = int(kind), int(n)
+        self.params = np.ascontiguousarray(params, dtype=np.float64).reshape(-1)
+
+    def _c(self):
+        return _CField(self.kind, self.n,
+                       self.params.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+
+    @staticmethod
+    def gaussians(centres, sigmas, amps=None):
+        c = np.asarray(centres, dtype=np.float64).reshape(-1, 3)
+        sg = np.broadcast_to(np.asarray(sigmas, dtype=np.float64), (len(c),))
+        a = np.ones(len(c)) if amps is None else np.broadcast_to(np.asarray(amps, float), (len(c),))
+        return Field(Field.GAUSSIANS, np.column_stack([c, sg, a]), len(c))
+
+    @staticmethod
+    def rotation(omega=1.0):
+        return Field(Field.ROTATION, [omega])
+
+    @staticmethod
+    def taylor_green():
+        return Field(Field.TAYLOR_GREEN)
+
+    @staticmethod
+    def fourier(ks, A, B):
+        ks = np.asarray(ks, dtype=np.float64).reshape(-1, 3)
+        return Field(Field.FOURIER, np.column_stack([ks, np.asarray(A).reshape(-1, 3),
+                                                    np.asarray(B).reshape(-1, 3)]), len(ks))
+
+    @property
+    def dof(self):
+        return 1 if self.kind in (Field.GAUSSIANS, Field.GAUSSIAN_3D, Field.EXP_ALPHA) else 3
+
+
+def construct_tree(ctx, field, q, tol, min_depth, max_depth, bc=FreeSpace):
+    """ConstructTree on the device (tbslas_tree_construct): an adaptive tree
+    of the analytic field, fitted."""
+    h = ctypes.c_void_p()
+    f = field._c()
+    call("tbslas_tree_construct", ctx.handle, ctypes.byref(f), int(q), float(tol), int(min_depth),
+         int(max_depth), int(bc), ctypes.byref(h))
+    t = Tree.__new__(Tree)
+    t.ctx, t.handle, t.q, t.dof = ctx, h, int(q), field.dof
+    L = ctypes.c_int64()
+    call("tbslas_tree_info", h, ctypes.byref(L), None, None, None)
+    t.n_leaves = int(L.value)
+    t.anchor, t.depth = t.leaves()
+    return t
 
 
 class NodeFieldFunctor:

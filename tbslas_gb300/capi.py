@@ -55,6 +55,8 @@ SIGNATURES = {
     "tbslas_semilag_bdf2": [_vp, _vp, _vp, _vp, _vp, _c.c_double, _c.c_double, _i32, _i32, _vp],
     "tbslas_semilag_in_situ_tv": [_vp, _i32, _vp, _vp, _vp, _i32, _c.c_double, _i32, _i32, _vp],
     "tbslas_cubic_time_weights": [_vp, _c.c_double, _vp],
+    "tbslas_tree_fit_field": [_vp, _vp, _vp, _vp],
+    "tbslas_tree_construct": [_vp, _vp, _i32, _c.c_double, _i32, _i32, _i32, _c.POINTER(_vp)],
     "tbslas_collect_grid_points": [_vp, _vp, _vp, _vp],
     "tbslas_eval_tree": [_vp, _vp, _vp, _i64, _vp, _i32, _vp],
     "tbslas_eval_tree_host": [_vp, _vp, _vp, _i64, _vp, _i32],

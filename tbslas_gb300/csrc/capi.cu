@@ -126,6 +126,7 @@ enum Slot {
   kTvC2s,
   kTvN2,
   kTvFlag,
+  kField,
   kNumSlots
 };
 
@@ -833,7 +834,8 @@ TreeView mesh_view(const tbslas_tree t, const MeshState& m, const int32_t* table
 // the restriction of their parent (transfer + FP64 refit), merged parents the
 // rows of merge_c.
 int apply_actions(tbslas_ctx ctx, tbslas_tree t, MeshState& m, const int8_t* act,
-                  const int64_t* aux, const double* merge_c, cudaStream_t s, int64_t* launches) {
+                  const int64_t* aux, const double* merge_c, cudaStream_t s, int64_t* launches,
+                  bool coeffs = true) {
   const int q = t->q, dof = t->dof;
   const int64_t L = m.L, np = n_points(q), stride = t->stride;
   int64_t *nleaf, *nxfer, *pos, *xpos;
@@ -864,6 +866,10 @@ int apply_actions(tbslas_ctx ctx, tbslas_tree t, MeshState& m, const int8_t* act
   launch_rebuild(m.keys, m.geom, act, aux, pos, xpos, L, n.keys, n.geom, src_of, items, s);
   *launches += 1;
   TRY(check_launch("re-meshing leaves"));
+  if (!coeffs) {  // the leaves only (the caller refits them)
+    m = n;
+    return TBSLAS_OK;
+  }
   double* split_c = nullptr;
   if (nx > 0) {
     const double* F = nullptr;
@@ -881,6 +887,86 @@ int apply_actions(tbslas_ctx ctx, tbslas_tree t, MeshState& m, const int8_t* act
   *launches += 1;
   TRY(check_launch("re-meshing coefficients"));
   m = n;
+  return TBSLAS_OK;
+}
+
+// Leaves of a re-meshing or construction into the tree's arrays (grown with
+// headroom when the leaf count outgrows them), the lookup table rebuilt and
+// the derived coefficient arrays refreshed.
+int install_mesh(tbslas_ctx ctx, tbslas_tree t, const MeshState& m, cudaStream_t s,
+                 int64_t* launches_out) {
+  const int dof = t->dof;
+  const int64_t stride = t->stride;
+  int64_t launches = 0;
+  int64_t* sc;
+  TRY(scratch_t(ctx, kRmScalars, 2, &sc));
+  CUDA_TRY(cudaMemsetAsync(sc + 1, 0, sizeof(int64_t), s));
+  launch_max_depth(m.geom, m.L, reinterpret_cast<int*>(sc + 1), s);
+  launches += 1;
+  int64_t md = 0;
+  const int64_t* mdp = sc + 1;
+  TRY(read_scalars(ctx, &mdp, 1, &md, s));
+  const int maxd = (int)(md & 0xffffffff);
+  const int T = std::min(maxd, 7);
+  const int64_t ntab = (1ll << (3 * T)) + 1;
+  if (m.L > t->cap_L) {
+    const int64_t cap = m.L + m.L / 4;
+    uint64_t* k = nullptr;
+    Geom* g = nullptr;
+    double *c = nullptr, *cn = nullptr;
+    float2* c2 = nullptr;
+    if (cudaMalloc(&k, cap * sizeof(uint64_t)) != cudaSuccess ||
+        cudaMalloc(&g, cap * sizeof(Geom)) != cudaSuccess ||
+        cudaMalloc(&c, cap * stride * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c2, cap * stride * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&cn, cap * dof * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(k);
+      cudaFree(g);
+      cudaFree(c);
+      cudaFree(c2);
+      cudaFree(cn);
+      return fail(TBSLAS_ERR_ALLOC, "re-meshing: growing the tree to %lld leaves failed",
+                  (long long)cap);
+    }
+    CUDA_TRY(cudaMemsetAsync(c2, 0, cap * stride * sizeof(float2), s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    cudaFree(t->d_keys);
+    cudaFree(t->d_geom);
+    cudaFree(t->d_coeff);
+    cudaFree(t->d_coeff2);
+    cudaFree(t->d_cnorm);
+    t->d_keys = k;
+    t->d_geom = g;
+    t->d_coeff = c;
+    t->d_coeff2 = c2;
+    t->d_cnorm = cn;
+    t->cap_L = cap;
+  }
+  if (ntab > t->cap_table) {
+    int32_t* tab = nullptr;
+    if (cudaMalloc(&tab, ntab * sizeof(int32_t)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(TBSLAS_ERR_ALLOC, "re-meshing: lookup table allocation failed");
+    }
+    CUDA_TRY(cudaStreamSynchronize(s));
+    cudaFree(t->d_table);
+    t->d_table = tab;
+    t->cap_table = ntab;
+  }
+  CUDA_TRY(cudaMemcpyAsync(t->d_keys, m.keys, m.L * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(t->d_geom, m.geom, m.L * sizeof(Geom), cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(t->d_coeff, m.coeff, m.L * stride * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s));
+  t->L = m.L;
+  t->max_depth = maxd;
+  t->T = T;
+  launch_build_table(t->d_keys, t->L, T, t->d_table, s);
+  launches += 3;  // the table, then the split and norms of derived_coeffs
+  TRY(check_launch("lookup table"));
+  TRY(derived_coeffs(t, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  *launches_out += launches;
   return TBSLAS_OK;
 }
 
@@ -979,73 +1065,7 @@ int tree_remesh(tbslas_ctx ctx, tbslas_tree t, double tol, int min_depth, int ma
     balanced += n;
     TRY(apply_actions(ctx, t, m, act, nullptr, nullptr, s, &launches));
   }
-  // install into the tree's arrays (grown when the leaf count outgrows them)
-  CUDA_TRY(cudaMemsetAsync(sc + 1, 0, sizeof(int64_t), s));
-  launch_max_depth(m.geom, m.L, reinterpret_cast<int*>(sc + 1), s);
-  launches += 1;
-  int64_t md = 0;
-  const int64_t* mdp = sc + 1;
-  TRY(read_scalars(ctx, &mdp, 1, &md, s));
-  const int maxd = (int)(md & 0xffffffff);
-  const int T = std::min(maxd, 7);
-  const int64_t ntab = (1ll << (3 * T)) + 1;
-  if (m.L > t->cap_L) {
-    const int64_t cap = m.L + m.L / 4;
-    uint64_t* k = nullptr;
-    Geom* g = nullptr;
-    double *c = nullptr, *cn = nullptr;
-    float2* c2 = nullptr;
-    if (cudaMalloc(&k, cap * sizeof(uint64_t)) != cudaSuccess ||
-        cudaMalloc(&g, cap * sizeof(Geom)) != cudaSuccess ||
-        cudaMalloc(&c, cap * stride * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&c2, cap * stride * sizeof(float2)) != cudaSuccess ||
-        cudaMalloc(&cn, cap * dof * sizeof(double)) != cudaSuccess) {
-      cudaGetLastError();
-      cudaFree(k);
-      cudaFree(g);
-      cudaFree(c);
-      cudaFree(c2);
-      cudaFree(cn);
-      return fail(TBSLAS_ERR_ALLOC, "re-meshing: growing the tree to %lld leaves failed",
-                  (long long)cap);
-    }
-    CUDA_TRY(cudaMemsetAsync(c2, 0, cap * stride * sizeof(float2), s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    cudaFree(t->d_keys);
-    cudaFree(t->d_geom);
-    cudaFree(t->d_coeff);
-    cudaFree(t->d_coeff2);
-    cudaFree(t->d_cnorm);
-    t->d_keys = k;
-    t->d_geom = g;
-    t->d_coeff = c;
-    t->d_coeff2 = c2;
-    t->d_cnorm = cn;
-    t->cap_L = cap;
-  }
-  if (ntab > t->cap_table) {
-    int32_t* tab = nullptr;
-    if (cudaMalloc(&tab, ntab * sizeof(int32_t)) != cudaSuccess) {
-      cudaGetLastError();
-      return fail(TBSLAS_ERR_ALLOC, "re-meshing: lookup table allocation failed");
-    }
-    CUDA_TRY(cudaStreamSynchronize(s));
-    cudaFree(t->d_table);
-    t->d_table = tab;
-    t->cap_table = ntab;
-  }
-  CUDA_TRY(cudaMemcpyAsync(t->d_keys, m.keys, m.L * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
-  CUDA_TRY(cudaMemcpyAsync(t->d_geom, m.geom, m.L * sizeof(Geom), cudaMemcpyDeviceToDevice, s));
-  CUDA_TRY(cudaMemcpyAsync(t->d_coeff, m.coeff, m.L * stride * sizeof(double),
-                           cudaMemcpyDeviceToDevice, s));
-  t->L = m.L;
-  t->max_depth = maxd;
-  t->T = T;
-  launch_build_table(t->d_keys, t->L, T, t->d_table, s);
-  launches += 3;  // the table, then the split and norms of derived_coeffs
-  TRY(check_launch("lookup table"));
-  TRY(derived_coeffs(t, s));
-  CUDA_TRY(cudaStreamSynchronize(s));
+  TRY(install_mesh(ctx, t, m, s, &launches));
   if (stats) {
     stats[0] = t->L;
     stats[1] = merged;
@@ -1054,6 +1074,129 @@ int tree_remesh(tbslas_ctx ctx, tbslas_tree t, double tol, int min_depth, int ma
     stats[4] = launches;
   }
   return TBSLAS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Analytic input fields (construct.cu) for the device tree construction.
+int field_dof(int kind) {
+  switch (kind) {
+    case TBSLAS_FIELD_GAUSSIANS:
+    case TBSLAS_FIELD_GAUSSIAN_3D:
+    case TBSLAS_FIELD_EXP_ALPHA:
+      return 1;
+    case TBSLAS_FIELD_ROTATION:
+    case TBSLAS_FIELD_TAYLOR_GREEN:
+    case TBSLAS_FIELD_TAYLOR_GREEN_ABC:
+    case TBSLAS_FIELD_HOPF:
+    case TBSLAS_FIELD_FOURIER:
+      return 3;
+    default:
+      return 0;
+  }
+}
+
+int64_t field_params(const tbslas_field& f) {
+  switch (f.kind) {
+    case TBSLAS_FIELD_GAUSSIANS: return 5ll * f.n;
+    case TBSLAS_FIELD_GAUSSIAN_3D: return 7;
+    case TBSLAS_FIELD_EXP_ALPHA: return 5;
+    case TBSLAS_FIELD_ROTATION: return 1;
+    case TBSLAS_FIELD_TAYLOR_GREEN: return 0;
+    case TBSLAS_FIELD_TAYLOR_GREEN_ABC: return 6;
+    case TBSLAS_FIELD_HOPF: return 5;
+    case TBSLAS_FIELD_FOURIER: return 9ll * f.n;
+    default: return -1;
+  }
+}
+
+// Validates a field and copies its parameters to the device.
+int upload_field(tbslas_ctx ctx, const tbslas_field* f, const double** dev, cudaStream_t s) {
+  if (!f) return fail(TBSLAS_ERR_INVALID_ARG, "null field");
+  if (field_dof(f->kind) == 0) return fail(TBSLAS_ERR_INVALID_ARG, "field kind %d", f->kind);
+  if ((f->kind == TBSLAS_FIELD_GAUSSIANS || f->kind == TBSLAS_FIELD_FOURIER) &&
+      (f->n < 1 || f->n > (1 << 20)))
+    return fail(TBSLAS_ERR_INVALID_ARG, "field terms %d", f->n);
+  const int64_t np = field_params(*f);
+  if (np > 0 && !f->p) return fail(TBSLAS_ERR_INVALID_ARG, "null field parameters");
+  for (int64_t i = 0; i < np; ++i)
+    if (!std::isfinite(f->p[i])) return fail(TBSLAS_ERR_INVALID_ARG, "field parameter %lld",
+                                             (long long)i);
+  double* d;
+  TRY(scratch_t(ctx, kField, np > 0 ? np : 1, &d));
+  if (np > 0) CUDA_TRY(cudaMemcpyAsync(d, f->p, np * sizeof(double), cudaMemcpyHostToDevice, s));
+  *dev = d;
+  return TBSLAS_OK;
+}
+
+// Field values at the leaves' nodes, FP64 fit into coeff (SetTreeGridValues).
+int fit_field_on(tbslas_ctx ctx, const tbslas_field* f, const double* prm, const Geom* geom,
+                 int64_t L, int q, int dof, int64_t stride, double* coeff, cudaStream_t s) {
+  const double* F = nullptr;
+  TRY(device_F(ctx, q, &F));
+  double* vals;
+  TRY(scratch_t(ctx, kRmVals, L * dof * n_points(q), &vals));
+  launch_field_values(f->kind, f->n, prm, geom, L, nodes_1d(q), q, dof, vals, s);
+  launch_refit(vals, F, q, L * dof, dof, stride, coeff, nullptr, ctx->d_err, false, s);
+  return check_launch("field fit");
+}
+
+// ConstructTree (src/tree/tree_utils.h:83-126) on the device: the uniform
+// tree of min_depth; while a leaf's fit has tail > tol below max_depth,
+// split it (the children are fitted afresh); 2:1 balance; the final fit.
+int tree_construct(tbslas_ctx ctx, tbslas_tree t, const tbslas_field* f, const double* prm,
+                   double tol, int min_depth, int max_depth, int bc, cudaStream_t s) {
+  const int q = t->q, dof = t->dof;
+  const int64_t stride = t->stride;
+  int64_t launches = 0;
+  MeshState m;
+  m.L = 1ll << (3 * min_depth);
+  TRY(scratch_t(ctx, kMeshKeys[0], m.L, &m.keys));
+  TRY(scratch_t(ctx, kMeshGeom[0], m.L, &m.geom));
+  launch_uniform_leaves(min_depth, m.keys, m.geom, s);
+  TRY(check_launch("uniform leaves"));
+  int64_t* sc;
+  TRY(scratch_t(ctx, kRmScalars, 2, &sc));
+  for (int it = 0; it <= TBSLAS_MAX_DEPTH + 1; ++it) {
+    TRY(scratch_t(ctx, kMeshCoeff[m.set], m.L * stride, &m.coeff));
+    CUDA_TRY(cudaMemsetAsync(m.coeff, 0, m.L * stride * sizeof(double), s));  // row padding
+    TRY(fit_field_on(ctx, f, prm, m.geom, m.L, q, dof, stride, m.coeff, s));
+    double* tail;
+    int8_t* act;
+    TRY(scratch_t(ctx, kRmTail, m.L, &tail));
+    TRY(scratch_t(ctx, kRmAct, m.L, &act));
+    CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(int64_t), s));
+    launch_leaf_tails(m.coeff, m.L, dof, q, stride, tail, s);
+    launch_split_actions(tail, m.geom, m.L, tol, max_depth, act,
+                         reinterpret_cast<unsigned long long*>(sc), s);
+    TRY(check_launch("refinement flags"));
+    int64_t n = 0;
+    TRY(read_scalars(ctx, &sc, 1, &n, s));
+    if (n == 0) break;
+    TRY(apply_actions(ctx, t, m, act, nullptr, nullptr, s, &launches, false));
+  }
+  bool split = false;
+  for (int it = 0; it <= TBSLAS_MAX_DEPTH; ++it) {
+    int32_t* table;
+    int8_t* act;
+    TRY(scratch_t(ctx, kRmTable, (1ll << 21) + 1, &table));
+    TRY(scratch_t(ctx, kRmAct, m.L, &act));
+    launch_build_table(m.keys, m.L, 7, table, s);
+    CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(int64_t), s));
+    launch_balance_flags(mesh_view(t, m, table, 7), bc, act,
+                         reinterpret_cast<unsigned long long*>(sc), s);
+    TRY(check_launch("balance flags"));
+    int64_t n = 0;
+    TRY(read_scalars(ctx, &sc, 1, &n, s));
+    if (n == 0) break;
+    split = true;
+    TRY(apply_actions(ctx, t, m, act, nullptr, nullptr, s, &launches, false));
+  }
+  if (split) {  // the final leaves' fit
+    TRY(scratch_t(ctx, kMeshCoeff[m.set], m.L * stride, &m.coeff));
+    CUDA_TRY(cudaMemsetAsync(m.coeff, 0, m.L * stride * sizeof(double), s));
+    TRY(fit_field_on(ctx, f, prm, m.geom, m.L, q, dof, stride, m.coeff, s));
+  }
+  return install_mesh(ctx, t, m, s, &launches);
 }
 
 template <class T>
@@ -1392,6 +1535,55 @@ int tbslas_tree_remesh(tbslas_ctx ctx, tbslas_tree tree, double tol, int min_dep
                 max_depth, TBSLAS_MAX_DEPTH);
   if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
   return tree_remesh(ctx, tree, tol, min_depth, max_depth, bc, stats);
+}
+
+int tbslas_tree_fit_field(tbslas_ctx ctx, tbslas_tree tree, const tbslas_field* field,
+                          void* stream) {
+  TRY(check_tree(tree));
+  TRY(bind(ctx));
+  if (tree->ctx != ctx) return fail(TBSLAS_ERR_INVALID_ARG, "tree belongs to another context");
+  cudaStream_t s = (cudaStream_t)stream;
+  const double* prm = nullptr;
+  TRY(upload_field(ctx, field, &prm, s));
+  if (field_dof(field->kind) != tree->dof)
+    return fail(TBSLAS_ERR_INVALID_ARG, "field has dof %d, the tree %d", field_dof(field->kind),
+                tree->dof);
+  TRY(fit_field_on(ctx, field, prm, tree->d_geom, tree->L, tree->q, tree->dof, tree->stride,
+                   tree->d_coeff, s));
+  return derived_coeffs(tree, s);
+}
+
+int tbslas_tree_construct(tbslas_ctx ctx, const tbslas_field* field, int q, double tol,
+                          int min_depth, int max_depth, int bc, tbslas_tree* out) {
+  if (!out) return fail(TBSLAS_ERR_INVALID_ARG, "null output pointer");
+  *out = nullptr;
+  TRY(bind(ctx));
+  if (q < 1 || q > TBSLAS_MAX_DEGREE)
+    return fail(TBSLAS_ERR_UNSUPPORTED, "Chebyshev degree %d outside [1,%d]", q,
+                TBSLAS_MAX_DEGREE);
+  if (!(tol >= 0.0)) return fail(TBSLAS_ERR_INVALID_ARG, "tolerance %g", tol);
+  if (min_depth < 0 || min_depth > 6 || max_depth < min_depth || max_depth > TBSLAS_MAX_DEPTH)
+    return fail(TBSLAS_ERR_INVALID_ARG, "depth range [%d, %d] (min_depth <= 6, max_depth <= %d)",
+                min_depth, max_depth, TBSLAS_MAX_DEPTH);
+  if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
+  cudaStream_t s = ctx->stream;
+  CUDA_TRY(cudaDeviceSynchronize());
+  const double* prm = nullptr;
+  TRY(upload_field(ctx, field, &prm, s));
+  tbslas_tree t = new tbslas_tree_s();
+  t->ctx = ctx;
+  t->q = q;
+  t->dof = field_dof(field->kind);
+  t->stride = (t->dof * n_coeff(q) + 1) & ~(int64_t)1;
+  int st = tree_construct(ctx, t, field, prm, tol, min_depth, max_depth, bc, s);
+  if (st != TBSLAS_OK) {
+    std::string msg = g_err;
+    tbslas_tree_destroy(t);
+    g_err = msg;
+    return st;
+  }
+  *out = t;
+  return TBSLAS_OK;
 }
 
 int tbslas_tree_get_leaves(tbslas_tree t, double* anchor_host, int32_t* depth_host) {

@@ -275,6 +275,11 @@ void launch_balance_flags(const TreeView& t, int periodic, int8_t* act, unsigned
                           cudaStream_t s);
 void launch_build_table(const uint64_t* keys, int64_t L, int T, int32_t* table, cudaStream_t s);
 void launch_max_depth(const Geom* geom, int64_t L, int* out, cudaStream_t s);
+// Analytic fields (construct.cu): out[(leaf * dof + l) * Np + p] at the
+// leaves' nodes; the 8^d leaves of the uniform depth-d tree.
+void launch_field_values(int kind, int n, const double* prm, const Geom* geom, int64_t L,
+                         const Nodes1D& nodes, int q, int dof, double* out, cudaStream_t s);
+void launch_uniform_leaves(int d, uint64_t* keys, Geom* geom, cudaStream_t s);
 
 // misc kernels (capi.cu)
 void launch_collect(const TreeView& t, const Nodes1D& nodes, double* out, cudaStream_t s);

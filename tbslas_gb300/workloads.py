@@ -59,9 +59,11 @@ def tree_adaptive_q14(seed=SEED):
     vc = trees.fit(fields.taylor_green(), va, vd, q, 3, M)
     finest = int(max(cd.max(), vd.max()))
     dt = 1.0 / (2.0 ** finest * q * q)
-    return TreeWorkload("tree_adaptive_q14", (va, vd, vc), (ca, cd, cc), q, dt, 0,
-                        "adaptive octrees (tol 1e-6, depth 3..8), q=14, Taylor-Green + 4 "
-                        "Gaussians, CFL=1 on the finest leaf")
+    wl = TreeWorkload("tree_adaptive_q14", (va, vd, vc), (ca, cd, cc), q, dt, 0,
+                      "adaptive octrees (tol 1e-6, depth 3..8), q=14, Taylor-Green + 4 "
+                      "Gaussians, CFL=1 on the finest leaf")
+    wl.blobs = blobs
+    return wl
 
 
 def tree_adaptive_q8_remesh():
@@ -295,6 +297,11 @@ def make(name):
         return Bdf2Workload()
     if name == "tree_uniform_q8_tv":
         return TvWorkload()
+    if name == "construct_q14":
+        wl = tree_adaptive_q14()
+        wl.name = "construct_q14"
+        wl.construct = (1e-6, 3, 8)
+        return wl
     if name == "adjoint_q8":
         return AdjointWorkload()
     if name == "adjoint_q8_d4":
