@@ -99,23 +99,33 @@ __global__ void __launch_bounds__(128, 6) k_semilag_bdf2_df(const Bdf2Args a) {
                  g.z + h * a.nodes.x[p / (D * D)]};
   const bool per = a.periodic != 0;
   double px[3], m0[3] = {0.0, 0.0, 0.0}, mp[3] = {0.0, 0.0, 0.0};
-  // first stage from the node grid (exact), then the rest of the backtrace
+  // first stage from the node grid (exact)
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     if (per) x[k] = wrap1(x[k]);
     px[k] = fma(0.5 * a.tau1, __ldg(a.vn + 3 * t + k), x[k]);
   }
-  bool amb = rk2_df_stages<D>(a.vel, x, px, m0, mp, 1, a.nrk, a.tau1, per, slots);
-  double cn[1], cp[1], e[1];
-  amb |= eval_point_df<D, 1, false>(a.cur, x[0], x[1], x[2], per, m0, cn, e, slots);
-  // second backtrace from X1 (wrapped in place by the evaluation)
+  // the two backtraces share one copy of the stage loop and of the
+  // evaluation (the instruction caches hold one): pass 0 continues from the
+  // midpoint and evaluates c_n at X1, pass 1 starts from X1 (wrapped in place
+  // by that evaluation) and evaluates c_{n-1} at X2
+  bool amb = false;
+  double cv[2], e[1];
+#pragma unroll 1
+  for (int pass = 0; pass < 2; ++pass) {
+    amb |= rk2_df_stages<D>(a.vel, x, px, m0, mp, pass == 0 ? 1 : 0, a.nrk,
+                            pass == 0 ? a.tau1 : a.tau2, per, slots);
+    double c[1];
+    amb |= eval_point_df<D, 1, false>(pass == 0 ? a.cur : a.prev, x[0], x[1], x[2], per, m0, c,
+                                      e, slots);
+    cv[pass] = c[0];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    px[k] = x[k];
-    mp[k] = m0[k];
+    for (int k = 0; k < 3; ++k) {
+      px[k] = x[k];
+      mp[k] = m0[k];
+    }
   }
-  amb |= rk2_df_stages<D>(a.vel, x, px, m0, mp, 0, a.nrk, a.tau2, per, slots);
-  amb |= eval_point_df<D, 1, false>(a.prev, x[0], x[1], x[2], per, m0, cp, e, slots);
+  const double cn[1] = {cv[0]}, cp[1] = {cv[1]};
   a.vals[t] = bdf2_combine(cn[0], cp[0]);
   if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = t;
 }
