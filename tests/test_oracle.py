@@ -241,3 +241,20 @@ def test_bdf2_translation_exact(ora):
     got = ora.eval_tree(a, d, q, 1, out, pts)
     ref = at(t)(pts)
     assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max()
+
+
+def test_cubic_time_weights_match_interp_cubic(ora):
+    """tbslas_cubic_time_weights (host) against the oracle's restatement of
+    CubicInterpPolicy::InterpCubic1D (src/utils/cubic.h:42-56): the
+    interpolant is linear in the four values."""
+    import tbslas_gb300 as tb
+    rng = np.random.default_rng(9)
+    for _ in range(20):
+        times = np.sort(rng.uniform(0, 1, 4)) + np.arange(4) * 0.1
+        t = rng.uniform(times[0], times[3])
+        w = tb.cubic_time_weights(times, t)
+        p = rng.standard_normal(4)
+        ref = ora.interp_cubic_1d(t, times, p)
+        assert abs(w @ p - ref) <= 1e-14 * max(1.0, abs(ref))
+    w = tb.cubic_time_weights([0.0, 1.0, 2.0, 3.0], 1.5)
+    assert np.allclose(w, [-0.0625, 0.5625, 0.5625, -0.0625], rtol=0, atol=1e-16)
