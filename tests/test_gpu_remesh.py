@@ -111,3 +111,20 @@ def test_step_after_remesh_matches_oracle(ctx, ora):
     assert np.abs(got - ref2).max() <= 1e-12 * np.abs(ref2).max()
     tv.close()
     tc.close()
+
+
+def test_remesh_velocity_tree_matches_oracle(ctx):
+    """A dof-3 tree (the driver also re-meshes its velocity tree after each
+    step): the tail sums over the three components."""
+    q, tol = 5, 2e-3
+    a, d = trees.adaptive_tree(fields.gaussian((0.5, 0.5, 0.5), 0.1), q, 1, 1e-3, 1, 3)
+    vfn = fields.fourier_velocity(np.random.default_rng(8), 2)
+    c = trees.fit(lambda p: 0.3 * vfn(p), a, d, q, 3)
+    from oracle import remesh as rm
+    t = tb.Tree(ctx, a, d, q, 3, c)
+    t.remesh(tol, 1, 4, tb.Periodic)
+    ga, gd = t.leaves()
+    ra, rd, rc = rm.remesh(a, d, q, c, tol, 1, 4, True)
+    assert np.array_equal(gd, rd) and np.array_equal(ga, ra)
+    assert np.abs(t.get_coeffs() - rc).max() <= 1e-12 * np.abs(rc).max()
+    t.close()
