@@ -374,7 +374,9 @@ int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
  * TBSLAS_SUMS_DOUBLE_FLOAT sums, which the batch always uses), bit for bit.  No
  * single-call counterpart in the reference (a driver loops over
  * SolveSemilagInSitu, src/tree/tree_semilag.h:92-135).  The batch keeps
- * pointers to the trees: they must outlive it and keep their shapes. */
+ * pointers to the trees: they must outlive it and keep their shapes (running
+ * or tuning a batch whose tree was re-meshed since it was built returns
+ * TBSLAS_ERR_INVALID_ARG). */
 int tbslas_batch_create(tbslas_ctx ctx, int n_problems, const tbslas_tree* vel,
                         const tbslas_tree* con, const double* dt, int nrk, int bc,
                         tbslas_batch* out);

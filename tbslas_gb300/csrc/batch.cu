@@ -36,6 +36,8 @@ struct tbslas_batch_s {
   int device = 0, num_sms = 0;
   int n = 0, nrk = 1, bc = 0;
   std::vector<BatchProblem> h_probs;
+  std::vector<tbslas_tree> trees;   // every velocity and concentration tree
+  std::vector<uint64_t> tree_gen;   // their generations when the batch was built
   std::vector<double*> con_coeff;
   std::vector<float2*> con_coeff2;
   std::vector<int64_t> con_coeff_n;
@@ -227,6 +229,10 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     st = tree_view(vel[i], &p.vel, &cv);
     if (st == TBSLAS_OK) st = tree_view(con[i], &p.con, &cc);
     if (st != TBSLAS_OK) break;
+    for (tbslas_tree tr : {vel[i], con[i]}) {
+      b->trees.push_back(tr);
+      b->tree_gen.push_back(tree_generation(tr));
+    }
     if (cv != ctx || cc != ctx) {
       st = fail_status(TBSLAS_ERR_INVALID_ARG, "batch trees belong to another context");
       break;
@@ -385,9 +391,21 @@ int tbslas_batch_get_params(tbslas_batch b, int* block, int* targets_per_item, i
   return TBSLAS_OK;
 }
 
+// The batch holds its trees' device arrays: a tree re-meshed since the batch
+// was built invalidates it.
+static int check_generations(const tbslas_batch b) {
+  for (size_t i = 0; i < b->trees.size(); ++i)
+    if (tree_generation(b->trees[i]) != b->tree_gen[i])
+      return fail_status(TBSLAS_ERR_INVALID_ARG,
+                         "a tree of the batch was re-meshed after the batch was built; "
+                         "rebuild the batch");
+  return TBSLAS_OK;
+}
+
 int tbslas_batch_run(tbslas_batch b, int timestep0, int nsteps, int use_graph, void* stream) {
   if (!b) return fail_status(TBSLAS_ERR_INVALID_ARG, "null batch");
   if (nsteps < 0) return fail_status(TBSLAS_ERR_INVALID_ARG, "negative step count");
+  if (check_generations(b) != TBSLAS_OK) return TBSLAS_ERR_INVALID_ARG;
   if (nsteps == 0) return TBSLAS_OK;
   BCUDA(cudaSetDevice(b->device));
   return run(b, timestep0, nsteps, use_graph != 0, (cudaStream_t)stream);
@@ -395,6 +413,7 @@ int tbslas_batch_run(tbslas_batch b, int timestep0, int nsteps, int use_graph, v
 
 int tbslas_batch_autotune(tbslas_batch b, int* block, int* targets_per_item, int* ctas_per_sm) {
   if (!b) return fail_status(TBSLAS_ERR_INVALID_ARG, "null batch");
+  if (check_generations(b) != TBSLAS_OK) return TBSLAS_ERR_INVALID_ARG;
   BCUDA(cudaSetDevice(b->device));
   BCUDA(cudaDeviceSynchronize());
   // Save every concentration tree: each trial step overwrites them.

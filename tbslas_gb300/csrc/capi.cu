@@ -183,6 +183,7 @@ struct tbslas_tree_s {
   int32_t* d_table = nullptr;
   int64_t cap_L = 0;      // leaves the per-leaf arrays hold (>= L after a re-meshing)
   int64_t cap_table = 0;  // entries d_table holds
+  uint64_t generation = 0;  // bumped whenever the leaf list changes (re-meshing)
 
   TreeView view() const {
     TreeView v;
@@ -961,6 +962,7 @@ int install_mesh(tbslas_ctx ctx, tbslas_tree t, const MeshState& m, cudaStream_t
   t->L = m.L;
   t->max_depth = maxd;
   t->T = T;
+  ++t->generation;
   launch_build_table(t->d_keys, t->L, T, t->d_table, s);
   launches += 3;  // the table, then the split and norms of derived_coeffs
   TRY(check_launch("lookup table"));
@@ -1278,6 +1280,8 @@ int tree_view(tbslas_tree t, TreeView* v, tbslas_ctx* ctx) {
   *ctx = t->ctx;
   return TBSLAS_OK;
 }
+
+uint64_t tree_generation(tbslas_tree t) { return t ? t->generation : 0; }
 
 int tree_coeff2(tbslas_tree t, float2** coeff2) {
   if (!t || !t->ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null tree");

@@ -147,6 +147,9 @@ int fail_status(int code, const char* msg);
 int tree_view(tbslas_tree t, TreeView* v, tbslas_ctx* ctx);
 int tree_coeff(tbslas_tree t, double** coeff, int64_t* n_doubles);
 int tree_coeff2(tbslas_tree t, float2** coeff2);
+// Changes whenever the tree's leaf list (and with it its device arrays) is
+// rebuilt, e.g. by tbslas_tree_remesh.
+uint64_t tree_generation(tbslas_tree t);
 int ctx_info(tbslas_ctx ctx, int* device, int* num_sms);
 int ctx_F(tbslas_ctx ctx, int q, const double** F);
 int ctx_mu_scratch(tbslas_ctx ctx, size_t n, double** out);

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import tbslas_gb300 as tb
-from tbslas_gb300 import capi, trees, workloads
+from tbslas_gb300 import capi, fields, trees, workloads
 
 pytestmark = pytest.mark.gpu
 
@@ -73,3 +73,23 @@ def test_batch_rejects_mixed_degrees(ctx):
     assert e.value.status == 4
     with pytest.raises(capi.TbslasError):
         tb.Batch(ctx, [(tv, tv, 0.01)])
+
+
+def test_batch_refuses_a_remeshed_tree(ctx):
+    """The batch holds its trees' device arrays; after one of its trees is
+    re-meshed, running it is refused until it is rebuilt."""
+    import math
+    a, d = trees.uniform_tree(2)
+    q = 4
+    v = trees.fit(fields.rotation(2 * math.pi), a, d, q, 3)
+    c = trees.fit(fields.gaussian((0.6, 0.5, 0.45), 0.1), a, d, q, 1)
+    tv, tc = tb.Tree(ctx, a, d, q, 3, v), tb.Tree(ctx, a, d, q, 1, c)
+    b = tb.Batch(ctx, [(tv, tc, 0.01)], 1, tb.FreeSpace)
+    b.run(1, 1, False)
+    tc.remesh(1e-3, 1, 3)
+    with pytest.raises(tb.capi.TbslasError):
+        b.run(2, 1, False)
+    b.close()
+    b = tb.Batch(ctx, [(tv, tc, 0.01)], 1, tb.FreeSpace)
+    b.run(2, 1, False)
+    b.close()
