@@ -313,8 +313,12 @@ int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con
  *    trees {v_n, v_{n-1}}, w = {1, 0, 1.5, -0.5} per sub-step.
  * Trees of one leaf structure with nrk = 1 run the fused step on the
  * per-stage blends of their coefficients (the context's sum mode); otherwise
- * every tree is evaluated at every stage point in FP64.  Velocity trees share
- * the concentration's degree; the concentration has dof 1. */
+ * every tree is evaluated at every stage point in FP64.  Blending
+ * coefficients equals blending values up to rounding (~1e-16); where a
+ * blended velocity component vanishes at a point on a leaf face or the
+ * domain's boundary, that rounding can put the point on the other side than
+ * the reference's value blend does.  Velocity trees share the
+ * concentration's degree; the concentration has dof 1. */
 int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, const double* w,
                               tbslas_tree con, int timestep, double dt, int nrk, int bc,
                               void* stream);
