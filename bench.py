@@ -1080,8 +1080,9 @@ def run_construct(args, wl, rank, world, local_rank):
 
 
 def run_batched(args, wl, rank, world, local_rank):
-    """Config 4: the batched, graph-captured step vs the plain per-problem
-    loop of in-situ steps on the same problems, from the same state."""
+    """The batched, graph-captured step of 64 uneven problems vs the plain
+    per-problem loop of in-situ steps on the same problems, from the same
+    state."""
     import torch
     import tbslas_gb300 as tb
 
@@ -1174,8 +1175,8 @@ def run_batched(args, wl, rank, world, local_rank):
 
 
 def run_adjoint(args, wl, rank, world, local_rank):
-    """Config 5: forward (plain and checkpointed) and adjoint passes of the
-    T-step advection, timed; gradients checked by central differences."""
+    """The differentiable T-step advection: forward (plain and checkpointed)
+    and adjoint passes, timed; gradients checked by central differences."""
     import torch
     import tbslas_gb300 as tb
     from tbslas_gb300 import adjoint
