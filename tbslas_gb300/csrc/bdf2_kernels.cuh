@@ -81,11 +81,13 @@ __device__ __forceinline__ bool rk2_df_stages(const TreeView& vel, double (&x)[3
 }
 
 // Double-float sums, FP64 coordinates and lookups (as k_semilag_tree_df);
-// targets whose lookup the bounds make ambiguous go to the FP64 pass.  Six
-// CTAs per SM (<= 80 registers): the second backtrace keeps more state live
-// than the single one.
+// targets whose lookup the bounds make ambiguous go to the FP64 pass.  Eight
+// (degree <= 9) or seven CTAs per SM, as the single-backtrace kernel: with
+// the two backtraces in one loop the register cap costs a few spills but the
+// extra warps hide the coefficient loads (q = 8 on GB300: six CTAs 5.47 ms,
+// seven 5.21 ms, eight 5.02 ms per step).
 template <int D>
-__global__ void __launch_bounds__(128, 6) k_semilag_bdf2_df(const Bdf2Args a) {
+__global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_bdf2_df(const Bdf2Args a) {
   constexpr int NP = D * D * D;
   extern __shared__ float2 s_slots[];
   const ThreadSlots slots{s_slots + threadIdx.x, (int)blockDim.x};
