@@ -670,6 +670,7 @@ def run_remesh(args, wl, rank, world, local_rank):
     for i in range(args.warmup):
         flush.fill_(float(i))
         advance(tc, i + 1)
+    barrier(world)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -723,6 +724,8 @@ def run_remesh(args, wl, rank, world, local_rank):
     torch.cuda.synchronize()
     e2e_sec = time.perf_counter() - t0
     tc3.close()
+    tot_points, tot_sec = aggregate(points, ms * 1e-3, world)
+    e_points, e2e_sec = aggregate(e_points, e2e_sec, world)
     if rank != 0:
         return
 
@@ -770,7 +773,7 @@ def run_remesh(args, wl, rank, world, local_rank):
                 "l2": "flushed between timed steps (256 MiB write inside the timed loop)",
                 "parallelism": "replicas x%d" % world, "nrk": 1,
                 "departure_points_per_step": "varies with the leaf count"})
-    line = {"metric": METRIC, "value": points / (ms * 1e-3), "unit": UNIT + " (step + re-mesh)",
+    line = {"metric": METRIC, "value": tot_points / tot_sec, "unit": UNIT + " (step + re-mesh)",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded analytic fields)",
@@ -844,6 +847,7 @@ def run_bdf2(args, wl, rank, world, local_rank):
     for i in range(args.warmup):
         flush.fill_(float(i))
         step(i + 1)
+    barrier(world)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -877,6 +881,8 @@ def run_bdf2(args, wl, rank, world, local_rank):
     torch.cuda.synchronize()
     e2e_sec = time.perf_counter() - t0
     points = wl.points_per_step * args.steps
+    e_points, e2e_sec = aggregate(points, e2e_sec, world)
+    tot_points, tot_sec = aggregate(points, ms * 1e-3, world)
     if rank != 0:
         return
     cpu, ref, k = cpu_baseline_bdf2(wl)
@@ -902,14 +908,14 @@ def run_bdf2(args, wl, rank, world, local_rank):
     cfg = wl.describe()
     cfg.update({"l2": "flushed between timed steps (256 MiB write inside the timed loop)",
                 "parallelism": "replicas x%d" % world, "nrk": 1})
-    line = {"metric": METRIC, "value": points / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+    line = {"metric": METRIC, "value": tot_points / tot_sec, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded analytic fields)", "config": cfg,
-            "e2e": {"value": points / e2e_sec, "unit": UNIT,
+            "e2e": {"value": e_points / e2e_sec, "unit": UNIT,
                     "h2d_bytes_per_step": int(hp.nbytes + hc.nbytes),
                     "d2h_bytes_per_step": int(hn.nbytes)},
-            "targets_per_s": points / 2 / (ms * 1e-3),
+            "targets_per_s": tot_points / 2 / tot_sec,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
             "clocks": clk.summary(), "gpu_launches": int(sum(v[1] for v in prof.values()))}
     print(json.dumps(line))
@@ -965,6 +971,7 @@ def run_tv(args, wl, rank, world, local_rank):
     for i in range(args.warmup):
         flush.fill_(float(i))
         step(i + 1)
+    barrier(world)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -994,6 +1001,8 @@ def run_tv(args, wl, rank, world, local_rank):
     torch.cuda.synchronize()
     e2e_sec = time.perf_counter() - t0
     points = wl.points_per_step * args.steps
+    e_points, e2e_sec = aggregate(points, e2e_sec, world)
+    tot_points, tot_sec = aggregate(points, ms * 1e-3, world)
     if rank != 0:
         return
     cpu, ref, k = cpu_baseline_tv(wl)
@@ -1019,11 +1028,11 @@ def run_tv(args, wl, rank, world, local_rank):
     cfg = wl.describe()
     cfg.update({"l2": "flushed between timed steps (256 MiB write inside the timed loop)",
                 "parallelism": "replicas x%d" % world, "nrk": 1})
-    line = {"metric": METRIC, "value": points / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+    line = {"metric": METRIC, "value": tot_points / tot_sec, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded analytic fields)", "config": cfg,
-            "e2e": {"value": points / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(host.nbytes),
+            "e2e": {"value": e_points / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(host.nbytes),
                     "d2h_bytes_per_step": int(host.nbytes)},
             "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
             "clocks": clk.summary(), "gpu_launches": int(sum(v[1] for v in prof.values()))}
@@ -1074,6 +1083,7 @@ def run_construct(args, wl, rank, world, local_rank):
         for t in ts:
             t.close()
     ms = 1e3 * float(np.median(sec))
+    tot_nodes, tot_sec = aggregate(nodes, ms * 1e-3, world)
     if rank != 0:
         return
     t0 = time.perf_counter()
@@ -1085,14 +1095,14 @@ def run_construct(args, wl, rank, world, local_rank):
            "trees": "4 Gaussians (concentration), Taylor-Green (velocity)",
            "note": "ConstructTree on the device: fit, refine by the Chebyshev tail, "
                    "2:1 balance, final fit"}
-    line = {"metric": METRIC, "value": nodes / (ms * 1e-3),
+    line = {"metric": METRIC, "value": tot_nodes / tot_sec,
             "unit": "Chebyshev nodes of the final trees fitted per second (tree construction)",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded analytic fields)", "config": cfg,
             "timing": "wall clock around each synchronous construction of both trees (median "
                       "of K)",
-            "e2e": {"value": nodes / (ms * 1e-3), "unit": "fitted nodes/s",
+            "e2e": {"value": tot_nodes / tot_sec, "unit": "fitted nodes/s",
                     "h2d_bytes_per_step": 8 * (fc.params.size + fv.params.size),
                     "d2h_bytes_per_step": 0},
             "cpu_baseline": {"value": nodes / cpu_sec, "unit": "fitted nodes/s",
