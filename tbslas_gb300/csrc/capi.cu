@@ -910,26 +910,34 @@ int install_mesh(tbslas_ctx ctx, tbslas_tree t, const MeshState& m, cudaStream_t
   const int maxd = (int)(md & 0xffffffff);
   const int T = std::min(maxd, 7);
   const int64_t ntab = (1ll << (3 * T)) + 1;
-  if (m.L > t->cap_L) {
-    const int64_t cap = m.L + m.L / 4;
-    uint64_t* k = nullptr;
-    Geom* g = nullptr;
-    double *c = nullptr, *cn = nullptr;
-    float2* c2 = nullptr;
-    if (cudaMalloc(&k, cap * sizeof(uint64_t)) != cudaSuccess ||
-        cudaMalloc(&g, cap * sizeof(Geom)) != cudaSuccess ||
-        cudaMalloc(&c, cap * stride * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&c2, cap * stride * sizeof(float2)) != cudaSuccess ||
-        cudaMalloc(&cn, cap * dof * sizeof(double)) != cudaSuccess) {
-      cudaGetLastError();
-      cudaFree(k);
-      cudaFree(g);
-      cudaFree(c);
-      cudaFree(c2);
-      cudaFree(cn);
-      return fail(TBSLAS_ERR_ALLOC, "re-meshing: growing the tree to %lld leaves failed",
-                  (long long)cap);
-    }
+  // allocate everything that has to grow before touching the tree, so a
+  // failed allocation leaves it as it was
+  const bool grow = m.L > t->cap_L, grow_tab = ntab > t->cap_table;
+  const int64_t cap = grow ? m.L + m.L / 4 : t->cap_L;
+  uint64_t* k = nullptr;
+  Geom* g = nullptr;
+  double *c = nullptr, *cn = nullptr;
+  float2* c2 = nullptr;
+  int32_t* tab = nullptr;
+  bool ok = true;
+  if (grow)
+    ok = cudaMalloc(&k, cap * sizeof(uint64_t)) == cudaSuccess &&
+         cudaMalloc(&g, cap * sizeof(Geom)) == cudaSuccess &&
+         cudaMalloc(&c, cap * stride * sizeof(double)) == cudaSuccess &&
+         cudaMalloc(&c2, cap * stride * sizeof(float2)) == cudaSuccess &&
+         cudaMalloc(&cn, cap * dof * sizeof(double)) == cudaSuccess;
+  if (ok && grow_tab) ok = cudaMalloc(&tab, ntab * sizeof(int32_t)) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    cudaFree(k);
+    cudaFree(g);
+    cudaFree(c);
+    cudaFree(c2);
+    cudaFree(cn);
+    cudaFree(tab);
+    return fail(TBSLAS_ERR_ALLOC, "growing the tree to %lld leaves failed", (long long)cap);
+  }
+  if (grow) {
     CUDA_TRY(cudaMemsetAsync(c2, 0, cap * stride * sizeof(float2), s));
     CUDA_TRY(cudaStreamSynchronize(s));
     cudaFree(t->d_keys);
@@ -944,12 +952,7 @@ int install_mesh(tbslas_ctx ctx, tbslas_tree t, const MeshState& m, cudaStream_t
     t->d_cnorm = cn;
     t->cap_L = cap;
   }
-  if (ntab > t->cap_table) {
-    int32_t* tab = nullptr;
-    if (cudaMalloc(&tab, ntab * sizeof(int32_t)) != cudaSuccess) {
-      cudaGetLastError();
-      return fail(TBSLAS_ERR_ALLOC, "re-meshing: lookup table allocation failed");
-    }
+  if (grow_tab) {
     CUDA_TRY(cudaStreamSynchronize(s));
     cudaFree(t->d_table);
     t->d_table = tab;
