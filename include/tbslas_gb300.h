@@ -311,9 +311,10 @@ int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con
  *    current field as the first-stage functor (the two-functor
  *    SolveSemilagInSitu, src/tree/tree_semilag.h:137-180, traj.inc:71-93):
  *    trees {v_n, v_{n-1}}, w = {1, 0, 1.5, -0.5} per sub-step.
- * Trees of one leaf structure with nrk = 1 run the fused step on the
- * per-stage blends of their coefficients (the context's sum mode); otherwise
- * every tree is evaluated at every stage point in FP64.  Blending
+ * Trees of one leaf structure with nrk = 1 run, in the double-float mode,
+ * the fused step on the per-stage blends of their coefficients; otherwise
+ * (and always in TBSLAS_SUMS_FP64) every tree is evaluated at every stage
+ * point in FP64 and the values blended.  Blending
  * coefficients equals blending values up to rounding (~1e-16); where a
  * blended velocity component vanishes at a point on a leaf face or the
  * domain's boundary, that rounding can put the point on the other side than

@@ -1853,9 +1853,10 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
     if (!std::isfinite(w[j])) return fail(TBSLAS_ERR_INVALID_ARG, "weight %d is not finite", j);
   cudaStream_t s = (cudaStream_t)stream;
   const double tau = sl_tau(timestep, dt, nrk);
-  // one leaf structure (and nrk = 1): blend the coefficients per stage and run
-  // the fused step
-  bool same = nrk == 1;
+  // one leaf structure, nrk = 1 and the double-float mode: blend the
+  // coefficients per stage and run the fused step (the FP64 mode evaluates
+  // every tree and blends the values, as the reference's functors do)
+  bool same = nrk == 1 && ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT;
   for (int k = 1; k < m && same; ++k) same = vel[k]->L == vel[0]->L;
   if (same && m > 1) {
     int* flag;
