@@ -83,31 +83,6 @@ struct GlobalLoadDF {
   }
 };
 
-// sum_i tz_i sum_{j<D-i} ty_j sum_{k<D-i-j} c[i][j][k] tx_k in double-float,
-// same nesting as tri_sum.
-template <int D, class Load>
-__device__ __forceinline__ df tri_sum_df(Load c, const df (&tx)[D], const df (&ty)[D],
-                                         const df (&tz)[D]) {
-  df u{0.f, 0.f};
-  int idx = 0;
-#pragma unroll
-  for (int i = 0; i < D; ++i) {
-    df v{0.f, 0.f};
-#pragma unroll
-    for (int j = 0; j < D - i; ++j) {
-      df w{0.f, 0.f};
-#pragma unroll
-      for (int k = 0; k < D - i - j; ++k) {
-        df_fma_acc(w, c(idx), tx[k]);
-        ++idx;
-      }
-      df_fma_acc(v, ty[j], df_norm(w));
-    }
-    df_fma_acc(u, tz[i], df_norm(v));
-  }
-  return df_norm(u);
-}
-
 // One thread's array in shared memory: element k at s[k * bs] (bs = the
 // block size), so a warp's accesses to one element are conflict-free.
 struct ThreadSlots {

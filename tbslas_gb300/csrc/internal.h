@@ -284,8 +284,6 @@ void launch_field_values(int kind, int n, const double* prm, const Geom* geom, i
                          const Nodes1D& nodes, int q, int dof, double* out, cudaStream_t s);
 void launch_uniform_leaves(int d, uint64_t* keys, Geom* geom, cudaStream_t s);
 
-// misc kernels (capi.cu)
-void launch_collect(const TreeView& t, const Nodes1D& nodes, double* out, cudaStream_t s);
 
 // grid.cu
 void launch_fast_interp(const double* grid, int dof, int nreg, const double* pts, int64_t n,
