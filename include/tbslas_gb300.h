@@ -351,8 +351,9 @@ int tbslas_semilag_bdf2(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con_prev,
  * tree of the same degree. */
 /* tbslas_semilag_in_situ with nrk = 1 (same kernels, same result, the
  * context's sum mode) that also stores, per target node (leaf-major, node
- * order of CollectChebTreeGridPoints), the RK2 midpoint xmid_dev[N*3] and
- * departure point xdep_dev[N*3], N = L (q+1)^3.  In the double-float mode the
+ * order of CollectChebTreeGridPoints), the RK2 midpoint xmid_dev[N*3] (or
+ * NULL: departure points only, 24 B per target) and departure point
+ * xdep_dev[N*3], N = L (q+1)^3.  In the double-float mode the
  * points lie in the FP64 step's leaves (targets near a face are recomputed in
  * FP64) and within ~1e-15 of its points. */
 int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
@@ -361,8 +362,10 @@ int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con
 /* Adjoint of step `timestep`: con_coeff_k_dev [L][Nc] = the concentration
  * coefficients the step started from; lambda_next_dev [L][Nc] = dJ/dC^{k+1};
  * writes lambda_k_dev [L][Nc] = dJ/dC^k and ADDS the step's dJ/dV to
- * grad_vel_dev [Lv][3][Nc].  xmid/xdep: the step's checkpoints, or both NULL
- * to recompute them.  Velocity coefficients are read from `vel`. */
+ * grad_vel_dev [Lv][3][Nc].  xmid/xdep: the step's checkpoints; xmid NULL
+ * with xdep given rebuilds the midpoints from the node-grid velocity (the
+ * forward's own arithmetic); both NULL recompute the points.  Velocity
+ * coefficients are read from `vel`. */
 int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
                            const double* con_coeff_k_dev, int timestep, double dt, int bc,
                            const double* lambda_next_dev, double* lambda_k_dev,

@@ -14,7 +14,9 @@ concentration and velocity Chebyshev coefficients); the result is the
 concentration coefficients after nsteps in-situ SL steps (nrk = 1).  Backward
 gives dJ/dc0 and dJ/dvcoeff.  checkpoint=True stores every step's RK2
 midpoints and departure points (48 bytes per node per step); False
-recomputes them in the backward pass.
+recomputes them in the backward pass; checkpoint="departure" stores the
+departure points only (24 bytes per node per step) and rebuilds the
+midpoints from the node-grid velocity in the backward pass.
 """
 import numpy as np
 
@@ -70,8 +72,8 @@ def _function():
             for k in range(nsteps):
                 states.append(con_tree.get_coeffs(torch.empty_like(c0)))
                 if checkpoint:
-                    xm = torch.empty((n, 3), dtype=torch.float64, device=c0.device)
-                    xd = torch.empty_like(xm)
+                    xd = torch.empty((n, 3), dtype=torch.float64, device=c0.device)
+                    xm = None if checkpoint == "departure" else torch.empty_like(xd)
                     step_ckpt(vf, con_tree, timestep0 + k, dt, xm, xd)
                     ckpts.append((xm, xd))
                 else:
@@ -108,5 +110,7 @@ def advect(c0, vcoeff, vel_tree, con_tree, dt, timestep0=1, nsteps=1, bc=api.Fre
     global _FN
     if _FN is None:
         _FN = _function()
+    if checkpoint not in (True, False, "departure"):
+        raise ValueError("checkpoint must be True, False or 'departure'")
     return _FN.apply(c0, vcoeff, vel_tree, con_tree, float(dt), int(timestep0), int(nsteps),
-                     int(bc), bool(checkpoint))
+                     int(bc), checkpoint)

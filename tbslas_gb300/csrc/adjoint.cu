@@ -66,7 +66,7 @@ extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbsl
   TreeView tv, tc;
   int st = check_pair(ctx, vel, con, dt, bc, &tv, &tc);
   if (st != TBSLAS_OK) return st;
-  if (!xmid_dev || !xdep_dev) return fail_status(TBSLAS_ERR_INVALID_ARG, "null checkpoint buffer");
+  if (!xdep_dev) return fail_status(TBSLAS_ERR_INVALID_ARG, "null departure-point buffer");
   return semilag_in_situ_points(ctx, vel, con, timestep, dt, bc, xmid_dev, xdep_dev,
                                 (cudaStream_t)stream);
 }
@@ -81,8 +81,8 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   if (st != TBSLAS_OK) return st;
   if (!con_coeff_k_dev || !lambda_next_dev || !lambda_k_dev || !grad_vel_dev)
     return fail_status(TBSLAS_ERR_INVALID_ARG, "null buffer");
-  if ((xmid_dev == nullptr) != (xdep_dev == nullptr))
-    return fail_status(TBSLAS_ERR_INVALID_ARG, "give both checkpoint buffers or neither");
+  if (xmid_dev && !xdep_dev)
+    return fail_status(TBSLAS_ERR_INVALID_ARG, "midpoints without departure points");
   const int q = tc.q, d = q + 1;
   const int64_t np = (int64_t)d * d * d, nc = (int64_t)d * (d + 1) * (d + 2) / 6;
   double* mu = nullptr;
@@ -126,7 +126,7 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
     if (st != TBSLAS_OK) return st;
     st = ctx_wnode_scratch(ctx, tc.L * np * 3, &a.wnode);
     if (st != TBSLAS_OK) return st;
-    if (!xmid_dev) {
+    if (!xdep_dev) {
       // recompute: the step's points by its double-float kernels (FP64 for
       // the ambiguous targets)
       double *xm = nullptr, *xd = nullptr;
@@ -134,6 +134,13 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
       if (st != TBSLAS_OK) return st;
       a.xmid = xm;
       a.xdep = xd;
+    } else if (!xmid_dev) {
+      // departure points checkpointed: the midpoints from the node-grid
+      // velocity, exactly as the forward formed them
+      double* xm = nullptr;
+      st = step_midpoints(ctx, vel, con, timestep, dt, bc, &xm, s);
+      if (st != TBSLAS_OK) return st;
+      a.xmid = xm;
     }
     {
       ProfBracket pb(ctx, "adjoint_split", s);

@@ -1925,8 +1925,24 @@ int semilag_in_situ_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int
   if (vel->q != con->q || vel->dof != 3 || con->dof != 1)
     return fail(TBSLAS_ERR_UNSUPPORTED, "points of the step need a dof-3 velocity and a dof-1 "
                                         "concentration tree of one degree");
-  if (!xmid || !xdep) return fail(TBSLAS_ERR_INVALID_ARG, "null point buffer");
+  if (!xdep) return fail(TBSLAS_ERR_INVALID_ARG, "null departure-point buffer");
   return semilag_in_situ_dev(ctx, vel, con, timestep, dt, 1, bc, s, xmid, xdep);
+}
+
+int step_midpoints(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
+                   int bc, double** xmid, cudaStream_t s) {
+  TRY(check_step_args(ctx, vel, con, dt, 1, bc));
+  const int q = con->q;
+  const int64_t N = con->L * n_points(q);
+  double* vn = nullptr;
+  TRY(scratch_t(ctx, kVN, N * 3, &vn));
+  TRY(scratch_t(ctx, kXA, N * 3, xmid));
+  {
+    ProfScope pv(ctx, "adjoint_vel_at_nodes", s, 3);
+    launch_eval_on_nodes(vel->view(), con->view(), bc, vn, s);
+    launch_midpoints(con->view(), nodes_1d(q), q, sl_tau(timestep, dt, 1), bc, vn, *xmid, s);
+  }
+  return check_launch("midpoints");
 }
 
 ProfBracket::ProfBracket(tbslas_ctx ctx, const char* name, cudaStream_t s, int kernels)

@@ -109,7 +109,37 @@ __global__ void k_uniform_leaves(int d, uint64_t* __restrict__ keys, Geom* __res
                  ldexp(2.0, d)};
 }
 
+// Midpoints of the in-situ step's first RK2 stage from the node-grid velocity:
+// the arithmetic of rk2_backtrace_from_node (X wrapped in place, then one
+// fused multiply-add per axis).
+__global__ void k_midpoints(const TreeView con, const Nodes1D nodes, int D, double tau,
+                            int periodic, const double* __restrict__ vn,
+                            double* __restrict__ xmid) {
+  const int64_t NP = (int64_t)D * D * D;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= con.L * NP) return;
+  const int64_t leaf = t / NP;
+  const int p = (int)(t - leaf * NP);
+  const Geom g = con.geom[leaf];
+  const double h = 2.0 / g.w;
+  double X[3] = {g.x + h * nodes.x[p % D], g.y + h * nodes.x[(p / D) % D],
+                 g.z + h * nodes.x[p / (D * D)]};
+  const double half_tau = 0.5 * tau;
+  for (int k = 0; k < 3; ++k) {
+    if (periodic) X[k] = wrap1(X[k]);
+    xmid[3 * t + k] = fma(half_tau, vn[3 * t + k], X[k]);
+  }
+}
+
 }  // namespace
+
+void launch_midpoints(const TreeView& con, const Nodes1D& nodes, int q, double tau, int periodic,
+                      const double* vn, double* xmid, cudaStream_t s) {
+  const int64_t N = con.L * (int64_t)(q + 1) * (q + 1) * (q + 1);
+  if (N > 0)
+    k_midpoints<<<(unsigned)((N + 127) / 128), 128, 0, s>>>(con, nodes, q + 1, tau, periodic, vn,
+                                                            xmid);
+}
 
 void launch_field_values(int kind, int n, const double* prm, const Geom* geom, int64_t L,
                          const Nodes1D& nodes, int q, int dof, double* out, cudaStream_t s) {

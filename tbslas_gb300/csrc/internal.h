@@ -176,6 +176,13 @@ class ProfBracket {
   int kernels_;
   cudaEvent_t start_ = nullptr;
 };
+// The midpoints of that step, X + tau/2 v(X) with v(X) from the node grid
+// (the forward's own arithmetic), into scratch of the context ([Lc * Np][3]).
+int step_midpoints(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
+                   int bc, double** xmid, cudaStream_t s);
+// xmid[t] = (X_t wrapped under periodic boundaries) + tau/2 vn[t] (construct.cu)
+void launch_midpoints(const TreeView& con, const Nodes1D& nodes, int q, double tau, int periodic,
+                      const double* vn, double* xmid, cudaStream_t s);
 // The midpoints and departure points of that step only, into scratch of the
 // context (*xmid, *xdep: [Lc * Np][3]), for the double-float adjoint's
 // recompute: the double-float step's kernels, FP64 for ambiguous targets.
