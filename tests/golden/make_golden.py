@@ -44,7 +44,7 @@ def main():
     out["grid_vel"], out["grid_con"] = gv, gc
     out["grid_out"] = ora.semilag_grid(gv, gc, 16, 1.0 / 16, 1, True)
     # re-meshing of the step's result
-    ra, rd, rc = rm.remesh(a, d, q, out["step_out"], 1e-4, 1, 3)
+    ra, rd, rc = rm.remesh(a, d, q, out["step_out"], 1e-3, 1, 3)
     out["remesh_anchor"], out["remesh_depth"], out["remesh_coeff"] = ra, rd, rc
     # BDF2 step (c_{n-1} = the initial field, c_n = the step's result)
     cur = dict(anchor=a, depth=d, q=q, dof=1, coeff=out["step_out"])
@@ -53,14 +53,18 @@ def main():
     # in time, periodic (no velocity component vanishes on a face, where the
     # coefficient blend of the fast path and the reference's value blend could
     # round to different sides)
+    a1, d1 = trees.uniform_tree(1)
     vcs = []
     for k in range(4):
         fn = fields.fourier_velocity(np.random.default_rng(40 + k), 2)
-        vcs.append(trees.fit(lambda p, fn=fn: 0.5 * fn(p), a, d, q, 3))
+        vcs.append(trees.fit(lambda p, fn=fn: 0.5 * fn(p), a1, d1, q, 3))
+    c1 = trees.fit(fields.gaussian((0.55, 0.5, 0.45), 0.12), a1, d1, q, 1)
+    out["tv_anchor"], out["tv_depth"], out["tv_cc"] = a1, d1, c1
     out["tv_vcs"] = np.stack(vcs)
-    out["tv_out"] = ora.semilag_in_situ_tv([dict(anchor=a, depth=d, q=q, dof=3, coeff=v)
-                                            for v in vcs], con, 2, 0.01, 1, True,
-                                           times=[0.0, 0.01, 0.02, 0.03])
+    out["tv_out"] = ora.semilag_in_situ_tv([dict(anchor=a1, depth=d1, q=q, dof=3, coeff=v)
+                                            for v in vcs],
+                                           dict(anchor=a1, depth=d1, q=q, dof=1, coeff=c1), 2,
+                                           0.01, 1, True, times=[0.0, 0.01, 0.02, 0.03])
     np.savez_compressed(os.path.join(HERE, "path_q6.npz"), **out)
 
 

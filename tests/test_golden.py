@@ -30,7 +30,7 @@ def test_oracle_reproduces_the_fixtures(ora, g):
     assert np.abs(tr - g["traj_out"]).max() <= 1e-15
     assert _rel(ora.semilag_grid(g["grid_vel"], g["grid_con"], 16, 1.0 / 16, 1, True),
                 g["grid_out"]) <= 1e-14
-    ra, rd, rc = rm.remesh(a, d, q, g["step_out"], 1e-4, 1, 3)
+    ra, rd, rc = rm.remesh(a, d, q, g["step_out"], 1e-3, 1, 3)
     assert np.array_equal(rd, g["remesh_depth"]) and np.array_equal(ra, g["remesh_anchor"])
     assert _rel(rc, g["remesh_coeff"]) <= 1e-14
 
@@ -54,7 +54,7 @@ def test_device_matches_the_fixtures(ctx, g):
     assert _rel(np.asarray(out).reshape(-1), g["grid_out"].reshape(-1)) <= 1e-12
     # re-meshing of the step's result
     tr = tb.Tree(ctx, a, d, q, 1, g["step_out"])
-    tr.remesh(1e-4, 1, 3)
+    tr.remesh(1e-3, 1, 3)
     ra, rd = tr.leaves()
     assert np.array_equal(rd, g["remesh_depth"]) and np.array_equal(ra, g["remesh_anchor"])
     assert _rel(tr.get_coeffs(), g["remesh_coeff"]) <= 1e-12
@@ -65,8 +65,9 @@ def test_device_matches_the_fixtures(ctx, g):
     tb.solve_semilag_bdf2(vf, tp, tcur, tn, 0.02, 0.01)
     assert _rel(tn.get_coeffs(), g["bdf2_out"]) <= 1e-12
     # time-dependent velocity, cubic in time over four trees
-    vts = [tb.Tree(ctx, a, d, q, 3, v) for v in g["tv_vcs"]]
-    t2 = tb.Tree(ctx, a, d, q, 1, g["step_cc"])
+    a1, d1 = g["tv_anchor"], g["tv_depth"]
+    vts = [tb.Tree(ctx, a1, d1, q, 3, v) for v in g["tv_vcs"]]
+    t2 = tb.Tree(ctx, a1, d1, q, 1, g["tv_cc"])
     tb.solve_semilag_in_situ_tv(tb.FieldSetFunctor(vts, [0.0, 0.01, 0.02, 0.03], tb.Periodic),
                                 t2, 2, 0.01)
     assert _rel(t2.get_coeffs(), g["tv_out"]) <= 1e-12
