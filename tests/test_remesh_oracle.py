@@ -104,3 +104,43 @@ def test_balance_across_the_periodic_boundary(ora):
     assert d2.size == d.size
     a3, d3, _ = rm.remesh(a, d, q, c, np.inf, 5, 5, True)
     assert d3.size > d.size and _balanced(rm, a3, d3, True)
+
+
+def test_construct_oracle_properties(ora):
+    """The construction oracle: a field the degree-q basis represents (a
+    Gaussian of huge width is smooth, a rotation is linear) needs no
+    refinement; a sharp Gaussian is refined near its centre only, the result
+    2:1 balanced and its fit equal to InitTree's on the final leaves."""
+    from oracle import construct as oc
+    from oracle import remesh as rm
+    a, d, c = oc.construct(3, 0, [1.0], 4, 1e-10, 1, 4)  # rotation, linear
+    assert len(d) == 8 and (d == 1).all()
+    f = (0, 1, [0.3, 0.6, 0.5, 0.05, 1.0])  # one sharp Gaussian
+    a, d, c = oc.construct(*f, 5, 1e-4, 1, 4)
+    assert d.max() == 4 and d.min() <= 2
+    assert not rm.balance_flags(a, d, False).any()
+    assert np.array_equal(c, oc.fit(*f, a, d, 5))
+    deep = a[d == 4] + 0.5 ** 4 / 2
+    assert (np.linalg.norm(deep - [0.3, 0.6, 0.5], axis=1) < 0.4).all()
+
+
+def test_functor_stage_weights():
+    """FieldSetFunctor / FieldExtrapFunctor produce IntegrateRK2's stage
+    weights: the cubic's at tinit and tinit + tau/2 of each sub-step, and
+    (v_n, 1.5 v_n - 0.5 v_{n-1})."""
+    import tbslas_gb300 as tb
+    times = [0.0, 0.1, 0.2, 0.3]
+    f = tb.FieldSetFunctor([None] * 4, times)
+    _, w = f.stage_weights(2, 0.1, 1)
+    assert np.allclose(w[:4], tb.cubic_time_weights(times, 0.2), atol=0)
+    assert np.allclose(w[4:], tb.cubic_time_weights(times, 0.15), atol=0)
+    _, w2 = f.stage_weights(2, 0.1, 2)
+    assert len(w2) == 16
+    assert np.allclose(w2[12:], tb.cubic_time_weights(times, 0.2 - 0.05 - 0.025), atol=1e-15)
+    f.update("new", 0.4)
+    assert f.times == [0.1, 0.2, 0.3, 0.4] and f.trees[-1] == "new"
+    e = tb.FieldExtrapFunctor("p", "c")
+    trees_, w3 = e.stage_weights(1, 0.1, 2)
+    assert trees_ == ["c", "p"] and list(w3) == [1.0, 0.0, 1.5, -0.5] * 2
+    e.update("n")
+    assert (e.tp, e.tc) == ("c", "n")
