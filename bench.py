@@ -1074,14 +1074,19 @@ def run_construct(args, wl, rank, world, local_rank):
         for t in build():
             t.close()
     torch.cuda.synchronize()
+    ctx.profile(True)
+    ctx.profile_reset()
     sec = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        ts = build()
-        torch.cuda.synchronize()
-        sec.append(time.perf_counter() - t0)
-        for t in ts:
-            t.close()
+    with ClockSampler(local_rank) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            ts = build()
+            torch.cuda.synchronize()
+            sec.append(time.perf_counter() - t0)
+            for t in ts:
+                t.close()
+    prof = ctx.profile_totals()
+    ctx.profile(False)
     ms = 1e3 * float(np.median(sec))
     tot_nodes, tot_sec = aggregate(nodes, ms * 1e-3, world)
     if rank != 0:
@@ -1109,7 +1114,8 @@ def run_construct(args, wl, rank, world, local_rank):
                              "cores": ora.num_threads(), "kind": "port",
                              "sample": "the oracle's construction of both trees (numpy, the C "
                                        "oracle's fit), once: %.2f s" % cpu_sec},
-            "accuracy": check}
+            "accuracy": check, "clocks": clk.summary(),
+            "gpu_launches": int(prof.get("construct", (0, 0, 0.0))[1])}
     print(json.dumps(line))
     assert ctx.check() == 0
 

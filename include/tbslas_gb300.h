@@ -186,7 +186,9 @@ int tbslas_tree_fit_field(tbslas_ctx ctx, tbslas_tree tree, const tbslas_field* 
  * depth < max_depth is split, its children fitted afresh, until none is; then
  * 2:1 balance (periodic images under TBSLAS_BC_PERIODIC) and the final fit.
  * The refinement rule is PVFMM's (not vendored); this is the project's
- * restatement, the one tbslas_tree_remesh applies.  Synchronous. */
+ * restatement, the one tbslas_tree_remesh applies.  Synchronous.  With
+ * profiling on, the whole construction is one launch group "construct" that
+ * counts every kernel it launched. */
 int tbslas_tree_construct(tbslas_ctx ctx, const tbslas_field* field, int q, double tol,
                           int min_depth, int max_depth, int bc, tbslas_tree* out);
 

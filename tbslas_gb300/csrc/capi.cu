@@ -1148,8 +1148,10 @@ int fit_field_on(tbslas_ctx ctx, const tbslas_field* f, const double* prm, const
 // ConstructTree (src/tree/tree_utils.h:83-126) on the device: the uniform
 // tree of min_depth; while a leaf's fit has tail > tol below max_depth,
 // split it (the children are fitted afresh); 2:1 balance; the final fit.
+// *launches_out gets the number of kernels launched.
 int tree_construct(tbslas_ctx ctx, tbslas_tree t, const tbslas_field* f, const double* prm,
-                   double tol, int min_depth, int max_depth, int bc, cudaStream_t s) {
+                   double tol, int min_depth, int max_depth, int bc, cudaStream_t s,
+                   int64_t* launches_out) {
   const int q = t->q, dof = t->dof;
   const int64_t stride = t->stride;
   int64_t launches = 0;
@@ -1158,6 +1160,7 @@ int tree_construct(tbslas_ctx ctx, tbslas_tree t, const tbslas_field* f, const d
   TRY(scratch_t(ctx, kMeshKeys[0], m.L, &m.keys));
   TRY(scratch_t(ctx, kMeshGeom[0], m.L, &m.geom));
   launch_uniform_leaves(min_depth, m.keys, m.geom, s);
+  launches += 1;
   TRY(check_launch("uniform leaves"));
   int64_t* sc;
   TRY(scratch_t(ctx, kRmScalars, 2, &sc));
@@ -1173,6 +1176,7 @@ int tree_construct(tbslas_ctx ctx, tbslas_tree t, const tbslas_field* f, const d
     launch_leaf_tails(m.coeff, m.L, dof, q, stride, tail, s);
     launch_split_actions(tail, m.geom, m.L, tol, max_depth, act,
                          reinterpret_cast<unsigned long long*>(sc), s);
+    launches += 4;  // field values, refit, tails, flags
     TRY(check_launch("refinement flags"));
     int64_t n = 0;
     TRY(read_scalars(ctx, &sc, 1, &n, s));
@@ -1189,6 +1193,7 @@ int tree_construct(tbslas_ctx ctx, tbslas_tree t, const tbslas_field* f, const d
     CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(int64_t), s));
     launch_balance_flags(mesh_view(t, m, table, 7), bc, act,
                          reinterpret_cast<unsigned long long*>(sc), s);
+    launches += 2;
     TRY(check_launch("balance flags"));
     int64_t n = 0;
     TRY(read_scalars(ctx, &sc, 1, &n, s));
@@ -1200,8 +1205,11 @@ int tree_construct(tbslas_ctx ctx, tbslas_tree t, const tbslas_field* f, const d
     TRY(scratch_t(ctx, kMeshCoeff[m.set], m.L * stride, &m.coeff));
     CUDA_TRY(cudaMemsetAsync(m.coeff, 0, m.L * stride * sizeof(double), s));
     TRY(fit_field_on(ctx, f, prm, m.geom, m.L, q, dof, stride, m.coeff, s));
+    launches += 2;
   }
-  return install_mesh(ctx, t, m, s, &launches);
+  TRY(install_mesh(ctx, t, m, s, &launches));
+  *launches_out = launches;
+  return TBSLAS_OK;
 }
 
 template <class T>
@@ -1582,7 +1590,10 @@ int tbslas_tree_construct(tbslas_ctx ctx, const tbslas_field* field, int q, doub
   t->q = q;
   t->dof = field_dof(field->kind);
   t->stride = (t->dof * n_coeff(q) + 1) & ~(int64_t)1;
-  int st = tree_construct(ctx, t, field, prm, tol, min_depth, max_depth, bc, s);
+  ProfBracket pb(ctx, "construct", s, 0);
+  int64_t launches = 0;
+  int st = tree_construct(ctx, t, field, prm, tol, min_depth, max_depth, bc, s, &launches);
+  pb.set_kernels((int)launches);
   if (st != TBSLAS_OK) {
     std::string msg = g_err;
     tbslas_tree_destroy(t);

@@ -168,6 +168,8 @@ class ProfBracket {
   ~ProfBracket();
   ProfBracket(const ProfBracket&) = delete;
   ProfBracket& operator=(const ProfBracket&) = delete;
+  // For groups whose launch count is known only at their end.
+  void set_kernels(int kernels) { kernels_ = kernels; }
 
  private:
   tbslas_ctx ctx_;

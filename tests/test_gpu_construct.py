@@ -59,3 +59,18 @@ def test_fit_field_matches_host_fit(ctx):
     ref = trees.fit(fields.taylor_green(), a, d, q, 3)
     assert np.abs(t.get_coeffs() - ref).max() <= 1e-12 * np.abs(ref).max()
     t.close()
+
+
+def test_construct_profiled_launches(ctx):
+    """The construction reports its kernels to the context's profiler: with
+    nothing to refine or balance, the uniform tree, one fit and refinement
+    check (4), one balance check (2) and the install (maximum depth, lookup
+    table, split and norms of the coefficients) make 11."""
+    ctx.profile(True)
+    ctx.profile_reset()
+    t = tb.construct_tree(ctx, tb.Field.taylor_green(), 4, float("inf"), 2, 4)
+    prof = ctx.profile_totals()
+    ctx.profile(False)
+    assert t.n_leaves == 64
+    assert prof["construct"][:2] == (1, 11)
+    t.close()
