@@ -173,6 +173,8 @@ def test_semilag_in_situ_stagnation_on_faces(ctx, ora):
     for step in (1, 2, 3):
         tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv), tc, step, 0.004)
         ref["coeff"] = ora.semilag_in_situ(vel, ref, step, 0.004)
+        listed, whole = ctx.last_near_face_targets(), ctx.last_fp64_targets()
+        assert 0 < listed and 0 <= whole <= listed
     assert rel_err(tc.get_coeffs(), ref["coeff"]) <= TOL
 
 
