@@ -264,29 +264,32 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(cons
 // leaf) lies in Xd's leaf, so does the FP64 path's departure point, and the
 // double-float value at Xd stands, as for any unambiguous target.  Returns
 // false when the target needs the whole FP64 recomputation.
+// (The batched step's pass calls it with each problem's trees, so both
+// forms stay bitwise equal.)
 template <int D>
-__device__ __forceinline__ bool fix_by_axes(const SemilagTreeArgs& a, int64_t t,
+__device__ __forceinline__ bool fix_by_axes(const TreeView& vel, const TreeView& con,
+                                            const Nodes1D& nodes, const double* vn, double tau,
+                                            bool per, double* vals, int64_t t,
                                             ThreadSlots slots) {
   constexpr int NP = D * D * D;
   const int64_t leaf = t / NP;
   const int p = (int)(t - leaf * NP);
-  const Geom g = load_geom(a.con.geom + leaf);
+  const Geom g = load_geom(con.geom + leaf);
   const double h = 2.0 / g.w;
-  double X[3] = {g.x + h * a.nodes.x[p % D], g.y + h * a.nodes.x[(p / D) % D],
-                 g.z + h * a.nodes.x[p / (D * D)]};
-  const bool per = a.periodic != 0;
-  const double half_tau = 0.5 * a.tau;
+  double X[3] = {g.x + h * nodes.x[p % D], g.y + h * nodes.x[(p / D) % D],
+                 g.z + h * nodes.x[p / (D * D)]};
+  const double half_tau = 0.5 * tau;
   double pm[3], pw[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     if (per) X[k] = wrap1(X[k]);
-    pm[k] = pw[k] = fma(half_tau, __ldg(a.vn + 3 * t + k), X[k]);
+    pm[k] = pw[k] = fma(half_tau, __ldg(vn + 3 * t + k), X[k]);
   }
   const double zero[3] = {0.0, 0.0, 0.0};
   double v[3], ev[3], xd[3], m[3];
-  eval_point_df<D, 3, true>(a.vel, pw[0], pw[1], pw[2], per, zero, v, ev, slots);
+  eval_point_df<D, 3, true>(vel, pw[0], pw[1], pw[2], per, zero, v, ev, slots);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) df_update(a.tau, v[k], ev[k], X[k], 0.0, xd[k], m[k]);
+  for (int k = 0; k < 3; ++k) df_update(tau, v[k], ev[k], X[k], 0.0, xd[k], m[k]);
   // the concentration lookup at Xd, per axis
   double q[3] = {xd[0], xd[1], xd[2]};
   if (per) {
@@ -294,8 +297,8 @@ __device__ __forceinline__ bool fix_by_axes(const SemilagTreeArgs& a, int64_t t,
     for (int k = 0; k < 3; ++k) q[k] = wrap1(q[k]);
   }
   if (!inside(q[0], q[1], q[2], per)) return false;
-  const int64_t cl = find_leaf(a.con, morton3(quantise(q[0]), quantise(q[1]), quantise(q[2])));
-  const Geom gc = load_geom(a.con.geom + cl);
+  const int64_t cl = find_leaf(con, morton3(quantise(q[0]), quantise(q[1]), quantise(q[2])));
+  const Geom gc = load_geom(con.geom + cl);
   const double xi[3] = {(q[0] - gc.x) * gc.w - 1.0, (q[1] - gc.y) * gc.w - 1.0,
                         (q[2] - gc.z) * gc.w - 1.0};
   int axes = 0;
@@ -305,20 +308,20 @@ __device__ __forceinline__ bool fix_by_axes(const SemilagTreeArgs& a, int64_t t,
   if (axes == 0) return false;
   // the FP64 path's coordinates on those axes
   double v64[3];
-  eval_point_axes<D>(a.vel, pm[0], pm[1], pm[2], per, axes, v64);
+  eval_point_axes<D>(vel, pm[0], pm[1], pm[2], per, axes, v64);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     if ((axes >> k) & 1) {
-      const double c = fma(a.tau, v64[k], X[k]);
+      const double c = fma(tau, v64[k], X[k]);
       q[k] = per ? wrap1(c) : c;
     }
   }
   if (!inside(q[0], q[1], q[2], per)) return false;
-  if (find_leaf(a.con, morton3(quantise(q[0]), quantise(q[1]), quantise(q[2]))) != cl)
+  if (find_leaf(con, morton3(quantise(q[0]), quantise(q[1]), quantise(q[2]))) != cl)
     return false;
   double c[1], e[1];
-  eval_point_df<D, 1, false>(a.con, xd[0], xd[1], xd[2], per, m, c, e, slots);
-  a.vals[t] = c[0];
+  eval_point_df<D, 1, false>(con, xd[0], xd[1], xd[2], per, m, c, e, slots);
+  vals[t] = c[0];
   return true;
 }
 
@@ -337,7 +340,9 @@ __global__ void __launch_bounds__(128, 4) k_semilag_fix(const SemilagTreeArgs a)
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t t = a.fix_list[i];
-    if (by_axes && fix_by_axes<D>(a, t, slots)) continue;
+    if (by_axes &&
+        fix_by_axes<D>(a.vel, a.con, a.nodes, a.vn, a.tau, a.periodic != 0, a.vals, t, slots))
+      continue;
     atomicAdd(a.fix_count + 1, 1ull);
     const int64_t leaf = t / NP;
     const int p = (int)(t - leaf * NP);
