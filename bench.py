@@ -435,7 +435,6 @@ def run_gpu(args, wl, rank, world, local_rank):
     points = wl.points_per_step * args.steps
 
     fp64_targets = None if is_grid else ctx.last_fp64_targets()
-    near_face = None if is_grid else ctx.last_near_face_targets()
     # the same step with every Chebyshev sum in FP64 (TBSLAS_SUMS_FP64), timed
     # the same way on a copy of the initial state, plus its distance from the
     # default double-float step after one step
@@ -628,7 +627,6 @@ def run_gpu(args, wl, rank, world, local_rank):
             "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
             "fp64_sums": fp64, "clocks": clk.summary(), "gpu_launches": gpu_launches}
     if fp64_targets is not None:
-        line["near_face_targets_last_step"] = int(near_face)
         line["fp64_recomputed_targets_last_step"] = int(fp64_targets)
     print(json.dumps(line))
     assert ctx.check() == 0

@@ -110,12 +110,8 @@ int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launch
 enum { TBSLAS_SUMS_DOUBLE_FLOAT = 0, TBSLAS_SUMS_FP64 = 1 };
 int tbslas_ctx_set_sums(tbslas_ctx ctx, int mode);
 int tbslas_ctx_get_sums(tbslas_ctx ctx, int* mode);
-/* Targets of the last double-float in-situ step on ctx whose lookups were
- * ambiguous (handed to the near-face pass), and those of them the pass
- * recomputed entirely in FP64 (the others were settled by recomputing only
- * the ambiguous axes' coordinates in FP64); synchronise the device.
- * Diagnostic. */
-int tbslas_ctx_last_near_face_targets(tbslas_ctx ctx, int64_t* n);
+/* Targets of the last double-float in-situ step on ctx that were recomputed
+ * in FP64 (ambiguous lookups); synchronises the device.  Diagnostic. */
 int tbslas_ctx_last_fp64_targets(tbslas_ctx ctx, int64_t* n);
 
 /* Measured FP64 FMA throughput of the device (FLOP/s, 2 per FMA): the

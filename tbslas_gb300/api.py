@@ -128,17 +128,9 @@ class Context:
         call("tbslas_ctx_set_sums", self.handle, int(mode))
 
     def last_fp64_targets(self):
-        """Targets of the last double-float in-situ step recomputed entirely
-        in FP64."""
+        """Targets of the last double-float in-situ step recomputed in FP64."""
         n = ctypes.c_int64(0)
         call("tbslas_ctx_last_fp64_targets", self.handle, ctypes.byref(n))
-        return n.value
-
-    def last_near_face_targets(self):
-        """Targets of the last double-float in-situ step whose lookups were
-        ambiguous (handed to the near-face pass)."""
-        n = ctypes.c_int64(0)
-        call("tbslas_ctx_last_near_face_targets", self.handle, ctypes.byref(n))
         return n.value
 
     def fp32_fma_peak(self):

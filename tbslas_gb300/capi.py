@@ -41,7 +41,6 @@ SIGNATURES = {
     "tbslas_ctx_set_sums": [_vp, _i32],
     "tbslas_ctx_get_sums": [_vp, _c.POINTER(_i32)],
     "tbslas_ctx_last_fp64_targets": [_vp, _c.POINTER(_i64)],
-    "tbslas_ctx_last_near_face_targets": [_vp, _c.POINTER(_i64)],
     "tbslas_cheb_nodes": [_i32, _vp],
     "tbslas_pt2coeff_matrix": [_i32, _vp],
     "tbslas_tree_create": [_vp, _i64, _vp, _vp, _i32, _i32, _c.POINTER(_vp)],

@@ -149,18 +149,6 @@ __device__ __forceinline__ void batch_dispatch_fp64(int q, const BatchProblem& p
   }
 }
 
-template <int QLO, int QHI>
-__device__ __forceinline__ bool batch_fix_by_axes(int q, const BatchProblem& p, int64_t t,
-                                                  double tau, bool per, ThreadSlots slots) {
-  if constexpr (QLO <= QHI) {
-    if (q == QLO)
-      return fix_by_axes<QLO + 1>(p.vel, p.con, p.nodes, p.vn, tau, per, p.vals, t, slots);
-    return batch_fix_by_axes<QLO + 1, QHI>(q, p, t, tau, per, slots);
-  } else {
-    return false;
-  }
-}
-
 // Persistent CTAs take chunks of targets from an atomic counter; the chunk's
 // problem descriptor is staged in shared memory.
 template <int QLO, int QHI>
@@ -187,13 +175,9 @@ __global__ void __launch_bounds__(256, 3) k_batch_semilag(const BatchLaunch a) {
   }
 }
 
-// Near-face pass over the listed targets whose problem's degree is in this
-// band: k_semilag_fix's arithmetic (fix_by_axes when nrk = 1, else the FP64
-// recomputation).  Dynamic shared memory: 2 (QHI + 1) float2 per thread.
+// FP64 pass over the listed targets whose problem's degree is in this band.
 template <int QLO, int QHI>
-__global__ void __launch_bounds__(128, 4) k_batch_fix(const BatchLaunch a) {
-  extern __shared__ float2 s_fix_slots[];
-  const ThreadSlots slots{s_fix_slots + threadIdx.x, (int)blockDim.x};
+__global__ void __launch_bounds__(128) k_batch_fix(const BatchLaunch a) {
   const bool per = a.periodic != 0;
   const int ts = *a.ts0 + a.step;
   const int64_t n = (int64_t)*a.fix_count;
@@ -204,9 +188,7 @@ __global__ void __launch_bounds__(128, 4) k_batch_fix(const BatchLaunch a) {
     const int64_t t = e & ((1ll << kFixShift) - 1);
     const BatchProblem& p = a.probs[prob];
     if (p.q < QLO || p.q > QHI) continue;
-    const double tau = step_tau(ts, p.dt, p.nrk);
-    if (p.nrk == 1 && batch_fix_by_axes<QLO, QHI>(p.q, p, t, tau, per, slots)) continue;
-    batch_dispatch_fp64<QLO, QHI>(p.q, p, t, tau, per);
+    batch_dispatch_fp64<QLO, QHI>(p.q, p, t, step_tau(ts, p.dt, p.nrk), per);
   }
 }
 
@@ -217,7 +199,7 @@ __global__ void __launch_bounds__(128, 4) k_batch_fix(const BatchLaunch a) {
 template <int QLO, int QHI>
 void launch_band(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix) {
   if (fix) {
-    k_batch_fix<QLO, QHI><<<grid, 128, 2 * (QHI + 1) * 128 * sizeof(float2), s>>>(a);
+    k_batch_fix<QLO, QHI><<<grid, 128, 0, s>>>(a);
     return;
   }
   constexpr size_t kMaxSmem = 2 * (size_t)(QHI + 1) * 256 * sizeof(float2);

@@ -657,7 +657,7 @@ int fused_step(tbslas_ctx ctx, const TreeView& v1, const TreeView& v2, tbslas_tr
     a.vn = vn;
   }
   TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
-  TRY(scratch_t(ctx, kFixCount, 2, &a.fix_count));  // listed, recomputed
+  TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
   a.fix_grid = ctx->num_sms * 8;
   if (ctx->sums == TBSLAS_SUMS_FP64) {
     ProfScope p(ctx, "semilag_tree", s, 1);
@@ -1460,26 +1460,16 @@ int tbslas_ctx_get_sums(tbslas_ctx ctx, int* mode) {
   return TBSLAS_OK;
 }
 
-// The near-face counters of the last double-float in-situ step: [0] targets
-// handed to the near-face pass, [1] those it recomputed entirely in FP64.
-static int last_fix_counter(tbslas_ctx ctx, int which, int64_t* n) {
+int tbslas_ctx_last_fp64_targets(tbslas_ctx ctx, int64_t* n) {
   TRY(bind(ctx));
   if (!n) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
   *n = 0;
   if (!ctx->slots[kFixCount].p) return TBSLAS_OK;
-  unsigned long long c[2] = {0, 0};
+  unsigned long long c = 0;
   CUDA_TRY(cudaDeviceSynchronize());
-  CUDA_TRY(cudaMemcpy(c, ctx->slots[kFixCount].p, sizeof(c), cudaMemcpyDeviceToHost));
-  *n = (int64_t)c[which];
+  CUDA_TRY(cudaMemcpy(&c, ctx->slots[kFixCount].p, sizeof(c), cudaMemcpyDeviceToHost));
+  *n = (int64_t)c;
   return TBSLAS_OK;
-}
-
-int tbslas_ctx_last_fp64_targets(tbslas_ctx ctx, int64_t* n) {
-  return last_fix_counter(ctx, 1, n);
-}
-
-int tbslas_ctx_last_near_face_targets(tbslas_ctx ctx, int64_t* n) {
-  return last_fix_counter(ctx, 0, n);
 }
 
 int tbslas_fp64_fma_peak(tbslas_ctx ctx, double* flops_per_s) {
@@ -1825,7 +1815,7 @@ int tbslas_semilag_bdf2(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con_prev,
   TRY(scratch_t(ctx, kVals, N, &a.vals));
   TRY(scratch_t(ctx, kVN, N * 3, &vn));
   TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
-  TRY(scratch_t(ctx, kFixCount, 2, &a.fix_count));  // listed, recomputed
+  TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
   a.fix_grid = ctx->num_sms * 8;
   {
     ProfScope pv(ctx, "vel_at_nodes", s, 2);
@@ -2007,7 +1997,7 @@ int step_points_df(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timeste
   TRY(scratch_t(ctx, kXA, N * 3, &a.xmid));
   TRY(scratch_t(ctx, kXB, N * 3, &a.xdep));
   TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
-  TRY(scratch_t(ctx, kFixCount, 2, &a.fix_count));  // listed, recomputed
+  TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
   a.fix_grid = ctx->num_sms * 8;
   {
     ProfScope pp(ctx, "adjoint_points", s, 2);

@@ -176,41 +176,6 @@ __device__ __forceinline__ void eval_point(const TreeView& t, double& x, double&
   for (int l = 0; l < DOF; ++l) out[l] = tri_sum<D>(GlobalLoad{c + l * NC}, tx, ty, tz);
 }
 
-// The velocity components listed in mask (bit l: component l) at one point,
-// each bit-identical to eval_point<D, 3>'s; one copy of the sum serves all
-// components.  The point is wrapped under periodic boundaries (a copy).
-template <int D>
-__device__ __forceinline__ void eval_point_axes(const TreeView& t, double x, double y, double z,
-                                                bool periodic, int mask, double (&out)[3]) {
-  constexpr int NC = D * (D + 1) * (D + 2) / 6;
-  if (periodic) {
-    x = wrap1(x);
-    y = wrap1(y);
-    z = wrap1(z);
-  }
-  out[0] = out[1] = out[2] = 0.0;
-  if (!inside(x, y, z, periodic)) return;
-  const uint64_t key = morton3(quantise(x), quantise(y), quantise(z));
-  const int64_t leaf = find_leaf(t, key);
-  const Geom g = load_geom(t.geom + leaf);
-  double tx[D], ty[D], tz[D];
-  cheb_T<D>((x - g.x) * g.w - 1.0, tx);
-  cheb_T<D>((y - g.y) * g.w - 1.0, ty);
-  cheb_T<D>((z - g.z) * g.w - 1.0, tz);
-  const double* c = t.coeff + leaf * t.stride;
-#pragma unroll 1
-  for (int l = 0; l < 3; ++l) {
-    if (!((mask >> l) & 1)) continue;
-    const double r = tri_sum<D>(GlobalLoad{c + l * NC}, tx, ty, tz);
-    if (l == 0)
-      out[0] = r;
-    else if (l == 1)
-      out[1] = r;
-    else
-      out[2] = r;
-  }
-}
-
 // Double-float evaluation of DOF components at one point, for the fused
 // step; `slots` holds 2*D shared-memory elements of this thread (the y and z
 // Chebyshev values of tri_sum_df_rows).  m[a] bounds, per axis, the distance

@@ -27,7 +27,6 @@ struct SemilagTreeArgs {
   double* vals;       // [Lc * Np] node values at the departure points
   const double* vn;   // [Lc * Np][3] velocity at the targets (first RK stage) or null
   int64_t* fix_list;  // targets the double-float kernel hands to the FP64 pass
-  // [0] targets listed, [1] targets the pass recomputed entirely in FP64
   unsigned long long* fix_count;
   int fix_grid;       // CTAs of the FP64 pass (persistent)
   // nrk = 1 with vn given: every target's RK2 midpoint X* and departure point

@@ -250,100 +250,17 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(cons
   if (amb) a.fix_list[atomicAdd(a.fix_count, 1ull)] = t;
 }
 
-// The near-face pass's shortcut for a plain step (nrk = 1, first stage from
-// the node grid, no stored points).  The target's double-float departure
-// point Xd and its bounds m are recomputed as k_semilag_tree_df computes them
-// (the midpoint is exact, so its lookup is never ambiguous); the axes A on
-// which the concentration lookup at Xd is ambiguous get the FP64 path's
-// coordinate exactly, from the FP64 velocity components of A at the midpoint
-// (eval_point_axes).  Most listed targets are nodes on a plane where the
-// normal velocity vanishes (a stagnation plane of the flow lying on a leaf
-// face): their coordinate on A stays on the face in both paths, and the bound
-// alone cannot show it.  If the point with the exact coordinates on A and
-// Xd's on the other axes (each farther than its bound from a face of the
-// leaf) lies in Xd's leaf, so does the FP64 path's departure point, and the
-// double-float value at Xd stands, as for any unambiguous target.  Returns
-// false when the target needs the whole FP64 recomputation.
-// (The batched step's pass calls it with each problem's trees, so both
-// forms stay bitwise equal.)
-template <int D>
-__device__ __forceinline__ bool fix_by_axes(const TreeView& vel, const TreeView& con,
-                                            const Nodes1D& nodes, const double* vn, double tau,
-                                            bool per, double* vals, int64_t t,
-                                            ThreadSlots slots) {
-  constexpr int NP = D * D * D;
-  const int64_t leaf = t / NP;
-  const int p = (int)(t - leaf * NP);
-  const Geom g = load_geom(con.geom + leaf);
-  const double h = 2.0 / g.w;
-  double X[3] = {g.x + h * nodes.x[p % D], g.y + h * nodes.x[(p / D) % D],
-                 g.z + h * nodes.x[p / (D * D)]};
-  const double half_tau = 0.5 * tau;
-  double pm[3], pw[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    if (per) X[k] = wrap1(X[k]);
-    pm[k] = pw[k] = fma(half_tau, __ldg(vn + 3 * t + k), X[k]);
-  }
-  const double zero[3] = {0.0, 0.0, 0.0};
-  double v[3], ev[3], xd[3], m[3];
-  eval_point_df<D, 3, true>(vel, pw[0], pw[1], pw[2], per, zero, v, ev, slots);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) df_update(tau, v[k], ev[k], X[k], 0.0, xd[k], m[k]);
-  // the concentration lookup at Xd, per axis
-  double q[3] = {xd[0], xd[1], xd[2]};
-  if (per) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) q[k] = wrap1(q[k]);
-  }
-  if (!inside(q[0], q[1], q[2], per)) return false;
-  const int64_t cl = find_leaf(con, morton3(quantise(q[0]), quantise(q[1]), quantise(q[2])));
-  const Geom gc = load_geom(con.geom + cl);
-  const double xi[3] = {(q[0] - gc.x) * gc.w - 1.0, (q[1] - gc.y) * gc.w - 1.0,
-                        (q[2] - gc.z) * gc.w - 1.0};
-  int axes = 0;
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-    if (m[k] > 0.0 && fabs(xi[k]) >= 1.0 - m[k] * gc.w) axes |= 1 << k;
-  if (axes == 0) return false;
-  // the FP64 path's coordinates on those axes
-  double v64[3];
-  eval_point_axes<D>(vel, pm[0], pm[1], pm[2], per, axes, v64);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    if ((axes >> k) & 1) {
-      const double c = fma(tau, v64[k], X[k]);
-      q[k] = per ? wrap1(c) : c;
-    }
-  }
-  if (!inside(q[0], q[1], q[2], per)) return false;
-  if (find_leaf(con, morton3(quantise(q[0]), quantise(q[1]), quantise(q[2]))) != cl)
-    return false;
-  double c[1], e[1];
-  eval_point_df<D, 1, false>(con, xd[0], xd[1], xd[2], per, m, c, e, slots);
-  vals[t] = c[0];
-  return true;
-}
-
 // FP64 recomputation of the listed targets (the arithmetic of
 // k_semilag_tree, with the first-stage velocity from the node grid when
 // given -- it is bit-identical to eval_point there); stored midpoints and
-// departure points of those targets become the FP64 path's.  A plain step
-// first tries fix_by_axes.  Dynamic shared memory: 2 D float2 per thread.
+// departure points of those targets become the FP64 path's.
 template <int D, bool POINTS = false>
-__global__ void __launch_bounds__(128, 4) k_semilag_fix(const SemilagTreeArgs a) {
+__global__ void __launch_bounds__(128) k_semilag_fix(const SemilagTreeArgs a) {
   constexpr int NP = D * D * D;
-  extern __shared__ float2 s_fix_slots[];
-  const ThreadSlots slots{s_fix_slots + threadIdx.x, (int)blockDim.x};
-  const bool by_axes = !POINTS && a.vn && a.nrk == 1 && !a.xmid && !a.xdep;
   const int64_t n = (int64_t)*a.fix_count;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t t = a.fix_list[i];
-    if (by_axes &&
-        fix_by_axes<D>(a.vel, a.con, a.nodes, a.vn, a.tau, a.periodic != 0, a.vals, t, slots))
-      continue;
-    atomicAdd(a.fix_count + 1, 1ull);
     const int64_t leaf = t / NP;
     const int p = (int)(t - leaf * NP);
     const Geom g = load_geom(a.con.geom + leaf);
@@ -373,10 +290,10 @@ void launch_semilag_tree_df(const SemilagTreeArgs& a, cudaStream_t s) {
   const int threads = 128;
   const int64_t blocks = (n + threads - 1) / threads;
   if (blocks == 0) return;
-  cudaMemsetAsync(a.fix_count, 0, 2 * sizeof(unsigned long long), s);
+  cudaMemsetAsync(a.fix_count, 0, sizeof(unsigned long long), s);
   const size_t smem = 2 * D * threads * sizeof(float2);
   k_semilag_tree_df<D><<<(unsigned)blocks, threads, smem, s>>>(a);
-  k_semilag_fix<D><<<a.fix_grid, threads, smem, s>>>(a);
+  k_semilag_fix<D><<<a.fix_grid, threads, 0, s>>>(a);
 }
 
 // Midpoints and departure points only (the double-float adjoint's recompute).
@@ -387,7 +304,7 @@ void launch_points_df(const SemilagTreeArgs& a, cudaStream_t s) {
   const int threads = 128;
   const int64_t blocks = (n + threads - 1) / threads;
   if (blocks == 0) return;
-  cudaMemsetAsync(a.fix_count, 0, 2 * sizeof(unsigned long long), s);
+  cudaMemsetAsync(a.fix_count, 0, sizeof(unsigned long long), s);
   const size_t smem = 2 * D * threads * sizeof(float2);
   k_semilag_tree_df<D, true><<<(unsigned)blocks, threads, smem, s>>>(a);
   k_semilag_fix<D, true><<<a.fix_grid, threads, 0, s>>>(a);
