@@ -805,7 +805,7 @@ def cpu_baseline_bdf2(wl, budget_s=12.0):
     def run(k):
         return ora.semilag_bdf2(vel, prev, cur, dict(anchor=wl.a[:k], depth=wl.d[:k], q=wl.q),
                                 wl.t0, wl.dt)
-    probe = 8
+    probe = min(8, len(wl.d))
     t0 = time.perf_counter()
     run(probe)
     per_leaf = max((time.perf_counter() - t0) / probe, 1e-6)
@@ -933,7 +933,7 @@ def cpu_baseline_tv(wl, budget_s=12.0):
     def run(k):
         return ora.semilag_in_situ_tv(vels, con, wl.timestep, wl.dt, 1, False, times=wl.times,
                                       leaf_end=k)
-    probe = 8
+    probe = min(8, len(wl.d))
     t0 = time.perf_counter()
     run(probe)
     per_leaf = max((time.perf_counter() - t0) / probe, 1e-6)

@@ -80,3 +80,36 @@ def test_reference_arm_tree_and_adapters(capsys):
     t = bench._pick(batch, 3)
     assert t.q == wl.q and t.bc == 1 and t.cc is wl.cc
     assert bench._pick(wl, 0) is wl
+
+
+def _tiny_next_row_workloads():
+    """Tiny stand-ins of the re-meshing, BDF2, time-dependent velocity and
+    construction workloads (q = 3, depth-1/2 trees)."""
+    import numpy as np
+    from tbslas_gb300 import fields, trees, workloads
+    rm = _tiny_tree_workload()
+    rm.name = "tiny_remesh"
+    rm.remesh = (1e-3, 1, 2)
+    bdf2 = workloads.Bdf2Workload(q=3, depth=1, name="tiny_bdf2")
+    tv = workloads.TvWorkload(q=3, depth=1, name="tiny_tv")
+    con = _tiny_tree_workload()
+    con.name = "tiny_construct"
+    con.blobs = fields.gaussian_blobs(np.random.default_rng(2), 2)
+    con.construct = (1e-3, 1, 2)
+    return [rm, bdf2, tv, con]
+
+
+@pytest.mark.parametrize("i", range(4))
+def test_reference_arm_next_rows(capsys, i):
+    """--impl reference on the re-meshing, BDF2, time-dependent velocity and
+    construction workloads: the oracle's own loop, one contract line each."""
+    import json
+    wl = _tiny_next_row_workloads()[i]
+    bench.run_reference(_Args(), wl)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["e2e"]["value"] == line["value"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["config"]["workload"] == wl.name
+    if hasattr(wl, "construct"):
+        assert "construction" in line["unit"]
