@@ -251,7 +251,7 @@ def run_reference(args, wl):
               "sample": "the oracle's construction of both trees, %d of %d steps" % (n, args.steps)}
         timed_steps = max(n, 1)
     elif hasattr(wl, "remesh"):
-        # the driver's loop on the CPU: oracle step + oracle re-mesh, advancing
+        # the reference driver's loop on the CPU: oracle step + oracle re-mesh, advancing
         # the state, as many of the K steps as fit the time budget
         from oracle import oracle as ora
         from oracle import remesh as rm
