@@ -258,3 +258,26 @@ def test_cubic_time_weights_match_interp_cubic(ora):
         assert abs(w @ p - ref) <= 1e-14 * max(1.0, abs(ref))
     w = tb.cubic_time_weights([0.0, 1.0, 2.0, 3.0], 1.5)
     assert np.allclose(w, [-0.0625, 0.5625, 0.5625, -0.0625], rtol=0, atol=1e-16)
+
+
+@pytest.mark.parametrize("functor", ["set", "extrap"])
+def test_time_dependent_step_with_one_velocity_is_the_plain_step(ora, functor):
+    """FieldSetFunctor over four copies of one tree (cubic weights summing to
+    1) and FieldExtrapFunctor over two copies (1.5 v - 0.5 v) are that tree's
+    velocity: the time-dependent step equals the plain step up to the
+    rounding of the blend, on a generic periodic Fourier velocity (no
+    stagnation on leaf faces)."""
+    q, dt = 4, 0.01
+    a, d = trees.uniform_tree(2)
+    vel_fn = fields.fourier_velocity(np.random.default_rng(12))
+    vc = trees.fit(vel_fn, a, d, q, 3)
+    cc = trees.fit(fields.gaussian_blobs(np.random.default_rng(13), 2, (0.1, 0.15)), a, d, q, 1)
+    vel = dict(anchor=a, depth=d, q=q, dof=3, coeff=vc)
+    con = dict(anchor=a, depth=d, q=q, dof=1, coeff=cc)
+    ref = ora.semilag_in_situ(vel, con, 3, dt, 1, True)
+    if functor == "set":
+        got = ora.semilag_in_situ_tv([vel] * 4, con, 3, dt, 1, True,
+                                     times=[0.0, dt, 2 * dt, 3 * dt])
+    else:
+        got = ora.semilag_in_situ_tv([vel, vel], con, 3, dt, 1, True)
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
