@@ -113,3 +113,20 @@ def test_reference_arm_next_rows(capsys, i):
     assert line["config"]["workload"] == wl.name
     if hasattr(wl, "construct"):
         assert "construction" in line["unit"]
+
+
+def test_clock_sampler_summary_parses_nvidia_smi_rows(tmp_path):
+    """The clocks block of every bench line: median SM clock under load, the
+    maximum, and the throttle reasons seen Active in any sample."""
+    s = bench.ClockSampler(0)
+    s.path = str(tmp_path / "clocks.csv")
+    with open(s.path, "w") as f:
+        f.write("0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active\n")
+        f.write("0, 1995, 2070, 1390.5, 0x4, Not Active, Not Active, Not Active, Active\n")
+        f.write("0, 2070, 2070, 1200.0, 0x0, Not Active, Not Active, Not Active, Not Active\n")
+        f.write("[N/A]\n")
+    out = s.summary()
+    assert out == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"],
+                   "samples": 3}
+    empty = bench.ClockSampler(0)
+    assert empty.summary()["reasons"] == ["unavailable"]
