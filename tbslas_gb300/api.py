@@ -238,9 +238,19 @@ class Field:
     GAUSSIANS, GAUSSIAN_3D, EXP_ALPHA, ROTATION = 0, 1, 2, 3
     TAYLOR_GREEN, TAYLOR_GREEN_ABC, HOPF, FOURIER = 4, 5, 6, 7
 
+    # parameters per kind (per term for the sums), as the C ABI reads them
+    _NPARAM = {GAUSSIANS: 5, GAUSSIAN_3D: 7, EXP_ALPHA: 5, ROTATION: 1, TAYLOR_GREEN: 0,
+               TAYLOR_GREEN_ABC: 6, HOPF: 5, FOURIER: 9}
+
     def __init__(self, kind, params=(), n=0):
         self.kind, self.n = int(kind), int(n)
         self.params = np.ascontiguousarray(params, dtype=np.float64).reshape(-1)
+        per = Field._NPARAM.get(self.kind)  # unknown kinds: the C ABI rejects them
+        want = per * self.n if self.kind in (Field.GAUSSIANS, Field.FOURIER) else per
+        # the C ABI reads exactly `want` doubles from the array
+        if per is not None and self.params.size != want:
+            raise ValueError("field kind %d takes %d parameters, got %d"
+                             % (self.kind, want, self.params.size))
 
     def _c(self):
         return _CField(self.kind, self.n,
