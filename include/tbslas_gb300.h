@@ -80,6 +80,16 @@ int tbslas_ctx_destroy(tbslas_ctx ctx);
 /* Kernel-side error word (bounded waits that ran out, ...); 0 if clean.
  * Synchronises the context's device; clears the word. */
 int tbslas_ctx_check(tbslas_ctx ctx, uint32_t* device_error);
+/* Polls a bounded device-side wait makes before it gives up (default
+ * TBSLAS_WAIT_LIMIT_DEFAULT).  The functor's per-tile wait for its
+ * coefficient copy uses it; a wait that runs out sets bit
+ * TBSLAS_DEVICE_ERR_WAIT_TIMEOUT of the error word, lets the copy in flight
+ * land, and its kernel returns, leaving the context usable (that call's
+ * output is incomplete).  A small limit (0 = give up at once) is how a test
+ * drives that path without faulting anything.  No reference counterpart. */
+#define TBSLAS_WAIT_LIMIT_DEFAULT (1u << 22)
+#define TBSLAS_DEVICE_ERR_WAIT_TIMEOUT 1u
+int tbslas_ctx_set_wait_limit(tbslas_ctx ctx, uint32_t polls);
 
 /* ---- profiling --------------------------------------------------------------- */
 /* Per-kernel CUDA-event timing, accumulated per kernel name.  Replaces
@@ -94,19 +104,26 @@ int tbslas_profile_count(tbslas_ctx ctx, int* n);
  * name: valid until the next reset or destroy of ctx. */
 int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launches,
                        int64_t* kernels, double* total_ms);
-/* Arithmetic of the in-situ step's Chebyshev sums (targets, RK2 updates,
- * Morton keys, leaf search and leaf-local coordinates are FP64 either way):
- *  - TBSLAS_SUMS_DOUBLE_FLOAT (default): the sums at the midpoint and the
- *    departure point run as double-float (hi + lo float pairs, 48-bit
- *    significand, error-free products and sums) on the FP32 pipe -- GB300
- *    runs FP64 at 1/72 of its FP32 rate.  Every coordinate carries a
- *    rigorous bound on its distance from the all-FP64 one; targets whose
- *    lookup that bound makes ambiguous are recomputed in FP64, so every leaf
- *    choice equals the FP64 path's.  Values agree with the FP64 path to
- *    ~1e-14 relative (the parity tolerance is 1e-12).
- *  - TBSLAS_SUMS_FP64: every sum in FP64 in the reference's order; departure
- *    points and node values bit-identical to the oracle.
- * The first RK2 stage (the velocity at the nodes) is FP64 and exact in both. */
+/* Arithmetic of the Chebyshev sums of the SL steps on ctx (targets, RK2
+ * updates, Morton keys, leaf search and leaf-local coordinates are FP64
+ * either way):
+ *  - TBSLAS_SUMS_FP64 (default): every sum in FP64 in the reference's order,
+ *    as the reference computes them (vec_eval<double>,
+ *    src/tree/tree_functor.h:27-84); departure points and node values are
+ *    bit-identical to the oracle.
+ *  - TBSLAS_SUMS_DOUBLE_FLOAT (opt-in, narrower than FP64): the sums at the
+ *    midpoint and the departure point run as double-float (hi + lo float
+ *    pairs: 48-bit significand, FP32's exponent range, so magnitudes below
+ *    2^-126 flush and above 2^100 are rejected through the device error
+ *    word) on the FP32 pipe -- GB300 runs FP64 at 1/72 of its FP32 rate.
+ *    Every coordinate carries a rigorous bound on its distance from the
+ *    all-FP64 one; targets whose lookup that bound makes ambiguous are
+ *    recomputed in FP64, so every leaf choice equals the FP64 path's.
+ *    Values agree with the FP64 path to ~1e-14 relative (the parity
+ *    tolerance is 1e-12).
+ * The first RK2 stage (the velocity at the nodes) is FP64 and exact in both.
+ * The batch (tbslas_batch_*) follows the mode its context had when the batch
+ * was created. */
 enum { TBSLAS_SUMS_DOUBLE_FLOAT = 0, TBSLAS_SUMS_FP64 = 1 };
 int tbslas_ctx_set_sums(tbslas_ctx ctx, int mode);
 int tbslas_ctx_get_sums(tbslas_ctx ctx, int* mode);
@@ -244,13 +261,13 @@ int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_ho
 
 /* Allocation-free form of tbslas_eval_tree, for callers that cannot allocate
  * device memory while they evaluate: a solver loop running under a memory
- * budget fixed up front, a host application whose own pool owns every device
- * allocation (library-side cudaMalloc/cudaFree would synchronise the device
- * and fragment that pool), or code that records its work into a stream
- * capture, where a cudaMalloc breaks the capture.  No counterpart in the
- * reference (it allocates freely: static grow-on-demand buffers in
- * EvalTree).  Same inputs, outputs and results as tbslas_eval_tree; the call
- * itself makes no cudaMalloc, cudaFree or allocating library call.
+ * budget fixed up front, or a host application whose own pool owns every
+ * device allocation (library-side cudaMalloc/cudaFree would synchronise the
+ * device and fragment that pool).  No counterpart in the reference (it
+ * allocates freely: static grow-on-demand buffers in EvalTree).  Same inputs,
+ * outputs and results as tbslas_eval_tree; the call itself makes no
+ * cudaMalloc, cudaFree or allocating library call.  The caller's current
+ * device is left as it was.
  *  - Scratch lives in one static device array of TBSLAS_NOALLOC_SCRATCH_BYTES
  *    (about 5 MiB) that every GPU which loads this library holds until the
  *    process exits.
@@ -259,7 +276,9 @@ int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_ho
  *    TBSLAS_ERR_SIZE (split the points over several calls).
  *  - The first call on a device looks up the array's device address
  *    (cudaGetSymbolAddress) with that device current; make that first call
- *    before any stream capture.
+ *    before any stream capture.  If the host application destroys the
+ *    device's primary context (cudaDeviceReset), the next call sees a new
+ *    context and looks the address up again.
  *  - Every call on a device shares the one array: calls whose work overlaps
  *    on the GPU (other streams, other host threads) race and corrupt each
  *    other.  Serialise them (one stream, or events).  The parts that must

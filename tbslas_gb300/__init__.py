@@ -5,7 +5,7 @@ include/tbslas_gb300.h); this package is its Python face.
 """
 from . import capi  # noqa: F401
 from .api import (  # noqa: F401
-    SUMS_DOUBLE_FLOAT, SUMS_FP64, Batch, Context, FieldExtrapFunctor, FieldSetFunctor, FreeSpace,
+    DEVICE_ERR_WAIT_TIMEOUT, SUMS_DOUBLE_FLOAT, SUMS_FP64, WAIT_LIMIT_DEFAULT, Batch, Context, FieldExtrapFunctor, FieldSetFunctor, FreeSpace,
     Field, NodeFieldFunctor, Periodic, Tree, construct_tree, cubic_time_weights,
     collect_cheb_tree_grid_points,
     compute_traj_rk2, fast_interp, get_pt2coeff_matrix, n_coeff, n_points, new_nodes,

@@ -11,6 +11,7 @@ Device arrays are torch CUDA float64 tensors; host arrays are numpy float64
 arrays (the *_host entry points).  Every call goes to the CUDA library; there
 is no CPU path.
 """
+import contextlib
 import ctypes
 
 import numpy as np
@@ -21,6 +22,8 @@ from .capi import BC_FREESPACE, BC_PERIODIC, call
 FreeSpace = BC_FREESPACE
 Periodic = BC_PERIODIC
 SUMS_DOUBLE_FLOAT, SUMS_FP64 = 0, 1
+WAIT_LIMIT_DEFAULT = 1 << 22
+DEVICE_ERR_WAIT_TIMEOUT = 1
 
 
 def n_coeff(q):
@@ -117,8 +120,10 @@ class Context:
 
     @property
     def sums(self):
-        """Arithmetic of the in-situ step's Chebyshev sums: SUMS_DOUBLE_FLOAT
-        (default) or SUMS_FP64 (bit-identical to the oracle)."""
+        """Arithmetic of the SL steps' Chebyshev sums: SUMS_FP64 (default,
+        the reference's FP64 arithmetic, bit-identical to the oracle) or
+        SUMS_DOUBLE_FLOAT (opt-in: hi/lo float pairs on the FP32 pipe, within
+        ~1e-14 of FP64, leaf choices equal to FP64's)."""
         m = ctypes.c_int(0)
         call("tbslas_ctx_get_sums", self.handle, ctypes.byref(m))
         return m.value
@@ -126,6 +131,22 @@ class Context:
     @sums.setter
     def sums(self, mode):
         call("tbslas_ctx_set_sums", self.handle, int(mode))
+
+    @contextlib.contextmanager
+    def sums_mode(self, mode):
+        """`with ctx.sums_mode(SUMS_DOUBLE_FLOAT): ...` -- the mode for the
+        block, the previous one restored after it."""
+        prev = self.sums
+        self.sums = mode
+        try:
+            yield self
+        finally:
+            self.sums = prev
+
+    def set_wait_limit(self, polls=WAIT_LIMIT_DEFAULT):
+        """Polls of the bounded device-side waits before they give up (and
+        set DEVICE_ERR_WAIT_TIMEOUT in the error word ctx.check reports)."""
+        call("tbslas_ctx_set_wait_limit", self.handle, int(polls))
 
     def last_fp64_targets(self):
         """Targets of the last double-float in-situ step recomputed in FP64."""
@@ -144,6 +165,16 @@ class Context:
         w = ctypes.c_uint32(0)
         st = capi.lib().tbslas_ctx_check(self.handle, ctypes.byref(w))
         capi.check(st, "tbslas_ctx_check")
+        return w.value
+
+    def take_device_error(self):
+        """Synchronise, return the device error word and clear it, without
+        raising (0 when clean; bit DEVICE_ERR_WAIT_TIMEOUT: a bounded wait
+        ran out)."""
+        w = ctypes.c_uint32(0)
+        st = capi.lib().tbslas_ctx_check(self.handle, ctypes.byref(w))
+        if st not in (0, capi.ERR_DEVICE):
+            capi.check(st, "tbslas_ctx_check")
         return w.value
 
 

@@ -11,6 +11,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libtbslas_gb300.so")
 
 OK = 0
+ERR_DEVICE = 7  # TBSLAS_ERR_DEVICE: a kernel reported an error status
 BC_FREESPACE = 0
 BC_PERIODIC = 1
 MAX_DEGREE = 16
@@ -20,6 +21,7 @@ NOALLOC_MAX_LEAVES = 1 << 15
 
 _c = ctypes
 _vp, _i64, _i32, _f64 = _c.c_void_p, _c.c_int64, _c.c_int, _c.c_double
+_u32 = _c.c_uint32
 _u32p = _c.POINTER(_c.c_uint32)
 _i64p = _c.POINTER(_c.c_int64)
 _i32p = _c.POINTER(_c.c_int)
@@ -39,6 +41,7 @@ SIGNATURES = {
     "tbslas_fp64_fma_peak": [_vp, _c.POINTER(_f64)],
     "tbslas_fp32_fma_peak": [_vp, _c.POINTER(_f64)],
     "tbslas_ctx_set_sums": [_vp, _i32],
+    "tbslas_ctx_set_wait_limit": [_vp, _u32],
     "tbslas_ctx_get_sums": [_vp, _c.POINTER(_i32)],
     "tbslas_ctx_last_fp64_targets": [_vp, _c.POINTER(_i64)],
     "tbslas_cheb_nodes": [_i32, _vp],

@@ -63,6 +63,7 @@ extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbsl
                                            int timestep, double dt, int bc, double* xmid_dev,
                                            double* xdep_dev, void* stream) {
   // the in-situ step itself (the context's sum mode), storing the points
+  DeviceRestore restore;
   TreeView tv, tc;
   int st = check_pair(ctx, vel, con, dt, bc, &tv, &tc);
   if (st != TBSLAS_OK) return st;
@@ -76,6 +77,7 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
                                       int bc, const double* lambda_next_dev, double* lambda_k_dev,
                                       double* grad_vel_dev, const double* xmid_dev,
                                       const double* xdep_dev, void* stream) {
+  DeviceRestore restore;
   TreeView tv, tc;
   int st = check_pair(ctx, vel, con, dt, bc, &tv, &tc);
   if (st != TBSLAS_OK) return st;

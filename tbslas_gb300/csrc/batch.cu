@@ -35,6 +35,7 @@ struct tbslas_batch_s {
   tbslas_ctx ctx = nullptr;
   int device = 0, num_sms = 0;
   int n = 0, nrk = 1, bc = 0;
+  bool df = false;  // double-float sums (the context's mode at creation), else FP64
   std::vector<BatchProblem> h_probs;
   std::vector<tbslas_tree> trees;   // every velocity and concentration tree
   std::vector<uint64_t> tree_gen;   // their generations when the batch was built
@@ -132,14 +133,15 @@ int enqueue_steps(tbslas_batch b, int nsteps, cudaStream_t s) {
       BatchLaunch a{b->d_probs, b->d_items + b->band_begin[band], n,
                     b->d_counters + (int64_t)i * kPer + band, b->d_ts0, i, b->bc,
                     b->d_fix, fix_count};
-      launch_batch_band(band, a, (int)std::min<int64_t>(grid, n), b->block, s, false);
+      launch_batch_band(band, a, (int)std::min<int64_t>(grid, n), b->block, s,
+                        b->df ? kBandStepDF : kBandStepFP64);
     }
-    for (int band = 0; band < kBands; ++band) {
+    for (int band = 0; band < kBands && b->df; ++band) {
       if (b->band_begin[band + 1] == b->band_begin[band]) continue;
       BatchLaunch a{b->d_probs, nullptr, 0, nullptr, b->d_ts0, i, b->bc, b->d_fix, fix_count};
-      launch_batch_band(band, a, b->num_sms * 4, 128, s, true);
+      launch_batch_band(band, a, b->num_sms * 4, 128, s, kBandFix);
     }
-    launch_batch_refit(b->d_jobs, b->d_ritems, b->n_ritems, b->max_q, s);
+    launch_batch_refit(b->d_jobs, b->d_ritems, b->n_ritems, b->max_q, b->df, s);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch step launch");
@@ -207,6 +209,7 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
   if (nrk < 1) return fail_status(TBSLAS_ERR_INVALID_ARG, "nrk < 1");
   if (bc != TBSLAS_BC_FREESPACE && bc != TBSLAS_BC_PERIODIC)
     return fail_status(TBSLAS_ERR_INVALID_ARG, "invalid boundary condition");
+  DeviceRestore restore;
   tbslas_batch b = new tbslas_batch_s();
   b->ctx = ctx;
   b->n = n;
@@ -217,6 +220,7 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     delete b;
     return st;
   }
+  b->df = ctx_sums(ctx) == TBSLAS_SUMS_DOUBLE_FLOAT;
   cudaSetDevice(b->device);
   std::vector<RefitJob> jobs;
   std::vector<RefitItem> ritems;
@@ -348,6 +352,7 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
 
 int tbslas_batch_destroy(tbslas_batch b) {
   if (!b) return TBSLAS_OK;
+  DeviceRestore restore;
   cudaSetDevice(b->device);
   cudaDeviceSynchronize();
   drop_graph(b);
@@ -372,6 +377,7 @@ int tbslas_batch_set_params(tbslas_batch b, int block, int targets_per_item, int
   if (!params_ok(block, targets_per_item, ctas_per_sm))
     return fail_status(TBSLAS_ERR_INVALID_ARG,
                        "block must be 64/128/256, targets_per_item 1..2^20, ctas_per_sm 1..32");
+  DeviceRestore restore;
   cudaSetDevice(b->device);
   b->block = block;
   b->cps = ctas_per_sm;
@@ -407,6 +413,7 @@ int tbslas_batch_run(tbslas_batch b, int timestep0, int nsteps, int use_graph, v
   if (nsteps < 0) return fail_status(TBSLAS_ERR_INVALID_ARG, "negative step count");
   if (check_generations(b) != TBSLAS_OK) return TBSLAS_ERR_INVALID_ARG;
   if (nsteps == 0) return TBSLAS_OK;
+  DeviceRestore restore;
   BCUDA(cudaSetDevice(b->device));
   return run(b, timestep0, nsteps, use_graph != 0, (cudaStream_t)stream);
 }
@@ -414,6 +421,7 @@ int tbslas_batch_run(tbslas_batch b, int timestep0, int nsteps, int use_graph, v
 int tbslas_batch_autotune(tbslas_batch b, int* block, int* targets_per_item, int* ctas_per_sm) {
   if (!b) return fail_status(TBSLAS_ERR_INVALID_ARG, "null batch");
   if (check_generations(b) != TBSLAS_OK) return TBSLAS_ERR_INVALID_ARG;
+  DeviceRestore restore;
   BCUDA(cudaSetDevice(b->device));
   BCUDA(cudaDeviceSynchronize());
   // Save every concentration tree: each trial step overwrites them.

@@ -175,6 +175,32 @@ __global__ void __launch_bounds__(256, 3) k_batch_semilag(const BatchLaunch a) {
   }
 }
 
+// The TBSLAS_SUMS_FP64 form of k_batch_semilag: every target of a chunk runs
+// k_semilag_tree<D>'s FP64 arithmetic (batch_target), so a batch step equals
+// the per-problem loop in that mode bit for bit, and no near-face pass
+// follows.
+template <int QLO, int QHI>
+__global__ void __launch_bounds__(256) k_batch_semilag_fp64(const BatchLaunch a) {
+  __shared__ BatchProblem sp;
+  __shared__ int64_t s_item;
+  const bool per = a.periodic != 0;
+  const int ts = *a.ts0 + a.step;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int64_t)atomicAdd(a.counter, 1ull);
+    __syncthreads();
+    const int64_t it = s_item;
+    if (it >= a.n_items) return;
+    const BatchItem w = a.items[it];
+    if (threadIdx.x == 0) sp = a.probs[w.problem];
+    __syncthreads();
+    const double tau = step_tau(ts, sp.dt, sp.nrk);
+    const int q = sp.q;
+    for (int k = threadIdx.x; k < w.count; k += blockDim.x)
+      batch_dispatch_fp64<QLO, QHI>(q, sp, w.start + k, tau, per);
+    __syncthreads();  // s_item and sp are rewritten for the next chunk
+  }
+}
+
 // FP64 pass over the listed targets whose problem's degree is in this band.
 template <int QLO, int QHI>
 __global__ void __launch_bounds__(128) k_batch_fix(const BatchLaunch a) {
@@ -192,14 +218,22 @@ __global__ void __launch_bounds__(128) k_batch_fix(const BatchLaunch a) {
   }
 }
 
-// Launch of one band: the step kernel with 2 * (QHI + 1) shared-memory
-// elements per thread (its dynamic shared-memory limit raised once per
-// device: with the static descriptor, 48 KB of slots already exceeds the
-// default), or the FP64 pass.
+// What a band launch runs: the double-float step kernel, the FP64 pass over
+// its listed targets, or the FP64 step kernel.
+enum BandKernel : int { kBandStepDF = 0, kBandFix = 1, kBandStepFP64 = 2 };
+
+// Launch of one band: the double-float step kernel with 2 * (QHI + 1)
+// shared-memory elements per thread (its dynamic shared-memory limit raised
+// once per device: with the static descriptor, 48 KB of slots already
+// exceeds the default), the FP64 pass, or the FP64 step kernel.
 template <int QLO, int QHI>
-void launch_band(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix) {
-  if (fix) {
+void launch_band(const BatchLaunch& a, int grid, int block, cudaStream_t s, int what) {
+  if (what == kBandFix) {
     k_batch_fix<QLO, QHI><<<grid, 128, 0, s>>>(a);
+    return;
+  }
+  if (what == kBandStepFP64) {
+    k_batch_semilag_fp64<QLO, QHI><<<grid, block, 0, s>>>(a);
     return;
   }
   constexpr size_t kMaxSmem = 2 * (size_t)(QHI + 1) * 256 * sizeof(float2);
@@ -219,21 +253,21 @@ void launch_band(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool
 }  // namespace tbg
 
 namespace tbg {
-void launch_batch_band_0(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
-void launch_batch_band_1(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
-void launch_batch_band_2(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
-void launch_batch_band_3(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
-void launch_batch_band_4(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
-void launch_batch_band_5(const BatchLaunch& a, int grid, int block, cudaStream_t s, bool fix);
+void launch_batch_band_0(const BatchLaunch& a, int grid, int block, cudaStream_t s, int what);
+void launch_batch_band_1(const BatchLaunch& a, int grid, int block, cudaStream_t s, int what);
+void launch_batch_band_2(const BatchLaunch& a, int grid, int block, cudaStream_t s, int what);
+void launch_batch_band_3(const BatchLaunch& a, int grid, int block, cudaStream_t s, int what);
+void launch_batch_band_4(const BatchLaunch& a, int grid, int block, cudaStream_t s, int what);
+void launch_batch_band_5(const BatchLaunch& a, int grid, int block, cudaStream_t s, int what);
 inline void launch_batch_band(int band, const BatchLaunch& a, int grid, int block,
-                              cudaStream_t s, bool fix) {
+                              cudaStream_t s, int what) {
   switch (band) {
-    case 0: launch_batch_band_0(a, grid, block, s, fix); break;
-    case 1: launch_batch_band_1(a, grid, block, s, fix); break;
-    case 2: launch_batch_band_2(a, grid, block, s, fix); break;
-    case 3: launch_batch_band_3(a, grid, block, s, fix); break;
-    case 4: launch_batch_band_4(a, grid, block, s, fix); break;
-    default: launch_batch_band_5(a, grid, block, s, fix); break;
+    case 0: launch_batch_band_0(a, grid, block, s, what); break;
+    case 1: launch_batch_band_1(a, grid, block, s, what); break;
+    case 2: launch_batch_band_2(a, grid, block, s, what); break;
+    case 3: launch_batch_band_3(a, grid, block, s, what); break;
+    case 4: launch_batch_band_4(a, grid, block, s, what); break;
+    default: launch_batch_band_5(a, grid, block, s, what); break;
   }
 }
 }  // namespace tbg

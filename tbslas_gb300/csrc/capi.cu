@@ -162,7 +162,8 @@ struct tbslas_ctx_s {
   uint32_t* d_err = nullptr;
   DevBuf slots[kNumSlots];
   double* d_F[TBSLAS_MAX_DEGREE + 1] = {};  // separable refit factors per degree
-  int sums = TBSLAS_SUMS_DOUBLE_FLOAT;       // arithmetic of the in-situ step's sums
+  int sums = TBSLAS_SUMS_FP64;  // arithmetic of the SL steps' Chebyshev sums
+  uint32_t wait_limit = kWaitLimit;  // polls of the bounded device-side waits
   bool profile = false;
   int64_t* h_pinned = nullptr;  // small pinned host buffer for scalar read-backs
   std::vector<ProfRecord> prof_pending;
@@ -266,6 +267,12 @@ int bind(tbslas_ctx ctx) {
   CUDA_TRY(cudaSetDevice(ctx->device));
   return TBSLAS_OK;
 }
+
+// Binds the context's device for the rest of the entry point and restores
+// the caller's current device when it returns.
+#define BIND(c)                        \
+  DeviceRestore device_restore_;       \
+  TRY(bind(c))
 
 // Grow-only scratch buffer.  Growing frees the old block (cudaFree waits for
 // the device), so no in-flight kernel can still be using it.
@@ -530,6 +537,7 @@ int eval_tree_dev(tbslas_ctx ctx, tbslas_tree tree, const double* pos, int64_t n
   a.periodic = bc;
   a.out = out;
   a.err = ctx->d_err;
+  a.wait_limit = ctx->wait_limit;
   a.grid = (int)std::min<int64_t>(max_tiles, (int64_t)ctx->num_sms * 8);
   ProfScope p(ctx, "eval_tiles", s);
   g_kernels[tree->q].eval_tiles(a, s);
@@ -1214,7 +1222,7 @@ int tree_construct(tbslas_ctx ctx, tbslas_tree t, const tbslas_field* f, const d
 
 template <class T>
 int fma_peak(tbslas_ctx ctx, int iters, double* flops_per_s) {
-  TRY(bind(ctx));
+  BIND(ctx);
   if (!flops_per_s) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
   const int blocks = ctx->num_sms * 8, threads = 256;
   double* out;
@@ -1277,6 +1285,7 @@ int bucketed_eval_on(const BucketScratch& b, tbslas_tree tree, const double* pos
   a.periodic = bc;
   a.out = out;
   a.err = tree->ctx->d_err;
+  a.wait_limit = tree->ctx->wait_limit;
   a.grid = (int)std::min<int64_t>(max_tiles, (int64_t)tree->ctx->num_sms * 8);
   g_kernels[tree->q].eval_tiles(a, s);
   return check_launch("eval_tiles");
@@ -1325,7 +1334,7 @@ int ctx_wnode_scratch(tbslas_ctx ctx, size_t n, double** out) {
 int ctx_vn_scratch(tbslas_ctx ctx, size_t n, double** out) { return scratch_t(ctx, kVN, n, out); }
 
 int ctx_F(tbslas_ctx ctx, int q, const double** F) {
-  TRY(bind(ctx));
+  BIND(ctx);
   return device_F(ctx, q, F);
 }
 
@@ -1367,6 +1376,7 @@ int tbslas_ctx_create(int device, tbslas_ctx* out) {
   CUDA_TRY(cudaGetDeviceCount(&ndev));
   if (device < 0 || device >= ndev)
     return fail(TBSLAS_ERR_INVALID_ARG, "device %d outside [0,%d)", device, ndev);
+  DeviceRestore restore;
   CUDA_TRY(cudaSetDevice(device));
   tbslas_ctx c = new tbslas_ctx_s();
   c->device = device;
@@ -1384,6 +1394,7 @@ int tbslas_ctx_create(int device, tbslas_ctx* out) {
 
 int tbslas_ctx_destroy(tbslas_ctx ctx) {
   if (!ctx) return TBSLAS_OK;
+  DeviceRestore restore;
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
   for (auto& b : ctx->slots)
@@ -1400,7 +1411,7 @@ int tbslas_ctx_destroy(tbslas_ctx ctx) {
 }
 
 int tbslas_ctx_check(tbslas_ctx ctx, uint32_t* device_error) {
-  TRY(bind(ctx));
+  BIND(ctx);
   CUDA_TRY(cudaDeviceSynchronize());
   uint32_t e = 0;
   CUDA_TRY(cudaMemcpy(&e, ctx->d_err, sizeof(e), cudaMemcpyDeviceToHost));
@@ -1411,20 +1422,20 @@ int tbslas_ctx_check(tbslas_ctx ctx, uint32_t* device_error) {
 }
 
 int tbslas_profile_enable(tbslas_ctx ctx, int enable) {
-  TRY(bind(ctx));
+  BIND(ctx);
   ctx->profile = enable != 0;
   return TBSLAS_OK;
 }
 
 int tbslas_profile_reset(tbslas_ctx ctx) {
-  TRY(bind(ctx));
+  BIND(ctx);
   prof_collect(ctx);
   ctx->prof_totals.clear();
   return TBSLAS_OK;
 }
 
 int tbslas_profile_count(tbslas_ctx ctx, int* n) {
-  TRY(bind(ctx));
+  BIND(ctx);
   if (!n) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
   prof_collect(ctx);
   *n = (int)ctx->prof_totals.size();
@@ -1433,7 +1444,7 @@ int tbslas_profile_count(tbslas_ctx ctx, int* n) {
 
 int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launches,
                        int64_t* kernels, double* total_ms) {
-  TRY(bind(ctx));
+  BIND(ctx);
   prof_collect(ctx);
   if (i < 0 || i >= (int)ctx->prof_totals.size())
     return fail(TBSLAS_ERR_INVALID_ARG, "profile index %d", i);
@@ -1446,22 +1457,28 @@ int tbslas_profile_get(tbslas_ctx ctx, int i, const char** name, int64_t* launch
 }
 
 int tbslas_ctx_set_sums(tbslas_ctx ctx, int mode) {
-  TRY(bind(ctx));
+  BIND(ctx);
   if (mode != TBSLAS_SUMS_DOUBLE_FLOAT && mode != TBSLAS_SUMS_FP64)
     return fail(TBSLAS_ERR_INVALID_ARG, "sums mode %d", mode);
   ctx->sums = mode;
   return TBSLAS_OK;
 }
 
+int tbslas_ctx_set_wait_limit(tbslas_ctx ctx, uint32_t polls) {
+  BIND(ctx);
+  ctx->wait_limit = polls;
+  return TBSLAS_OK;
+}
+
 int tbslas_ctx_get_sums(tbslas_ctx ctx, int* mode) {
-  TRY(bind(ctx));
+  BIND(ctx);
   if (!mode) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
   *mode = ctx->sums;
   return TBSLAS_OK;
 }
 
 int tbslas_ctx_last_fp64_targets(tbslas_ctx ctx, int64_t* n) {
-  TRY(bind(ctx));
+  BIND(ctx);
   if (!n) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
   *n = 0;
   if (!ctx->slots[kFixCount].p) return TBSLAS_OK;
@@ -1500,7 +1517,7 @@ int tbslas_tree_create(tbslas_ctx ctx, int64_t n_leaves, const double* anchor_ho
                        const int32_t* depth_host, int q, int dof, tbslas_tree* out) {
   if (!out) return fail(TBSLAS_ERR_INVALID_ARG, "null output pointer");
   *out = nullptr;
-  TRY(bind(ctx));
+  BIND(ctx);
   if (n_leaves < 1 || n_leaves > (int64_t)INT32_MAX)
     return fail(TBSLAS_ERR_INVALID_ARG, "leaf count %lld", (long long)n_leaves);
   if (!anchor_host || !depth_host) return fail(TBSLAS_ERR_INVALID_ARG, "null leaf arrays");
@@ -1527,6 +1544,7 @@ int tbslas_tree_create(tbslas_ctx ctx, int64_t n_leaves, const double* anchor_ho
 
 int tbslas_tree_destroy(tbslas_tree t) {
   if (!t) return TBSLAS_OK;
+  DeviceRestore restore;
   if (t->ctx) cudaSetDevice(t->ctx->device);
   if (t->d_keys) cudaFree(t->d_keys);
   if (t->d_geom) cudaFree(t->d_geom);
@@ -1541,7 +1559,7 @@ int tbslas_tree_destroy(tbslas_tree t) {
 int tbslas_tree_remesh(tbslas_ctx ctx, tbslas_tree tree, double tol, int min_depth,
                        int max_depth, int bc, int64_t* stats) {
   TRY(check_tree(tree));
-  TRY(bind(ctx));
+  BIND(ctx);
   if (tree->ctx != ctx) return fail(TBSLAS_ERR_INVALID_ARG, "tree belongs to another context");
   if (!(tol >= 0.0))  // +inf: refine nothing
     return fail(TBSLAS_ERR_INVALID_ARG, "tolerance %g is negative or NaN", tol);
@@ -1555,7 +1573,7 @@ int tbslas_tree_remesh(tbslas_ctx ctx, tbslas_tree tree, double tol, int min_dep
 int tbslas_tree_fit_field(tbslas_ctx ctx, tbslas_tree tree, const tbslas_field* field,
                           void* stream) {
   TRY(check_tree(tree));
-  TRY(bind(ctx));
+  BIND(ctx);
   if (tree->ctx != ctx) return fail(TBSLAS_ERR_INVALID_ARG, "tree belongs to another context");
   cudaStream_t s = (cudaStream_t)stream;
   const double* prm = nullptr;
@@ -1572,7 +1590,7 @@ int tbslas_tree_construct(tbslas_ctx ctx, const tbslas_field* field, int q, doub
                           int min_depth, int max_depth, int bc, tbslas_tree* out) {
   if (!out) return fail(TBSLAS_ERR_INVALID_ARG, "null output pointer");
   *out = nullptr;
-  TRY(bind(ctx));
+  BIND(ctx);
   if (q < 1 || q > TBSLAS_MAX_DEGREE)
     return fail(TBSLAS_ERR_UNSUPPORTED, "Chebyshev degree %d outside [1,%d]", q,
                 TBSLAS_MAX_DEGREE);
@@ -1606,7 +1624,7 @@ int tbslas_tree_construct(tbslas_ctx ctx, const tbslas_field* field, int q, doub
 
 int tbslas_tree_get_leaves(tbslas_tree t, double* anchor_host, int32_t* depth_host) {
   TRY(check_tree(t));
-  TRY(bind(t->ctx));
+  BIND(t->ctx);
   if (!anchor_host || !depth_host) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
   CUDA_TRY(cudaDeviceSynchronize());  // queued work may still change the leaves
   std::vector<Geom> g(t->L);
@@ -1631,7 +1649,7 @@ int tbslas_tree_info(tbslas_tree t, int64_t* n_leaves, int* q, int* dof, int* ma
 
 int tbslas_tree_set_coeffs_host(tbslas_tree t, const double* coeff_host) {
   TRY(check_tree(t));
-  TRY(bind(t->ctx));
+  BIND(t->ctx);
   if (!coeff_host) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
   CUDA_TRY(cudaDeviceSynchronize());  // queued work on any stream may still use the tree
   TRY(copy_coeffs(t, t->d_coeff, coeff_host, true, cudaMemcpyHostToDevice, t->ctx->stream));
@@ -1641,7 +1659,7 @@ int tbslas_tree_set_coeffs_host(tbslas_tree t, const double* coeff_host) {
 
 int tbslas_tree_get_coeffs_host(tbslas_tree t, double* coeff_host) {
   TRY(check_tree(t));
-  TRY(bind(t->ctx));
+  BIND(t->ctx);
   if (!coeff_host) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
   CUDA_TRY(cudaDeviceSynchronize());
   TRY(copy_coeffs(t, coeff_host, t->d_coeff, false, cudaMemcpyDeviceToHost, t->ctx->stream));
@@ -1651,7 +1669,7 @@ int tbslas_tree_get_coeffs_host(tbslas_tree t, double* coeff_host) {
 
 int tbslas_tree_set_coeffs(tbslas_tree t, const double* coeff_dev, void* stream) {
   TRY(check_tree(t));
-  TRY(bind(t->ctx));
+  BIND(t->ctx);
   if (!coeff_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
   return copy_coeffs(t, t->d_coeff, coeff_dev, true, cudaMemcpyDeviceToDevice,
                      (cudaStream_t)stream);
@@ -1659,7 +1677,7 @@ int tbslas_tree_set_coeffs(tbslas_tree t, const double* coeff_dev, void* stream)
 
 int tbslas_tree_get_coeffs(tbslas_tree t, double* coeff_dev, void* stream) {
   TRY(check_tree(t));
-  TRY(bind(t->ctx));
+  BIND(t->ctx);
   if (!coeff_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
   return copy_coeffs(t, coeff_dev, t->d_coeff, false, cudaMemcpyDeviceToDevice,
                      (cudaStream_t)stream);
@@ -1667,7 +1685,7 @@ int tbslas_tree_get_coeffs(tbslas_tree t, double* coeff_dev, void* stream) {
 
 int tbslas_collect_grid_points(tbslas_ctx ctx, tbslas_tree tree, double* out_dev, void* stream) {
   TRY(check_tree(tree));
-  TRY(bind(ctx));
+  BIND(ctx);
   if (!out_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null output");
   return collect_dev(tree, out_dev, (cudaStream_t)stream);
 }
@@ -1675,7 +1693,7 @@ int tbslas_collect_grid_points(tbslas_ctx ctx, tbslas_tree tree, double* out_dev
 int tbslas_eval_tree(tbslas_ctx ctx, tbslas_tree tree, const double* pos_dev, int64_t n,
                      double* out_dev, int bc, void* stream) {
   TRY(check_tree(tree));
-  TRY(bind(ctx));
+  BIND(ctx);
   if (n < 0) return fail(TBSLAS_ERR_INVALID_ARG, "negative point count");
   if (n > 0 && (!pos_dev || !out_dev)) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
   if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
@@ -1686,7 +1704,7 @@ int tbslas_eval_tree_on_nodes(tbslas_ctx ctx, tbslas_tree src, tbslas_tree dst, 
                               int bc, void* stream) {
   TRY(check_tree(src));
   TRY(check_tree(dst));
-  TRY(bind(ctx));
+  BIND(ctx);
   if (src->ctx != ctx || dst->ctx != ctx)
     return fail(TBSLAS_ERR_INVALID_ARG, "trees belong to another context");
   if (!out_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
@@ -1700,7 +1718,7 @@ int tbslas_eval_tree_on_nodes(tbslas_ctx ctx, tbslas_tree src, tbslas_tree dst, 
 int tbslas_eval_tree_host(tbslas_ctx ctx, tbslas_tree tree, const double* pos_host, int64_t n,
                           double* out_host, int bc) {
   TRY(check_tree(tree));
-  TRY(bind(ctx));
+  BIND(ctx);
   if (n < 0) return fail(TBSLAS_ERR_INVALID_ARG, "negative point count");
   if (n == 0) return TBSLAS_OK;
   if (!pos_host || !out_host) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
@@ -1722,7 +1740,7 @@ int tbslas_traj_rk2(tbslas_ctx ctx, tbslas_tree vel, const double* x_dev, int64_
                     double tinit, double tfinal, int nrk, int bc, double* xdep_dev,
                     void* stream) {
   TRY(check_tree(vel));
-  TRY(bind(ctx));
+  BIND(ctx);
   if (vel->dof != 3) return fail(TBSLAS_ERR_INVALID_ARG, "velocity tree has dof %d, not 3", vel->dof);
   if (n < 0 || nrk < 1) return fail(TBSLAS_ERR_INVALID_ARG, "n=%lld nrk=%d", (long long)n, nrk);
   if (n > 0 && (!x_dev || !xdep_dev)) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
@@ -1735,7 +1753,7 @@ int tbslas_traj_rk2(tbslas_ctx ctx, tbslas_tree vel, const double* x_dev, int64_
 int tbslas_traj_rk2_host(tbslas_ctx ctx, tbslas_tree vel, const double* x_host, int64_t n,
                          double tinit, double tfinal, int nrk, int bc, double* xdep_host) {
   TRY(check_tree(vel));
-  TRY(bind(ctx));
+  BIND(ctx);
   if (vel->dof != 3) return fail(TBSLAS_ERR_INVALID_ARG, "velocity tree has dof %d, not 3", vel->dof);
   if (n < 0 || nrk < 1) return fail(TBSLAS_ERR_INVALID_ARG, "n=%lld nrk=%d", (long long)n, nrk);
   if (n == 0) return TBSLAS_OK;
@@ -1756,7 +1774,7 @@ int tbslas_traj_rk2_host(tbslas_ctx ctx, tbslas_tree vel, const double* x_host, 
 int tbslas_set_tree_grid_values(tbslas_ctx ctx, tbslas_tree tree, const double* vals_dev,
                                 void* stream) {
   TRY(check_tree(tree));
-  TRY(bind(ctx));
+  BIND(ctx);
   if (!vals_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null values");
   return refit_dev(ctx, tree, vals_dev, (cudaStream_t)stream);
 }
@@ -1777,6 +1795,7 @@ static int check_step_args(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, dou
 
 int tbslas_semilag_in_situ(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
                            double dt, int nrk, int bc, void* stream) {
+  DeviceRestore restore;
   TRY(check_step_args(ctx, vel, con, dt, nrk, bc));
   return semilag_in_situ_dev(ctx, vel, con, timestep, dt, nrk, bc, (cudaStream_t)stream);
 }
@@ -1786,6 +1805,7 @@ int tbslas_semilag_in_situ(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int
 int tbslas_semilag_bdf2(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con_prev,
                         tbslas_tree con_cur, tbslas_tree con_next, double t, double dt, int nrk,
                         int bc, void* stream) {
+  DeviceRestore restore;
   TRY(check_step_args(ctx, vel, con_cur, dt, nrk, bc));
   TRY(check_tree(con_prev));
   TRY(check_tree(con_next));
@@ -1848,6 +1868,7 @@ int tbslas_cubic_time_weights(const double* times, double t, double* w) {
 int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, const double* w,
                               tbslas_tree con, int timestep, double dt, int nrk, int bc,
                               void* stream) {
+  DeviceRestore restore;
   if (m < 1 || m > kTvMaxTrees)
     return fail(TBSLAS_ERR_INVALID_ARG, "%d velocity trees (1..%d)", m, kTvMaxTrees);
   if (!vel || !w) return fail(TBSLAS_ERR_INVALID_ARG, "null pointer");
@@ -2015,6 +2036,7 @@ extern "C" {
 int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
                                 double* con_coeff_host, int timestep, double dt, int nrk,
                                 int bc) {
+  DeviceRestore restore;
   TRY(check_step_args(ctx, vel, con, dt, nrk, bc));
   if (!con_coeff_host) return fail(TBSLAS_ERR_INVALID_ARG, "null coefficients");
   CUDA_TRY(cudaDeviceSynchronize());  // queued work on any stream may still use the trees
@@ -2028,7 +2050,7 @@ int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con
 
 int tbslas_fast_interp(tbslas_ctx ctx, const double* grid_dev, int dof, int n_reg,
                        const double* pts_dev, int64_t n, double* out_dev, int bc, void* stream) {
-  TRY(bind(ctx));
+  BIND(ctx);
   if (n_reg < 4) return fail(TBSLAS_ERR_INVALID_ARG, "grid size %d < 4", n_reg);
   if ((int64_t)n_reg * n_reg * n_reg > (int64_t)1 << 40)
     return fail(TBSLAS_ERR_SIZE, "grid size %d too large", n_reg);
@@ -2058,6 +2080,7 @@ static int check_grid_args(tbslas_ctx ctx, const void* vel, const void* con, con
 int tbslas_semilag_grid(tbslas_ctx ctx, const double* vel_dev, const double* con_dev,
                         double* con_out_dev, int n_reg, double dt, int nrk, int bc,
                         void* stream) {
+  DeviceRestore restore;
   TRY(check_grid_args(ctx, vel_dev, con_dev, con_out_dev, n_reg, dt, nrk, bc));
   const double tau = (-dt - 0.0) / nrk;
   return semilag_grid_dev(ctx, vel_dev, con_dev, con_out_dev, n_reg, tau, nrk, bc,
@@ -2066,6 +2089,7 @@ int tbslas_semilag_grid(tbslas_ctx ctx, const double* vel_dev, const double* con
 
 int tbslas_semilag_grid_host(tbslas_ctx ctx, const double* vel_host, const double* con_host,
                              double* con_out_host, int n_reg, double dt, int nrk, int bc) {
+  DeviceRestore restore;
   TRY(check_grid_args(ctx, vel_host, con_host, con_out_host, n_reg, dt, nrk, bc));
   CUDA_TRY(cudaDeviceSynchronize());  // earlier queued work may still use the scratch
   const int64_t n3 = (int64_t)n_reg * n_reg * n_reg;

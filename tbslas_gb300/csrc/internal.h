@@ -8,6 +8,26 @@
 
 namespace tbg {
 
+// Entry points make their context's device current for their own work and
+// put the calling thread's previous current device back when they return
+// (on every return path), so a host application that drives several
+// devices from one thread keeps its own choice of device.
+struct DeviceRestore {
+  int prev = -1;
+  DeviceRestore() {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+    }
+  }
+  ~DeviceRestore() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+  DeviceRestore(const DeviceRestore&) = delete;
+  DeviceRestore& operator=(const DeviceRestore&) = delete;
+};
+
 // One tile of the bucketed functor evaluation: `count` (<= kTile) points of
 // one leaf, stored at perm[start, start+count).
 struct Tile {
@@ -46,6 +66,11 @@ struct TrajArgs {
   double* xdep;
 };
 
+// Polls of a bounded device-side wait before it gives up and sets
+// kErrBarrierTimeout (each poll is an mbarrier try_wait, which itself blocks
+// for a hardware-defined time slice).
+constexpr uint32_t kWaitLimit = 1u << 22;
+
 struct EvalTilesArgs {
   TreeView tree;
   const double* pos;
@@ -56,6 +81,7 @@ struct EvalTilesArgs {
   double* out;
   uint32_t* err;
   int grid;
+  uint32_t wait_limit;  // polls of the wait for each tile's coefficient copy
 };
 
 // Scratch of one bucketed tree evaluation, carved by the caller.
@@ -242,7 +268,7 @@ struct RefitItem {
   int64_t row;
 };
 void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_items, int max_q,
-                        cudaStream_t s);
+                        bool df_sums, cudaStream_t s);
 void launch_split(const double* c, float2* c2, int64_t n, uint32_t* err, cudaStream_t s);
 uint32_t* ctx_err(tbslas_ctx ctx);
 int ctx_sums(tbslas_ctx ctx);

@@ -2,16 +2,16 @@
 //
 // Some callers cannot allocate device memory when they evaluate: code that
 // runs under a fixed memory budget decided up front (a real-time or embedded
-// solver loop), code whose host application owns every device allocation
+// solver loop), and code whose host application owns every device allocation
 // through its own pool and forbids library-side cudaMalloc/cudaFree (both can
-// synchronise the device and fragment the pool), and code that records its
-// work into a stream capture, where a cudaMalloc would break the capture.
-// For them this entry point keeps its scratch (per-point leaf ids, per-leaf
-// counts and offsets, the permutation and the tile list) in one file-scope
-// device array of fixed size, TBSLAS_NOALLOC_SCRATCH_BYTES, which the CUDA
-// module reserves on every GPU that loads this library until the process
-// exits.  The entry point itself calls no cudaMalloc, cudaFree or allocating
-// library routine.
+// synchronise the device and fragment the pool).  For them this entry point
+// keeps its scratch (per-point leaf ids, per-leaf counts and offsets, the
+// permutation and the tile list) in one file-scope device array of fixed
+// size, TBSLAS_NOALLOC_SCRATCH_BYTES, which the CUDA module reserves on every
+// GPU that loads this library until the process exits.  The entry point
+// itself calls no cudaMalloc, cudaFree or allocating library routine.
+#include <cuda.h>  // CUcontext/CUresult types; the two driver calls come through the runtime
+
 #include <mutex>
 
 #include "internal.h"
@@ -43,22 +43,66 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[TBSLAS_NOALLOC_
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_scratch_dev[kMaxDevices] = {};
+struct ScratchAddress {
+  void* ptr = nullptr;
+  unsigned long long context_id = 0;  // context the address was looked up in
+};
+ScratchAddress g_scratch_dev[kMaxDevices];
 
-// Once per device, with that device current: the device address of the array.
+// Process-unique id of the calling thread's current context (0 when the
+// driver cannot tell).  The driver never reuses an id, so a primary context
+// that the host application destroyed (cudaDeviceReset) and the runtime
+// created anew reads as a different context, and the array's address is
+// looked up again in it.  The two driver functions are reached through the
+// runtime's entry-point table; the library does not link the driver library.
+unsigned long long current_context_id() {
+  typedef CUresult (*GetCurrentFn)(CUcontext*);
+  typedef CUresult (*GetIdFn)(CUcontext, unsigned long long*);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {  // under g_setup_mutex
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetIdFn>(f);
+    cudaGetLastError();
+    looked_up = true;
+  }
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c ||
+      get_id(c, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// Set-up, once per device and context, with that device current: the device
+// address of the array (host code only knows a stand-in symbol for it).
 int scratch_address(int device, unsigned char** out) {
   if (device < 0 || device >= kMaxDevices)
     return tbg::fail_status(TBSLAS_ERR_UNSUPPORTED, "device index outside the supported range");
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_dev[device]) {
+  const unsigned long long id = current_context_id();
+  ScratchAddress& a = g_scratch_dev[device];
+  if (!a.ptr || a.context_id != id) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      a.ptr = nullptr;
       return tbg::fail_status(TBSLAS_ERR_CUDA,
                               "cudaGetSymbolAddress of the no-alloc scratch array failed");
-    g_scratch_dev[device] = p;
+    }
+    a.ptr = p;
+    a.context_id = id;
   }
-  *out = static_cast<unsigned char*>(g_scratch_dev[device]);
+  *out = static_cast<unsigned char*>(a.ptr);
   return TBSLAS_OK;
 }
 
@@ -83,6 +127,7 @@ extern "C" int tbslas_eval_tree_noalloc(tbslas_tree tree, const double* pos_dev,
     return tbg::fail_status(TBSLAS_ERR_INVALID_ARG, "null buffer");
   if (bc != TBSLAS_BC_FREESPACE && bc != TBSLAS_BC_PERIODIC)
     return tbg::fail_status(TBSLAS_ERR_INVALID_ARG, "invalid boundary condition");
+  tbg::DeviceRestore restore;
   if (cudaSetDevice(device) != cudaSuccess)
     return tbg::fail_status(TBSLAS_ERR_CUDA, "cudaSetDevice failed");
   unsigned char* base = nullptr;

@@ -324,7 +324,7 @@ void allow_smem(K kernel, std::atomic<uint64_t>& done) {
 }
 
 std::atomic<uint64_t> g_smem_refit{0}, g_smem_refit_df{0}, g_smem_refit_t{0},
-    g_smem_refit_t_df{0}, g_smem_batch{0};
+    g_smem_refit_t_df{0}, g_smem_batch{0}, g_smem_batch_f64{0};
 
 }  // namespace
 
@@ -357,11 +357,17 @@ void launch_refit_t(const double* lam, const double* F, int q, int64_t rows, dou
 }
 
 void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_items, int max_q,
-                        cudaStream_t s) {
+                        bool df_sums, cudaStream_t s) {
   if (n_items <= 0) return;
-  allow_smem(k_batch_refit<ArithDF>, g_smem_batch);
-  k_batch_refit<ArithDF><<<(unsigned)n_items, kRefitThreads, refit_smem(max_q), s>>>(jobs,
-                                                                                     items);
+  if (df_sums) {
+    allow_smem(k_batch_refit<ArithDF>, g_smem_batch);
+    k_batch_refit<ArithDF><<<(unsigned)n_items, kRefitThreads, refit_smem(max_q), s>>>(jobs,
+                                                                                       items);
+  } else {
+    allow_smem(k_batch_refit<ArithF64>, g_smem_batch_f64);
+    k_batch_refit<ArithF64><<<(unsigned)n_items, kRefitThreads, refit_smem(max_q), s>>>(jobs,
+                                                                                        items);
+  }
 }
 
 // Split FP64 coefficients into their double-float form.

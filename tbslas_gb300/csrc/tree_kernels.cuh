@@ -54,8 +54,6 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
-constexpr uint32_t kWaitLimit = 1u << 22;
-
 // ---------------------------------------------------------------------------
 // nrk midpoint-RK2 sub-steps of (x,y,z) through the velocity tree:
 //   V = v(X); X* = X + tau/2 V; V = v(X*); X = X + tau V
@@ -372,7 +370,7 @@ __global__ void __launch_bounds__(kTile) k_eval_tiles(const EvalTilesArgs a) {
       cheb_T<D>((y - g.y) * g.w - 1.0, ty);
       cheb_T<D>((z - g.z) * g.w - 1.0, tz);
     }
-    const bool timed_out = !mbar_wait_bounded(&bar, parity, kWaitLimit);
+    const bool timed_out = !mbar_wait_bounded(&bar, parity, a.wait_limit);
     parity ^= 1u;
     if (__syncthreads_or(timed_out)) {
       if (threadIdx.x == 0) {

@@ -9,11 +9,46 @@ it is shallower than `max_depth`; leaves are then 2:1 balanced across faces,
 edges and corners.  Initial coefficients are the least-squares fit at the
 leaf's Chebyshev nodes (the SetTreeGridValues operator).
 """
+import contextlib
+
 import numpy as np
 
 from . import api
 
 KEY_BITS = 21
+
+
+class HostMath:
+    """Where host-side set-up takes the Chebyshev nodes of degree q
+    ((q+1)^3 x 3, new_nodes order) and the point-to-coefficient matrix M
+    (GetPt2CoeffMatrix) from: by default this library's own host routines
+    (tbslas_cheb_nodes / tbslas_pt2coeff_matrix)."""
+
+    def __init__(self, nodes=None, pt2coeff=None):
+        self.nodes = nodes or api.new_nodes
+        self.pt2coeff = pt2coeff or api.get_pt2coeff_matrix
+
+
+_math = HostMath()
+
+
+@contextlib.contextmanager
+def host_math(math):
+    """Builds trees and fits with `math` (a HostMath) inside the block."""
+    global _math
+    prev, _math = _math, math
+    try:
+        yield math
+    finally:
+        _math = prev
+
+
+def cheb_nodes(q):
+    return _math.nodes(q)
+
+
+def pt2coeff(q):
+    return _math.pt2coeff(q)
 
 
 def _spread3(v):
@@ -56,14 +91,14 @@ def split(anchor, depth):
 
 def leaf_nodes(anchor, depth, q):
     """Chebyshev nodes of every leaf [L*Np, 3] (CollectChebTreeGridPoints order)."""
-    nodes = api.new_nodes(q)
+    nodes = _math.nodes(q)
     h = np.ldexp(1.0, -depth.astype(np.int64))
     return (anchor[:, None, :] + h[:, None, None] * nodes[None, :, :]).reshape(-1, 3)
 
 
 def fit(fn, anchor, depth, q, dof, M=None):
     """[L, dof, Nc] coefficients of fn (pts[n,3] -> vals[n,dof]) on every leaf."""
-    M = api.get_pt2coeff_matrix(q) if M is None else M
+    M = _math.pt2coeff(q) if M is None else M
     L = depth.size
     np_ = (q + 1) ** 3
     vals = np.asarray(fn(leaf_nodes(anchor, depth, q)), dtype=np.float64).reshape(L, np_, dof)
@@ -122,7 +157,7 @@ def adaptive_tree(fn, q, dof, tol, min_depth, max_depth, balance=True, periodic=
     """Leaves refined by the coefficient-tail rule; returns (anchor, depth).
 
     fitter(anchor, depth) -> [L, dof, Nc] replaces fit(fn, ...) when given."""
-    M = api.get_pt2coeff_matrix(q) if M is None else M
+    M = _math.pt2coeff(q) if M is None else M
     anchor, depth = uniform_tree(min_depth)
     while True:
         c = fitter(anchor, depth) if fitter is not None else fit(fn, anchor, depth, q, dof, M)

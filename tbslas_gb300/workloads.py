@@ -48,20 +48,21 @@ def tree_uniform_q8():
                         "uniform depth-4 octree (4096 leaves), q=8, rotation + Gaussian")
 
 
-def tree_adaptive_q14(seed=SEED):
-    q, tol = 14, 1e-6
+def tree_adaptive_q14(seed=SEED, tol=1e-6, depths=(3, 8)):
+    q = 14
+    lo, hi = depths
     rng = np.random.default_rng(seed)
     blobs = fields.gaussian_blobs(rng, 4)
-    ca, cd = trees.adaptive_tree(blobs, q, 1, tol, 3, 8)
-    va, vd = trees.adaptive_tree(fields.taylor_green(), q, 3, tol, 3, 8)
+    ca, cd = trees.adaptive_tree(blobs, q, 1, tol, lo, hi)
+    va, vd = trees.adaptive_tree(fields.taylor_green(), q, 3, tol, lo, hi)
     M = None
     cc = trees.fit(blobs, ca, cd, q, 1, M)
     vc = trees.fit(fields.taylor_green(), va, vd, q, 3, M)
     finest = int(max(cd.max(), vd.max()))
     dt = 1.0 / (2.0 ** finest * q * q)
     wl = TreeWorkload("tree_adaptive_q14", (va, vd, vc), (ca, cd, cc), q, dt, 0,
-                      "adaptive octrees (tol 1e-6, depth 3..8), q=14, Taylor-Green + 4 "
-                      "Gaussians, CFL=1 on the finest leaf")
+                      "adaptive octrees (tol %g, depth %d..%d), q=14, Taylor-Green + 4 "
+                      "Gaussians, CFL=1 on the finest leaf" % (tol, lo, hi))
     wl.blobs = blobs
     return wl
 
@@ -206,8 +207,7 @@ def fourier_fitter(modes, q, M):
 
 
 def api_nodes(q):
-    from . import api
-    return api.new_nodes(q)
+    return trees.cheb_nodes(q)
 
 
 class BatchWorkload:
@@ -219,7 +219,6 @@ class BatchWorkload:
 
     def __init__(self, n=64, seed=SEED, qs=(8, 14), depths=(4, 7), tol=1e-5, min_depth=2,
                  name="batched_64", qlist=None):
-        from . import api
         rng = np.random.default_rng(seed)
         self.name, self.bc, self.problems = name, 1, []
         Ms = {}
@@ -228,7 +227,7 @@ class BatchWorkload:
             if qlist is not None:
                 q = int(qlist[i % len(qlist)])
             dmax = int(rng.integers(depths[0], depths[1] + 1))
-            M = Ms.setdefault(q, api.get_pt2coeff_matrix(q))
+            M = Ms.setdefault(q, trees.pt2coeff(q))
             modes = fields.fourier_modes(rng)
             blobs = fields.gaussian_blobs(rng, int(rng.integers(1, 9)))
             vfit = fourier_fitter(modes, q, M)

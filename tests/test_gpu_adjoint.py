@@ -65,7 +65,7 @@ def test_ckpt_step_matches_plain_step_and_oracle(ctx, ora):
                 assert np.abs(xd - ref).max() <= 1e-13
                 assert np.array_equal(leaf_of(xd), leaf_of(ref))
     finally:
-        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        ctx.sums = tb.SUMS_FP64  # the library default
 
 
 def _J(c, V, cobs):
@@ -178,7 +178,7 @@ def test_adjoint_matches_dual_number_oracle(ctx, ora, vel_kind, q):
 
 @pytest.mark.parametrize("checkpoint", [True, False])
 def test_adjoint_fp64_sums_matches_double_float(ctx, checkpoint):
-    """The all-FP64 adjoint kernel (TBSLAS_SUMS_FP64) and the default
+    """The all-FP64 adjoint kernel (TBSLAS_SUMS_FP64, the default) and the
     double-float one give the same gradients to 1e-12."""
     import torch
     a, d, q, vc, c0, cobs, tv, tc = _problem(ctx, q=6, seed=9)
@@ -194,6 +194,6 @@ def test_adjoint_fp64_sums_matches_double_float(ctx, checkpoint):
                co).backward()
             grads.append((c0t.grad.cpu().numpy(), vct.grad.cpu().numpy()))
     finally:
-        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        ctx.sums = tb.SUMS_FP64  # the library default
     for x, y in zip(grads[0], grads[1]):
         assert np.abs(x - y).max() <= 1e-12 * np.abs(y).max()

@@ -1,6 +1,8 @@
 """Batched in-situ SL (one persistent kernel per degree band per step, CUDA
 graph replay, autotuned launch parameters) against the per-problem loop of
-tbslas_semilag_in_situ calls: identical coefficients, bit for bit."""
+tbslas_semilag_in_situ calls in the same sums mode (FP64, the default, and
+double-float): identical coefficients, bit for bit.  The per-problem loop is
+itself checked against the oracle (test_gpu_tree.py)."""
 import numpy as np
 import pytest
 
@@ -25,16 +27,22 @@ def _trees(ctx, wl):
     return out
 
 
+MODES = {"fp64": tb.SUMS_FP64, "df": tb.SUMS_DOUBLE_FLOAT}
+
+
+@pytest.mark.parametrize("mode", ["fp64", "df"])
 @pytest.mark.parametrize("use_graph", [False, True])
-def test_batch_equals_per_problem_loop(ctx, small_batch, use_graph):
+def test_batch_equals_per_problem_loop(ctx, small_batch, use_graph, mode):
     import torch
     wl = small_batch
-    ref = _trees(ctx, wl)
-    for step in range(1, 4):
-        for tv, tc, dt in ref:
-            tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv, wl.bc), tc, step, dt)
-    got = _trees(ctx, wl)
-    b = tb.Batch(ctx, got, 1, wl.bc)
+    with ctx.sums_mode(MODES[mode]):
+        ref = _trees(ctx, wl)
+        for step in range(1, 4):
+            for tv, tc, dt in ref:
+                tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv, wl.bc), tc, step, dt)
+        got = _trees(ctx, wl)
+        b = tb.Batch(ctx, got, 1, wl.bc)
+    # the batch keeps the mode it was created in
     b.set_params(128, 256, 4)
     b.run(1, 2, use_graph)
     b.run(3, 1, use_graph)
@@ -45,15 +53,17 @@ def test_batch_equals_per_problem_loop(ctx, small_batch, use_graph):
     assert total == wl.points_per_step and items > len(wl.problems)
 
 
-def test_batch_graph_replay_and_autotune_keep_state(ctx, small_batch):
+@pytest.mark.parametrize("mode", ["fp64", "df"])
+def test_batch_graph_replay_and_autotune_keep_state(ctx, small_batch, mode):
     import torch
     wl = small_batch
-    ref = _trees(ctx, wl)
-    for step in range(1, 5):
-        for tv, tc, dt in ref:
-            tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv, wl.bc), tc, step, dt)
-    got = _trees(ctx, wl)
-    b = tb.Batch(ctx, got, 1, wl.bc)
+    with ctx.sums_mode(MODES[mode]):
+        ref = _trees(ctx, wl)
+        for step in range(1, 5):
+            for tv, tc, dt in ref:
+                tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv, wl.bc), tc, step, dt)
+        got = _trees(ctx, wl)
+        b = tb.Batch(ctx, got, 1, wl.bc)
     blk, tpi, cps = b.autotune()
     assert blk in (64, 128, 256) and tpi % blk == 0 and 1 <= cps <= 32
     assert b.params() == (blk, tpi, cps)

@@ -43,7 +43,7 @@ def test_bdf2_matches_oracle(ctx, ora, bc, mode):
         tb.solve_semilag_bdf2(tb.NodeFieldFunctor(tv, bc), tp, tcur, tn, t, dt)
         got = tn.get_coeffs()
     finally:
-        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        ctx.sums = tb.SUMS_FP64  # the library default
     per = bc == tb.Periodic
     ref = ora.semilag_bdf2(dict(anchor=av, depth=dv, q=q, dof=3, coeff=vc),
                            dict(anchor=ap, depth=dp, q=q, dof=1, coeff=cp),

@@ -54,9 +54,9 @@ def test_semilag_grid_matches_oracle(ctx, ora, bc, nrk, N):
 
 def test_semilag_grid_full_size_shift_and_sample(ctx, ora):
     """256^3 periodic: (1) a velocity that moves every departure point one
-    node reproduces the shifted field -- exactly with FP64 stencil sums, to
-    the double-float split (2^-48 relative per value) with the default
-    sums; (2) one step of the config's random Fourier field matches the
+    node reproduces the shifted field -- exactly with FP64 stencil sums (the
+    default), to the double-float split (2^-48 relative per value) with
+    double-float sums; (2) one step of the config's random Fourier field matches the
     oracle on a sample of nodes."""
     import torch
     N = 256
@@ -65,13 +65,11 @@ def test_semilag_grid_full_size_shift_and_sample(ctx, ora):
     vel = np.zeros((3, N, N, N))
     vel[1] = -0.5
     shifted = np.roll(con, -1, axis=1)
-    try:
-        ctx.sums = tb.SUMS_FP64
+    with ctx.sums_mode(tb.SUMS_FP64):
         out = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, 2.0 / N, 1, 1).cpu().numpy()
-    finally:
-        ctx.sums = tb.SUMS_DOUBLE_FLOAT
     assert np.array_equal(out, shifted)
-    out = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, 2.0 / N, 1, 1).cpu().numpy()
+    with ctx.sums_mode(tb.SUMS_DOUBLE_FLOAT):
+        out = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, 2.0 / N, 1, 1).cpu().numpy()
     assert np.all(np.abs(out - shifted) <= 2.0 ** -47 * np.abs(shifted))
     vel = fields.fourier_velocity_grid(rng, N)
     dt = 2.0 / N / np.abs(vel).max()
@@ -93,12 +91,10 @@ def test_semilag_grid_nan_velocity_matches_fp64_sums(ctx, N):
     vel[0, 3, 4, 5] = np.nan
     vel[2, 1, 7, 2] = np.inf
     dt = 1.5 / N
-    out = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, dt, 1, 1).cpu().numpy()
-    try:
-        ctx.sums = tb.SUMS_FP64
+    with ctx.sums_mode(tb.SUMS_DOUBLE_FLOAT):
+        out = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, dt, 1, 1).cpu().numpy()
+    with ctx.sums_mode(tb.SUMS_FP64):
         ref = tb.semilag_grid(ctx, _dev(vel), _dev(con), N, dt, 1, 1).cpu().numpy()
-    finally:
-        ctx.sums = tb.SUMS_DOUBLE_FLOAT
     assert np.array_equal(np.isnan(out), np.isnan(ref))
     ok = ~np.isnan(ref)
     assert np.abs(out[ok] - ref[ok]).max() <= 1e-13 * np.abs(ref[ok]).max()

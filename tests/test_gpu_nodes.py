@@ -60,8 +60,8 @@ def test_in_situ_step_first_stage_is_exact(ctx, ora):
 @pytest.mark.parametrize("bc", [0, 1])
 def test_in_situ_fp64_sums_mode(ctx, ora, bc):
     """TBSLAS_SUMS_FP64: every sum in FP64 -- matches the oracle to 1e-12 (the
-    refit's summation order is the only difference) and the default
-    double-float mode to 1e-12; the mode is a context setting."""
+    refit's summation order is the only difference) and the double-float
+    mode to 1e-12; the mode is a context setting, FP64 by default."""
     q = 8
     a, d = trees.adaptive_tree(fields.gaussian((0.45, 0.5, 0.52), 0.08), q, 1, 1e-4, 1, 3)
     vc = trees.fit(fields.taylor_green(), a, d, q, 3)
@@ -70,7 +70,7 @@ def test_in_situ_fp64_sums_mode(ctx, ora, bc):
     ref = ora.semilag_in_situ(dict(anchor=a, depth=d, q=q, dof=3, coeff=vc),
                               dict(anchor=a, depth=d, q=q, dof=1, coeff=cc), 2, 0.01, 1, bool(bc))
     got = {}
-    assert ctx.sums == tb.SUMS_DOUBLE_FLOAT
+    assert ctx.sums == tb.SUMS_FP64  # the library default
     try:
         for mode in (tb.SUMS_FP64, tb.SUMS_DOUBLE_FLOAT):
             ctx.sums = mode
@@ -78,7 +78,7 @@ def test_in_situ_fp64_sums_mode(ctx, ora, bc):
             tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv, bc), tc, 2, 0.01, 1)
             got[mode] = tc.get_coeffs()
     finally:
-        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        ctx.sums = tb.SUMS_FP64  # the library default
     scale = np.abs(ref).max()
     assert np.abs(got[tb.SUMS_FP64] - ref).max() <= 1e-12 * scale
     assert np.abs(got[tb.SUMS_DOUBLE_FLOAT] - ref).max() <= 1e-12 * scale

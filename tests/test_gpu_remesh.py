@@ -101,7 +101,7 @@ def test_step_after_remesh_matches_oracle(ctx, ora):
         got_a, got_d = tc.leaves()
         got = tc.get_coeffs()
     finally:
-        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        ctx.sums = tb.SUMS_FP64  # the library default
     vel = dict(anchor=av, depth=dv, q=q, dof=3, coeff=vc)
     ref1 = ora.semilag_in_situ(vel, dict(anchor=a, depth=d, q=q, dof=1, coeff=c), 1, 0.02)
     assert np.abs(c1 - ref1).max() <= 1e-12 * np.abs(ref1).max()

@@ -1,10 +1,11 @@
 """GPU parity of the tree path (C ABI -> CUDA) against the oracle.
 
 Tolerance: max |gpu - oracle| <= 1e-12 * max |oracle| (L-infinity relative)
-on coefficients of the in-situ step (its Chebyshev sums run in double-float;
-near-face targets are recomputed in FP64 so leaf choices match the oracle);
-bit-exact for the functor values and departure points (all FP64) and for the
-collected node coordinates."""
+on coefficients of the in-situ step, in both sums modes: FP64 (the default;
+only the refit's summation order differs from the oracle's) and
+double-float (near-face targets are recomputed in FP64, so leaf choices
+match the oracle's); bit-exact for the functor values and departure points
+(all FP64) and for the collected node coordinates."""
 import math
 
 import numpy as np
@@ -15,6 +16,7 @@ from tbslas_gb300 import capi, fields, trees
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
+MODES = {"fp64": tb.SUMS_FP64, "df": tb.SUMS_DOUBLE_FLOAT}
 
 
 def rel_err(a, b):
@@ -139,10 +141,11 @@ def _sl_case(kind, qv, qc, dofc, rng):
     return (av, dv, vc), (ac, dc, cc)
 
 
+@pytest.mark.parametrize("mode", ["fp64", "df"])
 @pytest.mark.parametrize("kind", ["uniform", "adaptive"])
 @pytest.mark.parametrize("qv,qc,dofc", [(8, 8, 1), (5, 5, 1), (6, 4, 1), (4, 4, 2)])
 @pytest.mark.parametrize("bc,nrk", [(0, 1), (1, 2)])
-def test_semilag_in_situ_matches_oracle(ctx, ora, kind, qv, qc, dofc, bc, nrk):
+def test_semilag_in_situ_matches_oracle(ctx, ora, kind, qv, qc, dofc, bc, nrk, mode):
     rng = np.random.default_rng(qv * 10 + qc)
     (av, dv, vc), (ac, dc, cc) = _sl_case(kind, qv, qc, dofc, rng)
     tv = tb.Tree(ctx, av, dv, qv, 3, vc)
@@ -151,13 +154,74 @@ def test_semilag_in_situ_matches_oracle(ctx, ora, kind, qv, qc, dofc, bc, nrk):
     ref_con = dict(anchor=ac, depth=dc, q=qc, dof=dofc, coeff=cc.copy())
     ref_vel = dict(anchor=av, depth=dv, q=qv, dof=3, coeff=vc)
     dt = 0.02
-    for step in (1, 2):
-        tb.solve_semilag_in_situ(vel, tc, step, dt, nrk)
-        ref_con["coeff"] = ora.semilag_in_situ(ref_vel, ref_con, step, dt, nrk, periodic=bool(bc))
-        assert rel_err(tc.get_coeffs(), ref_con["coeff"]) <= TOL, step
+    with ctx.sums_mode(MODES[mode]):
+        for step in (1, 2):
+            tb.solve_semilag_in_situ(vel, tc, step, dt, nrk)
+            ref_con["coeff"] = ora.semilag_in_situ(ref_vel, ref_con, step, dt, nrk,
+                                                   periodic=bool(bc))
+            assert rel_err(tc.get_coeffs(), ref_con["coeff"]) <= TOL, step
 
 
-def test_semilag_in_situ_stagnation_on_faces(ctx, ora):
+@pytest.mark.parametrize("mode", ["fp64", "df"])
+@pytest.mark.parametrize("bc", [0, 1])
+@pytest.mark.parametrize("q,dofc", [(9, 1), (11, 1), (12, 1), (12, 3), (14, 1), (16, 1)])
+def test_semilag_in_situ_high_degree_matches_oracle(ctx, ora, q, dofc, bc, mode):
+    """Degrees above 8 (each its own kernel instantiation; q = 14 is the
+    headline degree, q = 16 the largest supported) on adaptive trees: a
+    Taylor-Green velocity tree and a concentration tree refined around
+    seeded Gaussians, two steps against the oracle.  dofc = 3 takes the
+    general path (trajectory + bucketed functor + refit per dof)."""
+    rng = np.random.default_rng(100 + q)
+    av, dv = trees.adaptive_tree(fields.taylor_green(), 4, 3, 1e-2, 1, 2)
+    blobs = fields.gaussian_blobs(rng, 3, (0.05, 0.1))
+    ac, dc = trees.adaptive_tree(blobs, 4, 1, 1e-3, 1, 2)
+    vc = trees.fit(fields.taylor_green(), av, dv, q, 3)
+    cc = trees.fit(lambda p: np.repeat(blobs(p), dofc, axis=1) * (1 + np.arange(dofc)),
+                   ac, dc, q, dofc)
+    tv = tb.Tree(ctx, av, dv, q, 3, vc)
+    tc = tb.Tree(ctx, ac, dc, q, dofc, cc)
+    vel = tb.NodeFieldFunctor(tv, bc)
+    ref_vel = dict(anchor=av, depth=dv, q=q, dof=3, coeff=vc)
+    ref_con = dict(anchor=ac, depth=dc, q=q, dof=dofc, coeff=cc.copy())
+    dt = 1.0 / (2.0 ** int(max(dv.max(), dc.max())) * q * q)  # Chebyshev CFL 1
+    with ctx.sums_mode(MODES[mode]):
+        for step in (1, 2):
+            tb.solve_semilag_in_situ(vel, tc, step, dt, 1)
+            ref_con["coeff"] = ora.semilag_in_situ(ref_vel, ref_con, step, dt, 1,
+                                                   periodic=bool(bc))
+            assert rel_err(tc.get_coeffs(), ref_con["coeff"]) <= TOL, step
+
+
+@pytest.mark.parametrize("mode", ["fp64", "df"])
+def test_headline_shape_reduced_matches_oracle(ctx, ora, mode):
+    """The headline configuration's shape at a size the oracle finishes in
+    seconds: q = 14, a Taylor-Green velocity tree and a concentration tree
+    of 4 seeded Gaussians (sigma 0.03-0.08, centres U[0.2,0.8]^3), both
+    refined by the coefficient-tail rule (tolerance 1e-3, depths 2..3 instead
+    of 1e-6 and 3..8), FreeSpace, dt for Chebyshev CFL 1 on the finest leaf;
+    two steps against the oracle."""
+    from tbslas_gb300 import workloads
+    wl = workloads.tree_adaptive_q14(tol=1e-3, depths=(2, 3))
+    assert wl.q == 14 and wl.bc == 0 and int(wl.cd.max()) > int(wl.cd.min())
+    tv = tb.Tree(ctx, wl.va, wl.vd, wl.q, 3, wl.vc)
+    tc = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
+    vel = tb.NodeFieldFunctor(tv, wl.bc)
+    ref_vel = dict(anchor=wl.va, depth=wl.vd, q=wl.q, dof=3, coeff=wl.vc)
+    ref_con = dict(anchor=wl.ca, depth=wl.cd, q=wl.q, dof=1, coeff=wl.cc.copy())
+    with ctx.sums_mode(MODES[mode]):
+        for step in (1, 2):
+            tb.solve_semilag_in_situ(vel, tc, step, wl.dt, 1)
+            ref_con["coeff"] = ora.semilag_in_situ(ref_vel, ref_con, step, wl.dt, 1)
+            got = tc.get_coeffs()
+            assert rel_err(got, ref_con["coeff"]) <= TOL, step
+            if mode == "fp64" and step == 1:
+                # the FP64 mode's node values are the oracle's bit for bit; the
+                # coefficients differ only by the refit's summation order
+                assert rel_err(got, ref_con["coeff"]) <= 1e-14
+
+
+@pytest.mark.parametrize("mode", ["fp64", "df"])
+def test_semilag_in_situ_stagnation_on_faces(ctx, ora, mode):
     """Taylor-Green's velocity vanishes on planes that are leaf faces; at q=6
     the fit's error moves the nodes there off the face (at q=14 it does not,
     and those nodes make most of the near-face targets of that workload)."""
@@ -170,9 +234,10 @@ def test_semilag_in_situ_stagnation_on_faces(ctx, ora):
     tc = tb.Tree(ctx, anchor, depth, q, 1, cc)
     ref = dict(anchor=anchor, depth=depth, q=q, dof=1, coeff=cc)
     vel = dict(anchor=anchor, depth=depth, q=q, dof=3, coeff=vc)
-    for step in (1, 2, 3):
-        tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv), tc, step, 0.004)
-        ref["coeff"] = ora.semilag_in_situ(vel, ref, step, 0.004)
+    with ctx.sums_mode(MODES[mode]):
+        for step in (1, 2, 3):
+            tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv), tc, step, 0.004)
+            ref["coeff"] = ora.semilag_in_situ(vel, ref, step, 0.004)
     assert rel_err(tc.get_coeffs(), ref["coeff"]) <= TOL
 
 
@@ -198,11 +263,12 @@ def test_semilag_in_situ_strain_flow_near_face(ctx, ora, flow, bc):
     ref = dict(anchor=anchor, depth=depth, q=q, dof=1, coeff=cc)
     vel = dict(anchor=anchor, depth=depth, q=q, dof=3, coeff=vc)
     counts = []
-    for step in (1, 2):
-        tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv, bc), tc, step, 0.01)
-        ref["coeff"] = ora.semilag_in_situ(vel, ref, step, 0.01, periodic=bool(bc))
-        counts.append(ctx.last_fp64_targets())
-        assert rel_err(tc.get_coeffs(), ref["coeff"]) <= TOL, (step, counts)
+    with ctx.sums_mode(tb.SUMS_DOUBLE_FLOAT):
+        for step in (1, 2):
+            tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv, bc), tc, step, 0.01)
+            ref["coeff"] = ora.semilag_in_situ(vel, ref, step, 0.01, periodic=bool(bc))
+            counts.append(ctx.last_fp64_targets())
+            assert rel_err(tc.get_coeffs(), ref["coeff"]) <= TOL, (step, counts)
     assert all(n > 0 for n in counts), counts
 
 
@@ -219,7 +285,8 @@ def test_semilag_in_situ_host_equals_device(ctx):
     assert np.array_equal(host, dev)
 
 
-def test_config1_full_size_one_step_matches_oracle(ctx, ora):
+@pytest.mark.parametrize("mode", ["fp64", "df"])
+def test_config1_full_size_one_step_matches_oracle(ctx, ora, mode):
     """Depth-4 uniform tree (4096 leaves), q=8, rotation omega=2pi, Gaussian
     sigma=0.05 at (0.7,0.5,0.5), dt=0.01: one full SL step (2,985,984
     departure points) against the oracle."""
@@ -229,7 +296,8 @@ def test_config1_full_size_one_step_matches_oracle(ctx, ora):
     cc = trees.fit(fields.gaussian((0.7, 0.5, 0.5), 0.05), anchor, depth, q, 1)
     tv = tb.Tree(ctx, anchor, depth, q, 3, vc)
     tc = tb.Tree(ctx, anchor, depth, q, 1, cc)
-    tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv), tc, 1, 0.01)
+    with ctx.sums_mode(MODES[mode]):
+        tb.solve_semilag_in_situ(tb.NodeFieldFunctor(tv), tc, 1, 0.01)
     ref = ora.semilag_in_situ(dict(anchor=anchor, depth=depth, q=q, dof=3, coeff=vc),
                               dict(anchor=anchor, depth=depth, q=q, dof=1, coeff=cc), 1, 0.01)
     assert rel_err(tc.get_coeffs(), ref) <= TOL

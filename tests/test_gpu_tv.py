@@ -64,7 +64,7 @@ def test_tv_matches_oracle(ctx, ora, same, bc, mode, kind):
         tb.solve_semilag_in_situ_tv(f, tc, ts, dt)
         got = tc.get_coeffs()
     finally:
-        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        ctx.sums = tb.SUMS_FP64  # the library default
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
     for x in vt + [tc]:
         x.close()
@@ -101,4 +101,4 @@ def test_single_tree_weight_one_is_the_plain_step(ctx, mode):
         tb.solve_semilag_in_situ(tb.NodeFieldFunctor(vt[0]), t2, 1, 0.02)
         assert np.array_equal(tc.get_coeffs(), t2.get_coeffs())
     finally:
-        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        ctx.sums = tb.SUMS_FP64  # the library default
