@@ -219,9 +219,25 @@ def cpu_baseline_grid(wl, budget_s=12.0):
 
 
 # ---------------------------------------------------------------------------
-def run_reference(args, wl):
+def oracle_workload(name):
+    """The workload built with the oracle's own Chebyshev nodes and
+    pseudo-inverse (the reference arm loads nothing of the library under
+    test)."""
+    from oracle import oracle as ora
+    from tbslas_gb300 import trees
+    from tbslas_gb300.workloads import make
+
+    def nodes(q):
+        return ora.collect_grid_points(np.zeros((1, 3)), np.zeros(1, dtype=np.int32), q)
+    with trees.host_math(trees.HostMath(nodes=nodes, pt2coeff=ora.pt2coeff)):
+        return make(name)
+
+
+def run_reference(args, name):
     """--impl reference: the reference algorithm (oracle port, all host
-    threads) timed on bounded samples of the same workload, K steps."""
+    threads) timed on bounded samples of the same workload (a name, built
+    with the oracle's own set-up math, or a workload object), K steps."""
+    wl = oracle_workload(name) if isinstance(name, str) else name
     total_budget = 150.0
     per_step = total_budget / max(1, args.steps + args.warmup)
     timed_steps = args.steps
@@ -333,7 +349,7 @@ def run_reference(args, wl):
     line = {"metric": METRIC, "value": value, "unit": unit, "impl": "reference", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / timed_steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded analytic fields)", "config": wl.describe(),
+            "data": "synthetic (seeded analytic fields)", "config": describe_config(wl),
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -363,13 +379,59 @@ def GridWorkloadType():
 
 
 # ---------------------------------------------------------------------------
+def fused_flops_per_point_tree(q, nrk=1):
+    """Algorithmic FLOPs per target of the fused step kernel, counted as the
+    reference counts an evaluation (3*d*3 + 2*Nc*dof, src/tree/tree_functor.h:
+    389-394) and an RK2 update (2*3 per sub-step and stage, src/semilag/
+    traj.inc:44): the 2*nrk - 1 velocity evaluations after the first (the
+    first, at the target node itself, is the node-grid kernel's) and the
+    concentration at the departure point."""
+    d = q + 1
+    nc = d * (d + 1) * (d + 2) // 6
+    ev = lambda dof: 9 * d + 2 * nc * dof
+    return (2 * nrk - 1) * ev(3) + 18 * nrk + ev(1)
+
+
+def _traffic(wl_name, kernel):
+    """DRAM bytes per launch of `kernel` on workload `wl_name` from one ncu
+    capture (profiles/traffic.json), or None."""
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(tpath):
+        return None
+    return json.load(open(tpath)).get(wl_name, {}).get(kernel)
+
+
+def fp64_roofline(ctx, kernel, flops_per_point, points_per_launch, prof, name, steps,
+                  counting):
+    """roofline object of an FP64-pipe-bound kernel: its algorithmic FLOPs per
+    launch over its mean launch time (the profiler's brackets named `name`),
+    against the FP64 FMA peak measured in this run."""
+    groups, _, kms = prof.get(name, (0, 0, 0.0))
+    launch_ms = kms / max(groups, 1)
+    peak = ctx.fp64_fma_peak() / 1e12
+    achieved = flops_per_point * points_per_launch / (max(launch_ms, 1e-9) * 1e-3) / 1e12
+    return {"kernel": kernel, "bound": "fp64", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": "FP64 FMA throughput measured in this run (tbslas_fp64_fma_peak); "
+                           "MEASURED_PEAKS.json holds no FP64 figure",
+            "algorithmic_flops_per_point": flops_per_point, "counting": counting,
+            "launch_ms": launch_ms, "traffic": None,
+            "kernels_ms_per_step": {k: v[2] / steps for k, v in prof.items()}}
+
+
 def run_gpu(args, wl, rank, world, local_rank):
+    """The plain step (tree or grid workload) in the library's default FP64
+    arithmetic: K timed steps with inputs resident, a profiled pass for the
+    per-kernel split, the same step in the opt-in double-float mode, an
+    end-to-end pass through the host-buffer entry point, and (rank 0, N = 1)
+    the oracle on a bounded sample.  Returns the bench line on rank 0."""
     import torch
     import tbslas_gb300 as tb
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     ctx = tb.Context(local_rank)
+    assert ctx.sums == tb.SUMS_FP64
     stream = torch.cuda.current_stream()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     is_grid = isinstance(wl, GridWorkloadType())
@@ -380,123 +442,95 @@ def run_gpu(args, wl, rank, world, local_rank):
         con0 = torch.from_numpy(wl.con).to(dev)
         bufs = [con0.clone(), torch.empty_like(con0)]
 
-        def step(i):
-            tb.semilag_grid(ctx, vel, bufs[i % 2], N, wl.dt, 1, wl.bc, out=bufs[(i + 1) % 2])
+        def step(i, b=bufs):
+            tb.semilag_grid(ctx, vel, b[i % 2], N, wl.dt, 1, wl.bc, out=b[(i + 1) % 2])
+
+        def result(b=bufs):
+            return b[1].cpu().numpy().ravel()
         flops_kernel = GRID_FLOPS_PER_POINT
         bytes_kernel = GRID_BYTES_PER_POINT
         dominant = "semilag_grid"
-        kernel_points = wl.points_per_step
     else:
         tv = tb.Tree(ctx, wl.va, wl.vd, wl.q, 3, wl.vc)
         tc = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
         vf = tb.NodeFieldFunctor(tv, wl.bc)
 
-        def step(i):
-            tb.solve_semilag_in_situ(vf, tc, i + 1, wl.dt, 1)
-        _, flops_kernel = flops_per_point_tree(wl.q)
+        def step(i, t=tc):
+            tb.solve_semilag_in_situ(vf, t, i + 1, wl.dt, 1)
+
+        def result(t=tc):
+            return t.get_coeffs()
+        flops_kernel = fused_flops_per_point_tree(wl.q)
         _, bytes_kernel = bytes_per_point_tree(wl.q, len(wl.vd), len(wl.cd))
         dominant = "semilag_tree"
-        kernel_points = wl.points_per_step
+    kernel_points = wl.points_per_step
+
+    def timed_steps(k, first_step, stepf):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(k):
+            flush.fill_(float(i))  # L2 flush: the step's working set fits in L2
+            stepf(first_step + i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    def profiled(k, first_step, stepf):
+        ctx.profile(True)
+        ctx.profile_reset()
+        for i in range(k):
+            flush.fill_(float(i))
+            stepf(first_step + i)
+        torch.cuda.synchronize()
+        prof = ctx.profile_totals()
+        ctx.profile(False)
+        return prof
 
     # one step from the initial state, kept for the in-run parity check
     step(0)
     torch.cuda.synchronize()
-    first = (bufs[1].cpu().numpy().ravel() if is_grid else tc.get_coeffs())
+    first = result()
     for i in range(args.warmup):
         flush.fill_(float(i))  # the flush's own first launch stays out of the timed loop
         step(i + 1)
     torch.cuda.synchronize()
-
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local_rank) as clk:
-        e0.record(stream)
-        for i in range(args.steps):
-            flush.fill_(float(i))  # L2 flush: the step's working set fits in L2
-            step(args.warmup + 1 + i)
-        e1.record(stream)
-        torch.cuda.synchronize()
+        ms = timed_steps(args.steps, args.warmup + 1, step)
     barrier(world)
-    ms = e0.elapsed_time(e1)
-
     # per-kernel breakdown from a separate pass with the library's event
-    # profiler on (same steps, same L2 flushes), so the timed loop carries no
+    # profiler on (same steps, same L2 flushes): the timed loop carries no
     # profiling events
-    ctx.profile(True)
-    ctx.profile_reset()
-    for i in range(args.steps):
-        flush.fill_(float(i))
-        step(args.warmup + 1 + args.steps + i)
-    torch.cuda.synchronize()
-    prof = ctx.profile_totals()
-    ctx.profile(False)
+    prof = profiled(args.steps, args.warmup + 1 + args.steps, step)
     points = wl.points_per_step * args.steps
+    gpu_launches = int(sum(v[1] for v in prof.values()))  # same step sequence as the timed loop
 
-    fp64_targets = None if is_grid else ctx.last_fp64_targets()
-    # the same step with every Chebyshev sum in FP64 (TBSLAS_SUMS_FP64), timed
-    # the same way on a copy of the initial state, plus its distance from the
-    # default double-float step after one step
-    fp64, first64 = None, None
-    if is_grid and wl.bc == 1:
-        # the periodic grid step with FP64 stencil sums (TBSLAS_SUMS_FP64)
-        gb = [con0.clone(), torch.empty_like(con0)]
-        ctx.sums = tb.SUMS_FP64
-        try:
-            tb.semilag_grid(ctx, vel, gb[0], N, wl.dt, 1, wl.bc, out=gb[1])
-            torch.cuda.synchronize()
-            g64 = gb[1].cpu().numpy().ravel()
-            n64 = max(3, min(args.steps, 10))
-            f0 = torch.cuda.Event(enable_timing=True)
-            f1 = torch.cuda.Event(enable_timing=True)
-            f0.record(stream)
-            for i in range(n64):
-                flush.fill_(float(i))
-                tb.semilag_grid(ctx, vel, gb[i % 2], N, wl.dt, 1, wl.bc, out=gb[(i + 1) % 2])
-            f1.record(stream)
-            torch.cuda.synchronize()
-        finally:
-            ctx.sums = tb.SUMS_DOUBLE_FLOAT
-        ms64 = f0.elapsed_time(f1) / n64
-        fp64 = {"value": wl.points_per_step / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64,
-                "steps": n64,
-                "rel_diff_vs_default_first_step": float(np.abs(g64 - first).max()
-                                                        / np.abs(g64).max()),
-                "note": "TBSLAS_SUMS_FP64: the stencil sums in FP64"}
-        del gb
-    if not is_grid:
-        tc64 = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
-        ctx.sums = tb.SUMS_FP64
-        try:
-            tb.solve_semilag_in_situ(vf, tc64, 1, wl.dt, 1)
-            torch.cuda.synchronize()
-            first64 = tc64.get_coeffs()
-            n64 = max(3, min(args.steps, 10))
-            for i in range(3):
-                tb.solve_semilag_in_situ(vf, tc64, i + 2, wl.dt, 1)
-            torch.cuda.synchronize()
-            f0 = torch.cuda.Event(enable_timing=True)
-            f1 = torch.cuda.Event(enable_timing=True)
-            f0.record(stream)
-            for i in range(n64):
-                flush.fill_(float(i))
-                tb.solve_semilag_in_situ(vf, tc64, i + 5, wl.dt, 1)
-            f1.record(stream)
-            torch.cuda.synchronize()
-        finally:
-            ctx.sums = tb.SUMS_DOUBLE_FLOAT
-        ms64 = f0.elapsed_time(f1) / n64
-        fp64 = {"value": wl.points_per_step / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64,
-                "steps": n64,
-                "rel_diff_vs_default_first_step": float(np.abs(first64 - first).max()
-                                                        / np.abs(first64).max()),
-                "note": "TBSLAS_SUMS_FP64: every Chebyshev sum in FP64 (departure points and "
-                        "node values bit-identical to the oracle)"}
-        del tc64
+    # the opt-in double-float mode, timed the same way from the initial state
+    n_df = max(3, min(args.steps, 10))
+    with ctx.sums_mode(tb.SUMS_DOUBLE_FLOAT):
+        if is_grid:
+            gb = [con0.clone(), torch.empty_like(con0)]
+            step_df = lambda i: step(i, gb)
+            result_df = lambda: result(gb)
+        else:
+            tdf = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
+            step_df = lambda i: step(i, tdf)
+            result_df = lambda: result(tdf)
+        step_df(0)
+        torch.cuda.synchronize()
+        first_df = result_df()
+        for i in range(3):
+            step_df(i + 1)
+        torch.cuda.synchronize()
+        ms_df = timed_steps(n_df, 4, step_df)
+        prof_df = profiled(n_df, 4 + n_df, step_df)
+        fixed = None if is_grid else ctx.last_fp64_targets()
+    df_launch_ms = prof_df.get(dominant, (1, 0, 0.0))[2] / max(prof_df.get(dominant, (1,))[0], 1)
+
     tot_points, tot_sec = aggregate(points, ms * 1e-3, world)
     value = tot_points / tot_sec
-    gpu_launches = int(sum(v[1] for v in prof.values()))  # same step sequence as the timed loop
 
     # end-to-end through the host-buffer C-ABI entry point: host->device copy of
     # the step's input state and device->host copy of its result every step
@@ -527,109 +561,84 @@ def run_gpu(args, wl, rank, world, local_rank):
     e_points, e_sec = aggregate(points, e2e_sec, world)
 
     if rank != 0:
-        return
+        return None
     peaks, peak_src = measured_peaks()
     fp64_peak = ctx.fp64_fma_peak()
+    fp32_peak = ctx.fp32_fma_peak()
     groups, kernels, kms = prof.get(dominant, (0, 0, 0.0))
     launch_ms = kms / max(groups, 1)
-    achieved_tflops = flops_kernel * kernel_points / (launch_ms * 1e-3) / 1e12
+    achieved = flops_kernel * kernel_points / (launch_ms * 1e-3) / 1e12
     achieved_gbs = bytes_kernel * kernel_points / (launch_ms * 1e-3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get(wl.name, {}).get(dominant)
-    hbm = {"achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-           "frac": achieved_gbs / peaks["hbm_gbs"], "peak_source": peak_src}
     per_kernel = {k: v[2] / args.steps for k, v in prof.items()}
-    if is_grid and wl.bc == 1:
-        # periodic grid step: stencil sums in double-float on the FP32 pipe
-        fp32_peak = ctx.fp32_fma_peak()
-        macs = GRID_DF_MACS_PER_POINT
-        fp32_flops = 2 * DF_FP32_INSTR_PER_MAC * macs
-        achieved32 = fp32_flops * kernel_points / (launch_ms * 1e-3) / 1e12
-        roofline = {
-            "kernel": dominant + " (hi/lo split of the grids + double-float stencil sums)",
-            "bound": "fp32",
-            "achieved": achieved32, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved32 / (fp32_peak / 1e12),
-            "peak_source": "FP32 FMA throughput measured in this run (tbslas_fp32_fma_peak)",
-            "counting": "%d double-float multiply-adds per point x %d FP32 instructions, "
-                        "each counted as 2 FLOP" % (macs, DF_FP32_INSTR_PER_MAC),
-            "fp64_equivalent": {
-                "achieved": achieved_tflops, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
-                "frac": achieved_tflops / (fp64_peak / 1e12),
-                "algorithmic_flops_per_point": flops_kernel},
-            "algorithmic_bytes_per_point": bytes_kernel,
-            "launch_ms": launch_ms, "traffic": traffic, "hbm": hbm,
-            "kernels_ms_per_step": per_kernel}
-    elif is_grid:
-        roofline = {
-            "kernel": dominant, "bound": "fp64",
-            "achieved": achieved_tflops, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved_tflops / (fp64_peak / 1e12),
-            "peak_source": "FP64 FMA throughput measured in this run (tbslas_fp64_fma_peak)",
-            "algorithmic_flops_per_point": flops_kernel,
-            "algorithmic_bytes_per_point": bytes_kernel,
-            "launch_ms": launch_ms, "traffic": traffic, "hbm": hbm,
-            "kernels_ms_per_step": per_kernel}
-    else:
-        # the fused step's Chebyshev sums run in double-float on the FP32 pipe:
-        # its work is FP32 instructions, each counted as an FMA (2 FLOP) against
-        # the measured FP32 FMA peak, so frac is the FP32 pipe's issue share
-        fp32_peak = ctx.fp32_fma_peak()
-        macs = df_macs_per_point_tree(wl.q)
-        fp32_flops = 2 * DF_FP32_INSTR_PER_MAC * macs
-        achieved32 = fp32_flops * kernel_points / (launch_ms * 1e-3) / 1e12
-        roofline = {
-            "kernel": dominant + " (double-float sums + FP64 near-face pass)",
-            "bound": "fp32",
-            "achieved": achieved32, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved32 / (fp32_peak / 1e12),
-            "peak_source": "FP32 FMA throughput measured in this run (tbslas_fp32_fma_peak)",
-            "counting": "%d double-float multiply-adds per point x %d FP32 instructions, "
-                        "each counted as 2 FLOP" % (macs, DF_FP32_INSTR_PER_MAC),
-            "fp64_equivalent": {
-                "achieved": achieved_tflops, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
-                "frac": achieved_tflops / (fp64_peak / 1e12),
-                "algorithmic_flops_per_point": flops_kernel,
-                "note": "the reference's FP64 FLOP count per point over the measured FP64 "
-                        "FMA peak: above 1 means faster than an all-FP64 kernel could be"},
-            "algorithmic_bytes_per_point": bytes_kernel,
-            "launch_ms": launch_ms, "traffic": traffic, "hbm": hbm,
-            "kernels_ms_per_step": per_kernel}
+    roofline = {
+        "kernel": dominant + (" (k_semilag_grid, FP64)" if is_grid
+                              else " (k_semilag_tree<%d>, FP64)" % (wl.q + 1)),
+        "bound": "fp64",
+        "achieved": achieved, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+        "frac": achieved / (fp64_peak / 1e12),
+        "peak_source": "FP64 FMA throughput measured in this run (tbslas_fp64_fma_peak); "
+                       "MEASURED_PEAKS.json holds no FP64 figure",
+        "algorithmic_flops_per_point": flops_kernel,
+        "algorithmic_bytes_per_point": bytes_kernel,
+        "launch_ms": launch_ms, "traffic": _traffic(wl.name, dominant),
+        "hbm": {"achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved_gbs / peaks["hbm_gbs"], "peak_source": peak_src},
+        "kernels_ms_per_step": per_kernel}
+
+    # the double-float mode's own roofline: its sums are FP32 instructions,
+    # each counted as an FMA (2 FLOP) against the measured FP32 FMA peak
+    macs = GRID_DF_MACS_PER_POINT if is_grid else df_macs_per_point_tree(wl.q) - 3 * tb.n_coeff(wl.q)
+    fp32_flops = 2 * DF_FP32_INSTR_PER_MAC * macs
+    achieved32 = fp32_flops * kernel_points / (df_launch_ms * 1e-3) / 1e12
+    df64 = {"value": wl.points_per_step / (ms_df / n_df * 1e-3), "unit": UNIT,
+            "ms_per_step": ms_df / n_df, "steps": n_df,
+            "dtype": "f64 coordinates, double-float sums (hi/lo float pairs: 48-bit "
+                     "significand, FP32 exponent range)",
+            "rel_diff_vs_fp64_first_step": float(np.abs(first_df - first).max()
+                                                 / np.abs(first).max()),
+            "roofline": {"kernel": dominant + " (double-float sums%s)"
+                         % ("" if is_grid else " + FP64 near-face pass"),
+                         "bound": "fp32", "achieved": achieved32, "peak": fp32_peak / 1e12,
+                         "unit": "TFLOP/s", "frac": achieved32 / (fp32_peak / 1e12),
+                         "peak_source": "FP32 FMA throughput measured in this run "
+                                        "(tbslas_fp32_fma_peak)",
+                         "counting": "%d double-float multiply-adds per point x %d FP32 "
+                                     "instructions, each counted as 2 FLOP"
+                                     % (macs, DF_FP32_INSTR_PER_MAC),
+                         "launch_ms": df_launch_ms,
+                         "traffic": _traffic(wl.name, dominant + "_df")},
+            "note": "TBSLAS_SUMS_DOUBLE_FLOAT, opt-in: narrower than the reference's FP64; "
+                    "not the headline"}
+    if fixed is not None:
+        df64["fp64_recomputed_targets_last_step"] = int(fixed)
 
     cpu = None
     accuracy = None
     if world == 1:
         if is_grid:
             cpu, ref, k = cpu_baseline_grid(wl)
-            got = first[:k]
         else:
             cpu, ref, k = cpu_baseline_tree(wl)
-            got = first[:k]
-        accuracy = {"rel_err_vs_oracle": float(np.abs(got - ref).max() / np.abs(ref).max()),
-                    "compared": "first GPU step vs the oracle on the CPU-baseline sample"}
-        if first64 is not None:
-            g64 = first64[:k]
-            accuracy["fp64_sums_rel_err_vs_oracle"] = float(np.abs(g64 - ref).max()
-                                                            / np.abs(ref).max())
+        scale = np.abs(ref).max()
+        accuracy = {"rel_err_vs_oracle": float(np.abs(first[:k] - ref).max() / scale),
+                    "compared": "first GPU step (FP64) vs the oracle on the CPU-baseline sample",
+                    "tolerance": 1e-12}
+        df64["rel_err_vs_oracle"] = float(np.abs(first_df[:k] - ref).max() / scale)
         cpu.pop("seconds", None)
 
-    cfg = wl.describe()
-    cfg.update({"l2": "flushed between timed steps (256 MiB write inside the timed loop)",
-                "parallelism": "replicas x%d" % world, "nrk": 1})
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded analytic fields)", "config": cfg,
+            "data": "synthetic (seeded analytic fields)", "config": describe_config(wl),
             "e2e": {"value": e_points / e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
-            "fp64_sums": fp64, "clocks": clk.summary(), "gpu_launches": gpu_launches}
-    if fp64_targets is not None:
-        line["fp64_recomputed_targets_last_step"] = int(fp64_targets)
-    print(json.dumps(line))
+            "df64_sums": df64, "clocks": clk.summary(), "gpu_launches": gpu_launches,
+            "run_notes": {"l2": "flushed between timed steps (256 MiB write inside the timed "
+                                "loop)", "parallelism": "replicas x%d" % world, "nrk": 1}}
     assert ctx.check() == 0
+    ctx.close()
+    return line
 
 
 def run_remesh(args, wl, rank, world, local_rank):
@@ -751,21 +760,12 @@ def run_remesh(args, wl, rank, world, local_rank):
                      "points): oracle step %.2f s (OpenMP C++), re-mesh %.2f s (numpy)"
                      % (len(wl.cd), len(wl.cd) * npl, t_step, t_rm)}
 
-    sl = prof.get("semilag_tree", (0, 0, 0.0))
-    launch_ms = sl[2] / max(sl[0], 1)
-    fp32_peak = ctx.fp32_fma_peak()
-    macs = df_macs_per_point_tree(wl.q)
-    achieved32 = 2 * DF_FP32_INSTR_PER_MAC * macs * (pts2 / args.steps) / (launch_ms * 1e-3) / 1e12
-    roofline = {
-        "kernel": "semilag_tree (double-float sums + FP64 near-face pass)", "bound": "fp32",
-        "achieved": achieved32, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
-        "frac": achieved32 / (fp32_peak / 1e12),
-        "peak_source": "FP32 FMA throughput measured in this run (tbslas_fp32_fma_peak)",
-        "counting": "%d double-float multiply-adds per point x %d FP32 instructions, each "
-                    "counted as 2 FLOP; points per launch = the mean leaf count x (q+1)^3"
-                    % (macs, DF_FP32_INSTR_PER_MAC),
-        "launch_ms": launch_ms, "traffic": None,
-        "kernels_ms_per_step": {k: v[2] / args.steps for k, v in prof.items()}}
+    roofline = fp64_roofline(
+        ctx, "semilag_tree (k_semilag_tree<%d>, FP64)" % (wl.q + 1),
+        fused_flops_per_point_tree(wl.q), pts2 / args.steps, prof, "semilag_tree", args.steps,
+        "one velocity evaluation after the node-grid first stage, one concentration evaluation "
+        "and the RK2 updates per point, as the reference counts them; points per launch = "
+        "the mean leaf count x (q+1)^3")
     step_launches = int(sum(v[1] for v in prof.values()))
     remesh_launches = int(sum(st["kernels"] for st in stats))
     cfg = wl.describe()
@@ -789,8 +789,8 @@ def run_remesh(args, wl, rank, world, local_rank):
                        "split_by_balance": int(sum(st["balanced"] for st in stats))},
             "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
             "clocks": clk.summary(), "gpu_launches": step_launches + remesh_launches}
-    print(json.dumps(line))
     assert ctx.check() == 0
+    return line
 
 
 def cpu_baseline_bdf2(wl, budget_s=12.0):
@@ -889,22 +889,14 @@ def run_bdf2(args, wl, rank, world, local_rank):
     cpu.pop("seconds", None)
     accuracy = {"rel_err_vs_oracle": float(np.abs(first[:k] - ref).max() / np.abs(ref).max()),
                 "compared": "first GPU step vs the oracle on the CPU-baseline sample"}
-    groups, kernels, kms = prof.get("semilag_bdf2", (0, 0, 0.0))
-    launch_ms = kms / max(groups, 1)
-    fp32_peak = ctx.fp32_fma_peak()
-    macs = 2 * df_macs_per_point_tree(wl.q)  # both backtraces and both evaluations
-    targets = wl.points_per_step // 2
-    achieved32 = 2 * DF_FP32_INSTR_PER_MAC * macs * targets / (launch_ms * 1e-3) / 1e12
-    roofline = {
-        "kernel": "semilag_bdf2 (double-float sums + FP64 near-face pass)", "bound": "fp32",
-        "achieved": achieved32, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
-        "frac": achieved32 / (fp32_peak / 1e12),
-        "peak_source": "FP32 FMA throughput measured in this run (tbslas_fp32_fma_peak)",
-        "counting": "%d double-float multiply-adds per target (both backtraces and both "
-                    "evaluations; the first stage from the node grid) x %d FP32 instructions, "
-                    "each counted as 2 FLOP" % (macs, DF_FP32_INSTR_PER_MAC),
-        "launch_ms": launch_ms, "traffic": None,
-        "kernels_ms_per_step": {k2: v[2] / args.steps for k2, v in prof.items()}}
+    d = wl.q + 1
+    nc = d * (d + 1) * (d + 2) // 6
+    ev = lambda dof: 9 * d + 2 * nc * dof
+    roofline = fp64_roofline(
+        ctx, "semilag_bdf2 (k_semilag_bdf2<%d>, FP64)" % d, 3 * ev(3) + 2 * ev(1) + 36,
+        wl.points_per_step // 2, prof, "semilag_bdf2", args.steps,
+        "per target: three velocity evaluations (the first stage of the first backtrace is "
+        "the node grid's), two concentration evaluations, four RK2 updates")
     cfg = wl.describe()
     cfg.update({"l2": "flushed between timed steps (256 MiB write inside the timed loop)",
                 "parallelism": "replicas x%d" % world, "nrk": 1})
@@ -918,8 +910,8 @@ def run_bdf2(args, wl, rank, world, local_rank):
             "targets_per_s": tot_points / 2 / tot_sec,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
             "clocks": clk.summary(), "gpu_launches": int(sum(v[1] for v in prof.values()))}
-    print(json.dumps(line))
     assert ctx.check() == 0
+    return line
 
 
 def cpu_baseline_tv(wl, budget_s=12.0):
@@ -1009,22 +1001,15 @@ def run_tv(args, wl, rank, world, local_rank):
     cpu.pop("seconds", None)
     accuracy = {"rel_err_vs_oracle": float(np.abs(first[:k] - ref).max() / np.abs(ref).max()),
                 "compared": "first GPU step vs the oracle on the CPU-baseline sample"}
-    groups, kernels, kms = prof.get("semilag_tree", (0, 0, 0.0))
-    launch_ms = kms / max(groups, 1)
-    fp32_peak = ctx.fp32_fma_peak()
-    macs = df_macs_per_point_tree(wl.q)
-    achieved32 = (2 * DF_FP32_INSTR_PER_MAC * macs * wl.points_per_step / (launch_ms * 1e-3)
-                  / 1e12)
-    roofline = {
-        "kernel": "semilag_tree on the blended velocity (double-float sums + FP64 near-face "
-                  "pass)", "bound": "fp32",
-        "achieved": achieved32, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
-        "frac": achieved32 / (fp32_peak / 1e12),
-        "peak_source": "FP32 FMA throughput measured in this run (tbslas_fp32_fma_peak)",
-        "counting": "%d double-float multiply-adds per point x %d FP32 instructions, each "
-                    "counted as 2 FLOP" % (macs, DF_FP32_INSTR_PER_MAC),
-        "launch_ms": launch_ms, "traffic": None,
-        "kernels_ms_per_step": {k2: v[2] / args.steps for k2, v in prof.items()}}
+    d = wl.q + 1
+    nc = d * (d + 1) * (d + 2) // 6
+    ev = lambda dof: 9 * d + 2 * nc * dof
+    m = len(wl.vcs)
+    roofline = fp64_roofline(
+        ctx, "semilag_tv (k_semilag_tv<%d>, FP64: every tree at every stage point)" % d,
+        2 * m * ev(3) + ev(1) + 18, wl.points_per_step, prof, "semilag_tv", args.steps,
+        "per point: the %d velocity trees evaluated at both RK2 stage points and blended (as "
+        "the reference's FieldSetFunctor does), the concentration at the departure point" % m)
     cfg = wl.describe()
     cfg.update({"l2": "flushed between timed steps (256 MiB write inside the timed loop)",
                 "parallelism": "replicas x%d" % world, "nrk": 1})
@@ -1036,8 +1021,8 @@ def run_tv(args, wl, rank, world, local_rank):
                     "d2h_bytes_per_step": int(host.nbytes)},
             "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
             "clocks": clk.summary(), "gpu_launches": int(sum(v[1] for v in prof.values()))}
-    print(json.dumps(line))
     assert ctx.check() == 0
+    return line
 
 
 def run_construct(args, wl, rank, world, local_rank):
@@ -1116,64 +1101,84 @@ def run_construct(args, wl, rank, world, local_rank):
                                        "oracle's fit), once: %.2f s" % cpu_sec},
             "accuracy": check, "clocks": clk.summary(),
             "gpu_launches": int(prof.get("construct", (0, 0, 0.0))[1])}
-    print(json.dumps(line))
     assert ctx.check() == 0
+    return line
 
 
 def run_batched(args, wl, rank, world, local_rank):
     """The batched, graph-captured step of 64 uneven problems vs the plain
     per-problem loop of in-situ steps on the same problems, from the same
-    state."""
+    state: in the default FP64 arithmetic (the headline of this line) and in
+    the opt-in double-float mode.  The plain loop's idle time between its
+    launches (wall time minus the summed kernel time the library's event
+    profiler brackets) bounds what batching can gain at an equal per-target
+    rate."""
     import torch
     import tbslas_gb300 as tb
 
     torch.cuda.set_device(local_rank)
     ctx = tb.Context(local_rank)
     stream = torch.cuda.current_stream()
-    probs = [(tb.Tree(ctx, p["va"], p["vd"], p["q"], 3, p["vc"]),
-              tb.Tree(ctx, p["ca"], p["cd"], p["q"], 1, p["cc"]), p["dt"]) for p in wl.problems]
-    funcs = [tb.NodeFieldFunctor(tv, wl.bc) for tv, _, _ in probs]
 
-    def reset():
-        for (tv, tc, _), p in zip(probs, wl.problems):
-            tc.set_coeffs(p["cc"])
+    def measure(mode):
+        with ctx.sums_mode(mode):
+            probs = [(tb.Tree(ctx, p["va"], p["vd"], p["q"], 3, p["vc"]),
+                      tb.Tree(ctx, p["ca"], p["cd"], p["q"], 1, p["cc"]), p["dt"])
+                     for p in wl.problems]
+            funcs = [tb.NodeFieldFunctor(tv, wl.bc) for tv, _, _ in probs]
 
-    def plain(ts0, k):
-        for i in range(k):
-            for f, (tv, tc, dt) in zip(funcs, probs):
-                tb.solve_semilag_in_situ(f, tc, ts0 + i, dt)
+            def reset():
+                for (tv, tc, _), p in zip(probs, wl.problems):
+                    tc.set_coeffs(p["cc"])
 
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # plain per-problem loop
-    reset()
-    plain(1, args.warmup)
-    reset()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    plain(1, args.steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    plain_ms = e0.elapsed_time(e1)
-    plain_state = [tc.get_coeffs() for _, tc, _ in probs]
+            def plain(ts0, k):
+                for i in range(k):
+                    for f, (tv, tc, dt) in zip(funcs, probs):
+                        tb.solve_semilag_in_situ(f, tc, ts0 + i, dt)
 
-    batch = tb.Batch(ctx, probs, 1, wl.bc)
-    reset()
-    tune = batch.autotune()
-    reset()
-    batch.run(1, args.steps, True)          # capture + warm replay
-    reset()
-    torch.cuda.synchronize()
-    barrier(world)
-    with ClockSampler(local_rank) as clk:
-        e0.record(stream)
-        batch.run(1, args.steps, True)      # the captured K-step graph
-        e1.record(stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reset()
+            plain(1, args.warmup)
+            reset()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            plain(1, args.steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            plain_ms = e0.elapsed_time(e1)
+            plain_state = [tc.get_coeffs() for _, tc, _ in probs]
+            # the plain loop's kernel time (the profiler's event brackets)
+            reset()
+            ctx.profile(True)
+            ctx.profile_reset()
+            plain(1, args.steps)
+            torch.cuda.synchronize()
+            busy_ms = sum(v[2] for v in ctx.profile_totals().values())
+            plain_launches = sum(v[1] for v in ctx.profile_totals().values())
+            ctx.profile(False)
+            batch = tb.Batch(ctx, probs, 1, wl.bc)
+        reset()
+        tune = batch.autotune()
+        reset()
+        batch.run(1, args.steps, True)          # capture + warm replay
+        reset()
         torch.cuda.synchronize()
-    barrier(world)
-    ms = e0.elapsed_time(e1)
-    same = all(np.array_equal(tc.get_coeffs(), ref) for (_, tc, _), ref in zip(probs, plain_state))
+        barrier(world)
+        with ClockSampler(local_rank) as clk:
+            e0.record(stream)
+            batch.run(1, args.steps, True)      # the captured K-step graph
+            e1.record(stream)
+            torch.cuda.synchronize()
+        barrier(world)
+        ms = e0.elapsed_time(e1)
+        same = all(np.array_equal(tc.get_coeffs(), ref)
+                   for (_, tc, _), ref in zip(probs, plain_state))
+        return dict(probs=probs, batch=batch, plain_ms=plain_ms, busy_ms=busy_ms, ms=ms,
+                    same=same, tune=tune, clk=clk, plain_launches=plain_launches)
 
-    # e2e: host coefficients in, one graph step, host coefficients out, per step
+    r64 = measure(tb.SUMS_FP64)
+    # e2e (FP64): host coefficients in, one graph step, host coefficients out, per step
+    probs, batch = r64["probs"], r64["batch"]
     pinned = [torch.from_numpy(np.ascontiguousarray(p["cc"])).pin_memory().numpy()
               for p in wl.problems]
     h2d = sum(a.nbytes for a in pinned)
@@ -1188,42 +1193,103 @@ def run_batched(args, wl, rank, world, local_rank):
             tc.get_coeffs(a)
     torch.cuda.synchronize()
     e2e_sec = time.perf_counter() - t0
+    batch.close()
+    for tv, tc, _ in probs:
+        tv.close()
+        tc.close()
+    rdf = measure(tb.SUMS_DOUBLE_FLOAT)
+    rdf["batch"].close()
 
     points = wl.points_per_step * args.steps
-    tot_points, tot_sec = aggregate(points, ms * 1e-3, world)
+    tot_points, tot_sec = aggregate(points, r64["ms"] * 1e-3, world)
     e_points, e_sec = aggregate(points, e2e_sec, world)
     if rank != 0:
-        return
-    cfg = wl.describe()
-    cfg.update({"l2": "inputs larger than L2 (all problems' trees)",
-                "parallelism": "replicas x%d" % world, "nrk": 1,
-                "autotuned": {"block": tune[0], "targets_per_item": tune[1], "ctas_per_sm": tune[2]},
-                "graph": "the K-step run is one captured CUDA graph"})
+        return None
+
+    def summary(r):
+        return {"batched": {"value": points / (r["ms"] * 1e-3), "ms_per_step": r["ms"] / args.steps},
+                "plain_loop": {"value": points / (r["plain_ms"] * 1e-3),
+                               "ms_per_step": r["plain_ms"] / args.steps,
+                               "kernel_ms_per_step": r["busy_ms"] / args.steps,
+                               "launch_groups_per_step": r["plain_launches"] / args.steps,
+                               "idle_fraction": max(0.0, 1.0 - r["busy_ms"] / r["plain_ms"]),
+                               "max_gain_from_removing_idle": r["plain_ms"] / r["busy_ms"]},
+                "batched_vs_plain": r["plain_ms"] / r["ms"],
+                "batched_equals_plain_bitwise": bool(r["same"]),
+                "autotuned": {"block": r["tune"][0], "targets_per_item": r["tune"][1],
+                              "ctas_per_sm": r["tune"][2]}}
+    cfg = describe_config(wl)
+    s64, sdf = summary(r64), summary(rdf)
     line = {"metric": METRIC, "value": tot_points / tot_sec, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r64["ms"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded analytic fields)", "config": cfg,
-            "batched_vs_plain": plain_ms / ms,
-            "plain_loop": {"value": points / (plain_ms * 1e-3), "ms_per_step": plain_ms / args.steps,
-                           "launches_per_step": 2 * len(probs)},
-            "accuracy": {"batched_equals_plain_bitwise": bool(same)},
+            "batched_vs_plain": s64["batched_vs_plain"],
+            "plain_loop": s64["plain_loop"],
+            "accuracy": {"batched_equals_plain_bitwise": s64["batched_equals_plain_bitwise"],
+                         "plain_loop": "oracle-checked per problem (tests/test_gpu_tree.py)"},
+            "autotuned": s64["autotuned"],
             "e2e": {"value": e_points / e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(h2d)},
-            "clocks": clk.summary(),
-            "gpu_launches": int(args.steps * (1 + 2 * len({_band(p["q"]) for p in wl.problems})))}
-    print(json.dumps(line))
+            "df64_sums": dict(sdf, dtype="f64 coordinates, double-float sums",
+                              note="TBSLAS_SUMS_DOUBLE_FLOAT, opt-in; not the headline"),
+            "clocks": r64["clk"].summary(),
+            "run_notes": {"l2": "inputs larger than L2 (all problems' trees)",
+                          "parallelism": "replicas x%d" % world, "nrk": 1,
+                          "graph": "the K-step run is one captured CUDA graph"},
+            "gpu_launches": int(args.steps * (len({p["q"] for p in wl.problems})
+                                              + len({_band(p["q"]) for p in wl.problems}) + 1))}
     assert ctx.check() == 0
+    ctx.close()
+    return line
+
+
+def bubble_directions(wl, rng, n, leaves=None):
+    """n seeded velocity-coefficient directions [Lv, 3, Nc] that vanish on
+    every leaf face: per leaf and component, (1 - xi^2)(1 - eta^2)(1 - zeta^2)
+    times a random polynomial of total degree q - 6 in the leaf's local
+    coordinates, fitted at the leaf's nodes (exact: the product has total
+    degree q).  Nodes that sit on a leaf face with zero normal velocity -- on
+    Taylor-Green, the stagnation planes and every z face (v_z = 0) -- stay
+    exactly on that face under such a perturbation.  leaves (optional): per
+    direction, the one leaf that carries it (zero elsewhere)."""
+    from tbslas_gb300 import trees
+    q = wl.q
+    d = q + 1
+    xi = 2.0 * trees.cheb_nodes(q) - 1.0                      # [Np, 3]
+    bub = np.prod(1.0 - xi ** 2, axis=1)                      # [Np]
+    r = q - 6
+    mono = [(a, b, c) for a in range(r + 1) for b in range(r + 1 - a)
+            for c in range(r + 1 - a - b)]
+    P = np.stack([xi[:, 0] ** a * xi[:, 1] ** b * xi[:, 2] ** c for a, b, c in mono], axis=1)
+    M = trees.pt2coeff(q)
+    L = len(wl.d)
+    out = []
+    for k in range(n):
+        w = rng.standard_normal((L, 3, len(mono)))
+        if leaves is not None:
+            keep = np.zeros(L, dtype=bool)
+            keep[leaves[k]] = True
+            w[~keep] = 0.0
+        vals = np.einsum("pm,lam->lap", P, w) * bub[None, None, :]   # [L, 3, Np]
+        out.append((vals.reshape(L * 3, d ** 3) @ M).reshape(L, 3, -1))
+    return out
 
 
 def run_adjoint(args, wl, rank, world, local_rank):
-    """The differentiable T-step advection: forward (plain and checkpointed)
-    and adjoint passes, timed; gradients checked by central differences."""
+    """The differentiable T-step advection in the default FP64 arithmetic:
+    the forward (plain and checkpointed) and adjoint passes timed; gradients
+    checked by central differences on the configuration itself (16 c0
+    directions, 8 velocity directions that vanish on leaf faces) and by the
+    oracle's dual numbers at a reduced depth.  The same passes in the opt-in
+    double-float mode are reported beside it."""
     import torch
     import tbslas_gb300 as tb
     from tbslas_gb300 import adjoint
 
     torch.cuda.set_device(local_rank)
     ctx = tb.Context(local_rank)
+    assert ctx.sums == tb.SUMS_FP64
     stream = torch.cuda.current_stream()
     dev = torch.device("cuda", local_rank)
     tv = tb.Tree(ctx, wl.a, wl.d, wl.q, 3, wl.vc)
@@ -1262,30 +1328,22 @@ def run_adjoint(args, wl, rank, world, local_rank):
         torch.cuda.synchronize()
         return c, v, j
 
-    def fwd_default():
-        # the production step (tbslas_semilag_in_situ, double-float sums) for
-        # the same T steps from c0
-        tc.set_coeffs(c0)
-        vf = tb.NodeFieldFunctor(tv, wl.bc)
-        for k in range(T):
-            tb.solve_semilag_in_situ(vf, tc, 1 + k, wl.dt, 1)
-
-    for _ in range(args.warmup if args.warmup < 3 else 1):
+    def passes(modes):
         fwd_plain()
-        fwd_default()
-    fwd_ms, _ = timed(fwd_plain)
-    fwd_df_ms, _ = timed(fwd_default)
-    # one untimed gradient each way: the first autograd pass of a process
-    # carries one-time setup
-    for ck in (True, "departure", False):
-        _, _, j0 = grad(ck)
-        j0.backward()
-    torch.cuda.synchronize()
-    res = {}
-    for ck in (True, "departure", False):
-        fms, (c, v, j) = timed(lambda: grad(ck))
-        bms, _ = timed(lambda: j.backward())
-        res[ck] = (fms, bms, c.grad.clone(), v.grad.clone(), j.item())
+        fms_plain, _ = timed(fwd_plain)
+        for ck in modes:  # the first autograd pass of a process carries one-time setup
+            _, _, j0 = grad(ck)
+            j0.backward()
+        torch.cuda.synchronize()
+        res = {}
+        for ck in modes:
+            fms, (c, v, j) = timed(lambda: grad(ck))
+            bms, _ = timed(lambda: j.backward())
+            res[ck] = (fms, bms, c.grad.clone(), v.grad.clone(), j.item())
+        return fms_plain, res
+
+    with ClockSampler(local_rank) as clk:
+        fwd_ms, res = passes((True, "departure", False))
     # per-kernel breakdown of one more adjoint pass each way (profiler on,
     # outside the timed passes)
     by_kernel = {}
@@ -1298,110 +1356,90 @@ def run_adjoint(args, wl, rank, world, local_rank):
         by_kernel["checkpoint" if ck else "recompute"] = {
             k: round(v[2] / T, 3) for k, v in sorted(ctx.profile_totals().items())}
         ctx.profile(False)
-    gc = res[True][2]
+    with ctx.sums_mode(tb.SUMS_DOUBLE_FLOAT):
+        fwd_df_ms, res_df = passes((True,))
+    gc, gv = res[True][2], res[True][3]
     rng = np.random.default_rng(123)
     eps = 1e-6
-    errs_c, errs_v = [], []
 
     def J_at(cc, vv):
         with torch.no_grad():
             return J(adjoint.advect(cc, vv, tv, tc, wl.dt, 1, T, wl.bc, False)).item()
 
-    for k in range(8):
+    errs_c, errs_v = [], []
+    t_fd = time.perf_counter()
+    for k in range(16):
         d = torch.from_numpy(rng.standard_normal(wl.c0.shape)).to(dev)
         fd = (J_at(c0 + eps * d, vct) - J_at(c0 - eps * d, vct)) / (2 * eps)
         an = (gc * d).sum().item()
         errs_c.append(abs(fd - an) / abs(an))
-    errs_v = fd_velocity_companion(wl, ctx, dev, eps, 8)
+    # velocity directions: one face-vanishing bubble each, on a seeded leaf
+    # where the concentration is large (so dJ/ds is), i.e. at most a few
+    # thousand targets move: an eps-move of a departure point across a leaf
+    # face (a jump of J by the fit's face discontinuity) stays improbable
+    big = np.flatnonzero(np.abs(wl.c0[:, 0, 0]) > 0.3 * np.abs(wl.c0[:, 0, 0]).max())
+    vleaves = rng.choice(big, size=8, replace=False)
+    for dvn in bubble_directions(wl, rng, 8, leaves=vleaves):
+        dv = torch.from_numpy(dvn).to(dev)
+        fd = (J_at(c0, vct + eps * dv) - J_at(c0, vct - eps * dv)) / (2 * eps)
+        an = (gv * dv).sum().item()
+        errs_v.append(abs(fd - an) / abs(an))
+    t_fd = time.perf_counter() - t_fd
     dual = dual_check_adjoint(wl, ctx, dev)
     ck_fms, ck_bms = res[True][0], res[True][1]
     rc_fms, rc_bms = res[False][0], res[False][1]
     ck_gap = max(float((res[True][2] - res[False][2]).abs().max() / res[False][2].abs().max()),
                  float((res[True][3] - res[False][3]).abs().max() / res[False][3].abs().max()))
+    df_gap = max(float((res_df[True][2] - gc).abs().max() / gc.abs().max()),
+                 float((res_df[True][3] - gv).abs().max() / gv.abs().max()))
     points = wl.points_per_step * T
     if rank != 0:
-        return
-    cfg = wl.describe()
+        return None
+    fd_max = max(errs_c + errs_v)
     line = {"metric": METRIC, "value": points / (ck_bms * 1e-3), "unit": UNIT + " (adjoint pass)",
             "n_gpus": world, "steps": T, "warmup": 1, "ms_per_step": ck_bms / T,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded analytic fields)", "config": cfg,
+            "data": "synthetic (seeded analytic fields)", "config": describe_config(wl),
+            "adj_over_fwd": ck_bms / fwd_ms,
+            "fd_max_rel": fd_max, "dual_max_rel": dual["max_rel_err"],
             "forward": {"ms": fwd_ms, "points_per_s": points / (fwd_ms * 1e-3),
-                        "kind": "the differentiable forward without checkpoints (the "
-                                "in-situ step, double-float sums)"},
-            "forward_default": {"ms": fwd_df_ms, "points_per_s": points / (fwd_df_ms * 1e-3),
-                                "kind": "tbslas_semilag_in_situ (double-float sums)"},
+                        "kind": "the in-situ step (FP64 sums), no checkpoints"},
             "checkpoint": {"forward_ms": ck_fms, "adjoint_ms": ck_bms,
                            "adj_over_fwd": ck_bms / fwd_ms,
-                           "adj_over_fwd_default": ck_bms / fwd_df_ms,
                            "grad_over_fwd": (ck_fms + ck_bms) / fwd_ms,
                            "stored_bytes": int(points * 48)},
             "checkpoint_departure_only": {
                 "forward_ms": res["departure"][0], "adjoint_ms": res["departure"][1],
                 "adj_over_fwd": res["departure"][1] / fwd_ms,
+                "grad_over_fwd": (res["departure"][0] + res["departure"][1]) / fwd_ms,
                 "stored_bytes": int(points * 24),
                 "note": "departure points stored; midpoints rebuilt from the node-grid "
                         "velocity in the backward pass"},
             "recompute": {"forward_ms": rc_fms, "adjoint_ms": rc_bms,
                           "adj_over_fwd": rc_bms / fwd_ms,
-                          "adj_over_fwd_default": rc_bms / fwd_df_ms,
                           "grad_over_fwd": (rc_fms + rc_bms) / fwd_ms, "stored_bytes": 0},
-            "fd_check": {"eps": eps, "directions": 16,
-                         "directions_kind": "8 N(0,1) c0 directions on this configuration; 8 "
-                                            "smooth random velocity directions on a companion "
-                                            "problem (same q, steps, dt; depth 2; generic "
-                                            "Fourier velocity) -- on Taylor-Green, nodes sit "
-                                            "on leaf faces with zero normal velocity, so J is "
-                                            "not differentiable in V there (the dual-number "
-                                            "check below is the exact test)",
-                         "max_rel_err_dJ_dc0": max(errs_c), "max_rel_err_dJ_dV": max(errs_v)},
+            "fd_check": {"eps": eps, "directions": len(errs_c) + len(errs_v),
+                         "directions_kind": "16 N(0,1) c0 directions and 8 velocity directions, "
+                                            "each a face bubble times a random polynomial "
+                                            "on one seeded leaf inside the Gaussian (zero "
+                                            "on every leaf face, so nodes held on faces by "
+                                            "zero normal velocity stay there), all on this "
+                                            "configuration",
+                         "max_rel_err_dJ_dc0": max(errs_c), "max_rel_err_dJ_dV": max(errs_v),
+                         "seconds": t_fd, "tolerance": 1e-6},
             "dual_number_check": dual,
             "adjoint_ms_per_step_by_kernel": by_kernel,
-            "checkpoint_vs_recompute_rel_diff": ck_gap, "J": res[True][4]}
-    print(json.dumps(line))
+            "checkpoint_vs_recompute_rel_diff": ck_gap, "J": res[True][4],
+            "df64_sums": {"forward_ms": fwd_df_ms, "adjoint_ms": res_df[True][1],
+                          "adj_over_fwd": res_df[True][1] / fwd_df_ms,
+                          "adj_over_fp64_fwd": res_df[True][1] / fwd_ms,
+                          "grad_rel_diff_vs_fp64": df_gap,
+                          "dtype": "f64 coordinates, double-float sums",
+                          "note": "TBSLAS_SUMS_DOUBLE_FLOAT, opt-in; not the headline"},
+            "clocks": clk.summary()}
     assert ctx.check() == 0
-
-
-def fd_velocity_companion(wl, ctx, dev, eps, ndir, depth=2, seed=7):
-    """Central differences of J in the velocity coefficients on a companion
-    of the configuration: same q, steps and dt on a uniform depth-2 tree,
-    with a seeded generic Fourier velocity (no node pinned on a leaf face).
-    J is piecewise smooth in V (a departure point pushed across a leaf face
-    changes polynomial); the expected number of such crossings under an
-    eps-perturbation grows with the number of targets, so the check runs on
-    64 leaves."""
-    import torch
-    import tbslas_gb300 as tb
-    from tbslas_gb300 import adjoint, fields, trees
-    rng = np.random.default_rng(seed)
-    a, d = trees.uniform_tree(depth)
-    fn = fields.fourier_velocity(rng)
-    vc = trees.fit(lambda p: 0.5 * fn(p), a, d, wl.q, 3)
-    c0 = trees.fit(fields.gaussian((0.45, 0.5, 0.5), 0.08), a, d, wl.q, 1)
-    cob = trees.fit(fields.gaussian((0.47, 0.49, 0.52), 0.085), a, d, wl.q, 1)
-    tv, tc = tb.Tree(ctx, a, d, wl.q, 3, vc), tb.Tree(ctx, a, d, wl.q, 1, c0)
-    V = torch.from_numpy(adjoint.basis_at_nodes(wl.q)).to(dev)
-    co, c0t = torch.from_numpy(cob).to(dev), torch.from_numpy(c0).to(dev)
-
-    def J(c):
-        return 0.5 * ((torch.einsum("ln,pn->lp", c[:, 0, :] - co[:, 0, :], V)) ** 2).sum()
-
-    v = torch.from_numpy(vc).to(dev).requires_grad_(True)
-    J(adjoint.advect(c0t, v, tv, tc, wl.dt, 1, wl.steps, tb.Periodic, True)).backward()
-    gv = v.grad
-
-    def J_at(vv):
-        with torch.no_grad():
-            return J(adjoint.advect(c0t, vv, tv, tc, wl.dt, 1, wl.steps, tb.Periodic,
-                                    False)).item()
-
-    errs = []
-    for _ in range(ndir):
-        dv = torch.from_numpy(trees.fit(fields.fourier_velocity(rng), a, d, wl.q, 3)).to(dev)
-        fd = (J_at(v.detach() + eps * dv) - J_at(v.detach() - eps * dv)) / (2 * eps)
-        an = (gv * dv).sum().item()
-        errs.append(abs(fd - an) / abs(an))
-    return errs
+    ctx.close()
+    return line
 
 
 def dual_check_adjoint(wl, ctx, dev, depth=3, ndir=2):
@@ -1454,13 +1492,72 @@ def _band(q):
     return 0 if q <= 8 else (1 if q <= 11 else (2 if q <= 13 else q - 11))
 
 
+# The configurations measured beside the headline in the default run (N = 1):
+# key -> (workload, runner name, steps cap).  The headline is the adaptive q = 14
+# configuration; these are the uniform q = 8 tree, the tricubic grid, the
+# 64-problem batch and the adjoint, each in the library's default FP64
+# arithmetic with its own roofline, CPU baseline, accuracy check and clocks.
+EXTRA_CONFIGS = [
+    ("cfg1_uniform_q8", "tree_uniform_q8", "run_gpu", None),
+    ("cfg3_grid_256", "grid_periodic_256", "run_gpu", 20),
+    ("cfg4_batched_64", "batched_64", "run_batched", 10),
+    ("cfg5_adjoint_q8", "adjoint_q8", "run_adjoint", None),
+]
+
+
+def describe_config(wl):
+    """The `config` object of a workload: the same dict in both arms."""
+    return wl.describe()
+
+
+def dispatch(args, wl, rank, world, local_rank):
+    if wl.name.startswith("batched"):
+        return run_batched(args, wl, rank, world, local_rank)
+    if wl.name.startswith("adjoint"):
+        return run_adjoint(args, wl, rank, world, local_rank)
+    if hasattr(wl, "remesh"):
+        return run_remesh(args, wl, rank, world, local_rank)
+    if hasattr(wl, "c_prev"):
+        return run_bdf2(args, wl, rank, world, local_rank)
+    if hasattr(wl, "vcs"):
+        return run_tv(args, wl, rank, world, local_rank)
+    if hasattr(wl, "construct"):
+        return run_construct(args, wl, rank, world, local_rank)
+    return run_gpu(args, wl, rank, world, local_rank)
+
+
+def extra_configs(args, rank, world, local_rank, only=None):
+    """{key: line} of EXTRA_CONFIGS (each a complete bench line of its own)."""
+    from tbslas_gb300.workloads import make
+    out = {}
+    for key, name, runner, cap in EXTRA_CONFIGS:
+        if only and key not in only:
+            continue
+        sub = argparse.Namespace(**vars(args))
+        if cap is not None:
+            sub.steps = min(args.steps, cap)
+        t0 = time.perf_counter()
+        try:
+            line = globals()[runner](sub, make(name), rank, world, local_rank)
+        except Exception as e:  # recorded in the line; the headline still prints
+            line = {"error": "%s: %s" % (type(e).__name__, e)}
+        if line is not None:
+            line.pop("metric", None)
+            line["wall_s"] = time.perf_counter() - t0
+            out[key] = line
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="tree_adaptive_q14")
+    ap.add_argument("--extras", default="all",
+                    help="with the default workload at N = 1: 'all', 'none' or a comma list "
+                         "of %s" % ",".join(k for k, *_ in EXTRA_CONFIGS))
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -1468,8 +1565,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        from tbslas_gb300.workloads import make
-        run_reference(args, make(args.workload))
+        run_reference(args, args.workload)
         return
     if world > 1:
         import torch
@@ -1481,20 +1577,14 @@ def main():
     from tbslas_gb300.workloads import make
     wl = make(args.workload)
     try:
-        if args.workload.startswith("batched"):
-            run_batched(args, wl, rank, world, local_rank)
-        elif args.workload.startswith("adjoint"):
-            run_adjoint(args, wl, rank, world, local_rank)
-        elif hasattr(wl, "remesh"):
-            run_remesh(args, wl, rank, world, local_rank)
-        elif hasattr(wl, "c_prev"):
-            run_bdf2(args, wl, rank, world, local_rank)
-        elif hasattr(wl, "vcs"):
-            run_tv(args, wl, rank, world, local_rank)
-        elif hasattr(wl, "construct"):
-            run_construct(args, wl, rank, world, local_rank)
-        else:
-            run_gpu(args, wl, rank, world, local_rank)
+        line = dispatch(args, wl, rank, world, local_rank)
+        if (args.workload == "tree_adaptive_q14" and world == 1 and args.extras != "none"):
+            only = None if args.extras == "all" else set(args.extras.split(","))
+            extras = extra_configs(args, rank, world, local_rank, only)
+            if line is not None:
+                line.update(extras)
+        if line is not None:
+            print(json.dumps(line))
     finally:
         if world > 1:
             import torch.distributed as dist

@@ -76,6 +76,8 @@ int tbslas_version(void);
 /* Binds `device`, owns cached scratch buffers.  No reference counterpart
  * (the reference keeps static buffers: src/tree/tree_functor.h:166,:519-584). */
 int tbslas_ctx_create(int device, tbslas_ctx* out);
+/* Destroy a context's trees and batches first: while any are alive the
+ * context is left intact and TBSLAS_ERR_INVALID_ARG is returned. */
 int tbslas_ctx_destroy(tbslas_ctx ctx);
 /* Kernel-side error word (bounded waits that ran out, ...); 0 if clean.
  * Synchronises the context's device; clears the word. */

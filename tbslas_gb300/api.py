@@ -13,6 +13,7 @@ is no CPU path.
 """
 import contextlib
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -81,9 +82,18 @@ class Context:
         call("tbslas_ctx_create", int(device), ctypes.byref(h))
         self.handle = h
         self.device = int(device)
+        self._objects = weakref.WeakSet()  # trees and batches made on this context
 
     def close(self):
+        """Closes the context's remaining batches, then its trees, then the
+        context (the C ABI destroys a context only after its objects)."""
         if self.handle:
+            objs = list(self._objects)
+            for o in objs:
+                if isinstance(o, Batch):
+                    o.close()
+            for o in objs:
+                o.close()
             capi.lib().tbslas_ctx_destroy(self.handle)
             self.handle = None
 
@@ -190,6 +200,7 @@ class Tree:
         call("tbslas_tree_create", ctx.handle, depth.size, anchor.ctypes.data, depth.ctypes.data,
              int(q), int(dof), ctypes.byref(h))
         self.ctx, self.handle = ctx, h
+        ctx._objects.add(self)
         self.anchor, self.depth, self.q, self.dof = anchor, depth, int(q), int(dof)
         self.n_leaves = depth.size
         if coeff is not None:
@@ -322,6 +333,7 @@ def construct_tree(ctx, field, q, tol, min_depth, max_depth, bc=FreeSpace):
          int(max_depth), int(bc), ctypes.byref(h))
     t = Tree.__new__(Tree)
     t.ctx, t.handle, t.q, t.dof = ctx, h, int(q), field.dof
+    ctx._objects.add(t)
     L = ctypes.c_int64()
     call("tbslas_tree_info", h, ctypes.byref(L), None, None, None)
     t.n_leaves = int(L.value)
@@ -512,6 +524,7 @@ class Batch:
              ctypes.cast(con, ctypes.c_void_p), ctypes.cast(dt, ctypes.c_void_p),
              int(num_rk_step), int(bc), ctypes.byref(h))
         self.ctx, self.handle, self.problems = ctx, h, list(problems)
+        ctx._objects.add(self)
 
     def close(self):
         if self.handle:

@@ -117,45 +117,46 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   a.lambda = lambda_k_dev;
   a.grad_vel = grad_vel_dev;
   a.wnode = nullptr;
-  if (ctx_sums(ctx) == TBSLAS_SUMS_FP64) {
-    ProfBracket pb(ctx, "adjoint_fp64", s);
-    g_adj.adj[q](a, s);
-  } else {
-    // the sums in double-float over a hi/lo split of c^k; the node term by
-    // the transposed node-grid passes
+  const bool df = ctx_sums(ctx) == TBSLAS_SUMS_DOUBLE_FLOAT;
+  st = ctx_wnode_scratch(ctx, tc.L * np * 3, &a.wnode);
+  if (st != TBSLAS_OK) return st;
+  if (!xdep_dev) {
+    // recompute: the step's points by its own kernels (double-float: FP64
+    // for the ambiguous targets)
+    double *xm = nullptr, *xd = nullptr;
+    st = step_points(ctx, vel, con, timestep, dt, bc, &xm, &xd, s);
+    if (st != TBSLAS_OK) return st;
+    a.xmid = xm;
+    a.xdep = xd;
+  } else if (!xmid_dev) {
+    // departure points checkpointed: the midpoints from the node-grid
+    // velocity, exactly as the forward formed them
+    double* xm = nullptr;
+    st = step_midpoints(ctx, vel, con, timestep, dt, bc, &xm, s);
+    if (st != TBSLAS_OK) return st;
+    a.xmid = xm;
+  }
+  if (df) {
+    // the sums in double-float over a hi/lo split of c^k
     float2* c2 = nullptr;
     st = ctx_c2_scratch(ctx, tc.L * nc, &c2);
     if (st != TBSLAS_OK) return st;
-    st = ctx_wnode_scratch(ctx, tc.L * np * 3, &a.wnode);
-    if (st != TBSLAS_OK) return st;
-    if (!xdep_dev) {
-      // recompute: the step's points by its double-float kernels (FP64 for
-      // the ambiguous targets)
-      double *xm = nullptr, *xd = nullptr;
-      st = step_points_df(ctx, vel, con, timestep, dt, bc, &xm, &xd, s);
-      if (st != TBSLAS_OK) return st;
-      a.xmid = xm;
-      a.xdep = xd;
-    } else if (!xmid_dev) {
-      // departure points checkpointed: the midpoints from the node-grid
-      // velocity, exactly as the forward formed them
-      double* xm = nullptr;
-      st = step_midpoints(ctx, vel, con, timestep, dt, bc, &xm, s);
-      if (st != TBSLAS_OK) return st;
-      a.xmid = xm;
-    }
     {
       ProfBracket pb(ctx, "adjoint_split", s);
       launch_split(con_coeff_k_dev, c2, tc.L * nc, ctx_err(ctx), s);
     }
-    {
-      ProfBracket pb(ctx, "adjoint_df", s);
-      g_adj.adj_df[q](a, c2, s);
-    }
-    st = launched("adjoint step launch");
-    if (st != TBSLAS_OK) return st;
+    ProfBracket pb(ctx, "adjoint_df", s);
+    g_adj.adj_df[q](a, c2, s);
+  } else {
+    ProfBracket pb(ctx, "adjoint_fp64", s);
+    g_adj.adj[q](a, s);
+  }
+  st = launched("adjoint step launch");
+  if (st != TBSLAS_OK) return st;
+  {
+    // the node term by the transposed node-grid passes
     ProfBracket pb(ctx, "adjoint_node_scatter", s);
-    launch_scatter_on_nodes(tv, tc, bc, a.wnode, grad_vel_dev, 3 * nc, true, s);
+    launch_scatter_on_nodes(tv, tc, bc, a.wnode, grad_vel_dev, 3 * nc, df, s);
   }
   return launched("adjoint step launch");
 }

@@ -9,7 +9,7 @@
 // adjoint by the sums' rounding (~1e-15 relative).
 #pragma once
 
-#include "adjoint_kernels.cuh"
+#include "adjoint_f64.cuh"
 
 namespace tbg {
 
@@ -379,7 +379,7 @@ void launch_adjoint_df(const AdjArgs& a, const float2* con2, cudaStream_t s) {
 
 template <int D>
 void register_adjoint_degree(AdjFn* a, AdjDfFn* d) {
-  a[D - 1] = &launch_adjoint<D>;
+  a[D - 1] = &launch_adjoint_f64<D>;
   d[D - 1] = &launch_adjoint_df<D>;
 }
 

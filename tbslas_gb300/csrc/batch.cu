@@ -35,6 +35,7 @@ struct tbslas_batch_s {
   tbslas_ctx ctx = nullptr;
   int device = 0, num_sms = 0;
   int n = 0, nrk = 1, bc = 0;
+  bool counted = false;  // counted in the context's live objects
   bool df = false;  // double-float sums (the context's mode at creation), else FP64
   std::vector<BatchProblem> h_probs;
   std::vector<tbslas_tree> trees;   // every velocity and concentration tree
@@ -346,6 +347,8 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     tbslas_batch_destroy(b);
     return st;
   }
+  b->counted = true;
+  ctx_count_object(ctx, +1);
   *out = b;
   return TBSLAS_OK;
 }
@@ -353,6 +356,7 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
 int tbslas_batch_destroy(tbslas_batch b) {
   if (!b) return TBSLAS_OK;
   DeviceRestore restore;
+  if (b->counted) ctx_count_object(b->ctx, -1);
   cudaSetDevice(b->device);
   cudaDeviceSynchronize();
   drop_graph(b);

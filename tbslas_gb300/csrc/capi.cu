@@ -165,6 +165,7 @@ struct tbslas_ctx_s {
   int sums = TBSLAS_SUMS_FP64;  // arithmetic of the SL steps' Chebyshev sums
   uint32_t wait_limit = kWaitLimit;  // polls of the bounded device-side waits
   bool profile = false;
+  int64_t live_objects = 0;     // trees and batches created on this context, not yet destroyed
   int64_t* h_pinned = nullptr;  // small pinned host buffer for scalar read-backs
   std::vector<ProfRecord> prof_pending;
   std::vector<cudaEvent_t> prof_pool;
@@ -173,6 +174,8 @@ struct tbslas_ctx_s {
 
 struct tbslas_tree_s {
   tbslas_ctx ctx = nullptr;
+  int device = 0;        // the context's device (the tree's arrays live there)
+  bool counted = false;  // counted in ctx->live_objects
   int64_t L = 0;
   int q = 0, dof = 0, max_depth = 0, T = 0;
   int64_t stride = 0;
@@ -1325,6 +1328,7 @@ int ctx_info(tbslas_ctx ctx, int* device, int* num_sms) {
 
 uint32_t* ctx_err(tbslas_ctx ctx) { return ctx ? ctx->d_err : nullptr; }
 int ctx_sums(tbslas_ctx ctx) { return ctx->sums; }
+void ctx_count_object(tbslas_ctx ctx, int delta) { ctx->live_objects += delta; }
 int ctx_c2_scratch(tbslas_ctx ctx, size_t n, float2** out) {
   return scratch_t(ctx, kAdjC2, n, out);
 }
@@ -1394,6 +1398,10 @@ int tbslas_ctx_create(int device, tbslas_ctx* out) {
 
 int tbslas_ctx_destroy(tbslas_ctx ctx) {
   if (!ctx) return TBSLAS_OK;
+  if (ctx->live_objects > 0)
+    return fail(TBSLAS_ERR_INVALID_ARG,
+                "%lld trees or batches of this context are still alive; destroy them first",
+                (long long)ctx->live_objects);
   DeviceRestore restore;
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
@@ -1527,6 +1535,7 @@ int tbslas_tree_create(tbslas_ctx ctx, int64_t n_leaves, const double* anchor_ho
   if (dof < 1 || dof > 16) return fail(TBSLAS_ERR_UNSUPPORTED, "dof %d outside [1,16]", dof);
   tbslas_tree t = new tbslas_tree_s();
   t->ctx = ctx;
+  t->device = ctx->device;
   t->L = n_leaves;
   t->q = q;
   t->dof = dof;
@@ -1538,6 +1547,8 @@ int tbslas_tree_create(tbslas_ctx ctx, int64_t n_leaves, const double* anchor_ho
     g_err = msg;
     return s;
   }
+  t->counted = true;
+  ctx->live_objects += 1;
   *out = t;
   return TBSLAS_OK;
 }
@@ -1545,7 +1556,8 @@ int tbslas_tree_create(tbslas_ctx ctx, int64_t n_leaves, const double* anchor_ho
 int tbslas_tree_destroy(tbslas_tree t) {
   if (!t) return TBSLAS_OK;
   DeviceRestore restore;
-  if (t->ctx) cudaSetDevice(t->ctx->device);
+  if (t->counted) t->ctx->live_objects -= 1;
+  cudaSetDevice(t->device);
   if (t->d_keys) cudaFree(t->d_keys);
   if (t->d_geom) cudaFree(t->d_geom);
   if (t->d_coeff) cudaFree(t->d_coeff);
@@ -1605,6 +1617,7 @@ int tbslas_tree_construct(tbslas_ctx ctx, const tbslas_field* field, int q, doub
   TRY(upload_field(ctx, field, &prm, s));
   tbslas_tree t = new tbslas_tree_s();
   t->ctx = ctx;
+  t->device = ctx->device;
   t->q = q;
   t->dof = field_dof(field->kind);
   t->stride = (t->dof * n_coeff(q) + 1) & ~(int64_t)1;
@@ -1618,6 +1631,8 @@ int tbslas_tree_construct(tbslas_ctx ctx, const tbslas_field* field, int q, doub
     g_err = msg;
     return st;
   }
+  t->counted = true;
+  ctx->live_objects += 1;
   *out = t;
   return TBSLAS_OK;
 }
@@ -1992,11 +2007,12 @@ ProfBracket::~ProfBracket() {
   }
 }
 
-int step_points_df(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
-                   int bc, double** xmid, double** xdep, cudaStream_t s) {
+int step_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
+                int bc, double** xmid, double** xdep, cudaStream_t s) {
   TRY(check_step_args(ctx, vel, con, dt, 1, bc));
   const int q = con->q;
-  if (vel->q != q || con->dof != 1 || !g_kernels[q].points_df)
+  const bool df = ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT;
+  if (vel->q != q || con->dof != 1 || !g_kernels[q].points_df || !g_kernels[q].points_fp64)
     return fail(TBSLAS_ERR_UNSUPPORTED, "step points: degree %d", q);
   const int64_t N = con->L * n_points(q);
   SemilagTreeArgs a;
@@ -2021,8 +2037,8 @@ int step_points_df(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timeste
   TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
   a.fix_grid = ctx->num_sms * 8;
   {
-    ProfScope pp(ctx, "adjoint_points", s, 2);
-    g_kernels[q].points_df(a, s);
+    ProfScope pp(ctx, "adjoint_points", s, df ? 2 : 1);
+    (df ? g_kernels[q].points_df : g_kernels[q].points_fp64)(a, s);
   }
   TRY(check_launch("step points"));
   *xmid = a.xmid;

@@ -150,6 +150,7 @@ struct DegreeKernels {
   SemilagTreeFn semilag = nullptr;     // FP64 fused step
   SemilagTreeFn semilag_df = nullptr;  // double-float fused step + FP64 pass over near-face targets
   SemilagTreeFn points_df = nullptr;   // its midpoints and departure points only (q <= 10)
+  SemilagTreeFn points_fp64 = nullptr;  // the FP64 step's midpoints and departure points (q <= 10)
   TrajFn traj = nullptr;
   EvalTilesFn eval_tiles = nullptr;
   int eval_tiles_max_threads_hint = 0;
@@ -212,10 +213,11 @@ int step_midpoints(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timeste
 void launch_midpoints(const TreeView& con, const Nodes1D& nodes, int q, double tau, int periodic,
                       const double* vn, double* xmid, cudaStream_t s);
 // The midpoints and departure points of that step only, into scratch of the
-// context (*xmid, *xdep: [Lc * Np][3]), for the double-float adjoint's
-// recompute: the double-float step's kernels, FP64 for ambiguous targets.
-int step_points_df(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
-                   int bc, double** xmid, double** xdep, cudaStream_t s);
+// context (*xmid, *xdep: [Lc * Np][3]), for the adjoint's recompute: the
+// step's own kernels in the context's sums mode (double-float: FP64 for the
+// ambiguous targets).
+int step_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
+                int bc, double** xmid, double** xdep, cudaStream_t s);
 
 // node_eval.cu: src evaluated at every node of dst's leaves, [dst.L * Np][src.dof]
 // (bit-identical to the pointwise FP64 evaluation)
@@ -272,6 +274,8 @@ void launch_batch_refit(const RefitJob* jobs, const RefitItem* items, int64_t n_
 void launch_split(const double* c, float2* c2, int64_t n, uint32_t* err, cudaStream_t s);
 uint32_t* ctx_err(tbslas_ctx ctx);
 int ctx_sums(tbslas_ctx ctx);
+// Trees and batches alive on a context (tbslas_ctx_destroy refuses while any are).
+void ctx_count_object(tbslas_ctx ctx, int delta);
 int ctx_c2_scratch(tbslas_ctx ctx, size_t n, float2** out);
 int ctx_wnode_scratch(tbslas_ctx ctx, size_t n, double** out);
 int ctx_vn_scratch(tbslas_ctx ctx, size_t n, double** out);

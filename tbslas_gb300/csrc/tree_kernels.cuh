@@ -137,7 +137,9 @@ __device__ __forceinline__ void store_point(double* p, int64_t t, double x, doub
 //   value   = c(X)                                     (semilag.inc:43)
 // Targets and departure points never touch memory; only the node values are
 // written, [leaf][node], for the refit.
-template <int D>
+// POINTS: only the midpoints and departure points (xmid, xdep required, vn
+// given, nrk = 1) -- the adjoint's recomputation; no value is written.
+template <int D, bool POINTS = false>
 __global__ void __launch_bounds__(128) k_semilag_tree(const SemilagTreeArgs a) {
   constexpr int NP = D * D * D;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -156,6 +158,7 @@ __global__ void __launch_bounds__(128) k_semilag_tree(const SemilagTreeArgs a) {
   else
     rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
   store_point(a.xdep, t, x, y, z);
+  if (POINTS) return;
   double c[1];
   eval_point<D, 1>(a.con, x, y, z, per, c);
   a.vals[t] = c[0];
@@ -294,6 +297,16 @@ void launch_semilag_tree_df(const SemilagTreeArgs& a, cudaStream_t s) {
   k_semilag_fix<D><<<a.fix_grid, threads, 0, s>>>(a);
 }
 
+// Midpoints and departure points only, FP64 (the FP64 adjoint's recompute).
+template <int D>
+void launch_points_fp64(const SemilagTreeArgs& a, cudaStream_t s) {
+  constexpr int NP = D * D * D;
+  const int64_t n = a.con.L * NP;
+  const int threads = 128;
+  const int64_t blocks = (n + threads - 1) / threads;
+  if (blocks > 0) k_semilag_tree<D, true><<<(unsigned)blocks, threads, 0, s>>>(a);
+}
+
 // Midpoints and departure points only (the double-float adjoint's recompute).
 template <int D>
 void launch_points_df(const SemilagTreeArgs& a, cudaStream_t s) {
@@ -405,7 +418,10 @@ void register_degree(DegreeKernels* table) {
   table[D - 1].semilag_df = &launch_semilag_tree_df<D>;
   table[D - 1].traj = &launch_traj<D>;
   table[D - 1].eval_tiles = &launch_eval_tiles<D>;
-  if constexpr (D <= 11) table[D - 1].points_df = &launch_points_df<D>;  // the adjoint's degrees
+  if constexpr (D <= 11) {  // the adjoint's degrees
+    table[D - 1].points_df = &launch_points_df<D>;
+    table[D - 1].points_fp64 = &launch_points_fp64<D>;
+  }
 }
 
 }  // namespace tbg

@@ -17,6 +17,55 @@ def test_flop_accounting_matches_reference_model():
     assert total8 == 27 * 9 + 16 * 165 + 18
 
 
+def test_fused_kernel_flop_accounting():
+    """The fused step kernel's own work: one velocity evaluation after the
+    node-grid first stage, one concentration evaluation and the RK2 updates."""
+    d, nc = 15, 680
+    assert bench.fused_flops_per_point_tree(14) == (9 * d + 2 * nc * 3) + 18 + (9 * d + 2 * nc)
+    assert bench.fused_flops_per_point_tree(8, nrk=2) == 3 * (81 + 990) + 36 + (81 + 330)
+
+
+def test_reference_arm_workload_loads_no_library_code():
+    """The reference arm builds its inputs with the oracle's nodes and
+    pseudo-inverse: the process never maps the library under test, and the
+    trees are the same as the library-built workload's."""
+    import subprocess
+    import sys
+    code = ("import bench, json; wl = bench.oracle_workload('tree_uniform_q8'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print(json.dumps([wl.describe(), 'libtbslas_gb300' in maps]))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=os.path.dirname(bench.__file__),
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    import json
+    desc, mapped = json.loads(out.stdout.strip().splitlines()[-1])
+    assert mapped is False
+    from tbslas_gb300 import workloads
+    assert desc == json.loads(json.dumps(workloads.make("tree_uniform_q8").describe()))
+
+
+def test_bubble_directions_vanish_on_leaf_faces(ora):
+    """The velocity FD directions of the adjoint check vanish on every leaf
+    face (evaluated through the oracle at points on the faces)."""
+    import numpy as np
+    from tbslas_gb300 import trees
+    wl = type("W", (), {})()
+    wl.q = 8
+    wl.a, wl.d = trees.uniform_tree(2)
+    dirs = bench.bubble_directions(wl, np.random.default_rng(0), 2)
+    rng = np.random.default_rng(1)
+    pts = rng.uniform(0, 1, size=(3000, 3))
+    face = np.round(pts * 4) / 4  # snap one coordinate per point to a face of the 4^3 grid
+    axis = rng.integers(0, 3, size=len(pts))
+    pts[np.arange(len(pts)), axis] = face[np.arange(len(pts)), axis]
+    inner = rng.uniform(0.05, 0.95, size=(3000, 3)) / 4 + np.floor(rng.uniform(0, 4, (3000, 3))) / 4
+    for dv in dirs:
+        on = ora.eval_tree(wl.a, wl.d, wl.q, 3, dv, pts)
+        off = ora.eval_tree(wl.a, wl.d, wl.q, 3, dv, inner)
+        assert np.abs(on).max() <= 1e-12 * np.abs(off).max()
+        assert np.abs(off).max() > 0.1
+
+
 def _free_port():
     s = socket.socket()
     s.bind(("127.0.0.1", 0))

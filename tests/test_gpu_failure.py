@@ -40,3 +40,19 @@ def test_bounded_wait_runs_out_and_context_stays_usable(ctx, ora, q, dof):
     ref = ora.eval_tree(anchor, depth, q, dof, coeff, pts)
     assert np.array_equal(out, ref)
     assert ctx.take_device_error() == 0
+
+
+def test_context_is_destroyed_only_after_its_trees():
+    """The C ABI refuses to destroy a context whose trees are alive (it would
+    leave them pointing at freed state) and leaves the context usable; the
+    Python Context closes its trees first."""
+    from tbslas_gb300 import capi
+    c = tb.Context(0)
+    a, d = trees.uniform_tree(1)
+    t = tb.Tree(c, a, d, 3, 1)
+    st = capi.lib().tbslas_ctx_destroy(c.handle)
+    assert st == 1 and "still alive" in capi.last_error()
+    t.set_coeffs(np.ones(t.coeff_shape))  # the context and its tree still work
+    assert np.array_equal(t.get_coeffs(), np.ones(t.coeff_shape))
+    c.close()
+    assert t.handle is None and c.handle is None
