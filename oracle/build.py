@@ -1,9 +1,10 @@
 """Build recipe for the oracle's C++ restatement (test infrastructure only).
 
 Compiles oracle/oracle.cpp into oracle/_build/liboracle.so with g++ and
-OpenMP.  The reference itself cannot be compiled here (it needs PVFMM, MPI,
-BLAS/LAPACK and FFTW, none of which are vendored or installed), so there is no
-oracle/_ref build.
+OpenMP.  The reference's own SL-path code is built separately into
+oracle/_ref by oracle/build_ref.py (its drivers need PVFMM, MPI, BLAS/LAPACK
+and FFTW, which are absent; the SL-path headers compile against the
+stand-ins of oracle/ref_stubs/).
 """
 import os
 import platform

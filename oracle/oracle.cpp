@@ -5,12 +5,17 @@
 // and by bench.py's CPU-baseline leg, always as the checker or the timed CPU
 // reference, never as the thing measured on the GPU.
 //
-// Parity status: the reference cannot be built (its PVFMM dependency is not
-// vendored) and ships no golden vectors, so this restatement is pinned by the
-// analytic known-answer tests in tests/test_oracle.py (polynomial exactness,
-// rotation return, translation, time reversal) and by tests/golden/ fixtures
-// generated from it; against the reference's own binary outputs it is
-// "parity unpinned".
+// Parity status: pinned.  The reference's SL-path sources (traj.inc,
+// semilag.inc, tree_functor.h, tree_utils.h, tree_semilag.h, cheb.h) compile
+// here against stand-ins for PVFMM and MPI (oracle/ref_stubs/, recipe
+// oracle/build_ref.py, library oracle/_ref/libref.so); tests/test_ref_pin.py
+// and the fixtures tests/golden/ref_*.npz written from that library check
+// this restatement against it: Chebyshev nodes, grid points, tree
+// evaluation, trajectories and the tricubic interpolant bit for bit, the
+// in-situ step to the pseudo-inverse's and GEMM's rounding.  PVFMM's own
+// routines (MortonId, cheb_poly, cheb_eval, pinv, GEMM) are restated in both
+// places from their published algorithms; PVFMM is not vendored.  The
+// analytic known-answer tests of tests/test_oracle.py pin the physics.
 //
 // Every routine cites the reference file:line it restates (paths relative to
 // the tbslas source tree).  PVFMM routines that the reference calls but that
@@ -89,9 +94,13 @@ static std::vector<Real> new_nodes(int deg, int dim) {
 // src/tree/tree_functor.h:328-330 (three-term recurrence, 2x*T_{k-1}-T_{k-2}).
 //
 // Multiply-adds are written as explicit fused multiply-adds (std::fma)
-// wherever a contracting compiler fuses them in the reference's build (the
-// recurrence, vec_eval's accumulations, the RK2 updates), so the oracle's
-// rounding is fixed and the same on every host.
+// exactly where g++ -O3 -ffp-contract=fast for an FMA target (with a tuning
+// that fuses accumulation chains) fuses them when it compiles the
+// reference's own sources -- the recurrence, vec_eval's accumulations, the
+// RK2 updates, fast_interp's accumulation -- so the oracle's rounding is
+// fixed and the same on every host.  tests/test_ref_pin.py checks the oracle
+// bit for bit against that build of the reference (oracle/_ref, recipe
+// oracle/build_ref.py).
 template <class R>
 static void cheb_poly(int q, const R* in, int n, R* out) {
   for (int j = 0; j < n; j++) {
@@ -468,7 +477,7 @@ static void fast_interp(const Real* grid, int dof, int Nr, Real* pts, size_t n, 
           Real M1M2 = M[1][j1] * M[2][j2];
           long ij = Nr * (idx[1][j1] + Nr * idx[2][j2]);
           for (int j0 = 0; j0 < 4; j0++)
-            val += M[0][j0] * M1M2 * grid[idx[0][j0] + ij + k * N3];
+            val = std::fma(M[0][j0] * M1M2, grid[idx[0][j0] + ij + k * N3], val);
         }
       out[i * dof + k] = val;
     }

@@ -1,0 +1,98 @@
+"""Writes tests/golden/ref_pin.npz: outputs of the reference's own SL-path
+code (oracle/_ref, built from the reference's sources by
+oracle/build_ref.py) on small seeded cases.  Run from the repository root
+where the reference's sources are present:
+
+    python tests/golden/make_ref_golden.py
+
+The inputs are built with the oracle's set-up math only (its Chebyshev nodes
+and pseudo-inverse).  tests/test_ref_pin.py checks the oracle against these
+vectors on every machine (bit for bit where the arithmetic is the same) and
+the CUDA path against them on the GPU."""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as ora  # noqa: E402
+from oracle import ref  # noqa: E402
+from tbslas_gb300 import fields, trees  # noqa: E402
+
+
+def oracle_math():
+    def nodes(q):
+        return ora.collect_grid_points(np.zeros((1, 3)), np.zeros(1, dtype=np.int32), q)
+    return trees.HostMath(nodes=nodes, pt2coeff=ora.pt2coeff)
+
+
+def special_points(rng, n):
+    """Points in [0,1]^3 with leaf faces, the domain faces and 1.0 among them."""
+    p = rng.uniform(0.0, 1.0, size=(n, 3))
+    p[:8] = [[1.0, 0.5, 0.5], [0.0, 0.0, 0.0], [1.0, 1.0, 1.0], [0.5, 0.5, 0.5],
+             [0.25, 0.75, 1.0], [0.125, 0.375, 0.0], [1.0 - 2 ** -53, 0.5, 0.25],
+             [0.5, 0.0625, 0.9375]]
+    return p
+
+
+def main():
+    if ref.lib() is None:
+        raise SystemExit("the reference's sources are not present; nothing to generate")
+    rng = np.random.default_rng(2024)
+    out = {}
+    with trees.host_math(oracle_math()):
+        blob = fields.gaussian((0.35, 0.6, 0.45), 0.07)
+        a, d = trees.adaptive_tree(blob, 4, 1, 1e-3, 1, 2)
+        out["tree_anchor"], out["tree_depth"] = a, d
+        out["collect_q3"] = ref.collect_grid_points(a, d, 3)
+        for q in (6, 8, 14):
+            out["nodes_q%d" % q] = ref.new_nodes(q)
+        ua1, ud1 = trees.uniform_tree(1)
+        out["tree1_anchor"], out["tree1_depth"] = ua1, ud1
+        for q, dof in ((5, 1), (8, 3), (14, 1)):
+            ta, td = (a, d) if q < 14 else (ua1, ud1)  # q = 14 on the 8-leaf tree
+            c = rng.standard_normal((len(td), dof, ref.nc(q))) / (1 + np.arange(ref.nc(q)))
+            out["eval_q%d_coeff" % q] = c
+            for bc in (0, 1):
+                p = (special_points(rng, 1000) if bc == 0
+                     else rng.uniform(-0.05, 1.05, size=(1000, 3)))
+                out["eval_q%d_bc%d_pts" % (q, bc)] = p
+                out["eval_q%d_bc%d_out" % (q, bc)] = ref.eval_tree(ta, td, q, dof, c, p, bc)
+        q = 8
+        ua, ud = trees.uniform_tree(1)
+        vt = trees.fit(fields.taylor_green(), ua, ud, q, 3)
+        out["traj_anchor"], out["traj_depth"], out["traj_vc"] = ua, ud, vt
+        x = special_points(rng, 1000)
+        out["traj_pts"] = x
+        for bc, nrk in ((0, 1), (1, 1), (0, 3)):
+            out["traj_bc%d_nrk%d" % (bc, nrk)] = ref.traj_rk2(ua, ud, q, vt, x, 0.3, 0.25, nrk,
+                                                                bc)
+        N = 12
+        g = rng.standard_normal((3, N, N, N))
+        pg = rng.uniform(-0.1, 1.1, size=(2000, 3))
+        pg[:4] = [[1.0, 1.0, 1.0], [0.0, 0.0, 0.0], [0.5, 1.0, 0.0], [1 - 1e-17, 0.3, 0.3]]
+        out["interp_grid"], out["interp_pts"] = g, pg
+        out["interp_out"] = ref.fast_interp(g, 3, N, pg)
+        # one in-situ step (dof 1): Taylor-Green velocity tree, Gaussian blobs
+        q = 6
+        va, vd = trees.adaptive_tree(fields.taylor_green(), 4, 3, 1e-2, 1, 2)
+        blobs = fields.gaussian_blobs(rng, 3, (0.05, 0.1))
+        ca, cd = trees.adaptive_tree(blobs, 4, 1, 1e-3, 1, 2)
+        vc = trees.fit(fields.taylor_green(), va, vd, q, 3)
+        cc = trees.fit(blobs, ca, cd, q, 1)
+        for k, v in (("va", va), ("vd", vd), ("vc", vc), ("ca", ca), ("cd", cd), ("cc", cc)):
+            out["step_" + k] = v
+        for bc in (0, 1):
+            out["step_bc%d_out" % bc] = ref.semilag_in_situ(
+                dict(anchor=va, depth=vd, q=q, dof=3, coeff=vc),
+                dict(anchor=ca, depth=cd, q=q, dof=1, coeff=cc), 2, 0.02, 1, bc)
+    path = os.path.join(HERE, "ref_pin.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()
