@@ -1,6 +1,7 @@
 """tbslas_eval_tree_noalloc: the tree functor for callers that cannot
-allocate device memory while they evaluate (fixed memory budgets, host-owned
-memory pools, stream capture).  Called through the C ABI and checked against
+allocate device memory while they evaluate (a memory budget fixed up front,
+or a host application whose own pool owns every device allocation).  Called
+through the C ABI and checked against
 tbslas_eval_tree on two calls in a row (the scratch array keeps the previous
 call's contents, so the second call shows it is cleared where it must be)."""
 import ctypes
