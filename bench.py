@@ -521,11 +521,32 @@ def run_gpu(args, wl, rank, world, local_rank):
         step_df(0)
         torch.cuda.synchronize()
         first_df = result_df()
-        for i in range(3):
-            step_df(i + 1)
-        torch.cuda.synchronize()
-        ms_df = timed_steps(n_df, 4, step_df)
-        prof_df = profiled(n_df, 4 + n_df, step_df)
+        if is_grid:
+            # the velocity is stationary: n_df steps in one call split its
+            # hi/lo copy once (tbslas_semilag_grid_steps)
+            def steps_df(k, _first_step):
+                tb.semilag_grid_steps(ctx, vel, gb[0], N, wl.dt, k, 1, wl.bc, out=gb[1])
+            steps_df(3, 1)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            steps_df(n_df, 4)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_df = e0.elapsed_time(e1)
+            ctx.profile(True)
+            ctx.profile_reset()
+            steps_df(n_df, 4)
+            torch.cuda.synchronize()
+            prof_df = ctx.profile_totals()
+            ctx.profile(False)
+        else:
+            for i in range(3):
+                step_df(i + 1)
+            torch.cuda.synchronize()
+            ms_df = timed_steps(n_df, 4, step_df)
+            prof_df = profiled(n_df, 4 + n_df, step_df)
         fixed = None if is_grid else ctx.last_fp64_targets()
     df_launch_ms = prof_df.get(dominant, (1, 0, 0.0))[2] / max(prof_df.get(dominant, (1,))[0], 1)
 

@@ -448,6 +448,17 @@ int tbslas_semilag_grid(tbslas_ctx ctx, const double* vel_dev, const double* con
  * con_out_host[N^3] out. */
 int tbslas_semilag_grid_host(tbslas_ctx ctx, const double* vel_host, const double* con_host,
                              double* con_out_host, int n_reg, double dt, int nrk, int bc);
+/* nsteps grid SL steps through one stationary velocity (a driver's time loop
+ * over tbslas_semilag_grid with an unchanged velocity grid): con_dev is the
+ * initial concentration, con_out_dev (not aliasing it) the result after
+ * nsteps.  The intermediate steps ping-pong through con_out_dev and a
+ * context scratch grid.  In the double-float mode the velocity's hi/lo split
+ * is made once per call instead of once per step.  No single-call reference
+ * counterpart (the reference loops; the velocity is stationary there too,
+ * tree_functor.h:808-811). */
+int tbslas_semilag_grid_steps(tbslas_ctx ctx, const double* vel_dev, const double* con_dev,
+                              double* con_out_dev, int n_reg, double dt, int nsteps, int nrk,
+                              int bc, void* stream);
 
 #ifdef __cplusplus
 }

@@ -9,5 +9,5 @@ from .api import (  # noqa: F401
     Field, NodeFieldFunctor, Periodic, Tree, construct_tree, cubic_time_weights,
     collect_cheb_tree_grid_points,
     compute_traj_rk2, fast_interp, get_pt2coeff_matrix, n_coeff, n_points, new_nodes,
-    semilag_grid, set_tree_grid_values, solve_semilag_bdf2, solve_semilag_in_situ,
+    semilag_grid, semilag_grid_steps, set_tree_grid_values, solve_semilag_bdf2, solve_semilag_in_situ,
     solve_semilag_in_situ_tv)

@@ -573,6 +573,18 @@ def fast_interp(ctx, grid, dof, n_reg, pts, bc=FreeSpace, out=None, stream=None)
     return out
 
 
+def semilag_grid_steps(ctx, vel, con, n_reg, dt, nsteps, num_rk_step=1, bc=Periodic, out=None,
+                       stream=None):
+    """nsteps grid SL steps through one stationary velocity (CUDA tensors):
+    the concentration after nsteps (out must not alias con)."""
+    import torch
+    if out is None:
+        out = torch.empty_like(con)
+    call("tbslas_semilag_grid_steps", ctx.handle, _ptr(vel), _ptr(con), _ptr(out), int(n_reg),
+         float(dt), int(nsteps), int(num_rk_step), int(bc), _stream(stream))
+    return out
+
+
 def semilag_grid(ctx, vel, con, n_reg, dt, num_rk_step=1, bc=Periodic, out=None, stream=None):
     """One grid SL step.  vel [3,N,N,N], con [N,N,N] (CUDA tensors or numpy arrays)."""
     if isinstance(con, np.ndarray):

@@ -83,6 +83,7 @@ SIGNATURES = {
     "tbslas_fast_interp": [_vp, _vp, _i32, _i32, _vp, _i64, _vp, _i32, _vp],
     "tbslas_semilag_grid": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _i32, _vp],
     "tbslas_semilag_grid_host": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _i32],
+    "tbslas_semilag_grid_steps": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _i32, _i32, _vp],
 }
 _RESTYPES = {"tbslas_status_string": _c.c_char_p, "tbslas_last_error": _c.c_char_p}
 

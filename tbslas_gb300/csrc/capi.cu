@@ -96,6 +96,7 @@ enum Slot {
   kVN,
   kGridV2,
   kGridC2,
+  kGridTmp,
   kAdjC2,
   kAdjW,
   // re-meshing: two sets of leaf arrays (ping-pong) and the temporaries
@@ -589,15 +590,19 @@ int collect_dev(tbslas_tree tree, double* out, cudaStream_t s) {
 
 // The grid step: double-float stencil sums on periodic grids (unless the
 // context asks for FP64 sums), FP64 otherwise.
+// split_vel = false: the previous call of this context split the same,
+// unchanged velocity grid (a multi-step call), so its hi/lo copy is reused.
 int semilag_grid_dev(tbslas_ctx ctx, const double* vel, const double* con, double* cout,
-                     int n_reg, double tau, int nrk, int bc, cudaStream_t s) {
+                     int n_reg, double tau, int nrk, int bc, cudaStream_t s,
+                     bool split_vel = true) {
   if (bc == TBSLAS_BC_PERIODIC && ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT) {
     const int64_t n3 = (int64_t)n_reg * n_reg * n_reg;
     float2 *v2, *c2;
     TRY(scratch_t(ctx, kGridV2, n3 * 3, &v2));
     TRY(scratch_t(ctx, kGridC2, n3, &c2));
-    ProfScope p(ctx, "semilag_grid", s, 3);
-    launch_semilag_grid_df(vel, con, cout, n_reg, tau, nrk, v2, c2, ctx->d_err, ctx->num_sms, s);
+    ProfScope p(ctx, "semilag_grid", s, split_vel ? 3 : 2);
+    launch_semilag_grid_df(vel, con, cout, n_reg, tau, nrk, v2, c2, ctx->d_err, ctx->num_sms,
+                           split_vel, s);
     return check_launch("semilag_grid");
   }
   ProfScope p(ctx, "semilag_grid", s);
@@ -2101,6 +2106,27 @@ int tbslas_semilag_grid(tbslas_ctx ctx, const double* vel_dev, const double* con
   const double tau = (-dt - 0.0) / nrk;
   return semilag_grid_dev(ctx, vel_dev, con_dev, con_out_dev, n_reg, tau, nrk, bc,
                           (cudaStream_t)stream);
+}
+
+int tbslas_semilag_grid_steps(tbslas_ctx ctx, const double* vel_dev, const double* con_dev,
+                              double* con_out_dev, int n_reg, double dt, int nsteps, int nrk,
+                              int bc, void* stream) {
+  DeviceRestore restore;
+  TRY(check_grid_args(ctx, vel_dev, con_dev, con_out_dev, n_reg, dt, nrk, bc));
+  if (nsteps < 1) return fail(TBSLAS_ERR_INVALID_ARG, "nsteps %d < 1", nsteps);
+  const int64_t n3 = (int64_t)n_reg * n_reg * n_reg;
+  double* tmp = nullptr;
+  if (nsteps > 1) TRY(scratch_t(ctx, kGridTmp, n3, &tmp));
+  const double tau = (-dt - 0.0) / nrk;
+  cudaStream_t s = (cudaStream_t)stream;
+  const double* in = con_dev;
+  for (int k = 0; k < nsteps; ++k) {
+    // the last step writes con_out_dev; steps alternate between it and tmp
+    double* out = ((nsteps - 1 - k) % 2 == 0) ? con_out_dev : tmp;
+    TRY(semilag_grid_dev(ctx, vel_dev, in, out, n_reg, tau, nrk, bc, s, k == 0));
+    in = out;
+  }
+  return TBSLAS_OK;
 }
 
 int tbslas_semilag_grid_host(tbslas_ctx ctx, const double* vel_host, const double* con_host,

@@ -389,11 +389,11 @@ void launch_semilag_grid(const double* vel, const double* con, double* cout, int
 
 void launch_semilag_grid_df(const double* vel, const double* con, double* cout, int nreg,
                             double tau, int nrk, float2* vel2, float2* con2, uint32_t* err,
-                            int num_sms, cudaStream_t s) {
+                            int num_sms, bool split_vel, cudaStream_t s) {
   const int64_t n = (int64_t)nreg * nreg * nreg;
   const bool pow2 = (nreg & (nreg - 1)) == 0;
   const int split_grid = num_sms * 8;
-  k_split_grid<<<split_grid, 256, 0, s>>>(vel, vel2, 3 * n, err);
+  if (split_vel) k_split_grid<<<split_grid, 256, 0, s>>>(vel, vel2, 3 * n, err);
   k_split_grid<<<split_grid, 256, 0, s>>>(con, con2, n, err);
   int nl = -1;
   if (pow2)

@@ -330,9 +330,10 @@ void launch_fast_interp(const double* grid, int dof, int nreg, const double* pts
 void launch_semilag_grid(const double* vel, const double* con, double* cout, int nreg,
                          double tau, int nrk, int periodic, cudaStream_t s);
 // periodic grids, stencil sums in double-float over hi/lo copies of the grids
-// (vel2: 3 n^3, con2: n^3 float2 scratch)
+// (vel2: 3 n^3, con2: n^3 float2 scratch); split_vel = false reuses vel2 as
+// the previous call on the same velocity left it
 void launch_semilag_grid_df(const double* vel, const double* con, double* cout, int nreg,
                             double tau, int nrk, float2* vel2, float2* con2, uint32_t* err,
-                            int num_sms, cudaStream_t s);
+                            int num_sms, bool split_vel, cudaStream_t s);
 
 }  // namespace tbg

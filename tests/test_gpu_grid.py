@@ -102,3 +102,28 @@ def test_semilag_grid_nan_velocity_matches_fp64_sums(ctx, N):
     with pytest.raises(tb.capi.TbslasError) as e:
         ctx.check()
     assert e.value.status == 7  # TBSLAS_ERR_DEVICE
+
+
+@pytest.mark.parametrize("mode", ["fp64", "df"])
+@pytest.mark.parametrize("bc,N", [(1, 32), (1, 20), (0, 24)])
+def test_grid_steps_equal_repeated_single_steps(ctx, mode, bc, N):
+    """tbslas_semilag_grid_steps (one stationary velocity, split once in the
+    double-float mode) equals the same number of single steps bit for bit."""
+    import torch
+    rng = np.random.default_rng(N + bc)
+    vel = fields.fourier_velocity_grid(rng, N) if bc else rng.standard_normal((3, N, N, N)) * 0.3
+    con = (fields.periodic_blob_grid(N, (0.4, 0.55, 0.5), 0.12) if bc
+           else rng.standard_normal((N, N, N)))
+    dt = 1.5 / N
+    v, c0 = _dev(vel), _dev(con)
+    with ctx.sums_mode(tb.SUMS_FP64 if mode == "fp64" else tb.SUMS_DOUBLE_FLOAT):
+        a, b = c0.clone(), torch.empty_like(c0)
+        for k in range(5):
+            tb.semilag_grid(ctx, v, a, N, dt, 1, bc, out=b)
+            a, b = b, a
+        many = tb.semilag_grid_steps(ctx, v, c0, N, dt, 5, 1, bc)
+        one = tb.semilag_grid_steps(ctx, v, c0, N, dt, 1, 1, bc)
+        single = tb.semilag_grid(ctx, v, c0, N, dt, 1, bc)
+    assert torch.equal(many, a)
+    assert torch.equal(one, single)
+    assert np.abs(many.cpu().numpy()).max() > 0
