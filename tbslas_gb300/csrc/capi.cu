@@ -1960,7 +1960,17 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
   a.nrk = nrk;
   a.periodic = bc;
   for (int j = 0; j < 2 * nrk * m; ++j) a.w[j] = w[j];
-  TRY(scratch_t(ctx, kVals, con->L * n_points(con->q), &a.vals));
+  const int64_t N = con->L * n_points(con->q);
+  TRY(scratch_t(ctx, kVals, N, &a.vals));
+  {
+    // first stage: every tree at the target nodes by sum factorisation
+    double* vn = nullptr;
+    TRY(scratch_t(ctx, kVN, (size_t)m * N * 3, &vn));
+    ProfScope pv(ctx, "vel_at_nodes", s, 2 * m);
+    for (int k = 0; k < m; ++k) launch_eval_on_nodes(vel[k]->view(), a.con, bc, vn + 3 * k * N, s);
+    TRY(check_launch("velocity set at nodes"));
+    a.vn = vn;
+  }
   {
     ProfScope p(ctx, "semilag_tv", s);
     g_tv[con->q](a, s);

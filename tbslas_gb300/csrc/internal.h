@@ -133,6 +133,10 @@ struct TvArgs {
   int nrk;
   int periodic;
   double* vals;  // [con.L * Np]
+  // the trees' velocities at the targets (first stage of the first
+  // sub-step), tree k at vn + 3 k con.L Np, from the node-grid pass
+  // (bit-identical to evaluating them there), or null
+  const double* vn = nullptr;
   double w[2 * kTvMaxSubsteps * kTvMaxTrees];
 };
 typedef void (*TvFn)(const TvArgs&, cudaStream_t);

@@ -6,9 +6,10 @@
 // 47-78) as IntegrateRK2 calls them at each stage (src/semilag/traj.inc:
 // 20-45, :71-93).  This is the general kernel, instantiated per degree by
 // tv_deg_*.cu: every tree is evaluated at every stage point in FP64 and the
-// values blended, so the trees may have different leaf structures.  Trees of
-// one structure take the fast path in capi.cu instead (blended coefficients
-// through the fused step).
+// values blended, so the trees may have different leaf structures; the
+// first stage, at the target node, comes from each tree's node-grid pass.
+// In the double-float mode, trees of one structure take the fast path in
+// capi.cu instead (blended coefficients through the fused step).
 #pragma once
 
 #include "tree_kernels.cuh"
@@ -46,7 +47,25 @@ __global__ void __launch_bounds__(128) k_semilag_tv(const TvArgs a) {
 #pragma unroll 1
   for (int s = 0; s < a.nrk; ++s) {
     double v[3];
-    tv_velocity<D>(a, 2 * s, x, y, z, per, v);  // at X (wrapped in place)
+    if (s == 0 && a.vn) {
+      // the trees' values at the target node from the node-grid pass, blended
+      // in the order tv_velocity blends them; X wrapped as eval_point wraps it
+      if (per) {
+        x = wrap1(x);
+        y = wrap1(y);
+        z = wrap1(z);
+      }
+      const int64_t N = a.con.L * NP;
+      v[0] = v[1] = v[2] = 0.0;
+      for (int k = 0; k < a.m; ++k) {
+        const double* u = a.vn + 3 * (k * N + t);
+        v[0] = fma(a.w[k], __ldg(u + 0), v[0]);
+        v[1] = fma(a.w[k], __ldg(u + 1), v[1]);
+        v[2] = fma(a.w[k], __ldg(u + 2), v[2]);
+      }
+    } else {
+      tv_velocity<D>(a, 2 * s, x, y, z, per, v);  // at X (wrapped in place)
+    }
     double px = fma(half_tau, v[0], x), py = fma(half_tau, v[1], y),
            pz = fma(half_tau, v[2], z);
     tv_velocity<D>(a, 2 * s + 1, px, py, pz, per, v);  // at X*
