@@ -394,6 +394,28 @@ int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
                            const double* lambda_next_dev, double* lambda_k_dev,
                            double* grad_vel_dev, const double* xmid_dev, const double* xdep_dev,
                            void* stream);
+/* The same adjoint step inside a sequence of steps through one stationary
+ * velocity tree and one concentration tree shape (the in-situ steps of a
+ * time loop).  Instead of scattering its node term (tau^2/2 J_v(X*)^T g at
+ * every node X) into grad_vel_dev, the step ADDS the per-node weights to
+ * node_weights_dev [N][3] (N = L (q+1)^3, zeroed by the caller before the
+ * sequence's first step); tbslas_semilag_adjoint_node_term then scatters
+ * their sum once, which equals the per-step scatters up to rounding (the
+ * scatter is linear and its nodes and velocity leaves do not change).
+ * vel_at_nodes_dev [N][3] (optional, NULL to compute it per step): the
+ * velocity at the concentration tree's nodes from tbslas_eval_tree_on_nodes,
+ * used where the step rebuilds its points (xmid NULL). */
+int tbslas_semilag_adjoint_seq(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                               const double* con_coeff_k_dev, int timestep, double dt, int bc,
+                               const double* lambda_next_dev, double* lambda_k_dev,
+                               double* grad_vel_dev, const double* xmid_dev,
+                               const double* xdep_dev, const double* vel_at_nodes_dev,
+                               double* node_weights_dev, void* stream);
+/* ADDS the node term of the summed weights to grad_vel_dev [Lv][3][Nc]: the
+ * transposed node-grid pass, once per sequence. */
+int tbslas_semilag_adjoint_node_term(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int bc,
+                                     const double* node_weights_dev, double* grad_vel_dev,
+                                     void* stream);
 
 /* ---- batched in-situ SL --------------------------------------------------------- */
 /* Many independent in-situ SL problems advanced together: problem i is

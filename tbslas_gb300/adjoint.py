@@ -58,6 +58,22 @@ def step_adjoint(vel_functor, tree, coeff_k, timestep, dt, lam_next, lam_k, grad
          api._ptr(lam_k), api._ptr(grad_vel), api._ptr(xmid), api._ptr(xdep), api._stream(stream))
 
 
+def step_adjoint_seq(vel_functor, tree, coeff_k, timestep, dt, lam_next, lam_k, grad_vel,
+                     node_w, xmid=None, xdep=None, vel_at_nodes=None, stream=None):
+    """One adjoint step of a sequence through one stationary velocity: the
+    node term's weights are added to node_w ([N, 3], zeroed before the first
+    step) for node_term to scatter once."""
+    call("tbslas_semilag_adjoint_seq", tree.ctx.handle, vel_functor.tree.handle, tree.handle,
+         api._ptr(coeff_k), int(timestep), float(dt), vel_functor.bc, api._ptr(lam_next),
+         api._ptr(lam_k), api._ptr(grad_vel), api._ptr(xmid), api._ptr(xdep),
+         api._ptr(vel_at_nodes), api._ptr(node_w), api._stream(stream))
+
+
+def node_term(vel_functor, tree, node_w, grad_vel, stream=None):
+    call("tbslas_semilag_adjoint_node_term", tree.ctx.handle, vel_functor.tree.handle,
+         tree.handle, vel_functor.bc, api._ptr(node_w), api._ptr(grad_vel), api._stream(stream))
+
+
 def _function():
     import torch
 
@@ -91,12 +107,22 @@ def _function():
             vf = api.NodeFieldFunctor(vel_tree, ctx.bc)
             lam = grad_cT.contiguous().clone()
             gv = torch.zeros(ctx.vshape, dtype=torch.float64, device=grad_cT.device)
+            # The velocity is one parameter for every step and the tree shapes
+            # stay fixed: the node term's weights are summed over the steps and
+            # scattered once, and where the steps rebuild their points the
+            # velocity at the nodes is evaluated once.
+            n = con_tree.n_leaves * api.n_points(con_tree.q)
+            node_w = torch.zeros((n, 3), dtype=torch.float64, device=grad_cT.device)
+            rebuild = not ctx.ckpts or ctx.ckpts[0][0] is None
+            vn = vf.at_nodes(con_tree) if rebuild and ctx.states else None
             for k in reversed(range(len(ctx.states))):
                 lam_k = torch.empty_like(lam)
                 xm, xd = ctx.ckpts[k] if ctx.ckpts else (None, None)
-                step_adjoint(vf, con_tree, ctx.states[k], ctx.ts0 + k, ctx.dt, lam, lam_k, gv,
-                             xm, xd)
+                step_adjoint_seq(vf, con_tree, ctx.states[k], ctx.ts0 + k, ctx.dt, lam, lam_k, gv,
+                                 node_w, xm, xd, vn)
                 lam = lam_k
+            if ctx.states:
+                node_term(vf, con_tree, node_w, gv)
             return lam, gv, None, None, None, None, None, None, None
 
     return SemilagAdvect

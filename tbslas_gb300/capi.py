@@ -73,6 +73,9 @@ SIGNATURES = {
     "tbslas_semilag_in_situ_ckpt": [_vp, _vp, _vp, _i32, _f64, _i32, _vp, _vp, _vp],
     "tbslas_semilag_adjoint": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _vp, _vp, _vp, _vp, _vp,
                                _vp],
+    "tbslas_semilag_adjoint_seq": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _vp, _vp, _vp, _vp,
+                                   _vp, _vp, _vp, _vp],
+    "tbslas_semilag_adjoint_node_term": [_vp, _vp, _vp, _i32, _vp, _vp, _vp],
     "tbslas_batch_create": [_vp, _i32, _vp, _vp, _vp, _i32, _i32, _c.POINTER(_vp)],
     "tbslas_batch_destroy": [_vp],
     "tbslas_batch_info": [_vp, _i64p, _i64p],

@@ -72,12 +72,16 @@ extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbsl
                                 (cudaStream_t)stream);
 }
 
-extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
-                                      const double* con_coeff_k_dev, int timestep, double dt,
-                                      int bc, const double* lambda_next_dev, double* lambda_k_dev,
-                                      double* grad_vel_dev, const double* xmid_dev,
-                                      const double* xdep_dev, void* stream) {
-  DeviceRestore restore;
+namespace tbg {
+
+// One adjoint step.  vn_given: the velocity at con's nodes (or null); wnode_acc:
+// where the node term's weights are summed over a sequence of steps (null:
+// this step scatters its own).
+int semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                    const double* con_coeff_k_dev, int timestep, double dt, int bc,
+                    const double* lambda_next_dev, double* lambda_k_dev, double* grad_vel_dev,
+                    const double* xmid_dev, const double* xdep_dev, const double* vn_given,
+                    double* wnode_acc, cudaStream_t s) {
   TreeView tv, tc;
   int st = check_pair(ctx, vel, con, dt, bc, &tv, &tc);
   if (st != TBSLAS_OK) return st;
@@ -93,7 +97,6 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   const double* F = nullptr;
   st = ctx_F(ctx, q, &F);
   if (st != TBSLAS_OK) return st;
-  cudaStream_t s = (cudaStream_t)stream;
   // mu = lambda^{k+1} M^T, one row of Np node weights per leaf
   {
     ProfBracket pb(ctx, "adjoint_refit_t", s);
@@ -116,15 +119,18 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   a.xdep = xdep_dev;
   a.lambda = lambda_k_dev;
   a.grad_vel = grad_vel_dev;
-  a.wnode = nullptr;
+  a.wnode = wnode_acc;
+  a.wnode_add = wnode_acc ? 1 : 0;
   const bool df = ctx_sums(ctx) == TBSLAS_SUMS_DOUBLE_FLOAT;
-  st = ctx_wnode_scratch(ctx, tc.L * np * 3, &a.wnode);
-  if (st != TBSLAS_OK) return st;
+  if (!wnode_acc) {
+    st = ctx_wnode_scratch(ctx, tc.L * np * 3, &a.wnode);
+    if (st != TBSLAS_OK) return st;
+  }
   if (!xdep_dev) {
     // recompute: the step's points by its own kernels (double-float: FP64
     // for the ambiguous targets)
     double *xm = nullptr, *xd = nullptr;
-    st = step_points(ctx, vel, con, timestep, dt, bc, &xm, &xd, s);
+    st = step_points(ctx, vel, con, timestep, dt, bc, &xm, &xd, s, vn_given);
     if (st != TBSLAS_OK) return st;
     a.xmid = xm;
     a.xdep = xd;
@@ -132,7 +138,7 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
     // departure points checkpointed: the midpoints from the node-grid
     // velocity, exactly as the forward formed them
     double* xm = nullptr;
-    st = step_midpoints(ctx, vel, con, timestep, dt, bc, &xm, s);
+    st = step_midpoints(ctx, vel, con, timestep, dt, bc, &xm, s, vn_given);
     if (st != TBSLAS_OK) return st;
     a.xmid = xm;
   }
@@ -153,10 +159,57 @@ extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tr
   }
   st = launched("adjoint step launch");
   if (st != TBSLAS_OK) return st;
-  {
+  if (!wnode_acc) {
     // the node term by the transposed node-grid passes
     ProfBracket pb(ctx, "adjoint_node_scatter", s);
     launch_scatter_on_nodes(tv, tc, bc, a.wnode, grad_vel_dev, 3 * nc, df, s);
   }
   return launched("adjoint step launch");
+}
+
+}  // namespace tbg
+
+extern "C" int tbslas_semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                      const double* con_coeff_k_dev, int timestep, double dt,
+                                      int bc, const double* lambda_next_dev, double* lambda_k_dev,
+                                      double* grad_vel_dev, const double* xmid_dev,
+                                      const double* xdep_dev, void* stream) {
+  DeviceRestore restore;
+  return semilag_adjoint(ctx, vel, con, con_coeff_k_dev, timestep, dt, bc, lambda_next_dev,
+                         lambda_k_dev, grad_vel_dev, xmid_dev, xdep_dev, nullptr, nullptr,
+                         (cudaStream_t)stream);
+}
+
+extern "C" int tbslas_semilag_adjoint_seq(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                          const double* con_coeff_k_dev, int timestep, double dt,
+                                          int bc, const double* lambda_next_dev,
+                                          double* lambda_k_dev, double* grad_vel_dev,
+                                          const double* xmid_dev, const double* xdep_dev,
+                                          const double* vel_at_nodes_dev,
+                                          double* node_weights_dev, void* stream) {
+  DeviceRestore restore;
+  if (!node_weights_dev) return fail_status(TBSLAS_ERR_INVALID_ARG, "null node-weight buffer");
+  return semilag_adjoint(ctx, vel, con, con_coeff_k_dev, timestep, dt, bc, lambda_next_dev,
+                         lambda_k_dev, grad_vel_dev, xmid_dev, xdep_dev, vel_at_nodes_dev,
+                         node_weights_dev, (cudaStream_t)stream);
+}
+
+extern "C" int tbslas_semilag_adjoint_node_term(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                                int bc, const double* node_weights_dev,
+                                                double* grad_vel_dev, void* stream) {
+  DeviceRestore restore;
+  TreeView tv, tc;
+  int st = check_pair(ctx, vel, con, 0.0, bc, &tv, &tc);
+  if (st != TBSLAS_OK) return st;
+  if (!node_weights_dev || !grad_vel_dev)
+    return fail_status(TBSLAS_ERR_INVALID_ARG, "null buffer");
+  const int d = tc.q + 1;
+  const int64_t nc = (int64_t)d * (d + 1) * (d + 2) / 6;
+  cudaStream_t s = (cudaStream_t)stream;
+  {
+    ProfBracket pb(ctx, "adjoint_node_scatter", s);
+    launch_scatter_on_nodes(tv, tc, bc, node_weights_dev, grad_vel_dev, 3 * nc,
+                            ctx_sums(ctx) == TBSLAS_SUMS_DOUBLE_FLOAT, s);
+  }
+  return launched("adjoint node-term launch");
 }

@@ -241,9 +241,16 @@ __global__ void __launch_bounds__(kAdjF64Threads, (D <= 10 ? 2 : 1))
   // tau^2/2 J_v(X*)^T g (x) phi(X): X is a node, the node-grid scatter adds it
   if (active) {
     const double c2 = 0.5 * a.tau * a.tau;
-    a.wnode[3 * t + 0] = c2 * jtg[0];
-    a.wnode[3 * t + 1] = c2 * jtg[1];
-    a.wnode[3 * t + 2] = c2 * jtg[2];
+    double* w = a.wnode + 3 * t;
+    if (a.wnode_add) {
+      w[0] += c2 * jtg[0];
+      w[1] += c2 * jtg[1];
+      w[2] += c2 * jtg[2];
+    } else {
+      w[0] = c2 * jtg[0];
+      w[1] = c2 * jtg[1];
+      w[2] = c2 * jtg[2];
+    }
   }
 }
 

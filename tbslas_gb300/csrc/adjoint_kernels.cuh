@@ -32,6 +32,8 @@ struct AdjArgs {
   double* grad_vel;    // [Lv][3][Nc] accumulated
   double* wnode;       // [Lc * Np][3]: weights of the tau^2/2 term at the nodes for
                        // the node-grid scatter (launch_scatter_on_nodes)
+  int wnode_add = 0;   // 1: the weights are added to wnode (a sequence of steps
+                       // through one velocity sums them and scatters once)
 };
 
 // T_k and dT_k/dxi for k < D; zero outside [-1,1] like cheb_T.

@@ -1992,16 +1992,21 @@ int semilag_in_situ_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int
 }
 
 int step_midpoints(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
-                   int bc, double** xmid, cudaStream_t s) {
+                   int bc, double** xmid, cudaStream_t s, const double* vn_given) {
   TRY(check_step_args(ctx, vel, con, dt, 1, bc));
   const int q = con->q;
   const int64_t N = con->L * n_points(q);
-  double* vn = nullptr;
-  TRY(scratch_t(ctx, kVN, N * 3, &vn));
+  const double* vn = vn_given;
+  if (!vn) {
+    double* v = nullptr;
+    TRY(scratch_t(ctx, kVN, N * 3, &v));
+    ProfScope pv(ctx, "adjoint_vel_at_nodes", s, 2);
+    launch_eval_on_nodes(vel->view(), con->view(), bc, v, s);
+    vn = v;
+  }
   TRY(scratch_t(ctx, kXA, N * 3, xmid));
   {
-    ProfScope pv(ctx, "adjoint_vel_at_nodes", s, 3);
-    launch_eval_on_nodes(vel->view(), con->view(), bc, vn, s);
+    ProfScope pm(ctx, "adjoint_midpoints", s);
     launch_midpoints(con->view(), nodes_1d(q), q, sl_tau(timestep, dt, 1), bc, vn, *xmid, s);
   }
   return check_launch("midpoints");
@@ -2023,7 +2028,7 @@ ProfBracket::~ProfBracket() {
 }
 
 int step_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
-                int bc, double** xmid, double** xdep, cudaStream_t s) {
+                int bc, double** xmid, double** xdep, cudaStream_t s, const double* vn_given) {
   TRY(check_step_args(ctx, vel, con, dt, 1, bc));
   const int q = con->q;
   const bool df = ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT;
@@ -2038,14 +2043,18 @@ int step_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, 
   a.nrk = 1;
   a.periodic = bc;
   a.vals = nullptr;
-  double* vn = nullptr;
-  TRY(scratch_t(ctx, kVN, N * 3, &vn));
-  {
-    ProfScope pv(ctx, "adjoint_vel_at_nodes", s, 2);
-    launch_eval_on_nodes(a.vel, a.con, bc, vn, s);
+  if (vn_given) {
+    a.vn = vn_given;
+  } else {
+    double* vn = nullptr;
+    TRY(scratch_t(ctx, kVN, N * 3, &vn));
+    {
+      ProfScope pv(ctx, "adjoint_vel_at_nodes", s, 2);
+      launch_eval_on_nodes(a.vel, a.con, bc, vn, s);
+    }
+    TRY(check_launch("velocity at nodes"));
+    a.vn = vn;
   }
-  TRY(check_launch("velocity at nodes"));
-  a.vn = vn;
   TRY(scratch_t(ctx, kXA, N * 3, &a.xmid));
   TRY(scratch_t(ctx, kXB, N * 3, &a.xdep));
   TRY(scratch_t(ctx, kFixList, N, &a.fix_list));

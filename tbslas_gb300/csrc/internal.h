@@ -211,8 +211,10 @@ class ProfBracket {
 };
 // The midpoints of that step, X + tau/2 v(X) with v(X) from the node grid
 // (the forward's own arithmetic), into scratch of the context ([Lc * Np][3]).
+// vn_given: the velocity at con's nodes when the caller has it (a sequence of
+// steps through one stationary velocity), else null (computed here).
 int step_midpoints(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
-                   int bc, double** xmid, cudaStream_t s);
+                   int bc, double** xmid, cudaStream_t s, const double* vn_given = nullptr);
 // xmid[t] = (X_t wrapped under periodic boundaries) + tau/2 vn[t] (construct.cu)
 void launch_midpoints(const TreeView& con, const Nodes1D& nodes, int q, double tau, int periodic,
                       const double* vn, double* xmid, cudaStream_t s);
@@ -221,7 +223,8 @@ void launch_midpoints(const TreeView& con, const Nodes1D& nodes, int q, double t
 // step's own kernels in the context's sums mode (double-float: FP64 for the
 // ambiguous targets).
 int step_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
-                int bc, double** xmid, double** xdep, cudaStream_t s);
+                int bc, double** xmid, double** xdep, cudaStream_t s,
+                const double* vn_given = nullptr);
 
 // node_eval.cu: src evaluated at every node of dst's leaves, [dst.L * Np][src.dof]
 // (bit-identical to the pointwise FP64 evaluation)

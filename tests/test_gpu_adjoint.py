@@ -197,3 +197,50 @@ def test_adjoint_fp64_sums_matches_double_float(ctx, checkpoint):
         ctx.sums = tb.SUMS_FP64  # the library default
     for x, y in zip(grads[0], grads[1]):
         assert np.abs(x - y).max() <= 1e-12 * np.abs(y).max()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "double_float"])
+@pytest.mark.parametrize("checkpoint", [True, "departure", False])
+def test_adjoint_sequence_equals_per_step_scatters(ctx, checkpoint, mode):
+    """The backward pass sums the node term's weights over the steps and
+    scatters them once (tbslas_semilag_adjoint_seq + _node_term), with the
+    velocity at the nodes evaluated once where the points are rebuilt.  It
+    equals a loop of tbslas_semilag_adjoint calls, each scattering its own
+    node term, up to the order of the FP64 additions."""
+    import torch
+    a, d, q, vc, c0, cobs, tv, tc = _problem(ctx, q=5, seed=7)
+    V = torch.from_numpy(adjoint.basis_at_nodes(q)).cuda()
+    co = torch.from_numpy(cobs).cuda()
+    dt, steps, n = 0.02, 4, len(d) * (q + 1) ** 3
+    try:
+        ctx.sums = tb.SUMS_FP64 if mode == "fp64" else tb.SUMS_DOUBLE_FLOAT
+        c0t = torch.from_numpy(c0).cuda().requires_grad_(True)
+        vct = torch.from_numpy(vc).cuda().requires_grad_(True)
+        cT = adjoint.advect(c0t, vct, tv, tc, dt, 1, steps, tb.Periodic, checkpoint)
+        _J(cT, V, co).backward()
+        # per-step reference: forward states and points, then one
+        # tbslas_semilag_adjoint per step
+        vf = tb.NodeFieldFunctor(tv, tb.Periodic)
+        tv.set_coeffs(vc)
+        tc.set_coeffs(c0)
+        states, pts = [], []
+        for k in range(steps):
+            states.append(tc.get_coeffs(torch.empty_like(c0t)))
+            xd = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+            xm = torch.empty_like(xd)
+            adjoint.step_ckpt(vf, tc, 1 + k, dt, xm, xd)
+            pts.append((xm if checkpoint is True else None, xd if checkpoint else None))
+        cT2 = tc.get_coeffs(torch.empty_like(c0t))
+        assert torch.equal(cT2, cT.detach())
+        cT2.requires_grad_(True)
+        _J(cT2, V, co).backward()
+        lam = cT2.grad.contiguous().clone()
+        gv = torch.zeros_like(vct)
+        for k in reversed(range(steps)):
+            lam_k = torch.empty_like(lam)
+            adjoint.step_adjoint(vf, tc, states[k], 1 + k, dt, lam, lam_k, gv, *pts[k])
+            lam = lam_k
+    finally:
+        ctx.sums = tb.SUMS_FP64  # the library default
+    assert np.abs((c0t.grad - lam).cpu().numpy()).max() <= 1e-14 * lam.abs().max().item()
+    assert np.abs((vct.grad - gv).cpu().numpy()).max() <= 1e-13 * gv.abs().max().item()
