@@ -421,10 +421,11 @@ int tbslas_semilag_adjoint_node_term(tbslas_ctx ctx, tbslas_tree vel, tbslas_tre
 /* Many independent in-situ SL problems advanced together: problem i is
  * (vel[i] (dof 3), con[i] (dof 1, same degree), dt[i]); all share nrk and bc.
  * Each step is one node-grid kernel per degree, one persistent kernel per
- * degree band over a flattened worklist of target chunks of every problem,
- * the FP64 near-face passes and one batched refit kernel; results equal a
- * loop of tbslas_semilag_in_situ calls over the problems (with the default
- * TBSLAS_SUMS_DOUBLE_FLOAT sums, which the batch always uses), bit for bit.  No
+ * degree band over a flattened worklist of target chunks of every problem
+ * (plus, in the double-float mode, the FP64 near-face passes) and one batched
+ * refit kernel; results equal a loop of tbslas_semilag_in_situ calls over the
+ * problems in the sums mode the context had when the batch was created, bit
+ * for bit.  No
  * single-call counterpart in the reference (a driver loops over
  * SolveSemilagInSitu, src/tree/tree_semilag.h:92-135).  The batch keeps
  * pointers to the trees: they must outlive it and keep their shapes (running

@@ -289,10 +289,15 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     nj.dst = p.con;
     nj.nodes = p.nodes;
     nj.out = nullptr;  // rebased below
+    nj.face = tree_face_map(con[i], bc, nullptr);  // built on the legacy stream; synchronised below
     njobs.push_back(nj);
     for (int64_t r = 0; r < p.con.L; ++r) nitems.push_back(NodeEvalItem{i, 0, r});
   }
   cudaError_t e = cudaSuccess;
+  if (st == TBSLAS_OK) {
+    e = cudaDeviceSynchronize();  // the face maps are ready before any run
+    if (e != cudaSuccess) st = cuda_fail(e, "batch face maps");
+  }
   if (st == TBSLAS_OK) {
     b->total_targets = off;
     e = cudaMalloc(&b->d_vals, sizeof(double) * std::max<int64_t>(off, 1));

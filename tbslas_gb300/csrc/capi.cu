@@ -2,6 +2,7 @@
 // host-side validation, the bucketing kernels of the tree functor, and the
 // entry points of the SL path.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -189,6 +190,12 @@ struct tbslas_tree_s {
   int64_t cap_L = 0;      // leaves the per-leaf arrays hold (>= L after a re-meshing)
   int64_t cap_table = 0;  // entries d_table holds
   uint64_t generation = 0;  // bumped whenever the leaf list changes (re-meshing)
+  // face maps of the node-grid pass, one per boundary condition, built on
+  // first use for the current generation (tree_face_map)
+  int32_t* d_face[2] = {nullptr, nullptr};
+  int64_t face_cap[2] = {0, 0};
+  uint64_t face_gen[2] = {0, 0};
+  bool face_ok[2] = {false, false};
 
   TreeView view() const {
     TreeView v;
@@ -667,8 +674,9 @@ int fused_step(tbslas_ctx ctx, const TreeView& v1, const TreeView& v2, tbslas_tr
     // first RK stage: the velocity at the targets by sum factorisation
     double* vn = nullptr;
     TRY(scratch_t(ctx, kVN, N * 3, &vn));
-    ProfScope pv(ctx, "vel_at_nodes", s);
-    launch_eval_on_nodes(v1, a.con, bc, vn, s);
+    const int32_t* face = tree_face_map(con, bc, s);
+    ProfScope pv(ctx, "vel_at_nodes", s, face ? 2 : 1);
+    launch_eval_on_nodes(v1, a.con, bc, vn, s, face);
     TRY(check_launch("velocity at nodes"));
     a.vn = vn;
   }
@@ -1311,6 +1319,31 @@ int tree_view(tbslas_tree t, TreeView* v, tbslas_ctx* ctx) {
 
 uint64_t tree_generation(tbslas_tree t) { return t ? t->generation : 0; }
 
+const int32_t* tree_face_map(tbslas_tree t, int bc, cudaStream_t s) {
+  if (!t || (bc != TBSLAS_BC_FREESPACE && bc != TBSLAS_BC_PERIODIC)) return nullptr;
+  const int64_t n = t->L * n_points(t->q);
+  if (n <= 0 || n > INT32_MAX) return nullptr;  // node indices must fit the map
+  if (t->face_ok[bc] && t->face_gen[bc] == t->generation) return t->d_face[bc];
+  if (t->face_cap[bc] < n) {
+    int32_t* f = nullptr;
+    if (cudaMalloc(&f, n * sizeof(int32_t)) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;  // evaluated without the map: every node, no copy
+    }
+    if (t->d_face[bc]) {
+      cudaStreamSynchronize(s);
+      cudaFree(t->d_face[bc]);
+    }
+    t->d_face[bc] = f;
+    t->face_cap[bc] = n;
+  }
+  launch_face_map(t->view(), bc, t->d_face[bc], s);
+  if (cudaGetLastError() != cudaSuccess) return nullptr;
+  t->face_ok[bc] = true;
+  t->face_gen[bc] = t->generation;
+  return t->d_face[bc];
+}
+
 int tree_coeff2(tbslas_tree t, float2** coeff2) {
   if (!t || !t->ctx) return fail(TBSLAS_ERR_INVALID_ARG, "null tree");
   *coeff2 = t->d_coeff2;
@@ -1569,6 +1602,8 @@ int tbslas_tree_destroy(tbslas_tree t) {
   if (t->d_coeff2) cudaFree(t->d_coeff2);
   if (t->d_cnorm) cudaFree(t->d_cnorm);
   if (t->d_table) cudaFree(t->d_table);
+  for (int b = 0; b < 2; ++b)
+    if (t->d_face[b]) cudaFree(t->d_face[b]);
   delete t;
   return TBSLAS_OK;
 }
@@ -1730,8 +1765,9 @@ int tbslas_eval_tree_on_nodes(tbslas_ctx ctx, tbslas_tree src, tbslas_tree dst, 
   if (!out_dev) return fail(TBSLAS_ERR_INVALID_ARG, "null buffer");
   if (!bc_ok(bc)) return fail(TBSLAS_ERR_INVALID_ARG, "boundary condition %d", bc);
   cudaStream_t s = (cudaStream_t)stream;
-  ProfScope p(ctx, "eval_on_nodes", s);
-  launch_eval_on_nodes(src->view(), dst->view(), bc, out_dev, s);
+  const int32_t* face = tree_face_map(dst, bc, s);
+  ProfScope p(ctx, "eval_on_nodes", s, face ? 2 : 1);
+  launch_eval_on_nodes(src->view(), dst->view(), bc, out_dev, s, face);
   return check_launch("eval on nodes");
 }
 
@@ -1858,8 +1894,9 @@ int tbslas_semilag_bdf2(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con_prev,
   TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
   a.fix_grid = ctx->num_sms * 8;
   {
-    ProfScope pv(ctx, "vel_at_nodes", s, 2);
-    launch_eval_on_nodes(a.vel, a.next, bc, vn, s);
+    const int32_t* face = tree_face_map(con_next, bc, s);
+    ProfScope pv(ctx, "vel_at_nodes", s, face ? 2 : 1);
+    launch_eval_on_nodes(a.vel, a.next, bc, vn, s, face);
   }
   TRY(check_launch("velocity at nodes"));
   a.vn = vn;
@@ -1966,8 +2003,10 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
     // first stage: every tree at the target nodes by sum factorisation
     double* vn = nullptr;
     TRY(scratch_t(ctx, kVN, (size_t)m * N * 3, &vn));
-    ProfScope pv(ctx, "vel_at_nodes", s, 2 * m);
-    for (int k = 0; k < m; ++k) launch_eval_on_nodes(vel[k]->view(), a.con, bc, vn + 3 * k * N, s);
+    const int32_t* face = tree_face_map(con, bc, s);
+    ProfScope pv(ctx, "vel_at_nodes", s, face ? 2 * m : m);
+    for (int k = 0; k < m; ++k)
+      launch_eval_on_nodes(vel[k]->view(), a.con, bc, vn + 3 * k * N, s, face);
     TRY(check_launch("velocity set at nodes"));
     a.vn = vn;
   }
@@ -2001,7 +2040,7 @@ int step_midpoints(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timeste
     double* v = nullptr;
     TRY(scratch_t(ctx, kVN, N * 3, &v));
     ProfScope pv(ctx, "adjoint_vel_at_nodes", s, 2);
-    launch_eval_on_nodes(vel->view(), con->view(), bc, v, s);
+    launch_eval_on_nodes(vel->view(), con->view(), bc, v, s, tree_face_map(con, bc, s));
     vn = v;
   }
   TRY(scratch_t(ctx, kXA, N * 3, xmid));
@@ -2050,7 +2089,7 @@ int step_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, 
     TRY(scratch_t(ctx, kVN, N * 3, &vn));
     {
       ProfScope pv(ctx, "adjoint_vel_at_nodes", s, 2);
-      launch_eval_on_nodes(a.vel, a.con, bc, vn, s);
+      launch_eval_on_nodes(a.vel, a.con, bc, vn, s, tree_face_map(con, bc, s));
     }
     TRY(check_launch("velocity at nodes"));
     a.vn = vn;

@@ -181,6 +181,11 @@ int tree_coeff2(tbslas_tree t, float2** coeff2);
 // Changes whenever the tree's leaf list (and with it its device arrays) is
 // rebuilt, e.g. by tbslas_tree_remesh.
 uint64_t tree_generation(tbslas_tree t);
+// The tree's face map for boundary condition bc (launch_eval_on_nodes),
+// built on `s` the first time it is asked for at the tree's current leaf
+// structure; null when it cannot be had (the evaluation then computes every
+// node itself).
+const int32_t* tree_face_map(tbslas_tree t, int bc, cudaStream_t s);
 int ctx_info(tbslas_ctx ctx, int* device, int* num_sms);
 int ctx_F(tbslas_ctx ctx, int q, const double** F);
 int ctx_mu_scratch(tbslas_ctx ctx, size_t n, double** out);
@@ -228,8 +233,13 @@ int step_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, 
 
 // node_eval.cu: src evaluated at every node of dst's leaves, [dst.L * Np][src.dof]
 // (bit-identical to the pointwise FP64 evaluation)
+// face: dst's face map for this boundary condition (tree_face_map), or null
+// (every node evaluated, no copy)
 void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic, double* out,
-                          cudaStream_t s);
+                          cudaStream_t s, const int32_t* face = nullptr);
+// face[t] = the target index whose value the shared upper-face node t takes
+// (same point, same source leaf), else -1; [dst.L * Np]
+void launch_face_map(const TreeView& dst, int periodic, int32_t* face, cudaStream_t s);
 // Transposed: out[V * out_stride + l * Nc + n] += sum over dst's nodes p in
 // leaf V of W[p][l] phi_n(X_p) (FP64 atomics); W: [dst.L * Np][src.dof].
 void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int periodic,
@@ -242,6 +252,7 @@ struct NodeEvalJob {
   TreeView dst;
   Nodes1D nodes;  // 1-D nodes of dst's degree
   double* out;
+  const int32_t* face;  // dst's face map, or null
 };
 struct NodeEvalItem {
   int32_t job, pad;

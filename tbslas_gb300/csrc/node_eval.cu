@@ -18,7 +18,10 @@
 //
 // Neighbouring leaves of one depth share their face nodes (the stretched end
 // nodes are exactly 0 and 1 at most degrees): a leaf's shared upper-face
-// nodes are not evaluated but copied from the neighbour afterwards.
+// nodes are not evaluated but copied from the neighbour afterwards.  Which
+// nodes those are depends only on the destination tree's leaves, so the map
+// (face_source per node) is built once per leaf structure and boundary
+// condition (k_face_map) and read by every evaluation.
 //
 // One CTA per destination leaf.  Leaves tile the unit cube (tree_create
 // checks it), so the nodes a source leaf holds are those inside its box:
@@ -139,14 +142,15 @@ __device__ __forceinline__ int64_t face_source(const TreeView& dst, const Nodes1
 // holds are those inside its box: starting from the first node not yet
 // visited, one key search finds its source leaf and per-axis box tests give
 // the sub-grid.  outside(p) is called for nodes outside the domain, fn(sub)
-// for every sub-grid (all threads, block-synchronised around it); with
-// dedup, nodes that face_source maps to a neighbour's node are skipped.  The
-// walk's shared memory is the first walk_smem(Ds, Dd) bytes of sm.
+// for every sub-grid (all threads, block-synchronised around it); with a face
+// map (k_face_map's output, else null), nodes it maps to a neighbour's node
+// are skipped.  The walk's shared memory is the first walk_smem(Ds, Dd)
+// bytes of sm.
 template <int Ds, class Outside, class Fn>
 __device__ __forceinline__ void for_each_subgrid(const TreeView& S, const TreeView& dst,
                                                  const Nodes1D& nodes, bool per, int64_t leaf,
-                                                 bool dedup, double* sm, Outside outside,
-                                                 Fn fn) {
+                                                 const int32_t* __restrict__ face, double* sm,
+                                                 Outside outside, Fn fn) {
   __shared__ int s_first;
   __shared__ int s_n[3];
   const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
@@ -170,12 +174,12 @@ __device__ __forceinline__ void for_each_subgrid(const TreeView& S, const TreeVi
     sq[tid] = in ? (uint32_t)quantise(c) : 0xffffffffu;
   }
   __syncthreads();
+  const int32_t* lface = face ? face + leaf * Dd3 : nullptr;
   for (int p = tid; p < Dd3; p += bs) {
     const bool in = sq[p % Dd] != 0xffffffffu && sq[Dd + (p / Dd) % Dd] != 0xffffffffu &&
                     sq[2 * Dd + p / Dd2] != 0xffffffffu;
-    // with dedup, shared upper-face nodes are left to copy_face_nodes
-    const bool skip =
-        !in || (dedup && face_source(dst, nodes, per, leaf, g, p % Dd, (p / Dd) % Dd, p / Dd2) >= 0);
+    // shared upper-face nodes are left to the face copy
+    const bool skip = !in || (lface && __ldg(lface + p) >= 0);
     sdone[p] = skip ? 1 : 0;
     if (!in) outside(p);
   }
@@ -237,13 +241,14 @@ __device__ __forceinline__ void for_each_subgrid(const TreeView& S, const TreeVi
 template <int Ds>
 __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const TreeView& dst,
                                                    const Nodes1D& nodes, bool per, int64_t leaf,
+                                                   const int32_t* face,
                                                    double* __restrict__ out_all, double* sm) {
   const int Dd = dst.q + 1, Dd3 = Dd * Dd * Dd;
   const int dof = S.dof;
   double* sw = sm + walk_smem(Ds, Dd) / 8;  // [dof][pair(i,j)][Dd]
   double* out = out_all + leaf * (int64_t)Dd3 * dof;
   for_each_subgrid<Ds>(
-      S, dst, nodes, per, leaf, true, sm,
+      S, dst, nodes, per, leaf, face, sm,
       [&](int p) {
         for (int l = 0; l < dof; ++l) out[(int64_t)p * dof + l] = 0.0;
       },
@@ -272,7 +277,7 @@ __device__ __forceinline__ void scatter_on_nodes_leaf(const TreeView& S, const T
   T* sG = sH + Ds * Dd2;      // [pair(i,j)][a']
   const double* Wl = W + leaf * (int64_t)Dd3 * dof;
   for_each_subgrid<Ds>(
-      S, dst, nodes, per, leaf, false, sm, [](int) {},
+      S, dst, nodes, per, leaf, nullptr, sm, [](int) {},
       [&](const SubGrid& sg) {
         const int na = sg.na, nb = sg.nb, nz = sg.nz;
         const int* sidx = sg.sidx;
@@ -335,42 +340,54 @@ __device__ __forceinline__ void scatter_on_nodes_leaf(const TreeView& S, const T
       });
 }
 
-// The values the walk left to copy: every shared upper-face node of the
-// leaf takes its neighbour's value (run after the evaluation).
-__device__ __forceinline__ void copy_face_nodes_leaf(const TreeView& dst, const Nodes1D& nodes,
-                                                     bool per, int64_t leaf, int dof,
-                                                     double* __restrict__ out) {
+// The face map of a destination tree: per node, face_source's target index
+// for shared upper-face nodes, else -1.  One CTA per leaf.
+__global__ void __launch_bounds__(kNodeEvalThreads) k_face_map(const TreeView dst,
+                                                               const Nodes1D nodes, int periodic,
+                                                               int32_t* __restrict__ face) {
   const int Dd = dst.q + 1, Dd2 = Dd * Dd, Dd3 = Dd2 * Dd;
+  const int64_t leaf = blockIdx.x;
   const Geom g = load_geom(dst.geom + leaf);
   for (int p = threadIdx.x; p < Dd3; p += blockDim.x) {
     const int a = p % Dd, b = (p / Dd) % Dd, c = p / Dd2;
-    if (a != Dd - 1 && b != Dd - 1 && c != Dd - 1) continue;
-    const int64_t src = face_source(dst, nodes, per, leaf, g, a, b, c);
-    if (src < 0) continue;
-    const int64_t t = leaf * Dd3 + p;
-    for (int l = 0; l < dof; ++l) out[t * dof + l] = out[src * dof + l];
+    const int64_t src = face_source(dst, nodes, periodic != 0, leaf, g, a, b, c);
+    face[leaf * Dd3 + p] = (int32_t)src;
   }
 }
 
-__global__ void __launch_bounds__(kNodeEvalThreads) k_copy_face_nodes(const NodeEvalJob j,
-                                                                      int periodic) {
-  copy_face_nodes_leaf(j.dst, j.nodes, periodic != 0, blockIdx.x, j.src.dof, j.out);
+// The values the walk left to copy: every shared upper-face node takes its
+// neighbour's value (run after the evaluation; a source node is never itself
+// a shared upper-face node, so the copies do not chain).
+__global__ void __launch_bounds__(kNodeEvalThreads) k_copy_face_nodes(
+    const int32_t* __restrict__ face, int64_t n, int dof, double* __restrict__ out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int32_t src = __ldg(face + t);
+  if (src < 0) return;
+  for (int l = 0; l < dof; ++l) out[t * dof + l] = out[(int64_t)src * dof + l];
 }
 
 __global__ void __launch_bounds__(kNodeEvalThreads) k_batch_copy_face_nodes(
-    const NodeEvalJob* __restrict__ jobs, const NodeEvalItem* __restrict__ items, int periodic) {
+    const NodeEvalJob* __restrict__ jobs, const NodeEvalItem* __restrict__ items) {
   __shared__ NodeEvalJob sj;
   const NodeEvalItem it = items[blockIdx.x];
   if (threadIdx.x == 0) sj = jobs[it.job];
   __syncthreads();
-  copy_face_nodes_leaf(sj.dst, sj.nodes, periodic != 0, it.leaf, sj.src.dof, sj.out);
+  if (!sj.face) return;
+  const int Dd = sj.dst.q + 1, Dd3 = Dd * Dd * Dd, dof = sj.src.dof;
+  for (int p = threadIdx.x; p < Dd3; p += blockDim.x) {
+    const int64_t t = it.leaf * Dd3 + p;
+    const int32_t src = __ldg(sj.face + t);
+    if (src >= 0)
+      for (int l = 0; l < dof; ++l) sj.out[t * dof + l] = sj.out[(int64_t)src * dof + l];
+  }
 }
 
 template <int Ds>
 __global__ void __launch_bounds__(kNodeEvalThreads) k_eval_on_nodes(const NodeEvalJob j,
                                                                     int periodic) {
   extern __shared__ __align__(16) double sm[];
-  eval_on_nodes_leaf<Ds>(j.src, j.dst, j.nodes, periodic != 0, blockIdx.x, j.out, sm);
+  eval_on_nodes_leaf<Ds>(j.src, j.dst, j.nodes, periodic != 0, blockIdx.x, j.face, j.out, sm);
 }
 
 // Batched: one CTA per (job, destination leaf) item; the jobs of one launch
@@ -383,7 +400,7 @@ __global__ void __launch_bounds__(kNodeEvalThreads) k_batch_eval_on_nodes(
   const NodeEvalItem it = items[blockIdx.x];
   if (threadIdx.x == 0) sj = jobs[it.job];
   __syncthreads();
-  eval_on_nodes_leaf<Ds>(sj.src, sj.dst, sj.nodes, periodic != 0, it.leaf, sj.out, sm);
+  eval_on_nodes_leaf<Ds>(sj.src, sj.dst, sj.nodes, periodic != 0, it.leaf, sj.face, sj.out, sm);
 }
 
 template <int Ds, class A>
@@ -475,8 +492,17 @@ void dispatch_batched(int ds, const NodeEvalJob* jobs, const NodeEvalItem* items
 
 }  // namespace
 
+void launch_face_map(const TreeView& dst, int periodic, int32_t* face, cudaStream_t s) {
+  if (dst.L <= 0) return;
+  Nodes1D nodes;
+  std::memset(&nodes, 0, sizeof(nodes));
+  const std::vector<double> x = cheb_nodes_1d(dst.q);
+  for (int i = 0; i <= dst.q; ++i) nodes.x[i] = x[i];
+  k_face_map<<<(unsigned)dst.L, kNodeEvalThreads, 0, s>>>(dst, nodes, periodic, face);
+}
+
 void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic, double* out,
-                          cudaStream_t s) {
+                          cudaStream_t s, const int32_t* face) {
   if (dst.L <= 0) return;
   NodeEvalJob j;
   j.src = src;
@@ -485,8 +511,13 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
   const std::vector<double> x = cheb_nodes_1d(dst.q);
   for (int i = 0; i <= dst.q; ++i) j.nodes.x[i] = x[i];
   j.out = out;
+  j.face = face;
   dispatch_single<1>(src.q + 1, j, dst.L, periodic, s);
-  k_copy_face_nodes<<<(unsigned)dst.L, kNodeEvalThreads, 0, s>>>(j, periodic);
+  if (face) {
+    const int64_t n = dst.L * (int64_t)(dst.q + 1) * (dst.q + 1) * (dst.q + 1);
+    k_copy_face_nodes<<<(unsigned)((n + kNodeEvalThreads - 1) / kNodeEvalThreads),
+                        kNodeEvalThreads, 0, s>>>(face, n, src.dof, out);
+  }
 }
 
 void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int periodic,
@@ -500,6 +531,7 @@ void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int perio
   const std::vector<double> x = cheb_nodes_1d(dst.q);
   for (int i = 0; i <= dst.q; ++i) j.nodes.x[i] = x[i];
   j.out = out;
+  j.face = nullptr;
   dispatch_scatter<1>(src.q + 1, j, W, out_stride, dst.L, periodic, df_sums, s);
 }
 
@@ -508,7 +540,7 @@ void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* ite
                                 cudaStream_t s) {
   if (n_items <= 0) return;
   dispatch_batched<1>(q_src + 1, jobs, items, n_items, max_q_dst, periodic, s);
-  k_batch_copy_face_nodes<<<(unsigned)n_items, kNodeEvalThreads, 0, s>>>(jobs, items, periodic);
+  k_batch_copy_face_nodes<<<(unsigned)n_items, kNodeEvalThreads, 0, s>>>(jobs, items);
 }
 
 }  // namespace tbg
