@@ -74,13 +74,52 @@ __device__ __forceinline__ Factors<A> stage_factors(const double* __restrict__ F
   return Factors<A>{sm, sm + dd, sm + 2 * dd, sm + 3 * dd};
 }
 
+// Box positions of the triangle T and of its (j, k) pairs, so that the passes
+// inside T run over compact lists (every lane of a warp busy) rather than
+// over the box with most lanes masked:
+//   tri[n]  = i D^2 + j D + k of triangular index n (i outer, j, k inner),
+//   pair[n] = j D + k of the n-th pair with j + k < D (j outer).
+// Built by the block; followed by a barrier.
+struct TriLists {
+  const int* tri;
+  const int* pair;
+};
+__device__ __forceinline__ TriLists build_tri_lists(int D, int* tri, int* pair) {
+  const int D2 = D * D, NC = nc_of(D), NP = D * (D + 1) / 2;
+  for (int n = threadIdx.x; n < NC; n += blockDim.x) {
+    int i = 0, rem = n;
+    while (rem >= (D - i) * (D - i + 1) / 2) {
+      rem -= (D - i) * (D - i + 1) / 2;
+      ++i;
+    }
+    int j = 0;
+    while (rem >= D - i - j) {
+      rem -= D - i - j;
+      ++j;
+    }
+    tri[n] = i * D2 + j * D + rem;
+  }
+  for (int n = threadIdx.x; n < NP; n += blockDim.x) {
+    int j = 0, rem = n;
+    while (rem >= D - j) {
+      rem -= D - j;
+      ++j;
+    }
+    pair[n] = j * D + rem;
+  }
+  __syncthreads();
+  return TriLists{tri, pair};
+}
+
 // f (D^3 values, x fastest) in S0 -> coefficients, handed to `emit(t, c)`
 // with t the triangular index (FP64).  Ends with the block synchronised.
+// Every output is one thread's dot product in a fixed order, so the result
+// does not depend on which thread computes it.
 template <class A, class Emit>
-__device__ __forceinline__ void refit_row(const Factors<A>& f, int D, typename A::T* S0,
-                                          typename A::T* S1, Emit emit) {
+__device__ __forceinline__ void refit_row(const Factors<A>& f, const TriLists& tl, int D,
+                                          typename A::T* S0, typename A::T* S1, Emit emit) {
   typedef typename A::T T;
-  const int D2 = D * D, D3 = D2 * D;
+  const int D2 = D * D, D3 = D2 * D, NC = nc_of(D), NP = D * (D + 1) / 2;
   const int tid = threadIdx.x, bs = blockDim.x;
   // x: S1[c][b][k] = sum_a Q[a][k] S0[c][b][a]
   for (int o = tid; o < D3; o += bs) {
@@ -92,19 +131,19 @@ __device__ __forceinline__ void refit_row(const Factors<A>& f, int D, typename A
   }
   __syncthreads();
   // y: S0[c][j][k] = sum_b Q[b][j] S1[c][b][k],  j + k < D
-  for (int o = tid; o < D3; o += bs) {
-    const int k = o % D, j = (o / D) % D, c = o / D2;
-    if (j + k >= D) continue;
+  for (int m = tid; m < D * NP; m += bs) {
+    const int c = m / NP, jk = tl.pair[m - c * NP];
+    const int k = jk % D, j = jk / D;
     const T* col = S1 + c * D2 + k;
     T s = A::zero();
     for (int b = 0; b < D; ++b) A::mac(s, f.Q[b * D + j], col[b * D]);
-    S0[o] = A::done(s);
+    S0[c * D2 + jk] = A::done(s);
   }
   __syncthreads();
   // z: S1[i][j][k] = sum_c Q[c][i] S0[c][j][k],  i + j + k < D
-  for (int o = tid; o < D3; o += bs) {
+  for (int m = tid; m < NC; m += bs) {
+    const int o = tl.tri[m];
     const int k = o % D, j = (o / D) % D, i = o / D2;
-    if (i + j + k >= D) continue;
     const T* col = S0 + j * D + k;
     T s = A::zero();
     for (int c = 0; c < D; ++c) A::mac(s, f.Q[c * D + i], col[c * D2]);
@@ -112,10 +151,10 @@ __device__ __forceinline__ void refit_row(const Factors<A>& f, int D, typename A
   }
   __syncthreads();
   // R^-1 along x: S0[i][j][k'] = sum_{k >= k'} R^-1[k'][k] S1[i][j][k]
-  for (int o = tid; o < D3; o += bs) {
+  for (int m = tid; m < NC; m += bs) {
+    const int o = tl.tri[m];
     const int k = o % D, j = (o / D) % D, i = o / D2;
     const int n = D - i - j;
-    if (k >= n) continue;
     const T* row = S1 + (o - k);
     T s = A::zero();
     for (int kk = k; kk < n; ++kk) A::mac(s, f.RiT[kk * D + k], row[kk]);
@@ -123,10 +162,10 @@ __device__ __forceinline__ void refit_row(const Factors<A>& f, int D, typename A
   }
   __syncthreads();
   // R^-1 along y: S1[i][j'][k] = sum_{j >= j'} R^-1[j'][j] S0[i][j][k]
-  for (int o = tid; o < D3; o += bs) {
+  for (int m = tid; m < NC; m += bs) {
+    const int o = tl.tri[m];
     const int k = o % D, j = (o / D) % D, i = o / D2;
     const int n = D - i - k;
-    if (j >= n) continue;
     const T* col = S0 + i * D2 + k;
     T s = A::zero();
     for (int jj = j; jj < n; ++jj) A::mac(s, f.Ri[j * D + jj], col[jj * D]);
@@ -134,14 +173,14 @@ __device__ __forceinline__ void refit_row(const Factors<A>& f, int D, typename A
   }
   __syncthreads();
   // R^-1 along z: c[i'][j][k] = sum_{i >= i'} R^-1[i'][i] S1[i][j][k]
-  for (int o = tid; o < D3; o += bs) {
+  for (int m = tid; m < NC; m += bs) {
+    const int o = tl.tri[m];
     const int k = o % D, j = (o / D) % D, i = o / D2;
     const int n = D - j - k;
-    if (i >= n) continue;
     const T* col = S1 + j * D + k;
     T s = A::zero();
     for (int ii = i; ii < n; ++ii) A::mac(s, f.Ri[i * D + ii], col[ii * D2]);
-    emit(tri_index(D, i, j, k), A::value(A::done(s)));
+    emit(m, A::value(A::done(s)));  // m is the triangular index of (i, j, k)
   }
   __syncthreads();
 }
@@ -151,15 +190,15 @@ __device__ __forceinline__ void refit_row(const Factors<A>& f, int D, typename A
 //   f = (Q)^(x)3 ext_T( [ (R^-T)^(x)3 c ]_T ),
 // handed to `emit(p, value)` with p the node index (x fastest).
 template <class A, class Emit>
-__device__ __forceinline__ void refit_row_t(const Factors<A>& f, int D, typename A::T* S0,
-                                            typename A::T* S1, Emit emit) {
+__device__ __forceinline__ void refit_row_t(const Factors<A>& f, const TriLists& tl, int D,
+                                            typename A::T* S0, typename A::T* S1, Emit emit) {
   typedef typename A::T T;
-  const int D2 = D * D, D3 = D2 * D;
+  const int D2 = D * D, D3 = D2 * D, NC = nc_of(D), NP = D * (D + 1) / 2;
   const int tid = threadIdx.x, bs = blockDim.x;
   // R^-T along z: S1[i][j][k] = sum_{i' <= i} R^-1[i'][i] S0[i'][j][k]
-  for (int o = tid; o < D3; o += bs) {
+  for (int m = tid; m < NC; m += bs) {
+    const int o = tl.tri[m];
     const int k = o % D, j = (o / D) % D, i = o / D2;
-    if (i + j + k >= D) continue;
     const T* col = S0 + j * D + k;
     T s = A::zero();
     for (int ii = 0; ii <= i; ++ii) A::mac(s, f.RiT[i * D + ii], col[ii * D2]);
@@ -167,9 +206,9 @@ __device__ __forceinline__ void refit_row_t(const Factors<A>& f, int D, typename
   }
   __syncthreads();
   // R^-T along y
-  for (int o = tid; o < D3; o += bs) {
+  for (int m = tid; m < NC; m += bs) {
+    const int o = tl.tri[m];
     const int k = o % D, j = (o / D) % D, i = o / D2;
-    if (i + j + k >= D) continue;
     const T* col = S1 + i * D2 + k;
     T s = A::zero();
     for (int jj = 0; jj <= j; ++jj) A::mac(s, f.RiT[j * D + jj], col[jj * D]);
@@ -177,9 +216,9 @@ __device__ __forceinline__ void refit_row_t(const Factors<A>& f, int D, typename
   }
   __syncthreads();
   // R^-T along x
-  for (int o = tid; o < D3; o += bs) {
-    const int k = o % D, j = (o / D) % D, i = o / D2;
-    if (i + j + k >= D) continue;
+  for (int m = tid; m < NC; m += bs) {
+    const int o = tl.tri[m];
+    const int k = o % D;
     const T* row = S0 + (o - k);
     T s = A::zero();
     for (int kk = 0; kk <= k; ++kk) A::mac(s, f.Ri[kk * D + k], row[kk]);
@@ -187,14 +226,14 @@ __device__ __forceinline__ void refit_row_t(const Factors<A>& f, int D, typename
   }
   __syncthreads();
   // Q along z: S0[c][j][k] = sum_{i < D-j-k} Q[c][i] S1[i][j][k],  j + k < D
-  for (int o = tid; o < D3; o += bs) {
-    const int k = o % D, j = (o / D) % D, c = o / D2;
+  for (int m = tid; m < D * NP; m += bs) {
+    const int c = m / NP, jk = tl.pair[m - c * NP];
+    const int k = jk % D, j = jk / D;
     const int n = D - j - k;
-    if (n <= 0) continue;
     const T* col = S1 + j * D + k;
     T s = A::zero();
     for (int i = 0; i < n; ++i) A::mac(s, f.Q[c * D + i], col[i * D2]);
-    S0[o] = A::done(s);
+    S0[c * D2 + jk] = A::done(s);
   }
   __syncthreads();
   // Q along y: S1[c][b][k] = sum_{j < D-k} Q[b][j] S0[c][j][k]
@@ -241,7 +280,13 @@ struct CoeffOut {
 
 // Dynamic shared memory of the refit kernels at degree q.
 __host__ __device__ constexpr size_t refit_smem(int q) {
-  return (size_t)(4 * (q + 1) * (q + 1) + 2 * (q + 1) * (q + 1) * (q + 1)) * sizeof(double);
+  return (size_t)(4 * (q + 1) * (q + 1) + 2 * (q + 1) * (q + 1) * (q + 1)) * sizeof(double) +
+         (size_t)(nc_of(q + 1) + (q + 1) * (q + 2) / 2) * sizeof(int);
+}
+// The triangle lists sit after the two D^3 buffers.
+__device__ __forceinline__ TriLists tri_lists_at(void* after_buffers, int D) {
+  int* tri = reinterpret_cast<int*>(after_buffers);
+  return build_tri_lists(D, tri, tri + nc_of(D));
 }
 
 template <class A>
@@ -258,12 +303,13 @@ __global__ void __launch_bounds__(kRefitThreads) k_refit(const double* __restric
   const Factors<A> f = stage_factors<A>(F, D, sm);
   T* S0 = sm + 4 * D * D;
   T* S1 = S0 + D3;
+  const TriLists tl = tri_lists_at(S1 + D3, D);
   const int64_t r = blockIdx.x;
   const int64_t leaf = r / dof;
   const int l = (int)(r - leaf * dof);
   load_row<A>(vals + r * D3, D3, S0);
   const int64_t base = leaf * stride + (int64_t)l * nc_of(D);
-  refit_row<A>(f, D, S0, S1, CoeffOut{coeff + base, coeff2 ? coeff2 + base : nullptr, err});
+  refit_row<A>(f, tl, D, S0, S1, CoeffOut{coeff + base, coeff2 ? coeff2 + base : nullptr, err});
 }
 
 // mu[r][p] = sum_n M[p][n] lam[r][n] (the adjoint's transposed refit).
@@ -278,6 +324,7 @@ __global__ void __launch_bounds__(kRefitThreads) k_refit_t(const double* __restr
   const Factors<A> f = stage_factors<A>(F, D, sm);
   T* S0 = sm + 4 * D2;
   T* S1 = S0 + D3;
+  const TriLists tl = tri_lists_at(S1 + D3, D);
   const int64_t r = blockIdx.x;
   const double* c = lam + r * NC;
   for (int o = threadIdx.x; o < D3; o += blockDim.x) {
@@ -286,7 +333,7 @@ __global__ void __launch_bounds__(kRefitThreads) k_refit_t(const double* __restr
   }
   __syncthreads();
   double* out = mu + r * D3;
-  refit_row_t<A>(f, D, S0, S1, [out](int p, double v) { out[p] = v; });
+  refit_row_t<A>(f, tl, D, S0, S1, [out](int p, double v) { out[p] = v; });
 }
 
 // Batched refit: one CTA per (problem, row) item.
@@ -302,11 +349,13 @@ __global__ void __launch_bounds__(kRefitThreads) k_batch_refit(const RefitJob* _
   const Factors<A> f = stage_factors<A>(j.F, D, sm);
   T* S0 = sm + 4 * D * D;
   T* S1 = S0 + D3;
+  const TriLists tl = tri_lists_at(S1 + D3, D);
   const int64_t leaf = it.row / j.dof;
   const int l = (int)(it.row - leaf * j.dof);
   load_row<A>(j.vals + it.row * D3, D3, S0);
   const int64_t base = leaf * j.stride + (int64_t)l * nc_of(D);
-  refit_row<A>(f, D, S0, S1, CoeffOut{j.coeff + base, j.coeff2 ? j.coeff2 + base : nullptr, j.err});
+  refit_row<A>(f, tl, D, S0, S1,
+               CoeffOut{j.coeff + base, j.coeff2 ? j.coeff2 + base : nullptr, j.err});
 }
 
 // Raise a kernel's dynamic shared-memory limit to the degree-16 size, once

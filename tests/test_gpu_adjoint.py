@@ -206,7 +206,10 @@ def test_adjoint_sequence_equals_per_step_scatters(ctx, checkpoint, mode):
     scatters them once (tbslas_semilag_adjoint_seq + _node_term), with the
     velocity at the nodes evaluated once where the points are rebuilt.  It
     equals a loop of tbslas_semilag_adjoint calls, each scattering its own
-    node term, up to the order of the FP64 additions."""
+    node term, up to the order of the FP64 additions: the scatters' atomics
+    add in no fixed order (observed up to 2.5e-14 relative in the
+    double-float mode), so the gate is the suite's 1e-12; a missing or
+    doubled node term would be off by O(1)."""
     import torch
     a, d, q, vc, c0, cobs, tv, tc = _problem(ctx, q=5, seed=7)
     V = torch.from_numpy(adjoint.basis_at_nodes(q)).cuda()
@@ -242,5 +245,5 @@ def test_adjoint_sequence_equals_per_step_scatters(ctx, checkpoint, mode):
             lam = lam_k
     finally:
         ctx.sums = tb.SUMS_FP64  # the library default
-    assert np.abs((c0t.grad - lam).cpu().numpy()).max() <= 1e-14 * lam.abs().max().item()
-    assert np.abs((vct.grad - gv).cpu().numpy()).max() <= 1e-13 * gv.abs().max().item()
+    assert np.abs((c0t.grad - lam).cpu().numpy()).max() <= 1e-12 * lam.abs().max().item()
+    assert np.abs((vct.grad - gv).cpu().numpy()).max() <= 1e-12 * gv.abs().max().item()
