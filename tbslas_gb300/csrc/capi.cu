@@ -858,9 +858,11 @@ TreeView mesh_view(const tbslas_tree t, const MeshState& m, const int32_t* table
 // into their parent, drop), into the other scratch set: split children get
 // the restriction of their parent (transfer + FP64 refit), merged parents the
 // rows of merge_c.
+// splits >= 0: the actions are keep and split only, with that many splits,
+// so the new leaf and transfer counts are known without a read-back.
 int apply_actions(tbslas_ctx ctx, tbslas_tree t, MeshState& m, const int8_t* act,
                   const int64_t* aux, const double* merge_c, cudaStream_t s, int64_t* launches,
-                  bool coeffs = true) {
+                  bool coeffs = true, int64_t splits = -1) {
   const int q = t->q, dof = t->dof;
   const int64_t L = m.L, np = n_points(q), stride = t->stride;
   int64_t *nleaf, *nxfer, *pos, *xpos;
@@ -873,9 +875,11 @@ int apply_actions(tbslas_ctx ctx, tbslas_tree t, MeshState& m, const int8_t* act
   k_scan_excl<<<1, 1024, 0, s>>>(nxfer, xpos, L);
   *launches += 3;
   TRY(check_launch("re-meshing counts"));
-  const int64_t* ends[2] = {pos + L, xpos + L};
-  int64_t sz[2];
-  TRY(read_scalars(ctx, ends, 2, sz, s));
+  int64_t sz[2] = {L + 7 * splits, 8 * splits};
+  if (splits < 0) {
+    const int64_t* ends[2] = {pos + L, xpos + L};
+    TRY(read_scalars(ctx, ends, 2, sz, s));
+  }
   const int64_t Lnew = sz[0], nx = sz[1];
   const int o = 1 - m.set;
   MeshState n;
@@ -919,19 +923,22 @@ int apply_actions(tbslas_ctx ctx, tbslas_tree t, MeshState& m, const int8_t* act
 // headroom when the leaf count outgrows them), the lookup table rebuilt and
 // the derived coefficient arrays refreshed.
 int install_mesh(tbslas_ctx ctx, tbslas_tree t, const MeshState& m, cudaStream_t s,
-                 int64_t* launches_out) {
+                 int64_t* launches_out, int known_depth = -1) {
   const int dof = t->dof;
   const int64_t stride = t->stride;
   int64_t launches = 0;
-  int64_t* sc;
-  TRY(scratch_t(ctx, kRmScalars, 2, &sc));
-  CUDA_TRY(cudaMemsetAsync(sc + 1, 0, sizeof(int64_t), s));
-  launch_max_depth(m.geom, m.L, reinterpret_cast<int*>(sc + 1), s);
-  launches += 1;
-  int64_t md = 0;
-  const int64_t* mdp = sc + 1;
-  TRY(read_scalars(ctx, &mdp, 1, &md, s));
-  const int maxd = (int)(md & 0xffffffff);
+  int maxd = known_depth;
+  if (maxd < 0) {
+    int64_t* sc;
+    TRY(scratch_t(ctx, kRmScalars, 2, &sc));
+    CUDA_TRY(cudaMemsetAsync(sc + 1, 0, sizeof(int64_t), s));
+    launch_max_depth(m.geom, m.L, reinterpret_cast<int*>(sc + 1), s);
+    launches += 1;
+    int64_t md = 0;
+    const int64_t* mdp = sc + 1;
+    TRY(read_scalars(ctx, &mdp, 1, &md, s));
+    maxd = (int)(md & 0xffffffff);
+  }
   const int T = std::min(maxd, 7);
   const int64_t ntab = (1ll << (3 * T)) + 1;
   // allocate everything that has to grow before touching the tree, so a
@@ -1015,6 +1022,7 @@ int tree_remesh(tbslas_ctx ctx, tbslas_tree t, double tol, int min_depth, int ma
   CUDA_TRY(cudaMemcpyAsync(m.coeff, t->d_coeff, m.L * stride * sizeof(double),
                            cudaMemcpyDeviceToDevice, s));
   int64_t merged = 0, split = 0, balanced = 0, launches = 0;
+  int final_depth = -1;  // maximum depth of the final leaves, once read
   int64_t* sc;  // device scalars: [0] a count, [1] a maximum depth
   TRY(scratch_t(ctx, kRmScalars, 2, &sc));
   // 1. coarsen one level
@@ -1073,7 +1081,7 @@ int tree_remesh(tbslas_ctx ctx, tbslas_tree t, double tol, int min_depth, int ma
     TRY(read_scalars(ctx, &sc, 1, &n, s));
     if (n == 0) break;
     split += n;
-    TRY(apply_actions(ctx, t, m, act, nullptr, nullptr, s, &launches));
+    TRY(apply_actions(ctx, t, m, act, nullptr, nullptr, s, &launches, true, n));
   }
   // 3. balance 2:1 (the lookup table at level 7, which find_leaf accepts at
   // any maximum depth)
@@ -1088,13 +1096,23 @@ int tree_remesh(tbslas_ctx ctx, tbslas_tree t, double tol, int min_depth, int ma
                          reinterpret_cast<unsigned long long*>(sc), s);
     launches += 2;
     TRY(check_launch("balance flags"));
-    int64_t n = 0;
-    TRY(read_scalars(ctx, &sc, 1, &n, s));
-    if (n == 0) break;
+    // the maximum depth of these leaves comes back with the flag count: when
+    // nothing is flagged they are the final leaves
+    CUDA_TRY(cudaMemsetAsync(sc + 1, 0, sizeof(int64_t), s));
+    launch_max_depth(m.geom, m.L, reinterpret_cast<int*>(sc + 1), s);
+    launches += 1;
+    int64_t n_md[2] = {0, 0};
+    const int64_t* both[2] = {sc, sc + 1};
+    TRY(read_scalars(ctx, both, 2, n_md, s));
+    const int64_t n = n_md[0];
+    if (n == 0) {
+      final_depth = (int)(n_md[1] & 0xffffffff);
+      break;
+    }
     balanced += n;
-    TRY(apply_actions(ctx, t, m, act, nullptr, nullptr, s, &launches));
+    TRY(apply_actions(ctx, t, m, act, nullptr, nullptr, s, &launches, true, n));
   }
-  TRY(install_mesh(ctx, t, m, s, &launches));
+  TRY(install_mesh(ctx, t, m, s, &launches, final_depth));
   if (stats) {
     stats[0] = t->L;
     stats[1] = merged;
