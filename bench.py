@@ -662,6 +662,105 @@ def run_gpu(args, wl, rank, world, local_rank):
     return line
 
 
+def run_functor(args, wl, rank, world, local_rank):
+    """Config 2's step through the reference's separate calls, as
+    SolveSemilagInSitu makes them (src/tree/tree_semilag.h:92-135,
+    src/semilag/semilag.inc:26-45): CollectChebTreeGridPoints, ComputeTrajRK2
+    through the velocity functor, the concentration functor (EvalTree: Morton
+    bucketing of the departure points, leaf tiles staged by bulk copy) at the
+    departure points, SetTreeGridValues.  Same result as the fused step, bit
+    for bit; timed the same way (FP64, L2 flushed between steps)."""
+    import torch
+    import tbslas_gb300 as tb
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = tb.Context(local_rank)
+    assert ctx.sums == tb.SUMS_FP64
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    tv = tb.Tree(ctx, wl.va, wl.vd, wl.q, 3, wl.vc)
+    tc = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)
+    tf = tb.Tree(ctx, wl.ca, wl.cd, wl.q, 1, wl.cc)  # the fused step, for the bitwise check
+    vf = tb.NodeFieldFunctor(tv, wl.bc)
+    cf = tb.NodeFieldFunctor(tc, wl.bc)
+    n = wl.points_per_step
+    np_ = (wl.q + 1) ** 3
+    pts = torch.empty((n, 3), dtype=torch.float64, device=dev)
+    xdep = torch.empty_like(pts)
+    vals = torch.empty((len(wl.cd), 1, np_), dtype=torch.float64, device=dev)
+
+    def step(i):
+        tinit = (i + 1) * wl.dt
+        tb.collect_cheb_tree_grid_points(tc, out=pts)
+        tb.compute_traj_rk2(vf, pts, tinit, tinit - wl.dt, 1, xsol=xdep)
+        cf(xdep, out=vals.view(n, 1))
+        tb.set_tree_grid_values(tc, vals)
+
+    step(0)
+    tb.solve_semilag_in_situ(vf, tf, 1, wl.dt, 1)
+    torch.cuda.synchronize()
+    same = bool(np.array_equal(tc.get_coeffs(), tf.get_coeffs()))
+    for i in range(args.warmup):
+        flush.fill_(float(i))
+        step(i + 1)
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            step(args.warmup + 1 + i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ctx.profile(True)
+    ctx.profile_reset()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        step(args.warmup + 1 + args.steps + i)
+    torch.cuda.synchronize()
+    prof = ctx.profile_totals()
+    ctx.profile(False)
+    if rank != 0:
+        return None
+    fp64_peak = ctx.fp64_fma_peak() / 1e12
+    d = wl.q + 1
+    nc = tb.n_coeff(wl.q)
+    # the reference's count of an evaluation (3 d 3 + 2 Nc dof,
+    # src/tree/tree_functor.h:389-394): two velocity evaluations in the
+    # trajectory, one concentration evaluation in the functor
+    traj_flops = 2 * (3 * d * 3 + 2 * nc * 3) + 18
+    eval_flops = 3 * d * 3 + 2 * nc
+
+    def frac(name, flops):
+        g, _, kms = prof.get(name, (0, 0, 0.0))
+        if not g:
+            return None
+        launch_ms = kms / g
+        ach = flops * n / (launch_ms * 1e-3) / 1e12
+        return {"launch_ms": launch_ms, "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": ach / fp64_peak, "algorithmic_flops_per_point": flops}
+    line = {"metric": METRIC, "value": n * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded analytic fields)", "config": describe_config(wl),
+            "roofline": {"bound": "fp64", "peak_source": "FP64 FMA throughput measured in this "
+                         "run (tbslas_fp64_fma_peak)",
+                         "traj_rk2": frac("traj_rk2", traj_flops),
+                         "eval_tree (bucket_points + eval_tiles)": frac("eval_tiles", eval_flops),
+                         "kernels_ms_per_step": {k: v[2] / args.steps for k, v in prof.items()}},
+            "accuracy": {"equals_fused_step_bitwise": same},
+            "clocks": clk.summary(),
+            "gpu_launches": int(sum(v[1] for v in prof.values())),
+            "run_notes": {"l2": "flushed between timed steps (256 MiB write inside the timed "
+                                "loop)", "parallelism": "replicas x%d" % world, "nrk": 1}}
+    assert ctx.check() == 0
+    ctx.close()
+    return line
+
+
 def run_remesh(args, wl, rank, world, local_rank):
     """The adaptive advection loop of the reference's driver: an in-situ SL
     step, then RefineTree and Balance21 (src/applications/src/advection.cpp:
@@ -1517,12 +1616,16 @@ def _band(q):
 # key -> (workload, runner name, steps cap).  The headline is the adaptive q = 14
 # configuration; these are the uniform q = 8 tree, the tricubic grid, the
 # 64-problem batch and the adjoint, each in the library's default FP64
-# arithmetic with its own roofline, CPU baseline, accuracy check and clocks.
+# arithmetic with its own roofline, CPU baseline, accuracy check and clocks,
+# and the headline configuration once more through the reference's separate
+# calls (the general functor path).
 EXTRA_CONFIGS = [
     ("cfg1_uniform_q8", "tree_uniform_q8", "run_gpu", None),
     ("cfg3_grid_256", "grid_periodic_256", "run_gpu", 20),
     ("cfg4_batched_64", "batched_64", "run_batched", 10),
     ("cfg5_adjoint_q8", "adjoint_q8", "run_adjoint", None),
+    # config 2 through the reference's separate calls (the functor path)
+    ("cfg2_functor_path", "functor_q14", "run_functor", 10),
 ]
 
 
@@ -1544,6 +1647,8 @@ def dispatch(args, wl, rank, world, local_rank):
         return run_tv(args, wl, rank, world, local_rank)
     if hasattr(wl, "construct"):
         return run_construct(args, wl, rank, world, local_rank)
+    if hasattr(wl, "functor"):
+        return run_functor(args, wl, rank, world, local_rank)
     return run_gpu(args, wl, rank, world, local_rank)
 
 

@@ -296,6 +296,13 @@ def make(name):
         return Bdf2Workload()
     if name == "tree_uniform_q8_tv":
         return TvWorkload()
+    if name == "functor_q14":
+        # config 2 through the reference's separate calls (collect, ComputeTrajRK2,
+        # the EvalTree functor, SetTreeGridValues) instead of the fused step
+        wl = tree_adaptive_q14()
+        wl.name = "functor_q14"
+        wl.functor = True
+        return wl
     if name == "construct_q14":
         wl = tree_adaptive_q14()
         wl.name = "construct_q14"
