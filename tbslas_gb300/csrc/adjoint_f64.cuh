@@ -9,9 +9,12 @@
 // Work per target, in FP64 multiply-adds: 2 Nc for grad c^k(Xd), 5 Nc for
 // grad(g . v)(X*) (three to form sum_a g_a c_a per coefficient, two for the
 // value and derivative sums), and per (point, coefficient) of the scatters
-// one multiply-add for lambda (the weight folded into T_i(z) T_j(y)) and one
-// product T_i(z) T_j(y) * T_k(x) plus three multiply-adds for the velocity:
-// Nc + 4 Nc -- 12 Nc against the forward step's 4 Nc.
+// one multiply-add for lambda (the weight folded into T_i(z) T_j(y)) and
+// three for the velocity (each component's weight folded into its own copy
+// of T_k(x), 3 D products per point): Nc + 3 Nc -- 11 Nc against the forward
+// step's 4 Nc.  Where the three copies would cost the second CTA per SM
+// (q >= 9) the velocity scatter forms T_i(z) T_j(y) * T_k(x) once per pair
+// instead (4 Nc).
 #pragma once
 
 #include "adjoint_kernels.cuh"
@@ -28,13 +31,17 @@ constexpr int kAdjF64Threads = 192;
 // banks).  Slot map of a point, written before each scatter:
 //   [0, NIJ)          T_i(z) T_j(y) over the (i, j) triangle, i outer (times
 //                     the weight when the scatter has one component)
-//   [NIJ, NIJ + D)    T_k(x)
-//   [NIJ + D, +3)     the scatter's weights (one per component)
+//   one component:    [NIJ, NIJ + D) T_k(x)
+//   three, FOLD:      [NIJ + l D, + D) w_l T_k(x) for l = 0, 1, 2
+//   three, otherwise: [NIJ, NIJ + D) T_k(x), [NIJ + D, + 3) the weights
 template <int D>
 struct AdjF64Shared {
   static constexpr int BS = kAdjF64Threads + 1;
   static constexpr int NIJ = D * (D + 1) / 2;
-  static constexpr int NS = NIJ + D + 3;
+  // the folded layout where two CTAs per SM still fit (228 KB per SM, 1 KB
+  // reserved per CTA)
+  static constexpr bool FOLD = (size_t)(NIJ + 3 * D) * BS * 8 + 2048 <= 113 * 1024;
+  static constexpr int NS = FOLD ? NIJ + 3 * D : NIJ + D + 3;
   double slots[NS * BS];
   int leaf[kAdjF64Threads];            // scatter leaf of each point (-1: none / done)
   unsigned char list[kAdjF64Threads];  // points of the leaf in progress
@@ -96,9 +103,19 @@ __device__ __forceinline__ void scatter_f64(AdjF64Shared<D>& sm, double* __restr
       for (int j = 0; j < D - i; ++j, ++ij) col[ij * BS] = zi * ty[j];
     }
 #pragma unroll
-    for (int k = 0; k < D; ++k) col[(NIJ + k) * BS] = tx[k];
+    if (DOF == 1 || !AdjF64Shared<D>::FOLD) {
 #pragma unroll
-    for (int l = 0; l < DOF; ++l) col[(NIJ + D + l) * BS] = w[l];
+      for (int k = 0; k < D; ++k) col[(NIJ + k) * BS] = tx[k];
+      if (DOF > 1) {
+#pragma unroll
+        for (int l = 0; l < DOF; ++l) col[(NIJ + D + l) * BS] = w[l];
+      }
+    } else {
+#pragma unroll
+      for (int l = 0; l < DOF; ++l)
+#pragma unroll
+        for (int k = 0; k < D; ++k) col[(NIJ + l * D + k) * BS] = w[l] * tx[k];
+    }
   }
   const int my_leaf = lf >= 0 ? (int)lf : -1;
   sm.leaf[tid] = my_leaf;
@@ -152,6 +169,16 @@ __device__ __forceinline__ void scatter_f64(AdjF64Shared<D>& sm, double* __restr
           if (ozy[c] >= 0) acc[c][0] = fma(pc[ozy[c]], pc[ox[c]], acc[c][0]);
         continue;
       }
+      if (AdjF64Shared<D>::FOLD) {
+#pragma unroll
+        for (int c = 0; c < PER; ++c) {
+          if (ozy[c] < 0) continue;
+          const double zy = pc[ozy[c]];
+#pragma unroll
+          for (int l = 0; l < DOF; ++l) acc[c][l] = fma(zy, pc[ox[c] + l * D * BS], acc[c][l]);
+        }
+        continue;
+      }
       double wp[DOF];
 #pragma unroll
       for (int l = 0; l < DOF; ++l) wp[l] = pc[(NIJ + D + l) * BS];
@@ -176,7 +203,7 @@ __device__ __forceinline__ void scatter_f64(AdjF64Shared<D>& sm, double* __restr
 
 // One thread per target node, its X* and Xd from a.xmid / a.xdep (required)
 // and the node term's weights to a.wnode (required).  Two CTAs per SM up to
-// q = 9 (shared memory: 57 doubles per target at q = 8).
+// q = 9 (shared memory: 72 doubles per target at q = 8).
 template <int D>
 __global__ void __launch_bounds__(kAdjF64Threads, (D <= 10 ? 2 : 1))
     k_adjoint_f64(const AdjArgs a) {
