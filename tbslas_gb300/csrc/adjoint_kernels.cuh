@@ -39,7 +39,7 @@ struct AdjArgs {
 // T_k and dT_k/dxi for k < D; zero outside [-1,1] like cheb_T.
 template <int D>
 __device__ __forceinline__ void cheb_TdT(double xi, double (&T)[D], double (&dT)[D]) {
-  const bool ok = fabs(xi) <= 1.0;
+  const bool ok = abs_at_most_one(xi);
   const double x = ok ? xi : 0.0;
   T[0] = ok ? 1.0 : 0.0;
   dT[0] = 0.0;

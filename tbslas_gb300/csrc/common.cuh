@@ -35,25 +35,60 @@ __host__ __device__ inline uint64_t morton3(uint64_t x, uint64_t y, uint64_t z) 
   return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
 }
 
+// The comparisons of coordinates against 0 and 1 below are made on the bits
+// of the FP64 value with integer instructions: FP64 comparisons and
+// conversions issue to the FP64 pipe, which bounds every SL kernel, while
+// the integer pipe has room.  Each gives the FP64 comparison's answer for
+// every input, -0.0, subnormals, infinities and NaN included.
+__device__ __forceinline__ uint64_t dbits(double c) { return (uint64_t)__double_as_longlong(c); }
+constexpr uint64_t kBitsOne = 0x3FF0000000000000ull;   // 1.0
+constexpr uint64_t kBitsNegZero = 0x8000000000000000ull;
+constexpr uint64_t kBitsAbs = 0x7FFFFFFFFFFFFFFFull;
+
+// c < 0.0: sign set, not -0.0, not a NaN (bits in (-0.0, -inf]).
+__device__ __forceinline__ bool below_zero(double c) {
+  return dbits(c) - (kBitsNegZero + 1) < 0x7FF0000000000000ull;
+}
+// c >= 1.0: bits in [1.0, +inf].
+__device__ __forceinline__ bool at_least_one(double c) {
+  return dbits(c) - kBitsOne <= 0x4000000000000000ull;
+}
+// 0 <= c <= 1 (closed) or 0 <= c < 1.
+__device__ __forceinline__ bool in_unit_closed(double c) {
+  const uint64_t b = dbits(c);
+  return b <= kBitsOne || b == kBitsNegZero;
+}
+__device__ __forceinline__ bool in_unit_open(double c) {
+  const uint64_t b = dbits(c);
+  return b < kBitsOne || b == kBitsNegZero;
+}
+// |c| <= 1 (NaN false).
+__device__ __forceinline__ bool abs_at_most_one(double c) { return (dbits(c) & kBitsAbs) <= kBitsOne; }
+
 // Single periodic wrap of one coordinate, src/tree/tree_functor.h:442-448.
 __device__ __forceinline__ double wrap1(double c) {
-  if (c < 0.0) c = c + 1.0;
-  if (c >= 1.0) c = c - 1.0;
+  if (below_zero(c)) c = c + 1.0;
+  if (at_least_one(c)) c = c - 1.0;
   return c;
 }
 
-// Axis coordinate -> 21-bit integer.  The caller has checked 0 <= c <= 1
-// (c < 1 under periodic).  c == 1.0 is shifted into the last cell as the
-// reference does for non-periodic trees (src/tree/tree_functor.h:464-479).
+// Axis coordinate -> 21-bit integer, floor(c 2^21) (the product is exact, a
+// power-of-two scaling) formed from the mantissa and exponent.  The caller
+// has checked 0 <= c <= 1 (c < 1 under periodic).  c == 1.0 is shifted into
+// the last cell as the reference does for non-periodic trees
+// (src/tree/tree_functor.h:464-479).
 __device__ __forceinline__ uint64_t quantise(double c) {
-  return c >= 1.0 ? (kKeyScale - 1) : (uint64_t)(c * (double)kKeyScale);
+  const uint64_t b = dbits(c) & kBitsAbs;  // -0.0 -> +0.0
+  if (b >= kBitsOne) return kKeyScale - 1;
+  const int s = 1075 - kKeyBits - (int)(b >> 52);  // c 2^21 = M 2^-s, s >= 32
+  if (s > 52) return 0;                             // c < 2^-21, zero, subnormal
+  return ((b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull) >> s;
 }
 
 // Is the (already wrapped) point inside the domain?  NaN compares false.
 __device__ __forceinline__ bool inside(double x, double y, double z, bool periodic) {
-  if (periodic)
-    return x >= 0.0 && x < 1.0 && y >= 0.0 && y < 1.0 && z >= 0.0 && z < 1.0;
-  return x >= 0.0 && x <= 1.0 && y >= 0.0 && y <= 1.0 && z >= 0.0 && z <= 1.0;
+  if (periodic) return in_unit_open(x) && in_unit_open(y) && in_unit_open(z);
+  return in_unit_closed(x) && in_unit_closed(y) && in_unit_closed(z);
 }
 
 // Per-leaf geometry: anchor x, y, z and w = 2*2^depth (the scale that maps
@@ -101,7 +136,7 @@ __device__ __forceinline__ int64_t find_leaf(const TreeView& t, uint64_t key) {
 // called at src/tree/tree_functor.h:328-330).
 template <int D>
 __device__ __forceinline__ void cheb_T(double xi, double (&T)[D]) {
-  const bool ok = fabs(xi) <= 1.0;
+  const bool ok = abs_at_most_one(xi);
   const double x = ok ? xi : 0.0;
   T[0] = ok ? 1.0 : 0.0;
   if (D > 1) T[1] = x;

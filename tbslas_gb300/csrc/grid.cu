@@ -32,15 +32,35 @@ __device__ __forceinline__ void lagrange4(double t, double (&w)[4]) {
   }
 }
 
+// Stencil base and offset of one coordinate on a periodic grid of N = 2^nl
+// nodes, with integer operations on the bits of x in [0, 1): p = x N,
+// g = floor(p) - 1, t = p - g in [1, 2) -- the values make_stencil computes
+// in FP64 (x N is exact: a power-of-two scaling).
+__device__ __forceinline__ void grid_split_pow2(double x, int nl, int& g, double& t) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int s = 1075 - nl - (int)(b >> 52);  // p = M 2^-s, M = 2^52 + mantissa
+  if ((b << 1) == 0 || s > 52) {             // +-0, or p < 1 (first cell): FP64
+    g = -1;
+    t = fma(x, (double)(1 << nl), 1.0);
+    return;
+  }
+  const unsigned long long M = (b & ((1ull << 52) - 1)) | (1ull << 52);
+  g = (int)(M >> s) - 1;
+  const unsigned long long frac = s > 0 ? (M & ((1ull << s) - 1)) : 0ull;
+  t = __longlong_as_double((long long)((1023ull << 52) | (frac << (52 - s))));
+}
+
 struct Stencil {
   int64_t ix[4], iy[4], iz[4];  // x offsets, y*N, z*N*N
   double wx[4], wy[4], wz[4];
 };
 
 // Builds the stencil of a point; returns false when the point evaluates to 0.
-// Under PERIODIC the coordinates are wrapped in place.
+// Under PERIODIC the coordinates are wrapped in place.  nl >= 0 (periodic,
+// N = 2^nl): stencil bases and offsets by grid_split_pow2, the same values
+// without FP64 instructions.
 __device__ __forceinline__ bool make_stencil(double& x, double& y, double& z, int N,
-                                             bool periodic, Stencil& s) {
+                                             bool periodic, Stencil& s, int nl = -1) {
   if (periodic) {
     x = wrap1(x);
     y = wrap1(y);
@@ -53,6 +73,12 @@ __device__ __forceinline__ bool make_stencil(double& x, double& y, double& z, in
   double t[3];
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
+    if (periodic && nl >= 0) {
+      int g;
+      grid_split_pow2(c[j], nl, g, t[j]);
+      base[j] = g;
+      continue;
+    }
     const double p = c[j] * scale;
     int64_t g = (int64_t)p - 1;
     if (!periodic) {
@@ -128,7 +154,8 @@ __global__ void __launch_bounds__(256, 2) k_semilag_grid(const double* __restric
                                                       const double* __restrict__ con,
                                                       double* __restrict__ cout, int N,
                                                       double tau, int nrk, int periodic,
-                                                      int node_read) {
+                                                      int nl) {
+  const bool node_read = nl >= 0;  // periodic power-of-two grid
   const int64_t N3 = (int64_t)N * N * N;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= N3) return;
@@ -147,7 +174,7 @@ __global__ void __launch_bounds__(256, 2) k_semilag_grid(const double* __restric
       v[2] = __ldg(vel + 2 * N3 + t);
     } else {
       Stencil s;
-      if (make_stencil(px, py, pz, N, per, s)) {
+      if (make_stencil(px, py, pz, N, per, s, nl)) {
         v[0] = apply_stencil(vel, s);
         v[1] = apply_stencil(vel + N3, s);
         v[2] = apply_stencil(vel + 2 * N3, s);
@@ -172,7 +199,7 @@ __global__ void __launch_bounds__(256, 2) k_semilag_grid(const double* __restric
     }
   }
   Stencil s;
-  cout[t] = make_stencil(x, y, z, N, per, s) ? apply_stencil(con, s) : 0.0;
+  cout[t] = make_stencil(x, y, z, N, per, s, nl) ? apply_stencil(con, s) : 0.0;
 }
 
 // Stencil of the double-float path: grid indices per axis (32-bit; the
@@ -240,23 +267,6 @@ __device__ __forceinline__ void lagrange4_df(double t, df (&w)[4]) {
   w[3] = df_norm(df_mul_n(df_mul_n(df_mul_n(sixth, d0), d1), d2));
 }
 
-// Stencil base and offset of one coordinate on a periodic grid of N = 2^nl
-// nodes, with integer operations on the bits of x in [0, 1): p = x N,
-// g = floor(p) - 1, t = p - g in [1, 2) -- the values make_stencil computes
-// in FP64 (x N is exact: a power-of-two scaling).
-__device__ __forceinline__ void grid_split_pow2(double x, int nl, int& g, double& t) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int s = 1075 - nl - (int)(b >> 52);  // p = M 2^-s, M = 2^52 + mantissa
-  if (x == 0.0 || s > 52) {                  // p < 1 (first cell): FP64
-    g = -1;
-    t = fma(x, (double)(1 << nl), 1.0);
-    return;
-  }
-  const unsigned long long M = (b & ((1ull << 52) - 1)) | (1ull << 52);
-  g = (int)(M >> s) - 1;
-  const unsigned long long frac = s > 0 ? (M & ((1ull << s) - 1)) : 0ull;
-  t = __longlong_as_double((long long)((1023ull << 52) | (frac << (52 - s))));
-}
 
 // Stencil of a point on the periodic grid for the double-float sums: the
 // indices of make_stencil, the weights from lagrange4_df.  Returns false for
@@ -385,9 +395,12 @@ void launch_semilag_grid(const double* vel, const double* con, double* cout, int
                          double tau, int nrk, int periodic, cudaStream_t s) {
   const int64_t n = (int64_t)nreg * nreg * nreg;
   const bool pow2 = (nreg & (nreg - 1)) == 0;
-  const int node_read = (periodic && pow2) ? 1 : 0;
+  int nl = -1;
+  if (periodic && pow2)
+    for (nl = 0; (1 << nl) < nreg; ++nl) {
+    }
   k_semilag_grid<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(vel, con, cout, nreg, tau, nrk,
-                                                             periodic, node_read);
+                                                             periodic, nl);
 }
 
 void launch_semilag_grid_df(const double* vel, const double* con, double* cout, int nreg,

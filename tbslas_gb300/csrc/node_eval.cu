@@ -170,7 +170,7 @@ __device__ __forceinline__ void for_each_subgrid(const TreeView& S, const TreeVi
     if (per) c = wrap1(c);
     sx[tid] = c;
     // the per-axis part of inside(); a point is inside iff all three are
-    const bool in = per ? (c >= 0.0 && c < 1.0) : (c >= 0.0 && c <= 1.0);
+    const bool in = per ? in_unit_open(c) : in_unit_closed(c);
     sq[tid] = in ? (uint32_t)quantise(c) : 0xffffffffu;
   }
   __syncthreads();

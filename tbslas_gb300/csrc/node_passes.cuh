@@ -10,7 +10,7 @@ namespace tbg {
 template <int Ds>
 __device__ __forceinline__ void cheb_T_col(double xi, double* T, int stride) {
   // the operations of cheb_T<Ds>, written to a strided column
-  const bool ok = fabs(xi) <= 1.0;
+  const bool ok = abs_at_most_one(xi);
   const double x = ok ? xi : 0.0;
   const double t0 = ok ? 1.0 : 0.0;
   T[0] = t0;
