@@ -50,6 +50,39 @@ __device__ __forceinline__ void grid_split_pow2(double x, int nl, int& g, double
   t = __longlong_as_double((long long)((1023ull << 52) | (frac << (52 - s))));
 }
 
+// g 2^-52 as a double for 0 < g <= 2^53 (exact: g has at most 53 bits), with
+// the sign bit set when neg.
+__device__ __forceinline__ double scaled_mantissa(uint64_t g, bool neg) {
+  const int p = 63 - __clzll((long long)g);  // leading bit, <= 53
+  const uint64_t m = p <= 52 ? (g << (52 - p)) & 0x000FFFFFFFFFFFFFull : 0ull;
+  return __longlong_as_double(
+      (long long)((neg ? kBitsNegZero : 0ull) | ((uint64_t)(1023 + p - 52) << 52) | m));
+}
+
+// lagrange4 for an offset t in [1, 2) (a power-of-two grid's): the same
+// products in the same order, with t - 1, t - 2, t - 3 and the exact
+// halvings +-t/2 formed from the mantissa of t by integer operations (each
+// of those FP64 operations is exact, so the values are the same).  Other
+// offsets (t rounded up to 2 in the first cell) take lagrange4.
+__device__ __forceinline__ void lagrange4_unit(double t, double (&w)[4]) {
+  const uint64_t b = dbits(t);
+  if ((b >> 52) != 1023) {
+    lagrange4(t, w);
+    return;
+  }
+  const uint64_t f = b & 0x000FFFFFFFFFFFFFull;
+  const double d1 = f ? scaled_mantissa(f, false) : 0.0;      // t - 1 in [0, 1)
+  const double d2 = scaled_mantissa((1ull << 52) - f, true);  // t - 2 in [-1, 0)
+  const double d3 = scaled_mantissa((1ull << 53) - f, true);  // t - 3 in [-2, -1)
+  const uint64_t hb = b - (1ull << 52);                        // t / 2
+  const double h = __longlong_as_double((long long)hb);
+  const double hn = __longlong_as_double((long long)(hb | kBitsNegZero));
+  w[0] = ((-1.0 / 6.0 * d1) * d2) * d3;
+  w[1] = (h * d2) * d3;
+  w[2] = (hn * d1) * d3;
+  w[3] = ((1.0 / 6.0 * t) * d1) * d2;
+}
+
 struct Stencil {
   int64_t ix[4], iy[4], iz[4];  // x offsets, y*N, z*N*N
   double wx[4], wy[4], wz[4];
@@ -88,9 +121,15 @@ __device__ __forceinline__ bool make_stencil(double& x, double& y, double& z, in
     base[j] = g;
     t[j] = p - (double)g;
   }
-  lagrange4(t[0], s.wx);
-  lagrange4(t[1], s.wy);
-  lagrange4(t[2], s.wz);
+  if (periodic && nl >= 0) {
+    lagrange4_unit(t[0], s.wx);
+    lagrange4_unit(t[1], s.wy);
+    lagrange4_unit(t[2], s.wz);
+  } else {
+    lagrange4(t[0], s.wx);
+    lagrange4(t[1], s.wy);
+    lagrange4(t[2], s.wz);
+  }
   const int64_t NN = (int64_t)N * N;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
@@ -116,16 +155,20 @@ __device__ __forceinline__ double apply_stencil(const double* __restrict__ g, co
   double u = 0.0;
 #pragma unroll 1
   for (int j2 = 0; j2 < 4; ++j2) {
+    // the plane's offset and weight by selects, not by a run-time index:
+    // the stencil then stays in registers instead of local memory
+    const int64_t iz = j2 == 0 ? s.iz[0] : (j2 == 1 ? s.iz[1] : (j2 == 2 ? s.iz[2] : s.iz[3]));
+    const double wz = j2 == 0 ? s.wz[0] : (j2 == 1 ? s.wz[1] : (j2 == 2 ? s.wz[2] : s.wz[3]));
     double v = 0.0;
 #pragma unroll
     for (int j1 = 0; j1 < 4; ++j1) {
-      const double* row = g + s.iz[j2] + s.iy[j1];
+      const double* row = g + iz + s.iy[j1];
       double w = 0.0;
 #pragma unroll
       for (int j0 = 0; j0 < 4; ++j0) w = fma(s.wx[j0], __ldg(row + s.ix[j0]), w);
       v = fma(s.wy[j1], w, v);
     }
-    u = fma(s.wz[j2], v, u);
+    u = fma(wz, v, u);
   }
   return u;
 }
