@@ -175,6 +175,36 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+_NOMINAL = {}
+
+
+def fp64_nominal_tflops():
+    """The FP64 pipe's nominal rate: 2 FP64 FMA per clock per SM x 2 FLOP x
+    SMs x the GPU's maximum SM clock (nvidia-smi; the bench rejects runs whose
+    clock sat below it).  Reported beside the measured FMA probe, which
+    reaches ~95 % of it: a probe's own FMAs are limited by operand fetch."""
+    if "v" not in _NOMINAL:
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        mhz = None
+        try:
+            idx = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
+            out = subprocess.run(["nvidia-smi", "-i", idx, "--query-gpu=clocks.max.sm",
+                                  "--format=csv,noheader,nounits"], capture_output=True,
+                                 text=True, timeout=20).stdout.strip().splitlines()
+            mhz = float(out[0]) if out else None
+        except (OSError, ValueError, subprocess.SubprocessError):
+            mhz = None
+        _NOMINAL["v"] = 4.0 * sms * mhz * 1e6 / 1e12 if mhz else None
+    return _NOMINAL["v"]
+
+
+def nominal_fields(achieved):
+    nom = fp64_nominal_tflops()
+    return {"nominal_peak": nom, "frac_of_nominal": achieved / nom if nom else None,
+            "nominal_source": "2 FP64 FMA per clock per SM x SMs x maximum SM clock"}
+
+
 # ---------------------------------------------------------------------------
 def cpu_baseline_tree(wl, budget_s=12.0, steps=1):
     """The oracle (OpenMP C++ restatement of the reference CPU path) on a
@@ -200,6 +230,30 @@ def cpu_baseline_tree(wl, budget_s=12.0, steps=1):
             "sample": "%d of %d concentration leaves (%d departure points) x %d step(s), "
                       "one SL step from the initial state" % (k, len(wl.cd), k * npl, steps),
             "seconds": sec}, out, k
+
+
+def cpu_baseline_batched(wl, budget_s=10.0):
+    """The oracle on a bounded sample of the batched workload: one in-situ
+    step of the first leaves of each problem in turn (every problem's
+    degree), ~budget_s of CPU work."""
+    from oracle import oracle as ora
+    cores = ora.num_threads()
+    pts, sec, used = 0, 0.0, 0
+    for p in wl.problems:
+        vel = dict(anchor=p["va"], depth=p["vd"], q=p["q"], dof=3, coeff=p["vc"])
+        con = dict(anchor=p["ca"], depth=p["cd"], q=p["q"], dof=1, coeff=p["cc"])
+        ora.pt2coeff(p["q"])
+        k = min(len(p["cd"]), 8)
+        t0 = time.perf_counter()
+        ora.semilag_in_situ(vel, con, 1, p["dt"], 1, bool(wl.bc), leaf_begin=0, leaf_end=k)
+        sec += time.perf_counter() - t0
+        pts += k * (p["q"] + 1) ** 3
+        used += 1
+        if sec > budget_s:
+            break
+    return {"value": pts / sec, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "first %s leaves of %d of %d problems (%d departure points), one SL "
+                      "step each" % ("8", used, len(wl.problems), pts), "seconds": sec}
 
 
 def cpu_baseline_grid(wl, budget_s=12.0):
@@ -416,7 +470,8 @@ def fp64_roofline(ctx, kernel, flops_per_point, points_per_launch, prof, name, s
                            "MEASURED_PEAKS.json holds no FP64 figure",
             "algorithmic_flops_per_point": flops_per_point, "counting": counting,
             "launch_ms": launch_ms, "traffic": None,
-            "kernels_ms_per_step": {k: v[2] / steps for k, v in prof.items()}}
+            "kernels_ms_per_step": {k: v[2] / steps for k, v in prof.items()},
+            **nominal_fields(achieved)}
 
 
 def run_gpu(args, wl, rank, world, local_rank):
@@ -604,7 +659,7 @@ def run_gpu(args, wl, rank, world, local_rank):
         "launch_ms": launch_ms, "traffic": _traffic(wl.name, dominant),
         "hbm": {"achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved_gbs / peaks["hbm_gbs"], "peak_source": peak_src},
-        "kernels_ms_per_step": per_kernel}
+        "kernels_ms_per_step": per_kernel, **nominal_fields(achieved)}
 
     # the double-float mode's own roofline: its sums are FP32 instructions,
     # each counted as an FMA (2 FLOP) against the measured FP32 FMA peak
@@ -741,7 +796,8 @@ def run_functor(args, wl, rank, world, local_rank):
         launch_ms = kms / g
         ach = flops * n / (launch_ms * 1e-3) / 1e12
         return {"launch_ms": launch_ms, "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": ach / fp64_peak, "algorithmic_flops_per_point": flops}
+                "frac": ach / fp64_peak, "algorithmic_flops_per_point": flops,
+                **nominal_fields(ach)}
     line = {"metric": METRIC, "value": n * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -1340,6 +1396,23 @@ def run_batched(args, wl, rank, world, local_rank):
                               "ctas_per_sm": r["tune"][2]}}
     cfg = describe_config(wl)
     s64, sdf = summary(r64), summary(rdf)
+    # the whole batched step (node-grid kernels, band kernels, refit) over its
+    # graph time, counting per target the fused kernel's algorithmic FLOPs (the
+    # midpoint velocity and the departure concentration, as the headline's
+    # roofline counts them); the node-grid pass and the refit add time only
+    step_flops = sum(len(p["cd"]) * (p["q"] + 1) ** 3 * fused_flops_per_point_tree(p["q"])
+                     for p in wl.problems)
+    ach = step_flops / (r64["ms"] / args.steps * 1e-3) / 1e12
+    fp64_peak = ctx.fp64_fma_peak() / 1e12
+    roofline = {"kernel": "the batched step (k_batch_eval_on_nodes, k_batch_semilag_fp64 "
+                          "bands, k_batch_refit), FP64", "bound": "fp64",
+                "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                "peak_source": "FP64 FMA throughput measured in this run (tbslas_fp64_fma_peak)",
+                "counting": "per problem: targets x the fused step's FLOPs (3*d*3 + 2*Nc*dof "
+                            "per evaluation, velocity at the midpoint and concentration at the "
+                            "departure point, RK updates) over the whole step's graph time",
+                **nominal_fields(ach)}
+    cpu = cpu_baseline_batched(wl)
     line = {"metric": METRIC, "value": tot_points / tot_sec, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r64["ms"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -1349,6 +1422,7 @@ def run_batched(args, wl, rank, world, local_rank):
             "accuracy": {"batched_equals_plain_bitwise": s64["batched_equals_plain_bitwise"],
                          "plain_loop": "oracle-checked per problem (tests/test_gpu_tree.py)"},
             "autotuned": s64["autotuned"],
+            "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": e_points / e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(h2d)},
             "df64_sums": dict(sdf, dtype="f64 coordinates, double-float sums",
@@ -1463,22 +1537,24 @@ def run_adjoint(args, wl, rank, world, local_rank):
         return fms_plain, res
 
     with ClockSampler(local_rank) as clk:
-        fwd_ms, res = passes((True, "departure", False))
+        fwd_ms, res = passes(("jacobian", True, "departure", False))
     # per-kernel breakdown of one more adjoint pass each way (profiler on,
     # outside the timed passes)
     by_kernel = {}
-    for ck in (True, False):
+    for ck, name in (("jacobian", "checkpoint_jacobian"), (True, "checkpoint"),
+                     (False, "recompute")):
         _, _, j1 = grad(ck)
         ctx.profile(True)
         ctx.profile_reset()
         j1.backward()
         torch.cuda.synchronize()
-        by_kernel["checkpoint" if ck else "recompute"] = {
-            k: round(v[2] / T, 3) for k, v in sorted(ctx.profile_totals().items())}
+        by_kernel[name] = {k: round(v[2] / T, 3) for k, v in sorted(ctx.profile_totals().items())}
         ctx.profile(False)
     with ctx.sums_mode(tb.SUMS_DOUBLE_FLOAT):
         fwd_df_ms, res_df = passes((True,))
-    gc, gv = res[True][2], res[True][3]
+    # the headline mode: every step's points and velocity Jacobian stored
+    # (memory is plentiful at this size: 120 B per target per step)
+    gc, gv = res["jacobian"][2], res["jacobian"][3]
     rng = np.random.default_rng(123)
     eps = 1e-6
 
@@ -1506,24 +1582,57 @@ def run_adjoint(args, wl, rank, world, local_rank):
         errs_v.append(abs(fd - an) / abs(an))
     t_fd = time.perf_counter() - t_fd
     dual = dual_check_adjoint(wl, ctx, dev)
+    jk_fms, jk_bms = res["jacobian"][0], res["jacobian"][1]
     ck_fms, ck_bms = res[True][0], res[True][1]
     rc_fms, rc_bms = res[False][0], res[False][1]
-    ck_gap = max(float((res[True][2] - res[False][2]).abs().max() / res[False][2].abs().max()),
-                 float((res[True][3] - res[False][3]).abs().max() / res[False][3].abs().max()))
+
+    def gap(x, y):
+        return max(float((x[2] - y[2]).abs().max() / y[2].abs().max()),
+                   float((x[3] - y[3]).abs().max() / y[3].abs().max()))
+    ck_gap = gap(res[True], res[False])
+    jk_gap = gap(res["jacobian"], res[False])
     df_gap = max(float((res_df[True][2] - gc).abs().max() / gc.abs().max()),
                  float((res_df[True][3] - gv).abs().max() / gv.abs().max()))
     points = wl.points_per_step * T
+    # the adjoint kernel against the FP64 peak: per target, grad c^k(Xd)
+    # (2 Nc multiply-adds), the lambda scatter (Nc), J_v(X*)^T g (9) and the
+    # velocity scatter (3 Nc)
+    nc = tb.n_coeff(wl.q)
+    adj_flops = 2 * (6 * nc + 9)
+    kms = by_kernel["checkpoint_jacobian"].get("adjoint_fp64", 0.0)
+    ach = adj_flops * wl.points_per_step / (max(kms, 1e-9) * 1e-3) / 1e12
+    fp64_peak = ctx.fp64_fma_peak() / 1e12
+    roofline = {"kernel": "adjoint_fp64 (k_adjoint_f64<%d, true>)" % (wl.q + 1),
+                "bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": ach / fp64_peak, "launch_ms": kms,
+                "peak_source": "FP64 FMA throughput measured in this run (tbslas_fp64_fma_peak)",
+                "algorithmic_flops_per_point": adj_flops,
+                "counting": "2 x (6 Nc + 9) per target: grad c^k(Xd) 2 Nc, lambda scatter Nc, "
+                            "J_v(X*)^T g 9, velocity scatter 3 Nc multiply-adds",
+                **nominal_fields(ach)}
+    cpu = {"value": dual["points_per_s"], "unit": UNIT, "cores": dual["cores"], "kind": "port",
+           "sample": "the oracle's in-situ step on forward-mode dual numbers (one directional "
+                     "derivative of the T-step map, the CPU counterpart of one gradient "
+                     "direction; the reference has no adjoint): %s" % dual["tree"],
+           "seconds": dual["seconds"]}
     if rank != 0:
         return None
     fd_max = max(errs_c + errs_v)
-    line = {"metric": METRIC, "value": points / (ck_bms * 1e-3), "unit": UNIT + " (adjoint pass)",
-            "n_gpus": world, "steps": T, "warmup": 1, "ms_per_step": ck_bms / T,
+    line = {"metric": METRIC, "value": points / (jk_bms * 1e-3), "unit": UNIT + " (adjoint pass)",
+            "n_gpus": world, "steps": T, "warmup": 1, "ms_per_step": jk_bms / T,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded analytic fields)", "config": describe_config(wl),
-            "adj_over_fwd": ck_bms / fwd_ms,
+            "adj_over_fwd": jk_bms / fwd_ms, "mode": "checkpoint_jacobian",
             "fd_max_rel": fd_max, "dual_max_rel": dual["max_rel_err"],
+            "roofline": roofline, "cpu_baseline": cpu,
             "forward": {"ms": fwd_ms, "points_per_s": points / (fwd_ms * 1e-3),
                         "kind": "the in-situ step (FP64 sums), no checkpoints"},
+            "checkpoint_jacobian": {"forward_ms": jk_fms, "adjoint_ms": jk_bms,
+                                    "adj_over_fwd": jk_bms / fwd_ms,
+                                    "grad_over_fwd": (jk_fms + jk_bms) / fwd_ms,
+                                    "stored_bytes": int(points * 120),
+                                    "note": "midpoints, departure points and the velocity "
+                                            "Jacobian at the midpoints stored by the forward"},
             "checkpoint": {"forward_ms": ck_fms, "adjoint_ms": ck_bms,
                            "adj_over_fwd": ck_bms / fwd_ms,
                            "grad_over_fwd": (ck_fms + ck_bms) / fwd_ms,
@@ -1549,7 +1658,8 @@ def run_adjoint(args, wl, rank, world, local_rank):
                          "seconds": t_fd, "tolerance": 1e-6},
             "dual_number_check": dual,
             "adjoint_ms_per_step_by_kernel": by_kernel,
-            "checkpoint_vs_recompute_rel_diff": ck_gap, "J": res[True][4],
+            "checkpoint_vs_recompute_rel_diff": ck_gap,
+            "jacobian_vs_recompute_rel_diff": jk_gap, "J": res["jacobian"][4],
             "df64_sums": {"forward_ms": fwd_df_ms, "adjoint_ms": res_df[True][1],
                           "adj_over_fwd": res_df[True][1] / fwd_df_ms,
                           "adj_over_fp64_fwd": res_df[True][1] / fwd_ms,
@@ -1581,7 +1691,7 @@ def dual_check_adjoint(wl, ctx, dev, depth=3, ndir=2):
                               small.steps, small.bc, False).cpu().numpy()
     c = torch.from_numpy(small.c0).to(dev).requires_grad_(True)
     v = torch.from_numpy(small.vc).to(dev).requires_grad_(True)
-    cT = adjoint.advect(c, v, tv, tc, small.dt, 1, small.steps, small.bc, True)
+    cT = adjoint.advect(c, v, tv, tc, small.dt, 1, small.steps, small.bc, "jacobian")
     Vt = torch.from_numpy(Vb).to(dev)
     J = 0.5 * ((torch.einsum("ln,pn->lp", cT[:, 0, :], Vt) -
                 torch.einsum("ln,pn->lp", torch.from_numpy(cobs).to(dev)[:, 0, :], Vt)) ** 2).sum()
@@ -1602,9 +1712,11 @@ def dual_check_adjoint(wl, ctx, dev, depth=3, ndir=2):
         dJ = float((resid * (dcc[:, 0, :] @ Vb.T)).sum())
         an = float((gc * dc).sum() + (gv * dv).sum())
         errs.append(abs(dJ - an) / abs(dJ))
+    sec = time.perf_counter() - t0
+    pts = len(small.d) * (small.q + 1) ** 3 * small.steps * ndir
     return {"tree": "uniform depth %d (%d leaves), same q/velocity/steps" % (depth, len(small.d)),
-            "directions": ndir, "max_rel_err": max(errs),
-            "seconds": time.perf_counter() - t0}
+            "directions": ndir, "max_rel_err": max(errs), "gradient_mode": "checkpoint_jacobian",
+            "seconds": sec, "points_per_s": pts / sec, "cores": ora.num_threads()}
 
 
 def _band(q):

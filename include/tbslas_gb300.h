@@ -382,6 +382,16 @@ int tbslas_semilag_bdf2(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con_prev,
 int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
                                 double dt, int bc, double* xmid_dev, double* xdep_dev,
                                 void* stream);
+/* The same checkpointed step that also stores the velocity Jacobian at every
+ * midpoint, jac_dev[N*9] (row-major dv_a/dx_b, a the component), for
+ * tbslas_semilag_adjoint_jac: 120 B per target with xmid and xdep.  The
+ * step's node values and points are bit-identical to tbslas_semilag_in_situ's
+ * (the midpoint velocity comes out of the same sums as its gradient).  FP64
+ * sums only (TBSLAS_ERR_UNSUPPORTED in the double-float mode); all three
+ * buffers required. */
+int tbslas_semilag_in_situ_ckpt_jac(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                    int timestep, double dt, int bc, double* xmid_dev,
+                                    double* xdep_dev, double* jac_dev, void* stream);
 /* Adjoint of step `timestep`: con_coeff_k_dev [L][Nc] = the concentration
  * coefficients the step started from; lambda_next_dev [L][Nc] = dJ/dC^{k+1};
  * writes lambda_k_dev [L][Nc] = dJ/dC^k and ADDS the step's dJ/dV to
@@ -410,6 +420,19 @@ int tbslas_semilag_adjoint_seq(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
                                const double* lambda_next_dev, double* lambda_k_dev,
                                double* grad_vel_dev, const double* xmid_dev,
                                const double* xdep_dev, const double* vel_at_nodes_dev,
+                               double* node_weights_dev, void* stream);
+/* The adjoint step with the forward's Jacobian checkpoint (xmid, xdep and
+ * jac from tbslas_semilag_in_situ_ckpt_jac, all required): J_v(X*)^T g is
+ * read instead of evaluated, which takes the 5 Nc multiply-adds per target of
+ * the velocity-gradient term out of the adjoint pass.  node_weights_dev:
+ * as tbslas_semilag_adjoint_seq, or NULL for the step to scatter its own node
+ * term into grad_vel_dev (as tbslas_semilag_adjoint).  FP64 sums only.
+ * Gradients equal the other modes' up to rounding. */
+int tbslas_semilag_adjoint_jac(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                               const double* con_coeff_k_dev, int timestep, double dt, int bc,
+                               const double* lambda_next_dev, double* lambda_k_dev,
+                               double* grad_vel_dev, const double* xmid_dev,
+                               const double* xdep_dev, const double* jac_dev,
                                double* node_weights_dev, void* stream);
 /* ADDS the node term of the summed weights to grad_vel_dev [Lv][3][Nc]: the
  * transposed node-grid pass, once per sequence. */

@@ -16,7 +16,11 @@ gives dJ/dc0 and dJ/dvcoeff.  checkpoint=True stores every step's RK2
 midpoints and departure points (48 bytes per node per step); False
 recomputes them in the backward pass; checkpoint="departure" stores the
 departure points only (24 bytes per node per step) and rebuilds the
-midpoints from the node-grid velocity in the backward pass.
+midpoints from the node-grid velocity in the backward pass;
+checkpoint="jacobian" (FP64 sums) also stores the velocity Jacobian at every
+midpoint (120 bytes per node per step), which the forward forms from the same
+sums as the midpoint velocity and which takes the velocity-gradient term's
+evaluation out of the backward pass.
 """
 import numpy as np
 
@@ -49,6 +53,22 @@ def step_ckpt(vel_functor, tree, timestep, dt, xmid, xdep, stream=None):
     call("tbslas_semilag_in_situ_ckpt", tree.ctx.handle, vel_functor.tree.handle, tree.handle,
          int(timestep), float(dt), vel_functor.bc, api._ptr(xmid), api._ptr(xdep),
          api._stream(stream))
+
+
+def step_ckpt_jac(vel_functor, tree, timestep, dt, xmid, xdep, jac, stream=None):
+    call("tbslas_semilag_in_situ_ckpt_jac", tree.ctx.handle, vel_functor.tree.handle,
+         tree.handle, int(timestep), float(dt), vel_functor.bc, api._ptr(xmid), api._ptr(xdep),
+         api._ptr(jac), api._stream(stream))
+
+
+def step_adjoint_jac(vel_functor, tree, coeff_k, timestep, dt, lam_next, lam_k, grad_vel, xmid,
+                     xdep, jac, node_w=None, stream=None):
+    """One adjoint step from a Jacobian checkpoint; node_w as step_adjoint_seq
+    (None: the step scatters its own node term)."""
+    call("tbslas_semilag_adjoint_jac", tree.ctx.handle, vel_functor.tree.handle, tree.handle,
+         api._ptr(coeff_k), int(timestep), float(dt), vel_functor.bc, api._ptr(lam_next),
+         api._ptr(lam_k), api._ptr(grad_vel), api._ptr(xmid), api._ptr(xdep), api._ptr(jac),
+         api._ptr(node_w), api._stream(stream))
 
 
 def step_adjoint(vel_functor, tree, coeff_k, timestep, dt, lam_next, lam_k, grad_vel, xmid=None,
@@ -87,11 +107,17 @@ def _function():
             states, ckpts = [], []
             for k in range(nsteps):
                 states.append(con_tree.get_coeffs(torch.empty_like(c0)))
-                if checkpoint:
+                if checkpoint == "jacobian":
+                    xd = torch.empty((n, 3), dtype=torch.float64, device=c0.device)
+                    xm = torch.empty_like(xd)
+                    jac = torch.empty((n, 9), dtype=torch.float64, device=c0.device)
+                    step_ckpt_jac(vf, con_tree, timestep0 + k, dt, xm, xd, jac)
+                    ckpts.append((xm, xd, jac))
+                elif checkpoint:
                     xd = torch.empty((n, 3), dtype=torch.float64, device=c0.device)
                     xm = None if checkpoint == "departure" else torch.empty_like(xd)
                     step_ckpt(vf, con_tree, timestep0 + k, dt, xm, xd)
-                    ckpts.append((xm, xd))
+                    ckpts.append((xm, xd, None))
                 else:
                     api.solve_semilag_in_situ(vf, con_tree, timestep0 + k, dt, 1)
             cT = con_tree.get_coeffs(torch.empty_like(c0))
@@ -117,9 +143,13 @@ def _function():
             vn = vf.at_nodes(con_tree) if rebuild and ctx.states else None
             for k in reversed(range(len(ctx.states))):
                 lam_k = torch.empty_like(lam)
-                xm, xd = ctx.ckpts[k] if ctx.ckpts else (None, None)
-                step_adjoint_seq(vf, con_tree, ctx.states[k], ctx.ts0 + k, ctx.dt, lam, lam_k, gv,
-                                 node_w, xm, xd, vn)
+                xm, xd, jac = ctx.ckpts[k] if ctx.ckpts else (None, None, None)
+                if jac is not None:
+                    step_adjoint_jac(vf, con_tree, ctx.states[k], ctx.ts0 + k, ctx.dt, lam, lam_k,
+                                     gv, xm, xd, jac, node_w)
+                else:
+                    step_adjoint_seq(vf, con_tree, ctx.states[k], ctx.ts0 + k, ctx.dt, lam,
+                                     lam_k, gv, node_w, xm, xd, vn)
                 lam = lam_k
             if ctx.states:
                 node_term(vf, con_tree, node_w, gv)
@@ -136,7 +166,7 @@ def advect(c0, vcoeff, vel_tree, con_tree, dt, timestep0=1, nsteps=1, bc=api.Fre
     global _FN
     if _FN is None:
         _FN = _function()
-    if checkpoint not in (True, False, "departure"):
-        raise ValueError("checkpoint must be True, False or 'departure'")
+    if checkpoint not in (True, False, "departure", "jacobian"):
+        raise ValueError("checkpoint must be True, False, 'departure' or 'jacobian'")
     return _FN.apply(c0, vcoeff, vel_tree, con_tree, float(dt), int(timestep0), int(nsteps),
                      int(bc), checkpoint)

@@ -71,6 +71,9 @@ SIGNATURES = {
     "tbslas_semilag_in_situ": [_vp, _vp, _vp, _i32, _f64, _i32, _i32, _vp],
     "tbslas_semilag_in_situ_host": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _i32],
     "tbslas_semilag_in_situ_ckpt": [_vp, _vp, _vp, _i32, _f64, _i32, _vp, _vp, _vp],
+    "tbslas_semilag_in_situ_ckpt_jac": [_vp, _vp, _vp, _i32, _f64, _i32, _vp, _vp, _vp, _vp],
+    "tbslas_semilag_adjoint_jac": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _vp, _vp, _vp, _vp,
+                                   _vp, _vp, _vp, _vp],
     "tbslas_semilag_adjoint": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _vp, _vp, _vp, _vp, _vp,
                                _vp],
     "tbslas_semilag_adjoint_seq": [_vp, _vp, _vp, _vp, _i32, _f64, _i32, _vp, _vp, _vp, _vp,

@@ -12,13 +12,22 @@ constexpr int kAdjMaxDegree = 10;
 struct AdjTable {
   AdjFn adj[kAdjMaxDegree + 1] = {};
   AdjDfFn adj_df[kAdjMaxDegree + 1] = {};
+  JacStepFn jac[kAdjMaxDegree + 1] = {};
   AdjTable() {
-    register_adjoint_a(adj, adj_df);
-    register_adjoint_b(adj, adj_df);
-    register_adjoint_c(adj, adj_df);
+    register_adjoint_a(adj, adj_df, jac);
+    register_adjoint_b(adj, adj_df, jac);
+    register_adjoint_c(adj, adj_df, jac);
   }
 };
 const AdjTable g_adj;
+
+int launch_semilag_jac(int q, const SemilagTreeArgs& a, cudaStream_t s) {
+  if (q < 1 || q > kAdjMaxDegree || !g_adj.jac[q])
+    return fail_status(TBSLAS_ERR_UNSUPPORTED,
+                       "the velocity Jacobian checkpoint supports Chebyshev degree 1..10");
+  g_adj.jac[q](a, s);
+  return TBSLAS_OK;
+}
 
 int check_pair(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, double dt, int bc, TreeView* tv,
                TreeView* tc) {
@@ -72,16 +81,32 @@ extern "C" int tbslas_semilag_in_situ_ckpt(tbslas_ctx ctx, tbslas_tree vel, tbsl
                                 (cudaStream_t)stream);
 }
 
+extern "C" int tbslas_semilag_in_situ_ckpt_jac(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                               int timestep, double dt, int bc, double* xmid_dev,
+                                               double* xdep_dev, double* jac_dev, void* stream) {
+  DeviceRestore restore;
+  TreeView tv, tc;
+  int st = check_pair(ctx, vel, con, dt, bc, &tv, &tc);
+  if (st != TBSLAS_OK) return st;
+  if (!xmid_dev || !xdep_dev || !jac_dev)
+    return fail_status(TBSLAS_ERR_INVALID_ARG, "null checkpoint buffer");
+  if (ctx_sums(ctx) != TBSLAS_SUMS_FP64)
+    return fail_status(TBSLAS_ERR_UNSUPPORTED, "the velocity Jacobian checkpoint needs FP64 sums");
+  return semilag_in_situ_points(ctx, vel, con, timestep, dt, bc, xmid_dev, xdep_dev,
+                                (cudaStream_t)stream, jac_dev);
+}
+
 namespace tbg {
 
 // One adjoint step.  vn_given: the velocity at con's nodes (or null); wnode_acc:
 // where the node term's weights are summed over a sequence of steps (null:
-// this step scatters its own).
+// this step scatters its own); jac_dev: the forward's J_v(X*) checkpoint (or
+// null).
 int semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
                     const double* con_coeff_k_dev, int timestep, double dt, int bc,
                     const double* lambda_next_dev, double* lambda_k_dev, double* grad_vel_dev,
                     const double* xmid_dev, const double* xdep_dev, const double* vn_given,
-                    double* wnode_acc, cudaStream_t s) {
+                    double* wnode_acc, cudaStream_t s, const double* jac_dev = nullptr) {
   TreeView tv, tc;
   int st = check_pair(ctx, vel, con, dt, bc, &tv, &tc);
   if (st != TBSLAS_OK) return st;
@@ -89,6 +114,11 @@ int semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
     return fail_status(TBSLAS_ERR_INVALID_ARG, "null buffer");
   if (xmid_dev && !xdep_dev)
     return fail_status(TBSLAS_ERR_INVALID_ARG, "midpoints without departure points");
+  if (jac_dev && (!xmid_dev || !xdep_dev))
+    return fail_status(TBSLAS_ERR_INVALID_ARG,
+                       "the Jacobian checkpoint needs the midpoints and departure points");
+  if (jac_dev && ctx_sums(ctx) != TBSLAS_SUMS_FP64)
+    return fail_status(TBSLAS_ERR_UNSUPPORTED, "the velocity Jacobian checkpoint needs FP64 sums");
   const int q = tc.q, d = q + 1;
   const int64_t np = (int64_t)d * d * d, nc = (int64_t)d * (d + 1) * (d + 2) / 6;
   double* mu = nullptr;
@@ -121,6 +151,7 @@ int semilag_adjoint(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
   a.grad_vel = grad_vel_dev;
   a.wnode = wnode_acc;
   a.wnode_add = wnode_acc ? 1 : 0;
+  a.jac = jac_dev;
   const bool df = ctx_sums(ctx) == TBSLAS_SUMS_DOUBLE_FLOAT;
   if (!wnode_acc) {
     st = ctx_wnode_scratch(ctx, tc.L * np * 3, &a.wnode);
@@ -192,6 +223,20 @@ extern "C" int tbslas_semilag_adjoint_seq(tbslas_ctx ctx, tbslas_tree vel, tbsla
   return semilag_adjoint(ctx, vel, con, con_coeff_k_dev, timestep, dt, bc, lambda_next_dev,
                          lambda_k_dev, grad_vel_dev, xmid_dev, xdep_dev, vel_at_nodes_dev,
                          node_weights_dev, (cudaStream_t)stream);
+}
+
+extern "C" int tbslas_semilag_adjoint_jac(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,
+                                          const double* con_coeff_k_dev, int timestep, double dt,
+                                          int bc, const double* lambda_next_dev,
+                                          double* lambda_k_dev, double* grad_vel_dev,
+                                          const double* xmid_dev, const double* xdep_dev,
+                                          const double* jac_dev, double* node_weights_dev,
+                                          void* stream) {
+  DeviceRestore restore;
+  if (!jac_dev) return fail_status(TBSLAS_ERR_INVALID_ARG, "null Jacobian checkpoint");
+  return semilag_adjoint(ctx, vel, con, con_coeff_k_dev, timestep, dt, bc, lambda_next_dev,
+                         lambda_k_dev, grad_vel_dev, xmid_dev, xdep_dev, nullptr,
+                         node_weights_dev, (cudaStream_t)stream, jac_dev);
 }
 
 extern "C" int tbslas_semilag_adjoint_node_term(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con,

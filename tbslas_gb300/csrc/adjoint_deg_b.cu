@@ -2,9 +2,9 @@
 #include "adjoint_df.cuh"
 
 namespace tbg {
-void register_adjoint_b(AdjFn* a, AdjDfFn* d) {
-  register_adjoint_degree<7>(a, d);  // q = 6
-  register_adjoint_degree<8>(a, d);  // q = 7
-  register_adjoint_degree<9>(a, d);  // q = 8
+void register_adjoint_b(AdjFn* a, AdjDfFn* d, JacStepFn* j) {
+  register_adjoint_degree<7>(a, d, j);  // q = 6
+  register_adjoint_degree<8>(a, d, j);  // q = 7
+  register_adjoint_degree<9>(a, d, j);  // q = 8
 }
 }  // namespace tbg

@@ -2,8 +2,8 @@
 #include "adjoint_df.cuh"
 
 namespace tbg {
-void register_adjoint_c(AdjFn* a, AdjDfFn* d) {
-  register_adjoint_degree<10>(a, d);  // q = 9
-  register_adjoint_degree<11>(a, d);  // q = 10
+void register_adjoint_c(AdjFn* a, AdjDfFn* d, JacStepFn* j) {
+  register_adjoint_degree<10>(a, d, j);  // q = 9
+  register_adjoint_degree<11>(a, d, j);  // q = 10
 }
 }  // namespace tbg

@@ -385,9 +385,10 @@ void launch_adjoint_df(const AdjArgs& a, const float2* con2, cudaStream_t s) {
 }
 
 template <int D>
-void register_adjoint_degree(AdjFn* a, AdjDfFn* d) {
+void register_adjoint_degree(AdjFn* a, AdjDfFn* d, JacStepFn* j) {
   a[D - 1] = &launch_adjoint_f64<D>;
   d[D - 1] = &launch_adjoint_df<D>;
+  j[D - 1] = &launch_semilag_tree_jac<D>;
 }
 
 }  // namespace tbg

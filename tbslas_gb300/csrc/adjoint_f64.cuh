@@ -203,8 +203,10 @@ __device__ __forceinline__ void scatter_f64(AdjF64Shared<D>& sm, double* __restr
 
 // One thread per target node, its X* and Xd from a.xmid / a.xdep (required)
 // and the node term's weights to a.wnode (required).  Two CTAs per SM up to
-// q = 9 (shared memory: 72 doubles per target at q = 8).
-template <int D>
+// q = 9 (shared memory: 72 doubles per target at q = 8).  JAC: J_v(X*) from
+// the forward's checkpoint a.jac, so J_v(X*)^T g is nine multiply-adds
+// instead of 5 Nc.
+template <int D, bool JAC>
 __global__ void __launch_bounds__(kAdjF64Threads, (D <= 10 ? 2 : 1))
     k_adjoint_f64(const AdjArgs a) {
   constexpr int NP = D * D * D;
@@ -245,7 +247,24 @@ __global__ void __launch_bounds__(kAdjF64Threads, (D <= 10 ? 2 : 1))
   }
   // tau g (x) phi(X*) and J_v(X*)^T g = grad(g . v)(X*)
   double jtg[3] = {0.0, 0.0, 0.0};
-  {
+  if (JAC) {
+    Geom g;
+    int64_t lf = locate<D>(a.vel, xs, ys, zs, per, g);
+    if (!active) lf = -1;
+    double tx[D], ty[D], tz[D];
+    if (lf >= 0) {
+      cheb_T<D>((xs - g.x) * g.w - 1.0, tx);
+      cheb_T<D>((ys - g.y) * g.w - 1.0, ty);
+      cheb_T<D>((zs - g.z) * g.w - 1.0, tz);
+      const double* Jp = a.jac + 9 * tt;
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+        jtg[b] = fma(gvec[2], __ldg(Jp + 6 + b),
+                     fma(gvec[1], __ldg(Jp + 3 + b), gvec[0] * __ldg(Jp + b)));
+    }
+    const double w[3] = {a.tau * gvec[0], a.tau * gvec[1], a.tau * gvec[2]};
+    scatter_f64<D, 3, PER>(sm, a.grad_vel, 3 * NC, lf, tx, ty, tz, w, ozy, ox);
+  } else {
     Geom g;
     int64_t lf = locate<D>(a.vel, xs, ys, zs, per, g);
     if (!active) lf = -1;
@@ -287,13 +306,99 @@ void launch_adjoint_f64(const AdjArgs& a, cudaStream_t s) {
   const size_t smem = sizeof(AdjF64Shared<D>);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_adjoint_f64<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_adjoint_f64<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    cudaFuncSetAttribute(k_adjoint_f64<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     attr = true;
   }
-  if (n > 0)
-    k_adjoint_f64<D><<<(unsigned)((n + kAdjF64Threads - 1) / kAdjF64Threads), kAdjF64Threads,
-                       smem, s>>>(a);
+  if (n <= 0) return;
+  const unsigned grid = (unsigned)((n + kAdjF64Threads - 1) / kAdjF64Threads);
+  if (a.jac)
+    k_adjoint_f64<D, true><<<grid, kAdjF64Threads, smem, s>>>(a);
+  else
+    k_adjoint_f64<D, false><<<grid, kAdjF64Threads, smem, s>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// The checkpointed forward step with the velocity Jacobian: v and its
+// gradient at a point of a dof-3 tree (wrapped in place under periodic
+// boundaries, as eval_point), v bit-identical to eval_point<D, 3>, J[3a+b] =
+// dv_a/dx_b; all zero outside the domain.
+template <int D>
+__device__ __forceinline__ void eval_point_jac(const TreeView& t, double& x, double& y,
+                                               double& z, bool per, double (&v)[3],
+                                               double (&J)[9]) {
+  constexpr int NC = D * (D + 1) * (D + 2) / 6;
+  Geom g;
+  const int64_t lf = locate<D>(t, x, y, z, per, g);
+  if (lf < 0) {
+#pragma unroll
+    for (int l = 0; l < 3; ++l) v[l] = 0.0;
+#pragma unroll
+    for (int l = 0; l < 9; ++l) J[l] = 0.0;
+    return;
+  }
+  double tx[D], ty[D], tz[D], dx[D], dy[D], dz[D];
+  cheb_TdT<D>((x - g.x) * g.w - 1.0, tx, dx);
+  cheb_TdT<D>((y - g.y) * g.w - 1.0, ty, dy);
+  cheb_TdT<D>((z - g.z) * g.w - 1.0, tz, dz);
+  const double* c = t.coeff + lf * t.stride;
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    double gr[3];
+    tri_grad_val<D>(OneDof{c + l * NC}, tx, ty, tz, dx, dy, dz, gr, v[l]);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) J[3 * l + b] = gr[b] * g.w;
+  }
+}
+
+// k_semilag_tree<D> with the first stage from the node grid (a.vn), nrk = 1,
+// storing X* (a.xmid), Xd (a.xdep) and J_v(X*) (a.jac) of every target:
+// the same points and node values, bit for bit (the midpoint velocity by
+// tri_grad_val, whose value sums are tri_sum's).
+template <int D>
+__global__ void __launch_bounds__(128) k_semilag_tree_jac(const SemilagTreeArgs a) {
+  constexpr int NP = D * D * D;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= a.con.L * NP) return;
+  const int64_t leaf = t / NP;
+  const int p = (int)(t - leaf * NP);
+  const Geom g = load_geom(a.con.geom + leaf);
+  const double h = leaf_side(g);
+  double x = g.x + h * a.nodes.x[p % D];
+  double y = g.y + h * a.nodes.x[(p / D) % D];
+  double z = g.z + h * a.nodes.x[p / (D * D)];
+  const bool per = a.periodic != 0;
+  if (per) {
+    x = wrap1(x);
+    y = wrap1(y);
+    z = wrap1(z);
+  }
+  const double half_tau = 0.5 * a.tau;
+  const double* vn = a.vn + 3 * t;
+  double px = fma(half_tau, __ldg(vn + 0), x);
+  double py = fma(half_tau, __ldg(vn + 1), y);
+  double pz = fma(half_tau, __ldg(vn + 2), z);
+  store_point(a.xmid, t, px, py, pz);
+  double v[3], J[9];
+  eval_point_jac<D>(a.vel, px, py, pz, per, v, J);
+  x = fma(a.tau, v[0], x);
+  y = fma(a.tau, v[1], y);
+  z = fma(a.tau, v[2], z);
+  store_point(a.xdep, t, x, y, z);
+  double* Jo = a.jac + 9 * t;
+#pragma unroll
+  for (int l = 0; l < 9; ++l) Jo[l] = J[l];
+  double c[1];
+  eval_point<D, 1>(a.con, x, y, z, per, c);
+  a.vals[t] = c[0];
+}
+
+template <int D>
+void launch_semilag_tree_jac(const SemilagTreeArgs& a, cudaStream_t s) {
+  const int64_t n = a.con.L * D * D * D;
+  if (n > 0) k_semilag_tree_jac<D><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
 }
 
 }  // namespace tbg

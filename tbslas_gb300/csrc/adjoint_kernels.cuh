@@ -34,6 +34,8 @@ struct AdjArgs {
                        // the node-grid scatter (launch_scatter_on_nodes)
   int wnode_add = 0;   // 1: the weights are added to wnode (a sequence of steps
                        // through one velocity sums them and scatters once)
+  const double* jac = nullptr;  // [Lc * Np][9] the forward's J_v(X*) (row-major
+                                // dv_a/dx_b), or null: formed here from vel
 };
 
 // T_k and dT_k/dxi for k < D; zero outside [-1,1] like cheb_T.
@@ -47,7 +49,7 @@ __device__ __forceinline__ void cheb_TdT(double xi, double (&T)[D], double (&dT)
     T[1] = x;
     dT[1] = ok ? 1.0 : 0.0;
   }
-  const double x2 = 2.0 * x;
+  const double x2 = twice(x);
 #pragma unroll
   for (int k = 2; k < D; ++k) {
     T[k] = fma(x2, T[k - 1], -T[k - 2]);
@@ -71,37 +73,70 @@ struct Weighted3 {
 };
 
 // Gradient (d/dxi) of the triangular expansion with coefficients c(idx).
+// Each sum starts from +0.0 and adds its terms by fused multiply-adds; the
+// first terms (T_0 = 1 or 0, dT_0 = 0, from cheb_TdT) are formed by fma_t0
+// with the same bits.
+// val receives the expansion's value, bit-identical to tri_sum's (the same
+// sums in the same order).
 template <int D, class Load>
-__device__ __forceinline__ void tri_grad(Load c, const double (&tx)[D],
-                                         const double (&ty)[D], const double (&tz)[D],
-                                         const double (&dx)[D], const double (&dy)[D],
-                                         const double (&dz)[D], double (&g)[3]) {
-  double gx = 0.0, gy = 0.0, gz = 0.0;
+__device__ __forceinline__ void tri_grad_val(Load c, const double (&tx)[D],
+                                             const double (&ty)[D], const double (&tz)[D],
+                                             const double (&dx)[D], const double (&dy)[D],
+                                             const double (&dz)[D], double (&g)[3],
+                                             double& val) {
+  double gx = 0.0, gy = 0.0, gz = 0.0, u = 0.0;
   int idx = 0;
 #pragma unroll
   for (int i = 0; i < D; ++i) {
     double vx = 0.0, vy = 0.0, vz = 0.0;
 #pragma unroll
     for (int j = 0; j < D - i; ++j) {
-      double w = 0.0, wd = 0.0;
+      const double c0 = c(idx);
+      double w = fma_t0(tx[0], c0), wd = fma_t0(dx[0], c0);
+      ++idx;
 #pragma unroll
-      for (int k = 0; k < D - i - j; ++k) {
+      for (int k = 1; k < D - i - j; ++k) {
         const double ck = c(idx);
         w = fma(ck, tx[k], w);
         wd = fma(ck, dx[k], wd);
         ++idx;
       }
-      vx = fma(ty[j], wd, vx);
-      vy = fma(dy[j], w, vy);
-      vz = fma(ty[j], w, vz);
+      if (j == 0) {
+        vx = fma_t0(ty[0], wd);
+        vy = fma_t0(dy[0], w);
+        vz = fma_t0(ty[0], w);
+      } else {
+        vx = fma(ty[j], wd, vx);
+        vy = fma(dy[j], w, vy);
+        vz = fma(ty[j], w, vz);
+      }
     }
-    gx = fma(tz[i], vx, gx);
-    gy = fma(tz[i], vy, gy);
-    gz = fma(dz[i], vz, gz);
+    if (i == 0) {
+      gx = fma_t0(tz[0], vx);
+      gy = fma_t0(tz[0], vy);
+      gz = fma_t0(dz[0], vz);
+      u = fma_t0(tz[0], vz);
+    } else {
+      gx = fma(tz[i], vx, gx);
+      gy = fma(tz[i], vy, gy);
+      gz = fma(dz[i], vz, gz);
+      u = fma(tz[i], vz, u);
+    }
   }
   g[0] = gx;
   g[1] = gy;
   g[2] = gz;
+  val = u;
+}
+
+// Gradient only (the value's sums are dropped by the compiler).
+template <int D, class Load>
+__device__ __forceinline__ void tri_grad(Load c, const double (&tx)[D],
+                                         const double (&ty)[D], const double (&tz)[D],
+                                         const double (&dx)[D], const double (&dy)[D],
+                                         const double (&dz)[D], double (&g)[3]) {
+  double val;
+  tri_grad_val<D>(c, tx, ty, tz, dx, dy, dz, g, val);
 }
 
 // Locate a point (wrapping it in place under periodic boundaries): leaf index
@@ -122,8 +157,9 @@ __device__ __forceinline__ int64_t locate(const TreeView& t, double& x, double& 
 
 typedef void (*AdjFn)(const AdjArgs&, cudaStream_t);
 typedef void (*AdjDfFn)(const AdjArgs&, const float2*, cudaStream_t);
-void register_adjoint_a(AdjFn* a, AdjDfFn* d);
-void register_adjoint_b(AdjFn* a, AdjDfFn* d);
-void register_adjoint_c(AdjFn* a, AdjDfFn* d);
+typedef void (*JacStepFn)(const SemilagTreeArgs&, cudaStream_t);
+void register_adjoint_a(AdjFn* a, AdjDfFn* d, JacStepFn* j);
+void register_adjoint_b(AdjFn* a, AdjDfFn* d, JacStepFn* j);
+void register_adjoint_c(AdjFn* a, AdjDfFn* d, JacStepFn* j);
 
 }  // namespace tbg

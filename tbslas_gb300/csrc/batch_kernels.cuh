@@ -67,7 +67,7 @@ __device__ __forceinline__ void batch_target_df(const BatchProblem& p, int64_t t
   const int64_t leaf = t / NP;
   const int pi = (int)(t - leaf * NP);
   const Geom g = load_geom(p.con.geom + leaf);
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   double x = g.x + h * p.nodes.x[pi % D];
   double y = g.y + h * p.nodes.x[(pi / D) % D];
   double z = g.z + h * p.nodes.x[pi / (D * D)];
@@ -116,7 +116,7 @@ __device__ __forceinline__ void batch_target(const BatchProblem& p, int64_t t, d
   const int64_t leaf = t / NP;
   const int pi = (int)(t - leaf * NP);
   const Geom g = load_geom(p.con.geom + leaf);
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   double x = g.x + h * p.nodes.x[pi % D];
   double y = g.y + h * p.nodes.x[(pi / D) % D];
   double z = g.z + h * p.nodes.x[pi / (D * D)];

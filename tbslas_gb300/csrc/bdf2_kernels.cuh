@@ -28,7 +28,7 @@ __device__ __forceinline__ double bdf2_target_fp64(const Bdf2Args& a, int64_t t)
   const int64_t leaf = t / NP;
   const int p = (int)(t - leaf * NP);
   const Geom g = load_geom(a.next.geom + leaf);
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   double x = g.x + h * a.nodes.x[p % D];
   double y = g.y + h * a.nodes.x[(p / D) % D];
   double z = g.z + h * a.nodes.x[p / (D * D)];
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_bdf2_df(cons
   const int64_t leaf = t / NP;
   const int p = (int)(t - leaf * NP);
   const Geom g = load_geom(a.next.geom + leaf);
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   double x[3] = {g.x + h * a.nodes.x[p % D], g.y + h * a.nodes.x[(p / D) % D],
                  g.z + h * a.nodes.x[p / (D * D)]};
   const bool per = a.periodic != 0;

@@ -351,7 +351,7 @@ __global__ void k_collect(const TreeView t, const Nodes1D nodes, int d, double* 
   const int64_t leaf = i / np;
   const int p = (int)(i - leaf * np);
   const Geom g = load_geom(t.geom + leaf);
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   out[3 * i + 0] = g.x + h * nodes.x[p % d];
   out[3 * i + 1] = g.y + h * nodes.x[(p / d) % d];
   out[3 * i + 2] = g.z + h * nodes.x[p / (d * d)];
@@ -472,9 +472,13 @@ __global__ void k_point_to_dof_major(const double* __restrict__ in, int64_t L, i
 
 // FMA throughput probe (T = double: FP64 pipe, T = float: FP32 pipe): 8
 // independent dependency chains per thread, 64 FMAs per iteration; one store
-// per thread.
+// per thread.  The shared multiplier and addend sit in registers (b + 0 with
+// a run-time 0): taken from the constant bank, as kernel arguments, they
+// held the FP64 FMA rate at 1.6 per clock per SM instead of 1.9.
 template <class T>
-__global__ void __launch_bounds__(256) k_fma_probe(T* out, T b, T c, int iters) {
+__global__ void __launch_bounds__(256) k_fma_probe(T* out, T b_arg, T c_arg, int iters) {
+  const T zero = T(iters < 0);
+  const T b = b_arg + zero, c = c_arg + zero;
   T a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5,
     a6 = a0 + 6, a7 = a0 + 7;
   for (int i = 0; i < iters; ++i) {
@@ -656,7 +660,8 @@ double interp_cubic_1d(double x, const double* xx, const double* pp) {
 // the first RK stage from v1 at the nodes, the others from v2 (one tree for
 // the plain step; two blends of a velocity set for the time-dependent one).
 int fused_step(tbslas_ctx ctx, const TreeView& v1, const TreeView& v2, tbslas_tree con,
-               double tau, int nrk, int bc, cudaStream_t s, double* xmid, double* xdep) {
+               double tau, int nrk, int bc, cudaStream_t s, double* xmid, double* xdep,
+               double* jac = nullptr) {
   const int64_t N = con->L * n_points(con->q);
   double* vals;
   TRY(scratch_t(ctx, kVals, N, &vals));
@@ -683,7 +688,13 @@ int fused_step(tbslas_ctx ctx, const TreeView& v1, const TreeView& v2, tbslas_tr
   TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
   TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
   a.fix_grid = ctx->num_sms * 8;
-  if (ctx->sums == TBSLAS_SUMS_FP64) {
+  if (jac) {
+    if (ctx->sums != TBSLAS_SUMS_FP64)
+      return fail(TBSLAS_ERR_UNSUPPORTED, "the velocity Jacobian checkpoint needs FP64 sums");
+    a.jac = jac;
+    ProfScope p(ctx, "semilag_tree_jac", s, 1);
+    TRY(launch_semilag_jac(con->q, a, s));
+  } else if (ctx->sums == TBSLAS_SUMS_FP64) {
     ProfScope p(ctx, "semilag_tree", s, 1);
     g_kernels[con->q].semilag(a, s);
   } else {
@@ -696,13 +707,13 @@ int fused_step(tbslas_ctx ctx, const TreeView& v1, const TreeView& v2, tbslas_tr
 
 int semilag_in_situ_dev(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,
                         int nrk, int bc, cudaStream_t s, double* xmid = nullptr,
-                        double* xdep = nullptr) {
+                        double* xdep = nullptr, double* jac = nullptr) {
   const double tau = sl_tau(timestep, dt, nrk);
   const int64_t np = n_points(con->q);
   const int64_t N = con->L * np;
   if (vel->q == con->q && con->dof == 1) {
     const TreeView v = vel->view();
-    return fused_step(ctx, v, v, con, tau, nrk, bc, s, xmid, xdep);
+    return fused_step(ctx, v, v, con, tau, nrk, bc, s, xmid, xdep, jac);
   }
   double* vals;
   TRY(scratch_t(ctx, kVals, N * con->dof, &vals));
@@ -1265,9 +1276,11 @@ int fma_peak(tbslas_ctx ctx, int iters, double* flops_per_s) {
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0));
   CUDA_TRY(cudaEventCreate(&e1));
-  k_fma_probe<T><<<blocks, threads, 0, ctx->stream>>>(o, T(1), T(0), 10);
+  // b < 1 and c > 0 keep the chains at normal values (a -> c / (1 - b))
+  const T b = T(0.999999), c = T(1e-9);
+  k_fma_probe<T><<<blocks, threads, 0, ctx->stream>>>(o, b, c, 10);
   cudaEventRecord(e0, ctx->stream);
-  k_fma_probe<T><<<blocks, threads, 0, ctx->stream>>>(o, T(1), T(0), iters);
+  k_fma_probe<T><<<blocks, threads, 0, ctx->stream>>>(o, b, c, iters);
   cudaEventRecord(e1, ctx->stream);
   CUDA_TRY(cudaEventSynchronize(e1));
   float ms = 0.f;
@@ -2039,13 +2052,15 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
 // For the adjoint's checkpointed forward (adjoint.cu).
 namespace tbg {
 int semilag_in_situ_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
-                           double dt, int bc, double* xmid, double* xdep, cudaStream_t s) {
+                           double dt, int bc, double* xmid, double* xdep, cudaStream_t s,
+                           double* jac) {
   TRY(check_step_args(ctx, vel, con, dt, 1, bc));
   if (vel->q != con->q || vel->dof != 3 || con->dof != 1)
     return fail(TBSLAS_ERR_UNSUPPORTED, "points of the step need a dof-3 velocity and a dof-1 "
                                         "concentration tree of one degree");
   if (!xdep) return fail(TBSLAS_ERR_INVALID_ARG, "null departure-point buffer");
-  return semilag_in_situ_dev(ctx, vel, con, timestep, dt, 1, bc, s, xmid, xdep);
+  if (jac && !xmid) return fail(TBSLAS_ERR_INVALID_ARG, "the Jacobian checkpoint needs xmid");
+  return semilag_in_situ_dev(ctx, vel, con, timestep, dt, 1, bc, s, xmid, xdep, jac);
 }
 
 int step_midpoints(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, double dt,

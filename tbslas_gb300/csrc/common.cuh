@@ -65,6 +65,15 @@ __device__ __forceinline__ bool in_unit_open(double c) {
 // |c| <= 1 (NaN false).
 __device__ __forceinline__ bool abs_at_most_one(double c) { return (dbits(c) & kBitsAbs) <= kBitsOne; }
 
+// 2x for |x| <= 1 (the Chebyshev recurrence's multiplier), exact: the
+// exponent raised by one, or the mantissa shifted for zero and subnormals.
+__device__ __forceinline__ double twice(double x) {
+  const uint64_t b = dbits(x);
+  return __longlong_as_double((long long)((b & 0x7FF0000000000000ull)
+                                              ? b + (1ull << 52)
+                                              : (b & kBitsNegZero) | ((b & kBitsAbs) << 1)));
+}
+
 // Single periodic wrap of one coordinate, src/tree/tree_functor.h:442-448.
 __device__ __forceinline__ double wrap1(double c) {
   if (below_zero(c)) c = c + 1.0;
@@ -96,6 +105,11 @@ __device__ __forceinline__ bool inside(double x, double y, double z, bool period
 struct __align__(32) Geom {
   double x, y, z, w;
 };
+// 2 / w = 2^-depth, the leaf's side: exact, formed from the exponent of
+// w = 2^(depth+1) (an FP64 division is a sequence of FP64 instructions).
+__device__ __forceinline__ double leaf_side(const Geom& g) {
+  return __longlong_as_double((long long)((2047ull - (dbits(g.w) >> 52)) << 52));
+}
 __device__ __forceinline__ Geom load_geom(const Geom* p) {
   const double2 a = __ldg(reinterpret_cast<const double2*>(p));
   const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
@@ -140,16 +154,30 @@ __device__ __forceinline__ void cheb_T(double xi, double (&T)[D]) {
   const double x = ok ? xi : 0.0;
   T[0] = ok ? 1.0 : 0.0;
   if (D > 1) T[1] = x;
-  const double x2 = 2.0 * x;
+  const double x2 = twice(x);
 #pragma unroll
   for (int k = 2; k < D; ++k) T[k] = fma(x2, T[k - 1], -T[k - 2]);
+}
+
+// fma(t0, x, +0.0) for t0 = T_0 as cheb_T forms it (1.0 inside [-1, 1],
+// +0.0 outside), on the integer pipe: x with -0.0 read as +0.0 when t0 = 1;
+// +0.0 (NaN for a non-finite x) when t0 = 0 -- the FP64 fma's bits in both
+// cases.  The first term of every row of a Chebyshev sum is this product, so
+// a row costs one FP64 instruction less.
+__device__ __forceinline__ double fma_t0(double t0, double x) {
+  const uint64_t b = dbits(x);
+  if (dbits(t0) != 0) return __longlong_as_double((long long)(b == kBitsNegZero ? 0ull : b));
+  return __longlong_as_double(
+      (long long)((b & kBitsAbs) < 0x7FF0000000000000ull ? 0ull : 0x7FF8000000000000ull));
 }
 
 // Triangular tensor Chebyshev sum of one dof:
 //   sum_i tz_i sum_{j<D-i} ty_j sum_{k<D-i-j} c[i][j][k] tx_k
 // with the reference's summation order (pvfmm::vec_eval,
-// src/tree/tree_functor.h:38-77).  Fully unrolled; c is read with
-// compile-time offsets.
+// src/tree/tree_functor.h:38-77): each sum starts from +0.0 and adds its
+// terms in increasing index by fused multiply-adds.  The first term of each
+// sum (T_0 = 1) is formed by fma_t0 with the same bits.  tx/ty/tz as cheb_T
+// forms them.  Fully unrolled; c is read with compile-time offsets.
 template <int D, class Load>
 __device__ __forceinline__ double tri_sum(Load c, const double (&tx)[D], const double (&ty)[D],
                                           const double (&tz)[D]) {
@@ -160,15 +188,16 @@ __device__ __forceinline__ double tri_sum(Load c, const double (&tx)[D], const d
     double v = 0.0;
 #pragma unroll
     for (int j = 0; j < D - i; ++j) {
-      double w = 0.0;
+      double w = fma_t0(tx[0], c(idx));
+      ++idx;
 #pragma unroll
-      for (int k = 0; k < D - i - j; ++k) {
+      for (int k = 1; k < D - i - j; ++k) {
         w = fma(c(idx), tx[k], w);
         ++idx;
       }
-      v = fma(ty[j], w, v);
+      v = j == 0 ? fma_t0(ty[0], w) : fma(ty[j], w, v);
     }
-    u = fma(tz[i], v, u);
+    u = i == 0 ? fma_t0(tz[0], v) : fma(tz[i], v, u);
   }
   return u;
 }

@@ -86,7 +86,7 @@ __global__ void k_field_values(int kind, int n, const double* __restrict__ prm,
   const int64_t leaf = t / NP;
   const int pnode = (int)(t - leaf * NP);
   const Geom g = geom[leaf];
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   const double x = g.x + h * nodes.x[pnode % D];
   const double y = g.y + h * nodes.x[(pnode / D) % D];
   const double z = g.z + h * nodes.x[pnode / (D * D)];
@@ -121,7 +121,7 @@ __global__ void k_midpoints(const TreeView con, const Nodes1D nodes, int D, doub
   const int64_t leaf = t / NP;
   const int p = (int)(t - leaf * NP);
   const Geom g = con.geom[leaf];
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   double X[3] = {g.x + h * nodes.x[p % D], g.y + h * nodes.x[(p / D) % D],
                  g.z + h * nodes.x[p / (D * D)]};
   const double half_tau = 0.5 * tau;

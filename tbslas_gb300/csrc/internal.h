@@ -54,6 +54,10 @@ struct SemilagTreeArgs {
   // targets the FP64 pass recomputes), or null
   double* xmid = nullptr;
   double* xdep = nullptr;
+  // with xmid/xdep (FP64 sums): the velocity Jacobian at every midpoint,
+  // [Lc * Np][9] row-major dv_a/dx_b (the checkpoint of the adjoint's
+  // velocity-gradient term), or null
+  double* jac = nullptr;
 };
 
 struct TrajArgs {
@@ -193,9 +197,14 @@ int ctx_vals_scratch(tbslas_ctx ctx, size_t n, double** out);
 Nodes1D ctx_nodes(int q);
 // The in-situ step (nrk = 1, fused path: dof-3 velocity and dof-1
 // concentration of one degree) writing every target's RK2 midpoint and
-// departure point to xmid / xdep ([Lc * Np][3]).
+// departure point to xmid / xdep ([Lc * Np][3]) and, when jac is given (FP64
+// sums only), the velocity Jacobian at the midpoint ([Lc * Np][9]).
 int semilag_in_situ_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep,
-                           double dt, int bc, double* xmid, double* xdep, cudaStream_t s);
+                           double dt, int bc, double* xmid, double* xdep, cudaStream_t s,
+                           double* jac = nullptr);
+// The fused step kernel that also stores J_v(X*) (adjoint_f64.cuh), for
+// degree q (1..10); TBSLAS_ERR_UNSUPPORTED beyond.
+int launch_semilag_jac(int q, const SemilagTreeArgs& a, cudaStream_t s);
 // Profiling bracket for launch groups of other translation units (the
 // context's per-name CUDA-event timing; nothing when profiling is off).
 class ProfBracket {

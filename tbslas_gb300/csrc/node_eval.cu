@@ -103,7 +103,7 @@ __device__ __forceinline__ int64_t face_source(const TreeView& dst, const Nodes1
   const int Dd = dst.q + 1;
   if (a != Dd - 1 && b != Dd - 1 && c != Dd - 1) return -1;
   if (nodes.x[0] != 0.0 || nodes.x[Dd - 1] != 1.0) return -1;
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   double x = g.x + h * nodes.x[a], y = g.y + h * nodes.x[b], z = g.z + h * nodes.x[c];
   if (per) {
     x = wrap1(x);
@@ -162,7 +162,7 @@ __device__ __forceinline__ void for_each_subgrid(const TreeView& S, const TreeVi
   uint8_t* sdone = reinterpret_cast<uint8_t*>(sidx + 3 * Dd);   // [Dd^3]
 
   const Geom g = load_geom(dst.geom + leaf);
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   if (tid < 3 * Dd) {
     const int ax = tid / Dd, i = tid - ax * Dd;
     const double o = ax == 0 ? g.x : (ax == 1 ? g.y : g.z);

@@ -15,7 +15,7 @@ __device__ __forceinline__ void cheb_T_col(double xi, double* T, int stride) {
   const double t0 = ok ? 1.0 : 0.0;
   T[0] = t0;
   if (Ds > 1) T[stride] = x;
-  const double x2 = 2.0 * x;
+  const double x2 = twice(x);
   double a = t0, b = x;
 #pragma unroll
   for (int k = 2; k < Ds; ++k) {
@@ -40,8 +40,8 @@ struct SubGrid {
 //   w(l; i,j,a') = sum_k c[l][i][j][k] T_k(x_a')
 //   v(i)         = sum_j T_j(y_b') w(l; i,j,a')        (per column l, b', a')
 //   u(c')        = sum_i T_i(z_c') v(i)
-// -- tri_sum's nested sums with its fma order, so each value is
-// bit-identical to eval_point.  Node p = a + Dd (b + Dd c) of component l
+// -- tri_sum's nested sums with its fma order (the T_0 terms by fma_t0), so
+// each value is bit-identical to eval_point.  Node p = a + Dd (b + Dd c) of component l
 // goes to out[p * pstride + l * lstride].  sw: dof * Ds (Ds + 1) / 2 * Dd
 // doubles of shared memory.  All threads of the block call it; it contains a
 // barrier between the first two passes.
@@ -66,8 +66,8 @@ __device__ __forceinline__ void eval_subgrid(const TreeView& S, const SubGrid& s
     const int j = rem, m = Ds - i;
     const double* c =
         cV + l * NCs + (NCs - m * (m + 1) * (m + 2) / 6 + j * m - (j * (j - 1)) / 2);
-    double w = 0.0;
-    for (int k = 0; k < m - j; ++k) w = fma(__ldg(c + k), sg.Tx[k * Dd + ai], w);
+    double w = fma_t0(sg.Tx[ai], __ldg(c));  // T_0 term, as tri_sum
+    for (int k = 1; k < m - j; ++k) w = fma(__ldg(c + k), sg.Tx[k * Dd + ai], w);
     sw[(l * npair + pr) * Dd + ai] = w;
   }
   __syncthreads();
@@ -78,17 +78,17 @@ __device__ __forceinline__ void eval_subgrid(const TreeView& S, const SubGrid& s
     int prow = 0;
 #pragma unroll
     for (int i = 0; i < Ds; ++i) {
-      double s = 0.0;
+      double s = fma_t0(sg.Ty[bi], wl[prow * Dd]);
 #pragma unroll
-      for (int j = 0; j < Ds - i; ++j) s = fma(sg.Ty[j * Dd + bi], wl[(prow + j) * Dd], s);
+      for (int j = 1; j < Ds - i; ++j) s = fma(sg.Ty[j * Dd + bi], wl[(prow + j) * Dd], s);
       v[i] = s;
       prow += Ds - i;
     }
     const int pab = sidx[ai] + Dd * sidx[Dd + bi];
     for (int ci = 0; ci < nz; ++ci) {
-      double u = 0.0;
+      double u = fma_t0(sg.Tz[ci], v[0]);
 #pragma unroll
-      for (int i = 0; i < Ds; ++i) u = fma(sg.Tz[i * Dd + ci], v[i], u);
+      for (int i = 1; i < Ds; ++i) u = fma(sg.Tz[i * Dd + ci], v[i], u);
       out[(int64_t)(pab + Dd2 * sidx[2 * Dd + ci]) * pstride + l * lstride] = u;
     }
   }

@@ -234,7 +234,7 @@ __global__ void k_balance_flags(const TreeView t, int periodic, int8_t* __restri
   if (i >= t.L) return;
   const Geom g = t.geom[i];
   const int d = leaf_depth(g);
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   const double cx = g.x + 0.5 * h, cy = g.y + 0.5 * h, cz = g.z + 0.5 * h;
   const double r = 0.5 * h + 0x1p-22;
   bool split = false;

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(128) k_semilag_tree(const SemilagTreeArgs a) {
   const int64_t leaf = t / NP;
   const int p = (int)(t - leaf * NP);
   const Geom g = load_geom(a.con.geom + leaf);
-  const double h = 2.0 / g.w;  // 2^-depth, exact
+  const double h = leaf_side(g);  // 2^-depth, exact
   double x = g.x + h * a.nodes.x[p % D];
   double y = g.y + h * a.nodes.x[(p / D) % D];
   double z = g.z + h * a.nodes.x[p / (D * D)];
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(cons
   const int64_t leaf = t / NP;
   const int p = (int)(t - leaf * NP);
   const Geom g = load_geom(a.con.geom + leaf);
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   double x[3] = {g.x + h * a.nodes.x[p % D], g.y + h * a.nodes.x[(p / D) % D],
                  g.z + h * a.nodes.x[p / (D * D)]};
   const bool per = a.periodic != 0;
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(128) k_semilag_fix(const SemilagTreeArgs a) {
     const int64_t leaf = t / NP;
     const int p = (int)(t - leaf * NP);
     const Geom g = load_geom(a.con.geom + leaf);
-    const double h = 2.0 / g.w;
+    const double h = leaf_side(g);
     double x = g.x + h * a.nodes.x[p % D];
     double y = g.y + h * a.nodes.x[(p / D) % D];
     double z = g.z + h * a.nodes.x[p / (D * D)];

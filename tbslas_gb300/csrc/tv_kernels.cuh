@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(128) k_semilag_tv(const TvArgs a) {
   const int64_t leaf = t / NP;
   const int p = (int)(t - leaf * NP);
   const Geom g = load_geom(a.con.geom + leaf);
-  const double h = 2.0 / g.w;
+  const double h = leaf_side(g);
   double x = g.x + h * a.nodes.x[p % D];
   double y = g.y + h * a.nodes.x[(p / D) % D];
   double z = g.z + h * a.nodes.x[p / (D * D)];

@@ -75,7 +75,7 @@ def _J(c, V, cobs):
     return 0.5 * ((vals - ovals) ** 2).sum()
 
 
-@pytest.mark.parametrize("checkpoint", [True, False])
+@pytest.mark.parametrize("checkpoint", [True, False, "jacobian"])
 def test_adjoint_matches_central_differences(ctx, checkpoint):
     """Central differences, eps = 1e-6, along seeded random directions: N(0,1)
     coefficients for c0 (J is quadratic in c0), smooth random velocity fields
@@ -122,7 +122,7 @@ def test_adjoint_checkpoint_equals_recompute(ctx):
     V = torch.from_numpy(adjoint.basis_at_nodes(q)).cuda()
     co = torch.from_numpy(cobs).cuda()
     grads = []
-    for ck in (True, "departure", False):
+    for ck in (True, "departure", False, "jacobian"):
         c0t = torch.from_numpy(c0).cuda().requires_grad_(True)
         vct = torch.from_numpy(vc).cuda().requires_grad_(True)
         _J(adjoint.advect(c0t, vct, tv, tc, 0.02, 1, 4, tb.Periodic, ck), V, co).backward()
@@ -133,6 +133,62 @@ def test_adjoint_checkpoint_equals_recompute(ctx):
         assert np.abs(x - y).max() <= 1e-14 * np.abs(y).max()
     for x, y in zip(grads[0], grads[2]):
         assert np.abs(x - y).max() <= 1e-12 * np.abs(y).max()
+    # the Jacobian checkpoint forms J_v(X*)^T g from the stored Jacobian
+    # (rounding of a different order than the coefficient-level sum)
+    for x, y in zip(grads[3], grads[0]):
+        assert np.abs(x - y).max() <= 1e-12 * np.abs(y).max()
+
+
+@pytest.mark.parametrize("bc", [tb.FreeSpace, tb.Periodic])
+def test_ckpt_jac_step_equals_ckpt_step_and_linear_jacobian(ctx, bc):
+    """The Jacobian checkpoint's forward is the checkpointed step bit for bit
+    (coefficients, midpoints, departure points).  On a linear velocity
+    (represented exactly by the fit) the stored Jacobian is its matrix at
+    every midpoint inside the domain, to the fit's rounding, and zero
+    outside."""
+    import torch
+    q, A = 5, np.array([[0.3, -1.1, 0.2], [0.9, -0.4, 0.5], [-0.2, 0.7, 0.1]])
+    a, d = trees.uniform_tree(2)
+    vc = trees.fit(lambda p: (p - 0.5) @ A.T + 0.05, a, d, q, 3)
+    c0 = trees.fit(fields.gaussian((0.5, 0.45, 0.55), 0.12), a, d, q, 1)
+    tv = tb.Tree(ctx, a, d, q, 3, vc)
+    tc = tb.Tree(ctx, a, d, q, 1, c0)
+    vf = tb.NodeFieldFunctor(tv, bc)
+    n = len(d) * (q + 1) ** 3
+    out = []
+    for jac in (False, True):
+        tc.set_coeffs(c0)
+        xm = torch.full((n, 3), np.nan, dtype=torch.float64, device="cuda")
+        xd = torch.full_like(xm, np.nan)
+        if jac:
+            J = torch.full((n, 9), np.nan, dtype=torch.float64, device="cuda")
+            adjoint.step_ckpt_jac(vf, tc, 1, 0.05, xm, xd, J)
+        else:
+            adjoint.step_ckpt(vf, tc, 1, 0.05, xm, xd)
+        out.append((tc.get_coeffs(), xm.cpu().numpy(), xd.cpu().numpy()))
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(x, y)
+    J = J.cpu().numpy().reshape(n, 3, 3)
+    xm = out[1][1]
+    inside = np.all((xm >= 0.0) & (xm <= 1.0), axis=1) if bc == tb.FreeSpace else np.ones(n, bool)
+    assert inside.any()
+    assert np.abs(J[inside] - A[None]).max() <= 1e-12
+    assert np.all(J[~inside] == 0.0)
+
+
+def test_ckpt_jac_needs_fp64_sums(ctx):
+    import torch
+    a, d, q, vc, c0, cobs, tv, tc = _problem(ctx, q=3)
+    vf = tb.NodeFieldFunctor(tv, tb.Periodic)
+    n = len(d) * (q + 1) ** 3
+    xm = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
+    J = torch.zeros((n, 9), dtype=torch.float64, device="cuda")
+    try:
+        ctx.sums = tb.SUMS_DOUBLE_FLOAT
+        with pytest.raises(tb.capi.TbslasError):
+            adjoint.step_ckpt_jac(vf, tc, 1, 0.05, xm, xm.clone(), J)
+    finally:
+        ctx.sums = tb.SUMS_FP64
 
 
 @pytest.mark.parametrize("vel_kind,q", [("fourier", 4), ("taylor_green", 4), ("fourier", 5),
