@@ -98,9 +98,9 @@ __device__ __forceinline__ void scatter_f64(AdjF64Shared<D>& sm, double* __restr
     int ij = 0;
 #pragma unroll
     for (int i = 0; i < D; ++i) {
-      const double zi = DOF == 1 ? w[0] * tz[i] : tz[i];
+      const double zi = DOF == 1 ? (i == 0 ? mul_t0(tz[0], w[0]) : w[0] * tz[i]) : tz[i];
 #pragma unroll
-      for (int j = 0; j < D - i; ++j, ++ij) col[ij * BS] = zi * ty[j];
+      for (int j = 0; j < D - i; ++j, ++ij) col[ij * BS] = j == 0 ? mul_t0(ty[0], zi) : zi * ty[j];
     }
 #pragma unroll
     if (DOF == 1 || !AdjF64Shared<D>::FOLD) {
@@ -114,7 +114,8 @@ __device__ __forceinline__ void scatter_f64(AdjF64Shared<D>& sm, double* __restr
 #pragma unroll
       for (int l = 0; l < DOF; ++l)
 #pragma unroll
-        for (int k = 0; k < D; ++k) col[(NIJ + l * D + k) * BS] = w[l] * tx[k];
+        for (int k = 0; k < D; ++k)
+          col[(NIJ + l * D + k) * BS] = k == 0 ? mul_t0(tx[0], w[l]) : w[l] * tx[k];
     }
   }
   const int my_leaf = lf >= 0 ? (int)lf : -1;

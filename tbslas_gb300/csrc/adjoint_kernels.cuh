@@ -74,8 +74,8 @@ struct Weighted3 {
 
 // Gradient (d/dxi) of the triangular expansion with coefficients c(idx).
 // Each sum starts from +0.0 and adds its terms by fused multiply-adds; the
-// first terms (T_0 = 1 or 0, dT_0 = 0, from cheb_TdT) are formed by fma_t0
-// with the same bits.
+// first terms (T_0 = 1 or 0, dT_0 = 0, dT_1 = 1 or 0, from cheb_TdT) are
+// formed by fma_t0 with the same bits.
 // val receives the expansion's value, bit-identical to tri_sum's (the same
 // sums in the same order).
 template <int D, class Load>
@@ -92,10 +92,18 @@ __device__ __forceinline__ void tri_grad_val(Load c, const double (&tx)[D],
 #pragma unroll
     for (int j = 0; j < D - i; ++j) {
       const double c0 = c(idx);
-      double w = fma_t0(tx[0], c0), wd = fma_t0(dx[0], c0);
+      double w = fma_t0(tx[0], c0), wd = fma_t0(dx[0], c0);  // wd: +0, or NaN
       ++idx;
+      if (D - i - j > 1) {
+        // k = 1: dT_1 is 1 (or 0 outside [-1, 1]) and wd is +0 or NaN, so
+        // fma(c1, dT_1, wd) is fma_t0's product unless wd is a NaN
+        const double c1 = c(idx);
+        w = fma(c1, tx[1], w);
+        wd = (dbits(wd) & kBitsAbs) > 0x7FF0000000000000ull ? wd : fma_t0(dx[1], c1);
+        ++idx;
+      }
 #pragma unroll
-      for (int k = 1; k < D - i - j; ++k) {
+      for (int k = 2; k < D - i - j; ++k) {
         const double ck = c(idx);
         w = fma(ck, tx[k], w);
         wd = fma(ck, dx[k], wd);

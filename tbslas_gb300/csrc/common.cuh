@@ -171,6 +171,17 @@ __device__ __forceinline__ double fma_t0(double t0, double x) {
       (long long)((b & kBitsAbs) < 0x7FF0000000000000ull ? 0ull : 0x7FF8000000000000ull));
 }
 
+// t0 * x for t0 in {0, 1} (T_0, dT_1 as cheb_T / cheb_TdT form them), on the
+// integer pipe: x when t0 = 1; +-0 with x's sign (NaN for a non-finite x)
+// when t0 = 0 -- the FP64 product's bits in both cases.
+__device__ __forceinline__ double mul_t0(double t0, double x) {
+  const uint64_t b = dbits(x);
+  if (dbits(t0) != 0) return x;
+  return __longlong_as_double(
+      (long long)((b & kBitsAbs) < 0x7FF0000000000000ull ? (b & kBitsNegZero)
+                                                          : 0x7FF8000000000000ull));
+}
+
 // Triangular tensor Chebyshev sum of one dof:
 //   sum_i tz_i sum_{j<D-i} ty_j sum_{k<D-i-j} c[i][j][k] tx_k
 // with the reference's summation order (pvfmm::vec_eval,

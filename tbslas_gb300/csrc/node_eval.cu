@@ -201,11 +201,12 @@ __device__ __forceinline__ void for_each_subgrid(const TreeView& S, const TreeVi
     const int64_t V = find_leaf(S, morton3(sq[p0 % Dd], sq[Dd + (p0 / Dd) % Dd],
                                            sq[2 * Dd + p0 / Dd2]));
     const Geom vg = load_geom(S.geom + V);
-    // the box of V in key units: anchor * 2^21, side 2^21 / 2^depth = 2^22 / w
-    const uint32_t side = (uint32_t)(4194304.0 / vg.w);
+    // the box of V in key units: anchor * 2^21, side 2^21 / 2^depth, from
+    // the exponent of w = 2^(depth+1) (no FP64 division)
+    const uint32_t side = 1u << (kKeyBits - ((int)(dbits(vg.w) >> 52) - 1024));
     if (tid < 3) {
       const double o = tid == 0 ? vg.x : (tid == 1 ? vg.y : vg.z);
-      const uint32_t lo = (uint32_t)(o * (double)kKeyScale);
+      const uint32_t lo = (uint32_t)quantise(o);  // anchors are exact multiples of 2^-21
       int n = 0;
       for (int i = 0; i < Dd; ++i) {
         const uint32_t k = sq[tid * Dd + i];

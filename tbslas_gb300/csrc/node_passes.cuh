@@ -56,8 +56,10 @@ __device__ __forceinline__ void eval_subgrid(const TreeView& S, const SubGrid& s
   const int na = sg.na, nb = sg.nb, nz = sg.nz;
   const int* sidx = sg.sidx;
   const double* cV = S.coeff + sg.V * S.stride;
+  // items (a', l, pair) with the pair slowest: the lanes of a warp share
+  // one row length (the k loop) instead of diverging over several
   for (int o = tid; o < dof * npair * na; o += bs) {
-    const int ai = o % na, r = o / na, pr = r % npair, l = r / npair;
+    const int ai = o % na, r = o / na, l = r % dof, pr = r / dof;
     int i = 0, rem = pr;  // pair index -> (i, j): rows of length Ds - i
     while (rem >= Ds - i) {
       rem -= Ds - i;
