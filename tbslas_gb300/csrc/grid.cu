@@ -83,6 +83,15 @@ __device__ __forceinline__ void lagrange4_unit(double t, double (&w)[4]) {
   w[3] = ((1.0 / 6.0 * t) * d1) * d2;
 }
 
+// ix * 2^-nl as a double, exactly (the node coordinate ix h of a periodic
+// grid of 2^nl nodes), formed from the integer's bits.
+__device__ __forceinline__ double grid_coord_pow2(int64_t ix, int nl) {
+  if (ix == 0) return 0.0;
+  const int p = 63 - __clzll((long long)ix);
+  const uint64_t m = ((uint64_t)ix << (52 - p)) & 0x000FFFFFFFFFFFFFull;
+  return __longlong_as_double((long long)(((uint64_t)(1023 + p - nl) << 52) | m));
+}
+
 struct Stencil {
   int64_t ix[4], iy[4], iz[4];  // x offsets, y*N, z*N*N
   double wx[4], wy[4], wz[4];
@@ -193,20 +202,28 @@ __global__ void __launch_bounds__(256) k_fast_interp(const double* __restrict__ 
 // and output writes).  On a periodic power-of-two grid the first velocity
 // evaluation of the first sub-step sits exactly on the node (the Lagrange
 // weights there are exactly 0,1,0,0), so it is read, not interpolated.
+// h = the node spacing and half_tau = tau / 2, formed once on the host.
 __global__ void __launch_bounds__(256, 2) k_semilag_grid(const double* __restrict__ vel,
                                                       const double* __restrict__ con,
                                                       double* __restrict__ cout, int N,
-                                                      double tau, int nrk, int periodic,
-                                                      int nl) {
+                                                      double tau, double half_tau, double h,
+                                                      int nrk, int periodic, int nl) {
   const bool node_read = nl >= 0;  // periodic power-of-two grid
   const int64_t N3 = (int64_t)N * N * N;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= N3) return;
   const bool per = periodic != 0;
-  const double h = per ? 1.0 / N : 1.0 / (N - 1);
   const int64_t ix = t % N, iy = (t / N) % N, iz = t / ((int64_t)N * N);
-  double x = (double)ix * h, y = (double)iy * h, z = (double)iz * h;
-  const double half_tau = 0.5 * tau;
+  double x, y, z;
+  if (nl >= 0) {
+    x = grid_coord_pow2(ix, nl);
+    y = grid_coord_pow2(iy, nl);
+    z = grid_coord_pow2(iz, nl);
+  } else {
+    x = (double)ix * h;
+    y = (double)iy * h;
+    z = (double)iz * h;
+  }
   double px = x, py = y, pz = z;
 #pragma unroll 1
   for (int st = 0; st < 2 * nrk; ++st) {
@@ -442,8 +459,9 @@ void launch_semilag_grid(const double* vel, const double* con, double* cout, int
   if (periodic && pow2)
     for (nl = 0; (1 << nl) < nreg; ++nl) {
     }
-  k_semilag_grid<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(vel, con, cout, nreg, tau, nrk,
-                                                             periodic, nl);
+  const double h = periodic ? 1.0 / nreg : 1.0 / (nreg - 1);
+  k_semilag_grid<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(vel, con, cout, nreg, tau,
+                                                             0.5 * tau, h, nrk, periodic, nl);
 }
 
 void launch_semilag_grid_df(const double* vel, const double* con, double* cout, int nreg,
