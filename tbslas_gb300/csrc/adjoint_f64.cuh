@@ -197,7 +197,9 @@ __device__ __forceinline__ void scatter_f64(AdjF64Shared<D>& sm, double* __restr
       const int n = tid + c * kAdjF64Threads;
 #pragma unroll
       for (int l = 0; l < DOF; ++l)
-        if (acc[c][l] != 0.0) atomicAdd(out + (int64_t)cur * stride + l * NC + n, acc[c][l]);
+        // acc != 0.0 as a bit test (integer pipe; NaN counts as nonzero)
+        if (dbits(acc[c][l]) & kBitsAbs)
+          atomicAdd(out + (int64_t)cur * stride + l * NC + n, acc[c][l]);
     }
   }
 }

@@ -67,6 +67,32 @@ def test_eval_tree_matches_oracle(ctx, ora, kind, q, dof, bc):
     assert np.array_equal(host, out)
 
 
+@pytest.mark.parametrize("bc", [0, 1])
+def test_eval_tree_special_values_match_oracle(ctx, ora, bc):
+    """Coefficients with exact zeros and -0.0 (the first term of every row of
+    the Chebyshev sums is formed on the integer pipe: c_0 with -0 read as +0,
+    as the FP64 fma gives it) and coordinates at 0, -0.0, just below 0 and
+    above 1, subnormal, tiny, infinite and NaN (the domain tests, the
+    periodic wrap and the Morton quantisation run on the coordinates' bits):
+    the functor's values equal the oracle's exactly."""
+    q, dof = 6, 3
+    anchor, depth, coeff = _tree_case("adaptive", q, dof, seed=7)
+    coeff[::3, :, 0] = -0.0
+    coeff[1::5, :, ::4] = 0.0
+    coeff[2::7] = -0.0
+    rng = np.random.default_rng(77)
+    pts = _points(rng, 4000)
+    extra = np.array([[5e-324, 0.5, 0.5], [np.inf, 0.5, 0.5], [-np.inf, 0.5, 0.5],
+                      [-1e-300, 0.5, 0.5], [1 + 2 ** -52, 0.5, 0.5], [0.5, 2 ** -30, 0.5],
+                      [0.5, 0.5, -0.0], [-0.0, -0.0, -0.0], [np.nan, 0.1, 0.1],
+                      [0.5, -np.nan, 0.5], [2 ** -21, 2 ** -21 - 2 ** -74, 0.5]])
+    pts[20:20 + len(extra)] = extra
+    t = tb.Tree(ctx, anchor, depth, q, dof, coeff)
+    out = tb.NodeFieldFunctor(t, bc)(_dev(pts)).cpu().numpy()
+    ref = ora.eval_tree(anchor, depth, q, dof, coeff, pts.copy(), periodic=bool(bc))
+    assert np.array_equal(out, ref)
+
+
 def test_eval_tree_empty_and_errors(ctx):
     import torch
     anchor, depth = trees.uniform_tree(1)
