@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include "df64.cuh"
+#include "fp64_bits.cuh"
 #include "tbslas_gb300.h"
 
 namespace tbg {
@@ -35,45 +36,6 @@ __host__ __device__ inline uint64_t morton3(uint64_t x, uint64_t y, uint64_t z) 
   return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
 }
 
-// The comparisons of coordinates against 0 and 1 below are made on the bits
-// of the FP64 value with integer instructions: FP64 comparisons and
-// conversions issue to the FP64 pipe, which bounds every SL kernel, while
-// the integer pipe has room.  Each gives the FP64 comparison's answer for
-// every input, -0.0, subnormals, infinities and NaN included.
-__device__ __forceinline__ uint64_t dbits(double c) { return (uint64_t)__double_as_longlong(c); }
-constexpr uint64_t kBitsOne = 0x3FF0000000000000ull;   // 1.0
-constexpr uint64_t kBitsNegZero = 0x8000000000000000ull;
-constexpr uint64_t kBitsAbs = 0x7FFFFFFFFFFFFFFFull;
-
-// c < 0.0: sign set, not -0.0, not a NaN (bits in (-0.0, -inf]).
-__device__ __forceinline__ bool below_zero(double c) {
-  return dbits(c) - (kBitsNegZero + 1) < 0x7FF0000000000000ull;
-}
-// c >= 1.0: bits in [1.0, +inf].
-__device__ __forceinline__ bool at_least_one(double c) {
-  return dbits(c) - kBitsOne <= 0x4000000000000000ull;
-}
-// 0 <= c <= 1 (closed) or 0 <= c < 1.
-__device__ __forceinline__ bool in_unit_closed(double c) {
-  const uint64_t b = dbits(c);
-  return b <= kBitsOne || b == kBitsNegZero;
-}
-__device__ __forceinline__ bool in_unit_open(double c) {
-  const uint64_t b = dbits(c);
-  return b < kBitsOne || b == kBitsNegZero;
-}
-// |c| <= 1 (NaN false).
-__device__ __forceinline__ bool abs_at_most_one(double c) { return (dbits(c) & kBitsAbs) <= kBitsOne; }
-
-// 2x for |x| <= 1 (the Chebyshev recurrence's multiplier), exact: the
-// exponent raised by one, or the mantissa shifted for zero and subnormals.
-__device__ __forceinline__ double twice(double x) {
-  const uint64_t b = dbits(x);
-  return __longlong_as_double((long long)((b & 0x7FF0000000000000ull)
-                                              ? b + (1ull << 52)
-                                              : (b & kBitsNegZero) | ((b & kBitsAbs) << 1)));
-}
-
 // Single periodic wrap of one coordinate, src/tree/tree_functor.h:442-448.
 __device__ __forceinline__ double wrap1(double c) {
   if (below_zero(c)) c = c + 1.0;
@@ -86,13 +48,7 @@ __device__ __forceinline__ double wrap1(double c) {
 // has checked 0 <= c <= 1 (c < 1 under periodic).  c == 1.0 is shifted into
 // the last cell as the reference does for non-periodic trees
 // (src/tree/tree_functor.h:464-479).
-__device__ __forceinline__ uint64_t quantise(double c) {
-  const uint64_t b = dbits(c) & kBitsAbs;  // -0.0 -> +0.0
-  if (b >= kBitsOne) return kKeyScale - 1;
-  const int s = 1075 - kKeyBits - (int)(b >> 52);  // c 2^21 = M 2^-s, s >= 32
-  if (s > 52) return 0;                             // c < 2^-21, zero, subnormal
-  return ((b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull) >> s;
-}
+__device__ __forceinline__ uint64_t quantise(double c) { return floor_scaled(c, kKeyBits); }
 
 // Is the (already wrapped) point inside the domain?  NaN compares false.
 __device__ __forceinline__ bool inside(double x, double y, double z, bool periodic) {
@@ -105,11 +61,8 @@ __device__ __forceinline__ bool inside(double x, double y, double z, bool period
 struct __align__(32) Geom {
   double x, y, z, w;
 };
-// 2 / w = 2^-depth, the leaf's side: exact, formed from the exponent of
-// w = 2^(depth+1) (an FP64 division is a sequence of FP64 instructions).
-__device__ __forceinline__ double leaf_side(const Geom& g) {
-  return __longlong_as_double((long long)((2047ull - (dbits(g.w) >> 52)) << 52));
-}
+// 2 / w = 2^-depth, the leaf's side (exact, fp64_bits.cuh).
+__device__ __forceinline__ double leaf_side(const Geom& g) { return inverse_pow2_times2(g.w); }
 __device__ __forceinline__ Geom load_geom(const Geom* p) {
   const double2 a = __ldg(reinterpret_cast<const double2*>(p));
   const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
@@ -157,29 +110,6 @@ __device__ __forceinline__ void cheb_T(double xi, double (&T)[D]) {
   const double x2 = twice(x);
 #pragma unroll
   for (int k = 2; k < D; ++k) T[k] = fma(x2, T[k - 1], -T[k - 2]);
-}
-
-// fma(t0, x, +0.0) for t0 = T_0 as cheb_T forms it (1.0 inside [-1, 1],
-// +0.0 outside), on the integer pipe: x with -0.0 read as +0.0 when t0 = 1;
-// +0.0 (NaN for a non-finite x) when t0 = 0 -- the FP64 fma's bits in both
-// cases.  The first term of every row of a Chebyshev sum is this product, so
-// a row costs one FP64 instruction less.
-__device__ __forceinline__ double fma_t0(double t0, double x) {
-  const uint64_t b = dbits(x);
-  if (dbits(t0) != 0) return __longlong_as_double((long long)(b == kBitsNegZero ? 0ull : b));
-  return __longlong_as_double(
-      (long long)((b & kBitsAbs) < 0x7FF0000000000000ull ? 0ull : 0x7FF8000000000000ull));
-}
-
-// t0 * x for t0 in {0, 1} (T_0, dT_1 as cheb_T / cheb_TdT form them), on the
-// integer pipe: x when t0 = 1; +-0 with x's sign (NaN for a non-finite x)
-// when t0 = 0 -- the FP64 product's bits in both cases.
-__device__ __forceinline__ double mul_t0(double t0, double x) {
-  const uint64_t b = dbits(x);
-  if (dbits(t0) != 0) return x;
-  return __longlong_as_double(
-      (long long)((b & kBitsAbs) < 0x7FF0000000000000ull ? (b & kBitsNegZero)
-                                                          : 0x7FF8000000000000ull));
 }
 
 // Triangular tensor Chebyshev sum of one dof:

@@ -16,82 +16,6 @@
 
 namespace tbg {
 
-// Cubic Lagrange weights at offset t from the stencil base, formed exactly as
-// the reference does (denominators by repeated division, then the product of
-// (t - l) over l != k in increasing l): src/tree/tree_functor.h:93-99,
-// :126-135.
-__device__ __forceinline__ void lagrange4(double t, double (&w)[4]) {
-  const double den[4] = {-1.0 / 6.0, 0.5, -0.5, 1.0 / 6.0};
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    double m = den[k];
-#pragma unroll
-    for (int l = 0; l < 4; ++l)
-      if (k != l) m *= (t - (double)l);
-    w[k] = m;
-  }
-}
-
-// Stencil base and offset of one coordinate on a periodic grid of N = 2^nl
-// nodes, with integer operations on the bits of x in [0, 1): p = x N,
-// g = floor(p) - 1, t = p - g in [1, 2) -- the values make_stencil computes
-// in FP64 (x N is exact: a power-of-two scaling).
-__device__ __forceinline__ void grid_split_pow2(double x, int nl, int& g, double& t) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int s = 1075 - nl - (int)(b >> 52);  // p = M 2^-s, M = 2^52 + mantissa
-  if ((b << 1) == 0 || s > 52) {             // +-0, or p < 1 (first cell): FP64
-    g = -1;
-    t = fma(x, (double)(1 << nl), 1.0);
-    return;
-  }
-  const unsigned long long M = (b & ((1ull << 52) - 1)) | (1ull << 52);
-  g = (int)(M >> s) - 1;
-  const unsigned long long frac = s > 0 ? (M & ((1ull << s) - 1)) : 0ull;
-  t = __longlong_as_double((long long)((1023ull << 52) | (frac << (52 - s))));
-}
-
-// g 2^-52 as a double for 0 < g <= 2^53 (exact: g has at most 53 bits), with
-// the sign bit set when neg.
-__device__ __forceinline__ double scaled_mantissa(uint64_t g, bool neg) {
-  const int p = 63 - __clzll((long long)g);  // leading bit, <= 53
-  const uint64_t m = p <= 52 ? (g << (52 - p)) & 0x000FFFFFFFFFFFFFull : 0ull;
-  return __longlong_as_double(
-      (long long)((neg ? kBitsNegZero : 0ull) | ((uint64_t)(1023 + p - 52) << 52) | m));
-}
-
-// lagrange4 for an offset t in [1, 2) (a power-of-two grid's): the same
-// products in the same order, with t - 1, t - 2, t - 3 and the exact
-// halvings +-t/2 formed from the mantissa of t by integer operations (each
-// of those FP64 operations is exact, so the values are the same).  Other
-// offsets (t rounded up to 2 in the first cell) take lagrange4.
-__device__ __forceinline__ void lagrange4_unit(double t, double (&w)[4]) {
-  const uint64_t b = dbits(t);
-  if ((b >> 52) != 1023) {
-    lagrange4(t, w);
-    return;
-  }
-  const uint64_t f = b & 0x000FFFFFFFFFFFFFull;
-  const double d1 = f ? scaled_mantissa(f, false) : 0.0;      // t - 1 in [0, 1)
-  const double d2 = scaled_mantissa((1ull << 52) - f, true);  // t - 2 in [-1, 0)
-  const double d3 = scaled_mantissa((1ull << 53) - f, true);  // t - 3 in [-2, -1)
-  const uint64_t hb = b - (1ull << 52);                        // t / 2
-  const double h = __longlong_as_double((long long)hb);
-  const double hn = __longlong_as_double((long long)(hb | kBitsNegZero));
-  w[0] = ((-1.0 / 6.0 * d1) * d2) * d3;
-  w[1] = (h * d2) * d3;
-  w[2] = (hn * d1) * d3;
-  w[3] = ((1.0 / 6.0 * t) * d1) * d2;
-}
-
-// ix * 2^-nl as a double, exactly (the node coordinate ix h of a periodic
-// grid of 2^nl nodes), formed from the integer's bits.
-__device__ __forceinline__ double grid_coord_pow2(int64_t ix, int nl) {
-  if (ix == 0) return 0.0;
-  const int p = 63 - __clzll((long long)ix);
-  const uint64_t m = ((uint64_t)ix << (52 - p)) & 0x000FFFFFFFFFFFFFull;
-  return __longlong_as_double((long long)(((uint64_t)(1023 + p - nl) << 52) | m));
-}
-
 struct Stencil {
   int64_t ix[4], iy[4], iz[4];  // x offsets, y*N, z*N*N
   double wx[4], wy[4], wz[4];
