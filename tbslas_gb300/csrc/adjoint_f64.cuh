@@ -373,11 +373,7 @@ __global__ void __launch_bounds__(128) k_semilag_tree_jac(const SemilagTreeArgs 
   double y = g.y + h * a.nodes.x[(p / D) % D];
   double z = g.z + h * a.nodes.x[p / (D * D)];
   const bool per = a.periodic != 0;
-  if (per) {
-    x = wrap1(x);
-    y = wrap1(y);
-    z = wrap1(z);
-  }
+  if (per) wrap3(x, y, z);
   const double half_tau = 0.5 * a.tau;
   const double* vn = a.vn + 3 * t;
   double px = fma(half_tau, __ldg(vn + 0), x);

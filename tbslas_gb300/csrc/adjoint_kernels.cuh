@@ -152,11 +152,7 @@ __device__ __forceinline__ void tri_grad(Load c, const double (&tx)[D],
 template <int D>
 __device__ __forceinline__ int64_t locate(const TreeView& t, double& x, double& y, double& z,
                                           bool per, Geom& g) {
-  if (per) {
-    x = wrap1(x);
-    y = wrap1(y);
-    z = wrap1(z);
-  }
+  if (per) wrap3(x, y, z);
   if (!inside(x, y, z, per)) return -1;
   const int64_t leaf = find_leaf(t, morton3(quantise(x), quantise(y), quantise(z)));
   g = load_geom(t.geom + leaf);

@@ -43,6 +43,19 @@ __device__ __forceinline__ double wrap1(double c) {
   return c;
 }
 
+// wrap1 on a point's three coordinates, its FP64 additions issued only when
+// some lane of the warp needs them (a predicated-off FP64 instruction still
+// takes its slot in the FP64 pipe); wrap1 leaves coordinates in [0, 1) as
+// they are, so skipping it there changes nothing.
+__device__ __forceinline__ void wrap3(double& x, double& y, double& z) {
+  const bool need = !(in_unit_open(x) && in_unit_open(y) && in_unit_open(z));
+  if (__any_sync(__activemask(), need)) {
+    x = wrap1(x);
+    y = wrap1(y);
+    z = wrap1(z);
+  }
+}
+
 // Axis coordinate -> 21-bit integer, floor(c 2^21) (the product is exact, a
 // power-of-two scaling) formed from the mantissa and exponent.  The caller
 // has checked 0 <= c <= 1 (c < 1 under periodic).  c == 1.0 is shifted into
@@ -159,11 +172,7 @@ template <int D, int DOF>
 __device__ __forceinline__ void eval_point(const TreeView& t, double& x, double& y, double& z,
                                            bool periodic, double (&out)[DOF]) {
   constexpr int NC = D * (D + 1) * (D + 2) / 6;
-  if (periodic) {
-    x = wrap1(x);
-    y = wrap1(y);
-    z = wrap1(z);
-  }
+  if (periodic) wrap3(x, y, z);
   if (!inside(x, y, z, periodic)) {
 #pragma unroll
     for (int l = 0; l < DOF; ++l) out[l] = 0.0;
@@ -214,11 +223,7 @@ __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, doub
                                               bool periodic, const double (&m)[3],
                                               double (&out)[DOF], double (&err)[DOF],
                                               ThreadSlots slots) {
-  if (periodic) {
-    x = wrap1(x);
-    y = wrap1(y);
-    z = wrap1(z);
-  }
+  if (periodic) wrap3(x, y, z);
   const double mmax = fmax(m[0], fmax(m[1], m[2]));
   if (!inside(x, y, z, periodic)) {
 #pragma unroll
@@ -265,11 +270,7 @@ __device__ __forceinline__ bool eval_point_df(const TreeView& t, double& x, doub
 // could differ.
 __device__ __forceinline__ bool lookup_ambiguous(const TreeView& t, double x, double y, double z,
                                                  bool periodic, const double (&m)[3]) {
-  if (periodic) {
-    x = wrap1(x);
-    y = wrap1(y);
-    z = wrap1(z);
-  }
+  if (periodic) wrap3(x, y, z);
   if (!inside(x, y, z, periodic)) {
     if (fmax(m[0], fmax(m[1], m[2])) == 0.0) return false;
     return x >= -m[0] && x <= 1.0 + m[0] && y >= -m[1] && y <= 1.0 + m[1] && z >= -m[2] &&

@@ -129,18 +129,27 @@ TBG_BITS_FN double grid_coord_pow2(int64_t ix, int nl) {
 
 // Stencil base and offset of one coordinate x in [0, 1) (-0.0 included) on a
 // periodic grid of N = 2^nl nodes: p = x N, g = floor(p) - 1, t = p - g in
-// [1, 2] -- the values p - (double)g gives in FP64 (x N is exact; t is exact
-// for p >= 1 and a single rounding of p + 1 for p < 1, formed by the same
-// fused multiply-add).
+// [1, 2] -- the values p - (double)g gives in FP64: x N is exact; t is exact
+// for p >= 1, and for p < 1 (the first cell) it is 1 + p rounded to nearest
+// even, formed here from the bits of p.
 TBG_BITS_FN void grid_split_pow2(double x, int nl, int& g, double& t) {
   const uint64_t b = dbits(x);
-  const int s = 1075 - nl - (int)(b >> 52);  // p = M 2^-s, M = 2^52 + mantissa
-  if ((b << 1) == 0 || s > 52) {             // +-0, or p < 1 (first cell)
+  const uint64_t M = (b & kBitsMant) | (1ull << 52);  // x normal: p = M 2^-s
+  const int s = 1075 - nl - (int)(b >> 52);
+  if ((b << 1) == 0 || s > 52) {  // +-0, or p < 1 (subnormal x included)
     g = -1;
-    t = fma(x, (double)(1 << nl), 1.0);
+    // 1 + p = 1 + q 2^-52 with q = p 2^52 = M 2^-(s - 52) rounded to nearest
+    // even (M 2^-sh with sh = s - 52 >= 1; a subnormal or zero x gives 0)
+    uint64_t q = 0;
+    const int sh = s - 52;
+    if ((b & kBitsInf) != 0 && sh < 64) {
+      q = M >> sh;
+      const uint64_t rem = M & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+      if (rem > half || (rem == half && (q & 1))) ++q;
+    }
+    t = from_bits((1023ull << 52) + q);  // q = 2^52 carries into the exponent: t = 2
     return;
   }
-  const uint64_t M = (b & kBitsMant) | (1ull << 52);
   g = (int)(M >> s) - 1;
   const uint64_t frac = s > 0 ? (M & ((1ull << s) - 1)) : 0ull;
   t = from_bits((1023ull << 52) | (frac << (52 - s)));

@@ -27,11 +27,7 @@ struct Stencil {
 // without FP64 instructions.
 __device__ __forceinline__ bool make_stencil(double& x, double& y, double& z, int N,
                                              bool periodic, Stencil& s, int nl = -1) {
-  if (periodic) {
-    x = wrap1(x);
-    y = wrap1(y);
-    z = wrap1(z);
-  }
+  if (periodic) wrap3(x, y, z);
   if (!inside(x, y, z, periodic)) return false;
   const double scale = periodic ? (double)N : (double)(N - 1);
   const double c[3] = {x, y, z};
@@ -137,7 +133,16 @@ __global__ void __launch_bounds__(256, 2) k_semilag_grid(const double* __restric
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= N3) return;
   const bool per = periodic != 0;
-  const int64_t ix = t % N, iy = (t / N) % N, iz = t / ((int64_t)N * N);
+  int64_t ix, iy, iz;
+  if (nl >= 0) {  // N = 2^nl: the node's indices by shifts (no 64-bit division)
+    ix = t & (N - 1);
+    iy = (t >> nl) & (N - 1);
+    iz = t >> (2 * nl);
+  } else {
+    ix = t % N;
+    iy = (t / N) % N;
+    iz = t / ((int64_t)N * N);
+  }
   double x, y, z;
   if (nl >= 0) {
     x = grid_coord_pow2(ix, nl);
@@ -259,9 +264,7 @@ __device__ __forceinline__ void lagrange4_df(double t, df (&w)[4]) {
 __device__ __forceinline__ bool make_stencil_df(double& x, double& y, double& z, int N, int nl,
                                                 StencilDF& s, df (&wx)[4], df (&wy)[4],
                                                 df (&wz)[4]) {
-  x = wrap1(x);
-  y = wrap1(y);
-  z = wrap1(z);
+  wrap3(x, y, z);
   if (!inside(x, y, z, true)) return false;
   const double c[3] = {x, y, z};
   int base[3];

@@ -99,11 +99,7 @@ __device__ __forceinline__ void rk2_backtrace_from_node(const TreeView& vel, con
                                                         double& x, double& y, double& z,
                                                         double tau, int nrk, bool per,
                                                         double* mid = nullptr) {
-  if (per) {
-    x = wrap1(x);
-    y = wrap1(y);
-    z = wrap1(z);
-  }
+  if (per) wrap3(x, y, z);
   const double half_tau = 0.5 * tau;
   double px = fma(half_tau, __ldg(vn + 0), x);
   double py = fma(half_tau, __ldg(vn + 1), y);

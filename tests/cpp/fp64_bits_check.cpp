@@ -92,9 +92,17 @@ int main() {
     if (x >= 0.0 && x < 1.0) offs.push_back(x);
   offs.push_back(-0.0);
   offs.push_back(std::nextafter(1.0 / 256, 0.0) * (1.0 - 0x1p-53));
+  // first-cell offsets at ties: p = x N = m 2^-53 for odd m (1 + p halfway
+  // between two doubles), placed below each grid's 1 / N later
+  std::vector<double> tie_p;
+  for (int i = 0; i < 200000; ++i)
+    tie_p.push_back(std::ldexp((double)((rng() >> 11) | 1ull), -53));
+  for (int i = 0; i < 60; ++i) tie_p.push_back(std::ldexp(1.0, -i - 1) + 0x1p-53);
   for (int nl : {1, 4, 8, 10}) {
     const double N = (double)(1 << nl);
-    for (double x : offs) {
+    std::vector<double> xs_nl = offs;
+    for (double p : tie_p) xs_nl.push_back(p / N);  // exact: a power-of-two scaling
+    for (double x : xs_nl) {
       int g = 0;
       double t = 0.0;
       grid_split_pow2(x, nl, g, t);
