@@ -1182,10 +1182,12 @@ def run_tv(args, wl, rank, world, local_rank):
     ev = lambda dof: 9 * d + 2 * nc * dof
     m = len(wl.vcs)
     roofline = fp64_roofline(
-        ctx, "semilag_tv (k_semilag_tv<%d>, FP64: every tree at the midpoint)" % d,
-        m * ev(3) + ev(1) + 18, wl.points_per_step, prof, "semilag_tv", args.steps,
+        ctx, "semilag_tv (k_semilag_tv<%d, true>, FP64: every tree at the midpoint)" % d,
+        9 * d + m * 2 * nc * 3 + 3 * m + ev(1) + 18, wl.points_per_step, prof, "semilag_tv",
+        args.steps,
         "per point: the %d velocity trees evaluated at the RK2 midpoint and blended (as the "
-        "reference's FieldSetFunctor does; the first stage, at the node, is each tree's "
+        "reference's FieldSetFunctor does; the trees share their leaves, so one lookup and "
+        "one set of T_k serve all of them; the first stage, at the node, is each tree's "
         "node-grid pass, vel_at_nodes), the concentration at the departure point" % m)
     cfg = wl.describe()
     cfg.update({"l2": "flushed between timed steps (256 MiB write inside the timed loop)",

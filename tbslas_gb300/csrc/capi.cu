@@ -53,6 +53,7 @@ std::once_flag g_kernels_once;
 void init_kernels() {
   register_tv_a(g_tv);
   register_tv_b(g_tv);
+  register_tv_c(g_tv);
   register_bdf2_a(g_bdf2);
   register_bdf2_b(g_bdf2);
   register_degrees_a(g_kernels);
@@ -1974,9 +1975,10 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
   cudaStream_t s = (cudaStream_t)stream;
   const double tau = sl_tau(timestep, dt, nrk);
   // one leaf structure, nrk = 1 and the double-float mode: blend the
-  // coefficients per stage and run the fused step (the FP64 mode evaluates
-  // every tree and blends the values, as the reference's functors do)
-  bool same = nrk == 1 && ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT;
+  // coefficients per stage and run the fused step.  The FP64 mode evaluates
+  // every tree and blends the values, as the reference's functors do, with
+  // one leaf lookup per point when the trees share their structure.
+  bool same = true;
   for (int k = 1; k < m && same; ++k) same = vel[k]->L == vel[0]->L;
   if (same && m > 1) {
     int* flag;
@@ -1991,7 +1993,7 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
     CUDA_TRY(cudaStreamSynchronize(s));
     same = h == 0;
   }
-  if (same) {
+  if (same && nrk == 1 && ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT) {
     const tbslas_tree v0 = vel[0];
     const int64_t n = v0->L * v0->stride;
     const double* c[kTvMaxTrees];
@@ -2028,6 +2030,7 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
   a.nrk = nrk;
   a.periodic = bc;
   for (int j = 0; j < 2 * nrk * m; ++j) a.w[j] = w[j];
+  a.same_leaves = same ? 1 : 0;
   const int64_t N = con->L * n_points(con->q);
   TRY(scratch_t(ctx, kVals, N, &a.vals));
   {

@@ -142,10 +142,12 @@ struct TvArgs {
   // (bit-identical to evaluating them there), or null
   const double* vn = nullptr;
   double w[2 * kTvMaxSubsteps * kTvMaxTrees];
+  int same_leaves = 0;  // 1: every tree has vel[0]'s leaves (one lookup per point)
 };
 typedef void (*TvFn)(const TvArgs&, cudaStream_t);
 void register_tv_a(TvFn* table);  // index = Chebyshev degree q
 void register_tv_b(TvFn* table);
+void register_tv_c(TvFn* table);
 // out[i] = sum_k w[k] c_k[i], i < n (tv_deg_a.cu)
 void launch_blend_coeffs(const double* const* c, const double* w, int m, int64_t n, double* out,
                          cudaStream_t s);

@@ -1,4 +1,4 @@
-// Time-dependent velocity step kernels for Chebyshev degrees 10..16.
+// Time-dependent velocity step kernels for Chebyshev degrees 10..13.
 #include "tv_kernels.cuh"
 
 namespace tbg {
@@ -7,8 +7,5 @@ void register_tv_b(TvFn* table) {
   table[11] = &launch_semilag_tv<12>;
   table[12] = &launch_semilag_tv<13>;
   table[13] = &launch_semilag_tv<14>;
-  table[14] = &launch_semilag_tv<15>;
-  table[15] = &launch_semilag_tv<16>;
-  table[16] = &launch_semilag_tv<17>;
 }
 }  // namespace tbg

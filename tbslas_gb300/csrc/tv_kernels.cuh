@@ -16,21 +16,50 @@
 
 namespace tbg {
 
-template <int D>
+// SAME (the trees share their leaves): one leaf lookup and one set of T_k per
+// point serve every tree -- what each tree's eval_point would compute, so the
+// values are the same bits.
+template <int D, bool SAME>
 __device__ __forceinline__ void tv_velocity(const TvArgs& a, int stage, double& x, double& y,
                                             double& z, bool per, double (&v)[3]) {
+  constexpr int NC = D * (D + 1) * (D + 2) / 6;
   const double* w = a.w + stage * a.m;
   v[0] = v[1] = v[2] = 0.0;
-  for (int k = 0; k < a.m; ++k) {
-    double u[3];
-    eval_point<D, 3>(a.vel[k], x, y, z, per, u);  // wraps the point in place
-    v[0] = fma(w[k], u[0], v[0]);
-    v[1] = fma(w[k], u[1], v[1]);
-    v[2] = fma(w[k], u[2], v[2]);
+  if constexpr (SAME) {
+    if (per) wrap3(x, y, z);
+    const bool in = inside(x, y, z, per);
+    double tx[D], ty[D], tz[D];
+    int64_t leaf = 0;
+    if (in) {
+      leaf = find_leaf(a.vel[0], morton3(quantise(x), quantise(y), quantise(z)));
+      const Geom g = load_geom(a.vel[0].geom + leaf);
+      cheb_T<D>((x - g.x) * g.w - 1.0, tx);
+      cheb_T<D>((y - g.y) * g.w - 1.0, ty);
+      cheb_T<D>((z - g.z) * g.w - 1.0, tz);
+    }
+    for (int k = 0; k < a.m; ++k) {
+      double u[3] = {0.0, 0.0, 0.0};
+      if (in) {
+        const double* c = a.vel[k].coeff + leaf * a.vel[k].stride;
+#pragma unroll
+        for (int l = 0; l < 3; ++l) u[l] = tri_sum<D>(GlobalLoad{c + l * NC}, tx, ty, tz);
+      }
+      v[0] = fma(w[k], u[0], v[0]);
+      v[1] = fma(w[k], u[1], v[1]);
+      v[2] = fma(w[k], u[2], v[2]);
+    }
+  } else {
+    for (int k = 0; k < a.m; ++k) {
+      double u[3];
+      eval_point<D, 3>(a.vel[k], x, y, z, per, u);  // wraps the point in place
+      v[0] = fma(w[k], u[0], v[0]);
+      v[1] = fma(w[k], u[1], v[1]);
+      v[2] = fma(w[k], u[2], v[2]);
+    }
   }
 }
 
-template <int D>
+template <int D, bool SAME>
 __global__ void __launch_bounds__(128) k_semilag_tv(const TvArgs a) {
   constexpr int NP = D * D * D;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -64,11 +93,11 @@ __global__ void __launch_bounds__(128) k_semilag_tv(const TvArgs a) {
         v[2] = fma(a.w[k], __ldg(u + 2), v[2]);
       }
     } else {
-      tv_velocity<D>(a, 2 * s, x, y, z, per, v);  // at X (wrapped in place)
+      tv_velocity<D, SAME>(a, 2 * s, x, y, z, per, v);  // at X (wrapped in place)
     }
     double px = fma(half_tau, v[0], x), py = fma(half_tau, v[1], y),
            pz = fma(half_tau, v[2], z);
-    tv_velocity<D>(a, 2 * s + 1, px, py, pz, per, v);  // at X*
+    tv_velocity<D, SAME>(a, 2 * s + 1, px, py, pz, per, v);  // at X*
     x = fma(a.tau, v[0], x);
     y = fma(a.tau, v[1], y);
     z = fma(a.tau, v[2], z);
@@ -81,7 +110,12 @@ __global__ void __launch_bounds__(128) k_semilag_tv(const TvArgs a) {
 template <int D>
 void launch_semilag_tv(const TvArgs& a, cudaStream_t s) {
   const int64_t n = a.con.L * D * D * D;
-  if (n > 0) k_semilag_tv<D><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+  if (n <= 0) return;
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+  if (a.same_leaves)
+    k_semilag_tv<D, true><<<blocks, 128, 0, s>>>(a);
+  else
+    k_semilag_tv<D, false><<<blocks, 128, 0, s>>>(a);
 }
 
 }  // namespace tbg
