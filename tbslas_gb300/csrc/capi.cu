@@ -2038,9 +2038,16 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
     double* vn = nullptr;
     TRY(scratch_t(ctx, kVN, (size_t)m * N * 3, &vn));
     const int32_t* face = tree_face_map(con, bc, s);
-    ProfScope pv(ctx, "vel_at_nodes", s, face ? 2 * m : m);
-    for (int k = 0; k < m; ++k)
-      launch_eval_on_nodes(vel[k]->view(), a.con, bc, vn + 3 * k * N, s, face);
+    const int nl = same ? 1 : m;  // one walk for trees of one structure
+    ProfScope pv(ctx, "vel_at_nodes", s, face ? 2 * nl : nl);
+    if (same) {
+      TreeView v[kTvMaxTrees];
+      for (int k = 0; k < m; ++k) v[k] = vel[k]->view();
+      launch_eval_on_nodes_set(v, m, a.con, bc, vn, 3 * N, s, face);
+    } else {
+      for (int k = 0; k < m; ++k)
+        launch_eval_on_nodes(vel[k]->view(), a.con, bc, vn + 3 * k * N, s, face);
+    }
     TRY(check_launch("velocity set at nodes"));
     a.vn = vn;
   }

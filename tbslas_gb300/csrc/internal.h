@@ -248,6 +248,12 @@ int step_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, 
 // (every node evaluated, no copy)
 void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic, double* out,
                           cudaStream_t s, const int32_t* face = nullptr);
+// ntrees source trees of one leaf structure (src[k].keys all equal; the
+// walk is src[0]'s), tree k's values at out + k * tstride, each as
+// launch_eval_on_nodes writes them.  ntrees <= kTvMaxTrees.
+void launch_eval_on_nodes_set(const TreeView* src, int ntrees, const TreeView& dst, int periodic,
+                              double* out, int64_t tstride, cudaStream_t s,
+                              const int32_t* face = nullptr);
 // face[t] = the target index whose value the shared upper-face node t takes
 // (same point, same source leaf), else -1; [dst.L * Np]
 void launch_face_map(const TreeView& dst, int periodic, int32_t* face, cudaStream_t s);

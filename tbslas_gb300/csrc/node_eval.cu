@@ -30,6 +30,7 @@
 // evaluate it -- w in shared memory, then per (b, a) column v(., b, a) in
 // registers and every u of the column.  FP64 (FP64 pipe); templated on the
 // source degree (register arrays), runtime destination degree.
+#include <algorithm>
 #include <atomic>
 #include <climits>
 #include <cstring>
@@ -256,6 +257,50 @@ __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const Tree
       [&](const SubGrid& sg) { eval_subgrid<Ds>(S, sg, Dd, out, dof, 1, sw); });
 }
 
+// Several source trees of one leaf structure (the walk's source leaves are
+// the same for all of them): tree t's values go to out_all + t * tstride,
+// [dst.L * Dd^3][dof] each.  The sub-grid passes take `group` trees at a
+// time (3 group components; their w tables fill the shared memory), each
+// value as eval_on_nodes_leaf computes it.  s_coeff: the trees' coefficient
+// arrays, in shared memory.
+template <int Ds>
+__device__ __forceinline__ void eval_on_nodes_set_leaf(const TreeView& S, const TreeView& dst,
+                                                       const Nodes1D& nodes, bool per,
+                                                       int64_t leaf, const int32_t* face,
+                                                       const double* const* s_coeff, int ntrees,
+                                                       int group, double* __restrict__ out_all,
+                                                       int64_t tstride, double* sm) {
+  constexpr int NCs = Ds * (Ds + 1) * (Ds + 2) / 6;
+  const int Dd = dst.q + 1, Dd3 = Dd * Dd * Dd;
+  const int dof = S.dof;
+  const int64_t stride = S.stride;
+  double* sw = sm + walk_smem(Ds, Dd) / 8;
+  double* out = out_all + leaf * (int64_t)Dd3 * dof;
+  for_each_subgrid<Ds>(
+      S, dst, nodes, per, leaf, face, sm,
+      [&](int p) {
+        for (int t = 0; t < ntrees; ++t)
+          for (int l = 0; l < dof; ++l) out[t * tstride + (int64_t)p * dof + l] = 0.0;
+      },
+      [&](const SubGrid& sg) {
+        for (int t0 = 0; t0 < ntrees; t0 += group) {
+          if (t0 > 0) __syncthreads();  // the previous group is done with sw
+          const int nt = min(group, ntrees - t0);
+          eval_subgrid_comps<Ds>(
+              sg, Dd, nt * dof,
+              [=](int c) {
+                const int t = c / dof;
+                return s_coeff[t0 + t] + sg.V * stride + (c - t * dof) * NCs;
+              },
+              [=](int c) {
+                const int t = c / dof;
+                return out + (t0 + t) * tstride + (c - t * dof);
+              },
+              dof, sw);
+        }
+      });
+}
+
 // The transposed map (adjoint of the evaluation): for one destination leaf,
 // out[V * out_stride + l * Nc + n] += sum over its nodes p inside V of
 // W[p][l] phi_n(X_p), the basis of V at the node -- the same passes in
@@ -368,6 +413,19 @@ __global__ void __launch_bounds__(kNodeEvalThreads) k_copy_face_nodes(
   for (int l = 0; l < dof; ++l) out[t * dof + l] = out[(int64_t)src * dof + l];
 }
 
+// k_copy_face_nodes for ntrees outputs tstride apart.
+__global__ void __launch_bounds__(kNodeEvalThreads) k_copy_face_nodes_set(
+    const int32_t* __restrict__ face, int64_t n, int dof, int ntrees, int64_t tstride,
+    double* __restrict__ out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int32_t src = __ldg(face + t);
+  if (src < 0) return;
+  for (int k = 0; k < ntrees; ++k)
+    for (int l = 0; l < dof; ++l)
+      out[k * tstride + t * dof + l] = out[k * tstride + (int64_t)src * dof + l];
+}
+
 __global__ void __launch_bounds__(kNodeEvalThreads) k_batch_copy_face_nodes(
     const NodeEvalJob* __restrict__ jobs, const NodeEvalItem* __restrict__ items) {
   __shared__ NodeEvalJob sj;
@@ -389,6 +447,27 @@ __global__ void __launch_bounds__(kNodeEvalThreads) k_eval_on_nodes(const NodeEv
                                                                     int periodic) {
   extern __shared__ __align__(16) double sm[];
   eval_on_nodes_leaf<Ds>(j.src, j.dst, j.nodes, periodic != 0, blockIdx.x, j.face, j.out, sm);
+}
+
+struct NodeEvalSet {
+  NodeEvalJob j;  // j.src: the first tree (leaf structure, degree, dof)
+  const double* coeff[kTvMaxTrees];
+  int ntrees, group;
+  int64_t tstride;
+};
+
+template <int Ds>
+__global__ void __launch_bounds__(kNodeEvalThreads) k_eval_on_nodes_set(const NodeEvalSet a,
+                                                                        int periodic) {
+  extern __shared__ __align__(16) double sm[];
+  __shared__ const double* s_coeff[kTvMaxTrees];
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < kTvMaxTrees; ++k) s_coeff[k] = a.coeff[k];
+  }
+  __syncthreads();
+  eval_on_nodes_set_leaf<Ds>(a.j.src, a.j.dst, a.j.nodes, periodic != 0, blockIdx.x, a.j.face,
+                             s_coeff, a.ntrees, a.group, a.j.out, a.tstride, sm);
 }
 
 // Batched: one CTA per (job, destination leaf) item; the jobs of one launch
@@ -436,6 +515,25 @@ void launch_single(const NodeEvalJob& j, int64_t L, int periodic, cudaStream_t s
                         node_eval_smem(Ds, j.dst.q + 1, j.src.dof), s>>>(j, periodic);
 }
 
+// Shared memory of a set launch: the walk and `group` trees' w tables,
+// the largest group up to kSetSmem (at least one tree).
+constexpr size_t kSetSmem = 100 * 1024;
+template <int Ds>
+void launch_set(NodeEvalSet a, int64_t L, int periodic, cudaStream_t s) {
+  static std::atomic<uint64_t> done{0};
+  const int Dd = a.j.dst.q + 1, dof = a.j.src.dof;
+  const size_t walk = walk_smem(Ds, Dd), per_tree = (size_t)dof * Ds * (Ds + 1) / 2 * Dd * 8;
+  int g = a.ntrees;
+  while (g > 1 && walk + g * per_tree > kSetSmem) --g;
+  a.group = g;
+  const size_t bytes = walk + g * per_tree;
+  // a group's bytes stay within kSetSmem, one tree's within the single
+  // launch's largest
+  allow_smem((const void*)k_eval_on_nodes_set<Ds>, std::max(kSetSmem, node_eval_smem(Ds, kMaxD, 3)),
+             done);
+  k_eval_on_nodes_set<Ds><<<(unsigned)L, kNodeEvalThreads, bytes, s>>>(a, periodic);
+}
+
 template <int Ds>
 void launch_batched(const NodeEvalJob* jobs, const NodeEvalItem* items, int64_t n, int max_qd,
                     int periodic, cudaStream_t s) {
@@ -481,6 +579,16 @@ void dispatch_single(int ds, const NodeEvalJob& j, int64_t L, int periodic, cuda
 }
 
 template <int Ds>
+void dispatch_set(int ds, const NodeEvalSet& a, int64_t L, int periodic, cudaStream_t s) {
+  if constexpr (Ds <= kMaxD) {
+    if (ds == Ds)
+      launch_set<Ds>(a, L, periodic, s);
+    else
+      dispatch_set<Ds + 1>(ds, a, L, periodic, s);
+  }
+}
+
+template <int Ds>
 void dispatch_batched(int ds, const NodeEvalJob* jobs, const NodeEvalItem* items, int64_t n,
                       int max_qd, int periodic, cudaStream_t s) {
   if constexpr (Ds <= kMaxD) {
@@ -518,6 +626,29 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
     const int64_t n = dst.L * (int64_t)(dst.q + 1) * (dst.q + 1) * (dst.q + 1);
     k_copy_face_nodes<<<(unsigned)((n + kNodeEvalThreads - 1) / kNodeEvalThreads),
                         kNodeEvalThreads, 0, s>>>(face, n, src.dof, out);
+  }
+}
+
+void launch_eval_on_nodes_set(const TreeView* src, int ntrees, const TreeView& dst, int periodic,
+                              double* out, int64_t tstride, cudaStream_t s,
+                              const int32_t* face) {
+  if (dst.L <= 0 || ntrees <= 0) return;
+  NodeEvalSet a;
+  std::memset(&a, 0, sizeof(a));
+  a.j.src = src[0];
+  a.j.dst = dst;
+  const std::vector<double> x = cheb_nodes_1d(dst.q);
+  for (int i = 0; i <= dst.q; ++i) a.j.nodes.x[i] = x[i];
+  a.j.out = out;
+  a.j.face = face;
+  for (int k = 0; k < ntrees; ++k) a.coeff[k] = src[k].coeff;
+  a.ntrees = ntrees;
+  a.tstride = tstride;
+  dispatch_set<1>(src[0].q + 1, a, dst.L, periodic, s);
+  if (face) {
+    const int64_t n = dst.L * (int64_t)(dst.q + 1) * (dst.q + 1) * (dst.q + 1);
+    k_copy_face_nodes_set<<<(unsigned)((n + kNodeEvalThreads - 1) / kNodeEvalThreads),
+                            kNodeEvalThreads, 0, s>>>(face, n, src[0].dof, ntrees, tstride, out);
   }
 }
 

@@ -41,39 +41,37 @@ struct SubGrid {
 //   v(i)         = sum_j T_j(y_b') w(l; i,j,a')        (per column l, b', a')
 //   u(c')        = sum_i T_i(z_c') v(i)
 // -- tri_sum's nested sums with its fma order (the T_0 terms by fma_t0), so
-// each value is bit-identical to eval_point.  Node p = a + Dd (b + Dd c) of component l
-// goes to out[p * pstride + l * lstride].  sw: dof * Ds (Ds + 1) / 2 * Dd
-// doubles of shared memory.  All threads of the block call it; it contains a
-// barrier between the first two passes.
-template <int Ds>
-__device__ __forceinline__ void eval_subgrid(const TreeView& S, const SubGrid& sg, int Dd,
-                                             double* __restrict__ out, int64_t pstride,
-                                             int64_t lstride, double* sw) {
+// each value is bit-identical to eval_point.  ncomp components: coeff(l) is
+// component l's Nc coefficients in the sub-grid's source leaf, out(l) its
+// output, node p = a + Dd (b + Dd c) at out(l)[p * pstride].  sw: ncomp *
+// Ds (Ds + 1) / 2 * Dd doubles of shared memory.  All threads of the block
+// call it; it contains a barrier between the first two passes.
+template <int Ds, class CoeffOf, class OutOf>
+__device__ __forceinline__ void eval_subgrid_comps(const SubGrid& sg, int Dd, int ncomp,
+                                                   CoeffOf coeff, OutOf outp, int64_t pstride,
+                                                   double* sw) {
   constexpr int NCs = Ds * (Ds + 1) * (Ds + 2) / 6, npair = Ds * (Ds + 1) / 2;
   const int Dd2 = Dd * Dd;
-  const int dof = S.dof;
   const int tid = threadIdx.x, bs = blockDim.x;
   const int na = sg.na, nb = sg.nb, nz = sg.nz;
   const int* sidx = sg.sidx;
-  const double* cV = S.coeff + sg.V * S.stride;
   // items (a', l, pair) with the pair slowest: the lanes of a warp share
   // one row length (the k loop) instead of diverging over several
-  for (int o = tid; o < dof * npair * na; o += bs) {
-    const int ai = o % na, r = o / na, l = r % dof, pr = r / dof;
+  for (int o = tid; o < ncomp * npair * na; o += bs) {
+    const int ai = o % na, r = o / na, l = r % ncomp, pr = r / ncomp;
     int i = 0, rem = pr;  // pair index -> (i, j): rows of length Ds - i
     while (rem >= Ds - i) {
       rem -= Ds - i;
       ++i;
     }
     const int j = rem, m = Ds - i;
-    const double* c =
-        cV + l * NCs + (NCs - m * (m + 1) * (m + 2) / 6 + j * m - (j * (j - 1)) / 2);
+    const double* c = coeff(l) + (NCs - m * (m + 1) * (m + 2) / 6 + j * m - (j * (j - 1)) / 2);
     double w = fma_t0(sg.Tx[ai], __ldg(c));  // T_0 term, as tri_sum
     for (int k = 1; k < m - j; ++k) w = fma(__ldg(c + k), sg.Tx[k * Dd + ai], w);
     sw[(l * npair + pr) * Dd + ai] = w;
   }
   __syncthreads();
-  for (int o = tid; o < dof * nb * na; o += bs) {
+  for (int o = tid; o < ncomp * nb * na; o += bs) {
     const int ai = o % na, r = o / na, bi = r % nb, l = r / nb;
     const double* wl = sw + l * npair * Dd + ai;
     double v[Ds];
@@ -87,13 +85,27 @@ __device__ __forceinline__ void eval_subgrid(const TreeView& S, const SubGrid& s
       prow += Ds - i;
     }
     const int pab = sidx[ai] + Dd * sidx[Dd + bi];
+    double* ol = outp(l);
     for (int ci = 0; ci < nz; ++ci) {
       double u = fma_t0(sg.Tz[ci], v[0]);
 #pragma unroll
       for (int i = 1; i < Ds; ++i) u = fma(sg.Tz[i * Dd + ci], v[i], u);
-      out[(int64_t)(pab + Dd2 * sidx[2 * Dd + ci]) * pstride + l * lstride] = u;
+      ol[(int64_t)(pab + Dd2 * sidx[2 * Dd + ci]) * pstride] = u;
     }
   }
+}
+
+// The S.dof components of tree S's leaf sg.V; component l of node p goes to
+// out[p * pstride + l * lstride].
+template <int Ds>
+__device__ __forceinline__ void eval_subgrid(const TreeView& S, const SubGrid& sg, int Dd,
+                                             double* __restrict__ out, int64_t pstride,
+                                             int64_t lstride, double* sw) {
+  constexpr int NCs = Ds * (Ds + 1) * (Ds + 2) / 6;
+  const double* cV = S.coeff + sg.V * S.stride;
+  eval_subgrid_comps<Ds>(
+      sg, Dd, S.dof, [=](int l) { return cV + l * NCs; },
+      [=](int l) { return out + l * lstride; }, pstride, sw);
 }
 
 }  // namespace tbg

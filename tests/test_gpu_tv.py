@@ -70,6 +70,59 @@ def test_tv_matches_oracle(ctx, ora, same, bc, mode, kind):
         x.close()
 
 
+@pytest.mark.parametrize("j", [0, 1, 2, 3])
+@pytest.mark.parametrize("bc", [tb.FreeSpace, tb.Periodic])
+def test_one_hot_weights_equal_the_plain_step(ctx, j, bc):
+    """Four trees of one leaf structure, weight 1 on tree j and 0 on the
+    others at both stages: the FP64 step (one node-grid walk and one leaf
+    lookup for all four trees) equals the plain step through tree j bit for
+    bit -- each tree's values at the nodes and at the midpoints are the ones
+    its own evaluation gives."""
+    q = 6
+    vt, _ = _trees(ctx, q, bc, True)
+    tc, cd = _con(ctx, q)
+    t2 = tb.Tree(ctx, cd["anchor"], cd["depth"], q, 1, cd["coeff"])
+    w = np.zeros(8)
+    w[j] = w[4 + j] = 1.0
+
+    class OneHot:
+        pass
+    f = OneHot()
+    f.bc = bc
+    f.stage_weights = lambda timestep, dt, nrk: (vt, w)
+    tb.solve_semilag_in_situ_tv(f, tc, 1, 0.02)
+    tb.solve_semilag_in_situ(tb.NodeFieldFunctor(vt[j], bc), t2, 1, 0.02)
+    assert np.array_equal(tc.get_coeffs(), t2.get_coeffs())
+    for x in vt + [tc, t2]:
+        x.close()
+
+
+@pytest.mark.parametrize("q", [9, 11, 14])
+@pytest.mark.parametrize("bc", [tb.FreeSpace, tb.Periodic])
+def test_tv_shared_leaves_high_degree_matches_oracle(ctx, ora, q, bc):
+    """FP64 step through four velocity trees of one leaf structure at the
+    degrees of each instantiation unit (one lookup per point for all trees):
+    against the oracle, which evaluates every tree on its own."""
+    ts, dt = 3, 1.0 / (2 * q * q)
+    vt, vd = [], []
+    a, d = trees.uniform_tree(1)
+    for k in range(4):
+        c = trees.fit(_vel_fn(k, bc), a, d, q, 3)
+        vt.append(tb.Tree(ctx, a, d, q, 3, c))
+        vd.append(dict(anchor=a, depth=d, q=q, dof=3, coeff=c))
+    g = fields.gaussian((0.5, 0.45, 0.55), 0.15)
+    cc = trees.fit(g, a, d, q, 1)
+    tc = tb.Tree(ctx, a, d, q, 1, cc)
+    times = [0.0, 0.02, 0.04, 0.06]
+    ref = ora.semilag_in_situ_tv(vd, dict(anchor=a, depth=d, q=q, dof=1, coeff=cc), ts, dt, 1,
+                                 bc == tb.Periodic, times=times)
+    tb.solve_semilag_in_situ_tv(tb.FieldSetFunctor(vt, times, bc), tc, ts, dt)
+    got = tc.get_coeffs()
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+    for x in vt + [tc]:
+        x.close()
+
+
 def test_tv_two_substeps_matches_oracle(ctx, ora):
     q, ts, dt = 4, 2, 0.03
     vt, vd = _trees(ctx, q, tb.FreeSpace, True)
