@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(128) k_semilag_tree_jac(const SemilagTreeArgs 
   const bool per = a.periodic != 0;
   if (per) wrap3(x, y, z);
   const double half_tau = 0.5 * a.tau;
-  const double* vn = a.vn + 3 * t;
+  const double* vn = a.vn + 3 * node_source(a.face, t);
   double px = fma(half_tau, __ldg(vn + 0), x);
   double py = fma(half_tau, __ldg(vn + 1), y);
   double pz = fma(half_tau, __ldg(vn + 2), z);

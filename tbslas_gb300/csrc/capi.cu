@@ -680,11 +680,14 @@ int fused_step(tbslas_ctx ctx, const TreeView& v1, const TreeView& v2, tbslas_tr
     // first RK stage: the velocity at the targets by sum factorisation
     double* vn = nullptr;
     TRY(scratch_t(ctx, kVN, N * 3, &vn));
+    // shared upper-face nodes are not copied: the step kernels read them
+    // through the face map
     const int32_t* face = tree_face_map(con, bc, s);
-    ProfScope pv(ctx, "vel_at_nodes", s, face ? 2 : 1);
-    launch_eval_on_nodes(v1, a.con, bc, vn, s, face);
+    ProfScope pv(ctx, "vel_at_nodes", s, 1);
+    launch_eval_on_nodes(v1, a.con, bc, vn, s, face, false);
     TRY(check_launch("velocity at nodes"));
     a.vn = vn;
+    a.face = face;
   }
   TRY(scratch_t(ctx, kFixList, N, &a.fix_list));
   TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
@@ -2038,16 +2041,18 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
     double* vn = nullptr;
     TRY(scratch_t(ctx, kVN, (size_t)m * N * 3, &vn));
     const int32_t* face = tree_face_map(con, bc, s);
-    const int nl = same ? 1 : m;  // one walk for trees of one structure
-    ProfScope pv(ctx, "vel_at_nodes", s, face ? 2 * nl : nl);
-    if (same) {
+    // shared upper-face nodes are not copied: the step kernel reads them
+    // through the face map
+    ProfScope pv(ctx, "vel_at_nodes", s, same ? 1 : m);
+    if (same) {  // one walk for trees of one structure
       TreeView v[kTvMaxTrees];
       for (int k = 0; k < m; ++k) v[k] = vel[k]->view();
-      launch_eval_on_nodes_set(v, m, a.con, bc, vn, 3 * N, s, face);
+      launch_eval_on_nodes_set(v, m, a.con, bc, vn, 3 * N, s, face, false);
     } else {
       for (int k = 0; k < m; ++k)
-        launch_eval_on_nodes(vel[k]->view(), a.con, bc, vn + 3 * k * N, s, face);
+        launch_eval_on_nodes(vel[k]->view(), a.con, bc, vn + 3 * k * N, s, face, false);
     }
+    a.face = face;
     TRY(check_launch("velocity set at nodes"));
     a.vn = vn;
   }

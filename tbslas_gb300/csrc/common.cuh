@@ -168,6 +168,15 @@ struct SharedLoad {
 // Evaluate DOF components of a tree at one point.  The point is wrapped in
 // place under periodic boundaries (the caller sees the wrapped point, as
 // with EvalTree's in-place wrap, src/tree/tree_functor.h:442-448).
+// The target whose node values a node-grid output holds for target t: a
+// shared upper-face node reads its neighbour's node (the same point) when
+// the face map says so and the pass left it unwritten.
+__device__ __forceinline__ int64_t node_source(const int32_t* face, int64_t t) {
+  if (!face) return t;
+  const int32_t f = __ldg(face + t);
+  return f >= 0 ? (int64_t)f : t;
+}
+
 template <int D, int DOF>
 __device__ __forceinline__ void eval_point(const TreeView& t, double& x, double& y, double& z,
                                            bool periodic, double (&out)[DOF]) {

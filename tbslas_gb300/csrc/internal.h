@@ -58,6 +58,9 @@ struct SemilagTreeArgs {
   // [Lc * Np][9] row-major dv_a/dx_b (the checkpoint of the adjoint's
   // velocity-gradient term), or null
   double* jac = nullptr;
+  // con's face map when vn holds no shared upper-face nodes (node_source),
+  // or null
+  const int32_t* face = nullptr;
 };
 
 struct TrajArgs {
@@ -143,6 +146,7 @@ struct TvArgs {
   const double* vn = nullptr;
   double w[2 * kTvMaxSubsteps * kTvMaxTrees];
   int same_leaves = 0;  // 1: every tree has vel[0]'s leaves (one lookup per point)
+  const int32_t* face = nullptr;  // con's face map: vn holds no shared upper-face nodes
 };
 typedef void (*TvFn)(const TvArgs&, cudaStream_t);
 void register_tv_a(TvFn* table);  // index = Chebyshev degree q
@@ -246,14 +250,16 @@ int step_points(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con, int timestep, 
 // (bit-identical to the pointwise FP64 evaluation)
 // face: dst's face map for this boundary condition (tree_face_map), or null
 // (every node evaluated, no copy)
+// copy_faces false: the shared upper-face nodes are left unwritten (the
+// consumer reads face[t]'s value instead).
 void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic, double* out,
-                          cudaStream_t s, const int32_t* face = nullptr);
+                          cudaStream_t s, const int32_t* face = nullptr, bool copy_faces = true);
 // ntrees source trees of one leaf structure (src[k].keys all equal; the
 // walk is src[0]'s), tree k's values at out + k * tstride, each as
 // launch_eval_on_nodes writes them.  ntrees <= kTvMaxTrees.
 void launch_eval_on_nodes_set(const TreeView* src, int ntrees, const TreeView& dst, int periodic,
                               double* out, int64_t tstride, cudaStream_t s,
-                              const int32_t* face = nullptr);
+                              const int32_t* face = nullptr, bool copy_faces = true);
 // face[t] = the target index whose value the shared upper-face node t takes
 // (same point, same source leaf), else -1; [dst.L * Np]
 void launch_face_map(const TreeView& dst, int periodic, int32_t* face, cudaStream_t s);

@@ -611,7 +611,7 @@ void launch_face_map(const TreeView& dst, int periodic, int32_t* face, cudaStrea
 }
 
 void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic, double* out,
-                          cudaStream_t s, const int32_t* face) {
+                          cudaStream_t s, const int32_t* face, bool copy_faces) {
   if (dst.L <= 0) return;
   NodeEvalJob j;
   j.src = src;
@@ -622,7 +622,7 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
   j.out = out;
   j.face = face;
   dispatch_single<1>(src.q + 1, j, dst.L, periodic, s);
-  if (face) {
+  if (face && copy_faces) {
     const int64_t n = dst.L * (int64_t)(dst.q + 1) * (dst.q + 1) * (dst.q + 1);
     k_copy_face_nodes<<<(unsigned)((n + kNodeEvalThreads - 1) / kNodeEvalThreads),
                         kNodeEvalThreads, 0, s>>>(face, n, src.dof, out);
@@ -631,7 +631,7 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
 
 void launch_eval_on_nodes_set(const TreeView* src, int ntrees, const TreeView& dst, int periodic,
                               double* out, int64_t tstride, cudaStream_t s,
-                              const int32_t* face) {
+                              const int32_t* face, bool copy_faces) {
   if (dst.L <= 0 || ntrees <= 0) return;
   NodeEvalSet a;
   std::memset(&a, 0, sizeof(a));
@@ -645,7 +645,7 @@ void launch_eval_on_nodes_set(const TreeView* src, int ntrees, const TreeView& d
   a.ntrees = ntrees;
   a.tstride = tstride;
   dispatch_set<1>(src[0].q + 1, a, dst.L, periodic, s);
-  if (face) {
+  if (face && copy_faces) {
     const int64_t n = dst.L * (int64_t)(dst.q + 1) * (dst.q + 1) * (dst.q + 1);
     k_copy_face_nodes_set<<<(unsigned)((n + kNodeEvalThreads - 1) / kNodeEvalThreads),
                             kNodeEvalThreads, 0, s>>>(face, n, src[0].dof, ntrees, tstride, out);

@@ -149,8 +149,8 @@ __global__ void __launch_bounds__(128) k_semilag_tree(const SemilagTreeArgs a) {
   double z = g.z + h * a.nodes.x[p / (D * D)];
   const bool per = a.periodic != 0;
   if (a.vn)
-    rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * t, x, y, z, a.tau, a.nrk, per,
-                               a.xmid ? a.xmid + 3 * t : nullptr);
+    rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * node_source(a.face, t), x, y, z, a.tau, a.nrk,
+                               per, a.xmid ? a.xmid + 3 * t : nullptr);
   else
     rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
   store_point(a.xdep, t, x, y, z);
@@ -208,10 +208,11 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_tree_df(cons
   if (a.vn) {
     // first stage from the velocity at the nodes, bit-identical to the FP64
     // path's v(X): X wrapped in place as eval_point does, the midpoint exact
+    const double* vn = a.vn + 3 * node_source(a.face, t);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       if (per) x[k] = wrap1(x[k]);
-      px[k] = fma(half_tau, __ldg(a.vn + 3 * t + k), x[k]);
+      px[k] = fma(half_tau, __ldg(vn + k), x[k]);
     }
     st0 = 1;
     store_point(a.xmid, t, px[0], px[1], px[2]);
@@ -267,8 +268,8 @@ __global__ void __launch_bounds__(128) k_semilag_fix(const SemilagTreeArgs a) {
     double z = g.z + h * a.nodes.x[p / (D * D)];
     const bool per = a.periodic != 0;
     if (a.vn)
-      rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * t, x, y, z, a.tau, a.nrk, per,
-                                 a.xmid ? a.xmid + 3 * t : nullptr);
+      rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * node_source(a.face, t), x, y, z, a.tau,
+                                 a.nrk, per, a.xmid ? a.xmid + 3 * t : nullptr);
     else
       rk2_backtrace<D>(a.vel, x, y, z, a.tau, a.nrk, per);
     store_point(a.xdep, t, x, y, z);

@@ -85,9 +85,13 @@ __global__ void __launch_bounds__(128) k_semilag_tv(const TvArgs a) {
         z = wrap1(z);
       }
       const int64_t N = a.con.L * NP;
+      // a shared upper-face node takes its neighbour's node values (the
+      // same point; the node-grid pass left it unwritten)
+      const int32_t f = a.face ? __ldg(a.face + t) : -1;
+      const int64_t tv = f >= 0 ? (int64_t)f : t;
       v[0] = v[1] = v[2] = 0.0;
       for (int k = 0; k < a.m; ++k) {
-        const double* u = a.vn + 3 * (k * N + t);
+        const double* u = a.vn + 3 * (k * N + tv);
         v[0] = fma(a.w[k], __ldg(u + 0), v[0]);
         v[1] = fma(a.w[k], __ldg(u + 1), v[1]);
         v[2] = fma(a.w[k], __ldg(u + 2), v[2]);
