@@ -126,7 +126,8 @@ int enqueue_steps(tbslas_batch b, int nsteps, cudaStream_t s) {
     for (int q = 0; q <= TBSLAS_MAX_DEGREE; ++q) {
       const int64_t n = b->nitem_begin[q + 1] - b->nitem_begin[q];
       if (n > 0)
-        launch_batch_eval_on_nodes(b->d_njobs, b->d_nitems + b->nitem_begin[q], n, q, q, b->bc, s);
+        launch_batch_eval_on_nodes(b->d_njobs, b->d_nitems + b->nitem_begin[q], n, q, q, b->bc, s,
+                                   false);
     }
     for (int band = 0; band < kBands; ++band) {
       const int64_t n = b->band_begin[band + 1] - b->band_begin[band];
@@ -290,6 +291,7 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     nj.nodes = p.nodes;
     nj.out = nullptr;  // rebased below
     nj.face = tree_face_map(con[i], bc, nullptr);  // built on the legacy stream; synchronised below
+    b->h_probs[i].face = nj.face;  // the step reads shared face nodes through it
     njobs.push_back(nj);
     for (int64_t r = 0; r < p.con.L; ++r) nitems.push_back(NodeEvalItem{i, 0, r});
   }

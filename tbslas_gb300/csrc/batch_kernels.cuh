@@ -14,6 +14,7 @@ struct BatchProblem {
   Nodes1D nodes;  // 1-D Chebyshev nodes of degree q
   double* vals;   // [n_targets] node values of this problem
   const double* vn;  // [n_targets][3] velocity at the targets (first RK stage)
+  const int32_t* face;  // con's face map: vn holds no shared upper-face nodes, or null
   double dt;
   int64_t n_targets;
   int q;
@@ -77,10 +78,11 @@ __device__ __forceinline__ void batch_target_df(const BatchProblem& p, int64_t t
   double m0[3] = {0.0, 0.0, 0.0}, mp[3] = {0.0, 0.0, 0.0};
   bool amb = false;
   // first stage from the velocity at the nodes (as k_semilag_tree_df)
+  const double* vn = p.vn + 3 * node_source(p.face, t);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     if (per) xx[k] = wrap1(xx[k]);
-    px[k] = fma(half_tau, __ldg(p.vn + 3 * t + k), xx[k]);
+    px[k] = fma(half_tau, __ldg(vn + k), xx[k]);
   }
 #pragma unroll 1
   for (int st = 1; st < 2 * p.nrk; ++st) {
@@ -120,7 +122,7 @@ __device__ __forceinline__ void batch_target(const BatchProblem& p, int64_t t, d
   double x = g.x + h * p.nodes.x[pi % D];
   double y = g.y + h * p.nodes.x[(pi / D) % D];
   double z = g.z + h * p.nodes.x[pi / (D * D)];
-  rk2_backtrace_from_node<D>(p.vel, p.vn + 3 * t, x, y, z, tau, p.nrk, per);
+  rk2_backtrace_from_node<D>(p.vel, p.vn + 3 * node_source(p.face, t), x, y, z, tau, p.nrk, per);
   double c[1];
   eval_point<D, 1>(p.con, x, y, z, per, c);
   p.vals[t] = c[0];

@@ -283,7 +283,7 @@ struct NodeEvalItem {
 };
 void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* items,
                                 int64_t n_items, int q_src, int max_q_dst, int periodic,
-                                cudaStream_t s);
+                                cudaStream_t s, bool copy_faces = true);
 
 // Refit (refit.cu): node values -> coefficients through the separable
 // factors F = refit_factors(q) (4 D x D blocks on the device).

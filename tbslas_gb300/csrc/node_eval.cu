@@ -669,10 +669,11 @@ void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int perio
 
 void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* items,
                                 int64_t n_items, int q_src, int max_q_dst, int periodic,
-                                cudaStream_t s) {
+                                cudaStream_t s, bool copy_faces) {
   if (n_items <= 0) return;
   dispatch_batched<1>(q_src + 1, jobs, items, n_items, max_q_dst, periodic, s);
-  k_batch_copy_face_nodes<<<(unsigned)n_items, kNodeEvalThreads, 0, s>>>(jobs, items);
+  if (copy_faces)
+    k_batch_copy_face_nodes<<<(unsigned)n_items, kNodeEvalThreads, 0, s>>>(jobs, items);
 }
 
 }  // namespace tbg
