@@ -33,7 +33,8 @@ __device__ __forceinline__ double bdf2_target_fp64(const Bdf2Args& a, int64_t t)
   double y = g.y + h * a.nodes.x[(p / D) % D];
   double z = g.z + h * a.nodes.x[p / (D * D)];
   const bool per = a.periodic != 0;
-  rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * t, x, y, z, a.tau1, a.nrk, per);
+  rk2_backtrace_from_node<D>(a.vel, a.vn + 3 * node_source(a.face, t), x, y, z, a.tau1, a.nrk,
+                             per);
   double cn[1], cp[1];
   eval_point<D, 1>(a.cur, x, y, z, per, cn);  // wraps X1 in place
   rk2_backtrace<D>(a.vel, x, y, z, a.tau2, a.nrk, per);
@@ -102,10 +103,11 @@ __global__ void __launch_bounds__(128, (D <= 10 ? 8 : 7)) k_semilag_bdf2_df(cons
   const bool per = a.periodic != 0;
   double px[3], m0[3] = {0.0, 0.0, 0.0}, mp[3] = {0.0, 0.0, 0.0};
   // first stage from the node grid (exact)
+  const double* vn = a.vn + 3 * node_source(a.face, t);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     if (per) x[k] = wrap1(x[k]);
-    px[k] = fma(0.5 * a.tau1, __ldg(a.vn + 3 * t + k), x[k]);
+    px[k] = fma(0.5 * a.tau1, __ldg(vn + k), x[k]);
   }
   // the two backtraces share one copy of the stage loop and of the
   // evaluation (the instruction caches hold one): pass 0 continues from the

@@ -1929,9 +1929,10 @@ int tbslas_semilag_bdf2(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con_prev,
   TRY(scratch_t(ctx, kFixCount, 1, &a.fix_count));
   a.fix_grid = ctx->num_sms * 8;
   {
-    const int32_t* face = tree_face_map(con_next, bc, s);
-    ProfScope pv(ctx, "vel_at_nodes", s, face ? 2 : 1);
-    launch_eval_on_nodes(a.vel, a.next, bc, vn, s, face);
+    // shared upper-face nodes are read through the face map, not copied
+    a.face = tree_face_map(con_next, bc, s);
+    ProfScope pv(ctx, "vel_at_nodes", s, 1);
+    launch_eval_on_nodes(a.vel, a.next, bc, vn, s, a.face, false);
   }
   TRY(check_launch("velocity at nodes"));
   a.vn = vn;

@@ -120,6 +120,7 @@ struct Bdf2Args {
   int64_t* fix_list;  // targets the double-float kernel hands to the FP64 pass
   unsigned long long* fix_count;
   int fix_grid;
+  const int32_t* face = nullptr;  // next's face map: vn holds no shared upper-face nodes
 };
 
 typedef void (*Bdf2Fn)(const Bdf2Args&, bool df_sums, cudaStream_t);
