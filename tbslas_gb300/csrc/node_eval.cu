@@ -260,9 +260,9 @@ __device__ __forceinline__ void eval_on_nodes_leaf(const TreeView& S, const Tree
 // Several source trees of one leaf structure (the walk's source leaves are
 // the same for all of them): tree t's values go to out_all + t * tstride,
 // [dst.L * Dd^3][dof] each.  The sub-grid passes take `group` trees at a
-// time (3 group components; their w tables fill the shared memory), each
-// value as eval_on_nodes_leaf computes it.  s_coeff: the trees' coefficient
-// arrays, in shared memory.
+// time (dof x group components, whose w tables fill the shared memory),
+// each value as eval_on_nodes_leaf computes it.  s_coeff: the trees'
+// coefficient arrays, in shared memory.
 template <int Ds>
 __device__ __forceinline__ void eval_on_nodes_set_leaf(const TreeView& S, const TreeView& dst,
                                                        const Nodes1D& nodes, bool per,
