@@ -340,7 +340,9 @@ int tbslas_semilag_in_situ_host(tbslas_ctx ctx, tbslas_tree vel, tbslas_tree con
  * point in FP64 and the values blended -- for trees of one leaf structure
  * with one leaf lookup per point and one node-grid walk, the same values.
  * With m > 1 trees of one leaf count the call compares their leaf keys on
- * the device and waits for the answer (a stream synchronisation).  Blending
+ * the device and waits for the answer (a stream synchronisation), once per
+ * set of leaf lists: the context keeps the answer until one of the trees
+ * is re-meshed or another set is passed.  Blending
  * coefficients equals blending values up to rounding (~1e-16); where a
  * blended velocity component vanishes at a point on a leaf face or the
  * domain's boundary, that rounding can put the point on the other side than

@@ -2,6 +2,7 @@
 // host-side validation, the bucketing kernels of the tree functor, and the
 // entry points of the SL path.
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
 #include <cstdarg>
@@ -158,6 +159,21 @@ struct ProfTotal {
   double ms = 0.0;
 };
 
+// Leaf-list stamps (tbslas_tree_s::generation), unique across the process.
+uint64_t next_generation() {
+  static std::atomic<uint64_t> counter{0};
+  return counter.fetch_add(1) + 1;
+}
+
+// The last leaf-structure comparison of a velocity set
+// (tbslas_semilag_in_situ_tv): the trees' stamps and whether their leaves
+// were equal.
+struct TvStructure {
+  int m = 0;
+  uint64_t gen[kTvMaxTrees] = {};
+  bool same = false;
+};
+
 struct tbslas_ctx_s {
   int device = 0;
   int num_sms = 0;
@@ -173,6 +189,7 @@ struct tbslas_ctx_s {
   std::vector<ProfRecord> prof_pending;
   std::vector<cudaEvent_t> prof_pool;
   std::vector<ProfTotal> prof_totals;
+  TvStructure tv_structure;
 };
 
 struct tbslas_tree_s {
@@ -190,7 +207,9 @@ struct tbslas_tree_s {
   int32_t* d_table = nullptr;
   int64_t cap_L = 0;      // leaves the per-leaf arrays hold (>= L after a re-meshing)
   int64_t cap_table = 0;  // entries d_table holds
-  uint64_t generation = 0;  // bumped whenever the leaf list changes (re-meshing)
+  // a process-wide unique stamp of this tree's leaf list, new at creation
+  // and whenever the list changes (re-meshing): equal stamps, equal leaves
+  uint64_t generation = next_generation();
   // face maps of the node-grid pass, one per boundary condition, built on
   // first use for the current generation (tree_face_map)
   int32_t* d_face[2] = {nullptr, nullptr};
@@ -1011,7 +1030,7 @@ int install_mesh(tbslas_ctx ctx, tbslas_tree t, const MeshState& m, cudaStream_t
   t->L = m.L;
   t->max_depth = maxd;
   t->T = T;
-  ++t->generation;
+  t->generation = next_generation();
   launch_build_table(t->d_keys, t->L, T, t->d_table, s);
   launches += 3;  // the table, then the split and norms of derived_coeffs
   TRY(check_launch("lookup table"));
@@ -1984,7 +2003,13 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
   // one leaf lookup per point when the trees share their structure.
   bool same = true;
   for (int k = 1; k < m && same; ++k) same = vel[k]->L == vel[0]->L;
-  if (same && m > 1) {
+  // the keys are compared once per set of leaf lists (their stamps)
+  TvStructure& known = ctx->tv_structure;
+  bool cached = same && m > 1 && known.m == m;
+  for (int k = 0; k < m && cached; ++k) cached = known.gen[k] == vel[k]->generation;
+  if (cached) {
+    same = known.same;
+  } else if (same && m > 1) {
     int* flag;
     TRY(scratch_t(ctx, kTvFlag, 1, &flag));
     CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), s));
@@ -1996,6 +2021,9 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
     CUDA_TRY(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     same = h == 0;
+    known.m = m;
+    for (int k = 0; k < m; ++k) known.gen[k] = vel[k]->generation;
+    known.same = same;
   }
   if (same && nrk == 1 && ctx->sums == TBSLAS_SUMS_DOUBLE_FLOAT) {
     const tbslas_tree v0 = vel[0];

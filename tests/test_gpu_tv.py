@@ -97,6 +97,50 @@ def test_one_hot_weights_equal_the_plain_step(ctx, j, bc):
         x.close()
 
 
+def _same_count_other_leaves():
+    """64 leaves like uniform_tree(2), but not its leaves: the depth-1 leaf
+    at the origin kept, the other seven split, the depth-2 leaf at
+    (3/4, 3/4, 3/4) split again."""
+    anchor, depth = [np.zeros(3)], [1]
+    for i in range(1, 8):
+        a1 = np.array([i & 1, (i >> 1) & 1, (i >> 2) & 1]) / 2.0
+        for j in range(8):
+            a2 = a1 + np.array([j & 1, (j >> 1) & 1, (j >> 2) & 1]) / 4.0
+            if np.all(a2 == 0.75):
+                for k in range(8):
+                    anchor.append(a2 + np.array([k & 1, (k >> 1) & 1, (k >> 2) & 1]) / 8.0)
+                    depth.append(3)
+            else:
+                anchor.append(a2)
+                depth.append(2)
+    return trees.sort_leaves(np.array(anchor), np.array(depth, dtype=np.int32))
+
+
+def test_tv_structure_check_follows_the_trees(ctx, ora):
+    """The velocity set's leaf comparison is kept per set of leaf lists: a
+    set of one structure, then the same set with one tree swapped for a tree
+    of as many leaves but other ones, then the first set again -- each step
+    against the oracle."""
+    q, ts, dt, bc = 5, 3, 0.02, tb.FreeSpace
+    times = [0.0, 0.02, 0.04, 0.06]
+    vt, vd = _trees(ctx, q, bc, True)
+    a2, d2 = _same_count_other_leaves()
+    assert len(d2) == vt[1].n_leaves
+    c2 = trees.fit(_vel_fn(1, bc), a2, d2, q, 3)
+    other = tb.Tree(ctx, a2, d2, q, 3, c2)
+    od = dict(anchor=a2, depth=d2, q=q, dof=3, coeff=c2)
+    for vs, ds in ((vt, vd), ([vt[0], other, vt[2], vt[3]], [vd[0], od, vd[2], vd[3]]),
+                   (vt, vd)):
+        tc, cd = _con(ctx, q)
+        ref = ora.semilag_in_situ_tv(ds, cd, ts, dt, 1, False, times=times)
+        tb.solve_semilag_in_situ_tv(tb.FieldSetFunctor(vs, times, bc), tc, ts, dt)
+        got = tc.get_coeffs()
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+        tc.close()
+    for x in vt + [other]:
+        x.close()
+
+
 @pytest.mark.parametrize("q", [9, 11, 14])
 @pytest.mark.parametrize("bc", [tb.FreeSpace, tb.Periodic])
 def test_tv_shared_leaves_high_degree_matches_oracle(ctx, ora, q, bc):
