@@ -89,3 +89,44 @@ def test_fourier_grid_matches_point_function():
     KZ, KY, KX = np.meshgrid(k, k, k, indexing="ij")
     div = KX * np.fft.fftn(g[0]) + KY * np.fft.fftn(g[1]) + KZ * np.fft.fftn(g[2])
     assert np.abs(div).max() < 1e-9 * n ** 3
+
+
+def test_cubic_time_weights_match_interp_cubic_1d(built, ora):
+    """tbslas_cubic_time_weights: w . p equals CubicInterpPolicy::InterpCubic1D
+    (src/utils/cubic.h:42-56, the oracle's restatement) for any values p,
+    inside and outside the middle interval; non-increasing or non-finite
+    times are refused."""
+    rng = np.random.default_rng(7)
+    for _ in range(200):
+        times = np.sort(rng.uniform(-1.0, 1.0, 4))
+        if np.any(np.diff(times) <= 1e-3):
+            continue
+        t = rng.uniform(times[0] - 0.2, times[3] + 0.2)
+        w = tb.cubic_time_weights(times, t)
+        p = rng.normal(size=(4, 5))
+        ref = ora.interp_cubic_1d(t, times, list(p))
+        got = w @ p
+        assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+    with pytest.raises(capi.TbslasError):
+        tb.cubic_time_weights([0.0, 0.1, 0.1, 0.2], 0.05)
+    with pytest.raises(capi.TbslasError):
+        tb.cubic_time_weights([0.0, 0.1, 0.2, np.inf], 0.05)
+
+
+def test_field_set_stage_weights_follow_integrate_rk2(built, ora):
+    """FieldSetFunctor's per-stage weights are the cubic weights at the times
+    IntegrateRK2 queries (tinit and tinit + tau/2 of each sub-step,
+    src/semilag/traj.inc:20-45): two weight rows per sub-step."""
+    times = [0.0, 0.02, 0.04, 0.06]
+    f = tb.FieldSetFunctor([None] * 4, times)
+    for timestep, dt, nrk in ((3, 0.02, 1), (2, 0.03, 2), (5, 0.01, 3)):
+        _, w = f.stage_weights(timestep, dt, nrk)
+        assert w.shape == (2 * nrk * 4,)
+        tinit = timestep * dt
+        tau = (tinit - dt - tinit) / nrk
+        cur = tinit
+        for s in range(nrk):
+            np.testing.assert_array_equal(w[8 * s:8 * s + 4], tb.cubic_time_weights(times, cur))
+            np.testing.assert_array_equal(w[8 * s + 4:8 * s + 8],
+                                          tb.cubic_time_weights(times, cur + 0.5 * tau))
+            cur = cur + tau
