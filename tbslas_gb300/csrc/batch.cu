@@ -126,8 +126,7 @@ int enqueue_steps(tbslas_batch b, int nsteps, cudaStream_t s) {
     for (int q = 0; q <= TBSLAS_MAX_DEGREE; ++q) {
       const int64_t n = b->nitem_begin[q + 1] - b->nitem_begin[q];
       if (n > 0)
-        launch_batch_eval_on_nodes(b->d_njobs, b->d_nitems + b->nitem_begin[q], n, q, q, b->bc, s,
-                                   false);
+        launch_batch_eval_on_nodes(b->d_njobs, b->d_nitems + b->nitem_begin[q], n, q, q, b->bc, s);
     }
     for (int band = 0; band < kBands; ++band) {
       const int64_t n = b->band_begin[band + 1] - b->band_begin[band];
@@ -262,7 +261,7 @@ int tbslas_batch_create(tbslas_ctx ctx, int n, const tbslas_tree* vel, const tbs
     }
     p.dt = dt[i];
     const int d = p.q + 1;
-    const int np = d * d * d, nc = d * (d + 1) * (d + 2) / 6;
+    const int np = d * d * d;
     p.n_targets = p.con.L * np;
     p.vals = reinterpret_cast<double*>(off);  // offset; rebased below
     off += p.n_targets;

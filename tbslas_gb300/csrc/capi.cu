@@ -2076,7 +2076,7 @@ int tbslas_semilag_in_situ_tv(tbslas_ctx ctx, int m, const tbslas_tree* vel, con
     if (same) {  // one walk for trees of one structure
       TreeView v[kTvMaxTrees];
       for (int k = 0; k < m; ++k) v[k] = vel[k]->view();
-      launch_eval_on_nodes_set(v, m, a.con, bc, vn, 3 * N, s, face, false);
+      launch_eval_on_nodes_set(v, m, a.con, bc, vn, 3 * N, s, face);
     } else {
       for (int k = 0; k < m; ++k)
         launch_eval_on_nodes(vel[k]->view(), a.con, bc, vn + 3 * k * N, s, face, false);

@@ -257,10 +257,11 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
                           cudaStream_t s, const int32_t* face = nullptr, bool copy_faces = true);
 // ntrees source trees of one leaf structure (src[k].keys all equal; the
 // walk is src[0]'s), tree k's values at out + k * tstride, each as
-// launch_eval_on_nodes writes them.  ntrees <= kTvMaxTrees.
+// launch_eval_on_nodes writes them with copy_faces false (the shared
+// upper-face nodes of a face map left unwritten).  ntrees <= kTvMaxTrees.
 void launch_eval_on_nodes_set(const TreeView* src, int ntrees, const TreeView& dst, int periodic,
                               double* out, int64_t tstride, cudaStream_t s,
-                              const int32_t* face = nullptr, bool copy_faces = true);
+                              const int32_t* face = nullptr);
 // face[t] = the target index whose value the shared upper-face node t takes
 // (same point, same source leaf), else -1; [dst.L * Np]
 void launch_face_map(const TreeView& dst, int periodic, int32_t* face, cudaStream_t s);
@@ -282,9 +283,10 @@ struct NodeEvalItem {
   int32_t job, pad;
   int64_t leaf;
 };
+// The jobs' shared upper-face nodes (their face maps) are left unwritten.
 void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* items,
                                 int64_t n_items, int q_src, int max_q_dst, int periodic,
-                                cudaStream_t s, bool copy_faces = true);
+                                cudaStream_t s);
 
 // Refit (refit.cu): node values -> coefficients through the separable
 // factors F = refit_factors(q) (4 D x D blocks on the device).

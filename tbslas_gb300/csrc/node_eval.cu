@@ -413,35 +413,6 @@ __global__ void __launch_bounds__(kNodeEvalThreads) k_copy_face_nodes(
   for (int l = 0; l < dof; ++l) out[t * dof + l] = out[(int64_t)src * dof + l];
 }
 
-// k_copy_face_nodes for ntrees outputs tstride apart.
-__global__ void __launch_bounds__(kNodeEvalThreads) k_copy_face_nodes_set(
-    const int32_t* __restrict__ face, int64_t n, int dof, int ntrees, int64_t tstride,
-    double* __restrict__ out) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int32_t src = __ldg(face + t);
-  if (src < 0) return;
-  for (int k = 0; k < ntrees; ++k)
-    for (int l = 0; l < dof; ++l)
-      out[k * tstride + t * dof + l] = out[k * tstride + (int64_t)src * dof + l];
-}
-
-__global__ void __launch_bounds__(kNodeEvalThreads) k_batch_copy_face_nodes(
-    const NodeEvalJob* __restrict__ jobs, const NodeEvalItem* __restrict__ items) {
-  __shared__ NodeEvalJob sj;
-  const NodeEvalItem it = items[blockIdx.x];
-  if (threadIdx.x == 0) sj = jobs[it.job];
-  __syncthreads();
-  if (!sj.face) return;
-  const int Dd = sj.dst.q + 1, Dd3 = Dd * Dd * Dd, dof = sj.src.dof;
-  for (int p = threadIdx.x; p < Dd3; p += blockDim.x) {
-    const int64_t t = it.leaf * Dd3 + p;
-    const int32_t src = __ldg(sj.face + t);
-    if (src >= 0)
-      for (int l = 0; l < dof; ++l) sj.out[t * dof + l] = sj.out[(int64_t)src * dof + l];
-  }
-}
-
 template <int Ds>
 __global__ void __launch_bounds__(kNodeEvalThreads) k_eval_on_nodes(const NodeEvalJob j,
                                                                     int periodic) {
@@ -631,7 +602,7 @@ void launch_eval_on_nodes(const TreeView& src, const TreeView& dst, int periodic
 
 void launch_eval_on_nodes_set(const TreeView* src, int ntrees, const TreeView& dst, int periodic,
                               double* out, int64_t tstride, cudaStream_t s,
-                              const int32_t* face, bool copy_faces) {
+                              const int32_t* face) {
   if (dst.L <= 0 || ntrees <= 0) return;
   NodeEvalSet a;
   std::memset(&a, 0, sizeof(a));
@@ -645,11 +616,6 @@ void launch_eval_on_nodes_set(const TreeView* src, int ntrees, const TreeView& d
   a.ntrees = ntrees;
   a.tstride = tstride;
   dispatch_set<1>(src[0].q + 1, a, dst.L, periodic, s);
-  if (face && copy_faces) {
-    const int64_t n = dst.L * (int64_t)(dst.q + 1) * (dst.q + 1) * (dst.q + 1);
-    k_copy_face_nodes_set<<<(unsigned)((n + kNodeEvalThreads - 1) / kNodeEvalThreads),
-                            kNodeEvalThreads, 0, s>>>(face, n, src[0].dof, ntrees, tstride, out);
-  }
 }
 
 void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int periodic,
@@ -669,11 +635,9 @@ void launch_scatter_on_nodes(const TreeView& src, const TreeView& dst, int perio
 
 void launch_batch_eval_on_nodes(const NodeEvalJob* jobs, const NodeEvalItem* items,
                                 int64_t n_items, int q_src, int max_q_dst, int periodic,
-                                cudaStream_t s, bool copy_faces) {
+                                cudaStream_t s) {
   if (n_items <= 0) return;
   dispatch_batched<1>(q_src + 1, jobs, items, n_items, max_q_dst, periodic, s);
-  if (copy_faces)
-    k_batch_copy_face_nodes<<<(unsigned)n_items, kNodeEvalThreads, 0, s>>>(jobs, items);
 }
 
 }  // namespace tbg
