@@ -23,7 +23,9 @@ def lib():
         return None
     L = ctypes.CDLL(path)
     for name in ("ref_new_nodes", "ref_vec_eval", "ref_fast_interp", "ref_collect_grid_points",
-                 "ref_eval_tree", "ref_traj_rk2", "ref_pt2coeff", "ref_semilag_in_situ"):
+                 "ref_eval_tree", "ref_traj_rk2", "ref_pt2coeff", "ref_semilag_in_situ",
+                 "ref_semilag_in_situ_set", "ref_semilag_in_situ_extrap",
+                 "ref_interp_cubic_1d"):
         getattr(L, name).restype = None
     return L
 
@@ -91,4 +93,38 @@ def semilag_in_situ(vel, con, timestep, dt, nrk=1, periodic=False):
     lib().ref_semilag_in_situ(_L(len(dv)), _d(av), _d(dv), _d(vc), _L(len(dc)), _d(ac), _d(dc),
                               int(con["dof"]), _d(cc), int(con["q"]), int(timestep), _F(dt),
                               int(nrk), int(periodic), _d(out))
+    return out
+
+
+def _concat(trees):
+    return (_f64(np.concatenate([t["anchor"] for t in trees])),
+            _i32(np.concatenate([t["depth"] for t in trees])),
+            _f64(np.concatenate([np.ravel(t["coeff"]) for t in trees])))
+
+
+def semilag_in_situ_tv(vels, con, timestep, dt, nrk=1, periodic=False, times=None):
+    """The oracle's semilag_in_situ_tv signature: with times, vels are a
+    FieldSetFunctor's four trees; without, vels = [v_n, v_{n-1}] of the
+    two-functor step.  Returns the concentration's coefficients."""
+    av, dv, vc = _concat(vels)
+    ac, dc, cc = _f64(con["anchor"]), _i32(con["depth"]), _f64(con["coeff"])
+    out = np.empty_like(cc)
+    q = int(con["q"])
+    tail = (_L(len(dc)), _d(ac), _d(dc), _d(cc), q, int(timestep), _F(dt), int(nrk),
+            int(periodic), _d(out))
+    if times is not None:
+        Lv = np.ascontiguousarray([len(t["depth"]) for t in vels], dtype=np.int64)
+        tm = _f64(times)
+        lib().ref_semilag_in_situ_set(_d(Lv), _d(av), _d(dv), _d(vc), _d(tm), *tail)
+    else:
+        lib().ref_semilag_in_situ_extrap(_L(len(vels[0]["depth"])), _L(len(vels[1]["depth"])),
+                                         _d(av), _d(dv), _d(vc), *tail)
+    return out
+
+
+def interp_cubic_1d(x, xx, pp):
+    """InterpCubic1D for n triples: x [n], xx [n][4], pp [n][4]."""
+    x, xx, pp = _f64(x), _f64(xx), _f64(pp)
+    out = np.empty(len(x))
+    lib().ref_interp_cubic_1d(_L(len(x)), _d(x), _d(xx), _d(pp), _d(out))
     return out

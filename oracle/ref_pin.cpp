@@ -1,6 +1,7 @@
 // The reference's own SL-path code, compiled from its sources where they lie
 // (tbslas src/: semilag/traj.inc, semilag/semilag.inc, tree/tree_functor.h,
-// tree/tree_utils.h, tree/tree_semilag.h, utils/cheb.h) against the
+// tree/tree_utils.h, tree/tree_semilag.h, tree/tree_set_functor.h,
+// tree/tree_extrap_functor.h, utils/cheb.h, utils/cubic.h) against the
 // stand-ins of oracle/ref_stubs/ for its absent dependencies (PVFMM, MPI),
 // and driven on a linear octree given by its leaves.  It pins the oracle:
 // tests compare oracle/oracle.cpp with these entry points on the same inputs
@@ -22,8 +23,11 @@
 // headers use its SimConfigSingleton without including it)
 #include <utils/common.h>
 #include <tree/tree_semilag.h>
+#include <tree/tree_extrap_functor.h>
+#include <tree/tree_set_functor.h>
 
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 namespace refpin {
@@ -166,6 +170,64 @@ void ref_semilag_in_situ(long Lv, const double* av, const int* dv, const double*
   tbslas::NodeFieldFunctor<double, Tree> vel(&tv);
   tbslas::SolveSemilagInSitu(vel, tc, timestep, dt, nrk);
   tc.coeffs(coeff_out);
+}
+
+// SolveSemilagInSitu (src/tree/tree_semilag.h:92-135) through a
+// FieldSetFunctor (src/tree/tree_set_functor.h:49-72): four velocity trees
+// at times[4], cubic in time by CubicInterpPolicy::InterpCubic1D
+// (src/utils/cubic.h:42-56).  The trees' leaves are concatenated: tree k has
+// Lv[k] leaves (anchors av, depths dv, coefficients vc in that order).
+void ref_semilag_in_situ_set(const long* Lv, const double* av, const int* dv, const double* vc,
+                             const double* times, long Lc, const double* ac, const int* dc,
+                             const double* cc, int q, int timestep, double dt, int nrk,
+                             int periodic, double* coeff_out) {
+  refpin::set_bc(periodic);
+  const long nc = (long)(q + 1) * (q + 2) * (q + 3) / 6;
+  std::vector<std::unique_ptr<Tree>> own;
+  std::vector<Tree*> tv;
+  long o = 0;
+  for (int k = 0; k < 4; ++k) {
+    own.emplace_back(new Tree(Lv[k], av + 3 * o, dv + o, q, 3, vc + o * 3 * nc));
+    tv.push_back(own.back().get());
+    o += Lv[k];
+  }
+  Tree tc(Lc, ac, dc, q, 1, cc);
+  tbslas::FieldSetFunctor<double, Tree> vel(tv, std::vector<double>(times, times + 4));
+  tbslas::SolveSemilagInSitu(vel, tc, timestep, dt, nrk);
+  tc.coeffs(coeff_out);
+}
+
+// The two-functor SolveSemilagInSitu (src/tree/tree_semilag.h:137-180): v_n
+// (NodeFieldFunctor) at the first stage, FieldExtrapFunctor's
+// 1.5 v_n - 0.5 v_{n-1} (src/tree/tree_extrap_functor.h:47-78) at the
+// midpoint.  Trees: v_n (Ln leaves), then v_{n-1} (Lp leaves), concatenated.
+void ref_semilag_in_situ_extrap(long Ln, long Lp, const double* av, const int* dv,
+                                const double* vc, long Lc, const double* ac, const int* dc,
+                                const double* cc, int q, int timestep, double dt, int nrk,
+                                int periodic, double* coeff_out) {
+  refpin::set_bc(periodic);
+  const long nc = (long)(q + 1) * (q + 2) * (q + 3) / 6;
+  Tree tn(Ln, av, dv, q, 3, vc);
+  Tree tp(Lp, av + 3 * Ln, dv + Ln, q, 3, vc + Ln * 3 * nc);
+  Tree tc(Lc, ac, dc, q, 1, cc);
+  tbslas::NodeFieldFunctor<double, Tree> vel(&tn);
+  tbslas::FieldExtrapFunctor<double, Tree> extrap(&tp, &tn);
+  tbslas::SolveSemilagInSitu(vel, extrap, tc, timestep, dt, nrk);
+  tc.coeffs(coeff_out);
+}
+
+// CubicInterpPolicy<double>::InterpCubic1D (src/utils/cubic.h:42-56) for n
+// (x, xx[4], pp[4]) triples.
+void ref_interp_cubic_1d(long n, const double* x, const double* xx, const double* pp,
+                         double* out) {
+  for (long i = 0; i < n; ++i) {
+    double t[4], p[4];
+    for (int k = 0; k < 4; ++k) {
+      t[k] = xx[4 * i + k];
+      p[k] = pp[4 * i + k];
+    }
+    out[i] = tbslas::CubicInterpPolicy<double>::InterpCubic1D(x[i], t, p);
+  }
 }
 
 }  // extern "C"

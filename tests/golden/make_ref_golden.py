@@ -1,9 +1,12 @@
-"""Writes tests/golden/ref_pin.npz: outputs of the reference's own SL-path
-code (oracle/_ref, built from the reference's sources by
-oracle/build_ref.py) on small seeded cases.  Run from the repository root
-where the reference's sources are present:
+"""Writes tests/golden/ref_pin.npz and tests/golden/ref_tv.npz: outputs of
+the reference's own SL-path code (oracle/_ref, built from the reference's
+sources by oracle/build_ref.py) on small seeded cases -- the step, its
+parts, and the step through the time-dependent velocity functors
+(FieldSetFunctor, FieldExtrapFunctor, InterpCubic1D).  Run from the
+repository root where the reference's sources are present:
 
-    python tests/golden/make_ref_golden.py
+    python tests/golden/make_ref_golden.py          # both files
+    python tests/golden/make_ref_golden.py tv       # ref_tv.npz only
 
 The inputs are built with the oracle's set-up math only (its Chebyshev nodes
 and pseudo-inverse).  tests/test_ref_pin.py checks the oracle against these
@@ -94,5 +97,67 @@ def main():
     print(path, os.path.getsize(path), "bytes")
 
 
+def tv_velocity(k, periodic):
+    """Four related velocity fields of a time series (the ones
+    tests/test_gpu_tv.py uses)."""
+    if periodic:
+        base = fields.fourier_velocity(np.random.default_rng(20 + k))
+        return lambda p: 0.4 * base(p)
+    tg, rot, s = fields.taylor_green(), fields.rotation(2 * np.pi), 0.2 * k
+    return lambda p: (1.0 - s) * tg(p) + s * rot(p)
+
+
+def main_tv():
+    if ref.lib() is None:
+        raise SystemExit("the reference's sources are not present; nothing to generate")
+    rng = np.random.default_rng(2025)
+    out = {}
+    q, timestep, dt = 4, 3, 0.02
+    times = np.array([0.0, 0.02, 0.04, 0.06])
+    out["times"] = times
+    with trees.host_math(oracle_math()):
+        blob = fields.gaussian((0.5, 0.45, 0.55), 0.1)
+        ca, cd = trees.adaptive_tree(blob, q, 1, 1e-3, 1, 2)
+        out["con_anchor"], out["con_depth"] = ca, cd
+        out["con_coeff"] = trees.fit(blob, ca, cd, q, 1)
+        con = dict(anchor=ca, depth=cd, q=q, dof=1, coeff=out["con_coeff"])
+        i = 0
+        for periodic, same in ((0, True), (0, False), (1, True)):
+            vels = []
+            for k in range(4):
+                if same:
+                    a, d = trees.uniform_tree(1)
+                else:
+                    g = fields.gaussian((0.3 + 0.1 * k, 0.5, 0.5), 0.1)
+                    a, d = trees.adaptive_tree(g, q, 1, 1e-3, 1, 2)
+                c = trees.fit(tv_velocity(k, periodic), a, d, q, 3)
+                vels.append(dict(anchor=a, depth=d, q=q, dof=3, coeff=c))
+            for kind in ("set", "extrap"):
+                pre = "case%d_" % i
+                vs = vels if kind == "set" else [vels[1], vels[0]]
+                out[pre + "periodic"] = np.int32(periodic)
+                out[pre + "set"] = np.int32(kind == "set")
+                for k, v in enumerate(vs):
+                    for f in ("anchor", "depth", "coeff"):
+                        out[pre + "v%d_%s" % (k, f)] = v[f]
+                out[pre + "out"] = ref.semilag_in_situ_tv(
+                    vs, con, timestep, dt, 1, periodic, times=times if kind == "set" else None)
+                i += 1
+        out["n_cases"] = np.int32(i)
+        out["timestep"], out["dt"], out["q"] = np.int32(timestep), np.float64(dt), np.int32(q)
+        # InterpCubic1D on its own: increasing times, queries inside and
+        # outside the middle interval
+        xx = np.sort(rng.uniform(-1.0, 1.0, (500, 4)), axis=1) + np.arange(4) * 0.1
+        x = xx[:, 0] - 0.1 + rng.uniform(0.0, 1.0, 500) * (xx[:, 3] - xx[:, 0] + 0.2)
+        pp = rng.standard_normal((500, 4))
+        out["cubic_x"], out["cubic_xx"], out["cubic_pp"] = x, xx, pp
+        out["cubic_out"] = ref.interp_cubic_1d(x, xx, pp)
+    path = os.path.join(HERE, "ref_tv.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] != ["tv"]:
+        main()
+    main_tv()

@@ -1,14 +1,15 @@
 """The oracle pinned to the reference's own code.
 
-tests/golden/ref_pin.npz holds outputs of the reference's SL-path sources
-(tree_functor.h, traj.inc, semilag.inc, tree_utils.h, tree_semilag.h,
-cheb.h) compiled here against stand-ins for PVFMM and MPI (oracle/_ref,
-recipe oracle/build_ref.py, generator tests/golden/make_ref_golden.py).
+tests/golden/ref_pin.npz and ref_tv.npz hold outputs of the reference's
+SL-path sources (tree_functor.h, traj.inc, semilag.inc, tree_utils.h,
+tree_semilag.h, tree_set_functor.h, tree_extrap_functor.h, cheb.h, cubic.h)
+compiled here against stand-ins for PVFMM and MPI (oracle/_ref, recipe
+oracle/build_ref.py, generator tests/golden/make_ref_golden.py).
 The oracle must reproduce them bit for bit wherever its arithmetic is the
 reference's (Chebyshev nodes, grid points, tree evaluation, trajectories,
-the tricubic interpolant); the in-situ step differs only by the
-pseudo-inverse's and the refit GEMM's summation order (PVFMM's, restated on
-both sides).  Where the reference's sources are present the same checks also
+the tricubic interpolant); the in-situ step, also through the
+time-dependent velocity functors, differs only by the pseudo-inverse's and
+the refit GEMM's summation order (PVFMM's, restated on both sides).  Where the reference's sources are present the same checks also
 run live on fresh seeded cases.  The GPU tests compare the CUDA path with
 the same vectors."""
 import os
@@ -71,6 +72,41 @@ def test_oracle_in_situ_step_matches_the_reference(ora):
     for bc in (0, 1):
         got = ora.semilag_in_situ(vel, con, 2, 0.02, 1, bool(bc))
         assert _rel(got, G["step_bc%d_out" % bc]) <= STEP_TOL, bc
+
+
+TV = np.load(os.path.join(HERE, "golden", "ref_tv.npz"))
+
+
+def _tv_case(i):
+    pre = "case%d_" % i
+    nv = 4 if int(TV[pre + "set"]) else 2
+    q = int(TV["q"])
+    vels = [dict(anchor=TV[pre + "v%d_anchor" % k], depth=TV[pre + "v%d_depth" % k], q=q,
+                 dof=3, coeff=TV[pre + "v%d_coeff" % k]) for k in range(nv)]
+    con = dict(anchor=TV["con_anchor"], depth=TV["con_depth"], q=q, dof=1,
+               coeff=TV["con_coeff"])
+    times = TV["times"] if nv == 4 else None
+    return vels, con, bool(int(TV[pre + "periodic"])), times, TV[pre + "out"]
+
+
+def test_oracle_time_dependent_step_matches_the_reference(ora):
+    """The in-situ step through the reference's FieldSetFunctor (four trees,
+    cubic in time) and its two-functor form with FieldExtrapFunctor, on trees
+    of one and of different leaf structures, free space and periodic: the
+    oracle's composition to the refit's summation order."""
+    for i in range(int(TV["n_cases"])):
+        vels, con, periodic, times, want = _tv_case(i)
+        got = ora.semilag_in_situ_tv(vels, con, int(TV["timestep"]), float(TV["dt"]), 1,
+                                     periodic, times=times)
+        assert _rel(got, want) <= STEP_TOL, i
+
+
+def test_oracle_interp_cubic_1d_matches_the_reference(ora):
+    """CubicInterpPolicy::InterpCubic1D (src/utils/cubic.h:42-56): the oracle's
+    restatement to the rounding of the reference's contracted build."""
+    x, xx, pp, want = TV["cubic_x"], TV["cubic_xx"], TV["cubic_pp"], TV["cubic_out"]
+    got = np.array([ora.interp_cubic_1d(x[i], xx[i], pp[i]) for i in range(len(x))])
+    assert np.all(np.abs(got - want) <= 1e-13 * (1.0 + np.abs(want)))
 
 
 @pytest.fixture(scope="module")
@@ -197,3 +233,30 @@ def test_device_tricubic_interpolant_matches_the_reference(ctx):
     got = tb.fast_interp(ctx, _dev(G["interp_grid"]), 3, 12, _dev(G["interp_pts"]),
                          tb.FreeSpace).cpu().numpy()
     assert _rel(got, G["interp_out"]) <= 1e-12
+
+
+def test_live_time_dependent_step_matches_the_reference(ora, ref):
+    """A fresh case through the reference's time-dependent functors built
+    here: q = 6, periodic Fourier velocities of different leaf structures."""
+    from tbslas_gb300 import fields, trees
+    rng = np.random.default_rng(5)
+    with trees.host_math(trees.HostMath(
+            nodes=lambda q: ora.collect_grid_points(np.zeros((1, 3)),
+                                                    np.zeros(1, dtype=np.int32), q),
+            pt2coeff=ora.pt2coeff)):
+        q = 6
+        vels = []
+        for k in range(4):
+            base = fields.fourier_velocity(np.random.default_rng(40 + k))
+            g = fields.gaussian(tuple(rng.uniform(0.3, 0.7, 3)), 0.1)
+            a, d = trees.adaptive_tree(g, q, 1, 1e-3, 1, 2)
+            vels.append(dict(anchor=a, depth=d, q=q, dof=3,
+                             coeff=trees.fit(lambda p: 0.3 * base(p), a, d, q, 3)))
+        blob = fields.gaussian((0.4, 0.55, 0.5), 0.1)
+        ca, cd = trees.adaptive_tree(blob, q, 1, 1e-3, 1, 2)
+        con = dict(anchor=ca, depth=cd, q=q, dof=1, coeff=trees.fit(blob, ca, cd, q, 1))
+        times = [0.0, 0.015, 0.03, 0.05]
+        for vs, t in ((vels, times), (vels[:2], None)):
+            want = ref.semilag_in_situ_tv(vs, con, 2, 0.015, 2, True, times=t)
+            got = ora.semilag_in_situ_tv(vs, con, 2, 0.015, 2, True, times=t)
+            assert _rel(got, want) <= STEP_TOL
