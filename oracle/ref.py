@@ -25,7 +25,7 @@ def lib():
     for name in ("ref_new_nodes", "ref_vec_eval", "ref_fast_interp", "ref_collect_grid_points",
                  "ref_eval_tree", "ref_traj_rk2", "ref_pt2coeff", "ref_semilag_in_situ",
                  "ref_semilag_in_situ_set", "ref_semilag_in_situ_extrap",
-                 "ref_interp_cubic_1d"):
+                 "ref_semilag_bdf2", "ref_interp_cubic_1d"):
         getattr(L, name).restype = None
     return L
 
@@ -127,4 +127,19 @@ def interp_cubic_1d(x, xx, pp):
     x, xx, pp = _f64(x), _f64(xx), _f64(pp)
     out = np.empty(len(x))
     lib().ref_interp_cubic_1d(_L(len(x)), _d(x), _d(xx), _d(pp), _d(out))
+    return out
+
+
+def semilag_bdf2(vel, prev, cur, nxt, t, dt, nrk=1, periodic=False):
+    """The oracle's semilag_bdf2 signature: nxt's new coefficients."""
+    q = int(nxt["q"])
+    keep, args = [], []
+    for tr in (vel, prev, cur, nxt):
+        arrays = [_f64(tr["anchor"]), _i32(tr["depth"])]
+        if tr is not nxt:
+            arrays.append(_f64(tr["coeff"]))
+        keep += arrays
+        args += [_L(len(arrays[1]))] + [_d(a) for a in arrays]
+    out = np.empty((len(nxt["depth"]), 1, nc(q)))
+    lib().ref_semilag_bdf2(*args, q, _F(t), _F(dt), int(nrk), int(periodic), _d(out))
     return out

@@ -216,6 +216,38 @@ void ref_semilag_in_situ_extrap(long Ln, long Lp, const double* av, const int* d
   tc.coeffs(coeff_out);
 }
 
+// The advection-diffusion driver's BDF2 semi-Lagrangian step
+// (src/applications/src/advdiff-ss.cpp:485-521) -- a sequence inside the
+// driver's main(), so it is composed here from the reference's own
+// CollectChebTreeGridPoints, ComputeTrajRK2 (in place, as the driver calls
+// it), NodeFieldFunctor evaluations and SetTreeGridValues in the driver's
+// order, with the driver's combination of the two values (4/3 and 1/3).
+// Trees: velocity, c_{n-1}, c_n; the target tree's leaves (Ln, an, dn).
+void ref_semilag_bdf2(long Lv, const double* av, const int* dv, const double* vc, long Lp,
+                      const double* ap, const int* dp, const double* cp, long Lcur,
+                      const double* acur, const int* dcur, const double* ccur, long Ln,
+                      const double* an, const int* dn, int q, double t, double dt, int nrk,
+                      int periodic, double* coeff_out) {
+  refpin::set_bc(periodic);
+  Tree tv(Lv, av, dv, q, 3, vc);
+  Tree tp(Lp, ap, dp, q, 1, cp);
+  Tree tc(Lcur, acur, dcur, q, 1, ccur);
+  Tree tn(Ln, an, dn, q, 1, nullptr);
+  tbslas::NodeFieldFunctor<double, Tree> vel(&tv), cur(&tc), prev(&tp);
+  std::vector<double> pts;
+  tbslas::CollectChebTreeGridPoints(tn, pts);
+  const int n = (int)(pts.size() / 3);
+  std::vector<double> vc_n(n), vp_n(n), vals(n);
+  tbslas::ComputeTrajRK2(vel, pts, t, t - dt, nrk, pts);
+  cur(pts.data(), n, vc_n.data());
+  tbslas::ComputeTrajRK2(vel, pts, t - dt, t - dt * 2, nrk, pts);
+  prev(pts.data(), n, vp_n.data());
+  const double cc = 4.0 / 3, pc = 1.0 / 3;
+  for (int i = 0; i < n; ++i) vals[i] = cc * vc_n[i] - pc * vp_n[i];
+  tbslas::SetTreeGridValues(tn, q, 1, vals);
+  tn.coeffs(coeff_out);
+}
+
 // CubicInterpPolicy<double>::InterpCubic1D (src/utils/cubic.h:42-56) for n
 // (x, xx[4], pp[4]) triples.
 void ref_interp_cubic_1d(long n, const double* x, const double* xx, const double* pp,

@@ -1,12 +1,13 @@
-"""Writes tests/golden/ref_pin.npz and tests/golden/ref_tv.npz: outputs of
+"""Writes tests/golden/ref_pin.npz and tests/golden/ref_next.npz: outputs of
 the reference's own SL-path code (oracle/_ref, built from the reference's
-sources by oracle/build_ref.py) on small seeded cases -- the step, its
-parts, and the step through the time-dependent velocity functors
-(FieldSetFunctor, FieldExtrapFunctor, InterpCubic1D).  Run from the
-repository root where the reference's sources are present:
+sources by oracle/build_ref.py) on small seeded cases -- the step and its
+parts; the step through the time-dependent velocity functors
+(FieldSetFunctor, FieldExtrapFunctor, InterpCubic1D) and the driver's BDF2
+step.  Run from the repository root where the reference's sources are
+present:
 
     python tests/golden/make_ref_golden.py          # both files
-    python tests/golden/make_ref_golden.py tv       # ref_tv.npz only
+    python tests/golden/make_ref_golden.py next     # ref_next.npz only
 
 The inputs are built with the oracle's set-up math only (its Chebyshev nodes
 and pseudo-inverse).  tests/test_ref_pin.py checks the oracle against these
@@ -107,7 +108,7 @@ def tv_velocity(k, periodic):
     return lambda p: (1.0 - s) * tg(p) + s * rot(p)
 
 
-def main_tv():
+def main_next():
     if ref.lib() is None:
         raise SystemExit("the reference's sources are not present; nothing to generate")
     rng = np.random.default_rng(2025)
@@ -152,12 +153,32 @@ def main_tv():
         pp = rng.standard_normal((500, 4))
         out["cubic_x"], out["cubic_xx"], out["cubic_pp"] = x, xx, pp
         out["cubic_out"] = ref.interp_cubic_1d(x, xx, pp)
-    path = os.path.join(HERE, "ref_tv.npz")
+        # the BDF2 step: c_{n-1}, c_n and the target tree of different
+        # leaves, free space and periodic
+        b1, b2 = fields.gaussian((0.5, 0.45, 0.55), 0.1), fields.gaussian((0.52, 0.45, 0.55), 0.1)
+        pa, pd = trees.adaptive_tree(b1, q, 1, 1e-3, 1, 2)
+        ca2, cd2 = trees.adaptive_tree(b2, q, 1, 1e-3, 1, 3)
+        na, nd = trees.adaptive_tree(b2, q, 1, 1e-4, 1, 2)
+        for k, v in (("pa", pa), ("pd", pd), ("ca", ca2), ("cd", cd2), ("na", na), ("nd", nd)):
+            out["bdf2_" + k] = v
+        out["bdf2_pc"] = trees.fit(b1, pa, pd, q, 1)
+        out["bdf2_cc"] = trees.fit(b2, ca2, cd2, q, 1)
+        prev = dict(anchor=pa, depth=pd, q=q, dof=1, coeff=out["bdf2_pc"])
+        cur = dict(anchor=ca2, depth=cd2, q=q, dof=1, coeff=out["bdf2_cc"])
+        nxt = dict(anchor=na, depth=nd, q=q, dof=1)
+        for periodic in (0, 1):
+            va, vd = trees.uniform_tree(1)
+            vc = trees.fit(tv_velocity(1, periodic), va, vd, q, 3)
+            out["bdf2_bc%d_vc" % periodic] = vc
+            vel = dict(anchor=va, depth=vd, q=q, dof=3, coeff=vc)
+            out["bdf2_bc%d_out" % periodic] = ref.semilag_bdf2(vel, prev, cur, nxt, 0.3, 0.02, 1,
+                                                               periodic)
+    path = os.path.join(HERE, "ref_next.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path), "bytes")
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] != ["tv"]:
+    if sys.argv[1:] != ["next"]:
         main()
-    main_tv()
+    main_next()

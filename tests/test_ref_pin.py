@@ -1,6 +1,6 @@
 """The oracle pinned to the reference's own code.
 
-tests/golden/ref_pin.npz and ref_tv.npz hold outputs of the reference's
+tests/golden/ref_pin.npz and ref_next.npz hold outputs of the reference's
 SL-path sources (tree_functor.h, traj.inc, semilag.inc, tree_utils.h,
 tree_semilag.h, tree_set_functor.h, tree_extrap_functor.h, cheb.h, cubic.h)
 compiled here against stand-ins for PVFMM and MPI (oracle/_ref, recipe
@@ -8,8 +8,10 @@ oracle/build_ref.py, generator tests/golden/make_ref_golden.py).
 The oracle must reproduce them bit for bit wherever its arithmetic is the
 reference's (Chebyshev nodes, grid points, tree evaluation, trajectories,
 the tricubic interpolant); the in-situ step, also through the
-time-dependent velocity functors, differs only by the pseudo-inverse's and
-the refit GEMM's summation order (PVFMM's, restated on both sides).  Where the reference's sources are present the same checks also
+time-dependent velocity functors, and the advection-diffusion driver's BDF2
+step (composed from the reference's functions in the driver's order) differ
+only by the pseudo-inverse's and the refit GEMM's summation order (PVFMM's,
+restated on both sides).  Where the reference's sources are present the same checks also
 run live on fresh seeded cases.  The GPU tests compare the CUDA path with
 the same vectors."""
 import os
@@ -74,19 +76,19 @@ def test_oracle_in_situ_step_matches_the_reference(ora):
         assert _rel(got, G["step_bc%d_out" % bc]) <= STEP_TOL, bc
 
 
-TV = np.load(os.path.join(HERE, "golden", "ref_tv.npz"))
+NEXT = np.load(os.path.join(HERE, "golden", "ref_next.npz"))
 
 
 def _tv_case(i):
     pre = "case%d_" % i
-    nv = 4 if int(TV[pre + "set"]) else 2
-    q = int(TV["q"])
-    vels = [dict(anchor=TV[pre + "v%d_anchor" % k], depth=TV[pre + "v%d_depth" % k], q=q,
-                 dof=3, coeff=TV[pre + "v%d_coeff" % k]) for k in range(nv)]
-    con = dict(anchor=TV["con_anchor"], depth=TV["con_depth"], q=q, dof=1,
-               coeff=TV["con_coeff"])
-    times = TV["times"] if nv == 4 else None
-    return vels, con, bool(int(TV[pre + "periodic"])), times, TV[pre + "out"]
+    nv = 4 if int(NEXT[pre + "set"]) else 2
+    q = int(NEXT["q"])
+    vels = [dict(anchor=NEXT[pre + "v%d_anchor" % k], depth=NEXT[pre + "v%d_depth" % k], q=q,
+                 dof=3, coeff=NEXT[pre + "v%d_coeff" % k]) for k in range(nv)]
+    con = dict(anchor=NEXT["con_anchor"], depth=NEXT["con_depth"], q=q, dof=1,
+               coeff=NEXT["con_coeff"])
+    times = NEXT["times"] if nv == 4 else None
+    return vels, con, bool(int(NEXT[pre + "periodic"])), times, NEXT[pre + "out"]
 
 
 def test_oracle_time_dependent_step_matches_the_reference(ora):
@@ -94,17 +96,34 @@ def test_oracle_time_dependent_step_matches_the_reference(ora):
     cubic in time) and its two-functor form with FieldExtrapFunctor, on trees
     of one and of different leaf structures, free space and periodic: the
     oracle's composition to the refit's summation order."""
-    for i in range(int(TV["n_cases"])):
+    for i in range(int(NEXT["n_cases"])):
         vels, con, periodic, times, want = _tv_case(i)
-        got = ora.semilag_in_situ_tv(vels, con, int(TV["timestep"]), float(TV["dt"]), 1,
+        got = ora.semilag_in_situ_tv(vels, con, int(NEXT["timestep"]), float(NEXT["dt"]), 1,
                                      periodic, times=times)
         assert _rel(got, want) <= STEP_TOL, i
+
+
+def test_oracle_bdf2_step_matches_the_reference(ora):
+    """The driver's BDF2 step (src/applications/src/advdiff-ss.cpp:485-521:
+    two in-place ComputeTrajRK2 backtraces, c_n at X1, c_{n-1} at X2, 4/3 and
+    1/3, SetTreeGridValues) on three trees of different leaves."""
+    q = int(NEXT["q"])
+    prev = dict(anchor=NEXT["bdf2_pa"], depth=NEXT["bdf2_pd"], q=q, dof=1, coeff=NEXT["bdf2_pc"])
+    cur = dict(anchor=NEXT["bdf2_ca"], depth=NEXT["bdf2_cd"], q=q, dof=1, coeff=NEXT["bdf2_cc"])
+    nxt = dict(anchor=NEXT["bdf2_na"], depth=NEXT["bdf2_nd"], q=q, dof=1)
+    from tbslas_gb300 import trees
+    va, vd = trees.uniform_tree(1)
+    for bc in (0, 1):
+        vel = dict(anchor=va, depth=vd, q=q, dof=3, coeff=NEXT["bdf2_bc%d_vc" % bc])
+        got = ora.semilag_bdf2(vel, prev, cur, nxt, 0.3, 0.02, 1, bool(bc))
+        want = NEXT["bdf2_bc%d_out" % bc]
+        assert _rel(np.reshape(got, want.shape), want) <= STEP_TOL, bc
 
 
 def test_oracle_interp_cubic_1d_matches_the_reference(ora):
     """CubicInterpPolicy::InterpCubic1D (src/utils/cubic.h:42-56): the oracle's
     restatement to the rounding of the reference's contracted build."""
-    x, xx, pp, want = TV["cubic_x"], TV["cubic_xx"], TV["cubic_pp"], TV["cubic_out"]
+    x, xx, pp, want = NEXT["cubic_x"], NEXT["cubic_xx"], NEXT["cubic_pp"], NEXT["cubic_out"]
     got = np.array([ora.interp_cubic_1d(x[i], xx[i], pp[i]) for i in range(len(x))])
     assert np.all(np.abs(got - want) <= 1e-13 * (1.0 + np.abs(want)))
 
